@@ -1,0 +1,150 @@
+/*
+ * yael_gpu.h -- C ABI of the GB300 (sm_103a) implementation of yael's
+ * distance-GEMM path: exact k-NN, cross distances, k-means, hierarchical
+ * k-means.
+ *
+ * The first group of functions are drop-in replacements: same symbol names,
+ * argument order, meaning, ownership and error convention as the reference
+ * declarations cited beside each one (paths relative to the reference
+ * project).  Arrays are host memory in yael's layout: vector j of a set of n
+ * d-dimensional vectors is at x + j*d ("column-major d x n", yael/nn.h:11-24).
+ * Outputs are caller-allocated unless stated.  Failures print a message and
+ * abort(), as the reference does with assert()/abort(); no result is ever
+ * computed on the CPU.
+ *
+ * The yael_gpu_* group is new: explicit precision choice, device-pointer
+ * inputs, status codes instead of abort(), and batched (grouped) calls.
+ */
+#ifndef YAEL_GPU_H
+#define YAEL_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define YAEL_GPU_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ */
+/* drop-in: exact k-NN (yael/nn.h)                                     */
+
+/* yael/nn.h:41-45 (yael/nn.c:451-525).  distance_type 2 or 12 = squared L2,
+ * 16 = dot product (k smallest, like the reference's min-heap).  k <= nb.
+ * Neighbours are ordered by increasing distance, ties by increasing base
+ * index.  b_weights (may be NULL) multiplies each base vector's distance. */
+void knn_full(int distance_type, int nq, int nb, int d, int k, const float *b,
+              const float *q, const float *b_weights, int *assign, float *dis);
+
+/* yael/nn.h:49-54 (yael/nn.c:679-699).  n_thread is accepted and ignored. */
+void knn_full_thread(int distance_type, int nq, int nb, int d, int k,
+                     const float *b, const float *q, const float *b_weights,
+                     int *assign, float *dis, int n_thread);
+
+/* yael/nn.h:63-65 (yael/nn.c:608-621): 1-NN, returns the sum of distances. */
+double nn(int n, int nb, int d, const float *b, const float *v, int *assign);
+
+/* yael/nn.h:68-71 (yael/nn.c:715-726) */
+double nn_thread(int n, int nb, int d, const float *b, const float *v,
+                 int *assign, int n_thread);
+
+/* yael/nn.h:75-77 (yael/nn.c:624-632): returns malloc'd distances (free()). */
+float *knn(int n, int nb, int d, int k, const float *b, const float *v, int *assign);
+
+/* yael/nn.h:80-83 (yael/nn.c:704-711) */
+float *knn_thread(int nq, int nb, int d, int k, const float *b, const float *v,
+                  int *assign, int n_thread);
+
+/* yael/nn.h:103-105 (yael/nn.c:528-580): re-order each query's short list
+ * (stops at the first negative id) by exact distance, ties by list position. */
+void knn_reorder_shortlist(int n, int nb, int d, int k, const float *b,
+                           const float *v, int *idx, float *dis);
+
+/* yael/nn.h:128-131 (yael/nn.c:583-600) */
+void knn_recompute_exact_dists(int n, int nb, int d, int k, const float *b,
+                               const float *v, int label0, int *kp,
+                               const int *idx, float *dis);
+
+/* yael/nn.h:141-143 (yael/nn.c:92-97): dist2[i + na*j] = ||a_i - b_j||^2 */
+void compute_cross_distances(int d, int na, int nb, const float *a,
+                             const float *b, float *dist2);
+
+/* yael/nn.h:151-154 (yael/nn.c:100-129) */
+void compute_cross_distances_nonpacked(int d, int na, int nb, const float *a,
+                                       int lda, const float *b, int ldb,
+                                       float *dist2, int ldd);
+
+/* yael/nn.h:156-159 (yael/nn.c:777-792) */
+void compute_cross_distances_thread(int d, int na, int nb, const float *a,
+                                    const float *b, float *dist2, int nt);
+
+/* yael/nn.h:174-176 (yael/nn.c:352-356).  Types 2/12 (L2) and 16 (dot
+ * product) run on the GPU; other types abort with a message. */
+void compute_cross_distances_alt(int distance_type, int d, int na, int nb,
+                                 const float *a, const float *b, float *dist2);
+
+/* yael/nn.h:180-183 (yael/nn.c:280-350) */
+void compute_cross_distances_alt_nonpacked(int distance_type, int d, int na,
+                                           int nb, const float *a, int lda,
+                                           const float *b, int ldb,
+                                           float *dist2, int ldd);
+
+/* yael/nn.h:188-191 (yael/nn.c:795-810) */
+void compute_cross_distances_alt_thread(int distance_type, int d, int na, int nb,
+                                        const float *a, const float *b,
+                                        float *dist2, int nt);
+
+/* yael/nn.h:195-198 (yael/nn.c:156-162) */
+void compute_distances_1(int d, int nb, const float *a, const float *b, float *dist2);
+
+/* yael/nn.h:200-203 (yael/nn.c:132-154) */
+void compute_distances_1_nonpacked(int d, int nb, const float *a, const float *b,
+                                   int ldb, float *dist2);
+
+/* yael/nn.h:205-209 (yael/nn.c:830-837) */
+void compute_distances_1_thread(int d, int nb, const float *a, const float *b,
+                                float *dist2, int n_thread);
+
+/* yael/nn.h:211-215 (yael/nn.c:840-860) */
+void compute_distances_1_nonpacked_thread(int d, int nb, const float *a,
+                                          const float *b, int ldb, float *dist2,
+                                          int n_thread);
+
+/* ------------------------------------------------------------------ */
+/* extension API                                                       */
+
+#define YAEL_GPU_PREC_ENV (-1) /* take YAEL_GPU_PRECISION (fp32 | bf16), default fp32 */
+#define YAEL_GPU_PREC_FP32 0   /* FP32 CUDA-core distances (the plain drop-in path) */
+#define YAEL_GPU_PREC_BF16 1   /* BF16 tensor-core distances + exact FP32 re-rank */
+
+/* status codes of the yael_gpu_* functions */
+#define YAEL_GPU_OK 0
+#define YAEL_GPU_ECUDA 1
+#define YAEL_GPU_EARG 2
+#define YAEL_GPU_EUNSUPPORTED 3
+#define YAEL_GPU_ENOMEM 4
+#define YAEL_GPU_ETIMEOUT 5
+
+typedef struct {
+  int precision;   /* YAEL_GPU_PREC_* */
+  int metric;      /* yael distance_type: 2 (or 12) = squared L2, 16 = dot product */
+  int device_ptrs; /* 1: b, q, assign, dis are device pointers on the current device */
+  void *stream;    /* cudaStream_t for device_ptrs calls; NULL = the library's stream */
+  /* filled on return */
+  int n_fallback;   /* queries whose certificate failed and were recomputed exhaustively */
+  int n_candidates; /* total candidates re-ranked */
+  int exact_class;  /* 1 if every distance was computed exactly (integer-valued data) */
+} yael_gpu_knn_opts;
+
+/* k-NN with explicit options.  Same result contract as knn_full. */
+int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q,
+                    int *assign, float *dis, yael_gpu_knn_opts *opts);
+
+/* message of the last failure on the calling thread ("" if none) */
+const char *yael_gpu_last_error(void);
+
+/* YAEL_GPU_ABI_VERSION of the loaded library */
+int yael_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,647 @@
+/*
+ * yael_oracle.c -- TEST INFRASTRUCTURE ONLY (the checker, never the product).
+ *
+ * CPU restatement of yael's distance-GEMM path.  See yael_oracle.h for the two
+ * arithmetic modes.  Every function names the reference lines it restates
+ * (paths relative to the reference project).  Written from the reference's
+ * documented behaviour; the heap, RNG and update orders are kept step-for-step
+ * alike because the reference's results (tie order, random streams) depend on
+ * them.
+ */
+#define _GNU_SOURCE
+#include "yael_oracle.h"
+
+#include <assert.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int sgemm_(const char *ta, const char *tb, const int *m, const int *n,
+           const int *k, const float *alpha, const float *a, const int *lda,
+           const float *b, const int *ldb, const float *beta, float *c,
+           const int *ldc);
+
+#define TILE 256 /* yael/nn.c:371-372 BLOCK_N1 / BLOCK_N2 */
+
+/* ------------------------------------------------------------------ */
+/* bounded max-heap with yael's tie behaviour (yael/binheap.c:11-211)  */
+
+typedef struct {
+  int cnt, cap;
+  float *val; /* 1-based */
+  int *lab;   /* 1-based */
+} oheap;
+
+static void oheap_push(oheap *h, int lab, float v)
+{
+  /* sift up, stopping as soon as the parent is >= v (yael/binheap.c:89-103) */
+  int i = ++h->cnt;
+  while (i > 1) {
+    int f = i >> 1;
+    if (h->val[f] >= v) break;
+    h->val[i] = h->val[f];
+    h->lab[i] = h->lab[f];
+    i = f;
+  }
+  h->val[i] = v;
+  h->lab[i] = lab;
+}
+
+static void oheap_pop(oheap *h)
+{
+  /* remove the root; the last element sinks from the root.  The child test
+   * counts the not-yet-removed last slot (yael/binheap.c:55-86). */
+  float last = h->val[h->cnt];
+  int i = 1;
+  for (;;) {
+    int l = i << 1, r = l + 1, c;
+    if (l > h->cnt) break;
+    if (r == h->cnt + 1 || h->val[l] > h->val[r]) c = l; else c = r;
+    if (last > h->val[c]) break;
+    h->val[i] = h->val[c];
+    h->lab[i] = h->lab[c];
+    i = c;
+  }
+  h->val[i] = h->val[h->cnt];
+  h->lab[i] = h->lab[h->cnt];
+  h->cnt--;
+}
+
+/* fill with the first non-NaN values, then replace the root only on a strict
+ * improvement (yael/binheap.c:139-156) */
+static void oheap_add_range(oheap *h, int n, int label0, const float *v)
+{
+  int i = 0;
+  for (; i < n && h->cnt < h->cap; i++)
+    if (!isnan(v[i])) oheap_push(h, label0 + i, v[i]);
+  if (i >= n) return;
+  float lim = h->val[1];
+  for (; i < n; i++)
+    if (v[i] < lim) {
+      oheap_pop(h);
+      oheap_push(h, label0 + i, v[i]);
+      lim = h->val[1];
+    }
+}
+
+/* sort by (value, heap slot) -- fvec_sort_index semantics (yael/sorting.c:286-317) */
+static int cmp_slot(const void *a, const void *b, void *ctx)
+{
+  const float *key = (const float *)ctx;
+  int ia = *(const int *)a, ib = *(const int *)b;
+  float dt = key[ia] - key[ib];
+  if (dt) return dt > 0 ? 1 : -1;
+  return ia - ib;
+}
+
+static void sort_index_f(const float *key, int n, int *perm)
+{
+  for (int i = 0; i < n; i++) perm[i] = i;
+  qsort_r(perm, n, sizeof(int), cmp_slot, (void *)key);
+}
+
+static void oheap_sort_out(oheap *h, int *lab_out, float *val_out)
+{
+  int *perm = malloc(sizeof(int) * (h->cnt + 1));
+  sort_index_f(h->val + 1, h->cnt, perm);
+  for (int i = 0; i < h->cnt; i++) {
+    int p = perm[i] + 1;
+    lab_out[i] = h->lab[p];
+    val_out[i] = h->val[p];
+  }
+  free(perm);
+}
+
+/* ------------------------------------------------------------------ */
+/* expanded-form distances (yael/nn.c:54-67, 100-129, 266-275)         */
+
+void orc_cross_distances_port(int d, int na, int nb, const float *a, int lda,
+                              const float *b, int ldb, float *dist2, int ldd)
+{
+  float *sa = malloc(sizeof(float) * (na > 0 ? na : 1));
+  for (long i = 0; i < na; i++) { /* float accumulation for a */
+    float s = 0;
+    const float *x = a + (long)lda * i;
+    for (long j = 0; j < d; j++) s += x[j] * x[j];
+    sa[i] = s;
+  }
+  for (long i = 0; i < nb; i++) { /* double accumulation for b, rounded on store */
+    double s = 0;
+    const float *x = b + (long)ldb * i;
+    for (long j = 0; j < d; j++) s += x[j] * x[j];
+    float *row = dist2 + i * (long)ldd;
+    for (long j = 0; j < na; j++) row[j] = s + sa[j];
+  }
+  float m2 = -2, one = 1;
+  sgemm_("Transposed", "Not trans", &na, &nb, &d, &m2, a, &lda, b, &ldb, &one,
+         dist2, &ldd);
+  free(sa);
+}
+
+static void dot_products_port(int d, int na, int nb, const float *a, const float *b,
+                              float *dist2)
+{
+  float one = 1, zero = 0;
+  sgemm_("Trans", "Not", &na, &nb, &d, &one, a, &d, b, &d, &zero, dist2, &na);
+}
+
+static void tile_distances(int dt, int d, int na, int nb, const float *a,
+                           const float *b, float *out)
+{
+  if (dt == 2 || dt == 12)
+    orc_cross_distances_port(d, na, nb, a, d, b, d, out, na);
+  else if (dt == 16)
+    dot_products_port(d, na, nb, a, b, out);
+  else {
+    fprintf(stderr, "oracle: distance_type %d not restated\n", dt);
+    abort();
+  }
+}
+
+/* nn_single_full (yael/nn.c:383-446): blocked argmin, strict '<' */
+static void nn_single_port(int dt, int n1, int n2, int d, const float *b,
+                           const float *q, const float *w, int *vw, float *vwdis)
+{
+  int s1 = n1 < TILE ? n1 : TILE, s2 = n2 < TILE ? n2 : TILE;
+  float *dists = malloc(sizeof(float) * (size_t)(s1 > 0 ? s1 : 1) * (s2 > 0 ? s2 : 1));
+  for (long i1 = 0; i1 < n1; i1 += s1) {
+    int m1 = n1 - i1 < s1 ? n1 - i1 : s1;
+    for (long j = 0; j < m1; j++) { vw[i1 + j] = -1; vwdis[i1 + j] = 1e30f; }
+    for (long i2 = 0; i2 < n2; i2 += s2) {
+      int m2 = n2 - i2 < s2 ? n2 - i2 : s2;
+      tile_distances(dt, d, m2, m1, b + i2 * d, q + i1 * d, dists);
+      if (w)
+        for (long j1 = 0; j1 < m1; j1++)
+          for (long j2 = 0; j2 < m2; j2++) dists[j1 * m2 + j2] *= w[j2 + i2];
+      for (long j1 = 0; j1 < m1; j1++) {
+        const float *row = dists + j1 * m2;
+        int im = vw[i1 + j1];
+        float dm = vwdis[i1 + j1];
+        for (long j2 = 0; j2 < m2; j2++)
+          if (row[j2] < dm) { im = j2 + i2; dm = row[j2]; }
+        vw[i1 + j1] = im;
+        vwdis[i1 + j1] = dm;
+      }
+    }
+  }
+  free(dists);
+}
+
+/* knn_full (yael/nn.c:451-525) */
+static void knn_full_port(int dt, int n1, int n2, int d, int k, const float *b,
+                          const float *q, const float *w, int *vw, float *vwdis)
+{
+  assert(k <= n2);
+  if (k == 1) { nn_single_port(dt, n1, n2, d, b, q, w, vw, vwdis); return; }
+  int s1 = n1 < TILE ? n1 : TILE, s2 = n2 < TILE ? n2 : TILE;
+  if (s1 <= 0) return;
+  float *dists = malloc(sizeof(float) * (size_t)s1 * s2);
+  oheap *hs = malloc(sizeof(oheap) * s1);
+  float *hv = malloc(sizeof(float) * (size_t)s1 * (k + 1));
+  int *hl = malloc(sizeof(int) * (size_t)s1 * (k + 1));
+  for (int j = 0; j < s1; j++) {
+    hs[j].cap = k;
+    hs[j].val = hv + (size_t)j * (k + 1);
+    hs[j].lab = hl + (size_t)j * (k + 1);
+  }
+  for (long i1 = 0; i1 < n1; i1 += s1) {
+    int m1 = n1 - i1 < s1 ? n1 - i1 : s1;
+    for (int j = 0; j < m1; j++) hs[j].cnt = 0;
+    for (long i2 = 0; i2 < n2; i2 += s2) {
+      int m2 = n2 - i2 < s2 ? n2 - i2 : s2;
+      tile_distances(dt, d, m2, m1, b + i2 * d, q + i1 * d, dists);
+      if (w)
+        for (long j1 = 0; j1 < m1; j1++)
+          for (long j2 = 0; j2 < m2; j2++) dists[j1 * m2 + j2] *= w[j2 + i2];
+      for (long j1 = 0; j1 < m1; j1++)
+        oheap_add_range(&hs[j1], m2, (int)i2, dists + j1 * m2);
+    }
+    for (long j1 = 0; j1 < m1; j1++) {
+      oheap *h = &hs[j1];
+      oheap_sort_out(h, vw + (i1 + j1) * k, vwdis + (i1 + j1) * k);
+      if (h->cnt < k) { /* NaN-short heaps: -1 ids, all-ones distance bits (nn.c:515-518) */
+        memset(vw + (i1 + j1) * k + h->cnt, 0xff, sizeof(int) * (k - h->cnt));
+        memset(vwdis + (i1 + j1) * k + h->cnt, 0xff, sizeof(float) * (k - h->cnt));
+      }
+    }
+  }
+  free(dists); free(hs); free(hv); free(hl);
+}
+
+/* knn_full_thread (yael/nn.c:665-699): nt contiguous query slices */
+void orc_knn_port(int dt, int nq, int nb, int d, int k, const float *b,
+                  const float *q, const float *w, int *assign, float *dis, int nt)
+{
+  if (nq < nt || nt <= 1) { knn_full_port(dt, nq, nb, d, k, b, q, w, assign, dis); return; }
+#pragma omp parallel for schedule(dynamic) num_threads(nt)
+  for (int i = 0; i < nt; i++) {
+    long n0 = (long)nq * i / nt, n1 = (long)nq * (i + 1) / nt;
+    knn_full_port(dt, (int)(n1 - n0), nb, d, k, b, q + n0 * d, w, assign + n0 * k,
+                  dis + n0 * k);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 brute force (distance form of yael/vector.c:2348-2358)          */
+
+static double dist64(const float *x, const float *y, int d)
+{
+  double s = 0;
+  for (int i = 0; i < d; i++) { double a = (double)x[i] - (double)y[i]; s += a * a; }
+  return s;
+}
+
+/* lexicographic (distance, id) max-heap, 0-based */
+static int lex_gt(double da, int ia, double db, int ib)
+{
+  return da > db || (da == db && ia > ib);
+}
+
+static void lexheap_sift_down(double *v, int *id, int n, int i)
+{
+  for (;;) {
+    int l = 2 * i + 1, r = l + 1, m = i;
+    if (l < n && lex_gt(v[l], id[l], v[m], id[m])) m = l;
+    if (r < n && lex_gt(v[r], id[r], v[m], id[m])) m = r;
+    if (m == i) return;
+    double tv = v[i]; v[i] = v[m]; v[m] = tv;
+    int ti = id[i]; id[i] = id[m]; id[m] = ti;
+    i = m;
+  }
+}
+
+void orc_knn_exact(int nq, int nb, int d, int k, const float *b, const float *q,
+                   int *assign, float *dis, double *dis64, int nt)
+{
+  if (nt <= 0) nt = 1;
+#pragma omp parallel num_threads(nt)
+  {
+    double *hv = malloc(sizeof(double) * (k + 1));
+    int *hi = malloc(sizeof(int) * (k + 1));
+#pragma omp for schedule(dynamic, 4)
+    for (long iq = 0; iq < nq; iq++) {
+      const float *x = q + iq * (long)d;
+      int n = 0;
+      for (int j = 0; j < nb; j++) {
+        double v = dist64(x, b + (long)j * d, d);
+        if (isnan(v)) continue;
+        if (n < k) {
+          hv[n] = v; hi[n] = j; n++;
+          if (n == k)
+            for (int s = k / 2 - 1; s >= 0; s--) lexheap_sift_down(hv, hi, k, s);
+        } else if (lex_gt(hv[0], hi[0], v, j)) {
+          hv[0] = v; hi[0] = j;
+          lexheap_sift_down(hv, hi, k, 0);
+        }
+      }
+      if (n < k)
+        for (int s = n / 2 - 1; s >= 0; s--) lexheap_sift_down(hv, hi, n, s);
+      /* heap-sort ascending */
+      int m = n;
+      while (m > 1) {
+        double tv = hv[0]; hv[0] = hv[m - 1]; hv[m - 1] = tv;
+        int ti = hi[0]; hi[0] = hi[m - 1]; hi[m - 1] = ti;
+        m--;
+        lexheap_sift_down(hv, hi, m, 0);
+      }
+      for (int r = 0; r < k; r++) {
+        if (r < n) {
+          assign[iq * k + r] = hi[r];
+          dis[iq * k + r] = (float)hv[r];
+          if (dis64) dis64[iq * k + r] = hv[r];
+        } else {
+          assign[iq * k + r] = -1;
+          memset(&dis[iq * k + r], 0xff, sizeof(float));
+          if (dis64) dis64[iq * k + r] = NAN;
+        }
+      }
+    }
+    free(hv); free(hi);
+  }
+}
+
+void orc_cross_distances_exact(int d, int na, int nb, const float *a,
+                               const float *b, double *dist2)
+{
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < nb; j++)
+    for (long i = 0; i < na; i++)
+      dist2[i + (long)na * j] = dist64(a + i * d, b + j * d, d);
+}
+
+/* argmin in FP64, ties to the lowest index (the k=1 rule of yael/nn.c:431-435) */
+static void assign_exact(int d, int n, int k, const float *v, const float *c,
+                         int *assign, float *dis, int nt)
+{
+#pragma omp parallel for schedule(static) num_threads(nt > 0 ? nt : 1)
+  for (long i = 0; i < n; i++) {
+    double best = INFINITY;
+    int bi = -1;
+    for (int j = 0; j < k; j++) {
+      double t = dist64(v + i * d, c + (long)j * d, d);
+      if (t < best) { best = t; bi = j; }
+    }
+    assign[i] = bi;
+    dis[i] = bi >= 0 ? (float)best : 1e30f;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* RNG replay (yael/vector.c:134-155, 184-189, 226-253; kmeans.c:15-24) */
+
+static double drand_r(unsigned int *seed) { return rand_r(seed) / ((double)RAND_MAX + 1.0); }
+
+/* Kinderman-Monahan ratio-of-uniforms normal deviate with the reference's
+ * float/double roundings (u1, u2 and zz held in float). */
+double orc_gaussrand_r(unsigned int *seed)
+{
+  const double magic = 1.71552776992141; /* 4 exp(-1/2) / sqrt(2) */
+  double z;
+  for (;;) {
+    float u1 = (float)drand_r(seed);
+    float u2 = (float)drand_r(seed);
+    z = magic * (u1 - .5) / u2;
+    float zz = (float)(z * z / 4.0);
+    if (zz < -log(u2)) break;
+  }
+  return z;
+}
+
+/* first k entries of the partial Fisher-Yates permutation */
+void orc_random_init(int n, int k, unsigned int seed, int *sel)
+{
+  int *idx = malloc(sizeof(int) * (size_t)n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  for (int i = 0; i < k && i < n; i++) {
+    int j = i + rand_r(&seed) % (n - i);
+    int t = idx[i]; idx[i] = idx[j]; idx[j] = t;
+  }
+  memcpy(sel, idx, sizeof(int) * (size_t)k);
+  free(idx);
+}
+
+static double norm_l1(const float *v, long n)
+{
+  double s = 0;
+  for (long i = 0; i < n; i++) s += fabs(v[i]);
+  return s;
+}
+
+static double norm_l2(const float *v, long n)
+{
+  double s = 0;
+  for (long i = 0; i < n; i++) s += v[i] * v[i];
+  return sqrt(s);
+}
+
+static void mul_by(float *v, long n, double s)
+{
+  for (long i = 0; i < n; i++) v[i] *= s;
+}
+
+/* kmeans_reassign_empty (yael/kmeans.c:166-209) */
+static int reassign_empty(int d, int k, float *C, const int *nassign, unsigned int seed)
+{
+  int nre = 0;
+  float *p = malloc(sizeof(float) * k);
+  float *eps = malloc(sizeof(float) * d);
+  for (int c = 0; c < k; c++) {
+    /* nassign^2 - 1 in int arithmetic; large clusters wrap like the reference */
+    unsigned int sq = (unsigned int)nassign[c] * (unsigned int)nassign[c] - 1u;
+    p[c] = nassign[c] < 2 ? 0 : (float)(int)sq;
+  }
+  mul_by(p, k, 1. / norm_l1(p, k));
+  for (int c = 0; c < k; c++) {
+    if (nassign[c] != 0) continue;
+    nre++;
+    double rd = drand_r(&seed);
+    int j;
+    for (j = 0; j < k - 1; j++) {
+      rd -= p[j];
+      if (rd < 0) break;
+    }
+    memcpy(C + (long)c * d, C + (long)j * d, sizeof(float) * d);
+    double s = norm_l2(C + (long)j * d, d) * 0.0000001;
+    unsigned int s2 = rand_r(&seed);
+    for (int i = 0; i < d; i++) eps[i] = (float)orc_gaussrand_r(&s2);
+    mul_by(eps, d, s);
+    for (int i = 0; i < d; i++) C[(long)j * d + i] += eps[i];
+    for (int i = 0; i < d; i++) C[(long)c * d + i] -= eps[i];
+    p[j] = 0;
+    mul_by(p, k, 1. / norm_l1(p, k));
+  }
+  free(p); free(eps);
+  return nre;
+}
+
+/* ------------------------------------------------------------------ */
+/* exact fixed-point centroid sums                                     */
+
+int orc_fixed_shift(long n, long d, const float *v)
+{
+  /* largest |x| < 2^e; n terms of |x| 2^S stay below 2^62 */
+  float m = 0;
+  for (long i = 0; i < n * d; i++) {
+    float a = fabsf(v[i]);
+    if (a > m) m = a;
+  }
+  int e = 0;
+  if (m > 0) frexp((double)m, &e);
+  int lg = 0;
+  while ((1L << lg) < n) lg++;
+  return 62 - lg - e;
+}
+
+static void update_exact(int d, int n, int k, const float *v, const int *assign,
+                         const int *nassign, float *C, int S)
+{
+  int64_t *acc = calloc((size_t)k * d, sizeof(int64_t));
+  double sc = ldexp(1.0, S), inv = ldexp(1.0, -S);
+  for (long i = 0; i < n; i++) {
+    int a = assign[i];
+    if (a < 0) continue;
+    for (int j = 0; j < d; j++) acc[(long)a * d + j] += llrint((double)v[i * d + j] * sc);
+  }
+  for (long c = 0; c < k; c++) {
+    double r = 1.0 / nassign[c];
+    for (int j = 0; j < d; j++)
+      C[c * d + j] = (float)((double)acc[c * d + j] * inv * r);
+  }
+  free(acc);
+}
+
+void orc_kmeans_step_exact(int d, int n, int k, const float *v, const float *c_in,
+                           int *assign, float *dis, int *nassign, float *c_out,
+                           int S)
+{
+  assign_exact(d, n, k, v, c_in, assign, dis, 8);
+  memset(nassign, 0, sizeof(int) * k);
+  for (int i = 0; i < n; i++)
+    if (assign[i] >= 0) nassign[assign[i]]++;
+  update_exact(d, n, k, v, assign, nassign, c_out, S);
+}
+
+/* ------------------------------------------------------------------ */
+/* kmeans (yael/kmeans.c:213-447), L2 only                              */
+
+static int kmeans_core(int d, int n, int k, int niter, int nt, int flags, float *C,
+                       const float *v, unsigned int seed, int *assign, int *nassign,
+                       float *dis, double *qerr_out, long *iter_tot, int mode, int S)
+{
+  double qerr = HUGE_VAL, qerr_old;
+  int tot_re = 0;
+  for (int iter = 1; iter <= niter; iter++) {
+    (*iter_tot)++;
+    if (mode == ORC_PORT)
+      orc_knn_port(2, n, k, d, 1, C, v, NULL, assign, dis, nt);
+    else
+      assign_exact(d, n, k, v, C, assign, dis, nt);
+    memset(nassign, 0, sizeof(int) * k);
+    for (int i = 0; i < n; i++) nassign[assign[i]]++;
+    if (mode == ORC_PORT) {
+      memset(C, 0, sizeof(float) * (size_t)k * d);
+      for (long i = 0; i < n; i++) {
+        float *c = C + (long)assign[i] * d;
+        for (int j = 0; j < d; j++) c[j] += v[i * d + j];
+      }
+      for (long c = 0; c < k; c++) mul_by(C + c * d, d, 1.0 / nassign[c]);
+    } else {
+      update_exact(d, n, k, v, assign, nassign, C, S);
+    }
+    if (flags & ORC_KMEANS_NORMALIZE_CENTS)
+      for (long c = 0; c < k; c++) mul_by(C + c * d, d, 1. / norm_l2(C + c * d, d));
+    int nre = reassign_empty(d, k, C, nassign, rand_r(&seed));
+    tot_re += nre;
+    if (tot_re > n / 100 && tot_re > 1000) return -1;
+    qerr_old = qerr;
+    qerr = 0;
+    for (long i = 0; i < n; i++) qerr += dis[i];
+    if (qerr_old == qerr && nre == 0) break;
+  }
+  *qerr_out = qerr;
+  return 0;
+}
+
+float orc_kmeans(int d, int n, int k, int niter, const float *v, int flags,
+                 long seed_in, int redo, float *C_out, float *dis_out,
+                 int *assign_out, int *nassign_out, int mode, long *iters_out)
+{
+  int nt = flags & 0xffff;
+  if (nt == 0) nt = 1;
+  niter = niter == 0 ? 1000000 : niter;
+  int user = (flags & ORC_KMEANS_INIT_USER) != 0;
+  if (user) redo = 1;
+  if (k > n) return -2; /* the reference asserts (kmeans.c:377) */
+  float *C = malloc(sizeof(float) * (size_t)k * d);
+  float *dis = malloc(sizeof(float) * (size_t)n);
+  int *assign = malloc(sizeof(int) * (size_t)n);
+  int *nassign = malloc(sizeof(int) * (size_t)k);
+  int *sel = malloc(sizeof(int) * (size_t)k);
+  double qerr = 0, best = HUGE_VAL;
+  long iter_tot = 0;
+  int S = mode == ORC_EXACT ? orc_fixed_shift(n, d, v) : 0;
+  if (seed_in == 0) seed_in = lrand48();
+  unsigned int seed = (unsigned int)seed_in;
+  int ret = 0;
+  for (int run = 0; run < redo; run++) {
+    if (user) {
+      memcpy(C, C_out, sizeof(float) * (size_t)k * d);
+    } else {
+      if (flags & ORC_KMEANS_INIT_BERKELEY) {
+        fprintf(stderr, "oracle: k-means++ init not restated\n");
+        abort();
+      }
+      orc_random_init(n, k, rand_r(&seed), sel);
+      for (long i = 0; i < k; i++) memcpy(C + i * d, v + (long)sel[i] * d, sizeof(float) * d);
+    }
+    ret = kmeans_core(d, n, k, niter, nt, flags, C, v, rand_r(&seed), assign, nassign,
+                      dis, &qerr, &iter_tot, mode, S);
+    if (ret < 0) break;
+    if (qerr < best) {
+      best = qerr;
+      if (C_out) memcpy(C_out, C, sizeof(float) * (size_t)k * d);
+      if (dis_out) memcpy(dis_out, dis, sizeof(float) * (size_t)n);
+      if (assign_out) memcpy(assign_out, assign, sizeof(int) * (size_t)n);
+      if (nassign_out) memcpy(nassign_out, nassign, sizeof(int) * (size_t)k);
+    }
+  }
+  if (iters_out) *iters_out = iter_tot;
+  free(C); free(dis); free(assign); free(nassign); free(sel);
+  return ret < 0 ? -1 : (float)(best / n);
+}
+
+/* ------------------------------------------------------------------ */
+/* hierarchical k-means (yael/hkm.c:36-150)                             */
+
+static int cmp_key_then_index(const void *a, const void *b, void *ctx)
+{
+  const int *key = (const int *)ctx;
+  int ia = *(const int *)a, ib = *(const int *)b;
+  if (key[ia] != key[ib]) return key[ia] < key[ib] ? -1 : 1;
+  return ia - ib;
+}
+
+int orc_hkm_learn(int n, int d, int nlevel, int bf, const float *points,
+                  int nb_iter_max, float *centroids_out, int *assign_out, int mode)
+{
+  int *node = calloc((size_t)n, sizeof(int));
+  int *perm = malloc(sizeof(int) * (size_t)n);
+  float *v = malloc(sizeof(float) * (size_t)n * d);
+  long k = 1, off = 0;
+  int rc = 0;
+  for (int l = 0; l < nlevel && rc == 0; l++) {
+    for (int i = 0; i < n; i++) perm[i] = i;
+    qsort_r(perm, n, sizeof(int), cmp_key_then_index, node);
+    for (long i = 0; i < n; i++) memcpy(v + i * d, points + (long)perm[i] * d, sizeof(float) * d);
+    long pos = 0;
+    for (long parent = 0; parent < k; parent++) {
+      int na = 0;
+      while (pos + na < n && node[perm[pos + na]] == parent) na++;
+      if (na == 0 || na < bf) { rc = -1; break; }
+      int *ca = malloc(sizeof(int) * (size_t)na);
+      float *C = malloc(sizeof(float) * (size_t)bf * d);
+      orc_kmeans(d, na, bf, nb_iter_max, v + pos * d,
+                 8 | ORC_KMEANS_INIT_RANDOM | ORC_KMEANS_QUIET, 0, 1, C, NULL, ca,
+                 NULL, mode, NULL);
+      memcpy(centroids_out + off + parent * bf * d, C, sizeof(float) * (size_t)bf * d);
+      for (int i = 0; i < na; i++) {
+        int t = perm[pos + i];
+        node[t] = node[t] * bf + ca[i];
+      }
+      free(ca); free(C);
+      pos += na;
+    }
+    off += k * bf * d;
+    k *= bf;
+  }
+  if (assign_out) memcpy(assign_out, node, sizeof(int) * (size_t)n);
+  free(node); free(perm); free(v);
+  return rc;
+}
+
+void orc_hkm_quantize(int nlevel, int bf, int d, const float *centroids, int npt,
+                      const float *v, int *idx, int mode)
+{
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < npt; i++) {
+    long vw = 0, off = 0, k = bf;
+    for (int l = 0; l < nlevel; l++) {
+      const float *C = centroids + off + vw * d * bf;
+      int t;
+      float dd;
+      if (mode == ORC_PORT)
+        knn_full_port(2, 1, bf, d, 1, C, v + i * d, NULL, &t, &dd);
+      else
+        assign_exact(d, 1, bf, v + i * d, C, &t, &dd, 1);
+      vw = vw * bf + t;
+      off += k * d;
+      k *= bf;
+    }
+    idx[i] = (int)vw;
+  }
+}

@@ -1,0 +1,99 @@
+/*
+ * yael_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A CPU restatement of yael's distance-GEMM path (exact k-NN, k-means Lloyd loop,
+ * hierarchical k-means), used as the checker for the GPU library and as the timed
+ * CPU baseline.  Nothing in the product library links, loads or calls this code;
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU legs do.
+ *
+ * Two arithmetic modes:
+ *   ORC_PORT  -- the reference's own arithmetic, step for step: blocked 256x256
+ *                expanded-form FP32 distances through BLAS sgemm (yael/nn.c:100-129,
+ *                451-525), the bounded max-heap with yael's tie behaviour
+ *                (yael/binheap.c:139-156, 201-211), float centroid accumulation
+ *                (yael/kmeans.c:277-288).  Bit-exact with the compiled reference
+ *                when linked to the same BLAS.
+ *   ORC_EXACT -- the semantics the GPU library implements: FP64 distances
+ *                (yael/vector.c:2348-2358 form), canonical (distance, index) order,
+ *                argmin ties to the lowest index (the k=1 rule of yael/nn.c:431-435),
+ *                exact fixed-point centroid sums read out through FP64.  The RNG
+ *                stream (seeds, init, empty-cluster splits) is identical in both
+ *                modes and identical to the reference's.
+ */
+#ifndef YAEL_ORACLE_H
+#define YAEL_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_PORT 0
+#define ORC_EXACT 1
+
+/* kmeans flag bits, same values as yael/kmeans.h:11-18 */
+#define ORC_KMEANS_QUIET 0x10000
+#define ORC_KMEANS_INIT_BERKELEY 0x20000
+#define ORC_KMEANS_NORMALIZE_CENTS 0x40000
+#define ORC_KMEANS_INIT_RANDOM 0x80000
+#define ORC_KMEANS_INIT_USER 0x100000
+#define ORC_KMEANS_L1 0x200000
+#define ORC_KMEANS_CHI2 0x400000
+
+const char *oracle_blas_name(void);
+
+/* FP64 brute force: for each query the k smallest FP64 squared L2 distances,
+ * ordered by (distance, base index).  dis receives the FP64 value rounded to
+ * float; dis64 (may be NULL) the FP64 value.  Follows yael/nn.c:451-525 for
+ * the interface (b(d,nb), q(d,nq), outputs (k,nq)). */
+void orc_knn_exact(int nq, int nb, int d, int k, const float *b, const float *q,
+                   int *assign, float *dis, double *dis64, int nt);
+
+/* Restatement of knn_full_thread (yael/nn.c:679-699 -> 451-525): distance_type
+ * 2/12 (expanded form via sgemm) or 16 (sgemm dot product). */
+void orc_knn_port(int distance_type, int nq, int nb, int d, int k, const float *b,
+                  const float *q, const float *b_weights, int *assign, float *dis,
+                  int nt);
+
+/* Restatement of compute_cross_distances_nonpacked (yael/nn.c:100-129). */
+void orc_cross_distances_port(int d, int na, int nb, const float *a, int lda,
+                              const float *b, int ldb, float *dist2, int ldd);
+
+/* FP64 reference of the full cross-distance matrix dist2[i + ldd*j]. */
+void orc_cross_distances_exact(int d, int na, int nb, const float *a,
+                               const float *b, double *dist2);
+
+/* Restatement of kmeans() (yael/kmeans.c:332-447) in the given mode.
+ * Returns qerr/n, or -1 on abandon (yael/kmeans.c:302-306, 443-444).
+ * *iters_out (may be NULL) receives the total number of Lloyd iterations. */
+float orc_kmeans(int d, int n, int k, int niter, const float *v, int flags,
+                 long seed, int redo, float *centroids, float *dis, int *assign,
+                 int *nassign, int mode, long *iters_out);
+
+/* One Lloyd step of ORC_EXACT mode on given centroids (no RNG): assignment,
+ * counts, fixed-point centroid update.  Used to check a single GPU iteration. */
+void orc_kmeans_step_exact(int d, int n, int k, const float *v, const float *c_in,
+                           int *assign, float *dis, int *nassign, float *c_out,
+                           int fixed_shift);
+
+/* The fixed-point shift used by ORC_EXACT centroid sums for this data. */
+int orc_fixed_shift(long n, long d, const float *v);
+
+/* hierarchical k-means (yael/hkm.c:36-116).  centroids_out receives the
+ * levels concatenated (level l holds bf^(l+1) rows of d floats).  assign_out
+ * (n ints, may be NULL).  Returns 0, or -1 when a node is empty (where the
+ * reference exits, yael/hkm.c:77-80) or too small for bf clusters. */
+int orc_hkm_learn(int n, int d, int nlevel, int bf, const float *points,
+                  int nb_iter_max, float *centroids_out, int *assign_out, int mode);
+
+/* greedy descent (yael/hkm.c:131-150) */
+void orc_hkm_quantize(int nlevel, int bf, int d, const float *centroids, int npt,
+                      const float *v, int *idx, int mode);
+
+/* RNG pieces, exposed so the tests can compare them with the GPU library's. */
+double orc_gaussrand_r(unsigned int *seed);
+void orc_random_init(int n, int k, unsigned int seed, int *sel);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,146 @@
+"""GB300 (sm_103a) implementation of yael's distance-GEMM path.
+
+The product is the C-ABI library ``libyael_gb300.so`` (declared in
+``include/yael_gpu.h``): exact k-NN, cross distances, k-means and hierarchical
+k-means with yael's own symbol names and conventions.  This module loads it
+with ctypes and mirrors the reference's numpy front end (yael/ynumpy.py:46-130:
+``knn``, ``cross_distances``, ``kmeans``) on top of it.
+
+There is no CPU fallback: if the library (or a GPU) is missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libyael_gb300.so")
+
+_lib = None
+_lock = threading.Lock()
+
+c_int, c_long, c_float, c_double = ctypes.c_int, ctypes.c_long, ctypes.c_float, ctypes.c_double
+P = ctypes.c_void_p
+
+# kmeans flag bits (yael/kmeans.h:11-18)
+KMEANS_QUIET = 0x10000
+KMEANS_INIT_BERKELEY = 0x20000
+KMEANS_NORMALIZE_CENTS = 0x40000
+KMEANS_INIT_RANDOM = 0x80000
+KMEANS_INIT_USER = 0x100000
+KMEANS_L1 = 0x200000
+KMEANS_CHI2 = 0x400000
+
+PREC_ENV, PREC_FP32, PREC_BF16 = -1, 0, 1
+
+
+class KnnOpts(ctypes.Structure):
+    _fields_ = [("precision", c_int), ("metric", c_int), ("device_ptrs", c_int),
+                ("stream", P), ("n_fallback", c_int), ("n_candidates", c_int),
+                ("exact_class", c_int)]
+
+
+# name -> (restype, argtypes); every symbol of include/yael_gpu.h
+SIGNATURES = {
+    "knn_full": (None, [c_int, c_int, c_int, c_int, c_int, P, P, P, P, P]),
+    "knn_full_thread": (None, [c_int, c_int, c_int, c_int, c_int, P, P, P, P, P, c_int]),
+    "nn": (c_double, [c_int, c_int, c_int, P, P, P]),
+    "nn_thread": (c_double, [c_int, c_int, c_int, P, P, P, c_int]),
+    "knn": (P, [c_int, c_int, c_int, c_int, P, P, P]),
+    "knn_thread": (P, [c_int, c_int, c_int, c_int, P, P, P, c_int]),
+    "knn_reorder_shortlist": (None, [c_int, c_int, c_int, c_int, P, P, P, P]),
+    "knn_recompute_exact_dists": (None, [c_int, c_int, c_int, c_int, P, P, c_int, P, P, P]),
+    "compute_cross_distances": (None, [c_int, c_int, c_int, P, P, P]),
+    "compute_cross_distances_nonpacked": (None, [c_int, c_int, c_int, P, c_int, P, c_int, P, c_int]),
+    "compute_cross_distances_thread": (None, [c_int, c_int, c_int, P, P, P, c_int]),
+    "compute_cross_distances_alt": (None, [c_int, c_int, c_int, c_int, P, P, P]),
+    "compute_cross_distances_alt_nonpacked": (None, [c_int, c_int, c_int, c_int, P, c_int, P, c_int, P, c_int]),
+    "compute_cross_distances_alt_thread": (None, [c_int, c_int, c_int, c_int, P, P, P, c_int]),
+    "compute_distances_1": (None, [c_int, c_int, P, P, P]),
+    "compute_distances_1_nonpacked": (None, [c_int, c_int, P, P, c_int, P]),
+    "compute_distances_1_thread": (None, [c_int, c_int, P, P, P, c_int]),
+    "compute_distances_1_nonpacked_thread": (None, [c_int, c_int, P, P, c_int, P, c_int]),
+    "yael_gpu_knn_ex": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, ctypes.POINTER(KnnOpts)]),
+    "yael_gpu_last_error": (ctypes.c_char_p, []),
+    "yael_gpu_version": (c_int, []),
+}
+
+
+def lib() -> ctypes.CDLL:
+    """Load libyael_gb300.so (built by ``yael_gb300.build.build()``)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with "
+                    "`python -c 'import __graft_entry__ as g; g.build()'`")
+            L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_LOCAL)
+            for name, (res, args) in SIGNATURES.items():
+                if hasattr(L, name):
+                    f = getattr(L, name)
+                    f.restype = res
+                    f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    m = lib().yael_gpu_last_error()
+    return m.decode() if m else ""
+
+
+def _f32(x):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return x
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+# ---------------------------------------------------------------------------
+# numpy front end mirroring yael/ynumpy.py
+
+
+def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False):
+    """k nearest neighbours of each query row among the base rows.
+
+    Same contract as ynumpy.knn (yael/ynumpy.py:46-67): returns (idx, dis) of
+    shape (nq, nnn), int32 / float32, ordered by increasing distance with ties
+    by increasing base index.  ``precision`` ("fp32" | "bf16" | None = the
+    YAEL_GPU_PRECISION environment variable) picks the distance pass.
+    """
+    base = _f32(base)
+    queries = _f32(queries)
+    nb, d = base.shape
+    nq, d2 = queries.shape
+    assert d == d2, "base and queries must have the same dimension"
+    idx = np.empty((nq, nnn), dtype=np.int32)
+    dis = np.empty((nq, nnn), dtype=np.float32)
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
+    opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0)
+    rc = lib().yael_gpu_knn_ex(nq, nb, d, nnn, _ptr(base), _ptr(queries), _ptr(idx), _ptr(dis),
+                               ctypes.byref(opts))
+    if rc != 0:
+        raise RuntimeError(f"yael_gpu_knn_ex failed ({rc}): {last_error()}")
+    if stats:
+        return idx, dis, {"n_fallback": opts.n_fallback, "n_candidates": opts.n_candidates,
+                          "exact_class": opts.exact_class}
+    return idx, dis
+
+
+def cross_distances(a, b, distance_type=12):
+    """dis[j, i] = distance(a_i, b_j) (yael/ynumpy.py:69-84)."""
+    a = _f32(a)
+    b = _f32(b)
+    na, d = a.shape
+    nb, d2 = b.shape
+    assert d == d2
+    dis = np.empty((nb, na), dtype=np.float32)
+    lib().compute_cross_distances_alt_nonpacked(distance_type, d, na, nb, _ptr(a), d, _ptr(b), d,
+                                                _ptr(dis), na)
+    return dis

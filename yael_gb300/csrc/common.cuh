@@ -1,0 +1,107 @@
+// Shared definitions for the GB300 (sm_103a) implementation of yael's
+// distance-GEMM path: error handling, the per-thread stream, the grow-only
+// workspace, small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+#include <cstddef>
+#include <string>
+#include <vector>
+
+namespace yg {
+
+// ---------------------------------------------------------------------------
+// errors.  yael signals failure by assert()/abort() (nn.c:456, vector.c:34-41);
+// the drop-in entry points keep that convention (message on stderr, abort),
+// the *_ex entry points return a status and leave the message for
+// yael_gpu_last_error().
+enum Status : int {
+  OK = 0,
+  E_CUDA = 1,
+  E_ARG = 2,
+  E_UNSUPPORTED = 3,
+  E_NOMEM = 4,
+  E_TIMEOUT = 5,
+};
+
+void set_error(int code, const char *fmt, ...);
+int last_code();
+const char *last_message();
+[[noreturn]] void fatal_last(const char *where);
+
+#define YG_CUDA(call)                                                      \
+  do {                                                                     \
+    cudaError_t _e = (call);                                               \
+    if (_e != cudaSuccess) {                                               \
+      ::yg::set_error(::yg::E_CUDA, "%s:%d %s: %s", __FILE__, __LINE__,    \
+                      #call, cudaGetErrorString(_e));                      \
+      return ::yg::E_CUDA;                                                 \
+    }                                                                      \
+  } while (0)
+
+#define YG_CHECK(expr)                 \
+  do {                                 \
+    int _s = (expr);                   \
+    if (_s != ::yg::OK) return _s;     \
+  } while (0)
+
+#define YG_LAUNCH_CHECK() YG_CUDA(cudaGetLastError())
+
+// ---------------------------------------------------------------------------
+// execution context: one device per process (the current device at first
+// use), one non-blocking stream per calling host thread, one grow-only device
+// workspace per host thread.  Callers may run concurrently from several host
+// threads (the reference is reentrant, yael.swg:140-144).
+struct Workspace {
+  struct Buf {
+    void *p = nullptr;
+    size_t n = 0;
+  };
+  std::vector<Buf> bufs;
+  // slot-addressed scratch: the same slot is reused by every call.
+  int get(int slot, size_t bytes, void **out);
+  void release_all();
+  ~Workspace();
+};
+
+struct Ctx {
+  int device = 0;
+  int num_sms = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  Workspace ws;
+  Workspace host_ws;  // pinned host staging
+};
+
+// returns the calling thread's context (created on first use)
+int ctx_get(Ctx **out);
+
+// precision of the distance pass
+enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1 };
+int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16), default fp32
+
+// ---------------------------------------------------------------------------
+// device helpers
+__host__ __device__ inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
+__host__ __device__ inline int imin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
+
+// order-preserving map float -> uint32 (NaN sorts above +inf for +NaN)
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__device__ __forceinline__ unsigned long long d2ord(double f) {
+  unsigned long long u = __double_as_longlong(f);
+  return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+}  // namespace yg

@@ -1,0 +1,383 @@
+// Exact k-NN: the device pipeline (prepare -> fused distance pass with
+// selection -> re-rank + certificate -> exhaustive fallback) and the nn.h
+// drop-in entry points (yael/nn.h:41-83).
+#include <math.h>
+#include <string.h>
+
+#include "knn.cuh"
+#include "tc_scan.cuh"
+#include "../../include/yael_gpu.h"
+
+namespace yg {
+
+namespace {
+
+struct Small {
+  SetStats bs;
+  int fail_cnt;
+  int pad;
+  unsigned long long n_cand;
+};
+
+template <typename T>
+int ws_get(Workspace &ws, int slot, size_t count, T **p) {
+  void *v = nullptr;
+  YG_CHECK(ws.get(slot, count * sizeof(T), &v));
+  *p = reinterpret_cast<T *>(v);
+  return OK;
+}
+
+int pow2_at_least(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+__global__ void fill_f32(float *p, long n, float v) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// distance pass on whichever producer the precision selects
+int scan(const KnnJob &job, const float *q, int nq, const float *b, long ldb, int nb,
+         const float *bn, long bn_stride, const TcOperands *tc, const ScanSel &sel,
+         cudaStream_t st) {
+  if (job.prec == PREC_BF16) return tc_scan(*tc, nq, nb, sel, st);
+  return simt_scan(q, job.ldq, nq, b, ldb, nb, job.d, bn, bn_stride, job.metric, sel, st);
+}
+
+// one batch of queries (all buffers sized for nq of this batch)
+int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOperands *tcb,
+              int bstats_exact) {
+  Workspace &ws = ctx->ws;
+  const int nq = job.nq, nb = job.nb, d = job.d, k = job.k;
+  const bool bf16 = job.prec == PREC_BF16;
+  double *qn64;
+  unsigned char *qflag, *qexact;
+  float *qres = nullptr, *eps, *bn32 = nullptr;
+  YG_CHECK(ws_get(ws, WS_QN64, nq, &qn64));
+  YG_CHECK(ws_get(ws, WS_QFLAG, nq, &qflag));
+  YG_CHECK(ws_get(ws, WS_QEXACT, nq, &qexact));
+  YG_CHECK(ws_get(ws, WS_EPS, nq, &eps));
+  YG_CHECK(ws_get(ws, WS_QRES, nq, &qres));
+  YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32));  // written by knn_device
+
+  TcOperands tcq;
+  if (bf16) {
+    tcq = *tcb;
+    YG_CHECK(tc_prepare_queries(job.q, job.ldq, nq, d, job.metric, ws, WS_QPACK, WS_QNORMP,
+                                &tcq, qn64, qflag, qres, st));
+  } else {
+    YG_CHECK(prep_rows(job.q, job.ldq, nq, d, 1.f, qn64, nullptr, qflag, qres, nullptr, 0,
+                       nullptr, 0, nullptr, st));
+  }
+  YG_CHECK(compute_eps(nq, d, job.prec, job.metric, qn64, qres, qflag, &dsmall->bs, eps,
+                       qexact, st));
+
+  int *fail_list;
+  YG_CHECK(ws_get(ws, WS_FAIL, nq, &fail_list));
+  YG_CUDA(cudaMemsetAsync(&dsmall->fail_cnt, 0, sizeof(int), st));
+
+  RerankArgs ra;
+  ra.nq = nq; ra.nb = nb; ra.d = d; ra.k = k; ra.metric = job.metric;
+  ra.q = job.q; ra.ldq = job.ldq; ra.b = job.b; ra.ldb = job.ldb;
+  ra.qn64 = qn64; ra.eps = eps; ra.qexact = qexact; ra.bstats = &dsmall->bs;
+  ra.out_idx = job.out_idx; ra.out_dis = job.out_dis;
+  ra.fail_list = fail_list; ra.fail_cnt = &dsmall->fail_cnt; ra.n_cand = &dsmall->n_cand;
+
+  const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N;
+  const int tile_m = bf16 ? TC_TILE_M : 128;
+  const int nqt = (int)ceil_div(nq, tile_m);
+  const int ntb = (int)ceil_div(nb, tile_n);
+  const int ctas_per_sm = 1;
+  const int c_needed = bstats_exact ? k : 2 * k;
+
+  ScanSel sel;
+  if (c_needed <= 32) {
+    // ---- TOPC over the full base
+    sel.mode = SCAN_TOPC;
+    sel.C = pow2_at_least(c_needed);
+    int nchunk = choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4);
+    nchunk = imin(nchunk, kMaxCandidates / sel.C);
+    sel.nchunk = nchunk;
+    sel.tiles_per_chunk = (int)ceil_div(ntb, nchunk);
+    sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)sel.nchunk * nq * sel.C, &sel.topv));
+    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)sel.nchunk * nq * sel.C, &sel.topi));
+    YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
+  } else {
+    // ---- THRESH: thresholds from a strided sample of the base
+    sel.mode = SCAN_THRESH;
+    float *thr;
+    int *cnt;
+    YG_CHECK(ws_get(ws, WS_THR, nq, &thr));
+    YG_CHECK(ws_get(ws, WS_CNT, nq, &cnt));
+    const int c = 32;
+    int stride = (int)floor((double)k * 0.95 / ((double)c - 5.0 * sqrt((double)c)));
+    if (stride < 1) stride = 1;
+    const int ns = nb / stride;
+    if (nb <= kMaxCandidates || ns < 2 * c) {
+      sel.cap = pow2_at_least(nb);
+      if (sel.cap > kMaxCandidates) sel.cap = kMaxCandidates;
+      fill_f32<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(thr, nq, INFINITY);
+      YG_LAUNCH_CHECK();
+    } else {
+      sel.cap = imin(kMaxCandidates, pow2_at_least(3 * c * stride));
+      ScanSel ss;
+      ss.mode = SCAN_TOPC;
+      ss.C = c;
+      const int nts = (int)ceil_div(ns, tile_n);
+      int nch = choose_chunks(nqt, nts, ctx->num_sms, ctas_per_sm, 2);
+      nch = imin(nch, 64);
+      ss.tiles_per_chunk = (int)ceil_div(nts, nch);
+      ss.nchunk = (int)ceil_div(nts, ss.tiles_per_chunk);
+      YG_CHECK(ws_get(ws, WS_STOPV, (size_t)ss.nchunk * nq * c, &ss.topv));
+      YG_CHECK(ws_get(ws, WS_STOPI, (size_t)ss.nchunk * nq * c, &ss.topi));
+      if (bf16) {
+        TcOperands tcs = tcq;
+        YG_CHECK(tc_base_view(*tcb, stride, ns, &tcs));
+        YG_CHECK(tc_scan(tcs, nq, ns, ss, st));
+      } else {
+        YG_CHECK(simt_scan(job.q, job.ldq, nq, job.b, job.ldb * stride, ns, d, bn32, stride,
+                           job.metric, ss, st));
+      }
+      YG_CHECK(thresh_from_sample(nq, ss.nchunk, c, c, ss.topv, eps, thr, st));
+    }
+    sel.thr = thr;
+    sel.cnt = cnt;
+    YG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * nq, st));
+    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nq * sel.cap, &sel.candv));
+    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nq * sel.cap, &sel.candi));
+    sel.nchunk = imin(choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 4096);
+    sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
+    sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
+  }
+  ra.sel = sel;
+  YG_CHECK(rerank(ra, st));
+
+  // ---- exhaustive path for the queries the certificate rejected
+  Small hs;
+  YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
+  YG_CUDA(cudaStreamSynchronize(st));
+  job.n_fallback += hs.fail_cnt;
+  job.n_cand = (long long)hs.n_cand;
+  if (hs.fail_cnt > 0) {
+    size_t per = exhaustive_bytes_per_query(nb);
+    size_t want = per * (size_t)hs.fail_cnt;
+    const size_t cap_bytes = (size_t)1 << 30;
+    if (want > cap_bytes) want = cap_bytes > per ? cap_bytes : per;
+    void *scratch;
+    YG_CHECK(ws.get(WS_EXH, want, &scratch));
+    YG_CHECK(exhaustive(hs.fail_cnt, fail_list, nb, d, k, job.metric, job.q, job.ldq, job.b,
+                        job.ldb, nullptr, job.out_idx, job.out_dis, scratch, want, st));
+  }
+  return OK;
+}
+
+}  // namespace
+
+int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
+  const int nq = job.nq, nb = job.nb, d = job.d, k = job.k;
+  job.n_fallback = 0;
+  job.n_cand = 0;
+  job.exact_class = 0;
+  if (nq < 0 || nb < 1 || d < 1 || k < 1) {
+    set_error(E_ARG, "knn: invalid sizes nq=%d nb=%d d=%d k=%d", nq, nb, d, k);
+    return E_ARG;
+  }
+  if (k > nb) {
+    set_error(E_ARG, "knn: k=%d > nb=%d (yael asserts k <= nb)", k, nb);
+    return E_ARG;
+  }
+  if (k > kMaxK) {
+    set_error(E_UNSUPPORTED, "knn: k=%d above the supported maximum %d", k, kMaxK);
+    return E_UNSUPPORTED;
+  }
+  if (job.metric != METRIC_L2 && job.metric != METRIC_DOT) {
+    set_error(E_UNSUPPORTED, "knn: distance_type %d not supported on the GPU", job.metric);
+    return E_UNSUPPORTED;
+  }
+  if (nq == 0) return OK;
+  if (job.prec == PREC_BF16 && !tc_supported(d)) job.prec = PREC_FP32;
+  Workspace &ws = ctx->ws;
+
+  Small *dsmall;
+  YG_CHECK(ws_get(ws, WS_SMALL, 1, &dsmall));
+  {
+    Small h;
+    memset(&h, 0, sizeof(h));
+    h.bs.all_exact = 1;
+    YG_CUDA(cudaMemcpyAsync(dsmall, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  }
+
+  if (job.w) {
+    // weighted distances reorder per base row: exhaustive exact path
+    size_t per = exhaustive_bytes_per_query(nb);
+    size_t want = per * (size_t)nq;
+    const size_t cap_bytes = (size_t)1 << 30;
+    if (want > cap_bytes) want = cap_bytes > per ? cap_bytes : per;
+    void *scratch;
+    YG_CHECK(ws.get(WS_EXH, want, &scratch));
+    YG_CHECK(exhaustive(nq, nullptr, nb, d, k, job.metric, job.q, job.ldq, job.b, job.ldb,
+                        job.w, job.out_idx, job.out_dis, scratch, want, st));
+    job.n_fallback = nq;
+    return OK;
+  }
+
+  // base preparation (once for all query batches)
+  float *bn32, *bres = nullptr;
+  YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32));
+  TcOperands tcb;
+  if (job.prec == PREC_BF16) {
+    YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK, WS_BNORMP,
+                             WS_BRES, &tcb, bn32, &dsmall->bs, st));
+  } else {
+    YG_CHECK(prep_rows(job.b, job.ldb, nb, d, 1.f, nullptr, bn32, nullptr, bres, nullptr, 0,
+                       nullptr, 0, &dsmall->bs, st));
+  }
+  Small hs;
+  YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
+  YG_CUDA(cudaStreamSynchronize(st));
+  const int bexact = hs.bs.all_exact;
+  job.exact_class = bexact;
+
+  // query batches bounded by the candidate buffers (<= 1 GiB)
+  const size_t per_query = (size_t)kMaxCandidates * 8 + 64;
+  int qbatch = (int)imin(nq, (int)imax(256, (int)(((size_t)1 << 30) / per_query)));
+  for (int q0 = 0; q0 < nq; q0 += qbatch) {
+    KnnJob sub = job;
+    sub.nq = imin(qbatch, nq - q0);
+    sub.q = job.q + (long)q0 * job.ldq;
+    sub.out_idx = job.out_idx + (long)q0 * k;
+    sub.out_dis = job.out_dis + (long)q0 * k;
+    sub.n_fallback = 0;
+    YG_CHECK(knn_batch(sub, ctx, st, dsmall, &tcb, bexact));
+    job.n_fallback += sub.n_fallback;
+    job.n_cand += sub.n_cand;
+  }
+  if (job.prec == PREC_BF16) YG_CHECK(tc_take_error(st));
+  return OK;
+}
+
+// host-memory entry: copies in, runs, copies out
+static int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
+                    const float *q, const float *w, int *assign, float *dis, int prec,
+                    yael_gpu_knn_opts *opts) {
+  Ctx *ctx;
+  YG_CHECK(ctx_get(&ctx));
+  cudaStream_t st = ctx->stream;
+  KnnJob job;
+  job.nq = nq; job.nb = nb; job.d = d; job.k = k; job.metric = metric; job.prec = prec;
+  job.ldq = d; job.ldb = d;
+  if (opts && opts->device_ptrs) {
+    if (opts->stream) st = (cudaStream_t)opts->stream;
+    job.q = q; job.b = b; job.w = w; job.out_idx = assign; job.out_dis = dis;
+    YG_CHECK(knn_device(job, ctx, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+  } else {
+    if (nq == 0) return OK;
+    Workspace &ws = ctx->ws;
+    float *db, *dq, *dw = nullptr, *ddis;
+    int *didx;
+    YG_CHECK(ws_get(ws, WS_H_B, (size_t)nb * d, &db));
+    YG_CHECK(ws_get(ws, WS_H_Q, (size_t)nq * d, &dq));
+    YG_CHECK(ws_get(ws, WS_H_IDX, (size_t)nq * k, &didx));
+    YG_CHECK(ws_get(ws, WS_H_DIS, (size_t)nq * k, &ddis));
+    YG_CUDA(cudaMemcpyAsync(db, b, sizeof(float) * nb * (size_t)d, cudaMemcpyHostToDevice, st));
+    YG_CUDA(cudaMemcpyAsync(dq, q, sizeof(float) * nq * (size_t)d, cudaMemcpyHostToDevice, st));
+    if (w) {
+      YG_CHECK(ws_get(ws, WS_H_W, (size_t)nb, &dw));
+      YG_CUDA(cudaMemcpyAsync(dw, w, sizeof(float) * nb, cudaMemcpyHostToDevice, st));
+    }
+    job.q = dq; job.b = db; job.w = dw; job.out_idx = didx; job.out_dis = ddis;
+    YG_CHECK(knn_device(job, ctx, st));
+    YG_CUDA(cudaMemcpyAsync(assign, didx, sizeof(int) * nq * (size_t)k, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaMemcpyAsync(dis, ddis, sizeof(float) * nq * (size_t)k, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+  }
+  if (opts) {
+    opts->n_fallback = job.n_fallback;
+    opts->n_candidates = (int)(job.n_cand > 0x7fffffff ? 0x7fffffff : job.n_cand);
+    opts->exact_class = job.exact_class;
+  }
+  return OK;
+}
+
+static int metric_of(int distance_type) {
+  if (distance_type == 2 || distance_type == 12) return METRIC_L2;
+  if (distance_type == 16) return METRIC_DOT;
+  return -1;
+}
+
+}  // namespace yg
+
+using namespace yg;
+
+extern "C" {
+
+int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q,
+                    int *assign, float *dis, yael_gpu_knn_opts *opts) {
+  int prec = default_precision();
+  int metric = METRIC_L2;
+  if (opts) {
+    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16)
+      prec = opts->precision;
+    if (opts->metric) metric = metric_of(opts->metric);
+  }
+  if (metric < 0) {
+    set_error(E_UNSUPPORTED, "distance_type %d not supported", opts ? opts->metric : 0);
+    return E_UNSUPPORTED;
+  }
+  return knn_host(metric, nq, nb, d, k, b, q, nullptr, assign, dis, prec, opts);
+}
+
+void knn_full(int distance_type, int nq, int nb, int d, int k, const float *b,
+              const float *q, const float *b_weights, int *assign, float *dis) {
+  const int metric = metric_of(distance_type);
+  if (metric < 0) {
+    set_error(E_UNSUPPORTED,
+              "distance_type %d has no GPU implementation (supported: 2, 12, 16)",
+              distance_type);
+    fatal_last("knn_full");
+  }
+  if (knn_host(metric, nq, nb, d, k, b, q, b_weights, assign, dis, default_precision(),
+               nullptr) != OK)
+    fatal_last("knn_full");
+}
+
+void knn_full_thread(int distance_type, int nq, int nb, int d, int k, const float *b,
+                     const float *q, const float *b_weights, int *assign, float *dis,
+                     int n_thread) {
+  (void)n_thread;
+  knn_full(distance_type, nq, nb, d, k, b, q, b_weights, assign, dis);
+}
+
+double nn(int n, int nb, int d, const float *b, const float *v, int *assign) {
+  float *dis = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+  knn_full(2, n, nb, d, 1, b, v, nullptr, assign, dis);
+  double s = 0;  // fvec_sum order (yael/vector.c:2066-2073)
+  for (long i = 0; i < n; i++) s += dis[i];
+  free(dis);
+  return s;
+}
+
+double nn_thread(int n, int nb, int d, const float *b, const float *v, int *assign,
+                 int n_thread) {
+  (void)n_thread;
+  return nn(n, nb, d, b, v, assign);
+}
+
+float *knn(int n, int nb, int d, int k, const float *b, const float *v, int *assign) {
+  float *dis = (float *)malloc(sizeof(float) * (size_t)n * k + 4);
+  knn_full(2, n, nb, d, k, b, v, nullptr, assign, dis);
+  return dis;
+}
+
+float *knn_thread(int nq, int nb, int d, int k, const float *b, const float *v,
+                  int *assign, int n_thread) {
+  (void)n_thread;
+  return knn(nq, nb, d, k, b, v, assign);
+}
+
+}  // extern "C"

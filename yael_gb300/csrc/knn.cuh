@@ -1,0 +1,37 @@
+// Device-level exact k-NN driver shared by the drop-in entry points, the
+// k-means assignment step and the batched calls.
+#pragma once
+#include "select.cuh"
+
+namespace yg {
+
+struct KnnJob {
+  int nq = 0, nb = 0, d = 0, k = 1;
+  int metric = METRIC_L2;
+  int prec = PREC_FP32;
+  const float *q = nullptr;  // device, nq x d (row stride ldq)
+  long ldq = 0;
+  const float *b = nullptr;  // device, nb x d (row stride ldb)
+  long ldb = 0;
+  const float *w = nullptr;  // device base weights or null
+  int *out_idx = nullptr;    // device nq x k
+  float *out_dis = nullptr;  // device nq x k
+  // filled on return
+  int n_fallback = 0;
+  long long n_cand = 0;
+  int exact_class = 0;
+};
+
+// Runs the whole pipeline on stream st using the calling thread's workspace.
+int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st);
+
+// workspace slots (each slot is one grow-only device buffer per host thread)
+enum WsSlot : int {
+  WS_QN64 = 0, WS_QFLAG, WS_QRES, WS_BN32, WS_SMALL, WS_EPS, WS_QEXACT,
+  WS_TOPV, WS_TOPI, WS_THR, WS_CNT, WS_FAIL, WS_STOPV, WS_STOPI, WS_EXH,
+  WS_QPACK, WS_BPACK, WS_QNORMP, WS_BNORMP, WS_BRES,
+  WS_H_B = 40, WS_H_Q, WS_H_W, WS_H_IDX, WS_H_DIS, WS_H_EXTRA,
+  WS_KM0 = 60,  // k-means / hkm slots start here
+};
+
+}  // namespace yg

@@ -1,0 +1,117 @@
+// Runtime pieces: per-thread error state, per-thread stream and workspace,
+// configuration from the environment.
+#include <stdarg.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "../../include/yael_gpu.h"
+
+namespace yg {
+
+static thread_local int t_code = OK;
+static thread_local char t_msg[1024] = "";
+
+void set_error(int code, const char *fmt, ...) {
+  t_code = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(t_msg, sizeof(t_msg), fmt, ap);
+  va_end(ap);
+}
+int last_code() { return t_code; }
+const char *last_message() { return t_msg; }
+
+void fatal_last(const char *where) {
+  fprintf(stderr, "yael_gb300: %s failed: %s\n", where, t_msg[0] ? t_msg : "(no message)");
+  fflush(stderr);
+  abort();
+}
+
+int Workspace::get(int slot, size_t bytes, void **out) {
+  if (slot >= (int)bufs.size()) bufs.resize(slot + 1);
+  Buf &b = bufs[slot];
+  if (bytes == 0) bytes = 256;
+  if (b.n < bytes) {
+    if (b.p) {
+      cudaError_t e = cudaFree(b.p);
+      b.p = nullptr;
+      b.n = 0;
+      if (e != cudaSuccess) {
+        set_error(E_CUDA, "cudaFree: %s", cudaGetErrorString(e));
+        return E_CUDA;
+      }
+    }
+    size_t n = bytes + bytes / 8;  // headroom so slowly growing sizes do not thrash
+    n = (n + 255) & ~(size_t)255;
+    cudaError_t e = cudaMalloc(&b.p, n);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      b.p = nullptr;
+      set_error(E_NOMEM, "cudaMalloc(%zu bytes, workspace slot %d): %s", n, slot,
+                cudaGetErrorString(e));
+      return E_NOMEM;
+    }
+    b.n = n;
+  }
+  *out = b.p;
+  return OK;
+}
+
+void Workspace::release_all() {
+  for (auto &b : bufs)
+    if (b.p) cudaFree(b.p);
+  bufs.clear();
+}
+
+Workspace::~Workspace() { release_all(); }
+
+static thread_local Ctx *t_ctx = nullptr;
+
+int ctx_get(Ctx **out) {
+  if (t_ctx) {
+    *out = t_ctx;
+    return OK;
+  }
+  Ctx *c = new Ctx();
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    set_error(E_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    return E_CUDA;
+  }
+  cudaDeviceProp p;
+  e = cudaGetDeviceProperties(&p, c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    set_error(E_CUDA, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    return E_CUDA;
+  }
+  c->num_sms = p.multiProcessorCount;
+  c->cc_major = p.major;
+  c->cc_minor = p.minor;
+  c->smem_optin = p.sharedMemPerBlockOptin;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    set_error(E_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    return E_CUDA;
+  }
+  t_ctx = c;
+  *out = c;
+  return OK;
+}
+
+int default_precision() {
+  const char *s = getenv("YAEL_GPU_PRECISION");
+  if (!s || !*s) return PREC_FP32;
+  if (!strcmp(s, "bf16") || !strcmp(s, "BF16") || !strcmp(s, "1")) return PREC_BF16;
+  return PREC_FP32;
+}
+
+}  // namespace yg
+
+extern "C" const char *yael_gpu_last_error(void) { return yg::last_message(); }
+
+extern "C" int yael_gpu_version(void) { return YAEL_GPU_ABI_VERSION; }

@@ -1,0 +1,533 @@
+// Candidate re-ranking with the exactness certificate, THRESH thresholds,
+// per-query error bounds, and the exhaustive FP64 fallback (see select.cuh).
+#include <float.h>
+#include <math.h>
+
+#include "select.cuh"
+
+namespace yg {
+
+namespace {
+
+constexpr int RT = 256;  // threads per re-rank block
+constexpr float kU = 5.9604645e-08f;  // 2^-24
+
+__device__ __forceinline__ bool lex_less(unsigned long long ka, int ia,
+                                         unsigned long long kb, int ib) {
+  return ka < kb || (ka == kb && (unsigned)ia < (unsigned)ib);
+}
+
+// ascending bitonic sort of n (power of two) (key, id) pairs in shared memory
+__device__ void bitonic_sort(unsigned long long *K, int *I, int n) {
+  for (int size = 2; size <= n; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < (n >> 1); i += blockDim.x) {
+        const int lo = 2 * i - (i & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const unsigned long long klo = K[lo], khi = K[hi];
+        const int ilo = I[lo], ihi = I[hi];
+        const bool gt = lex_less(khi, ihi, klo, ilo);
+        if (gt == up) {
+          K[lo] = khi; K[hi] = klo;
+          I[lo] = ihi; I[hi] = ilo;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__device__ __forceinline__ int next_pow2(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// distance of query row qv (in shared memory) to base row j, FP32, by one warp
+__device__ __forceinline__ float warp_dist32(const float *qv, const float *brow, int d,
+                                             int metric) {
+  const int lane = threadIdx.x & 31;
+  float acc = 0.f;
+  for (int c = lane; c < d; c += 32) {
+    const float bv = __ldg(brow + c);
+    if (metric == METRIC_L2) {
+      const float t = qv[c] - bv;
+      acc = fmaf(t, t, acc);
+    } else {
+      acc = fmaf(qv[c], bv, acc);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
+// FP64 distance, sequential over coordinates (the oracle's summation order)
+__device__ __forceinline__ double dist64_seq(const float *qv, const float *brow, int d,
+                                             int metric) {
+  double s = 0;
+  for (int c = 0; c < d; c++) {
+    if (metric == METRIC_L2) {
+      const double t = (double)qv[c] - (double)__ldg(brow + c);
+      s += t * t;
+    } else {
+      s += (double)qv[c] * (double)__ldg(brow + c);
+    }
+  }
+  return s;
+}
+
+__global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  unsigned long long *K = reinterpret_cast<unsigned long long *>(sm_raw);
+  int *I = reinterpret_cast<int *>(K + Mp_alloc);
+  float *E = reinterpret_cast<float *>(I + Mp_alloc);
+  float *qv = E + Mp_alloc;  // the query row, d floats
+  __shared__ int sM, sfail, snband, sneed64;
+  __shared__ unsigned long long sT;  // TOPC boundary key (lexicographic (v, id))
+
+  const int q = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int k = a.k, d = a.d;
+  const bool L2 = a.metric == METRIC_L2;
+  const double qn = L2 ? a.qn64[q] : 0.0;
+  const float eps = a.eps ? a.eps[q] : 0.f;
+  const bool ex = a.qexact ? a.qexact[q] != 0 : false;
+
+  if (tid == 0) {
+    sM = 0; sfail = 0; sneed64 = 0;
+    sT = ~0ull;
+  }
+  for (int c = tid; c < d; c += RT) qv[c] = a.q[(long)q * a.ldq + c];
+  __syncthreads();
+
+  // ---- 1. gather candidates as (approx dist, id)
+  const ScanSel &s = a.sel;
+  if (s.mode == SCAN_TOPC) {
+    const int total = s.nchunk * s.C;
+    for (int idx = tid; idx < total; idx += RT) {
+      const int ch = idx / s.C, sl = idx - ch * s.C;
+      const long o = ((long)ch * a.nq + q) * s.C + sl;
+      const int id = s.topi[o];
+      if (id < 0) continue;
+      const float v = s.topv[o];
+      const float av = L2 ? (float)((double)v + qn) : v;
+      const int pos = atomicAdd(&sM, 1);
+      K[pos] = f2ord(av);
+      I[pos] = id;
+      if (sl == s.C - 1) {  // full chunk: its last entry bounds everything it dropped
+        const unsigned long long key = ((unsigned long long)f2ord(av) << 32) | (unsigned)id;
+        atomicMin(&sT, key);
+      }
+    }
+  } else {
+    const int cnt = s.cnt[q];
+    if (cnt > s.cap) {
+      if (tid == 0) sfail = 1;
+    } else {
+      for (int idx = tid; idx < cnt; idx += RT) {
+        const float v = s.candv[(long)q * s.cap + idx];
+        const float av = L2 ? (float)((double)v + qn) : v;
+        K[idx] = f2ord(av);
+        I[idx] = s.candi[(long)q * s.cap + idx];
+      }
+      if (tid == 0) sM = cnt;
+    }
+  }
+  __syncthreads();
+  const int M = sM;
+  if (sfail || M < k || M > Mp_alloc) goto failed;
+  {
+    const int Mp = next_pow2(M);
+    for (int i = M + tid; i < Mp; i += RT) { K[i] = ~0ull; I[i] = 0x7fffffff; }
+    __syncthreads();
+    bitonic_sort(K, I, Mp);
+    if (a.n_cand && tid == 0) atomicAdd(a.n_cand, (unsigned long long)M);
+
+    // boundary of the non-candidates, dist space
+    double bound;        // every non-candidate has approx >= bound (TOPC) / > bound (THRESH)
+    bool bound_strict;   // true: non-candidates are strictly above bound
+    if (s.mode == SCAN_TOPC) {
+      bound = (sT == ~0ull) ? INFINITY : (double)ord2f((unsigned)(sT >> 32));
+      bound_strict = false;
+    } else {
+      const float t = s.thr[q];
+      bound = L2 ? (double)t + qn : (double)t;
+      bound_strict = true;
+    }
+
+    if (ex) {
+      // approx values are exact: the sorted prefix is the answer.  TOPC:
+      // certified when (a_k, id_k) <= the lexicographic boundary.
+      if (s.mode == SCAN_TOPC && sT != ~0ull) {
+        const unsigned long long kk = K[k - 1];
+        const unsigned long long tk = sT >> 32;
+        const int tidb = (int)(sT & 0xffffffffu);
+        if (!(kk < tk || (kk == tk && (unsigned)I[k - 1] <= (unsigned)tidb))) goto failed;
+      }
+      for (int r = tid; r < k; r += RT) {
+        a.out_idx[(long)q * k + r] = I[r];
+        a.out_dis[(long)q * k + r] = ord2f((unsigned)K[r]);
+      }
+      return;
+    }
+
+    // ---- 2. band of candidates that can still be in the top k
+    const float ak = ord2f((unsigned)K[k - 1]);
+    const double slack = 4e-7 * fabs((double)ak) + 1e-30;
+    const double lim = (double)ak + 2.0 * (double)eps + slack;
+    if (tid == 0) snband = 0;
+    __syncthreads();
+    {
+      int local = 0;
+      for (int i = tid; i < M; i += RT)
+        if ((double)ord2f((unsigned)K[i]) <= lim) local++;
+      atomicAdd(&snband, local);
+    }
+    __syncthreads();
+    const int nband = snband;  // >= k: the sorted prefix up to a_k is inside
+
+    // ---- 3. FP32 re-rank of the band
+    const int warp = tid >> 5, nw = RT / 32;
+    for (int i = warp; i < nband; i += nw) {
+      const float e = warp_dist32(qv, a.b + (long)I[i] * a.ldb, d, a.metric);
+      if ((tid & 31) == 0) E[i] = e;
+    }
+    __syncthreads();
+    const int nbp = next_pow2(nband);
+    for (int i = tid; i < nbp; i += RT) {
+      if (i < nband) K[i] = f2ord(E[i]);
+      else { K[i] = ~0ull; I[i] = 0x7fffffff; }
+    }
+    __syncthreads();
+    bitonic_sort(K, I, nbp);
+
+    // error model of the FP32 re-rank
+    const float rho = (float)(d + 4) * kU;
+    float eta = 0.f;
+    if (!L2) {
+      const float B = __uint_as_float(a.bstats->max_norm_bits);
+      eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64 ? a.qn64[q] : 0.0, 0.0)) * B;
+    }
+    // near ties anywhere up to position k -> FP64 for the whole band
+    const int lastpair = imin(k, nband - 1);
+    for (int i = tid; i < lastpair; i += RT) {
+      const float e0 = ord2f((unsigned)K[i]), e1 = ord2f((unsigned)K[i + 1]);
+      const float tol = rho * (fabsf(e0) + fabsf(e1)) + 2.f * eta;
+      if (e1 - e0 <= tol) sneed64 = 1;
+    }
+    __syncthreads();
+    double ek_hi;
+    if (sneed64) {
+      // one thread per candidate, sequential FP64 sum
+      for (int i = tid; i < nband; i += RT) {
+        const double e = dist64_seq(qv, a.b + (long)I[i] * a.ldb, d, a.metric);
+        K[i] = d2ord(e);
+      }
+      __syncthreads();
+      bitonic_sort(K, I, nbp);
+      const unsigned long long kk = K[k - 1];
+      const unsigned long long u = (kk & 0x8000000000000000ull) ? (kk & 0x7fffffffffffffffull) : ~kk;
+      const double ek = __longlong_as_double((long long)u);
+      ek_hi = ek + 1e-12 * fabs(ek);
+      for (int r = tid; r < k; r += RT) {
+        const unsigned long long kr = K[r];
+        const unsigned long long ur = (kr & 0x8000000000000000ull) ? (kr & 0x7fffffffffffffffull) : ~kr;
+        a.out_idx[(long)q * k + r] = I[r];
+        a.out_dis[(long)q * k + r] = (float)__longlong_as_double((long long)ur);
+      }
+    } else {
+      const float ek = ord2f((unsigned)K[k - 1]);
+      ek_hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
+      for (int r = tid; r < k; r += RT) {
+        a.out_idx[(long)q * k + r] = I[r];
+        a.out_dis[(long)q * k + r] = ord2f((unsigned)K[r]);
+      }
+    }
+    // ---- 4. certificate: every non-candidate is provably worse than the k-th
+    const double bslack = 4e-7 * fabs(bound);
+    const double lowest_outside = bound - (double)eps - bslack;
+    const bool ok = bound_strict ? (ek_hi <= lowest_outside) : (ek_hi < lowest_outside);
+    if (ok) return;
+    __syncthreads();
+  }
+failed:
+  if (tid == 0) {
+    const int pos = atomicAdd(a.fail_cnt, 1);
+    a.fail_list[pos] = q;
+  }
+}
+
+__global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn64,
+                           const float *qres, const unsigned char *qflag,
+                           const SetStats *bs, float *eps, unsigned char *qexact) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const bool ex = qflag[q] && bs->all_exact;
+  qexact[q] = ex;
+  if (ex) { eps[q] = 0.f; return; }
+  const double u = 5.9604644775390625e-08;  // 2^-24
+  const double qn = sqrt(fmax(qn64[q], 0.0)) * (1 + 1e-6);
+  const double B = (double)__uint_as_float(bs->max_norm_bits);
+  double e;
+  if (prec == PREC_FP32) {
+    const double g = (d + 2) * u * 1.01;
+    e = metric == METRIC_L2 ? 2 * g * qn * B + u * (B * B + 2 * qn * B) + u * B * B
+                            : g * qn * B;
+  } else {
+    const double dq = qres ? (double)qres[q] : 0.0;
+    const double dB = (double)__uint_as_float(bs->max_resid_bits);
+    const double dot = dq * (B + dB) + qn * dB;
+    const double Kt = (double)(((d + 63) / 64) * 64 + 16);
+    const double acc = Kt * 2 * u * ((metric == METRIC_L2 ? 2 : 1) * (qn + dq) * (B + dB) +
+                                     (metric == METRIC_L2 ? 1.001 * B * B : 0.0));
+    e = metric == METRIC_L2 ? 2 * dot + u * B * B + acc : dot + acc;
+  }
+  e = e * 1.1 + 1e-30;
+  eps[q] = isfinite(e) ? (float)e : INFINITY;
+}
+
+__global__ void thresh_kernel(int nq, int nchunk, int C, int c, const float *topv,
+                              const float *eps, float *thr) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  // c-th smallest across the sorted per-chunk lists (small: linear merge)
+  int heads[64];
+  const int nc = nchunk < 64 ? nchunk : 64;
+  for (int i = 0; i < nc; i++) heads[i] = 0;
+  float v = INFINITY;
+  for (int r = 0; r < c; r++) {
+    int best = -1;
+    float bv = INFINITY;
+    for (int i = 0; i < nc; i++) {
+      if (heads[i] >= C) continue;
+      const float x = topv[((long)i * nq + q) * C + heads[i]];
+      if (x < bv) { bv = x; best = i; }
+    }
+    if (best < 0) { v = INFINITY; break; }
+    heads[best]++;
+    v = bv;
+  }
+  const double t = (double)v + 2.0 * (double)eps[q];
+  thr[q] = isfinite(t) ? __double2float_ru(t * (1 + 1e-7) + (t < 0 ? -t * 2e-7 : 0.0))
+                       : INFINITY;
+}
+
+// ---- exhaustive FP64 path ------------------------------------------------
+
+__global__ void fb_rows_kernel(const int *qlist, int q0, int nb, int d, int metric,
+                               const float *__restrict__ Q, long ldq,
+                               const float *__restrict__ B, long ldb,
+                               const float *__restrict__ w,
+                               unsigned long long *rows) {
+  extern __shared__ float qs[];
+  const int r = blockIdx.y;
+  const int qi = qlist ? qlist[q0 + r] : q0 + r;
+  for (int c = threadIdx.x; c < d; c += blockDim.x) qs[c] = Q[(long)qi * ldq + c];
+  __syncthreads();
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nb) return;
+  double e = dist64_seq(qs, B + j * ldb, d, metric);
+  if (w) e *= (double)w[j];
+  rows[(long)r * nb + j] = d2ord(e);
+}
+
+__global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0, int nb, int k,
+                                                       const unsigned long long *rows,
+                                                       int *out_idx, float *out_dis) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int kp = next_pow2(k);
+  unsigned long long *K = reinterpret_cast<unsigned long long *>(sm_raw);
+  int *I = reinterpret_cast<int *>(K + kp);
+  __shared__ unsigned int hist[256];
+  __shared__ unsigned long long sprefix, smask;
+  __shared__ int srank, snless, sneq_taken, svalid;
+  const int r = blockIdx.x;
+  const int qi = qlist ? qlist[q0 + r] : q0 + r;
+  const unsigned long long *row = rows + (long)r * nb;
+  const int tid = threadIdx.x;
+  const unsigned long long nan_lo = d2ord(INFINITY);  // keys above +inf are NaN
+
+  // number of non-NaN entries
+  if (tid == 0) svalid = 0;
+  __syncthreads();
+  {
+    int c = 0;
+    for (int j = tid; j < nb; j += RT) c += row[j] <= nan_lo;
+    atomicAdd(&svalid, c);
+  }
+  __syncthreads();
+  const int keff = imin(k, svalid);
+  if (keff > 0) {
+    if (tid == 0) { sprefix = 0; smask = 0; srank = keff - 1; }
+    __syncthreads();
+    for (int pass = 0; pass < 8; pass++) {
+      const int shift = 56 - 8 * pass;
+      for (int i = tid; i < 256; i += RT) hist[i] = 0;
+      __syncthreads();
+      const unsigned long long pre = sprefix, msk = smask;
+      for (int j = tid; j < nb; j += RT) {
+        const unsigned long long key = row[j];
+        if ((key & msk) == pre) atomicAdd(&hist[(key >> shift) & 255], 1u);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int rank = srank;
+        unsigned int cum = 0;
+        int dg = 0;
+        for (; dg < 256; dg++) {
+          if ((int)(cum + hist[dg]) > rank) break;
+          cum += hist[dg];
+        }
+        srank = rank - (int)cum;
+        sprefix = pre | ((unsigned long long)dg << shift);
+        smask = msk | (255ull << shift);
+      }
+      __syncthreads();
+    }
+    // sprefix = k-th key; take all smaller keys and the first srank+1 equal keys in index order
+    const unsigned long long kth = sprefix;
+    const int need_eq = srank + 1;
+    if (tid == 0) { snless = 0; sneq_taken = 0; }
+    __syncthreads();
+    for (int j0 = 0; j0 < nb; j0 += RT) {
+      const int j = j0 + tid;
+      const unsigned long long key = j < nb ? row[j] : ~0ull;
+      if (key < kth) {
+        const int pos = atomicAdd(&snless, 1);
+        K[pos] = key; I[pos] = j;
+      }
+      // ordered selection of equal keys
+      const bool eq = key == kth;
+      const unsigned ball = __ballot_sync(0xffffffffu, eq);
+      __shared__ int wsum[RT / 32];
+      const int lane = tid & 31, wid = tid >> 5;
+      if (lane == 0) wsum[wid] = __popc(ball);
+      __syncthreads();
+      int before = 0;
+      for (int w2 = 0; w2 < wid; w2++) before += wsum[w2];
+      const int rank_in = before + __popc(ball & ((1u << lane) - 1));
+      const int base = sneq_taken;
+      if (eq && base + rank_in < need_eq) {
+        const int pos = (keff - need_eq) + base + rank_in;
+        K[pos] = key; I[pos] = j;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int tot = 0;
+        for (int w2 = 0; w2 < RT / 32; w2++) tot += wsum[w2];
+        sneq_taken = base + tot;
+      }
+      __syncthreads();
+    }
+    for (int i = keff + tid; i < kp; i += RT) { K[i] = ~0ull; I[i] = 0x7fffffff; }
+    __syncthreads();
+    bitonic_sort(K, I, kp);
+  }
+  for (int i = tid; i < k; i += RT) {
+    if (i < keff) {
+      const unsigned long long kr = K[i];
+      const unsigned long long ur = (kr & 0x8000000000000000ull) ? (kr & 0x7fffffffffffffffull) : ~kr;
+      const float dv = (float)__longlong_as_double((long long)ur);
+      if (k == 1 && !(dv < 1e30f)) {
+        out_idx[(long)qi * k] = -1;
+        out_dis[(long)qi * k] = 1e30f;
+      } else {
+        out_idx[(long)qi * k + i] = I[i];
+        out_dis[(long)qi * k + i] = dv;
+      }
+    } else if (k == 1) {
+      out_idx[(long)qi * k] = -1;
+      out_dis[(long)qi * k] = 1e30f;
+    } else {
+      out_idx[(long)qi * k + i] = -1;
+      out_dis[(long)qi * k + i] = __uint_as_float(0xffffffffu);
+    }
+  }
+}
+
+}  // namespace
+
+int rerank(const RerankArgs &a, cudaStream_t st) {
+  if (a.nq <= 0) return OK;
+  int Mmax = a.sel.mode == SCAN_TOPC ? a.sel.nchunk * a.sel.C : a.sel.cap;
+  int Mp = 1;
+  while (Mp < Mmax) Mp <<= 1;
+  if (Mp > kMaxCandidates) {
+    set_error(E_ARG, "rerank: %d candidates per query exceed %d", Mmax, kMaxCandidates);
+    return E_ARG;
+  }
+  // K (8 B) + I (4 B) + E (4 B) per slot, then the query row
+  const size_t smem = (size_t)Mp * 16 + (size_t)a.d * 4 + 16;
+  static size_t attr = 48 * 1024;
+  if (smem > attr) {
+    YG_CUDA(cudaFuncSetAttribute(rerank_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = smem;
+  }
+  rerank_kernel<<<a.nq, RT, smem, st>>>(a, Mp);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int compute_eps(int nq, int d, int prec, int metric, const double *qn64,
+                const float *qres, const unsigned char *qflag, const SetStats *bstats,
+                float *eps, unsigned char *qexact, cudaStream_t st) {
+  if (nq <= 0) return OK;
+  eps_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(nq, d, prec, metric, qn64, qres,
+                                                          qflag, bstats, eps, qexact);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int thresh_from_sample(int nq, int nchunk, int C, int c, const float *topv,
+                       const float *eps, float *thr, cudaStream_t st) {
+  if (nq <= 0) return OK;
+  if (nchunk > 64) {
+    set_error(E_ARG, "thresh_from_sample: %d chunks > 64", nchunk);
+    return E_ARG;
+  }
+  thresh_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(nq, nchunk, C, c, topv, eps, thr);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int exhaustive(int nlist, const int *qlist_dev, int nb, int d, int k, int metric,
+               const float *q, long ldq, const float *b, long ldb, const float *w,
+               int *out_idx, float *out_dis, void *scratch, size_t scratch_bytes,
+               cudaStream_t st) {
+  if (nlist <= 0) return OK;
+  if (k > kMaxK) {
+    set_error(E_UNSUPPORTED, "k=%d above the supported maximum %d", k, kMaxK);
+    return E_UNSUPPORTED;
+  }
+  const size_t per = (size_t)nb * 8;
+  int batch = (int)(scratch_bytes / per);
+  if (batch < 1) {
+    set_error(E_NOMEM, "exhaustive: scratch of %zu bytes below one row of %zu", scratch_bytes, per);
+    return E_NOMEM;
+  }
+  if (batch > 65535) batch = 65535;
+  int kp = 1;
+  while (kp < k) kp <<= 1;
+  const size_t smem_sel = (size_t)kp * 12 + 16;
+  static size_t attr = 48 * 1024;
+  if (smem_sel > attr) {
+    YG_CUDA(cudaFuncSetAttribute(fb_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_sel));
+    attr = smem_sel;
+  }
+  unsigned long long *rows = reinterpret_cast<unsigned long long *>(scratch);
+  for (int q0 = 0; q0 < nlist; q0 += batch) {
+    const int nbt = imin(batch, nlist - q0);
+    dim3 g1((unsigned)ceil_div(nb, 256), (unsigned)nbt);
+    fb_rows_kernel<<<g1, 256, (size_t)d * 4, st>>>(qlist_dev, q0, nb, d, metric, q, ldq, b,
+                                                    ldb, w, rows);
+    YG_LAUNCH_CHECK();
+    fb_select_kernel<<<nbt, RT, smem_sel, st>>>(qlist_dev, q0, nb, k, rows, out_idx, out_dis);
+    YG_LAUNCH_CHECK();
+  }
+  return OK;
+}
+
+}  // namespace yg

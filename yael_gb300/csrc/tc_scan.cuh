@@ -1,0 +1,50 @@
+// BF16 tensor-core (tcgen05) producer of distance tiles with the fused
+// selection of scan.cuh.
+//
+// Operands are packed once per call: queries as bf16(-2 q) (L2) or bf16(q)
+// (dot), base rows as bf16(b); both padded to Kp = 64*ceil(d/64) columns.  For
+// L2 a 16-column side block carries ||b||^2 as three bf16 parts (hi, mid, lo;
+// their exact sum is the FP32 norm) and a matching block of ones on the query
+// side, so the MMA itself produces v = ||b||^2 - 2 q.b in FP32.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "prep.cuh"
+#include "scan.cuh"
+
+namespace yg {
+
+constexpr int TC_TILE_M = 128;  // query rows per tile (TMEM lanes)
+constexpr int TC_TILE_N = 256;  // base rows per tile (TMEM columns)
+
+struct TcOperands {
+  int d = 0, Kp = 0, metric = METRIC_L2;
+  const __nv_bfloat16 *q = nullptr;   // [nq][Kp]
+  const __nv_bfloat16 *qn = nullptr;  // [nq][16]   (L2)
+  const __nv_bfloat16 *b = nullptr;   // [rows][Kp]
+  const __nv_bfloat16 *bn = nullptr;  // [rows][16] (L2)
+  long b_rows = 0;                    // packed base rows
+  long b_step = 1;                    // scan row j reads packed row j*b_step
+};
+
+// true when the tensor-core pass handles this dimension (query tile resident
+// in shared memory: Kp <= 256)
+bool tc_supported(int d);
+
+int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Workspace &ws,
+                       int slot_pack, int slot_norm, TcOperands *op, double *qn64,
+                       unsigned char *qflag, float *qres, cudaStream_t st);
+
+int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspace &ws,
+                    int slot_pack, int slot_norm, int slot_res, TcOperands *op, float *bn32,
+                    SetStats *bs, cudaStream_t st);
+
+// strided view of the packed base (every stride-th row, nrows rows)
+int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out);
+
+int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
+
+// nonzero if a tensor-core pass gave up on a wait since the last call
+int tc_take_error(cudaStream_t st);
+
+}  // namespace yg
