@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark of the distance-GEMM hot path on GB300.
+
+Default workload: exact k-NN, L2, nb = 1,000,000 base and nq = 10,000 query
+vectors, d = 128, SIFT-like integer-valued float32 data, k = 100 (the k-NN
+configuration of the reference's headline metric).  One step = one complete
+exact k-NN of all queries (pack, threshold pass, fused BF16 tensor-core
+distance + selection pass, exact re-rank / certificate, fallback).
+
+Prints one JSON line (rank 0).  ``value`` is queries/s with the inputs already
+resident in HBM; ``e2e`` is the same metric through the drop-in C-ABI call
+``knn_full_thread`` with host (pinned) buffers, host<->device copies included.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
+import numpy as np  # noqa: E402
+
+METRIC = "k-means iters/s & exact kNN qps: BF16+rerank vs plain FP32, 1 GB300, exact ids"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 1900.0, 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_port_qps(b, q, k, budget_s=10.0, batch=250, max_q=5000):
+    """The oracle's restatement of knn_full_thread (BLAS sgemm + yael heap)
+    on the host cores, over a bounded sample of the queries."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _util import knn_port, oracle
+    nt = os.cpu_count() or 1
+    done, t0 = 0, time.perf_counter()
+    while done < min(max_q, q.shape[0]):
+        qq = np.ascontiguousarray(q[done:done + batch])
+        knn_port(b, qq, k, nt=nt)
+        done += qq.shape[0]
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, nt, done, oracle().oracle_blas_name().decode()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from yael_gb300 import synth
+    b = synth.sift_like(args.nb, args.d, seed=1)
+    q = synth.sift_like(args.nq, args.d, seed=2)
+    vals = []
+    nt = os.cpu_count() or 1
+    per_step = max(1, args.ref_queries)
+    for s in range(args.warmup + args.steps):
+        qq = q[(s * per_step) % args.nq:][:per_step]
+        t0 = time.perf_counter()
+        qps, nt, done, blas = cpu_port_qps(b, qq, args.k, budget_s=1e9, batch=per_step,
+                                           max_q=per_step)
+        if s >= args.warmup:
+            vals.append(qps)
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "queries/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * per_step / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_of(args),
+            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": nt, "kind": "port",
+                             "sample": f"{per_step} queries per step vs the full {args.nb}-row "
+                                       f"base (knn_full_thread restated, BLAS: {os.path.basename(blas)})"},
+            "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args):
+    return {"workload": f"exact kNN L2, SIFT-like float32 (30% zeros, floor|N(0,40)| clipped "
+                        f"to 255), nb={args.nb}, nq={args.nq}, d={args.d}, k={args.k}",
+            "nb": args.nb, "nq": args.nq, "d": args.d, "k": args.k,
+            "precision": args.prec,
+            "l2": "inputs larger than L2 (base alone is 4*nb*d bytes)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nb", type=int, default=1_000_000)
+    ap.add_argument("--nq", type=int, default=10_000)
+    ap.add_argument("--d", type=int, default=128)
+    ap.add_argument("--k", type=int, default=100)
+    ap.add_argument("--prec", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--fp32-steps", type=int, default=2, help="steps of the plain FP32 path")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--ref-queries", type=int, default=500)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import yael_gb300 as yg
+    from yael_gb300 import synth
+    L = yg.lib()
+    dev = torch.device("cuda", local)
+
+    # the same base on every rank, a different query set per rank (replicas: weak scaling)
+    b_h = synth.sift_like(args.nb, args.d, seed=1)
+    q_h = synth.sift_like(args.nq, args.d, seed=2 + 1000 * rank)
+    b = torch.from_numpy(b_h).to(dev)
+    q = torch.from_numpy(q_h).to(dev)
+    idx = torch.empty((args.nq, args.k), dtype=torch.int32, device=dev)
+    dis = torch.empty((args.nq, args.k), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    prec = {"bf16": yg.PREC_BF16, "fp32": yg.PREC_FP32}[args.prec]
+
+    def step(p, timing=1):
+        o = yg.KnnOpts(p, 2, 1, ctypes.c_void_p(stream.cuda_stream), 0, 0, 0, timing, 0, 0, 0, 0)
+        rc = L.yael_gpu_knn_ex(args.nq, args.nb, args.d, args.k, b.data_ptr(), q.data_ptr(),
+                               idx.data_ptr(), dis.data_ptr(), ctypes.byref(o))
+        if rc != 0:
+            raise RuntimeError(yg.last_error())
+        return o
+
+    def timed(p, steps, warmup):
+        for _ in range(warmup):
+            step(p)
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        l0 = L.yael_gpu_launch_count()
+        scan_ms, scan_n, fb, sample_ms, rr_ms = 0.0, 0, 0, 0.0, 0.0
+        with ClockSampler(local) as clk:
+            ev0.record(stream)
+            for _ in range(steps):
+                o = step(p)
+                scan_ms += o.ms_scan
+                scan_n += o.scan_launches
+                fb += o.n_fallback
+                sample_ms += o.ms_sample
+                rr_ms += o.ms_rerank
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+        ms = ev0.elapsed_time(ev1)
+        launches = L.yael_gpu_launch_count() - l0
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, launches, scan_ms / max(1, scan_n), fb, clk.summary(), sample_ms / steps, rr_ms / steps
+
+    ms, launches, scan_ms, fb, clocks, sample_ms, rr_ms = timed(prec, args.steps, args.warmup)
+    qps = world * args.nq * args.steps / (ms / 1e3)
+
+    # parity spot check of the timed configuration (first 64 queries, FP64 oracle)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _util import knn_exact
+    ridx, _, _ = knn_exact(b_h, q_h[:64], args.k, os.cpu_count() or 1)
+    exact_ids = bool((idx[:64].cpu().numpy() == ridx).all())
+
+    # plain FP32 path (the drop-in default) for the speed-up of the chosen form
+    fp32 = None
+    if args.prec == "bf16" and args.fp32_steps > 0:
+        ms32, _, scan32, _, _, _, _ = timed(yg.PREC_FP32, args.fp32_steps, 1)
+        fp32 = {"value": world * args.nq * args.fp32_steps / (ms32 / 1e3), "unit": "queries/s",
+                "main_pass_ms": scan32}
+        step(yg.PREC_FP32, 0)
+        i32 = idx.cpu().numpy().copy()
+        step(prec, 0)
+        fp32["ids_equal_bf16"] = bool((idx.cpu().numpy() == i32).all())
+
+    # end to end through the drop-in C ABI with pinned host buffers
+    os.environ["YAEL_GPU_PRECISION"] = args.prec
+    bp = torch.from_numpy(b_h).pin_memory()
+    qp = torch.from_numpy(q_h).pin_memory()
+    ip = torch.empty((args.nq, args.k), dtype=torch.int32).pin_memory()
+    dp = torch.empty((args.nq, args.k), dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        L.knn_full_thread(2, args.nq, args.nb, args.d, args.k, bp.data_ptr(), qp.data_ptr(), None,
+                          ip.data_ptr(), dp.data_ptr(), os.cpu_count() or 1)
+
+    e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_qps = world * args.nq * args.e2e_steps / e2e_s
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+        return
+
+    pk_tf, pk_hbm, pk_src = peaks()
+    flops = 2.0 * args.nq * args.nb * args.d
+    achieved = flops / (scan_ms / 1e3) / 1e12 if scan_ms > 0 else None
+    line = {
+        "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if args.prec == "bf16" else "f32", "data": "synthetic",
+        "config": config_of(args),
+        "exact_ids_vs_fp64_oracle_first64": exact_ids,
+        "fallback_queries_per_step": fb / args.steps,
+        "phase_ms": {"threshold_sample_pass": sample_ms, "main_pass": scan_ms, "rerank": rr_ms},
+        "roofline": {"bound": "tensor", "kernel": "tc_scan_kernel (THRESH, main pass)",
+                     "achieved": achieved, "peak": pk_tf, "unit": "TFLOP/s",
+                     "frac": (achieved / pk_tf) if achieved else None,
+                     "peak_source": pk_src, "traffic": None,
+                     "algorithmic": f"2*nq*nb*d = {flops:.4g} flop per launch"},
+        "e2e": {"value": e2e_qps, "unit": "queries/s",
+                "h2d_bytes_per_step": 4 * (args.nb + args.nq) * args.d,
+                "d2h_bytes_per_step": 8 * args.nq * args.k,
+                "api": "knn_full_thread (drop-in C ABI), pinned host buffers"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if fp32:
+        line["plain_fp32"] = fp32
+        line["speedup_vs_plain_fp32"] = qps / fp32["value"]
+    if not args.no_cpu and world >= 1:
+        cqps, nt, nq_done, blas = cpu_port_qps(b_h, q_h, args.k, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = {"value": cqps, "unit": "queries/s", "cores": nt, "kind": "port",
+                                "sample": f"{nq_done} queries vs the full {args.nb}-row base, "
+                                          f"knn_full_thread restated (BLAS {os.path.basename(blas)})"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

@@ -132,6 +132,11 @@ typedef struct {
   int n_fallback;   /* queries whose certificate failed and were recomputed exhaustively */
   int n_candidates; /* total candidates re-ranked */
   int exact_class;  /* 1 if every distance was computed exactly (integer-valued data) */
+  int timing;       /* 1: time the passes with CUDA events on the launching stream */
+  float ms_scan;    /* main fused distance + selection pass (sum over query batches) */
+  float ms_sample;  /* threshold-estimation pass over the base sample */
+  float ms_rerank;  /* re-rank + certificate */
+  int scan_launches; /* launches of the main pass included in ms_scan */
 } yael_gpu_knn_opts;
 
 /* k-NN with explicit options.  Same result contract as knn_full. */
@@ -143,6 +148,9 @@ const char *yael_gpu_last_error(void);
 
 /* YAEL_GPU_ABI_VERSION of the loaded library */
 int yael_gpu_version(void);
+
+/* number of kernels this library has launched in this process */
+long yael_gpu_launch_count(void);
 
 #ifdef __cplusplus
 }

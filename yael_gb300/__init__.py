@@ -40,7 +40,8 @@ PREC_ENV, PREC_FP32, PREC_BF16 = -1, 0, 1
 class KnnOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("metric", c_int), ("device_ptrs", c_int),
                 ("stream", P), ("n_fallback", c_int), ("n_candidates", c_int),
-                ("exact_class", c_int)]
+                ("exact_class", c_int), ("timing", c_int), ("ms_scan", c_float),
+                ("ms_sample", c_float), ("ms_rerank", c_float), ("scan_launches", c_int)]
 
 
 # name -> (restype, argtypes); every symbol of include/yael_gpu.h
@@ -66,6 +67,7 @@ SIGNATURES = {
     "yael_gpu_knn_ex": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, ctypes.POINTER(KnnOpts)]),
     "yael_gpu_last_error": (ctypes.c_char_p, []),
     "yael_gpu_version": (c_int, []),
+    "yael_gpu_launch_count": (c_long, []),
 }
 
 
@@ -122,7 +124,7 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
     idx = np.empty((nq, nnn), dtype=np.int32)
     dis = np.empty((nq, nnn), dtype=np.float32)
     prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
-    opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0)
+    opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0)
     rc = lib().yael_gpu_knn_ex(nq, nb, d, nnn, _ptr(base), _ptr(queries), _ptr(idx), _ptr(dis),
                                ctypes.byref(opts))
     if rc != 0:

@@ -49,7 +49,12 @@ const char *last_message();
     if (_s != ::yg::OK) return _s;     \
   } while (0)
 
-#define YG_LAUNCH_CHECK() YG_CUDA(cudaGetLastError())
+void count_launch();
+#define YG_LAUNCH_CHECK()          \
+  do {                             \
+    ::yg::count_launch();          \
+    YG_CUDA(cudaGetLastError());   \
+  } while (0)
 
 // ---------------------------------------------------------------------------
 // execution context: one device per process (the current device at first

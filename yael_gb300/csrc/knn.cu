@@ -4,6 +4,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <memory>
+
 #include "knn.cuh"
 #include "tc_scan.cuh"
 #include "../../include/yael_gpu.h"
@@ -37,6 +39,32 @@ __global__ void fill_f32(float *p, long n, float v) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
 }
+
+// CUDA events around a pass, on the launching stream; elapsed times are read
+// after the stream synchronizes at the end of the batch (no extra host sync)
+struct PassTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  float *dst;
+  PassTimer(bool enable, cudaStream_t st, float *out) : dst(enable ? out : nullptr) {
+    if (dst) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, st);
+    }
+  }
+  void stop(cudaStream_t st) {
+    if (dst) cudaEventRecord(b, st);
+  }
+  void collect() {  // call after the stream has been synchronized
+    if (!dst) return;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) *dst += ms;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    dst = nullptr;
+  }
+  ~PassTimer() { collect(); }
+};
 
 // distance pass on whichever producer the precision selects
 int scan(const KnnJob &job, const float *q, int nq, const float *b, long ldb, int nb,
@@ -92,6 +120,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
   const int ctas_per_sm = 1;
   const int c_needed = bstats_exact ? k : 2 * k;
 
+  std::unique_ptr<PassTimer> tm_scan, tm_sample;
   ScanSel sel;
   if (c_needed <= 32) {
     // ---- TOPC over the full base
@@ -104,7 +133,10 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     YG_CHECK(ws_get(ws, WS_TOPV, (size_t)sel.nchunk * nq * sel.C, &sel.topv));
     YG_CHECK(ws_get(ws, WS_TOPI, (size_t)sel.nchunk * nq * sel.C, &sel.topi));
+    tm_scan.reset(new PassTimer(job.timing, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
+    tm_scan->stop(st);
+    job.scan_launches++;
   } else {
     // ---- THRESH: thresholds from a strided sample of the base
     sel.mode = SCAN_THRESH;
@@ -133,14 +165,16 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
       ss.nchunk = (int)ceil_div(nts, ss.tiles_per_chunk);
       YG_CHECK(ws_get(ws, WS_STOPV, (size_t)ss.nchunk * nq * c, &ss.topv));
       YG_CHECK(ws_get(ws, WS_STOPI, (size_t)ss.nchunk * nq * c, &ss.topi));
+      tm_sample.reset(new PassTimer(job.timing, st, &job.ms_sample));
       if (bf16) {
         TcOperands tcs = tcq;
-        YG_CHECK(tc_base_view(*tcb, stride, ns, &tcs));
+        YG_CHECK(tc_base_view(tcq, stride, ns, &tcs));
         YG_CHECK(tc_scan(tcs, nq, ns, ss, st));
       } else {
         YG_CHECK(simt_scan(job.q, job.ldq, nq, job.b, job.ldb * stride, ns, d, bn32, stride,
                            job.metric, ss, st));
       }
+      tm_sample->stop(st);
       YG_CHECK(thresh_from_sample(nq, ss.nchunk, c, c, ss.topv, eps, thr, st));
     }
     sel.thr = thr;
@@ -151,15 +185,23 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
     sel.nchunk = imin(choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 4096);
     sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    tm_scan.reset(new PassTimer(job.timing, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
+    tm_scan->stop(st);
+    job.scan_launches++;
   }
   ra.sel = sel;
+  PassTimer tr(job.timing, st, &job.ms_rerank);
   YG_CHECK(rerank(ra, st));
+  tr.stop(st);
 
   // ---- exhaustive path for the queries the certificate rejected
   Small hs;
   YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
   YG_CUDA(cudaStreamSynchronize(st));
+  if (tm_scan) tm_scan->collect();
+  if (tm_sample) tm_sample->collect();
+  tr.collect();
   job.n_fallback += hs.fail_cnt;
   job.n_cand = (long long)hs.n_cand;
   if (hs.fail_cnt > 0) {
@@ -182,6 +224,8 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   job.n_fallback = 0;
   job.n_cand = 0;
   job.exact_class = 0;
+  job.ms_scan = job.ms_sample = job.ms_rerank = 0;
+  job.scan_launches = 0;
   if (nq < 0 || nb < 1 || d < 1 || k < 1) {
     set_error(E_ARG, "knn: invalid sizes nq=%d nb=%d d=%d k=%d", nq, nb, d, k);
     return E_ARG;
@@ -252,9 +296,15 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     sub.out_idx = job.out_idx + (long)q0 * k;
     sub.out_dis = job.out_dis + (long)q0 * k;
     sub.n_fallback = 0;
+    sub.ms_scan = sub.ms_sample = sub.ms_rerank = 0;
+    sub.scan_launches = 0;
     YG_CHECK(knn_batch(sub, ctx, st, dsmall, &tcb, bexact));
     job.n_fallback += sub.n_fallback;
     job.n_cand += sub.n_cand;
+    job.ms_scan += sub.ms_scan;
+    job.ms_sample += sub.ms_sample;
+    job.ms_rerank += sub.ms_rerank;
+    job.scan_launches += sub.scan_launches;
   }
   if (job.prec == PREC_BF16) YG_CHECK(tc_take_error(st));
   return OK;
@@ -270,6 +320,7 @@ static int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
   KnnJob job;
   job.nq = nq; job.nb = nb; job.d = d; job.k = k; job.metric = metric; job.prec = prec;
   job.ldq = d; job.ldb = d;
+  job.timing = opts ? opts->timing : 0;
   if (opts && opts->device_ptrs) {
     if (opts->stream) st = (cudaStream_t)opts->stream;
     job.q = q; job.b = b; job.w = w; job.out_idx = assign; job.out_dis = dis;
@@ -300,6 +351,10 @@ static int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
     opts->n_fallback = job.n_fallback;
     opts->n_candidates = (int)(job.n_cand > 0x7fffffff ? 0x7fffffff : job.n_cand);
     opts->exact_class = job.exact_class;
+    opts->ms_scan = job.ms_scan;
+    opts->ms_sample = job.ms_sample;
+    opts->ms_rerank = job.ms_rerank;
+    opts->scan_launches = job.scan_launches;
   }
   return OK;
 }

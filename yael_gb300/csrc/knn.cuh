@@ -16,6 +16,10 @@ struct KnnJob {
   const float *w = nullptr;  // device base weights or null
   int *out_idx = nullptr;    // device nq x k
   float *out_dis = nullptr;  // device nq x k
+  // CUDA-event timing of the passes (optional)
+  int timing = 0;
+  float ms_scan = 0, ms_sample = 0, ms_rerank = 0;
+  int scan_launches = 0;
   // filled on return
   int n_fallback = 0;
   long long n_cand = 0;

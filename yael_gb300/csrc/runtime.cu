@@ -3,12 +3,17 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
 #include "../../include/yael_gpu.h"
 
 namespace yg {
+
+static std::atomic<long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(); }
 
 static thread_local int t_code = OK;
 static thread_local char t_msg[1024] = "";
@@ -115,3 +120,5 @@ int default_precision() {
 extern "C" const char *yael_gpu_last_error(void) { return yg::last_message(); }
 
 extern "C" int yael_gpu_version(void) { return YAEL_GPU_ABI_VERSION; }
+
+extern "C" long yael_gpu_launch_count(void) { return yg::launch_count(); }

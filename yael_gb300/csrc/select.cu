@@ -329,7 +329,8 @@ __global__ void fb_rows_kernel(const int *qlist, int q0, int nb, int d, int metr
   if (j >= nb) return;
   double e = dist64_seq(qs, B + j * ldb, d, metric);
   if (w) e *= (double)w[j];
-  rows[(long)r * nb + j] = d2ord(e);
+  // NaN (whatever its sign bit) gets the largest key and is never selected
+  rows[(long)r * nb + j] = isnan(e) ? ~0ull : d2ord(e);
 }
 
 __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0, int nb, int k,
@@ -346,14 +347,13 @@ __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0,
   const int qi = qlist ? qlist[q0 + r] : q0 + r;
   const unsigned long long *row = rows + (long)r * nb;
   const int tid = threadIdx.x;
-  const unsigned long long nan_lo = d2ord(INFINITY);  // keys above +inf are NaN
 
   // number of non-NaN entries
   if (tid == 0) svalid = 0;
   __syncthreads();
   {
     int c = 0;
-    for (int j = tid; j < nb; j += RT) c += row[j] <= nan_lo;
+    for (int j = tid; j < nb; j += RT) c += row[j] != ~0ull;
     atomicAdd(&svalid, c);
   }
   __syncthreads();

@@ -349,6 +349,11 @@ int make_map(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t rows,
              uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows,
              CUtensorMapSwizzle sw) {
   YG_CHECK(get_encode());
+  if (!ptr || (reinterpret_cast<uintptr_t>(ptr) & 15) || (row_bytes & 15) || rows == 0) {
+    set_error(E_ARG, "tensor map: null / misaligned operand (ptr=%p pitch=%llu rows=%llu)", ptr,
+              (unsigned long long)row_bytes, (unsigned long long)rows);
+    return E_ARG;
+  }
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {row_bytes};
   cuuint32_t box[2] = {box_cols, box_rows};
