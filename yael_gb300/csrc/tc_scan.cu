@@ -53,6 +53,22 @@ __host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C) {
   return L;
 }
 
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// minimum of 32 values (three-input min, 16 instructions, depth 3)
+__device__ __forceinline__ float min32(const float (&v)[32]) {
+  float a[10];
+#pragma unroll
+  for (int g = 0; g < 10; g++) a[g] = fmin3(v[3 * g], v[3 * g + 1], v[3 * g + 2]);
+  const float b0 = fmin3(a[0], a[1], a[2]), b1 = fmin3(a[3], a[4], a[5]);
+  const float b2 = fmin3(a[6], a[7], a[8]), b3 = fmin3(a[9], v[30], v[31]);
+  return fmin3(b0, b1, fminf(b2, b3));
+}
+
 // sorted insertion of (x, j) into an ascending register list; the caller has
 // checked x < L[C-1].  Equal values keep their earlier (smaller) ids first.
 template <int C>
@@ -202,6 +218,58 @@ __global__ void __launch_bounds__(NT_TC, 1)
     if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
     const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
 
+    // one 32-column chunk already in registers: mask, cheap bound test, then
+    // (rarely) the per-element update; every index is static (no local memory)
+    auto process = [&](const uint32_t (&r)[32], int jc) {
+      float v[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+      if (jc + 32 > nb) {
+#pragma unroll
+        for (int i = 0; i < 32; i++)
+          if (jc + i >= nb) v[i] = NAN;
+      }
+      if (!rvalid) return;
+      const float m = min32(v);
+      if (MODE == SCAN_TOPC) {
+        if (!(m >= lmax)) {  // true when m < lmax or m is NaN
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            const float x = v[i];
+            if (x < lmax) {
+              if (C <= 8) {
+                reg_insert<CR>(RL, RI, x, jc + i);
+                lmax = RL[CR - 1];
+              } else {
+                int p = C - 1;
+                while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
+                  Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
+                  Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
+                  p--;
+                }
+                Lv[p * N_EPI + tslot] = x;
+                Li[p * N_EPI + tslot] = jc + i;
+                lmax = Lv[(C - 1) * N_EPI + tslot];
+              }
+            }
+          }
+        }
+      } else {
+        if (!(m > thr)) {  // true when m <= thr or m is NaN
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            if (v[i] <= thr) {
+              const int pos = atomicAdd(sel.cnt + qrow, 1);
+              if (pos < sel.cap) {
+                sel.candv[qrow * sel.cap + pos] = v[i];
+                sel.candi[qrow * sel.cap + pos] = jc + i;
+              }
+            }
+          }
+        }
+      }
+    };
+
     int it = 0;
     bool ok = true;
     for (int t = t_begin; t < t_end; t++, it++) {
@@ -212,71 +280,25 @@ __global__ void __launch_bounds__(NT_TC, 1)
       if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
       tc_fence_after();
       const uint32_t tcol = tmem + lane_base + (uint32_t)(a * TC_TILE_N + half * 128);
-      uint32_t r[32];
-      tmem_ld32(tcol, r);
-      tmem_ld_wait(r);
-      for (int c = 0; c < 4; c++) {
-        float v[32];
-#pragma unroll
-        for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-        if (c + 1 < 4) {
-          tmem_ld32(tcol + (uint32_t)((c + 1) * 32), r);
-        } else {
-          // last load of this accumulator done: hand it back to the MMA warp
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[a]);
-        }
-        const int jc = t * TC_TILE_N + half * 128 + c * 32;
-        if (jc + 32 > nb) {
-#pragma unroll
-          for (int i = 0; i < 32; i++)
-            if (jc + i >= nb) v[i] = NAN;
-        }
-        if (rvalid) {
-          float m = v[0];
-#pragma unroll
-          for (int i = 1; i < 32; i++) m = fminf(m, v[i]);
-          if (MODE == SCAN_TOPC) {
-            if (m < lmax) {
-#pragma unroll 1
-              for (int i = 0; i < 32; i++) {
-                const float x = v[i];
-                if (x < lmax) {
-                  if (C <= 8) {
-                    reg_insert<CR>(RL, RI, x, jc + i);
-                    lmax = RL[CR - 1];
-                  } else {
-                    int p = C - 1;
-                    while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
-                      Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
-                      Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
-                      p--;
-                    }
-                    Lv[p * N_EPI + tslot] = x;
-                    Li[p * N_EPI + tslot] = jc + i;
-                    lmax = Lv[(C - 1) * N_EPI + tslot];
-                  }
-                }
-              }
-            }
-          } else {
-            if (m <= thr) {
-#pragma unroll 1
-              for (int i = 0; i < 32; i++) {
-                if (v[i] <= thr) {
-                  const int pos = atomicAdd(sel.cnt + qrow, 1);
-                  if (pos < sel.cap) {
-                    sel.candv[qrow * sel.cap + pos] = v[i];
-                    sel.candi[qrow * sel.cap + pos] = jc + i;
-                  }
-                }
-              }
-            }
-          }
-        }
-        if (c + 1 < 4) tmem_ld_wait(r);
-      }
+      const int j0 = t * TC_TILE_N + half * 128;
+      // two register sets: the load of chunk c+1 is in flight while chunk c is scanned
+      uint32_t ra[32], rb[32];
+      tmem_ld32(tcol, ra);
+      tmem_ld_wait(ra);
+      tmem_ld32(tcol + 32, rb);
+      process(ra, j0);
+      tmem_ld_wait(rb);
+      tmem_ld32(tcol + 64, ra);
+      process(rb, j0 + 32);
+      tmem_ld_wait(ra);
+      tmem_ld32(tcol + 96, rb);
+      process(ra, j0 + 64);
+      tmem_ld_wait(rb);
+      // every load of this accumulator is complete: hand it back to the MMA warp
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[a]);
+      process(rb, j0 + 96);
     }
     (void)ok;
     if (MODE == SCAN_TOPC) {
