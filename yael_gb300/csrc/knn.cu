@@ -122,13 +122,12 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
 
   std::unique_ptr<PassTimer> tm_scan, tm_sample;
   ScanSel sel;
-  if (c_needed <= 32) {
-    // ---- TOPC over the full base
+  if (c_needed <= 16) {
+    // ---- TOPC over the full base (register lists)
     sel.mode = SCAN_TOPC;
     sel.C = pow2_at_least(c_needed);
     int nchunk = choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4);
     nchunk = imin(nchunk, kMaxCandidates / sel.C);
-    sel.nchunk = nchunk;
     sel.tiles_per_chunk = (int)ceil_div(ntb, nchunk);
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     YG_CHECK(ws_get(ws, WS_TOPV, (size_t)sel.nchunk * nq * sel.C, &sel.topv));
@@ -138,23 +137,29 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
     tm_scan->stop(st);
     job.scan_launches++;
   } else {
-    // ---- THRESH: thresholds from a strided sample of the base
+    // ---- THRESH: per-query thresholds from a strided sample of the base.
+    // The c-th smallest of a 1/stride sample lies below ~c*stride base values;
+    // with stride = k/3 the chance that fewer than k fall below it is the
+    // chance that a Poisson(3) exceeds c-1 (c = 16: ~3e-7 per query).
     sel.mode = SCAN_THRESH;
     float *thr;
-    int *cnt;
     YG_CHECK(ws_get(ws, WS_THR, nq, &thr));
-    YG_CHECK(ws_get(ws, WS_CNT, nq, &cnt));
-    const int c = 32;
-    int stride = (int)floor((double)k * 0.95 / ((double)c - 5.0 * sqrt((double)c)));
+    const int c = 16;
+    int stride = k / 3;
     if (stride < 1) stride = 1;
     const int ns = nb / stride;
-    if (nb <= kMaxCandidates || ns < 2 * c) {
-      sel.cap = pow2_at_least(nb);
-      if (sel.cap > kMaxCandidates) sel.cap = kMaxCandidates;
+    sel.nchunk = imin(choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 1024);
+    sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
+    sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    const int nreg = sel.nregion();
+    if (nb <= kMaxCandidates || ns < 4 * c) {
+      // every base row is a candidate; each region holds at most half of its chunk
+      sel.cap = pow2_at_least(imax(1, sel.tiles_per_chunk * tile_n / 2));
       fill_f32<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(thr, nq, INFINITY);
       YG_LAUNCH_CHECK();
     } else {
-      sel.cap = imin(kMaxCandidates, pow2_at_least(3 * c * stride));
+      const double er = (double)c * stride / nreg;  // expected hits per region
+      sel.cap = pow2_at_least((int)(2.0 * er + 6.0 * sqrt(er) + 16.0));
       ScanSel ss;
       ss.mode = SCAN_TOPC;
       ss.C = c;
@@ -178,13 +183,9 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
       YG_CHECK(thresh_from_sample(nq, ss.nchunk, c, c, ss.topv, eps, thr, st));
     }
     sel.thr = thr;
-    sel.cnt = cnt;
-    YG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * nq, st));
-    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nq * sel.cap, &sel.candv));
-    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nq * sel.cap, &sel.candi));
-    sel.nchunk = imin(choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 4096);
-    sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
-    sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    YG_CHECK(ws_get(ws, WS_CNT, (size_t)nreg * nq, &sel.cnt));
+    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nreg * nq * sel.cap, &sel.candv));
+    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nreg * nq * sel.cap, &sel.candi));
     tm_scan.reset(new PassTimer(job.timing, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
     tm_scan->stop(st);

@@ -9,9 +9,11 @@
 //   TOPC   -- every (query, base chunk) keeps its C smallest (v, j) in
 //             lexicographic order (strict '<' over increasing j), written to
 //             topv/topi[(chunk * nq + q) * C + s], ascending.
-//   THRESH -- every (q, j) with v <= thr[q] is appended to the query's
-//             candidate list (cnt[q] counts all hits, including those that
-//             did not fit in cap).
+//   THRESH -- every (q, j) with v <= thr[q] is appended to a candidate
+//             region owned by one thread: region r = chunk * 2 + column half,
+//             slots candv/candi[(r * nq + q) * cap + s], count cnt[r * nq + q]
+//             (all hits, including those that did not fit in cap).  No atomics:
+//             each (region, query) has exactly one writer.
 #pragma once
 #include "common.cuh"
 
@@ -31,7 +33,8 @@ struct ScanSel {
   int *cnt = nullptr;
   float *candv = nullptr;
   int *candi = nullptr;
-  int cap = 0;
+  int cap = 0;              // THRESH: slots per (region, query)
+  __host__ __device__ int nregion() const { return nchunk * 2; }
 };
 
 // FP32 CUDA-core producer.  q: nq rows (stride ldq floats); b: nb rows (stride

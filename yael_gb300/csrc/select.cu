@@ -121,17 +121,28 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
       }
     }
   } else {
-    const int cnt = s.cnt[q];
-    if (cnt > s.cap) {
-      if (tid == 0) sfail = 1;
-    } else {
-      for (int idx = tid; idx < cnt; idx += RT) {
-        const float v = s.candv[(long)q * s.cap + idx];
-        const float av = L2 ? (float)((double)v + qn) : v;
-        K[idx] = f2ord(av);
-        I[idx] = s.candi[(long)q * s.cap + idx];
+    // regions (chunk, half) of this query; any overflowing region fails the query
+    const int nreg = s.nregion();
+    for (int r = 0; r < nreg; r++) {
+      const int cnt = s.cnt[(long)r * a.nq + q];
+      if (cnt > s.cap) {
+        if (tid == 0) sfail = 1;
+        break;
       }
-      if (tid == 0) sM = cnt;
+      __shared__ int sbase;
+      if (tid == 0) { sbase = sM; sM += cnt; }
+      __syncthreads();
+      const int base = sbase;
+      if (base + cnt <= Mp_alloc) {
+        const long o = ((long)r * a.nq + q) * s.cap;
+        for (int idx = tid; idx < cnt; idx += RT) {
+          const float v = s.candv[o + idx];
+          const float av = L2 ? (float)((double)v + qn) : v;
+          K[base + idx] = f2ord(av);
+          I[base + idx] = s.candi[o + idx];
+        }
+      }
+      __syncthreads();
     }
   }
   __syncthreads();
@@ -450,13 +461,10 @@ __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0,
 
 int rerank(const RerankArgs &a, cudaStream_t st) {
   if (a.nq <= 0) return OK;
-  int Mmax = a.sel.mode == SCAN_TOPC ? a.sel.nchunk * a.sel.C : a.sel.cap;
+  int Mmax = a.sel.mode == SCAN_TOPC ? a.sel.nchunk * a.sel.C : a.sel.nregion() * a.sel.cap;
+  if (Mmax > kMaxCandidates) Mmax = kMaxCandidates;  // more candidates than this fail the query
   int Mp = 1;
   while (Mp < Mmax) Mp <<= 1;
-  if (Mp > kMaxCandidates) {
-    set_error(E_ARG, "rerank: %d candidates per query exceed %d", Mmax, kMaxCandidates);
-    return E_ARG;
-  }
   // K (8 B) + I (4 B) + E (4 B) per slot, then the query row
   const size_t smem = (size_t)Mp * 16 + (size_t)a.d * 4 + 16;
   static size_t attr = 48 * 1024;

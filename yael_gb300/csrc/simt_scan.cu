@@ -34,6 +34,8 @@ __global__ void __launch_bounds__(NT, 1)
   const int sr = tid & (BM - 1), sh = tid >> 7;
   const long qrow = q0 + sr;
   float lmax = INFINITY, thr = NAN;
+  int rcount = 0;  // THRESH: hits of this thread's region
+  const long rbase = ((long)(blockIdx.y * 2 + sh) * nq + qrow);
   if (MODE == SCAN_TOPC) {
 #pragma unroll
     for (int s = 0; s < C; s++) {
@@ -86,11 +88,11 @@ __global__ void __launch_bounds__(NT, 1)
           }
         } else {
           if (v <= thr) {
-            const int pos = atomicAdd(sel.cnt + qrow, 1);
-            if (pos < sel.cap) {
-              sel.candv[qrow * sel.cap + pos] = v;
-              sel.candi[qrow * sel.cap + pos] = jbase + c;
+            if (rcount < sel.cap) {
+              sel.candv[rbase * sel.cap + rcount] = v;
+              sel.candi[rbase * sel.cap + rcount] = jbase + c;
             }
+            rcount++;
           }
         }
       }
@@ -98,6 +100,7 @@ __global__ void __launch_bounds__(NT, 1)
     __syncthreads();  // staging tile is rewritten by the next tile
   }
 
+  if (MODE == SCAN_THRESH && qrow < nq) sel.cnt[rbase] = rcount;
   if (MODE == SCAN_TOPC) {
     if (sh == 0 && qrow < nq) {
       // merge the two half-row lists, lexicographic (v, id)

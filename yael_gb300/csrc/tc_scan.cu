@@ -46,7 +46,7 @@ __host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C) {
   L.qn_off = off;  off += QN_BYTES;
   L.stg_off = off; off += (size_t)S * STAGE_BYTES;
   L.list_off = off;
-  if (mode == SCAN_TOPC) off += (size_t)(C >= 16 ? N_EPI : 128) * C * 8;
+  if (mode == SCAN_TOPC) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
   off = (off + 15) & ~(size_t)15;
   L.bar_off = off; off += (size_t)(2 * S + 5) * 8 + 16;
   L.total = off + 1024;  // alignment slack for the 1024-byte aligned base
@@ -206,16 +206,18 @@ __global__ void __launch_bounds__(NT_TC, 1)
     const bool rvalid = qrow < nq;
     const int tslot = ew * 32 + lane;      // 0..255
     float lmax = INFINITY, thr = NAN;
-    constexpr int CR = (C <= 8) ? C : 1;
+    constexpr int CR = (C <= 16) ? C : 1;  // register lists up to 16 entries
     float RL[CR];
     int RI[CR];
 #pragma unroll
     for (int s = 0; s < CR; s++) { RL[s] = INFINITY; RI[s] = 0x7fffffff; }
-    int *Li = reinterpret_cast<int *>(Lv + (MODE == SCAN_TOPC && C >= 16 ? N_EPI * C : 0));
-    if (MODE == SCAN_TOPC && C >= 16) {
+    int *Li = reinterpret_cast<int *>(Lv + (MODE == SCAN_TOPC && C > 16 ? N_EPI * C : 0));
+    if (MODE == SCAN_TOPC && C > 16) {
       for (int s = 0; s < C; s++) { Lv[s * N_EPI + tslot] = INFINITY; Li[s * N_EPI + tslot] = 0x7fffffff; }
     }
     if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
+    int rcount = 0;  // THRESH: hits of this thread's region (chunk, half, query)
+    const long rbase = (long)(blockIdx.y * 2 + half) * nq + qrow;
     const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
 
     // one 32-column chunk already in registers: mask, cheap bound test, then
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           for (int i = 0; i < 32; i++) {
             const float x = v[i];
             if (x < lmax) {
-              if (C <= 8) {
+              if (C <= 16) {
                 reg_insert<CR>(RL, RI, x, jc + i);
                 lmax = RL[CR - 1];
               } else {
@@ -259,11 +261,11 @@ __global__ void __launch_bounds__(NT_TC, 1)
 #pragma unroll
           for (int i = 0; i < 32; i++) {
             if (v[i] <= thr) {
-              const int pos = atomicAdd(sel.cnt + qrow, 1);
-              if (pos < sel.cap) {
-                sel.candv[qrow * sel.cap + pos] = v[i];
-                sel.candi[qrow * sel.cap + pos] = jc + i;
+              if (rcount < sel.cap) {
+                sel.candv[rbase * sel.cap + rcount] = v[i];
+                sel.candi[rbase * sel.cap + rcount] = jc + i;
               }
+              rcount++;
             }
           }
         }
@@ -301,10 +303,11 @@ __global__ void __launch_bounds__(NT_TC, 1)
       process(rb, j0 + 96);
     }
     (void)ok;
+    if (MODE == SCAN_THRESH && rvalid) sel.cnt[rbase] = rcount;
     if (MODE == SCAN_TOPC) {
       // merge the two column halves of each row
       int *Xi = reinterpret_cast<int *>(Lv + 128 * C);
-      if (C <= 8 && half == 1) {
+      if (C <= 16 && half == 1) {
 #pragma unroll
         for (int s = 0; s < CR; s++) { Lv[row * C + s] = RL[s]; Xi[row * C + s] = RI[s]; }
       }
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
         for (int s = 0; s < C; s++) {
           float va, vb;
           int xa, xb;
-          if (C <= 8) {
+          if (C <= 16) {
             va = INFINITY; xa = 0x7fffffff;
 #pragma unroll
             for (int z = 0; z < CR; z++) if (z == ia) { va = RL[z]; xa = RI[z]; }
