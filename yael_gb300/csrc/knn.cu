@@ -161,7 +161,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
       const double er = (double)c * stride / nreg;  // expected hits per region
       sel.cap = pow2_at_least((int)(2.0 * er + 6.0 * sqrt(er) + 16.0));
       ScanSel ss;
-      ss.mode = SCAN_TOPC;
+      ss.mode = SCAN_TOPV;  // only the c-th value is needed
       ss.C = c;
       const int nts = (int)ceil_div(ns, tile_n);
       int nch = choose_chunks(nqt, nts, ctx->num_sms, ctas_per_sm, 2);

@@ -19,7 +19,9 @@
 
 namespace yg {
 
-enum ScanMode : int { SCAN_TOPC = 0, SCAN_THRESH = 1 };
+// SCAN_TOPV is SCAN_TOPC without ids (only the values are kept and written;
+// used where a rank statistic of the distances is all that is needed).
+enum ScanMode : int { SCAN_TOPC = 0, SCAN_THRESH = 1, SCAN_TOPV = 2 };
 enum Metric : int { METRIC_L2 = 2, METRIC_DOT = 16 };
 
 struct ScanSel {

@@ -151,6 +151,7 @@ int simt_scan(const float *q, long ldq, int nq, const float *b, long ldb, int nb
               int d, const float *bn, long bn_stride, int metric, const ScanSel &sel,
               cudaStream_t st) {
   if (nq <= 0 || nb <= 0) return OK;
+  // (SCAN_TOPV runs as SCAN_TOPC here: the ids are simply also written)
   if (sel.mode == SCAN_THRESH)
     return launch<SCAN_THRESH, 1>(q, ldq, nq, b, ldb, nb, d, bn, bn_stride, metric, sel, st);
   switch (sel.C) {

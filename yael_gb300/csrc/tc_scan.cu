@@ -46,7 +46,7 @@ __host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C) {
   L.qn_off = off;  off += QN_BYTES;
   L.stg_off = off; off += (size_t)S * STAGE_BYTES;
   L.list_off = off;
-  if (mode == SCAN_TOPC) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
+  if (mode != SCAN_THRESH) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
   off = (off + 15) & ~(size_t)15;
   L.bar_off = off; off += (size_t)(2 * S + 5) * 8 + 16;
   L.total = off + 1024;  // alignment slack for the 1024-byte aligned base
@@ -57,16 +57,6 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
   float r;
   asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
   return r;
-}
-
-// minimum of 32 values (three-input min, 16 instructions, depth 3)
-__device__ __forceinline__ float min32(const float (&v)[32]) {
-  float a[10];
-#pragma unroll
-  for (int g = 0; g < 10; g++) a[g] = fmin3(v[3 * g], v[3 * g + 1], v[3 * g + 2]);
-  const float b0 = fmin3(a[0], a[1], a[2]), b1 = fmin3(a[3], a[4], a[5]);
-  const float b2 = fmin3(a[6], a[7], a[8]), b3 = fmin3(a[9], v[30], v[31]);
-  return fmin3(b0, b1, fminf(b2, b3));
 }
 
 // sorted insertion of (x, j) into an ascending register list; the caller has
@@ -211,8 +201,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
     int RI[CR];
 #pragma unroll
     for (int s = 0; s < CR; s++) { RL[s] = INFINITY; RI[s] = 0x7fffffff; }
-    int *Li = reinterpret_cast<int *>(Lv + (MODE == SCAN_TOPC && C > 16 ? N_EPI * C : 0));
-    if (MODE == SCAN_TOPC && C > 16) {
+    int *Li = reinterpret_cast<int *>(Lv + (MODE != SCAN_THRESH && C > 16 ? N_EPI * C : 0));
+    if (MODE != SCAN_THRESH && C > 16) {
       for (int s = 0; s < C; s++) { Lv[s * N_EPI + tslot] = INFINITY; Li[s * N_EPI + tslot] = 0x7fffffff; }
     }
     if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
@@ -232,40 +222,63 @@ __global__ void __launch_bounds__(NT_TC, 1)
           if (jc + i >= nb) v[i] = NAN;
       }
       if (!rvalid) return;
-      const float m = min32(v);
-      if (MODE == SCAN_TOPC) {
-        if (!(m >= lmax)) {  // true when m < lmax or m is NaN
+      // four 8-column groups: a group is scanned element by element only when
+      // its minimum passes the bound (true when min < bound or min is NaN)
 #pragma unroll
-          for (int i = 0; i < 32; i++) {
-            const float x = v[i];
-            if (x < lmax) {
-              if (C <= 16) {
-                reg_insert<CR>(RL, RI, x, jc + i);
-                lmax = RL[CR - 1];
-              } else {
-                int p = C - 1;
-                while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
-                  Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
-                  Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
-                  p--;
+      for (int g = 0; g < 4; g++) {
+        const float mg = fmin3(fmin3(v[8 * g], v[8 * g + 1], v[8 * g + 2]),
+                               fmin3(v[8 * g + 3], v[8 * g + 4], v[8 * g + 5]),
+                               fminf(v[8 * g + 6], v[8 * g + 7]));
+        if (MODE == SCAN_TOPV) {
+          if (!(mg >= lmax)) {
+#pragma unroll
+            for (int i = 8 * g; i < 8 * g + 8; i++) {
+              float x = v[i];
+              if (x < lmax) {  // min/max bubble, values only
+#pragma unroll
+                for (int z = 0; z < CR; z++) {
+                  const float lo = fminf(RL[z], x);
+                  x = fmaxf(RL[z], x);
+                  RL[z] = lo;
                 }
-                Lv[p * N_EPI + tslot] = x;
-                Li[p * N_EPI + tslot] = jc + i;
-                lmax = Lv[(C - 1) * N_EPI + tslot];
+                lmax = RL[CR - 1];
               }
             }
           }
-        }
-      } else {
-        if (!(m > thr)) {  // true when m <= thr or m is NaN
+        } else if (MODE == SCAN_TOPC) {
+          if (!(mg >= lmax)) {
 #pragma unroll
-          for (int i = 0; i < 32; i++) {
-            if (v[i] <= thr) {
-              if (rcount < sel.cap) {
-                sel.candv[rbase * sel.cap + rcount] = v[i];
-                sel.candi[rbase * sel.cap + rcount] = jc + i;
+            for (int i = 8 * g; i < 8 * g + 8; i++) {
+              const float x = v[i];
+              if (x < lmax) {
+                if (C <= 16) {
+                  reg_insert<CR>(RL, RI, x, jc + i);
+                  lmax = RL[CR - 1];
+                } else {
+                  int p = C - 1;
+                  while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
+                    Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
+                    Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
+                    p--;
+                  }
+                  Lv[p * N_EPI + tslot] = x;
+                  Li[p * N_EPI + tslot] = jc + i;
+                  lmax = Lv[(C - 1) * N_EPI + tslot];
+                }
               }
-              rcount++;
+            }
+          }
+        } else {
+          if (!(mg > thr)) {
+#pragma unroll
+            for (int i = 8 * g; i < 8 * g + 8; i++) {
+              if (v[i] <= thr) {
+                if (rcount < sel.cap) {
+                  sel.candv[rbase * sel.cap + rcount] = v[i];
+                  sel.candi[rbase * sel.cap + rcount] = jc + i;
+                }
+                rcount++;
+              }
             }
           }
         }
@@ -283,28 +296,31 @@ __global__ void __launch_bounds__(NT_TC, 1)
       tc_fence_after();
       const uint32_t tcol = tmem + lane_base + (uint32_t)(a * TC_TILE_N + half * 128);
       const int j0 = t * TC_TILE_N + half * 128;
-      // two register sets: the load of chunk c+1 is in flight while chunk c is scanned
+      // two register sets: the load of chunk c+1 is in flight while chunk c is
+      // scanned; the loop keeps one copy of the chunk code per register set
       uint32_t ra[32], rb[32];
       tmem_ld32(tcol, ra);
       tmem_ld_wait(ra);
-      tmem_ld32(tcol + 32, rb);
-      process(ra, j0);
-      tmem_ld_wait(rb);
-      tmem_ld32(tcol + 64, ra);
-      process(rb, j0 + 32);
-      tmem_ld_wait(ra);
-      tmem_ld32(tcol + 96, rb);
-      process(ra, j0 + 64);
-      tmem_ld_wait(rb);
-      // every load of this accumulator is complete: hand it back to the MMA warp
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty[a]);
-      process(rb, j0 + 96);
+#pragma unroll 1
+      for (int cc = 0; cc < 2; cc++) {
+        tmem_ld32(tcol + (uint32_t)(64 * cc + 32), rb);
+        process(ra, j0 + 64 * cc);
+        tmem_ld_wait(rb);
+        if (cc == 0) {
+          tmem_ld32(tcol + 64, ra);
+        } else {
+          // every load of this accumulator is complete: hand it back to the MMA warp
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[a]);
+        }
+        process(rb, j0 + 64 * cc + 32);
+        if (cc == 0) tmem_ld_wait(ra);
+      }
     }
     (void)ok;
     if (MODE == SCAN_THRESH && rvalid) sel.cnt[rbase] = rcount;
-    if (MODE == SCAN_TOPC) {
+    if (MODE != SCAN_THRESH) {
       // merge the two column halves of each row
       int *Xi = reinterpret_cast<int *>(Lv + 128 * C);
       if (C <= 16 && half == 1) {
@@ -440,7 +456,9 @@ int dispatch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStrea
     case 2: return launch<SCAN_TOPC, 2, L2>(op, nq, nb, sel, st);
     case 4: return launch<SCAN_TOPC, 4, L2>(op, nq, nb, sel, st);
     case 8: return launch<SCAN_TOPC, 8, L2>(op, nq, nb, sel, st);
-    case 16: return launch<SCAN_TOPC, 16, L2>(op, nq, nb, sel, st);
+    case 16:
+      if (sel.mode == SCAN_TOPV) return launch<SCAN_TOPV, 16, L2>(op, nq, nb, sel, st);
+      return launch<SCAN_TOPC, 16, L2>(op, nq, nb, sel, st);
     case 32: return launch<SCAN_TOPC, 32, L2>(op, nq, nb, sel, st);
   }
   set_error(E_ARG, "tc_scan: unsupported list length C=%d", sel.C);
