@@ -109,6 +109,75 @@ void compute_distances_1_nonpacked_thread(int d, int nb, const float *a,
                                           int n_thread);
 
 /* ------------------------------------------------------------------ */
+/* drop-in: k-means (yael/kmeans.h)                                    */
+
+/* flag bits, same values as yael/kmeans.h:11-18 */
+#define YAEL_KMEANS_QUIET 0x10000
+#define YAEL_KMEANS_INIT_BERKELEY 0x20000
+#define YAEL_KMEANS_NORMALIZE_CENTS 0x40000
+#define YAEL_KMEANS_INIT_RANDOM 0x80000
+#define YAEL_KMEANS_INIT_USER 0x100000
+#define YAEL_KMEANS_L1 0x200000
+#define YAEL_KMEANS_CHI2 0x400000
+
+/* yael/kmeans.h:41-44 (yael/kmeans.c:332-447).  Same flags, seed (0 draws
+ * lrand48()), redo, outputs (each may be NULL) and return value (qerr / n, or
+ * -1 when too many empty clusters were split).  Assignments are exact:
+ * nearest centroid by FP64 distance, ties to the lowest index.  Centroids are
+ * exact integer sums (2^-S fixed point, S chosen from the data so nothing
+ * overflows) divided by the count.  flags & 0xffff (threads) is ignored;
+ * KMEANS_L1 / KMEANS_CHI2 abort with a message (not implemented). */
+float kmeans(int d, int n, int k, int niter, const float *v, int flags, long seed,
+             int redo, float *centroids, float *dis, int *assign, int *nassign);
+
+/* yael/kmeans.h:51-53 (yael/kmeans.c:492-504): malloc'd k x d centroids */
+float *clustering_kmeans(int n, int d, const float *points, int k, int nb_iter_max,
+                         double normalize);
+
+/* yael/kmeans.h:58-61 (yael/kmeans.c:484-490) */
+float *clustering_kmeans_assign(int n, int d, const float *points, int k,
+                                int nb_iter_max, double normalize,
+                                int **clust_assign_out);
+
+/* yael/kmeans.h:65-68 (yael/kmeans.c:452-482): nb_iter_max / 100000 = redo */
+float *clustering_kmeans_assign_with_score(int n, int d, const float *points, int k,
+                                           int nb_iter_max, double normalize,
+                                           int n_thread, double *score_out,
+                                           int **clust_assign_out);
+
+/* ------------------------------------------------------------------ */
+/* drop-in: hierarchical k-means (yael/hkm.h)                          */
+
+/* same layout as yael/hkm.h:10-16 */
+typedef struct hkm_s {
+  int nlevel;        /* number of levels */
+  int bf;            /* branching factor */
+  int k;             /* number of leaves, bf^nlevel */
+  int d;             /* dimension */
+  float **centroids; /* level l: bf^(l+1) x d centroids */
+} hkm_t;
+
+/* yael/hkm.h:21-23 (yael/hkm.c:36-116).  Every child clustering of a level
+ * runs in one grouped GPU pass; seeds are drawn with lrand48() in (level,
+ * parent) order as the reference does.  An empty node exits(1) like the
+ * reference. */
+hkm_t *hkm_learn(int n, int d, int nlevel, int bf, const float *v, int nb_iter_max,
+                 int nt, int verbose, int **clust_assign_out);
+
+/* yael/hkm.h:25 (yael/hkm.c:119-126) */
+void hkm_delete(hkm_t *hkm);
+
+/* yael/hkm.h:28 (yael/hkm.c:131-150): greedy descent, exact nearest child */
+void hkm_quantize(const hkm_t *hkm, int n, const float *v, int *idx);
+
+/* yael/hkm.h:31-32 (yael/hkm.c:181-232): same binary format */
+void hkm_write(const char *filename, const hkm_t *hkm);
+hkm_t *hkm_read(const char *filename);
+
+/* yael/hkm.h:35 (yael/hkm.c:154-157) */
+float *hkm_get_centroids(const hkm_t *hkm, int l, int no);
+
+/* ------------------------------------------------------------------ */
 /* extension API                                                       */
 
 #define YAEL_GPU_PREC_ENV (-1) /* take YAEL_GPU_PRECISION (fp32 | bf16), default fp32 */
@@ -142,6 +211,30 @@ typedef struct {
 /* k-NN with explicit options.  Same result contract as knn_full. */
 int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q,
                     int *assign, float *dis, yael_gpu_knn_opts *opts);
+
+typedef struct {
+  int precision;   /* YAEL_GPU_PREC_*: distance pass of the assignment step */
+  int device_ptrs; /* 1: v and the outputs are device pointers */
+  void *stream;    /* cudaStream_t for device_ptrs calls; NULL = the library's stream */
+  /* filled on return */
+  int status;      /* YAEL_GPU_OK or an error code (then the return value is -2) */
+  long iterations; /* total Lloyd iterations over all runs */
+  long n_fallback; /* points whose assignment certificate failed (recomputed exhaustively) */
+  float ms_assign; /* GPU time of the assignment steps */
+  float ms_update; /* GPU time of counts, sums, splits' uploads and objective */
+} yael_gpu_kmeans_opts;
+
+/* kmeans() with options; returns -2 on error (message: yael_gpu_last_error). */
+float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int flags,
+                         long seed, int redo, float *centroids, float *dis, int *assign,
+                         int *nassign, yael_gpu_kmeans_opts *opts);
+
+/* hkm_learn() with flat outputs: centroids = all levels concatenated
+ * (sum_l bf^(l+1) * d floats), assign (n ints, may be NULL).  Returns a status
+ * code; iterations and ms (GPU time) may be NULL. */
+int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v,
+                          int nb_iter_max, float *centroids, int *assign,
+                          long *iterations, float *ms);
 
 /* message of the last failure on the calling thread ("" if none) */
 const char *yael_gpu_last_error(void);

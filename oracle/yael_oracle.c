@@ -21,6 +21,9 @@
 #include <omp.h>
 #endif
 
+int sgemv_(const char *trans, const int *m, const int *n, const float *alpha,
+           const float *a, const int *lda, const float *x, const int *incx,
+           const float *beta, float *y, const int *incy);
 int sgemm_(const char *ta, const char *tb, const int *m, const int *n,
            const int *k, const float *alpha, const float *a, const int *lda,
            const float *b, const int *ldb, const float *beta, float *c,
@@ -486,6 +489,61 @@ void orc_kmeans_step_exact(int d, int n, int k, const float *v, const float *c_i
   update_exact(d, n, k, v, assign, nassign, c_out, S);
 }
 
+/* compute_distances_1_nonpacked (yael/nn.c:132-154): double norms + sgemv */
+static void distances_1_port(int d, int nb, const float *a, const float *b, int ldb,
+                             float *dist2)
+{
+  double sa = 0;
+  for (int j = 0; j < d; j++) sa += a[j] * a[j];
+  for (long i = 0; i < nb; i++) {
+    double s = 0;
+    const float *x = b + ldb * i;
+    for (int j = 0; j < d; j++) s += x[j] * x[j];
+    dist2[i] = s + sa;
+  }
+  float m2 = -2, one = 1;
+  int ione = 1;
+  sgemv_("Transposed", &d, &nb, &m2, b, &ldb, a, &ione, &one, dist2, &ione);
+}
+
+/* kmeanspp_init (yael/kmeans.c:27-82); the port computes the distances as
+ * compute_distances_1_thread does (yael/nn.c:840-860), the exact mode as
+ * FP64 rounded to float */
+static void kmeanspp_init(int d, int n, int k, const float *v, int *sel, unsigned int seed,
+                          int nt, int mode)
+{
+  float *best = malloc(sizeof(float) * (size_t)n);
+  float *tmp = malloc(sizeof(float) * (size_t)n);
+  for (long j = 0; j < n; j++) best[j] = HUGE_VAL;
+  sel[0] = rand_r(&seed) % k;
+  for (int i = 1; i < k; i++) {
+    int ns = sel[i - 1];
+    if (mode == ORC_PORT) {
+#pragma omp parallel for num_threads(nt > 0 ? nt : 1)
+      for (int t = 0; t < nt; t++) {
+        int i0 = t * n / nt, i1 = (t + 1) * n / nt;
+        distances_1_port(d, i1 - i0, v + (long)d * ns, v + (long)i0 * d, d, tmp + i0);
+      }
+    } else {
+#pragma omp parallel for schedule(static)
+      for (long j = 0; j < n; j++) tmp[j] = (float)dist64(v + j * d, v + (long)ns * d, d);
+    }
+    for (long j = 0; j < n; j++)
+      if (tmp[j] < best[j]) best[j] = tmp[j];
+    memcpy(tmp, best, sizeof(float) * (size_t)n);
+    mul_by(tmp, n, 1. / norm_l1(tmp, n));
+    double rd = drand_r(&seed);
+    long j;
+    for (j = 0; j < n - 1; j++) {
+      rd -= tmp[j];
+      if (rd < 0) break;
+    }
+    sel[i] = (int)j;
+  }
+  free(best);
+  free(tmp);
+}
+
 /* ------------------------------------------------------------------ */
 /* kmeans (yael/kmeans.c:213-447), L2 only                              */
 
@@ -553,10 +611,12 @@ float orc_kmeans(int d, int n, int k, int niter, const float *v, int flags,
       memcpy(C, C_out, sizeof(float) * (size_t)k * d);
     } else {
       if (flags & ORC_KMEANS_INIT_BERKELEY) {
-        fprintf(stderr, "oracle: k-means++ init not restated\n");
-        abort();
+        int nsub = n;
+        if (n > k * 8 && n > 8192) nsub = k * 8;
+        kmeanspp_init(d, nsub, k, v, sel, rand_r(&seed), nt, mode);
+      } else {
+        orc_random_init(n, k, rand_r(&seed), sel);
       }
-      orc_random_init(n, k, rand_r(&seed), sel);
       for (long i = 0; i < k; i++) memcpy(C + i * d, v + (long)sel[i] * d, sizeof(float) * d);
     }
     ret = kmeans_core(d, n, k, niter, nt, flags, C, v, rand_r(&seed), assign, nassign,

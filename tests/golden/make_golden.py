@@ -90,6 +90,14 @@ def main():
     np.savez_compressed(os.path.join(HERE, "kmeans_redo.npz"), v=v, k=10, niter=10, flags=quiet,
                         seed=5, redo=3, blas=blas, **res)
 
+    # 5b. k-means++ initialisation (KMEANS_INIT_BERKELEY), integer data so the
+    #     distances feeding the sampling are exact whatever the BLAS
+    v = rng.integers(0, 20, (3000, 12)).astype(np.float32)
+    fl = 0x10000 | 0x20000 | 4
+    res = run_kmeans(r, v, 30, 8, fl, 99, 1)
+    np.savez_compressed(os.path.join(HERE, "kmeans_pp.npz"), v=v, k=30, niter=8, flags=fl,
+                        seed=99, redo=1, blas=blas, **res)
+
     # 6. hierarchical k-means, seeds from lrand48 after srand48(42)
     centres = rng.standard_normal((64, 8)).astype(np.float32) * 2
     lab = rng.integers(0, 64, 4000)

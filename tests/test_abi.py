@@ -27,7 +27,7 @@ def built():
 
 def test_header_parses():
     names = declared_functions()
-    assert "knn_full" in names and "yael_gpu_knn_ex" in names
+    assert "knn_full" in names and "yael_gpu_knn_ex" in names and "kmeans" in names
     assert len(names) >= 20
 
 

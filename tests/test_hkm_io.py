@@ -1,0 +1,41 @@
+"""hkm_write / hkm_read of the C ABI (host code only, no GPU): the binary
+format of yael/hkm.c:181-232 -- int nlevel, bf, d, then one fvec record
+(int count, count floats) per level."""
+import ctypes
+import os
+import struct
+
+import numpy as np
+
+import yael_gb300 as yg
+
+
+def test_hkm_file_roundtrip(tmp_path):
+    from yael_gb300 import build
+    build.build()
+    L = yg.lib()
+    nlevel, bf, d = 2, 3, 4
+    path = str(tmp_path / "t.hkm")
+    rng = np.random.default_rng(0)
+    lv = [rng.standard_normal(bf ** (l + 1) * d).astype(np.float32) for l in range(nlevel)]
+    with open(path, "wb") as f:
+        f.write(struct.pack("iii", nlevel, bf, d))
+        for a in lv:
+            f.write(struct.pack("i", a.size))
+            f.write(a.tobytes())
+    h = L.hkm_read(path.encode())
+    assert h
+    hk = yg.Hkm.from_address(h)
+    assert (hk.nlevel, hk.bf, hk.d, hk.k) == (nlevel, bf, d, bf ** nlevel)
+    for l in range(nlevel):
+        got = np.ctypeslib.as_array(hk.centroids[l], shape=(lv[l].size,))
+        np.testing.assert_array_equal(got, lv[l])
+    c = L.hkm_get_centroids(h, 1, 2)
+    np.testing.assert_array_equal(
+        np.ctypeslib.as_array(ctypes.cast(c, ctypes.POINTER(ctypes.c_float)), shape=(bf * d,)),
+        lv[1][2 * bf * d:3 * bf * d])
+    out = str(tmp_path / "u.hkm")
+    L.hkm_write(out.encode(), h)
+    assert open(out, "rb").read() == open(path, "rb").read()
+    L.hkm_delete(h)
+    assert not L.hkm_read(str(tmp_path / "missing.hkm").encode())

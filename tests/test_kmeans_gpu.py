@@ -1,0 +1,158 @@
+"""k-means and hierarchical k-means on the GPU against the oracle.
+
+The oracle's exact mode implements the same semantics (FP64 nearest centroid,
+ties to the lowest index; exact fixed-point centroid sums; the reference's RNG
+stream for init and empty-cluster splits), so assignments, counts and
+centroids must be bit-identical; distances and the objective within FP32
+rounding of the FP64 values.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import yael_gb300 as yg
+from _util import GOLDEN, oracle, ptr, srand48
+from yael_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+QUIET = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM | 4
+
+
+def oracle_kmeans(v, k, niter, flags, seed, redo, C0=None):
+    n, d = v.shape
+    C = np.zeros((k, d), np.float32) if C0 is None else C0.copy()
+    dis = np.empty(n, np.float32)
+    assign = np.empty(n, np.int32)
+    nassign = np.empty(k, np.int32)
+    iters = ctypes.c_long(0)
+    q = oracle().orc_kmeans(d, n, k, niter, ptr(v), flags, seed, redo, ptr(C), ptr(dis),
+                            ptr(assign), ptr(nassign), 1, ctypes.addressof(iters))
+    return dict(C=C, dis=dis, assign=assign, nassign=nassign, qerr=q, iters=iters.value)
+
+
+def gpu_kmeans(v, k, niter, flags, seed, redo, prec, C0=None):
+    n, d = v.shape
+    C = np.zeros((k, d), np.float32) if C0 is None else C0.copy()
+    dis = np.empty(n, np.float32)
+    assign = np.empty(n, np.int32)
+    nassign = np.empty(k, np.int32)
+    o = yg.KmeansOpts({"fp32": 0, "bf16": 1}[prec], 0, None, 0, 0, 0, 0, 0)
+    q = yg.lib().yael_gpu_kmeans_ex(d, n, k, niter, ptr(v), flags, seed, redo, ptr(C), ptr(dis),
+                                    ptr(assign), ptr(nassign), ctypes.byref(o))
+    assert o.status == 0, yg.last_error()
+    return dict(C=C, dis=dis, assign=assign, nassign=nassign, qerr=q, iters=o.iterations)
+
+
+def same(g, o, rtol=2e-6):
+    np.testing.assert_array_equal(g["assign"], o["assign"])
+    np.testing.assert_array_equal(g["nassign"], o["nassign"])
+    np.testing.assert_array_equal(g["C"], o["C"])
+    np.testing.assert_allclose(g["dis"], o["dis"], rtol=rtol, atol=1e-6)
+    assert abs(g["qerr"] - o["qerr"]) <= 1e-6 * abs(o["qerr"]) + 1e-12
+    assert g["iters"] == o["iters"]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_kmeans_small_k(prec):
+    v, _, _ = synth.gaussian_mixture(5000, 16, 20, 0.3, seed=4)
+    same(gpu_kmeans(v, 20, 12, QUIET, 1234, 1, prec), oracle_kmeans(v, 20, 12, QUIET, 1234, 1))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_kmeans_large_k_knn_path(prec):
+    v, _, _ = synth.gaussian_mixture(20000, 32, 128, 0.15, seed=5)
+    same(gpu_kmeans(v, 100, 10, QUIET, 777, 1, prec), oracle_kmeans(v, 100, 10, QUIET, 777, 1))
+
+
+def test_kmeans_empty_cluster_splits():
+    g = np.load(os.path.join(GOLDEN, "kmeans_empty.npz"))
+    v = g["v"]
+    r = gpu_kmeans(v, 40, 20, QUIET, 77, 1, "fp32")
+    same(r, oracle_kmeans(v, 40, 20, QUIET, 77, 1))
+
+
+def test_kmeans_redo_keeps_best():
+    g = np.load(os.path.join(GOLDEN, "kmeans_redo.npz"))
+    v = g["v"]
+    same(gpu_kmeans(v, 10, 10, QUIET, 5, 3, "fp32"), oracle_kmeans(v, 10, 10, QUIET, 5, 3))
+
+
+def test_kmeans_plus_plus_init():
+    g = np.load(os.path.join(GOLDEN, "kmeans_pp.npz"))
+    v = g["v"]
+    fl = int(g["flags"])
+    same(gpu_kmeans(v, 30, 8, fl, 99, 1, "fp32"), oracle_kmeans(v, 30, 8, fl, 99, 1))
+
+
+def test_kmeans_init_user_and_normalize():
+    v, _, _ = synth.gaussian_mixture(3000, 24, 10, 0.2, seed=6)
+    C0 = v[:10].copy()
+    fl = yg.KMEANS_QUIET | yg.KMEANS_INIT_USER | yg.KMEANS_NORMALIZE_CENTS
+    same(gpu_kmeans(v, 10, 6, fl, 3, 5, "fp32", C0), oracle_kmeans(v, 10, 6, fl, 3, 5, C0))
+
+
+def test_kmeans_seed_zero_uses_lrand48():
+    v, _, _ = synth.gaussian_mixture(2000, 8, 12, 0.2, seed=7)
+    srand48(2024)
+    o = oracle_kmeans(v, 12, 5, QUIET, 0, 1)
+    srand48(2024)
+    same(gpu_kmeans(v, 12, 5, QUIET, 0, 1, "fp32"), o)
+
+
+def test_kmeans_drop_in_symbol(gpu_lib):
+    v, _, _ = synth.gaussian_mixture(4000, 16, 30, 0.2, seed=8)
+    n, d = v.shape
+    C = np.zeros((30, d), np.float32)
+    assign = np.empty(n, np.int32)
+    q = gpu_lib.kmeans(d, n, 30, 10, ptr(v), QUIET, 31, 1, ptr(C), None, ptr(assign), None)
+    o = oracle_kmeans(v, 30, 10, QUIET, 31, 1)
+    np.testing.assert_array_equal(assign, o["assign"])
+    np.testing.assert_array_equal(C, o["C"])
+    assert abs(q - o["qerr"]) <= 1e-6 * o["qerr"]
+
+
+def oracle_hkm(v, nlevel, bf, niter):
+    n, d = v.shape
+    sizes = [bf ** (l + 1) for l in range(nlevel)]
+    cent = np.zeros(sum(sizes) * d, np.float32)
+    assign = np.empty(n, np.int32)
+    rc = oracle().orc_hkm_learn(n, d, nlevel, bf, ptr(v), niter, ptr(cent), ptr(assign), 1)
+    assert rc == 0
+    return cent, assign
+
+
+def test_hkm_exact_vs_oracle():
+    v, _, _ = synth.gaussian_mixture(30000, 16, 200, 0.1, seed=9)
+    srand48(42)
+    oc, oa = oracle_hkm(v, 3, 5, 10)
+    srand48(42)
+    levels, ga = yg.hkm(v, 3, 5, 10)
+    np.testing.assert_array_equal(ga, oa)
+    np.testing.assert_array_equal(np.concatenate([l.ravel() for l in levels]), oc)
+
+
+def test_hkm_golden_and_quantize(gpu_lib):
+    g = np.load(os.path.join(GOLDEN, "hkm.npz"))
+    v = g["v"]
+    n, d = v.shape
+    srand48(int(g["srand"]))
+    ap = ctypes.POINTER(ctypes.c_int)()
+    h = gpu_lib.hkm_learn(n, d, 2, 4, ptr(v), 8, 4, 0, ctypes.byref(ap))
+    hk = yg.Hkm.from_address(h)
+    assign = np.ctypeslib.as_array(ap, shape=(n,)).copy()
+    lv0 = np.ctypeslib.as_array(hk.centroids[0], shape=(4 * d,)).reshape(4, d)
+    lv1 = np.ctypeslib.as_array(hk.centroids[1], shape=(16 * d,)).reshape(16, d)
+    # well separated data: the reference's FP32 path makes the same choices
+    np.testing.assert_array_equal(assign, g["assign"])
+    np.testing.assert_allclose(lv0, g["level0"], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(lv1, g["level1"], rtol=1e-5, atol=1e-5)
+    q = np.empty(n, np.int32)
+    gpu_lib.hkm_quantize(h, n, ptr(v), ptr(q))
+    cent = np.concatenate([lv0.ravel(), lv1.ravel()]).astype(np.float32)
+    oq = np.empty(n, np.int32)
+    oracle().orc_hkm_quantize(2, 4, d, ptr(cent), n, ptr(v), ptr(oq), 1)
+    np.testing.assert_array_equal(q, oq)
+    gpu_lib.hkm_delete(h)
+    ctypes.CDLL(None).free(ctypes.cast(ap, ctypes.c_void_p))

@@ -75,7 +75,8 @@ def run_kmeans(v, k, niter, flags, seed, redo, mode):
     return dict(C=C, dis=dis, assign=assign, nassign=nassign, qerr=np.float32(q))
 
 
-@pytest.mark.parametrize("name", ["kmeans_sep.npz", "kmeans_empty.npz", "kmeans_redo.npz"])
+@pytest.mark.parametrize("name", ["kmeans_sep.npz", "kmeans_empty.npz", "kmeans_redo.npz",
+                                  "kmeans_pp.npz"])
 def test_port_kmeans_matches_reference(name):
     g = load(name)
     r = run_kmeans(g["v"], int(g["k"]), int(g["niter"]), int(g["flags"]), int(g["seed"]),

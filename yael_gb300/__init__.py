@@ -37,6 +37,17 @@ KMEANS_CHI2 = 0x400000
 PREC_ENV, PREC_FP32, PREC_BF16 = -1, 0, 1
 
 
+class KmeansOpts(ctypes.Structure):
+    _fields_ = [("precision", c_int), ("device_ptrs", c_int), ("stream", P), ("status", c_int),
+                ("iterations", c_long), ("n_fallback", c_long), ("ms_assign", c_float),
+                ("ms_update", c_float)]
+
+
+class Hkm(ctypes.Structure):
+    _fields_ = [("nlevel", c_int), ("bf", c_int), ("k", c_int), ("d", c_int),
+                ("centroids", ctypes.POINTER(ctypes.POINTER(c_float)))]
+
+
 class KnnOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("metric", c_int), ("device_ptrs", c_int),
                 ("stream", P), ("n_fallback", c_int), ("n_candidates", c_int),
@@ -66,6 +77,18 @@ SIGNATURES = {
     "compute_distances_1_nonpacked_thread": (None, [c_int, c_int, P, P, c_int, P, c_int]),
     "yael_gpu_knn_ex": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, ctypes.POINTER(KnnOpts)]),
     "yael_gpu_last_error": (ctypes.c_char_p, []),
+    "kmeans": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P]),
+    "clustering_kmeans": (P, [c_int, c_int, P, c_int, c_int, c_double]),
+    "clustering_kmeans_assign": (P, [c_int, c_int, P, c_int, c_int, c_double, P]),
+    "clustering_kmeans_assign_with_score": (P, [c_int, c_int, P, c_int, c_int, c_double, c_int, P, P]),
+    "hkm_learn": (P, [c_int, c_int, c_int, c_int, P, c_int, c_int, c_int, P]),
+    "hkm_delete": (None, [P]),
+    "hkm_quantize": (None, [P, c_int, P, P]),
+    "hkm_write": (None, [ctypes.c_char_p, P]),
+    "hkm_read": (P, [ctypes.c_char_p]),
+    "hkm_get_centroids": (P, [P, c_int, c_int]),
+    "yael_gpu_kmeans_ex": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P, ctypes.c_void_p]),
+    "yael_gpu_hkm_learn_ex": (c_int, [c_int, c_int, c_int, c_int, P, c_int, P, P, P, P]),
     "yael_gpu_version": (c_int, []),
     "yael_gpu_launch_count": (c_long, []),
 }
@@ -146,3 +169,59 @@ def cross_distances(a, b, distance_type=12):
     lib().compute_cross_distances_alt_nonpacked(distance_type, d, na, nb, _ptr(a), d, _ptr(b), d,
                                                 _ptr(dis), na)
     return dis
+
+
+def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
+           normalize=False, init="random", output="centroids", precision=None,
+           stats=False):
+    """k-means with the contract of ynumpy.kmeans (yael/ynumpy.py:87-130)."""
+    v = _f32(v)
+    n, d = v.shape
+    centroids = np.zeros((k, d), dtype=np.float32)
+    dis = np.empty(n, dtype=np.float32)
+    assign = np.empty(n, dtype=np.int32)
+    nassign = np.empty(k, dtype=np.int32)
+    flags = nt
+    if not verbose:
+        flags |= KMEANS_QUIET
+    if distance_type == 1:
+        flags |= KMEANS_L1
+    elif distance_type == 3:
+        flags |= KMEANS_CHI2
+    if init == "random":
+        flags |= KMEANS_INIT_RANDOM
+    elif init == "kmeans++":
+        flags |= KMEANS_INIT_BERKELEY
+    if normalize:
+        flags |= KMEANS_NORMALIZE_CENTS
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
+    opts = KmeansOpts(prec, 0, None, 0, 0, 0, 0, 0)
+    qerr = lib().yael_gpu_kmeans_ex(d, n, k, niter, _ptr(v), flags, seed, redo, _ptr(centroids),
+                                    _ptr(dis), _ptr(assign), _ptr(nassign), ctypes.byref(opts))
+    if opts.status != 0:
+        raise RuntimeError(f"kmeans failed: {last_error()}")
+    if qerr < 0:
+        raise RuntimeError("kmeans: clustering failed. Is dataset diverse enough?")
+    res = centroids if output == "centroids" else (centroids, qerr, dis, assign, nassign)
+    if stats:
+        return res, {"iterations": opts.iterations, "n_fallback": opts.n_fallback,
+                     "ms_assign": opts.ms_assign, "ms_update": opts.ms_update}
+    return res
+
+
+def hkm(v, nlevel, bf, niter=15):
+    """Hierarchical k-means: (list of per-level centroid arrays, leaf assignment)."""
+    v = _f32(v)
+    n, d = v.shape
+    sizes = [bf ** (l + 1) for l in range(nlevel)]
+    cent = np.empty(sum(sizes) * d, dtype=np.float32)
+    assign = np.empty(n, dtype=np.int32)
+    rc = lib().yael_gpu_hkm_learn_ex(n, d, nlevel, bf, _ptr(v), niter, _ptr(cent), _ptr(assign),
+                                     None, None)
+    if rc != 0:
+        raise RuntimeError(f"hkm failed: {last_error()}")
+    out, o = [], 0
+    for s in sizes:
+        out.append(cent[o:o + s * d].reshape(s, d))
+        o += s * d
+    return out, assign

@@ -1,0 +1,868 @@
+// k-means Lloyd loop and hierarchical k-means on the GPU: the host control
+// flow of yael/kmeans.c:166-447 and yael/hkm.c:36-232 (seeds, init, empty
+// cluster splits, stopping rules, outputs) around the device step of
+// kmeans.cuh.  Every random draw is the reference's, from libc rand_r /
+// lrand48 in the same order, so runs are reproducible against it.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <memory>
+#include <unordered_map>
+#include <vector>
+
+#include "kmeans.cuh"
+#include "knn.cuh"
+#include "../../include/yael_gpu.h"
+
+namespace yg {
+
+namespace {
+
+template <typename T>
+int ws_get(Workspace &ws, int slot, size_t count, T **p) {
+  void *v = nullptr;
+  YG_CHECK(ws.get(slot, count * sizeof(T) + 16, &v));
+  *p = reinterpret_cast<T *>(v);
+  return OK;
+}
+
+enum KmSlot : int {
+  KS_V = WS_KM0, KS_C, KS_ASSIGN, KS_DIS, KS_COUNTS, KS_OFFS, KS_CURSOR, KS_PERM, KS_ACC,
+  KS_SHIFT, KS_ACTIVE, KS_PINST, KS_WORK, KS_SLICES, KS_PART, KS_ROWS, KS_AMAX,
+  KS_BEST_C, KS_BEST_DIS, KS_BEST_ASSIGN, KS_NODE, KS_VSORT, KS_TMP,
+};
+
+// ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
+
+double drand_r_(unsigned *seed) { return rand_r(seed) / ((double)RAND_MAX + 1.0); }
+
+// Kinderman-Monahan ratio of uniforms, with the reference's float / double
+// roundings: u1, u2 and zz are held in float.
+double gaussrand_r_(unsigned *seed) {
+  const double magic = 1.71552776992141;  // 4 exp(-1/2) / sqrt(2)
+  double z;
+  for (;;) {
+    const float u1 = (float)drand_r_(seed);
+    const float u2 = (float)drand_r_(seed);
+    z = magic * (u1 - .5) / u2;
+    const float zz = (float)(z * z / 4.0);
+    if (zz < -log(u2)) break;
+  }
+  return z;
+}
+
+// the first k entries of the partial Fisher-Yates shuffle of 0..n-1 that
+// ivec_new_random_perm_r performs (only the first k swaps reach them)
+void random_init_first_k(int n, int k, unsigned seed, long *sel) {
+  std::unordered_map<int, int> moved;
+  auto at = [&](int i) {
+    auto it = moved.find(i);
+    return it == moved.end() ? i : it->second;
+  };
+  for (int i = 0; i < k && i < n; i++) {
+    const int j = i + rand_r(&seed) % (n - i);
+    const int vi = at(i), vj = at(j);
+    sel[i] = vj;
+    moved[j] = vi;
+  }
+}
+
+double l1(const float *v, long n) {
+  double s = 0;
+  for (long i = 0; i < n; i++) s += fabs(v[i]);
+  return s;
+}
+double l2(const float *v, long n) {
+  double s = 0;
+  for (long i = 0; i < n; i++) s += v[i] * v[i];
+  return sqrt(s);
+}
+void mul_by(float *v, long n, double s) {
+  for (long i = 0; i < n; i++) v[i] *= s;
+}
+
+// kmeans_reassign_empty (yael/kmeans.c:166-209) on a host copy of the centroids
+int reassign_empty(int d, int k, float *C, const int *nassign, unsigned seed) {
+  int nre = 0;
+  std::vector<float> p(k), eps(d);
+  for (int c = 0; c < k; c++) {
+    // nassign^2 - 1 in int arithmetic (wraps for large clusters, like the reference)
+    const unsigned sq = (unsigned)nassign[c] * (unsigned)nassign[c] - 1u;
+    p[c] = nassign[c] < 2 ? 0.f : (float)(int)sq;
+  }
+  mul_by(p.data(), k, 1. / l1(p.data(), k));
+  for (int c = 0; c < k; c++) {
+    if (nassign[c] != 0) continue;
+    nre++;
+    double rd = drand_r_(&seed);
+    int j;
+    for (j = 0; j < k - 1; j++) {
+      rd -= p[j];
+      if (rd < 0) break;
+    }
+    memcpy(C + (long)c * d, C + (long)j * d, sizeof(float) * d);
+    const double s = l2(C + (long)j * d, d) * 0.0000001;
+    unsigned s2 = rand_r(&seed);
+    for (int i = 0; i < d; i++) eps[i] = (float)gaussrand_r_(&s2);
+    mul_by(eps.data(), d, s);
+    for (int i = 0; i < d; i++) C[(long)j * d + i] += eps[i];
+    for (int i = 0; i < d; i++) C[(long)c * d + i] -= eps[i];
+    p[j] = 0;
+    mul_by(p.data(), k, 1. / l1(p.data(), k));
+  }
+  return nre;
+}
+
+int fixed_shift(long n, float maxabs) {
+  int e = 0;
+  if (maxabs > 0) frexp((double)maxabs, &e);
+  int lg = 0;
+  while ((1L << lg) < n) lg++;
+  return 62 - lg - e;
+}
+
+// ---- the batched Lloyd engine --------------------------------------------
+
+struct Instance {
+  long p0 = 0;
+  int n = 0;
+  unsigned seed = 0;  // the kmeans() seed after the seed_in -> unsigned conversion
+  unsigned core = 0;  // rand_r stream of kmeans_core
+  int tot_re = 0, iters = 0, ret = 0;
+  double qerr = HUGE_VAL, qerr_old = HUGE_VAL;
+  bool done = false;
+};
+
+struct Engine {
+  Ctx *ctx;
+  cudaStream_t st;
+  int d, k, niter, flags, prec;
+  bool verbose;
+  const float *v;  // device points (all instances, contiguous)
+  long ntot;
+  std::vector<Instance> in;
+  // device buffers
+  float *C, *dis, *amax;
+  int *assign, *counts, *shift, *pinst;
+  unsigned char *active;
+  long *offs, *cursor, *perm, *rows;
+  long long *acc;
+  KmWork *work;
+  KmSlice *slices;
+  double *part;
+  int nwork = 0, nsl = 0;
+  std::vector<KmSlice> hsl;
+  std::vector<int> hcounts;
+  std::vector<double> hpart;
+  long n_fallback = 0;
+  float ms_assign = 0, ms_update = 0;
+
+  int setup() {
+    Workspace &ws = ctx->ws;
+    const int ni = (int)in.size();
+    const long ncl = (long)ni * k;
+    YG_CHECK(ws_get(ws, KS_C, (size_t)ncl * d, &C));
+    YG_CHECK(ws_get(ws, KS_ASSIGN, (size_t)ntot, &assign));
+    YG_CHECK(ws_get(ws, KS_DIS, (size_t)ntot, &dis));
+    YG_CHECK(ws_get(ws, KS_COUNTS, (size_t)ncl, &counts));
+    YG_CHECK(ws_get(ws, KS_OFFS, (size_t)ncl + 1, &offs));
+    YG_CHECK(ws_get(ws, KS_CURSOR, (size_t)ncl, &cursor));
+    YG_CHECK(ws_get(ws, KS_PERM, (size_t)ntot, &perm));
+    YG_CHECK(ws_get(ws, KS_ACC, (size_t)ncl * d, &acc));
+    YG_CHECK(ws_get(ws, KS_SHIFT, (size_t)ni, &shift));
+    YG_CHECK(ws_get(ws, KS_ACTIVE, (size_t)ni, &active));
+    YG_CHECK(ws_get(ws, KS_AMAX, (size_t)ni, &amax));
+    pinst = nullptr;
+    std::vector<KmWork> hw;
+    hsl.clear();
+    std::vector<int> hpinst;
+    if (ni > 1) hpinst.resize(ntot);
+    for (int i = 0; i < ni; i++) {
+      for (long o = 0; o < in[i].n; o += kAssignChunk)
+        hw.push_back({i, in[i].p0 + o, (int)std::min<long>(kAssignChunk, in[i].n - o)});
+      for (long o = 0; o < in[i].n; o += kSliceLen)
+        hsl.push_back({in[i].p0 + o, (int)std::min<long>(kSliceLen, in[i].n - o), i});
+      if (ni > 1)
+        for (long p = 0; p < in[i].n; p++) hpinst[in[i].p0 + p] = i;
+    }
+    nwork = (int)hw.size();
+    nsl = (int)hsl.size();
+    YG_CHECK(ws_get(ws, KS_WORK, (size_t)nwork, &work));
+    YG_CHECK(ws_get(ws, KS_SLICES, (size_t)nsl, &slices));
+    YG_CHECK(ws_get(ws, KS_PART, (size_t)nsl, &part));
+    YG_CUDA(cudaMemcpyAsync(work, hw.data(), sizeof(KmWork) * nwork, cudaMemcpyHostToDevice, st));
+    YG_CUDA(cudaMemcpyAsync(slices, hsl.data(), sizeof(KmSlice) * nsl, cudaMemcpyHostToDevice, st));
+    if (ni > 1) {
+      YG_CHECK(ws_get(ws, KS_PINST, (size_t)ntot, &pinst));
+      YG_CUDA(cudaMemcpyAsync(pinst, hpinst.data(), sizeof(int) * ntot, cudaMemcpyHostToDevice, st));
+    }
+    // fixed-point shift per instance from its data (exact integer sums)
+    YG_CUDA(cudaMemsetAsync(amax, 0, sizeof(float) * ni, st));
+    YG_CHECK(km_absmax(slices, nsl, v, d, amax, st));
+    std::vector<float> ha(ni);
+    YG_CUDA(cudaMemcpyAsync(ha.data(), amax, sizeof(float) * ni, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> hs(ni);
+    for (int i = 0; i < ni; i++) hs[i] = fixed_shift(in[i].n, ha[i]);
+    YG_CUDA(cudaMemcpyAsync(shift, hs.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, st));
+    hcounts.resize(ncl);
+    hpart.resize(nsl);
+    YG_CUDA(cudaStreamSynchronize(st));
+    return OK;
+  }
+
+  // random-point initialisation of every instance (yael/kmeans.c:401-405)
+  int init_random() {
+    const int ni = (int)in.size();
+    std::vector<long> hrows((size_t)ni * k);
+    for (int i = 0; i < ni; i++) {
+      random_init_first_k(in[i].n, k, rand_r(&in[i].seed), hrows.data() + (size_t)i * k);
+      for (int j = 0; j < k; j++) hrows[(size_t)i * k + j] += in[i].p0;
+    }
+    YG_CHECK(ws_get(ctx->ws, KS_ROWS, hrows.size(), &rows));
+    YG_CUDA(cudaMemcpyAsync(rows, hrows.data(), sizeof(long) * hrows.size(),
+                            cudaMemcpyHostToDevice, st));
+    YG_CHECK(km_gather(v, d, rows, (long)hrows.size(), C, st));
+    return OK;
+  }
+
+  int set_active() {
+    std::vector<unsigned char> h(in.size());
+    for (size_t i = 0; i < in.size(); i++) h[i] = !in[i].done;
+    YG_CUDA(cudaMemcpyAsync(active, h.data(), h.size(), cudaMemcpyHostToDevice, st));
+    YG_CUDA(cudaStreamSynchronize(st));  // h is a stack buffer
+    return OK;
+  }
+
+  int assign_step() {
+    if (in.size() == 1 && k > kSmallK) {
+      KnnJob job;
+      job.nq = in[0].n; job.nb = k; job.d = d; job.k = 1; job.metric = METRIC_L2;
+      job.prec = prec;
+      job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
+      job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
+      YG_CHECK(knn_device(job, ctx, st));
+      n_fallback += job.n_fallback;
+      return OK;
+    }
+    return km_assign_small(work, nwork, v, d, C, k, active, assign, dis, st);
+  }
+
+  // one Lloyd iteration for every active instance (yael/kmeans.c:237-318)
+  int iterate() {
+    const int ni = (int)in.size();
+    const long ncl = (long)ni * k;
+    for (auto &x : in)
+      if (!x.done) x.iters++;
+    cudaEvent_t e0, e1, e2;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventCreate(&e2);
+    cudaEventRecord(e0, st);
+    YG_CHECK(assign_step());
+    cudaEventRecord(e1, st);
+    YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
+    YG_CHECK(km_histogram(assign, pinst, ntot, k, active, counts, st));
+    YG_CHECK(km_scan(counts, ncl, offs, cursor, st));
+    YG_CHECK(km_scatter(assign, pinst, ntot, k, active, cursor, perm, st));
+    YG_CHECK(km_update(perm, offs + ncl, ntot, assign, pinst, counts, v, d, ncl, k, shift, active,
+                       acc, C, st));
+    if (flags & YAEL_KMEANS_NORMALIZE_CENTS) YG_CHECK(km_normalize(C, ncl, d, k, active, st));
+    YG_CHECK(km_slice_sums(slices, nsl, dis, part, st));
+    YG_CUDA(cudaMemcpyAsync(hcounts.data(), counts, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaMemcpyAsync(hpart.data(), part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
+    cudaEventRecord(e2, st);
+    YG_CUDA(cudaStreamSynchronize(st));
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, e0, e1);
+    cudaEventElapsedTime(&b, e1, e2);
+    ms_assign += a;
+    ms_update += b;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+
+    // objective per instance: slice sums in point order
+    std::vector<double> q(ni, 0.0);
+    for (int s = 0; s < nsl; s++) q[hsl[s].inst] += hpart[s];
+
+    std::vector<float> hc;
+    bool any_split = false;
+    for (int i = 0; i < ni; i++) {
+      Instance &x = in[i];
+      if (x.done) continue;
+      // empty clusters -> split (the draw happens every iteration)
+      const unsigned sseed = rand_r(&x.core);
+      const int *cnt = hcounts.data() + (long)i * k;
+      bool empty = false;
+      for (int c = 0; c < k; c++) empty |= cnt[c] == 0;
+      int nre = 0;
+      if (empty) {
+        hc.resize((size_t)k * d);
+        YG_CUDA(cudaMemcpyAsync(hc.data(), C + (long)i * k * d, sizeof(float) * k * d,
+                                cudaMemcpyDeviceToHost, st));
+        YG_CUDA(cudaStreamSynchronize(st));
+        nre = reassign_empty(d, k, hc.data(), cnt, sseed);
+        YG_CUDA(cudaMemcpyAsync(C + (long)i * k * d, hc.data(), sizeof(float) * k * d,
+                                cudaMemcpyHostToDevice, st));
+        YG_CUDA(cudaStreamSynchronize(st));
+        any_split = true;
+        if (nre > 0 && verbose)
+          fprintf(stderr, "# kmeans warning: %d empty clusters -> split\n", nre);
+      }
+      x.tot_re += nre;
+      if (x.tot_re > x.n / 100 && x.tot_re > 1000) {
+        fprintf(stderr, "# kmeans: reassigned %d times, abandoning\n", x.tot_re);
+        x.ret = -1;
+        x.done = true;
+        continue;
+      }
+      x.qerr_old = x.qerr;
+      x.qerr = q[i];
+      if (x.qerr_old == x.qerr && nre == 0) {
+        x.done = true;
+        continue;
+      }
+      if (verbose) {
+        printf(" -> %.3f", x.qerr / x.n);
+        fflush(stdout);
+      }
+      if (x.iters >= niter) x.done = true;
+    }
+    (void)any_split;
+    return set_active();
+  }
+
+  bool all_done() const {
+    for (auto &x : in)
+      if (!x.done) return false;
+    return true;
+  }
+};
+
+// D2H of whichever outputs are requested (device or host destinations)
+int copy_out(cudaStream_t st, void *dst, const void *src, size_t bytes, bool dev) {
+  if (!dst || bytes == 0) return OK;
+  YG_CUDA(cudaMemcpyAsync(dst, src, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          st));
+  return OK;
+}
+
+// kmeans++ initialisation (yael/kmeans.c:27-82): squared distances to each
+// newly selected point on the GPU (FP64, rounded to float), the sampling
+// (normalisation and the sequential double subtraction) on the host
+__global__ void kpp_kernel(const float *v, int d, long n, long newsel, float *best) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int c = 0; c < d; c++) {
+    const double t = (double)v[i * d + c] - (double)v[newsel * d + c];
+    s += t * t;
+  }
+  const float f = (float)s;
+  if (f < best[i]) best[i] = f;
+}
+
+__global__ void fill_kernel(float *p, long n, float x) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = x;
+}
+
+int kmeanspp(Ctx *ctx, cudaStream_t st, const float *v, int d, int nsub, int k, bool verbose,
+             unsigned seed, long *sel) {
+  float *best;
+  YG_CHECK(ws_get(ctx->ws, KS_TMP, (size_t)nsub, &best));
+  fill_kernel<<<(unsigned)ceil_div(nsub, 256), 256, 0, st>>>(best, nsub, HUGE_VALF);
+  YG_LAUNCH_CHECK();
+  std::vector<float> h(nsub);
+  sel[0] = rand_r(&seed) % k;  // the reference draws modulo k here
+  for (int i = 1; i < k; i++) {
+    if (verbose && i % 10 == 0) {
+      printf("%d/%d\r", i, k);
+      fflush(stdout);
+    }
+    kpp_kernel<<<(unsigned)ceil_div(nsub, 256), 256, 0, st>>>(v, d, nsub, sel[i - 1], best);
+    YG_LAUNCH_CHECK();
+    YG_CUDA(cudaMemcpyAsync(h.data(), best, sizeof(float) * nsub, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    mul_by(h.data(), nsub, 1. / l1(h.data(), nsub));
+    double rd = drand_r_(&seed);
+    long j;
+    for (j = 0; j < nsub - 1; j++) {
+      rd -= h[j];
+      if (rd < 0) break;
+    }
+    sel[i] = j;
+  }
+  if (verbose) printf("\n");
+  return OK;
+}
+
+}  // namespace
+
+// kmeans() (yael/kmeans.c:332-447) on device or host buffers
+int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, long seed_in,
+               int redo, float *C_out, float *dis_out, int *assign_out, int *nassign_out,
+               int prec, bool dev, cudaStream_t st_in, float *ret_out, long *iters_out,
+               long *fallback_out, float *ms_assign, float *ms_update) {
+  Ctx *ctx;
+  YG_CHECK(ctx_get(&ctx));
+  cudaStream_t st = st_in ? st_in : ctx->stream;
+  const bool verbose = !(flags & YAEL_KMEANS_QUIET);
+  niter = niter == 0 ? 1000000 : niter;
+  const bool user = (flags & YAEL_KMEANS_INIT_USER) != 0;
+  if (user) {
+    if (!C_out) {
+      set_error(E_ARG, "kmeans: KMEANS_INIT_USER needs the initial centroids");
+      return E_ARG;
+    }
+    redo = 1;
+  }
+  if (k > n || k < 1 || d < 1) {
+    set_error(E_ARG, "kmeans: k=%d n=%d d=%d (the reference asserts k <= n)", k, n, d);
+    return E_ARG;
+  }
+  if (flags & (YAEL_KMEANS_L1 | YAEL_KMEANS_CHI2)) {
+    set_error(E_UNSUPPORTED, "kmeans: L1 / chi2 k-means are not implemented on the GPU");
+    return E_UNSUPPORTED;
+  }
+  const float *v = v_in;
+  if (!dev) {
+    float *dv;
+    YG_CHECK(ws_get(ctx->ws, KS_V, (size_t)n * d, &dv));
+    YG_CUDA(cudaMemcpyAsync(dv, v_in, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
+    v = dv;
+  }
+  if (seed_in == 0) seed_in = lrand48();
+  Engine E;
+  E.ctx = ctx; E.st = st; E.d = d; E.k = k; E.niter = niter; E.flags = flags; E.prec = prec;
+  E.verbose = verbose; E.v = v; E.ntot = n;
+  E.in.resize(1);
+  E.in[0].n = n;
+  E.in[0].seed = (unsigned)seed_in;
+  YG_CHECK(E.setup());
+  double best = HUGE_VAL;
+  long iter_tot = 0;
+  int core_ret = 0;
+  float *bC = nullptr, *bdis = nullptr;
+  int *bassign = nullptr;
+  std::vector<int> bnassign(k);
+  for (int run = 0; run < redo; run++) {
+    if (verbose) printf("<><><><> kmeans / run %d <><><><><>\n", run);
+    Instance &x = E.in[0];
+    if (user) {
+      YG_CUDA(cudaMemcpyAsync(E.C, C_out, sizeof(float) * (size_t)k * d,
+                              dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    } else if (flags & YAEL_KMEANS_INIT_BERKELEY) {
+      int nsub = n;
+      if (n > k * 8 && n > 8192) {
+        nsub = k * 8;
+        if (verbose) printf("Restricting k-means++ initialization to %d points\n", nsub);
+      }
+      std::vector<long> sel(k);
+      YG_CHECK(kmeanspp(ctx, st, v, d, nsub, k, verbose, rand_r(&x.seed), sel.data()));
+      long *rows;
+      YG_CHECK(ws_get(ctx->ws, KS_ROWS, (size_t)k, &rows));
+      YG_CUDA(cudaMemcpyAsync(rows, sel.data(), sizeof(long) * k, cudaMemcpyHostToDevice, st));
+      YG_CHECK(km_gather(v, d, rows, k, E.C, st));
+      YG_CUDA(cudaStreamSynchronize(st));
+    } else {
+      YG_CHECK(E.init_random());
+    }
+    x.core = rand_r(&x.seed);
+    x.tot_re = 0; x.iters = 0; x.ret = 0; x.done = false;
+    x.qerr = HUGE_VAL; x.qerr_old = HUGE_VAL;
+    YG_CHECK(E.set_active());
+    while (!E.all_done()) YG_CHECK(E.iterate());
+    if (verbose) printf("\n");
+    iter_tot += x.iters;
+    core_ret = x.ret;
+    if (core_ret < 0) break;
+    if (x.qerr < best) {
+      best = x.qerr;
+      if (redo > 1) {
+        // keep this run's outputs on the device until a better run replaces them
+        YG_CHECK(ws_get(ctx->ws, KS_BEST_C, (size_t)k * d, &bC));
+        YG_CHECK(ws_get(ctx->ws, KS_BEST_DIS, (size_t)n, &bdis));
+        YG_CHECK(ws_get(ctx->ws, KS_BEST_ASSIGN, (size_t)n, &bassign));
+        YG_CUDA(cudaMemcpyAsync(bC, E.C, sizeof(float) * (size_t)k * d, cudaMemcpyDeviceToDevice, st));
+        YG_CUDA(cudaMemcpyAsync(bdis, E.dis, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+        YG_CUDA(cudaMemcpyAsync(bassign, E.assign, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+      } else {
+        bC = E.C; bdis = E.dis; bassign = E.assign;
+      }
+      bnassign.assign(E.hcounts.begin(), E.hcounts.begin() + k);
+    }
+  }
+  if (verbose && core_ret >= 0) {
+    printf("Total number of iterations: %ld\n", iter_tot);
+    // unbalanced factor of the last iteration's counts (yael/vector.c:2301-2314)
+    double tot = 0, uf = 0;
+    for (int c = 0; c < k; c++) {
+      tot += E.hcounts[c];
+      uf += E.hcounts[c] * (double)E.hcounts[c];
+    }
+    printf("Unbalanced factor of last iteration: %g\n", uf * k / (tot * tot));
+  }
+  if (best < HUGE_VAL && bC) {
+    YG_CHECK(copy_out(st, C_out, bC, sizeof(float) * (size_t)k * d, dev));
+    YG_CHECK(copy_out(st, dis_out, bdis, sizeof(float) * (size_t)n, dev));
+    YG_CHECK(copy_out(st, assign_out, bassign, sizeof(int) * (size_t)n, dev));
+    if (nassign_out) {
+      YG_CUDA(cudaMemcpyAsync(nassign_out, bnassign.data(), sizeof(int) * k,
+                              dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost, st));
+    }
+  }
+  YG_CUDA(cudaStreamSynchronize(st));
+  if (iters_out) *iters_out = iter_tot;
+  if (fallback_out) *fallback_out = E.n_fallback;
+  if (ms_assign) *ms_assign = E.ms_assign;
+  if (ms_update) *ms_update = E.ms_update;
+  *ret_out = core_ret < 0 ? -1.f : (float)(best / n);
+  return OK;
+}
+
+// ---- hierarchical k-means (yael/hkm.c) -----------------------------------
+
+__global__ void node_update_kernel(const long *perm_sorted, const int *child, long n, int bf,
+                                   int *node) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long p = perm_sorted[i];
+  node[p] = node[p] * bf + child[i];
+}
+
+int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bool verbose,
+            int prec, float **levels_out, int *assign_out, long *iters_out, float *ms_out) {
+  Ctx *ctx;
+  YG_CHECK(ctx_get(&ctx));
+  cudaStream_t st = ctx->stream;
+  float *dv, *vs;
+  int *node;
+  long *sorted;
+  YG_CHECK(ws_get(ctx->ws, KS_V, (size_t)n * d, &dv));
+  YG_CHECK(ws_get(ctx->ws, KS_VSORT, (size_t)n * d, &vs));
+  YG_CHECK(ws_get(ctx->ws, KS_NODE, (size_t)n, &node));
+  YG_CHECK(ws_get(ctx->ws, KS_TMP, (size_t)n * 2, &sorted));
+  YG_CUDA(cudaMemcpyAsync(dv, points, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
+  YG_CUDA(cudaMemsetAsync(node, 0, sizeof(int) * n, st));
+  std::vector<int> hnode(n, 0);
+  std::vector<long> hperm(n);
+  long k = 1, iters = 0;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, st);
+  for (int l = 0; l < nlevel; l++) {
+    // points grouped by parent, stable in point index (ivec_sort_index, hkm.c:56-62)
+    std::vector<long> start(k + 1, 0);
+    for (int i = 0; i < n; i++) start[hnode[i] + 1]++;
+    for (long p = 0; p < k; p++) start[p + 1] += start[p];
+    {
+      std::vector<long> pos(start.begin(), start.end() - 1);
+      for (int i = 0; i < n; i++) hperm[pos[hnode[i]]++] = i;
+    }
+    YG_CUDA(cudaMemcpyAsync(sorted, hperm.data(), sizeof(long) * n, cudaMemcpyHostToDevice, st));
+    YG_CHECK(km_gather(dv, d, sorted, n, vs, st));
+    Engine E;
+    E.ctx = ctx; E.st = st; E.d = d; E.k = bf; E.niter = niter == 0 ? 1000000 : niter;
+    E.flags = YAEL_KMEANS_INIT_RANDOM | YAEL_KMEANS_QUIET;
+    E.prec = prec; E.verbose = false; E.v = vs; E.ntot = n;
+    E.in.resize(k);
+    for (long p = 0; p < k; p++) {
+      const long na = start[p + 1] - start[p];
+      if (verbose)
+        fprintf(stderr, "[Level %d | Parent %ld] nassign=%ld | pos=%ld\n", l, p, na, start[p]);
+      if (na == 0) {
+        fprintf(stderr, "# Problem2: no enough vectors in a node\n");
+        exit(1);
+      }
+      if (na < bf) {
+        set_error(E_ARG, "hkm: node %ld of level %d has %ld points < bf=%d (kmeans asserts k <= n)",
+                  p, l, na, bf);
+        return E_ARG;
+      }
+      Instance &x = E.in[p];
+      x.p0 = start[p];
+      x.n = (int)na;
+      x.seed = (unsigned)lrand48();  // kmeans(..., seed 0, ...) per child, in parent order
+    }
+    YG_CHECK(E.setup());
+    YG_CHECK(E.init_random());
+    for (auto &x : E.in) x.core = rand_r(&x.seed);
+    YG_CHECK(E.set_active());
+    while (!E.all_done()) YG_CHECK(E.iterate());
+    for (auto &x : E.in) iters += x.iters;
+    // centroids of this level, then node = node * bf + child
+    YG_CUDA(cudaMemcpyAsync(levels_out[l], E.C, sizeof(float) * (size_t)k * bf * d,
+                            cudaMemcpyDeviceToHost, st));
+    node_update_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(sorted, E.assign, n, bf, node);
+    YG_LAUNCH_CHECK();
+    YG_CUDA(cudaMemcpyAsync(hnode.data(), node, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    k *= bf;
+  }
+  cudaEventRecord(t1, st);
+  YG_CUDA(cudaStreamSynchronize(st));
+  if (ms_out) cudaEventElapsedTime(ms_out, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (assign_out) memcpy(assign_out, hnode.data(), sizeof(int) * n);
+  if (iters_out) *iters_out = iters;
+  return OK;
+}
+
+// greedy descent (yael/hkm.c:131-150) with exact L2 (FP32 + FP64 near ties)
+__global__ void hkm_quantize_kernel(const float *cent, int nlevel, int bf, int d, long n,
+                                    const float *v, int *idx) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *x = v + i * d;
+  const float rho = (float)(d + 4) * 5.9604645e-08f;
+  long vw = 0, off = 0, k = bf;
+  for (int l = 0; l < nlevel; l++) {
+    const float *C = cent + off + vw * (long)bf * d;
+    float b1 = 1e30f, b2 = 1e30f;
+    int i1 = -1;
+    for (int j = 0; j < bf; j++) {
+      float s = 0.f;
+      for (int c = 0; c < d; c++) {
+        const float t = x[c] - C[(long)j * d + c];
+        s = fmaf(t, t, s);
+      }
+      if (s < b1) { b2 = b1; b1 = s; i1 = j; } else if (s < b2) { b2 = s; }
+    }
+    if (i1 >= 0 && b2 < 1e30f && b2 - b1 <= rho * (b1 + b2)) {
+      double best = INFINITY;
+      for (int j = 0; j < bf; j++) {
+        double s = 0;
+        for (int c = 0; c < d; c++) {
+          const double t = (double)x[c] - (double)C[(long)j * d + c];
+          s += t * t;
+        }
+        if (s < best) { best = s; i1 = j; }
+      }
+    }
+    vw = vw * bf + (i1 < 0 ? 0 : i1);
+    off += k * d;
+    k *= bf;
+  }
+  idx[i] = (int)vw;
+}
+
+int hkm_quantize_run(int nlevel, int bf, int d, float *const *levels, int n, const float *v,
+                     int *idx) {
+  if (n <= 0) return OK;
+  Ctx *ctx;
+  YG_CHECK(ctx_get(&ctx));
+  cudaStream_t st = ctx->stream;
+  long tot = 0, k = bf;
+  for (int l = 0; l < nlevel; l++, k *= bf) tot += k * d;
+  float *dc, *dv;
+  int *di;
+  YG_CHECK(ws_get(ctx->ws, KS_BEST_C, (size_t)tot, &dc));
+  YG_CHECK(ws_get(ctx->ws, KS_V, (size_t)n * d, &dv));
+  YG_CHECK(ws_get(ctx->ws, KS_ASSIGN, (size_t)n, &di));
+  k = bf;
+  long off = 0;
+  for (int l = 0; l < nlevel; l++, k *= bf) {
+    YG_CUDA(cudaMemcpyAsync(dc + off, levels[l], sizeof(float) * k * d, cudaMemcpyHostToDevice, st));
+    off += k * d;
+  }
+  YG_CUDA(cudaMemcpyAsync(dv, v, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
+  hkm_quantize_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(dc, nlevel, bf, d, n, dv, di);
+  YG_LAUNCH_CHECK();
+  YG_CUDA(cudaMemcpyAsync(idx, di, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  YG_CUDA(cudaStreamSynchronize(st));
+  return OK;
+}
+
+}  // namespace yg
+
+using namespace yg;
+
+static hkm_t *hkm_alloc(int d, int nlevel, int bf) {
+  hkm_t *h = (hkm_t *)malloc(sizeof(hkm_t));
+  h->nlevel = nlevel;
+  h->bf = bf;
+  h->d = d;
+  h->centroids = (float **)malloc(sizeof(float *) * nlevel);
+  long k = 1;
+  for (int l = 0; l < nlevel; l++) {
+    h->centroids[l] = (float *)malloc(sizeof(float) * k * bf * d);
+    k *= bf;
+  }
+  h->k = (int)k;
+  return h;
+}
+
+extern "C" {
+
+float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int flags, long seed,
+                         int redo, float *centroids, float *dis, int *assign, int *nassign,
+                         yael_gpu_kmeans_opts *opts) {
+  int prec = default_precision();
+  bool dev = false;
+  cudaStream_t st = nullptr;
+  if (opts) {
+    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16)
+      prec = opts->precision;
+    dev = opts->device_ptrs != 0;
+    st = (cudaStream_t)opts->stream;
+  }
+  float ret = -1;
+  long iters = 0, fb = 0;
+  float ma = 0, mu = 0;
+  const int rc = kmeans_run(d, n, k, niter, v, flags, seed, redo, centroids, dis, assign,
+                            nassign, prec, dev, st, &ret, &iters, &fb, &ma, &mu);
+  if (opts) {
+    opts->status = rc;
+    opts->iterations = iters;
+    opts->n_fallback = fb;
+    opts->ms_assign = ma;
+    opts->ms_update = mu;
+  }
+  if (rc != OK) return -2.f;
+  return ret;
+}
+
+float kmeans(int d, int n, int k, int niter, const float *v, int flags, long seed, int redo,
+             float *centroids, float *dis, int *assign, int *nassign) {
+  float ret = -1;
+  if (kmeans_run(d, n, k, niter, v, flags, seed, redo, centroids, dis, assign, nassign,
+                 default_precision(), false, nullptr, &ret, nullptr, nullptr, nullptr,
+                 nullptr) != OK)
+    fatal_last("kmeans");
+  return ret;
+}
+
+float *clustering_kmeans_assign_with_score(int n, int d, const float *points, int k,
+                                           int nb_iter_max, double normalize, int n_thread,
+                                           double *score_out, int **clust_assign_out) {
+  (void)normalize;
+  (void)score_out;  // never written by the reference either (yael/kmeans.c:452-482)
+  float *centroids = (float *)malloc(sizeof(float) * (size_t)k * d);
+  int *ca = clust_assign_out ? (int *)malloc(sizeof(int) * (size_t)n) : nullptr;
+  int nredo = 1;
+  if (nb_iter_max / 100000 != 0) {
+    nredo = nb_iter_max / 100000;
+    nb_iter_max = nb_iter_max % 100000;
+  }
+  const float ret = kmeans(d, n, k, nb_iter_max, points, n_thread | YAEL_KMEANS_INIT_RANDOM, 0,
+                           nredo, centroids, nullptr, ca, nullptr);
+  if (ret >= 0) {
+    if (clust_assign_out) *clust_assign_out = ca;
+    return centroids;
+  }
+  free(centroids);
+  free(ca);
+  if (clust_assign_out) *clust_assign_out = nullptr;
+  return nullptr;
+}
+
+float *clustering_kmeans_assign(int n, int d, const float *points, int k, int nb_iter_max,
+                                double normalize, int **clust_assign_out) {
+  return clustering_kmeans_assign_with_score(n, d, points, k, nb_iter_max, normalize, 1,
+                                             nullptr, clust_assign_out);
+}
+
+float *clustering_kmeans(int n, int d, const float *points, int k, int nb_iter_max,
+                         double normalize) {
+  int *ca = nullptr;
+  float *c = clustering_kmeans_assign_with_score(n, d, points, k, nb_iter_max, normalize, 1,
+                                                 nullptr, &ca);
+  free(ca);
+  return c;
+}
+
+hkm_t *hkm_learn(int n, int d, int nlevel, int bf, const float *v, int nb_iter_max, int nt,
+                 int verbose, int **clust_assign_out) {
+  (void)nt;  // the reference ignores it too (hkm.c:85)
+  hkm_t *h = hkm_alloc(d, nlevel, bf);
+  int *assign = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  if (hkm_run(n, d, nlevel, bf, v, nb_iter_max, verbose != 0, default_precision(),
+              h->centroids, assign, nullptr, nullptr) != OK)
+    fatal_last("hkm_learn");
+  if (clust_assign_out) *clust_assign_out = assign;
+  else free(assign);
+  return h;
+}
+
+int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v, int nb_iter_max,
+                          float *centroids, int *assign, long *iterations, float *ms) {
+  std::vector<float *> lv(nlevel);
+  long k = bf, off = 0;
+  for (int l = 0; l < nlevel; l++, k *= bf) {
+    lv[l] = centroids + off;
+    off += k * d;
+  }
+  return hkm_run(n, d, nlevel, bf, v, nb_iter_max, false, default_precision(), lv.data(), assign,
+                 iterations, ms);
+}
+
+void hkm_delete(hkm_t *hkm) {
+  for (int l = 0; l < hkm->nlevel; l++) free(hkm->centroids[l]);
+  free(hkm->centroids);
+  free(hkm);
+}
+
+void hkm_quantize(const hkm_t *hkm, int npt, const float *v, int *idx) {
+  if (hkm_quantize_run(hkm->nlevel, hkm->bf, hkm->d, hkm->centroids, npt, v, idx) != OK)
+    fatal_last("hkm_quantize");
+}
+
+float *hkm_get_centroids(const hkm_t *hkm, int l, int no) {
+  return hkm->centroids[l] + (long)hkm->d * hkm->bf * no;
+}
+
+// file format of yael/hkm.c:181-232: int nlevel, bf, d, then per level one
+// fvec record (int count, count floats) of bf^(l+1) * d centroids
+void hkm_write(const char *filename, const hkm_t *hkm) {
+  FILE *f = fopen(filename, "w");
+  if (!f) {
+    fprintf(stderr, "# Unable to write the hkm file %s\n", filename);
+    return;
+  }
+  if (fwrite(&hkm->nlevel, sizeof(int), 1, f) != 1 || fwrite(&hkm->bf, sizeof(int), 1, f) != 1 ||
+      fwrite(&hkm->d, sizeof(int), 1, f) != 1) {
+    fprintf(stderr, "# Unable to write the hkm file %s\n", filename);
+    fclose(f);
+    return;
+  }
+  long k = hkm->bf;
+  for (int l = 0; l < hkm->nlevel; l++, k *= hkm->bf) {
+    const int cnt = (int)(k * hkm->d);
+    if (fwrite(&cnt, sizeof(int), 1, f) != 1 ||
+        fwrite(hkm->centroids[l], sizeof(float), cnt, f) != (size_t)cnt)
+      perror("fvec_fwrite: write error");
+  }
+  fclose(f);
+}
+
+hkm_t *hkm_read(const char *filename) {
+  FILE *f = fopen(filename, "r");
+  int nlevel, bf, d;
+  if (!f || fread(&nlevel, sizeof(int), 1, f) != 1 || fread(&bf, sizeof(int), 1, f) != 1 ||
+      fread(&d, sizeof(int), 1, f) != 1 || nlevel < 1 || bf < 1 || d < 1) {
+    fprintf(stderr, "# Unable to read the hkm file %s\n", filename);
+    if (f) fclose(f);
+    return nullptr;
+  }
+  hkm_t *h = hkm_alloc(d, nlevel, bf);
+  long k = bf;
+  for (int l = 0; l < nlevel; l++, k *= bf) {
+    int cnt = 0;
+    if (fread(&cnt, sizeof(int), 1, f) != 1 || cnt != k * d ||
+        fread(h->centroids[l], sizeof(float), cnt, f) != (size_t)cnt) {
+      fprintf(stderr, "# Unable to read the hkm file %s\n", filename);
+      hkm_delete(h);
+      fclose(f);
+      return nullptr;
+    }
+  }
+  fclose(f);
+  return h;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// Device kernels of the k-means Lloyd step (yael/kmeans.c:213-329), written for
+// many independent instances at once (hierarchical k-means runs every child
+// clustering of a level together).  Instance i owns points [p0_i, p0_i + n_i)
+// of one contiguous point array and centroids [i*k, (i+1)*k) of one centroid
+// array; global cluster id = i*k + local id.
+#pragma once
+#include "common.cuh"
+
+namespace yg {
+
+struct KmWork {      // one block of the grouped assignment kernel
+  int inst;          // instance
+  long p0;           // first point (global index)
+  int n;             // points in this block (<= kAssignChunk)
+};
+constexpr int kAssignChunk = 1024;
+constexpr int kSmallK = 64;  // largest k of the direct grouped assignment
+
+// assign[p] = local argmin_j ||v_p - C_{inst,j}||^2 (ties to the lowest j),
+// dis[p] = that distance.  FP32 direct differences; when the two best are
+// closer than their rounding bound all k are recomputed in FP64.  Points with
+// a NaN distance everywhere get assign -1, dis 1e30 (yael/nn.c:404-407).
+// active[inst] == 0 skips the instance.
+int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const float *C,
+                    int k, const unsigned char *active, int *assign, float *dis,
+                    cudaStream_t st);
+
+// counts[inst*k + assign[p]]++ over points of active instances
+int km_histogram(const int *assign, const int *pinst, long n, int k,
+                 const unsigned char *active, int *counts, cudaStream_t st);
+
+// exclusive scan of counts -> offs (ncl + 1 entries, offs[ncl] = total),
+// cursor = offs
+int km_scan(const int *counts, long ncl, long *offs, long *cursor, cudaStream_t st);
+
+// perm[cursor[g]++] = p  (order inside a cluster is arbitrary; the sums below
+// are exact integers, so the result does not depend on it)
+int km_scatter(const int *assign, const int *pinst, long n, int k,
+               const unsigned char *active, long *cursor, long *perm, cudaStream_t st);
+
+// acc[g][c] = sum over the cluster's points of llrint(v * 2^shift[inst]),
+// then C[g][c] = (float)((double)acc * 2^-shift * (1.0 / count)).  Clusters
+// with count 0 become NaN (0 * inf), as in the reference before the split.
+// perm holds the *total cluster-sorted points (km_scatter); nmax bounds it.
+int km_update(const long *perm, const long *total, long nmax, const int *assign,
+              const int *pinst, const int *counts, const float *v, int d, long ncl, int k,
+              const int *shift, const unsigned char *active, long long *acc, float *C,
+              cudaStream_t st);
+
+// rows of C scaled to unit L2 norm (yael/vector.c:2016-2025 arithmetic)
+int km_normalize(float *C, long ncl, int d, int k, const unsigned char *active,
+                 cudaStream_t st);
+
+// fixed slices of one instance's points (<= kSliceLen each): the unit of the
+// deterministic objective sums and of the per-instance max |v|
+struct KmSlice {
+  long p0;
+  int n;
+  int inst;
+};
+constexpr int kSliceLen = 4096;
+int km_slice_sums(const KmSlice *sl, int nsl, const float *dis, double *out, cudaStream_t st);
+
+// out[inst] = max |v| over the instance's slices (out zeroed by the caller)
+int km_absmax(const KmSlice *sl, int nsl, const float *v, int d, float *out, cudaStream_t st);
+
+// C[i] = v[sel[i]] for rows of the listed instances
+int km_gather(const float *v, int d, const long *rows, long nrows, float *C, cudaStream_t st);
+
+}  // namespace yg

@@ -4,6 +4,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <memory>
 
 #include "knn.cuh"
@@ -287,9 +288,23 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   const int bexact = hs.bs.all_exact;
   job.exact_class = bexact;
 
-  // query batches bounded by the candidate buffers (<= 1 GiB)
-  const size_t per_query = (size_t)kMaxCandidates * 8 + 64;
-  int qbatch = (int)imin(nq, (int)imax(256, (int)(((size_t)1 << 30) / per_query)));
+  // query batches bounded by the candidate buffers (<= 2 GiB)
+  size_t per_query;
+  {
+    const int cn = bexact ? k : 2 * k;
+    const bool bf16 = job.prec == PREC_BF16;
+    const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N, tile_m = bf16 ? TC_TILE_M : 128;
+    const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
+    int C = 1;
+    while (C < cn) C <<= 1;
+    if (cn <= 16) {
+      int nch = imin(choose_chunks(nqt, ntb, ctx->num_sms, 1, 4), kMaxCandidates / C);
+      per_query = (size_t)nch * C * 8 + 64;
+    } else {
+      per_query = (size_t)2 * kMaxCandidates * 8 + 64;
+    }
+  }
+  int qbatch = (int)std::min<size_t>((size_t)nq, std::max<size_t>(256, ((size_t)2 << 30) / per_query));
   for (int q0 = 0; q0 < nq; q0 += qbatch) {
     KnnJob sub = job;
     sub.nq = imin(qbatch, nq - q0);

@@ -269,6 +269,132 @@ failed:
   }
 }
 
+// ---- warp-per-query variant for short TOPC lists (nchunk * C <= 32) -------
+
+__device__ __forceinline__ void warp_sort(unsigned long long &key, int &id) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      const unsigned long long pk = __shfl_xor_sync(0xffffffffu, key, stride);
+      const int pi = __shfl_xor_sync(0xffffffffu, id, stride);
+      const bool up = (lane & size) == 0 || size == 32;
+      const bool lower = (lane & stride) == 0;
+      const bool pless = lex_less(pk, pi, key, id);
+      const bool take = (lower == up) ? pless : (!pless && (pk != key || pi != id));
+      if (take) { key = pk; id = pi; }
+    }
+  }
+}
+
+__device__ __forceinline__ double ord2d(unsigned long long k) {
+  const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+__global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (q >= a.nq) return;  // uniform per warp
+  const ScanSel &s = a.sel;
+  const int M = s.nchunk * s.C, k = a.k, d = a.d;
+  const bool L2 = a.metric == METRIC_L2;
+  const double qn = L2 ? a.qn64[q] : 0.0;
+  const float eps = a.eps ? a.eps[q] : 0.f;
+  const bool ex = a.qexact ? a.qexact[q] != 0 : false;
+  const float *qv = a.q + (long)q * a.ldq;
+
+  unsigned long long key = ~0ull, tkey = ~0ull;
+  int id = 0x7fffffff;
+  if (lane < M) {
+    const int ch = lane / s.C, sl = lane - ch * s.C;
+    const long o = ((long)ch * a.nq + q) * s.C + sl;
+    const int j = s.topi[o];
+    if (j >= 0) {
+      const float v = s.topv[o];
+      const float av = L2 ? (float)((double)v + qn) : v;
+      key = f2ord(av);
+      id = j;
+      if (sl == s.C - 1) tkey = ((unsigned long long)f2ord(av) << 32) | (unsigned)j;
+    }
+  }
+  // boundary: smallest (value, id) that closes a full chunk list
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, tkey, o);
+    tkey = t < tkey ? t : tkey;
+  }
+  const int nvalid = __popc(__ballot_sync(0xffffffffu, id != 0x7fffffff));
+  bool ok = nvalid >= k;
+  if (ok) {
+    if (a.n_cand && lane == 0) atomicAdd(a.n_cand, (unsigned long long)nvalid);
+    warp_sort(key, id);
+    if (ex) {
+      if (tkey != ~0ull) {
+        const unsigned long long kk = __shfl_sync(0xffffffffu, key, k - 1);
+        const int ik = __shfl_sync(0xffffffffu, id, k - 1);
+        const unsigned long long tk = tkey >> 32;
+        const unsigned tid_b = (unsigned)(tkey & 0xffffffffu);
+        ok = kk < tk || (kk == tk && (unsigned)ik <= tid_b);
+      }
+      if (ok && lane < k) {
+        a.out_idx[(long)q * k + lane] = id;
+        a.out_dis[(long)q * k + lane] = ord2f((unsigned)key);
+      }
+    } else {
+      const float ak = ord2f((unsigned)__shfl_sync(0xffffffffu, key, k - 1));
+      const double lim = (double)ak + 2.0 * (double)eps + 4e-7 * fabs((double)ak) + 1e-30;
+      const bool inband = id != 0x7fffffff && (double)ord2f((unsigned)key) <= lim;
+      const int nband = __popc(__ballot_sync(0xffffffffu, inband));
+      // FP32 re-rank of the band, one candidate at a time across the warp
+      float e = INFINITY;
+      for (int c = 0; c < nband; c++) {
+        const int cid = __shfl_sync(0xffffffffu, id, c);
+        const float ec = warp_dist32(qv, a.b + (long)cid * a.ldb, d, a.metric);
+        if (lane == c) e = ec;
+      }
+      key = lane < nband ? (unsigned long long)f2ord(e) : ~0ull;
+      if (lane >= nband) id = 0x7fffffff;
+      warp_sort(key, id);
+      const float rho = (float)(d + 4) * kU;
+      float eta = 0.f;
+      if (!L2) eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64[q], 0.0)) *
+                     __uint_as_float(a.bstats->max_norm_bits);
+      const float e0 = ord2f((unsigned)key);
+      const float e1 = ord2f((unsigned)__shfl_down_sync(0xffffffffu, key, 1));
+      const bool tie = lane < imin(k, nband - 1) && (e1 - e0 <= rho * (fabsf(e0) + fabsf(e1)) + 2.f * eta);
+      double ek_hi;
+      if (__any_sync(0xffffffffu, tie)) {
+        // FP64, sequential over coordinates, for the whole band
+        unsigned long long k64 = ~0ull;
+        if (lane < nband) k64 = d2ord(dist64_seq(qv, a.b + (long)id * a.ldb, d, a.metric));
+        key = k64;
+        warp_sort(key, id);
+        const double ek = ord2d(__shfl_sync(0xffffffffu, key, k - 1));
+        ek_hi = ek + 1e-12 * fabs(ek);
+        if (lane < k) {
+          a.out_idx[(long)q * k + lane] = id;
+          a.out_dis[(long)q * k + lane] = (float)ord2d(key);
+        }
+      } else {
+        const float ek = ord2f((unsigned)__shfl_sync(0xffffffffu, key, k - 1));
+        ek_hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
+        if (lane < k) {
+          a.out_idx[(long)q * k + lane] = id;
+          a.out_dis[(long)q * k + lane] = ord2f((unsigned)key);
+        }
+      }
+      const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
+      ok = ek_hi < bound - (double)eps - 4e-7 * fabs(bound);
+    }
+  }
+  if (!ok && lane == 0) {
+    const int pos = atomicAdd(a.fail_cnt, 1);
+    a.fail_list[pos] = q;
+  }
+}
+
 __global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn64,
                            const float *qres, const unsigned char *qflag,
                            const SetStats *bs, float *eps, unsigned char *qexact) {
@@ -461,6 +587,11 @@ __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0,
 
 int rerank(const RerankArgs &a, cudaStream_t st) {
   if (a.nq <= 0) return OK;
+  if (a.sel.mode == SCAN_TOPC && a.sel.nchunk * a.sel.C <= 32) {
+    rerank_small_kernel<<<(unsigned)ceil_div(a.nq, 8), 256, 0, st>>>(a);
+    YG_LAUNCH_CHECK();
+    return OK;
+  }
   int Mmax = a.sel.mode == SCAN_TOPC ? a.sel.nchunk * a.sel.C : a.sel.nregion() * a.sel.cap;
   if (Mmax > kMaxCandidates) Mmax = kMaxCandidates;  // more candidates than this fail the query
   int Mp = 1;
