@@ -404,7 +404,9 @@ __global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn
   qexact[q] = ex;
   if (ex) { eps[q] = 0.f; return; }
   const double u = 5.9604644775390625e-08;  // 2^-24
-  const double qn = sqrt(fmax(qn64[q], 0.0)) * (1 + 1e-6);
+  // norms are FP32 sums: relative error <= (d/32 + 6) u, on both sides
+  const double un = ((d + 31) / 32 + 6) * u;
+  const double qn = sqrt(fmax(qn64[q], 0.0)) * (1 + 1e-5);
   const double B = (double)__uint_as_float(bs->max_norm_bits);
   double e;
   if (prec == PREC_FP32) {
@@ -420,6 +422,8 @@ __global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn
                                      (metric == METRIC_L2 ? 1.001 * B * B : 0.0));
     e = metric == METRIC_L2 ? 2 * dot + u * B * B + acc : dot + acc;
   }
+  // ||q||^2 (added in the re-rank) and ||b||^2 (inside v) each off by un relative
+  e += un * (qn * qn + B * B);
   e = e * 1.1 + 1e-30;
   eps[q] = isfinite(e) ? (float)e : INFINITY;
 }
