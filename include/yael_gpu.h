@@ -236,6 +236,26 @@ int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v,
                           int nb_iter_max, float *centroids, int *assign,
                           long *iterations, float *ms);
 
+/* Exact k-NN that allocates no GPU memory.  No counterpart in the reference:
+ * it exists for callers that cannot let a library call cudaMalloc -- a
+ * process whose device memory is all handed to its own pool allocator, or a
+ * latency-critical path where cudaMalloc / cudaFree would synchronise the
+ * device.  Same results as yael_gpu_knn_ex with the FP32 pass (L2, ids ordered
+ * by distance then index).  b (nb x d), q (nq x d), assign and dis (nq x k)
+ * are device pointers; the work is ordered on stream (a cudaStream_t, NULL =
+ * the default stream) and the call returns when it is complete.
+ * Scratch comes from one 32 MiB __device__ array that the library holds on
+ * every GPU that loads it.  Limits: k <= 16, and the scratch must fit (about
+ * 12 bytes per base row plus 8 C + 24 bytes per query, C the smallest power
+ * of two >= 2k; e.g. nb = 1M with nq = 20k at k = 10); larger requests
+ * return YAEL_GPU_EARG with the size in yael_gpu_last_error() -- use
+ * yael_gpu_knn_ex for them.  The first call on a device looks up the array's
+ * device address (make that first call before any stream capture).  All
+ * calls share the array: calls whose GPU work overlaps race and must be
+ * serialised by the caller. */
+int yael_gpu_knn_noalloc(int nq, int nb, int d, int k, const float *b, const float *q,
+                         int *assign, float *dis, void *stream);
+
 /* message of the last failure on the calling thread ("" if none) */
 const char *yael_gpu_last_error(void);
 

@@ -89,6 +89,7 @@ SIGNATURES = {
     "hkm_get_centroids": (P, [P, c_int, c_int]),
     "yael_gpu_kmeans_ex": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P, ctypes.c_void_p]),
     "yael_gpu_hkm_learn_ex": (c_int, [c_int, c_int, c_int, c_int, P, c_int, P, P, P, P]),
+    "yael_gpu_knn_noalloc": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, P]),
     "yael_gpu_version": (c_int, []),
     "yael_gpu_launch_count": (c_long, []),
 }
