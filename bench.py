@@ -152,6 +152,122 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+CLUSTER_CFG = {
+    # n, d, k, niter, seed, data
+    "kmeans1": dict(n=100_000, d=128, k=256, niter=20, seed=0, comps=256, sigma=0.15, zipf=None),
+    "kmeans3": dict(n=10_000_000, d=128, k=65536, niter=10, seed=1, comps=65536, sigma=0.2,
+                    zipf=1.1),
+    "hkm4": dict(n=2_000_000, d=96, bf=32, nlevel=3, niter=15, comps=4096, sigma=0.1),
+}
+
+
+def run_clustering(args, world, rank, local):
+    """k-means / hkm configurations: iterations per second on GB300, the plain
+    FP32 assignment beside the BF16+re-rank one, the reference algorithm
+    (oracle port) on the host cores for a bounded sample."""
+    import torch
+    import yael_gb300 as yg
+    from yael_gb300 import synth
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _util import oracle, ptr
+    torch.cuda.set_device(local)
+    L = yg.lib()
+    c = CLUSTER_CFG[args.workload]
+    w = synth.zipf_weights(c["comps"], c["zipf"]) if c.get("zipf") else None
+    v_h, _, _ = synth.gaussian_mixture(c["n"], c["d"], c["comps"], c["sigma"], seed=11, weights=w)
+    n, d = v_h.shape
+    line = {"metric": METRIC, "unit": "iterations/s", "n_gpus": world, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic", "dtype": args.prec}
+    if args.workload.startswith("kmeans"):
+        k, niter, seed = c["k"], c["niter"], c["seed"]
+        dv = torch.from_numpy(v_h).cuda()
+        C = torch.empty((k, d), device="cuda")
+        dis = torch.empty(n, device="cuda")
+        assign = torch.empty(n, dtype=torch.int32, device="cuda")
+        flags = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
+
+        def run(prec):
+            o = yg.KmeansOpts(prec, 1, None, 0, 0, 0, 0, 0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            q = L.yael_gpu_kmeans_ex(d, n, k, niter, dv.data_ptr(), flags, seed, 1, C.data_ptr(),
+                                     dis.data_ptr(), assign.data_ptr(), None, ctypes.byref(o))
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            assert o.status == 0, yg.last_error()
+            return q, dt, o
+
+        run(yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32)  # warm-up (and lrand48 draw)
+        prec = yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32
+        l0 = L.yael_gpu_launch_count()
+        q, dt, o = run(prec)
+        launches = L.yael_gpu_launch_count() - l0
+        a_bf = assign.cpu().numpy().copy()
+        q32, dt32, o32 = run(yg.PREC_FP32)
+        same_assign = bool((assign.cpu().numpy() == a_bf).all())
+        line.update({
+            "value": o.iterations / dt, "ms_per_step": 1e3 * dt / max(1, o.iterations),
+            "steps": int(o.iterations), "warmup": 1,
+            "config": {"workload": f"k-means n={n} d={d} k={k} niter={niter} seed={seed}, "
+                                   f"Gaussian mixture ({c['comps']} comps, sigma={c['sigma']}"
+                                   + (f", Zipf({c['zipf']}) weights" if c.get('zipf') else "")
+                                   + "), random init", "n": n, "d": d, "k": k},
+            "qerr": q, "assign_ms_per_iter": o.ms_assign / max(1, o.iterations),
+            "update_ms_per_iter": o.ms_update / max(1, o.iterations),
+            "fallback_points": int(o.n_fallback), "gpu_launches": launches,
+            "plain_fp32": {"value": o32.iterations / dt32, "qerr": q32,
+                           "assign_ms_per_iter": o32.ms_assign / max(1, o32.iterations),
+                           "same_assignments_as_bf16": same_assign},
+            "roofline": {"bound": "tensor", "kernel": "assignment pass",
+                         "achieved": 2.0 * n * k * d / (o.ms_assign / max(1, o.iterations) / 1e3) / 1e12,
+                         "unit": "TFLOP/s", "peak": peaks()[0], "peak_source": peaks()[2]},
+        })
+        line["roofline"]["frac"] = line["roofline"]["achieved"] / line["roofline"]["peak"]
+        if not args.no_cpu:
+            # reference algorithm (oracle port) on the host: whole run for the small
+            # configuration, one iteration on 1/100 of the points for the large one
+            nt = os.cpu_count() or 1
+            sub = v_h if n <= 200_000 else np.ascontiguousarray(v_h[: n // 100])
+            it = niter if n <= 200_000 else 1
+            Cc = np.zeros((k, d), np.float32)
+            t0 = time.perf_counter()
+            oracle().orc_kmeans(d, sub.shape[0], k, it, ptr(sub), nt | flags, 1234, 1, ptr(Cc),
+                                None, None, None, 0, None)
+            cdt = time.perf_counter() - t0
+            scale = sub.shape[0] / n
+            line["cpu_baseline"] = {"value": it * scale / cdt, "unit": "iterations/s",
+                                    "cores": nt, "kind": "port",
+                                    "sample": f"{it} iteration(s) on {sub.shape[0]} points "
+                                              f"(value scaled to the full n)"}
+    else:
+        nl, bf, niter = c["nlevel"], c["bf"], c["niter"]
+        cent = np.empty(sum(bf ** (l + 1) for l in range(nl)) * d, np.float32)
+        assign = np.empty(n, np.int32)
+        it, ms = ctypes.c_long(0), ctypes.c_float(0)
+        L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, ptr(cent), ptr(assign), None, None)
+        t0 = time.perf_counter()
+        rc = L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, ptr(cent), ptr(assign),
+                                     ctypes.byref(it), ctypes.byref(ms))
+        dt = time.perf_counter() - t0
+        assert rc == 0, yg.last_error()
+        line.update({"value": it.value / dt, "unit": "instance-iterations/s",
+                     "ms_per_step": 1e3 * dt, "steps": 1, "warmup": 1,
+                     "config": {"workload": f"hierarchical k-means n={n} d={d} bf={bf} "
+                                            f"nlevel={nl} niter={niter}", "n": n, "d": d},
+                     "hkm_seconds": dt, "gpu_ms": ms.value, "instance_iterations": it.value})
+        if not args.no_cpu:
+            nt = os.cpu_count() or 1
+            sub = np.ascontiguousarray(v_h[: n // 10])
+            oc = np.empty_like(cent)
+            t0 = time.perf_counter()
+            oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(oc), None, 0)
+            cdt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": None, "seconds_on_tenth": cdt, "cores": nt,
+                                    "kind": "port",
+                                    "sample": f"hkm_learn on n/10 = {sub.shape[0]} points"}
+    print(json.dumps(line), flush=True)
+
+
 def config_of(args):
     return {"workload": f"exact kNN L2, SIFT-like float32 (30% zeros, floor|N(0,40)| clipped "
                         f"to 255), nb={args.nb}, nq={args.nq}, d={args.d}, k={args.k}",
@@ -177,8 +293,14 @@ def main():
     ap.add_argument("--ref-queries", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the FP64 spot check")
+    ap.add_argument("--workload", default="knn", choices=["knn", "kmeans1", "kmeans3", "hkm4"],
+                    help="knn: the headline configuration; the others are the k-means / hkm "
+                         "configurations, reported separately")
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.workload != "knn":
+        run_clustering(args, world, rank, local)
+        return
 
     if args.impl == "reference":
         run_reference(args, world, rank)
