@@ -172,7 +172,9 @@ def run_clustering(args, world, rank, local):
     from _util import oracle, ptr
     torch.cuda.set_device(local)
     L = yg.lib()
-    c = CLUSTER_CFG[args.workload]
+    c = dict(CLUSTER_CFG[args.workload])
+    if args.niter:
+        c["niter"] = args.niter
     w = synth.zipf_weights(c["comps"], c["zipf"]) if c.get("zipf") else None
     v_h, _, _ = synth.gaussian_mixture(c["n"], c["d"], c["comps"], c["sigma"], seed=11, weights=w)
     n, d = v_h.shape
@@ -187,7 +189,7 @@ def run_clustering(args, world, rank, local):
         flags = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
 
         def run(prec):
-            o = yg.KmeansOpts(prec, 1, None, 0, 0, 0, 0, 0)
+            o = yg.KmeansOpts(prec, 1, None, 0, 0, 0, 0, 0, 0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             q = L.yael_gpu_kmeans_ex(d, n, k, niter, dv.data_ptr(), flags, seed, 1, C.data_ptr(),
@@ -214,7 +216,8 @@ def run_clustering(args, world, rank, local):
                                    + "), random init", "n": n, "d": d, "k": k},
             "qerr": q, "assign_ms_per_iter": o.ms_assign / max(1, o.iterations),
             "update_ms_per_iter": o.ms_update / max(1, o.iterations),
-            "fallback_points": int(o.n_fallback), "gpu_launches": launches,
+            "fallback_points": int(o.n_fallback), "second_pass_points": int(o.n_second),
+            "gpu_launches": launches,
             "plain_fp32": {"value": o32.iterations / dt32, "qerr": q32,
                            "assign_ms_per_iter": o32.ms_assign / max(1, o32.iterations),
                            "same_assignments_as_bf16": same_assign},
@@ -244,9 +247,10 @@ def run_clustering(args, world, rank, local):
         cent = np.empty(sum(bf ** (l + 1) for l in range(nl)) * d, np.float32)
         assign = np.empty(n, np.int32)
         it, ms = ctypes.c_long(0), ctypes.c_float(0)
-        L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, ptr(cent), ptr(assign), None, None)
+        L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, 1, ptr(cent), ptr(assign), None,
+                                None)
         t0 = time.perf_counter()
-        rc = L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, ptr(cent), ptr(assign),
+        rc = L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, 1, ptr(cent), ptr(assign),
                                      ctypes.byref(it), ctypes.byref(ms))
         dt = time.perf_counter() - t0
         assert rc == 0, yg.last_error()
@@ -293,6 +297,7 @@ def main():
     ap.add_argument("--ref-queries", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the FP64 spot check")
+    ap.add_argument("--niter", type=int, default=0, help="override the clustering iterations")
     ap.add_argument("--workload", default="knn", choices=["knn", "kmeans1", "kmeans3", "hkm4"],
                     help="knn: the headline configuration; the others are the k-means / hkm "
                          "configurations, reported separately")
@@ -328,7 +333,7 @@ def main():
     prec = {"bf16": yg.PREC_BF16, "fp32": yg.PREC_FP32}[args.prec]
 
     def step(p, timing=1):
-        o = yg.KnnOpts(p, 2, 1, ctypes.c_void_p(stream.cuda_stream), 0, 0, 0, timing, 0, 0, 0, 0)
+        o = yg.KnnOpts(p, 2, 1, ctypes.c_void_p(stream.cuda_stream), 0, 0, 0, timing, 0, 0, 0, 0, 0)
         rc = L.yael_gpu_knn_ex(args.nq, args.nb, args.d, args.k, b.data_ptr(), q.data_ptr(),
                                idx.data_ptr(), dis.data_ptr(), ctypes.byref(o))
         if rc != 0:

@@ -206,6 +206,7 @@ typedef struct {
   float ms_sample;  /* threshold-estimation pass over the base sample */
   float ms_rerank;  /* re-rank + certificate */
   int scan_launches; /* launches of the main pass included in ms_scan */
+  int n_second;     /* BF16-rejected queries settled by the FP32 pass (before any fallback) */
 } yael_gpu_knn_opts;
 
 /* k-NN with explicit options.  Same result contract as knn_full. */
@@ -219,7 +220,8 @@ typedef struct {
   /* filled on return */
   int status;      /* YAEL_GPU_OK or an error code (then the return value is -2) */
   long iterations; /* total Lloyd iterations over all runs */
-  long n_fallback; /* points whose assignment certificate failed (recomputed exhaustively) */
+  long n_fallback; /* points recomputed by the exhaustive FP64 path */
+  long n_second;   /* points the BF16 pass could not certify, settled by the FP32 pass */
   float ms_assign; /* GPU time of the assignment steps */
   float ms_update; /* GPU time of counts, sums, splits' uploads and objective */
 } yael_gpu_kmeans_opts;
@@ -231,9 +233,13 @@ float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int fla
 
 /* hkm_learn() with flat outputs: centroids = all levels concatenated
  * (sum_l bf^(l+1) * d floats), assign (n ints, may be NULL).  Returns a status
- * code; iterations and ms (GPU time) may be NULL. */
+ * code; iterations and ms (GPU time) may be NULL.
+ * small_nodes = 0: a node with fewer points than bf is an error, as in the
+ * reference (its kmeans asserts k <= n).  small_nodes = 1: such a node gets one
+ * child per point (children past the last point repeat it) without k-means;
+ * its lrand48() draw is still made so later seeds stay in step. */
 int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v,
-                          int nb_iter_max, float *centroids, int *assign,
+                          int nb_iter_max, int small_nodes, float *centroids, int *assign,
                           long *iterations, float *ms);
 
 /* Exact k-NN that allocates no GPU memory.  No counterpart in the reference:

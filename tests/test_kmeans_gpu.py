@@ -38,7 +38,7 @@ def gpu_kmeans(v, k, niter, flags, seed, redo, prec, C0=None):
     dis = np.empty(n, np.float32)
     assign = np.empty(n, np.int32)
     nassign = np.empty(k, np.int32)
-    o = yg.KmeansOpts({"fp32": 0, "bf16": 1}[prec], 0, None, 0, 0, 0, 0, 0)
+    o = yg.KmeansOpts({"fp32": 0, "bf16": 1}[prec], 0, None, 0, 0, 0, 0, 0, 0)
     q = yg.lib().yael_gpu_kmeans_ex(d, n, k, niter, ptr(v), flags, seed, redo, ptr(C), ptr(dis),
                                     ptr(assign), ptr(nassign), ctypes.byref(o))
     assert o.status == 0, yg.last_error()

@@ -39,7 +39,8 @@ PREC_ENV, PREC_FP32, PREC_BF16 = -1, 0, 1
 
 class KmeansOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("device_ptrs", c_int), ("stream", P), ("status", c_int),
-                ("iterations", c_long), ("n_fallback", c_long), ("ms_assign", c_float),
+                ("iterations", c_long), ("n_fallback", c_long), ("n_second", c_long),
+                ("ms_assign", c_float),
                 ("ms_update", c_float)]
 
 
@@ -52,7 +53,8 @@ class KnnOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("metric", c_int), ("device_ptrs", c_int),
                 ("stream", P), ("n_fallback", c_int), ("n_candidates", c_int),
                 ("exact_class", c_int), ("timing", c_int), ("ms_scan", c_float),
-                ("ms_sample", c_float), ("ms_rerank", c_float), ("scan_launches", c_int)]
+                ("ms_sample", c_float), ("ms_rerank", c_float), ("scan_launches", c_int),
+                ("n_second", c_int)]
 
 
 # name -> (restype, argtypes); every symbol of include/yael_gpu.h
@@ -88,7 +90,7 @@ SIGNATURES = {
     "hkm_read": (P, [ctypes.c_char_p]),
     "hkm_get_centroids": (P, [P, c_int, c_int]),
     "yael_gpu_kmeans_ex": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P, ctypes.c_void_p]),
-    "yael_gpu_hkm_learn_ex": (c_int, [c_int, c_int, c_int, c_int, P, c_int, P, P, P, P]),
+    "yael_gpu_hkm_learn_ex": (c_int, [c_int, c_int, c_int, c_int, P, c_int, c_int, P, P, P, P]),
     "yael_gpu_knn_noalloc": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, P]),
     "yael_gpu_version": (c_int, []),
     "yael_gpu_launch_count": (c_long, []),
@@ -148,7 +150,7 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
     idx = np.empty((nq, nnn), dtype=np.int32)
     dis = np.empty((nq, nnn), dtype=np.float32)
     prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
-    opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0)
+    opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     rc = lib().yael_gpu_knn_ex(nq, nb, d, nnn, _ptr(base), _ptr(queries), _ptr(idx), _ptr(dis),
                                ctypes.byref(opts))
     if rc != 0:
@@ -196,7 +198,7 @@ def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
     if normalize:
         flags |= KMEANS_NORMALIZE_CENTS
     prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
-    opts = KmeansOpts(prec, 0, None, 0, 0, 0, 0, 0)
+    opts = KmeansOpts(prec, 0, None, 0, 0, 0, 0, 0, 0)
     qerr = lib().yael_gpu_kmeans_ex(d, n, k, niter, _ptr(v), flags, seed, redo, _ptr(centroids),
                                     _ptr(dis), _ptr(assign), _ptr(nassign), ctypes.byref(opts))
     if opts.status != 0:
@@ -206,19 +208,20 @@ def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
     res = centroids if output == "centroids" else (centroids, qerr, dis, assign, nassign)
     if stats:
         return res, {"iterations": opts.iterations, "n_fallback": opts.n_fallback,
+                     "n_second": opts.n_second,
                      "ms_assign": opts.ms_assign, "ms_update": opts.ms_update}
     return res
 
 
-def hkm(v, nlevel, bf, niter=15):
+def hkm(v, nlevel, bf, niter=15, small_nodes=False):
     """Hierarchical k-means: (list of per-level centroid arrays, leaf assignment)."""
     v = _f32(v)
     n, d = v.shape
     sizes = [bf ** (l + 1) for l in range(nlevel)]
     cent = np.empty(sum(sizes) * d, dtype=np.float32)
     assign = np.empty(n, dtype=np.int32)
-    rc = lib().yael_gpu_hkm_learn_ex(n, d, nlevel, bf, _ptr(v), niter, _ptr(cent), _ptr(assign),
-                                     None, None)
+    rc = lib().yael_gpu_hkm_learn_ex(n, d, nlevel, bf, _ptr(v), niter, int(small_nodes),
+                                     _ptr(cent), _ptr(assign), None, None)
     if rc != 0:
         raise RuntimeError(f"hkm failed: {last_error()}")
     out, o = [], 0

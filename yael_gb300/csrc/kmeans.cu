@@ -155,7 +155,7 @@ struct Engine {
   std::vector<KmSlice> hsl;
   std::vector<int> hcounts;
   std::vector<double> hpart;
-  long n_fallback = 0;
+  long n_fallback = 0, n_second = 0;
   float ms_assign = 0, ms_update = 0;
 
   int setup() {
@@ -217,6 +217,10 @@ struct Engine {
     const int ni = (int)in.size();
     std::vector<long> hrows((size_t)ni * k);
     for (int i = 0; i < ni; i++) {
+      if (in[i].n < k) {  // a node too small for k clusters: one child per point
+        for (int j = 0; j < k; j++) hrows[(size_t)i * k + j] = in[i].p0 + std::min(j, in[i].n - 1);
+        continue;
+      }
       random_init_first_k(in[i].n, k, rand_r(&in[i].seed), hrows.data() + (size_t)i * k);
       for (int j = 0; j < k; j++) hrows[(size_t)i * k + j] += in[i].p0;
     }
@@ -244,6 +248,7 @@ struct Engine {
       job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
       YG_CHECK(knn_device(job, ctx, st));
       n_fallback += job.n_fallback;
+      n_second += job.n_second;
       return OK;
     }
     return km_assign_small(work, nwork, v, d, C, k, active, assign, dis, st);
@@ -405,7 +410,7 @@ int kmeanspp(Ctx *ctx, cudaStream_t st, const float *v, int d, int nsub, int k, 
 int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, long seed_in,
                int redo, float *C_out, float *dis_out, int *assign_out, int *nassign_out,
                int prec, bool dev, cudaStream_t st_in, float *ret_out, long *iters_out,
-               long *fallback_out, float *ms_assign, float *ms_update) {
+               long *fallback_out, long *second_out, float *ms_assign, float *ms_update) {
   Ctx *ctx;
   YG_CHECK(ctx_get(&ctx));
   cudaStream_t st = st_in ? st_in : ctx->stream;
@@ -517,6 +522,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
   YG_CUDA(cudaStreamSynchronize(st));
   if (iters_out) *iters_out = iter_tot;
   if (fallback_out) *fallback_out = E.n_fallback;
+  if (second_out) *second_out = E.n_second;
   if (ms_assign) *ms_assign = E.ms_assign;
   if (ms_update) *ms_update = E.ms_update;
   *ret_out = core_ret < 0 ? -1.f : (float)(best / n);
@@ -534,7 +540,8 @@ __global__ void node_update_kernel(const long *perm_sorted, const int *child, lo
 }
 
 int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bool verbose,
-            int prec, float **levels_out, int *assign_out, long *iters_out, float *ms_out) {
+            int prec, bool small_nodes, float **levels_out, int *assign_out, long *iters_out,
+            float *ms_out) {
   Ctx *ctx;
   YG_CHECK(ctx_get(&ctx));
   cudaStream_t st = ctx->stream;
@@ -578,7 +585,7 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
         fprintf(stderr, "# Problem2: no enough vectors in a node\n");
         exit(1);
       }
-      if (na < bf) {
+      if (na < bf && !small_nodes) {
         set_error(E_ARG, "hkm: node %ld of level %d has %ld points < bf=%d (kmeans asserts k <= n)",
                   p, l, na, bf);
         return E_ARG;
@@ -587,10 +594,19 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
       x.p0 = start[p];
       x.n = (int)na;
       x.seed = (unsigned)lrand48();  // kmeans(..., seed 0, ...) per child, in parent order
+      x.done = na < bf;              // small node: no k-means (see yael_gpu_hkm_learn_ex)
     }
     YG_CHECK(E.setup());
     YG_CHECK(E.init_random());
-    for (auto &x : E.in) x.core = rand_r(&x.seed);
+    std::vector<int> iota(bf);
+    for (int j = 0; j < bf; j++) iota[j] = j;
+    for (auto &x : E.in) {
+      x.core = rand_r(&x.seed);
+      if (x.done)  // each point is its own child
+        YG_CUDA(cudaMemcpyAsync(E.assign + x.p0, iota.data(), sizeof(int) * x.n,
+                                cudaMemcpyHostToDevice, st));
+    }
+    YG_CUDA(cudaStreamSynchronize(st));
     YG_CHECK(E.set_active());
     while (!E.all_done()) YG_CHECK(E.iterate());
     for (auto &x : E.in) iters += x.iters;
@@ -712,14 +728,15 @@ float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int fla
     st = (cudaStream_t)opts->stream;
   }
   float ret = -1;
-  long iters = 0, fb = 0;
+  long iters = 0, fb = 0, sec = 0;
   float ma = 0, mu = 0;
   const int rc = kmeans_run(d, n, k, niter, v, flags, seed, redo, centroids, dis, assign,
-                            nassign, prec, dev, st, &ret, &iters, &fb, &ma, &mu);
+                            nassign, prec, dev, st, &ret, &iters, &fb, &sec, &ma, &mu);
   if (opts) {
     opts->status = rc;
     opts->iterations = iters;
     opts->n_fallback = fb;
+    opts->n_second = sec;
     opts->ms_assign = ma;
     opts->ms_update = mu;
   }
@@ -731,7 +748,7 @@ float kmeans(int d, int n, int k, int niter, const float *v, int flags, long see
              float *centroids, float *dis, int *assign, int *nassign) {
   float ret = -1;
   if (kmeans_run(d, n, k, niter, v, flags, seed, redo, centroids, dis, assign, nassign,
-                 default_precision(), false, nullptr, &ret, nullptr, nullptr, nullptr,
+                 default_precision(), false, nullptr, &ret, nullptr, nullptr, nullptr, nullptr,
                  nullptr) != OK)
     fatal_last("kmeans");
   return ret;
@@ -781,7 +798,7 @@ hkm_t *hkm_learn(int n, int d, int nlevel, int bf, const float *v, int nb_iter_m
   (void)nt;  // the reference ignores it too (hkm.c:85)
   hkm_t *h = hkm_alloc(d, nlevel, bf);
   int *assign = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
-  if (hkm_run(n, d, nlevel, bf, v, nb_iter_max, verbose != 0, default_precision(),
+  if (hkm_run(n, d, nlevel, bf, v, nb_iter_max, verbose != 0, default_precision(), false,
               h->centroids, assign, nullptr, nullptr) != OK)
     fatal_last("hkm_learn");
   if (clust_assign_out) *clust_assign_out = assign;
@@ -790,15 +807,16 @@ hkm_t *hkm_learn(int n, int d, int nlevel, int bf, const float *v, int nb_iter_m
 }
 
 int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v, int nb_iter_max,
-                          float *centroids, int *assign, long *iterations, float *ms) {
+                          int small_nodes, float *centroids, int *assign, long *iterations,
+                          float *ms) {
   std::vector<float *> lv(nlevel);
   long k = bf, off = 0;
   for (int l = 0; l < nlevel; l++, k *= bf) {
     lv[l] = centroids + off;
     off += k * d;
   }
-  return hkm_run(n, d, nlevel, bf, v, nb_iter_max, false, default_precision(), lv.data(), assign,
-                 iterations, ms);
+  return hkm_run(n, d, nlevel, bf, v, nb_iter_max, false, default_precision(), small_nodes != 0,
+                 lv.data(), assign, iterations, ms);
 }
 
 void hkm_delete(hkm_t *hkm) {

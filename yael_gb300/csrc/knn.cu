@@ -36,6 +36,24 @@ int pow2_at_least(int x) {
   return p;
 }
 
+__global__ void gather_rows_kernel(const float *src, long ld, const int *map, int n, int d,
+                                   float *dst) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long)n * d) return;
+  const long r = i / d;
+  dst[i] = src[(long)map[r] * ld + (i - r * d)];
+}
+
+__global__ void scatter_rows_kernel(const int *sidx, const float *sdis, const int *map, int n,
+                                    int k, int *didx, float *ddis) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long)n * k) return;
+  const long r = i / k;
+  const long o = (long)map[r] * k + (i - r * k);
+  didx[o] = sidx[i];
+  ddis[o] = sdis[i];
+}
+
 __global__ void fill_f32(float *p, long n, float v) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -119,7 +137,9 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
   const int nqt = (int)ceil_div(nq, tile_m);
   const int ntb = (int)ceil_div(nb, tile_n);
   const int ctas_per_sm = 1;
-  const int c_needed = bstats_exact ? k : 2 * k;
+  // oversampling for inexact distances: the certificate needs a margin between
+  // the k-th exact value and the first excluded candidate
+  const int c_needed = bstats_exact ? k : (k <= 4 ? 8 : 2 * k);
 
   std::unique_ptr<PassTimer> tm_scan, tm_sample;
   ScanSel sel;
@@ -206,7 +226,39 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
   tr.collect();
   job.n_fallback += hs.fail_cnt;
   job.n_cand = (long long)hs.n_cand;
-  if (hs.fail_cnt > 0) {
+  if (hs.fail_cnt > 0 && job.prec == PREC_BF16 && job.w == nullptr) {
+    // second chance for the rejected queries: the FP32 pass, whose error bound
+    // is ~2^-16 of the BF16 one, on a compacted copy of just those queries
+    const int nf = hs.fail_cnt;
+    int *map;
+    float *cq, *cdis;
+    int *cidx;
+    YG_CHECK(ws_get(ws, WS_SC_MAP, nf, &map));
+    YG_CHECK(ws_get(ws, WS_SC_Q, (size_t)nf * d, &cq));
+    YG_CHECK(ws_get(ws, WS_SC_IDX, (size_t)nf * k, &cidx));
+    YG_CHECK(ws_get(ws, WS_SC_DIS, (size_t)nf * k, &cdis));
+    YG_CUDA(cudaMemcpyAsync(map, fail_list, sizeof(int) * nf, cudaMemcpyDeviceToDevice, st));
+    gather_rows_kernel<<<(unsigned)ceil_div((long)nf * d, 256), 256, 0, st>>>(job.q, job.ldq, map,
+                                                                            nf, d, cq);
+    YG_LAUNCH_CHECK();
+    KnnJob sub = job;
+    sub.prec = PREC_FP32;
+    sub.nq = nf;
+    sub.q = cq;
+    sub.ldq = d;
+    sub.out_idx = cidx;
+    sub.out_dis = cdis;
+    sub.n_fallback = 0;
+    sub.timing = 0;
+    YG_CHECK(knn_batch(sub, ctx, st, dsmall, tcb, bstats_exact));
+    scatter_rows_kernel<<<(unsigned)ceil_div((long)nf * k, 256), 256, 0, st>>>(cidx, cdis, map, nf,
+                                                                             k, job.out_idx,
+                                                                             job.out_dis);
+    YG_LAUNCH_CHECK();
+    job.n_second += nf;
+    job.n_fallback += sub.n_fallback - nf;  // only what the FP32 pass also rejected
+    YG_CUDA(cudaStreamSynchronize(st));
+  } else if (hs.fail_cnt > 0) {
     size_t per = exhaustive_bytes_per_query(nb);
     size_t want = per * (size_t)hs.fail_cnt;
     const size_t cap_bytes = (size_t)1 << 30;
@@ -224,6 +276,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
 int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   const int nq = job.nq, nb = job.nb, d = job.d, k = job.k;
   job.n_fallback = 0;
+  job.n_second = 0;
   job.n_cand = 0;
   job.exact_class = 0;
   job.ms_scan = job.ms_sample = job.ms_rerank = 0;
@@ -291,7 +344,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   // query batches bounded by the candidate buffers (<= 2 GiB)
   size_t per_query;
   {
-    const int cn = bexact ? k : 2 * k;
+    const int cn = bexact ? k : (k <= 4 ? 8 : 2 * k);
     const bool bf16 = job.prec == PREC_BF16;
     const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N, tile_m = bf16 ? TC_TILE_M : 128;
     const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
@@ -312,10 +365,12 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     sub.out_idx = job.out_idx + (long)q0 * k;
     sub.out_dis = job.out_dis + (long)q0 * k;
     sub.n_fallback = 0;
+    sub.n_second = 0;
     sub.ms_scan = sub.ms_sample = sub.ms_rerank = 0;
     sub.scan_launches = 0;
     YG_CHECK(knn_batch(sub, ctx, st, dsmall, &tcb, bexact));
     job.n_fallback += sub.n_fallback;
+    job.n_second += sub.n_second;
     job.n_cand += sub.n_cand;
     job.ms_scan += sub.ms_scan;
     job.ms_sample += sub.ms_sample;
@@ -371,6 +426,7 @@ static int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
     opts->ms_sample = job.ms_sample;
     opts->ms_rerank = job.ms_rerank;
     opts->scan_launches = job.scan_launches;
+    opts->n_second = job.n_second;
   }
   return OK;
 }

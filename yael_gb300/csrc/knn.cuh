@@ -21,7 +21,8 @@ struct KnnJob {
   float ms_scan = 0, ms_sample = 0, ms_rerank = 0;
   int scan_launches = 0;
   // filled on return
-  int n_fallback = 0;
+  int n_fallback = 0;   // queries recomputed by the exhaustive FP64 path
+  int n_second = 0;     // BF16-rejected queries re-run through the FP32 pass
   long long n_cand = 0;
   int exact_class = 0;
 };
@@ -34,6 +35,7 @@ enum WsSlot : int {
   WS_QN64 = 0, WS_QFLAG, WS_QRES, WS_BN32, WS_SMALL, WS_EPS, WS_QEXACT,
   WS_TOPV, WS_TOPI, WS_THR, WS_CNT, WS_FAIL, WS_STOPV, WS_STOPI, WS_EXH,
   WS_QPACK, WS_BPACK, WS_QNORMP, WS_BNORMP, WS_BRES,
+  WS_SC_MAP, WS_SC_Q, WS_SC_IDX, WS_SC_DIS,
   WS_H_B = 40, WS_H_Q, WS_H_W, WS_H_IDX, WS_H_DIS, WS_H_EXTRA,
   WS_KM0 = 60,  // k-means / hkm slots start here
 };
