@@ -180,9 +180,10 @@ float *hkm_get_centroids(const hkm_t *hkm, int l, int no);
 /* ------------------------------------------------------------------ */
 /* extension API                                                       */
 
-#define YAEL_GPU_PREC_ENV (-1) /* take YAEL_GPU_PRECISION (fp32 | bf16), default fp32 */
+#define YAEL_GPU_PREC_ENV (-1) /* take YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), default fp32 */
 #define YAEL_GPU_PREC_FP32 0   /* FP32 CUDA-core distances (the plain drop-in path) */
 #define YAEL_GPU_PREC_BF16 1   /* BF16 tensor-core distances + exact FP32 re-rank */
+#define YAEL_GPU_PREC_BF16X3 2 /* tensor cores on a 3xBF16 split (x = hi + lo) + re-rank */
 
 /* status codes of the yael_gpu_* functions */
 #define YAEL_GPU_OK 0

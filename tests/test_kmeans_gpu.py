@@ -38,7 +38,7 @@ def gpu_kmeans(v, k, niter, flags, seed, redo, prec, C0=None):
     dis = np.empty(n, np.float32)
     assign = np.empty(n, np.int32)
     nassign = np.empty(k, np.int32)
-    o = yg.KmeansOpts({"fp32": 0, "bf16": 1}[prec], 0, None, 0, 0, 0, 0, 0, 0)
+    o = yg.KmeansOpts({"fp32": 0, "bf16": 1, "bf16x3": 2}[prec], 0, None, 0, 0, 0, 0, 0, 0)
     q = yg.lib().yael_gpu_kmeans_ex(d, n, k, niter, ptr(v), flags, seed, redo, ptr(C), ptr(dis),
                                     ptr(assign), ptr(nassign), ctypes.byref(o))
     assert o.status == 0, yg.last_error()
@@ -60,7 +60,7 @@ def test_kmeans_small_k(prec):
     same(gpu_kmeans(v, 20, 12, QUIET, 1234, 1, prec), oracle_kmeans(v, 20, 12, QUIET, 1234, 1))
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
 def test_kmeans_large_k_knn_path(prec):
     v, _, _ = synth.gaussian_mixture(20000, 32, 128, 0.15, seed=5)
     same(gpu_kmeans(v, 100, 10, QUIET, 777, 1, prec), oracle_kmeans(v, 100, 10, QUIET, 777, 1))

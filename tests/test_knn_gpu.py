@@ -60,10 +60,11 @@ def test_golden_float(prec):
     np.testing.assert_array_equal(idx, g["idx_k1"])
 
 
-@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("prec", PRECS + ["bf16x3"])
 @pytest.mark.parametrize("nq,nb,d,k", [(1, 1, 1, 1), (7, 5, 3, 5), (33, 300, 129, 17),
                                         (130, 2000, 64, 100), (300, 9000, 96, 33),
-                                        (257, 1000, 7, 1), (64, 3000, 200, 250)])
+                                        (257, 1000, 7, 1), (64, 3000, 200, 250),
+                                        (100, 5000, 300, 10)])
 def test_shapes_gaussian(prec, nq, nb, d, k):
     rng = np.random.default_rng(nq * 7 + nb + d)
     b = rng.standard_normal((nb, d)).astype(np.float32)
@@ -83,7 +84,7 @@ def test_sift_like_medium(prec, k):
     assert st["exact_class"] == 1 and st["n_fallback"] == 0
 
 
-@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("prec", PRECS + ["bf16x3"])
 def test_unit_vectors_oversampled(prec):
     b = synth.unit_gaussian(50_000, 128, seed=3)
     q = synth.unit_gaussian(200, 128, seed=4)
@@ -208,3 +209,14 @@ def test_reorder_shortlist_and_recompute(gpu_lib):
         assert kp[r] == n_in
         d = ((v[r].astype(np.float64) - b[srt[r, :n_in]].astype(np.float64)) ** 2).sum(1)
         np.testing.assert_array_equal(d2[r, :n_in], d.astype(np.float32))
+
+
+def test_split_pass_settles_bf16_rejections():
+    """Clustered float data with close neighbours: the BF16 certificate rejects
+    many queries; the 3xBF16 second pass must settle them with exact ids."""
+    v, _, _ = synth.gaussian_mixture(60000, 64, 30, 0.05, seed=31)
+    q, _, _ = synth.gaussian_mixture(400, 64, 30, 0.05, seed=31)
+    st = assert_exact(v, q, 1, "bf16")
+    assert st["n_fallback"] <= 5
+    st = assert_exact(v, q, 3, "bf16")
+    assert st["n_fallback"] <= 5

@@ -34,7 +34,7 @@ KMEANS_INIT_USER = 0x100000
 KMEANS_L1 = 0x200000
 KMEANS_CHI2 = 0x400000
 
-PREC_ENV, PREC_FP32, PREC_BF16 = -1, 0, 1
+PREC_ENV, PREC_FP32, PREC_BF16, PREC_BF16X3 = -1, 0, 1, 2
 
 
 class KmeansOpts(ctypes.Structure):
@@ -149,7 +149,7 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
     assert d == d2, "base and queries must have the same dimension"
     idx = np.empty((nq, nnn), dtype=np.int32)
     dis = np.empty((nq, nnn), dtype=np.float32)
-    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3}[precision]
     opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     rc = lib().yael_gpu_knn_ex(nq, nb, d, nnn, _ptr(base), _ptr(queries), _ptr(idx), _ptr(dis),
                                ctypes.byref(opts))
@@ -157,7 +157,7 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
         raise RuntimeError(f"yael_gpu_knn_ex failed ({rc}): {last_error()}")
     if stats:
         return idx, dis, {"n_fallback": opts.n_fallback, "n_candidates": opts.n_candidates,
-                          "exact_class": opts.exact_class}
+                          "exact_class": opts.exact_class, "n_second": opts.n_second}
     return idx, dis
 
 
@@ -197,7 +197,7 @@ def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
         flags |= KMEANS_INIT_BERKELEY
     if normalize:
         flags |= KMEANS_NORMALIZE_CENTS
-    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16}[precision]
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3}[precision]
     opts = KmeansOpts(prec, 0, None, 0, 0, 0, 0, 0, 0)
     qerr = lib().yael_gpu_kmeans_ex(d, n, k, niter, _ptr(v), flags, seed, redo, _ptr(centroids),
                                     _ptr(dis), _ptr(assign), _ptr(nassign), ctypes.byref(opts))

@@ -87,8 +87,10 @@ struct Ctx {
 int ctx_get(Ctx **out);
 
 // precision of the distance pass
-enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1 };
-int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16), default fp32
+// PREC_BF16X3: the tensor cores on a 3xBF16 split of the operands
+// (x = hi + lo), about 2^-16 relative error instead of 2^-8
+enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1, PREC_BF16X3 = 2 };
+int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), default fp32
 
 // ---------------------------------------------------------------------------
 // device helpers

@@ -722,7 +722,8 @@ float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int fla
   bool dev = false;
   cudaStream_t st = nullptr;
   if (opts) {
-    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16)
+    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16 ||
+        opts->precision == YAEL_GPU_PREC_BF16X3)
       prec = opts->precision;
     dev = opts->device_ptrs != 0;
     st = (cudaStream_t)opts->stream;

@@ -16,10 +16,18 @@ namespace yg {
 namespace {
 
 struct Small {
-  SetStats bs;
+  SetStats bs;   // base statistics of the plain (bf16 / fp32) packing
+  SetStats bs3;  // base statistics of the split 3xBF16 packing
   int fail_cnt;
-  int pad;
+  int tc_err;    // set by a tensor-core pass whose bounded wait expired
   unsigned long long n_cand;
+};
+
+// packed base operands of the tensor-core passes (the split one is built on
+// first use by the second-chance pass)
+struct BaseOps {
+  TcOperands plain, split;
+  bool has_plain = false, has_split = false;
 };
 
 template <typename T>
@@ -89,16 +97,17 @@ struct PassTimer {
 int scan(const KnnJob &job, const float *q, int nq, const float *b, long ldb, int nb,
          const float *bn, long bn_stride, const TcOperands *tc, const ScanSel &sel,
          cudaStream_t st) {
-  if (job.prec == PREC_BF16) return tc_scan(*tc, nq, nb, sel, st);
+  if (job.prec != PREC_FP32) return tc_scan(*tc, nq, nb, sel, st);
   return simt_scan(q, job.ldq, nq, b, ldb, nb, job.d, bn, bn_stride, job.metric, sel, st);
 }
 
 // one batch of queries (all buffers sized for nq of this batch)
-int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOperands *tcb,
+int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bops,
               int bstats_exact) {
   Workspace &ws = ctx->ws;
   const int nq = job.nq, nb = job.nb, d = job.d, k = job.k;
-  const bool bf16 = job.prec == PREC_BF16;
+  const bool bf16 = job.prec != PREC_FP32;  // a tensor-core pass (bf16 or split)
+  const bool split = job.prec == PREC_BF16X3;
   double *qn64;
   unsigned char *qflag, *qexact;
   float *qres = nullptr, *eps, *bn32 = nullptr;
@@ -110,16 +119,22 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
   YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32));  // written by knn_device
 
   TcOperands tcq;
+  float *qlo = nullptr;
   if (bf16) {
-    tcq = *tcb;
+    tcq = split ? bops->split : bops->plain;
+    if (split) YG_CHECK(ws_get(ws, WS_QLO, nq, &qlo));
     YG_CHECK(tc_prepare_queries(job.q, job.ldq, nq, d, job.metric, ws, WS_QPACK, WS_QNORMP,
-                                &tcq, qn64, qflag, qres, st));
+                                &tcq, qn64, qflag, qres, split ? 1 : 0, qlo, st));
   } else {
     YG_CHECK(prep_rows(job.q, job.ldq, nq, d, 1.f, qn64, nullptr, qflag, qres, nullptr, 0,
                        nullptr, 0, nullptr, st));
   }
-  YG_CHECK(compute_eps(nq, d, job.prec, job.metric, qn64, qres, qflag, &dsmall->bs, eps,
-                       qexact, st));
+  if (split)
+    YG_CHECK(compute_eps_split(nq, d, job.metric, qn64, qlo, qres, qflag, &dsmall->bs3, eps,
+                               qexact, st));
+  else
+    YG_CHECK(compute_eps(nq, d, job.prec, job.metric, qn64, qres, qflag, &dsmall->bs, eps,
+                         qexact, st));
 
   int *fail_list;
   YG_CHECK(ws_get(ws, WS_FAIL, nq, &fail_list));
@@ -227,9 +242,18 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
   job.n_fallback += hs.fail_cnt;
   job.n_cand = (long long)hs.n_cand;
   if (hs.fail_cnt > 0 && job.prec == PREC_BF16 && job.w == nullptr) {
-    // second chance for the rejected queries: the FP32 pass, whose error bound
-    // is ~2^-16 of the BF16 one, on a compacted copy of just those queries
+    // second chance for the rejected queries: the 3xBF16 split pass, whose
+    // error bound is ~2^-8 of the BF16 one, on a compacted copy of just those
+    // queries (queries it also rejects go to the exhaustive FP64 path)
     const int nf = hs.fail_cnt;
+    if (!bops->has_split) {
+      float *bn32s;
+      YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32s));
+      YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK3, WS_BNORMP3,
+                               WS_BRES3, &bops->split, bn32s, &dsmall->bs3, 1, st));
+      bops->split.err = bops->plain.err;
+      bops->has_split = true;
+    }
     int *map;
     float *cq, *cdis;
     int *cidx;
@@ -242,7 +266,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
                                                                             nf, d, cq);
     YG_LAUNCH_CHECK();
     KnnJob sub = job;
-    sub.prec = PREC_FP32;
+    sub.prec = PREC_BF16X3;
     sub.nq = nf;
     sub.q = cq;
     sub.ldq = d;
@@ -250,13 +274,13 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, const TcOpe
     sub.out_dis = cdis;
     sub.n_fallback = 0;
     sub.timing = 0;
-    YG_CHECK(knn_batch(sub, ctx, st, dsmall, tcb, bstats_exact));
+    YG_CHECK(knn_batch(sub, ctx, st, dsmall, bops, bstats_exact));
     scatter_rows_kernel<<<(unsigned)ceil_div((long)nf * k, 256), 256, 0, st>>>(cidx, cdis, map, nf,
                                                                              k, job.out_idx,
                                                                              job.out_dis);
     YG_LAUNCH_CHECK();
     job.n_second += nf;
-    job.n_fallback += sub.n_fallback - nf;  // only what the FP32 pass also rejected
+    job.n_fallback += sub.n_fallback - nf;  // only what the split pass also rejected
     YG_CUDA(cudaStreamSynchronize(st));
   } else if (hs.fail_cnt > 0) {
     size_t per = exhaustive_bytes_per_query(nb);
@@ -298,7 +322,6 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     return E_UNSUPPORTED;
   }
   if (nq == 0) return OK;
-  if (job.prec == PREC_BF16 && !tc_supported(d)) job.prec = PREC_FP32;
   Workspace &ws = ctx->ws;
 
   Small *dsmall;
@@ -307,6 +330,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     Small h;
     memset(&h, 0, sizeof(h));
     h.bs.all_exact = 1;
+    h.bs3.all_exact = 1;
     YG_CUDA(cudaMemcpyAsync(dsmall, &h, sizeof(h), cudaMemcpyHostToDevice, st));
   }
 
@@ -327,10 +351,18 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   // base preparation (once for all query batches)
   float *bn32, *bres = nullptr;
   YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32));
-  TcOperands tcb;
+  BaseOps bops;
   if (job.prec == PREC_BF16) {
     YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK, WS_BNORMP,
-                             WS_BRES, &tcb, bn32, &dsmall->bs, st));
+                             WS_BRES, &bops.plain, bn32, &dsmall->bs, 0, st));
+    bops.has_plain = true;
+  } else if (job.prec == PREC_BF16X3) {
+    // the plain statistics (max norm) are needed too: dot-product bounds read them
+    YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK3, WS_BNORMP3,
+                             WS_BRES3, &bops.split, bn32, &dsmall->bs3, 1, st));
+    YG_CHECK(prep_rows(job.b, job.ldb, nb, d, 1.f, nullptr, nullptr, nullptr, nullptr, nullptr,
+                       0, nullptr, 0, &dsmall->bs, st));
+    bops.has_split = true;
   } else {
     YG_CHECK(prep_rows(job.b, job.ldb, nb, d, 1.f, nullptr, bn32, nullptr, bres, nullptr, 0,
                        nullptr, 0, &dsmall->bs, st));
@@ -340,12 +372,13 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   YG_CUDA(cudaStreamSynchronize(st));
   const int bexact = hs.bs.all_exact;
   job.exact_class = bexact;
+  bops.plain.err = bops.split.err = &dsmall->tc_err;
 
   // query batches bounded by the candidate buffers (<= 2 GiB)
   size_t per_query;
   {
     const int cn = bexact ? k : (k <= 4 ? 8 : 2 * k);
-    const bool bf16 = job.prec == PREC_BF16;
+    const bool bf16 = job.prec != PREC_FP32;
     const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N, tile_m = bf16 ? TC_TILE_M : 128;
     const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
     int C = 1;
@@ -368,7 +401,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     sub.n_second = 0;
     sub.ms_scan = sub.ms_sample = sub.ms_rerank = 0;
     sub.scan_launches = 0;
-    YG_CHECK(knn_batch(sub, ctx, st, dsmall, &tcb, bexact));
+    YG_CHECK(knn_batch(sub, ctx, st, dsmall, &bops, bexact));
     job.n_fallback += sub.n_fallback;
     job.n_second += sub.n_second;
     job.n_cand += sub.n_cand;
@@ -377,7 +410,14 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     job.ms_rerank += sub.ms_rerank;
     job.scan_launches += sub.scan_launches;
   }
-  if (job.prec == PREC_BF16) YG_CHECK(tc_take_error(st));
+  if (job.prec != PREC_FP32) {
+    YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    if (hs.tc_err) {
+      set_error(E_TIMEOUT, "tensor-core pass gave up waiting (bounded wait expired)");
+      return E_TIMEOUT;
+    }
+  }
   return OK;
 }
 
@@ -448,7 +488,8 @@ int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q
   int prec = default_precision();
   int metric = METRIC_L2;
   if (opts) {
-    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16)
+    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16 ||
+        opts->precision == YAEL_GPU_PREC_BF16X3)
       prec = opts->precision;
     if (opts->metric) metric = metric_of(opts->metric);
   }

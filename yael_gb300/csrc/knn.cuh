@@ -35,7 +35,7 @@ enum WsSlot : int {
   WS_QN64 = 0, WS_QFLAG, WS_QRES, WS_BN32, WS_SMALL, WS_EPS, WS_QEXACT,
   WS_TOPV, WS_TOPI, WS_THR, WS_CNT, WS_FAIL, WS_STOPV, WS_STOPI, WS_EXH,
   WS_QPACK, WS_BPACK, WS_QNORMP, WS_BNORMP, WS_BRES,
-  WS_SC_MAP, WS_SC_Q, WS_SC_IDX, WS_SC_DIS,
+  WS_SC_MAP, WS_SC_Q, WS_SC_IDX, WS_SC_DIS, WS_QLO, WS_BPACK3, WS_BNORMP3, WS_BRES3,
   WS_H_B = 40, WS_H_Q, WS_H_W, WS_H_IDX, WS_H_DIS, WS_H_EXTRA,
   WS_KM0 = 60,  // k-means / hkm slots start here
 };

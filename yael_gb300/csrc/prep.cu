@@ -128,10 +128,115 @@ __global__ void __launch_bounds__(PW * 32)
     if (nn) atomicAdd(&stats->n_nan, nn);
   }
 }
+
+__global__ void __launch_bounds__(PW * 32)
+    prep_split_kernel(const float *__restrict__ x, long ld, int n, int d, float scale, int layout,
+                      double *norm64, float *norm32, unsigned char *flags, float *lonorm,
+                      float *resid, __nv_bfloat16 *packed, int Kp1, __nv_bfloat16 *normpart,
+                      int normpart_mode, SetStats *stats) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long nwarps = (long)gridDim.x * PW;
+  const int Kp = 3 * Kp1;
+  float w_maxnorm = 0.f, w_maxres = 0.f, w_maxlo = 0.f;
+  int w_exact = 1, w_nan = 0;
+  for (long row = (long)blockIdx.x * PW + wid; row < n; row += nwarps) {
+    const float *xr = x + row * ld;
+    float s = 0.f, r = 0.f, l = 0.f;
+    int exact = 1, bad = 0;
+    for (int c = lane; c < Kp1; c += 32) {
+      const float v = c < d ? __ldg(xr + c) : 0.f;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      const float rest = v - __bfloat162float(hi);             // exact
+      const __nv_bfloat16 lo = __float2bfloat16_rn(rest);
+      const float r2 = rest - __bfloat162float(lo);            // exact
+      if (c < d) {
+        s = fmaf(v, v, s);
+        exact &= (v == rintf(v)) && (fabsf(v) <= 256.f);
+        bad |= !isfinite(v);
+        const float lf = __bfloat162float(lo);
+        l = fmaf(lf, lf, l);
+        r = fmaf(r2, r2, r);
+      }
+      const __nv_bfloat16 shi = __float2bfloat16_rn(scale * __bfloat162float(hi));
+      const __nv_bfloat16 slo = __float2bfloat16_rn(scale * __bfloat162float(lo));
+      __nv_bfloat16 *pr = packed + row * Kp;
+      pr[c] = shi;
+      pr[Kp1 + c] = layout == 0 ? shi : slo;
+      pr[2 * Kp1 + c] = layout == 0 ? slo : shi;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+      l += __shfl_xor_sync(0xffffffffu, l, o);
+      exact &= __shfl_xor_sync(0xffffffffu, exact, o);
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    exact &= (s <= kExactNorm2Max) && !bad;
+    if (normpart && lane < 16) {
+      __nv_bfloat16 val = __float2bfloat16_rn(0.f);
+      if (normpart_mode == 1) {
+        const float n32 = s;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(n32);
+        const float r1 = n32 - __bfloat162float(hi);
+        const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+        const float r2 = r1 - __bfloat162float(mid);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+        val = lane == 0 ? hi : lane == 1 ? mid : lane == 2 ? lo : val;
+      } else if (normpart_mode == 2) {
+        val = __float2bfloat16_rn(lane < 3 ? 1.f : 0.f);
+      }
+      normpart[row * 16 + lane] = val;
+    }
+    const float rr = sqrtf(r) * (1.f + 1e-5f), ll = sqrtf(l) * (1.f + 1e-5f);
+    if (lane == 0) {
+      if (norm64) norm64[row] = (double)s;
+      if (norm32) norm32[row] = s;
+      if (flags) flags[row] = (unsigned char)exact;
+      if (resid) resid[row] = rr;
+      if (lonorm) lonorm[row] = ll;
+    }
+    if (!bad) {
+      w_maxnorm = fmaxf(w_maxnorm, sqrtf(s) * (1.f + 1e-5f));
+      w_maxres = fmaxf(w_maxres, rr);
+      w_maxlo = fmaxf(w_maxlo, ll);
+    } else {
+      w_nan++;
+    }
+    w_exact &= exact;
+  }
+  if (!stats) return;
+  __shared__ float s_norm[PW], s_res[PW], s_lo[PW];
+  __shared__ int s_exact[PW], s_nan[PW];
+  if (lane == 0) {
+    s_norm[wid] = w_maxnorm;
+    s_res[wid] = w_maxres;
+    s_lo[wid] = w_maxlo;
+    s_exact[wid] = w_exact;
+    s_nan[wid] = w_nan;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float mn = 0.f, mr = 0.f, ml = 0.f;
+    int ex = 1, nn = 0;
+    for (int w = 0; w < PW; w++) {
+      mn = fmaxf(mn, s_norm[w]);
+      mr = fmaxf(mr, s_res[w]);
+      ml = fmaxf(ml, s_lo[w]);
+      ex &= s_exact[w];
+      nn += s_nan[w];
+    }
+    atomicMax(&stats->max_norm_bits, __float_as_uint(mn));
+    atomicMax(&stats->max_resid_bits, __float_as_uint(mr));
+    atomicMax(&stats->max_lo_bits, __float_as_uint(ml));
+    if (!ex) atomicAnd(&stats->all_exact, 0);
+    if (nn) atomicAdd(&stats->n_nan, nn);
+  }
+}
 }  // namespace
 
 int stats_reset(SetStats *stats, cudaStream_t st) {
-  SetStats h{0u, 0u, 1, 0};
+  SetStats h{0u, 0u, 1, 0, 0u};
   YG_CUDA(cudaMemcpyAsync(stats, &h, sizeof(h), cudaMemcpyHostToDevice, st));
   return OK;
 }
@@ -153,6 +258,23 @@ int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64
   prep_rows_kernel<<<(unsigned)blocks, PW * 32, 0, st>>>(x, ld, n, d, scale, norm64, norm32,
                                                          flags, resid, packed, Kp, normpart,
                                                          normpart_mode, stats);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int prep_rows_split(const float *x, long ld, int n, int d, float scale, int layout,
+                    double *norm64, float *norm32, unsigned char *flags, float *lonorm,
+                    float *resid, __nv_bfloat16 *packed, int Kp1, __nv_bfloat16 *normpart,
+                    int normpart_mode, SetStats *stats, cudaStream_t st) {
+  if (n <= 0) return OK;
+  int dev = 0, sms = 0;
+  YG_CUDA(cudaGetDevice(&dev));
+  YG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  long blocks = ceil_div(n, PW);
+  if (blocks > (long)sms * 16) blocks = (long)sms * 16;
+  prep_split_kernel<<<(unsigned)blocks, PW * 32, 0, st>>>(x, ld, n, d, scale, layout, norm64,
+                                                          norm32, flags, lonorm, resid, packed,
+                                                          Kp1, normpart, normpart_mode, stats);
   YG_LAUNCH_CHECK();
   return OK;
 }

@@ -13,6 +13,7 @@ struct SetStats {
   unsigned int max_resid_bits;  // max ||x - bf16(x)||
   int all_exact;                // 1 iff every row is "exact class" (see row_exact below)
   int n_nan;                    // rows with a NaN/Inf coordinate
+  unsigned int max_lo_bits;     // split packing: max ||lo||, lo = bf16(x - bf16(x))
 };
 
 // A row is exact class when all coordinates are integers of magnitude <= 256
@@ -35,6 +36,18 @@ int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64
               float *norm32, unsigned char *flags, float *resid,
               __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
               int normpart_mode, SetStats *stats, cudaStream_t st);
+
+// Split ("3xBF16") packing: x = hi + lo + r with hi = bf16(x), lo = bf16(x - hi),
+// written as three K segments of Kp1 = 64*ceil(d/64) columns each:
+//   layout 0 (queries): [hi | hi | lo] of scale*x
+//   layout 1 (base):    [hi | lo | hi]
+// so one MMA over the 3*Kp1 columns sums q_hi.b_hi + q_hi.b_lo + q_lo.b_hi
+// (only q_lo.b_lo and the residuals r are left out).  Per row: lonorm = ||lo||,
+// resid = ||r||; norms / flags / side block / stats as prep_rows.
+int prep_rows_split(const float *x, long ld, int n, int d, float scale, int layout,
+                    double *norm64, float *norm32, unsigned char *flags, float *lonorm,
+                    float *resid, __nv_bfloat16 *packed, int Kp1, __nv_bfloat16 *normpart,
+                    int normpart_mode, SetStats *stats, cudaStream_t st);
 
 int stats_reset(SetStats *stats, cudaStream_t st);
 

@@ -112,6 +112,7 @@ int default_precision() {
   const char *s = getenv("YAEL_GPU_PRECISION");
   if (!s || !*s) return PREC_FP32;
   if (!strcmp(s, "bf16") || !strcmp(s, "BF16") || !strcmp(s, "1")) return PREC_BF16;
+  if (!strcmp(s, "bf16x3") || !strcmp(s, "BF16X3") || !strcmp(s, "2")) return PREC_BF16X3;
   return PREC_FP32;
 }
 

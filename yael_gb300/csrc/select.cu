@@ -428,6 +428,31 @@ __global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn
   eps[q] = isfinite(e) ? (float)e : INFINITY;
 }
 
+__global__ void eps_split_kernel(int nq, int d, int metric, const double *qn64, const float *qlo,
+                                 const float *qres2, const unsigned char *qflag,
+                                 const SetStats *bs, float *eps, unsigned char *qexact) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const bool ex = qflag[q] && bs->all_exact;
+  qexact[q] = ex;
+  if (ex) { eps[q] = 0.f; return; }
+  const double u = 5.9604644775390625e-08;  // 2^-24
+  const double un = ((d + 31) / 32 + 6) * u;
+  const double qn = sqrt(fmax(qn64[q], 0.0)) * (1 + 1e-5);
+  const double B = (double)__uint_as_float(bs->max_norm_bits);
+  const double LB = (double)__uint_as_float(bs->max_lo_bits);
+  const double RB = (double)__uint_as_float(bs->max_resid_bits);
+  const double lq = (double)qlo[q], rq = (double)qres2[q];
+  // q.b - (qh.bh + qh.bl + ql.bh) = ql.bl + rq.b + (q - rq).rb
+  const double dot = lq * LB + rq * B + qn * RB;
+  const double Kt = (double)(3 * ((d + 63) / 64) * 64 + 16);
+  const double L2 = metric == METRIC_L2;
+  const double acc = Kt * 2 * u * ((L2 ? 2 : 1) * qn * B * 1.02 + (L2 ? 1.001 * B * B : 0.0));
+  double e = (L2 ? 2 * dot + u * B * B : dot) + acc + un * (qn * qn + B * B);
+  e = e * 1.1 + 1e-30;
+  eps[q] = isfinite(e) ? (float)e : INFINITY;
+}
+
 __global__ void thresh_kernel(int nq, int nchunk, int C, int c, const float *topv,
                               const float *eps, float *thr) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -619,6 +644,16 @@ int compute_eps(int nq, int d, int prec, int metric, const double *qn64,
   if (nq <= 0) return OK;
   eps_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(nq, d, prec, metric, qn64, qres,
                                                           qflag, bstats, eps, qexact);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int compute_eps_split(int nq, int d, int metric, const double *qn64, const float *qlo,
+                      const float *qres2, const unsigned char *qflag, const SetStats *bstats,
+                      float *eps, unsigned char *qexact, cudaStream_t st) {
+  if (nq <= 0) return OK;
+  eps_split_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(nq, d, metric, qn64, qlo, qres2,
+                                                                qflag, bstats, eps, qexact);
   YG_LAUNCH_CHECK();
   return OK;
 }

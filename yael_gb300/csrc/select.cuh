@@ -45,6 +45,12 @@ int compute_eps(int nq, int d, int prec, int metric, const double *qn64,
                 const float *qres, const unsigned char *qflag, const SetStats *bstats,
                 float *eps, unsigned char *qexact, cudaStream_t st);
 
+// eps[q] for the 3xBF16 split pass: the left-out q_lo.b_lo and residual
+// terms plus the FP32 accumulation of 3*Kp1 + 16 products.
+int compute_eps_split(int nq, int d, int metric, const double *qn64, const float *qlo,
+                      const float *qres2, const unsigned char *qflag, const SetStats *bstats,
+                      float *eps, unsigned char *qexact, cudaStream_t st);
+
 // THRESH thresholds from a TOPC pass over a sample: thr[q] (v space) = the
 // c-th smallest sampled value + 2 eps[q], rounded up.
 int thresh_from_sample(int nq, int nchunk, int C, int c, const float *topv,

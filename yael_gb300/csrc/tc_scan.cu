@@ -1,487 +1,32 @@
-// tcgen05 BF16 distance tiles with the fused selection (see tc_scan.cuh).
-//
-// One CTA = one 128-row query tile x one chunk of 256-row base tiles.
-//   warp 0      TMA producer: the query tile once (resident), then a ring of
-//               S stages, each one 64-column K block of a base tile (or the
-//               16-column norm block), 128B / 32B swizzled.
-//   warp 1      TMEM owner (512 columns = two 128x256 FP32 accumulators) and
-//               MMA issuer: Kp/16 (+1) tcgen05.mma 128x256x16 per base tile.
-//   warps 2-9   selection: TMEM lane = query row; warps 2-5 read columns
-//               0-127 and warps 6-9 columns 128-255 of each accumulator with
-//               tcgen05.ld 32x32b.x32, filter against a running bound and
-//               update the per-row list (TOPC) or append candidates (THRESH).
-// The accumulators are double-buffered so the selection of tile t overlaps the
-// MMAs of tile t+1.  All waits are bounded (tc_ptx.cuh).
-#include <cudaTypedefs.h>
-#include <math.h>
-
-#include "tc_ptx.cuh"
-#include "tc_scan.cuh"
+// tcgen05 BF16 distance tiles with the fused selection (see tc_scan.cuh and
+// tc_kernel.cuh): operand packing and the resident-query-tile dispatch.
+#include "tc_kernel.cuh"
 
 namespace yg {
 
-namespace {
-using namespace ptx;
-
-constexpr int NT_TC = 320;
-constexpr int N_EPI = 256;               // selection threads
-constexpr int STAGE_BYTES = 256 * 128;   // 256 rows x 64 bf16
-constexpr int QBLK_BYTES = 128 * 128;    // 128 rows x 64 bf16
-constexpr int QN_BYTES = 4096;           // 128 rows x 16 bf16 (padded to 4 KB)
-constexpr int BN_BYTES = 256 * 32;       // 256 rows x 16 bf16
-constexpr int TMEM_COLS = 512;
-
-__device__ int g_tc_err;
-
-struct Layout {
-  int nkb, S, C, mode;
-  size_t q_off, qn_off, stg_off, list_off, bar_off, total;
-};
-
-__host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C) {
-  Layout L;
-  L.nkb = nkb; L.S = S; L.mode = mode; L.C = C;
-  size_t off = 0;
-  L.q_off = off;   off += (size_t)nkb * QBLK_BYTES;
-  L.qn_off = off;  off += QN_BYTES;
-  L.stg_off = off; off += (size_t)S * STAGE_BYTES;
-  L.list_off = off;
-  if (mode != SCAN_THRESH) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
-  off = (off + 15) & ~(size_t)15;
-  L.bar_off = off; off += (size_t)(2 * S + 5) * 8 + 16;
-  L.total = off + 1024;  // alignment slack for the 1024-byte aligned base
-  return L;
-}
-
-__device__ __forceinline__ float fmin3(float a, float b, float c) {
-  float r;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-}
-
-// sorted insertion of (x, j) into an ascending register list; the caller has
-// checked x < L[C-1].  Equal values keep their earlier (smaller) ids first.
-template <int C>
-__device__ __forceinline__ void reg_insert(float (&L)[C], int (&I)[C], float x, int j) {
-  int p = 0;
-#pragma unroll
-  for (int s = 0; s < C; s++) p += (L[s] <= x);
-#pragma unroll
-  for (int s = C - 1; s >= 0; s--) {
-    const float lv = (s > 0) ? L[s - 1] : 0.f;
-    const int li = (s > 0) ? I[s - 1] : 0;
-    const bool shift = s > p;
-    const bool here = s == p;
-    L[s] = shift ? lv : (here ? x : L[s]);
-    I[s] = shift ? li : (here ? j : I[s]);
-  }
-}
-
-template <int MODE, int C, bool L2>
-__global__ void __launch_bounds__(NT_TC, 1)
-    tc_scan_kernel(const __grid_constant__ CUtensorMap mapQ,
-                   const __grid_constant__ CUtensorMap mapQn,
-                   const __grid_constant__ CUtensorMap mapB,
-                   const __grid_constant__ CUtensorMap mapBn, int nq, int nb, int nkb,
-                   int S, ScanSel sel) {
-  extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t *base = reinterpret_cast<uint8_t *>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  const Layout lay = make_layout(nkb, S, MODE, C);
-  uint8_t *Qs = base + lay.q_off;
-  uint8_t *Qn = base + lay.qn_off;
-  uint8_t *Stg = base + lay.stg_off;
-  float *Lv = reinterpret_cast<float *>(base + lay.list_off);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(base + lay.bar_off);
-  uint64_t *full = bars, *empty = bars + S, *tfull = bars + 2 * S, *tempty = bars + 2 * S + 2;
-  uint64_t *qfull = bars + 2 * S + 4;
-  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * S + 5);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_holder + 1);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long q0 = (long)blockIdx.x * TC_TILE_M;
-  const int ntb = (int)ceil_div(nb, TC_TILE_N);
-  const int t_begin = blockIdx.y * sel.tiles_per_chunk;
-  const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
-  const int nks = nkb + (L2 ? 1 : 0);
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < S; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    for (int a = 0; a < 2; a++) {
-      mbar_init(&tfull[a], 1);
-      mbar_init(&tempty[a], N_EPI / 32);
-    }
-    mbar_init(qfull, 1);
-    *abort_flag = 0;
-    fence_mbar_init();
-  }
-  if (warp == 1) {
-    tmem_alloc(tmem_holder, TMEM_COLS);
-    tmem_relinquish();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_holder;
-
-  if (warp == 0) {
-    // ---------------- TMA producer
-    if (lane == 0) {
-      mbar_arrive_expect_tx(qfull, (uint32_t)(nkb * QBLK_BYTES + (L2 ? 128 * 32 : 0)));
-      for (int kb = 0; kb < nkb; kb++)
-        tma_load_2d(&mapQ, qfull, Qs + kb * QBLK_BYTES, kb * 64, (int)q0);
-      if (L2) tma_load_2d(&mapQn, qfull, Qn, 0, (int)q0);
-      long g = 0;
-      bool ok = true;
-      for (int t = t_begin; t < t_end && ok; t++) {
-        for (int ks = 0; ks < nks; ks++, g++) {
-          const int s = (int)(g % S);
-          const uint32_t use = (uint32_t)(g / S);
-          if (!mbar_wait(&empty[s], (use & 1) ^ 1, abort_flag)) { ok = false; break; }
-          if (ks < nkb) {
-            mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-            tma_load_2d(&mapB, &full[s], Stg + (size_t)s * STAGE_BYTES, ks * 64, t * TC_TILE_N);
-          } else {
-            mbar_arrive_expect_tx(&full[s], BN_BYTES);
-            tma_load_2d(&mapBn, &full[s], Stg + (size_t)s * STAGE_BYTES, 0, t * TC_TILE_N);
-          }
-        }
-      }
-    }
-  } else if (warp == 1) {
-    // ---------------- MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(TC_TILE_M, TC_TILE_N);
-      bool ok = mbar_wait(qfull, 0, abort_flag);
-      tc_fence_after();
-      long g = 0;
-      int it = 0;
-      for (int t = t_begin; t < t_end && ok; t++, it++) {
-        const int a = it & 1;
-        const uint32_t u = (uint32_t)(it >> 1);
-        if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag)) { ok = false; break; }
-        tc_fence_after();
-        const uint32_t dt = tmem + (uint32_t)(a * TC_TILE_N);
-        for (int ks = 0; ks < nks; ks++, g++) {
-          const int s = (int)(g % S);
-          const uint32_t use = (uint32_t)(g / S);
-          if (!mbar_wait(&full[s], use & 1, abort_flag)) { ok = false; break; }
-          tc_fence_after();
-          const uint32_t sb = smem_u32(Stg + (size_t)s * STAGE_BYTES);
-          if (ks < nkb) {
-            const uint32_t sa = smem_u32(Qs + ks * QBLK_BYTES);
-#pragma unroll
-            for (int kk = 0; kk < 4; kk++)
-              umma_bf16(dt, desc_k_sw128(sa + kk * 32), desc_k_sw128(sb + kk * 32), idesc,
-                        (ks > 0 || kk > 0) ? 1u : 0u);
-          } else {
-            umma_bf16(dt, desc_k_sw32(smem_u32(Qn)), desc_k_sw32(sb), idesc, 1u);
-          }
-          umma_commit(&empty[s]);
-        }
-        if (!ok) break;
-        umma_commit(&tfull[a]);
-      }
-    }
-  } else {
-    // ---------------- selection warps
-    const int ew = warp - 2;               // 0..7
-    const int grp = warp & 3;              // TMEM lane group this warp may access
-    const int half = ew >> 2;              // column half
-    const int row = grp * 32 + lane;
-    const long qrow = q0 + row;
-    const bool rvalid = qrow < nq;
-    const int tslot = ew * 32 + lane;      // 0..255
-    float lmax = INFINITY, thr = NAN;
-    constexpr int CR = (C <= 16) ? C : 1;  // register lists up to 16 entries
-    float RL[CR];
-    int RI[CR];
-#pragma unroll
-    for (int s = 0; s < CR; s++) { RL[s] = INFINITY; RI[s] = 0x7fffffff; }
-    int *Li = reinterpret_cast<int *>(Lv + (MODE != SCAN_THRESH && C > 16 ? N_EPI * C : 0));
-    if (MODE != SCAN_THRESH && C > 16) {
-      for (int s = 0; s < C; s++) { Lv[s * N_EPI + tslot] = INFINITY; Li[s * N_EPI + tslot] = 0x7fffffff; }
-    }
-    if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
-    int rcount = 0;  // THRESH: hits of this thread's region (chunk, half, query)
-    const long rbase = (long)(blockIdx.y * 2 + half) * nq + qrow;
-    const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
-
-    // one 32-column chunk already in registers: mask, cheap bound test, then
-    // (rarely) the per-element update; every index is static (no local memory)
-    auto process = [&](const uint32_t (&r)[32], int jc) {
-      float v[32];
-#pragma unroll
-      for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-      if (jc + 32 > nb) {
-#pragma unroll
-        for (int i = 0; i < 32; i++)
-          if (jc + i >= nb) v[i] = NAN;
-      }
-      if (!rvalid) return;
-      // four 8-column groups: a group is scanned element by element only when
-      // its minimum passes the bound (true when min < bound or min is NaN)
-#pragma unroll
-      for (int g = 0; g < 4; g++) {
-        const float mg = fmin3(fmin3(v[8 * g], v[8 * g + 1], v[8 * g + 2]),
-                               fmin3(v[8 * g + 3], v[8 * g + 4], v[8 * g + 5]),
-                               fminf(v[8 * g + 6], v[8 * g + 7]));
-        if (MODE == SCAN_TOPV) {
-          if (!(mg >= lmax)) {
-#pragma unroll
-            for (int i = 8 * g; i < 8 * g + 8; i++) {
-              float x = v[i];
-              if (x < lmax) {  // min/max bubble, values only
-#pragma unroll
-                for (int z = 0; z < CR; z++) {
-                  const float lo = fminf(RL[z], x);
-                  x = fmaxf(RL[z], x);
-                  RL[z] = lo;
-                }
-                lmax = RL[CR - 1];
-              }
-            }
-          }
-        } else if (MODE == SCAN_TOPC) {
-          if (!(mg >= lmax)) {
-#pragma unroll
-            for (int i = 8 * g; i < 8 * g + 8; i++) {
-              const float x = v[i];
-              if (x < lmax) {
-                if (C <= 16) {
-                  reg_insert<CR>(RL, RI, x, jc + i);
-                  lmax = RL[CR - 1];
-                } else {
-                  int p = C - 1;
-                  while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
-                    Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
-                    Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
-                    p--;
-                  }
-                  Lv[p * N_EPI + tslot] = x;
-                  Li[p * N_EPI + tslot] = jc + i;
-                  lmax = Lv[(C - 1) * N_EPI + tslot];
-                }
-              }
-            }
-          }
-        } else {
-          if (!(mg > thr)) {
-#pragma unroll
-            for (int i = 8 * g; i < 8 * g + 8; i++) {
-              if (v[i] <= thr) {
-                if (rcount < sel.cap) {
-                  sel.candv[rbase * sel.cap + rcount] = v[i];
-                  sel.candi[rbase * sel.cap + rcount] = jc + i;
-                }
-                rcount++;
-              }
-            }
-          }
-        }
-      }
-    };
-
-    int it = 0;
-    bool ok = true;
-    for (int t = t_begin; t < t_end; t++, it++) {
-      const int a = it & 1;
-      const uint32_t u = (uint32_t)(it >> 1);
-      ok = mbar_wait(&tfull[a], u & 1, abort_flag);
-      __syncwarp();
-      if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
-      tc_fence_after();
-      const uint32_t tcol = tmem + lane_base + (uint32_t)(a * TC_TILE_N + half * 128);
-      const int j0 = t * TC_TILE_N + half * 128;
-      // two register sets: the load of chunk c+1 is in flight while chunk c is
-      // scanned; the loop keeps one copy of the chunk code per register set
-      uint32_t ra[32], rb[32];
-      tmem_ld32(tcol, ra);
-      tmem_ld_wait(ra);
-#pragma unroll 1
-      for (int cc = 0; cc < 2; cc++) {
-        tmem_ld32(tcol + (uint32_t)(64 * cc + 32), rb);
-        process(ra, j0 + 64 * cc);
-        tmem_ld_wait(rb);
-        if (cc == 0) {
-          tmem_ld32(tcol + 64, ra);
-        } else {
-          // every load of this accumulator is complete: hand it back to the MMA warp
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[a]);
-        }
-        process(rb, j0 + 64 * cc + 32);
-        if (cc == 0) tmem_ld_wait(ra);
-      }
-    }
-    (void)ok;
-    if (MODE == SCAN_THRESH && rvalid) sel.cnt[rbase] = rcount;
-    if (MODE != SCAN_THRESH) {
-      // merge the two column halves of each row
-      int *Xi = reinterpret_cast<int *>(Lv + 128 * C);
-      if (C <= 16 && half == 1) {
-#pragma unroll
-        for (int s = 0; s < CR; s++) { Lv[row * C + s] = RL[s]; Xi[row * C + s] = RI[s]; }
-      }
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      if (half == 0 && rvalid) {
-        const long o = ((long)blockIdx.y * nq + qrow) * C;
-        int ia = 0, ib = 0;
-        for (int s = 0; s < C; s++) {
-          float va, vb;
-          int xa, xb;
-          if (C <= 16) {
-            va = INFINITY; xa = 0x7fffffff;
-#pragma unroll
-            for (int z = 0; z < CR; z++) if (z == ia) { va = RL[z]; xa = RI[z]; }
-            vb = ib < C ? Lv[row * C + ib] : INFINITY;
-            xb = ib < C ? Xi[row * C + ib] : 0x7fffffff;
-          } else {
-            const int pt = tslot + 128;
-            va = ia < C ? Lv[ia * N_EPI + tslot] : INFINITY;
-            xa = ia < C ? Li[ia * N_EPI + tslot] : 0x7fffffff;
-            vb = ib < C ? Lv[ib * N_EPI + pt] : INFINITY;
-            xb = ib < C ? Li[ib * N_EPI + pt] : 0x7fffffff;
-          }
-          const bool takeA = ia < C && (ib >= C || va < vb || (va == vb && xa <= xb));
-          const float vo = takeA ? va : vb;
-          const int xo = takeA ? xa : xb;
-          sel.topv[o + s] = vo;
-          sel.topi[o + s] = (xo == 0x7fffffff) ? -1 : xo;
-          if (takeA) ia++; else ib++;
-        }
-      }
-    }
-  }
-
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  if (warp == 1) {
-    __syncwarp();
-    tmem_dealloc(tmem, TMEM_COLS);
-  }
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_err, 1);
-}
-
-// ---------------- host side
-
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-
-int get_encode() {
-  if (g_encode) return OK;
-  void *fn = nullptr;
-  cudaDriverEntryPointQueryResult qr;
-  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
-                                                   cudaEnableDefault, &qr);
-  if (e != cudaSuccess || qr != cudaDriverEntryPointSuccess || !fn) {
-    set_error(E_CUDA, "cuTensorMapEncodeTiled unavailable (%s)", cudaGetErrorString(e));
-    return E_CUDA;
-  }
-  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-  return OK;
-}
-
-int make_map(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t rows,
-             uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows,
-             CUtensorMapSwizzle sw) {
-  YG_CHECK(get_encode());
-  if (!ptr || (reinterpret_cast<uintptr_t>(ptr) & 15) || (row_bytes & 15) || rows == 0) {
-    set_error(E_ARG, "tensor map: null / misaligned operand (ptr=%p pitch=%llu rows=%llu)", ptr,
-              (unsigned long long)row_bytes, (unsigned long long)rows);
-    return E_ARG;
-  }
-  cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {row_bytes};
-  cuuint32_t box[2] = {box_cols, box_rows};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims,
-                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    set_error(E_CUDA, "cuTensorMapEncodeTiled failed (%d): cols=%llu rows=%llu pitch=%llu",
-              (int)r, (unsigned long long)cols, (unsigned long long)rows,
-              (unsigned long long)row_bytes);
-    return E_CUDA;
-  }
-  return OK;
-}
-
-template <int MODE, int C, bool L2>
-int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
-  const int nkb = op.Kp / 64;
-  int S = 6;
-  while (S > 2 && make_layout(nkb, S, MODE, C).total > 227 * 1024) S--;
-  const Layout lay = make_layout(nkb, S, MODE, C);
-  if (lay.total > 227 * 1024) {
-    set_error(E_UNSUPPORTED, "tc_scan: shared memory %zu too large (Kp=%d C=%d)", lay.total,
-              op.Kp, C);
-    return E_UNSUPPORTED;
-  }
-  static bool attr = false;
-  if (!attr) {
-    YG_CUDA(cudaFuncSetAttribute(tc_scan_kernel<MODE, C, L2>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr = true;
-  }
-  CUtensorMap mq, mqn, mb, mbn;
-  YG_CHECK(make_map(&mq, op.q, op.Kp, nq, (uint64_t)op.Kp * 2, 64, 128,
-                    CU_TENSOR_MAP_SWIZZLE_128B));
-  YG_CHECK(make_map(&mb, op.b, op.Kp, nb, (uint64_t)op.Kp * 2 * op.b_step, 64, 256,
-                    CU_TENSOR_MAP_SWIZZLE_128B));
-  if (L2) {
-    YG_CHECK(make_map(&mqn, op.qn, 16, nq, 32, 16, 128, CU_TENSOR_MAP_SWIZZLE_32B));
-    YG_CHECK(make_map(&mbn, op.bn, 16, nb, (uint64_t)32 * op.b_step, 16, 256,
-                      CU_TENSOR_MAP_SWIZZLE_32B));
-  } else {
-    mqn = mq;
-    mbn = mb;
-  }
-  dim3 grid((unsigned)ceil_div(nq, TC_TILE_M), (unsigned)sel.nchunk);
-  tc_scan_kernel<MODE, C, L2><<<grid, NT_TC, lay.total, st>>>(mq, mqn, mb, mbn, nq, nb, nkb, S,
-                                                              sel);
-  YG_LAUNCH_CHECK();
-  return OK;
-}
-
-template <bool L2>
-int dispatch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
-  if (sel.mode == SCAN_THRESH) return launch<SCAN_THRESH, 1, L2>(op, nq, nb, sel, st);
-  switch (sel.C) {
-    case 1: return launch<SCAN_TOPC, 1, L2>(op, nq, nb, sel, st);
-    case 2: return launch<SCAN_TOPC, 2, L2>(op, nq, nb, sel, st);
-    case 4: return launch<SCAN_TOPC, 4, L2>(op, nq, nb, sel, st);
-    case 8: return launch<SCAN_TOPC, 8, L2>(op, nq, nb, sel, st);
-    case 16:
-      if (sel.mode == SCAN_TOPV) return launch<SCAN_TOPV, 16, L2>(op, nq, nb, sel, st);
-      return launch<SCAN_TOPC, 16, L2>(op, nq, nb, sel, st);
-    case 32: return launch<SCAN_TOPC, 32, L2>(op, nq, nb, sel, st);
-  }
-  set_error(E_ARG, "tc_scan: unsupported list length C=%d", sel.C);
-  return E_ARG;
-}
-
-}  // namespace
-
-bool tc_supported(int d) { return d >= 1 && ((d + 63) / 64) * 64 <= 256; }
+bool tc_supported(int d) { return d >= 1; }
 
 int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Workspace &ws,
                        int slot_pack, int slot_norm, TcOperands *op, double *qn64,
-                       unsigned char *qflag, float *qres, cudaStream_t st) {
-  const int Kp = ((d + 63) / 64) * 64;
+                       unsigned char *qflag, float *qres, int split, float *lonorm,
+                       cudaStream_t st) {
+  const int Kp1 = ((d + 63) / 64) * 64, Kp = split ? 3 * Kp1 : Kp1;
   void *pack, *norm = nullptr;
   YG_CHECK(ws.get(slot_pack, (size_t)nq * Kp * 2, &pack));
   if (metric == METRIC_L2) YG_CHECK(ws.get(slot_norm, (size_t)nq * 32, &norm));
-  YG_CHECK(prep_rows(q, ldq, nq, d, metric == METRIC_L2 ? -2.f : 1.f, qn64, nullptr, qflag, qres,
-                     (__nv_bfloat16 *)pack, Kp, (__nv_bfloat16 *)norm,
-                     metric == METRIC_L2 ? 2 : 0, nullptr, st));
+  const float scale = metric == METRIC_L2 ? -2.f : 1.f;
+  const int nmode = metric == METRIC_L2 ? 2 : 0;
+  if (split)
+    YG_CHECK(prep_rows_split(q, ldq, nq, d, scale, 0, qn64, nullptr, qflag, lonorm, qres,
+                             (__nv_bfloat16 *)pack, Kp1, (__nv_bfloat16 *)norm, nmode, nullptr,
+                             st));
+  else
+    YG_CHECK(prep_rows(q, ldq, nq, d, scale, qn64, nullptr, qflag, qres, (__nv_bfloat16 *)pack,
+                       Kp, (__nv_bfloat16 *)norm, nmode, nullptr, st));
   op->d = d;
   op->Kp = Kp;
   op->metric = metric;
+  op->split = split;
   op->q = (const __nv_bfloat16 *)pack;
   op->qn = (const __nv_bfloat16 *)norm;
   return OK;
@@ -489,18 +34,23 @@ int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Work
 
 int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspace &ws,
                     int slot_pack, int slot_norm, int slot_res, TcOperands *op, float *bn32,
-                    SetStats *bs, cudaStream_t st) {
-  const int Kp = ((d + 63) / 64) * 64;
+                    SetStats *bs, int split, cudaStream_t st) {
+  const int Kp1 = ((d + 63) / 64) * 64, Kp = split ? 3 * Kp1 : Kp1;
   void *pack, *norm = nullptr, *res;
   YG_CHECK(ws.get(slot_pack, (size_t)nb * Kp * 2, &pack));
   if (metric == METRIC_L2) YG_CHECK(ws.get(slot_norm, (size_t)nb * 32, &norm));
   YG_CHECK(ws.get(slot_res, (size_t)nb * 4, &res));
-  YG_CHECK(prep_rows(b, ldb, nb, d, 1.f, nullptr, bn32, nullptr, (float *)res,
-                     (__nv_bfloat16 *)pack, Kp, (__nv_bfloat16 *)norm,
-                     metric == METRIC_L2 ? 1 : 0, bs, st));
+  const int nmode = metric == METRIC_L2 ? 1 : 0;
+  if (split)
+    YG_CHECK(prep_rows_split(b, ldb, nb, d, 1.f, 1, nullptr, bn32, nullptr, nullptr, (float *)res,
+                             (__nv_bfloat16 *)pack, Kp1, (__nv_bfloat16 *)norm, nmode, bs, st));
+  else
+    YG_CHECK(prep_rows(b, ldb, nb, d, 1.f, nullptr, bn32, nullptr, (float *)res,
+                       (__nv_bfloat16 *)pack, Kp, (__nv_bfloat16 *)norm, nmode, bs, st));
   op->d = d;
   op->Kp = Kp;
   op->metric = metric;
+  op->split = split;
   op->b = (const __nv_bfloat16 *)pack;
   op->bn = (const __nv_bfloat16 *)norm;
   op->b_rows = nb;
@@ -517,24 +67,9 @@ int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out)
 
 int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
   if (nq <= 0 || nb <= 0) return OK;
-  if (!tc_supported(op.d)) {
-    set_error(E_UNSUPPORTED, "tc_scan: d=%d not supported on the tensor-core path", op.d);
-    return E_UNSUPPORTED;
-  }
-  if (op.metric == METRIC_L2) return dispatch<true>(op, nq, nb, sel, st);
-  return dispatch<false>(op, nq, nb, sel, st);
-}
-
-int tc_take_error(cudaStream_t st) {
-  int h = 0, z = 0;
-  YG_CUDA(cudaMemcpyFromSymbolAsync(&h, g_tc_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
-  YG_CUDA(cudaMemcpyToSymbolAsync(g_tc_err, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st));
-  YG_CUDA(cudaStreamSynchronize(st));
-  if (h) {
-    set_error(E_TIMEOUT, "tensor-core pass gave up waiting (bounded wait expired)");
-    return E_TIMEOUT;
-  }
-  return OK;
+  if (op.Kp > 256) return tc_dispatch_streaming(op, nq, nb, sel, st);
+  if (op.metric == METRIC_L2) return tck::dispatch<true, false>(op, nq, nb, sel, st);
+  return tck::dispatch<false, false>(op, nq, nb, sel, st);
 }
 
 }  // namespace yg

@@ -25,26 +25,28 @@ struct TcOperands {
   const __nv_bfloat16 *bn = nullptr;  // [rows][16] (L2)
   long b_rows = 0;                    // packed base rows
   long b_step = 1;                    // scan row j reads packed row j*b_step
+  int split = 0;                      // 1: 3xBF16 split packing (Kp = 3 * Kp1)
+  int *err = nullptr;                 // device flag set when a bounded wait expires
 };
 
-// true when the tensor-core pass handles this dimension (query tile resident
-// in shared memory: Kp <= 256)
+// true when the tensor-core pass handles this dimension (any d: a query tile
+// of Kp <= 256 stays resident in shared memory, larger ones are streamed)
 bool tc_supported(int d);
 
+// split = 0: bf16 packing; split = 1: 3xBF16 split packing (prep.cuh); lonorm
+// (split only) receives ||lo|| per row
 int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Workspace &ws,
                        int slot_pack, int slot_norm, TcOperands *op, double *qn64,
-                       unsigned char *qflag, float *qres, cudaStream_t st);
+                       unsigned char *qflag, float *qres, int split, float *lonorm,
+                       cudaStream_t st);
 
 int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspace &ws,
                     int slot_pack, int slot_norm, int slot_res, TcOperands *op, float *bn32,
-                    SetStats *bs, cudaStream_t st);
+                    SetStats *bs, int split, cudaStream_t st);
 
 // strided view of the packed base (every stride-th row, nrows rows)
 int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out);
 
 int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
-
-// nonzero if a tensor-core pass gave up on a wait since the last call
-int tc_take_error(cudaStream_t st);
 
 }  // namespace yg
