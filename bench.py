@@ -188,7 +188,12 @@ def run_clustering(args, world, rank, local):
         assign = torch.empty(n, dtype=torch.int32, device="cuda")
         flags = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
 
+        libc = ctypes.CDLL(None)
+
         def run(prec):
+            # seed 0 draws the k-means seed from lrand48(): reset its state so
+            # every form clusters from the same seed
+            libc.srand48(ctypes.c_long(0))
             o = yg.KmeansOpts(prec, 1, None, 0, 0, 0, 0, 0, 0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -199,7 +204,7 @@ def run_clustering(args, world, rank, local):
             assert o.status == 0, yg.last_error()
             return q, dt, o
 
-        run(yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32)  # warm-up (and lrand48 draw)
+        run(yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32)  # warm-up
         prec = yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32
         l0 = L.yael_gpu_launch_count()
         q, dt, o = run(prec)
@@ -216,7 +221,8 @@ def run_clustering(args, world, rank, local):
                                    + "), random init", "n": n, "d": d, "k": k},
             "qerr": q, "assign_ms_per_iter": o.ms_assign / max(1, o.iterations),
             "update_ms_per_iter": o.ms_update / max(1, o.iterations),
-            "fallback_points": int(o.n_fallback), "second_pass_points": int(o.n_second),
+            "fallback_points": int(o.n_fallback), "band_pass_points": int(o.n_band),
+            "split_pass_points": int(o.n_second),
             "gpu_launches": launches,
             "plain_fp32": {"value": o32.iterations / dt32, "qerr": q32,
                            "assign_ms_per_iter": o32.ms_assign / max(1, o32.iterations),

@@ -207,7 +207,10 @@ typedef struct {
   float ms_sample;  /* threshold-estimation pass over the base sample */
   float ms_rerank;  /* re-rank + certificate */
   int scan_launches; /* launches of the main pass included in ms_scan */
-  int n_second;     /* BF16-rejected queries settled by the FP32 pass (before any fallback) */
+  int n_second;     /* queries re-run through the 3xBF16 split pass */
+  int n_band;       /* rejected queries re-run through a band pass (thresholds from the
+                       k-th exact distance the first re-rank found) */
+  float ms_second;  /* band, split and exhaustive passes together */
 } yael_gpu_knn_opts;
 
 /* k-NN with explicit options.  Same result contract as knn_full. */
@@ -222,9 +225,10 @@ typedef struct {
   int status;      /* YAEL_GPU_OK or an error code (then the return value is -2) */
   long iterations; /* total Lloyd iterations over all runs */
   long n_fallback; /* points recomputed by the exhaustive FP64 path */
-  long n_second;   /* points the BF16 pass could not certify, settled by the FP32 pass */
+  long n_second;   /* points re-run through the 3xBF16 split pass */
   float ms_assign; /* GPU time of the assignment steps */
   float ms_update; /* GPU time of counts, sums, splits' uploads and objective */
+  long n_band;     /* points re-run through a band pass */
 } yael_gpu_kmeans_opts;
 
 /* kmeans() with options; returns -2 on error (message: yael_gpu_last_error). */

@@ -220,3 +220,26 @@ def test_split_pass_settles_bf16_rejections():
     assert st["n_fallback"] <= 5
     st = assert_exact(v, q, 3, "bf16")
     assert st["n_fallback"] <= 5
+
+
+def shell_data(nb=4000, nq=64, d=64, seed=41):
+    """Base rows on thin shells around a far-away centre: the BF16 error bound
+    dwarfs the spread of the distances, so every later-chance pass runs."""
+    rng = np.random.default_rng(seed)
+    c = rng.standard_normal(d) * 3.0
+    u = rng.standard_normal((nb, d))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = 1.0 + 0.5 * rng.random(nb)
+    b = (c + r[:, None] * u).astype(np.float32)
+    q = (c + 1e-3 * rng.standard_normal((nq, d))).astype(np.float32)
+    return b, q
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
+@pytest.mark.parametrize("k", [1, 5])
+def test_later_chance_chain(prec, k):
+    b, q = shell_data()
+    st = assert_exact(b, q, k, prec)
+    assert st["n_fallback"] <= 2
+    if prec == "bf16":
+        assert st["n_band"] > 0 and st["n_second"] > 0

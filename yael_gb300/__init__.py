@@ -41,7 +41,7 @@ class KmeansOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("device_ptrs", c_int), ("stream", P), ("status", c_int),
                 ("iterations", c_long), ("n_fallback", c_long), ("n_second", c_long),
                 ("ms_assign", c_float),
-                ("ms_update", c_float)]
+                ("ms_update", c_float), ("n_band", c_long)]
 
 
 class Hkm(ctypes.Structure):
@@ -54,7 +54,7 @@ class KnnOpts(ctypes.Structure):
                 ("stream", P), ("n_fallback", c_int), ("n_candidates", c_int),
                 ("exact_class", c_int), ("timing", c_int), ("ms_scan", c_float),
                 ("ms_sample", c_float), ("ms_rerank", c_float), ("scan_launches", c_int),
-                ("n_second", c_int)]
+                ("n_second", c_int), ("n_band", c_int), ("ms_second", c_float)]
 
 
 # name -> (restype, argtypes); every symbol of include/yael_gpu.h
@@ -157,7 +157,8 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
         raise RuntimeError(f"yael_gpu_knn_ex failed ({rc}): {last_error()}")
     if stats:
         return idx, dis, {"n_fallback": opts.n_fallback, "n_candidates": opts.n_candidates,
-                          "exact_class": opts.exact_class, "n_second": opts.n_second}
+                          "exact_class": opts.exact_class, "n_second": opts.n_second,
+                          "n_band": opts.n_band, "ms_second": opts.ms_second}
     return idx, dis
 
 
@@ -208,7 +209,7 @@ def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
     res = centroids if output == "centroids" else (centroids, qerr, dis, assign, nassign)
     if stats:
         return res, {"iterations": opts.iterations, "n_fallback": opts.n_fallback,
-                     "n_second": opts.n_second,
+                     "n_second": opts.n_second, "n_band": opts.n_band,
                      "ms_assign": opts.ms_assign, "ms_update": opts.ms_update}
     return res
 

@@ -91,6 +91,9 @@ int ctx_get(Ctx **out);
 // (x = hi + lo), about 2^-16 relative error instead of 2^-8
 enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1, PREC_BF16X3 = 2 };
 int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), default fp32
+// YAEL_GPU_TRACE set (and not "0"): every k-NN pass is timed with CUDA events
+// and reported on stderr, one line per pass
+bool trace_enabled();
 
 // ---------------------------------------------------------------------------
 // device helpers

@@ -155,7 +155,7 @@ struct Engine {
   std::vector<KmSlice> hsl;
   std::vector<int> hcounts;
   std::vector<double> hpart;
-  long n_fallback = 0, n_second = 0;
+  long n_fallback = 0, n_second = 0, n_band = 0;
   float ms_assign = 0, ms_update = 0;
 
   int setup() {
@@ -239,16 +239,25 @@ struct Engine {
     return OK;
   }
 
+  // When the BF16 certificate rejects more than a quarter of the points, the
+  // band and split passes that settle them cost more than running the whole
+  // assignment on the 3xBF16 split operands; later iterations see similar
+  // centroid geometry, so the switch is kept for the rest of the run.
+  bool split_assign = false;
+
   int assign_step() {
     if (in.size() == 1 && k > kSmallK) {
       KnnJob job;
       job.nq = in[0].n; job.nb = k; job.d = d; job.k = 1; job.metric = METRIC_L2;
-      job.prec = prec;
+      job.prec = (prec == PREC_BF16 && split_assign) ? PREC_BF16X3 : prec;
       job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
       job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
       YG_CHECK(knn_device(job, ctx, st));
       n_fallback += job.n_fallback;
       n_second += job.n_second;
+      n_band += job.n_band;
+      if (job.prec == PREC_BF16 && 4L * (job.n_band + job.n_fallback) > (long)job.nq)
+        split_assign = true;
       return OK;
     }
     return km_assign_small(work, nwork, v, d, C, k, active, assign, dis, st);
@@ -410,7 +419,8 @@ int kmeanspp(Ctx *ctx, cudaStream_t st, const float *v, int d, int nsub, int k, 
 int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, long seed_in,
                int redo, float *C_out, float *dis_out, int *assign_out, int *nassign_out,
                int prec, bool dev, cudaStream_t st_in, float *ret_out, long *iters_out,
-               long *fallback_out, long *second_out, float *ms_assign, float *ms_update) {
+               long *fallback_out, long *second_out, float *ms_assign, float *ms_update,
+               long *band_out = nullptr) {
   Ctx *ctx;
   YG_CHECK(ctx_get(&ctx));
   cudaStream_t st = st_in ? st_in : ctx->stream;
@@ -523,6 +533,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
   if (iters_out) *iters_out = iter_tot;
   if (fallback_out) *fallback_out = E.n_fallback;
   if (second_out) *second_out = E.n_second;
+  if (band_out) *band_out = E.n_band;
   if (ms_assign) *ms_assign = E.ms_assign;
   if (ms_update) *ms_update = E.ms_update;
   *ret_out = core_ret < 0 ? -1.f : (float)(best / n);
@@ -729,15 +740,16 @@ float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int fla
     st = (cudaStream_t)opts->stream;
   }
   float ret = -1;
-  long iters = 0, fb = 0, sec = 0;
+  long iters = 0, fb = 0, sec = 0, bd = 0;
   float ma = 0, mu = 0;
   const int rc = kmeans_run(d, n, k, niter, v, flags, seed, redo, centroids, dis, assign,
-                            nassign, prec, dev, st, &ret, &iters, &fb, &sec, &ma, &mu);
+                            nassign, prec, dev, st, &ret, &iters, &fb, &sec, &ma, &mu, &bd);
   if (opts) {
     opts->status = rc;
     opts->iterations = iters;
     opts->n_fallback = fb;
     opts->n_second = sec;
+    opts->n_band = bd;
     opts->ms_assign = ma;
     opts->ms_update = mu;
   }

@@ -2,6 +2,7 @@
 // selection -> re-rank + certificate -> exhaustive fallback) and the nn.h
 // drop-in entry points (yael/nn.h:41-83).
 #include <math.h>
+#include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
@@ -62,6 +63,26 @@ __global__ void scatter_rows_kernel(const int *sidx, const float *sdis, const in
   ddis[o] = sdis[i];
 }
 
+// k-th bounds of the compacted queries: the smaller of the bound the pass was
+// given (band passes) and the one its re-rank found
+__global__ void gather_kth_kernel(const float *in_kth, const float *out_kth, const int *map, int n,
+                                  float *dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float o = out_kth[map[i]];
+  dst[i] = in_kth ? fminf(in_kth[map[i]], o) : o;
+}
+
+// per-thread list length of a TOPC pass: k when the distances are exact, else
+// an oversampled list whose extra entries give the certificate its margin (k = 1
+// keeps two: longer lists make the epilogue's insertions the bottleneck, and
+// the band pass settles what they would have)
+int list_length(int k, int exact) {
+  if (exact) return k;
+  if (k == 1) return 2;
+  return k <= 4 ? 8 : 2 * k;
+}
+
 __global__ void fill_f32(float *p, long n, float v) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -100,6 +121,28 @@ int scan(const KnnJob &job, const float *q, int nq, const float *b, long ldb, in
   if (job.prec != PREC_FP32) return tc_scan(*tc, nq, nb, sel, st);
   return simt_scan(q, job.ldq, nq, b, ldb, nb, job.d, bn, bn_stride, job.metric, sel, st);
 }
+
+// Candidate layout of a band pass over nq queries: chunks of the base and the
+// per-region capacity.  A band holds every base row whose exact distance can
+// still be <= the query's k-th; ctot bounds its size (more fails the query).
+struct BandLayout {
+  int nchunk, tiles_per_chunk, cap;
+  size_t bytes_per_query() const { return (size_t)nchunk * 2 * cap * 8 + nchunk * 8 + 64; }
+};
+
+BandLayout band_layout(int nq, int nb, int k, int tile_m, int tile_n, int num_sms) {
+  const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
+  BandLayout L;
+  L.nchunk = imin(choose_chunks(nqt, ntb, num_sms, 1, 4), 1024);
+  L.tiles_per_chunk = (int)ceil_div(ntb, L.nchunk);
+  L.nchunk = (int)ceil_div(ntb, L.tiles_per_chunk);
+  const int ctot = imin(kMaxCandidates / 2, imax(512, 4 * k));
+  L.cap = pow2_at_least(imax(8, 2 * ctot / (2 * L.nchunk)));
+  return L;
+}
+
+int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bops,
+                int bexact);
 
 // one batch of queries (all buffers sized for nq of this batch)
 int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bops,
@@ -146,7 +189,12 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   ra.qn64 = qn64; ra.eps = eps; ra.qexact = qexact; ra.bstats = &dsmall->bs;
   ra.out_idx = job.out_idx; ra.out_dis = job.out_dis;
   ra.fail_list = fail_list; ra.fail_cnt = &dsmall->fail_cnt; ra.n_cand = &dsmall->n_cand;
+  float *kth;
+  YG_CHECK(ws_get(ws, WS_KTH, nq, &kth));
+  ra.kth_out = kth;
+  const bool band = job.band_kth != nullptr;
 
+  const bool timed = job.timing || trace_enabled();
   const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N;
   const int tile_m = bf16 ? TC_TILE_M : 128;
   const int nqt = (int)ceil_div(nq, tile_m);
@@ -154,11 +202,11 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   const int ctas_per_sm = 1;
   // oversampling for inexact distances: the certificate needs a margin between
   // the k-th exact value and the first excluded candidate
-  const int c_needed = bstats_exact ? k : (k <= 4 ? 8 : 2 * k);
+  const int c_needed = list_length(k, bstats_exact);
 
   std::unique_ptr<PassTimer> tm_scan, tm_sample;
   ScanSel sel;
-  if (c_needed <= 16) {
+  if (!band && c_needed <= 16) {
     // ---- TOPC over the full base (register lists)
     sel.mode = SCAN_TOPC;
     sel.C = pow2_at_least(c_needed);
@@ -168,7 +216,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     YG_CHECK(ws_get(ws, WS_TOPV, (size_t)sel.nchunk * nq * sel.C, &sel.topv));
     YG_CHECK(ws_get(ws, WS_TOPI, (size_t)sel.nchunk * nq * sel.C, &sel.topi));
-    tm_scan.reset(new PassTimer(job.timing, st, &job.ms_scan));
+    tm_scan.reset(new PassTimer(timed, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
     tm_scan->stop(st);
     job.scan_launches++;
@@ -188,7 +236,14 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     const int nreg = sel.nregion();
-    if (nb <= kMaxCandidates || ns < 4 * c) {
+    if (band) {
+      // thresholds from the k-th exact distance an earlier pass found
+      const BandLayout L = band_layout(nq, nb, k, tile_m, tile_n, ctx->num_sms);
+      sel.nchunk = L.nchunk;
+      sel.tiles_per_chunk = L.tiles_per_chunk;
+      sel.cap = L.cap;
+      YG_CHECK(band_thresholds(nq, job.metric, job.band_kth, qn64, eps, thr, st));
+    } else if (nb <= kMaxCandidates || ns < 4 * c) {
       // every base row is a candidate; each region holds at most half of its chunk
       sel.cap = pow2_at_least(imax(1, sel.tiles_per_chunk * tile_n / 2));
       fill_f32<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(thr, nq, INFINITY);
@@ -206,7 +261,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       ss.nchunk = (int)ceil_div(nts, ss.tiles_per_chunk);
       YG_CHECK(ws_get(ws, WS_STOPV, (size_t)ss.nchunk * nq * c, &ss.topv));
       YG_CHECK(ws_get(ws, WS_STOPI, (size_t)ss.nchunk * nq * c, &ss.topi));
-      tm_sample.reset(new PassTimer(job.timing, st, &job.ms_sample));
+      tm_sample.reset(new PassTimer(timed, st, &job.ms_sample));
       if (bf16) {
         TcOperands tcs = tcq;
         YG_CHECK(tc_base_view(tcq, stride, ns, &tcs));
@@ -219,34 +274,62 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       YG_CHECK(thresh_from_sample(nq, ss.nchunk, c, c, ss.topv, eps, thr, st));
     }
     sel.thr = thr;
-    YG_CHECK(ws_get(ws, WS_CNT, (size_t)nreg * nq, &sel.cnt));
-    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nreg * nq * sel.cap, &sel.candv));
-    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nreg * nq * sel.cap, &sel.candi));
-    tm_scan.reset(new PassTimer(job.timing, st, &job.ms_scan));
+    const int nr = sel.nregion();
+    YG_CHECK(ws_get(ws, WS_CNT, (size_t)nr * nq, &sel.cnt));
+    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nr * nq * sel.cap, &sel.candv));
+    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nr * nq * sel.cap, &sel.candi));
+    tm_scan.reset(new PassTimer(timed, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
     tm_scan->stop(st);
     job.scan_launches++;
   }
   ra.sel = sel;
-  PassTimer tr(job.timing, st, &job.ms_rerank);
+  PassTimer tr(timed, st, &job.ms_rerank);
   YG_CHECK(rerank(ra, st));
   tr.stop(st);
 
-  // ---- exhaustive path for the queries the certificate rejected
+  // ---- later chances for the queries the certificate rejected
   Small hs;
   YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
   YG_CUDA(cudaStreamSynchronize(st));
   if (tm_scan) tm_scan->collect();
   if (tm_sample) tm_sample->collect();
   tr.collect();
-  job.n_fallback += hs.fail_cnt;
   job.n_cand = (long long)hs.n_cand;
-  if (hs.fail_cnt > 0 && job.prec == PREC_BF16 && job.w == nullptr) {
-    // second chance for the rejected queries: the 3xBF16 split pass, whose
-    // error bound is ~2^-8 of the BF16 one, on a compacted copy of just those
-    // queries (queries it also rejects go to the exhaustive FP64 path)
-    const int nf = hs.fail_cnt;
-    if (!bops->has_split) {
+  const int nf = hs.fail_cnt;
+  if (trace_enabled())
+    fprintf(stderr,
+            "[yael_gpu] knn level=%d prec=%d pass=%s nq=%d nb=%d d=%d k=%d chunks=%d "
+            "scan=%.3fms sample=%.3fms rerank=%.3fms rejected=%d\n",
+            job.level, job.prec, band ? "band" : (sel.mode == SCAN_TOPC ? "topc" : "thresh"), nq,
+            nb, d, k, sel.nchunk, job.ms_scan, job.ms_sample, job.ms_rerank, nf);
+  if (nf == 0) return OK;
+  // A regular pass's rejections go to a band pass at the same precision: its
+  // thresholds come from the k-th exact distance the re-rank found, so it
+  // collects every row that can still be in the top k.  A BF16 band pass's
+  // rejections (bands too wide for its candidate buffers) go to a band pass on
+  // the 3xBF16 split operands, whose error bound and so whose band is ~2^-8 of
+  // the BF16 one; everything else to the exhaustive FP64 path.
+  const bool to_band = !band && job.w == nullptr;
+  const bool to_split = band && job.prec == PREC_BF16 && job.w == nullptr;
+  PassTimer t2(timed, st, &job.ms_second);
+  if ((to_band || to_split) && job.level < 4) {
+    const int base = WS_SC0 + job.level * WS_SC_PER_LEVEL;
+    int *map, *cidx;
+    float *cq, *cdis, *ckth = nullptr;
+    YG_CHECK(ws_get(ws, base + 0, nf, &map));
+    YG_CHECK(ws_get(ws, base + 1, (size_t)nf * d, &cq));
+    YG_CHECK(ws_get(ws, base + 2, (size_t)nf * k, &cidx));
+    YG_CHECK(ws_get(ws, base + 3, (size_t)nf * k, &cdis));
+    YG_CUDA(cudaMemcpyAsync(map, fail_list, sizeof(int) * nf, cudaMemcpyDeviceToDevice, st));
+    gather_rows_kernel<<<(unsigned)ceil_div((long)nf * d, 256), 256, 0, st>>>(job.q, job.ldq, map,
+                                                                            nf, d, cq);
+    YG_LAUNCH_CHECK();
+    YG_CHECK(ws_get(ws, base + 4, nf, &ckth));
+    gather_kth_kernel<<<(unsigned)ceil_div(nf, 256), 256, 0, st>>>(job.band_kth, kth, map, nf,
+                                                                  ckth);
+    YG_LAUNCH_CHECK();
+    if (to_split && !bops->has_split) {
       float *bn32s;
       YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32s));
       YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK3, WS_BNORMP3,
@@ -254,44 +337,93 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       bops->split.err = bops->plain.err;
       bops->has_split = true;
     }
-    int *map;
-    float *cq, *cdis;
-    int *cidx;
-    YG_CHECK(ws_get(ws, WS_SC_MAP, nf, &map));
-    YG_CHECK(ws_get(ws, WS_SC_Q, (size_t)nf * d, &cq));
-    YG_CHECK(ws_get(ws, WS_SC_IDX, (size_t)nf * k, &cidx));
-    YG_CHECK(ws_get(ws, WS_SC_DIS, (size_t)nf * k, &cdis));
-    YG_CUDA(cudaMemcpyAsync(map, fail_list, sizeof(int) * nf, cudaMemcpyDeviceToDevice, st));
-    gather_rows_kernel<<<(unsigned)ceil_div((long)nf * d, 256), 256, 0, st>>>(job.q, job.ldq, map,
-                                                                            nf, d, cq);
-    YG_LAUNCH_CHECK();
     KnnJob sub = job;
-    sub.prec = PREC_BF16X3;
+    sub.prec = to_split ? PREC_BF16X3 : job.prec;
+    sub.band_kth = ckth;
+    sub.level = job.level + 1;
     sub.nq = nf;
     sub.q = cq;
     sub.ldq = d;
     sub.out_idx = cidx;
     sub.out_dis = cdis;
-    sub.n_fallback = 0;
     sub.timing = 0;
-    YG_CHECK(knn_batch(sub, ctx, st, dsmall, bops, bstats_exact));
+    YG_CHECK(knn_batches(sub, ctx, st, dsmall, bops, bstats_exact));
     scatter_rows_kernel<<<(unsigned)ceil_div((long)nf * k, 256), 256, 0, st>>>(cidx, cdis, map, nf,
                                                                              k, job.out_idx,
                                                                              job.out_dis);
     YG_LAUNCH_CHECK();
-    job.n_second += nf;
-    job.n_fallback += sub.n_fallback - nf;  // only what the split pass also rejected
-    YG_CUDA(cudaStreamSynchronize(st));
-  } else if (hs.fail_cnt > 0) {
+    if (to_band) job.n_band += nf;
+    else job.n_second += nf;
+    job.n_band += sub.n_band;
+    job.n_second += sub.n_second;
+    job.n_fallback += sub.n_fallback;
+  } else {
     size_t per = exhaustive_bytes_per_query(nb);
-    size_t want = per * (size_t)hs.fail_cnt;
+    size_t want = per * (size_t)nf;
     const size_t cap_bytes = (size_t)1 << 30;
     if (want > cap_bytes) want = cap_bytes > per ? cap_bytes : per;
     void *scratch;
     YG_CHECK(ws.get(WS_EXH, want, &scratch));
-    YG_CHECK(exhaustive(hs.fail_cnt, fail_list, nb, d, k, job.metric, job.q, job.ldq, job.b,
-                        job.ldb, nullptr, job.out_idx, job.out_dis, scratch, want, st));
+    YG_CHECK(exhaustive(nf, fail_list, nb, d, k, job.metric, job.q, job.ldq, job.b, job.ldb,
+                        nullptr, job.out_idx, job.out_dis, scratch, want, st));
+    job.n_fallback += nf;
   }
+  t2.stop(st);
+  YG_CUDA(cudaStreamSynchronize(st));
+  t2.collect();
+  return OK;
+}
+
+// the queries of job in batches whose candidate buffers stay <= 2 GiB
+int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bops,
+                int bexact) {
+  const int nq = job.nq, nb = job.nb, k = job.k;
+  const bool bf16 = job.prec != PREC_FP32;
+  const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N, tile_m = bf16 ? TC_TILE_M : 128;
+  const size_t budget = (size_t)2 << 30;
+  int qbatch;
+  if (job.band_kth) {
+    qbatch = nq;
+    while (qbatch > 256 &&
+           band_layout(qbatch, nb, k, tile_m, tile_n, ctx->num_sms).bytes_per_query() *
+                   (size_t)qbatch > budget)
+      qbatch = (qbatch + 1) / 2;
+  } else {
+    const int cn = list_length(k, bexact);
+    const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
+    const int C = pow2_at_least(cn);
+    size_t per_query;
+    if (cn <= 16) {
+      const int nch = imin(choose_chunks(nqt, ntb, ctx->num_sms, 1, 4), kMaxCandidates / C);
+      per_query = (size_t)nch * C * 8 + 64;
+    } else {
+      per_query = (size_t)2 * kMaxCandidates * 8 + 64;
+    }
+    qbatch = (int)std::min<size_t>((size_t)nq, std::max<size_t>(256, budget / per_query));
+  }
+  long long ncand = 0;
+  for (int q0 = 0; q0 < nq; q0 += qbatch) {
+    KnnJob sub = job;
+    sub.nq = imin(qbatch, nq - q0);
+    sub.q = job.q + (long)q0 * job.ldq;
+    sub.out_idx = job.out_idx + (long)q0 * k;
+    sub.out_dis = job.out_dis + (long)q0 * k;
+    if (job.band_kth) sub.band_kth = job.band_kth + q0;
+    sub.n_fallback = sub.n_band = sub.n_second = 0;
+    sub.ms_scan = sub.ms_sample = sub.ms_rerank = sub.ms_second = 0;
+    sub.scan_launches = 0;
+    YG_CHECK(knn_batch(sub, ctx, st, dsmall, bops, bexact));
+    job.n_fallback += sub.n_fallback;
+    job.n_band += sub.n_band;
+    job.n_second += sub.n_second;
+    ncand = sub.n_cand;  // the device counter is cumulative
+    job.ms_scan += sub.ms_scan;
+    job.ms_sample += sub.ms_sample;
+    job.ms_rerank += sub.ms_rerank;
+    job.ms_second += sub.ms_second;
+    job.scan_launches += sub.scan_launches;
+  }
+  job.n_cand = ncand;
   return OK;
 }
 
@@ -300,10 +432,13 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
 int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   const int nq = job.nq, nb = job.nb, d = job.d, k = job.k;
   job.n_fallback = 0;
+  job.n_band = 0;
   job.n_second = 0;
   job.n_cand = 0;
   job.exact_class = 0;
-  job.ms_scan = job.ms_sample = job.ms_rerank = 0;
+  job.ms_scan = job.ms_sample = job.ms_rerank = job.ms_second = 0;
+  job.band_kth = nullptr;
+  job.level = 0;
   job.scan_launches = 0;
   if (nq < 0 || nb < 1 || d < 1 || k < 1) {
     set_error(E_ARG, "knn: invalid sizes nq=%d nb=%d d=%d k=%d", nq, nb, d, k);
@@ -374,42 +509,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   job.exact_class = bexact;
   bops.plain.err = bops.split.err = &dsmall->tc_err;
 
-  // query batches bounded by the candidate buffers (<= 2 GiB)
-  size_t per_query;
-  {
-    const int cn = bexact ? k : (k <= 4 ? 8 : 2 * k);
-    const bool bf16 = job.prec != PREC_FP32;
-    const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N, tile_m = bf16 ? TC_TILE_M : 128;
-    const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
-    int C = 1;
-    while (C < cn) C <<= 1;
-    if (cn <= 16) {
-      int nch = imin(choose_chunks(nqt, ntb, ctx->num_sms, 1, 4), kMaxCandidates / C);
-      per_query = (size_t)nch * C * 8 + 64;
-    } else {
-      per_query = (size_t)2 * kMaxCandidates * 8 + 64;
-    }
-  }
-  int qbatch = (int)std::min<size_t>((size_t)nq, std::max<size_t>(256, ((size_t)2 << 30) / per_query));
-  for (int q0 = 0; q0 < nq; q0 += qbatch) {
-    KnnJob sub = job;
-    sub.nq = imin(qbatch, nq - q0);
-    sub.q = job.q + (long)q0 * job.ldq;
-    sub.out_idx = job.out_idx + (long)q0 * k;
-    sub.out_dis = job.out_dis + (long)q0 * k;
-    sub.n_fallback = 0;
-    sub.n_second = 0;
-    sub.ms_scan = sub.ms_sample = sub.ms_rerank = 0;
-    sub.scan_launches = 0;
-    YG_CHECK(knn_batch(sub, ctx, st, dsmall, &bops, bexact));
-    job.n_fallback += sub.n_fallback;
-    job.n_second += sub.n_second;
-    job.n_cand += sub.n_cand;
-    job.ms_scan += sub.ms_scan;
-    job.ms_sample += sub.ms_sample;
-    job.ms_rerank += sub.ms_rerank;
-    job.scan_launches += sub.scan_launches;
-  }
+  YG_CHECK(knn_batches(job, ctx, st, dsmall, &bops, bexact));
   if (job.prec != PREC_FP32) {
     YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
     YG_CUDA(cudaStreamSynchronize(st));
@@ -467,6 +567,8 @@ static int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
     opts->ms_rerank = job.ms_rerank;
     opts->scan_launches = job.scan_launches;
     opts->n_second = job.n_second;
+    opts->n_band = job.n_band;
+    opts->ms_second = job.ms_second;
   }
   return OK;
 }

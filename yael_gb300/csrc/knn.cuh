@@ -16,13 +16,19 @@ struct KnnJob {
   const float *w = nullptr;  // device base weights or null
   int *out_idx = nullptr;    // device nq x k
   float *out_dis = nullptr;  // device nq x k
+  // band pass (internal): when set, a THRESH pass with per-query thresholds
+  // from band_kth[q], an upper bound of the query's k-th exact distance
+  const float *band_kth = nullptr;
+  int level = 0;  // nesting depth of the later-chance passes (workspace slots)
   // CUDA-event timing of the passes (optional)
   int timing = 0;
   float ms_scan = 0, ms_sample = 0, ms_rerank = 0;
+  float ms_second = 0;  // all later-chance passes (band, split, exhaustive)
   int scan_launches = 0;
   // filled on return
   int n_fallback = 0;   // queries recomputed by the exhaustive FP64 path
-  int n_second = 0;     // BF16-rejected queries re-run through the FP32 pass
+  int n_band = 0;       // rejected queries re-run through a band pass
+  int n_second = 0;     // queries re-run through the 3xBF16 split pass
   long long n_cand = 0;
   int exact_class = 0;
 };
@@ -35,9 +41,12 @@ enum WsSlot : int {
   WS_QN64 = 0, WS_QFLAG, WS_QRES, WS_BN32, WS_SMALL, WS_EPS, WS_QEXACT,
   WS_TOPV, WS_TOPI, WS_THR, WS_CNT, WS_FAIL, WS_STOPV, WS_STOPI, WS_EXH,
   WS_QPACK, WS_BPACK, WS_QNORMP, WS_BNORMP, WS_BRES,
-  WS_SC_MAP, WS_SC_Q, WS_SC_IDX, WS_SC_DIS, WS_QLO, WS_BPACK3, WS_BNORMP3, WS_BRES3,
+  WS_QLO = 24, WS_BPACK3, WS_BNORMP3, WS_BRES3, WS_KTH,
   WS_H_B = 40, WS_H_Q, WS_H_W, WS_H_IDX, WS_H_DIS, WS_H_EXTRA,
   WS_KM0 = 60,  // k-means / hkm slots start here
+  // compacted queries of a later-chance pass, per nesting level
+  WS_SC0 = 100,
+  WS_SC_PER_LEVEL = 5,  // + 0 map, 1 rows, 2 ids, 3 distances, 4 k-th bounds
 };
 
 }  // namespace yg

@@ -116,6 +116,14 @@ int default_precision() {
   return PREC_FP32;
 }
 
+bool trace_enabled() {
+  static const bool on = [] {
+    const char *s = getenv("YAEL_GPU_TRACE");
+    return s && *s && strcmp(s, "0") != 0;
+  }();
+  return on;
+}
+
 }  // namespace yg
 
 extern "C" const char *yael_gpu_last_error(void) { return yg::last_message(); }

@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
   }
   __syncthreads();
   const int M = sM;
+  float kth_hi = INFINITY;  // upper bound of the k-th exact distance, when found
   if (sfail || M < k || M > Mp_alloc) goto failed;
   {
     const int Mp = next_pow2(M);
@@ -174,7 +175,10 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
         const unsigned long long kk = K[k - 1];
         const unsigned long long tk = sT >> 32;
         const int tidb = (int)(sT & 0xffffffffu);
-        if (!(kk < tk || (kk == tk && (unsigned)I[k - 1] <= (unsigned)tidb))) goto failed;
+        if (!(kk < tk || (kk == tk && (unsigned)I[k - 1] <= (unsigned)tidb))) {
+          kth_hi = ord2f((unsigned)kk);  // exact values
+          goto failed;
+        }
       }
       for (int r = tid; r < k; r += RT) {
         a.out_idx[(long)q * k + r] = I[r];
@@ -260,12 +264,15 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
     const double lowest_outside = bound - (double)eps - bslack;
     const bool ok = bound_strict ? (ek_hi <= lowest_outside) : (ek_hi < lowest_outside);
     if (ok) return;
+    // widened so that it also bounds a later FP32 re-rank of the same k-th value
+    kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
     __syncthreads();
   }
 failed:
   if (tid == 0) {
     const int pos = atomicAdd(a.fail_cnt, 1);
     a.fail_list[pos] = q;
+    if (a.kth_out) a.kth_out[q] = kth_hi;
   }
 }
 
@@ -327,6 +334,7 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
   }
   const int nvalid = __popc(__ballot_sync(0xffffffffu, id != 0x7fffffff));
   bool ok = nvalid >= k;
+  float kth_hi = INFINITY;  // upper bound of the k-th exact distance, when found
   if (ok) {
     if (a.n_cand && lane == 0) atomicAdd(a.n_cand, (unsigned long long)nvalid);
     warp_sort(key, id);
@@ -337,6 +345,7 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
         const unsigned long long tk = tkey >> 32;
         const unsigned tid_b = (unsigned)(tkey & 0xffffffffu);
         ok = kk < tk || (kk == tk && (unsigned)ik <= tid_b);
+        kth_hi = ord2f((unsigned)kk);  // exact values
       }
       if (ok && lane < k) {
         a.out_idx[(long)q * k + lane] = id;
@@ -387,11 +396,13 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
       }
       const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
       ok = ek_hi < bound - (double)eps - 4e-7 * fabs(bound);
+      kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
     }
   }
   if (!ok && lane == 0) {
     const int pos = atomicAdd(a.fail_cnt, 1);
     a.fail_list[pos] = q;
+    if (a.kth_out) a.kth_out[q] = kth_hi;
   }
 }
 
@@ -477,6 +488,24 @@ __global__ void thresh_kernel(int nq, int nchunk, int C, int c, const float *top
   const double t = (double)v + 2.0 * (double)eps[q];
   thr[q] = isfinite(t) ? __double2float_ru(t * (1 + 1e-7) + (t < 0 ? -t * 2e-7 : 0.0))
                        : INFINITY;
+}
+
+__global__ void band_thr_kernel(int nq, int metric, const float *kth, const double *qn64,
+                                const float *eps, float *thr) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const double kk = (double)kth[q], e = (double)eps[q];
+  if (!isfinite(kk) || !isfinite(e)) {
+    thr[q] = INFINITY;
+    return;
+  }
+  // a row with exact distance x <= kk has approx <= x + e; its v value is
+  // approx - ||q||^2 (L2).  The 1e-6 relative margin exceeds the re-rank's
+  // 4e-7 boundary slack, so the certificate passes whenever the band held
+  // every candidate.
+  const double hi = kk + e + 1e-6 * (fabs(kk) + e);
+  const double t = metric == METRIC_L2 ? hi - qn64[q] : hi;
+  thr[q] = __double2float_ru(t);
 }
 
 // ---- exhaustive FP64 path ------------------------------------------------
@@ -666,6 +695,14 @@ int thresh_from_sample(int nq, int nchunk, int C, int c, const float *topv,
     return E_ARG;
   }
   thresh_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(nq, nchunk, C, c, topv, eps, thr);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int band_thresholds(int nq, int metric, const float *kth, const double *qn64, const float *eps,
+                    float *thr, cudaStream_t st) {
+  if (nq <= 0) return OK;
+  band_thr_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(nq, metric, kth, qn64, eps, thr);
   YG_LAUNCH_CHECK();
   return OK;
 }

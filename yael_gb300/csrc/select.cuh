@@ -34,6 +34,9 @@ struct RerankArgs {
   unsigned long long *n_cand = nullptr;  // device stats (may be null)
   int use_query_list = 0;        // when set, row r of the pass is query qlist[r]
   const int *qlist = nullptr;
+  // optional: for each rejected query, an upper bound of its k-th smallest
+  // exact distance (INFINITY when none was found), for the band pass
+  float *kth_out = nullptr;
 };
 
 int rerank(const RerankArgs &a, cudaStream_t st);
@@ -55,6 +58,13 @@ int compute_eps_split(int nq, int d, int metric, const double *qn64, const float
 // c-th smallest sampled value + 2 eps[q], rounded up.
 int thresh_from_sample(int nq, int nchunk, int C, int c, const float *topv,
                        const float *eps, float *thr, cudaStream_t st);
+
+// Band-pass thresholds: thr[q] (v space) such that every base row whose exact
+// distance is <= kth[q] has approx value <= thr[q] (kth: an upper bound of the
+// k-th exact distance of query q), widened so that the THRESH certificate
+// (k-th <= thr + ||q||^2 - eps, with its relative slack) then holds.
+int band_thresholds(int nq, int metric, const float *kth, const double *qn64, const float *eps,
+                    float *thr, cudaStream_t st);
 
 // Exhaustive exact path for the queries in qlist[0..nlist): FP64 distances to
 // all nb base rows (optionally multiplied by weights), k smallest by
