@@ -243,3 +243,26 @@ def test_later_chance_chain(prec, k):
     assert st["n_fallback"] <= 2
     if prec == "bf16":
         assert st["n_band"] > 0 and st["n_second"] > 0
+
+
+def test_cta_pair_kernel_matches():
+    """The CTA-pair form of the tensor-core pass (tcgen05 cta_group::2, chosen
+    with YAEL_GPU_TC_PAIR=1) gives the same exact results; run in a child
+    process since the switch is read once per process."""
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np, sys; sys.path.insert(0, 'tests');"
+        "from _util import knn_exact; import yael_gb300 as yg;"
+        "rng = np.random.default_rng(77);"
+        "b = rng.standard_normal((20000, 128)).astype(np.float32);"
+        "q = rng.standard_normal((700, 128)).astype(np.float32);"
+        "i1, d1 = yg.knn(q, b, nnn=10, precision='bf16');"
+        "i2, d2 = yg.knn(q, b, nnn=1, precision='bf16x3');"
+        "r1 = knn_exact(b, q, 10)[0]; r2 = knn_exact(b, q, 1)[0];"
+        "assert (i1 == r1).all() and (i2 == r2).all(); print('pair ok')")
+    env = dict(os.environ, YAEL_GPU_TC_PAIR="1")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0 and "pair ok" in r.stdout, r.stdout + r.stderr

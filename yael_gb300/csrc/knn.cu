@@ -126,18 +126,21 @@ int scan(const KnnJob &job, const float *q, int nq, const float *b, long ldb, in
 // per-region capacity.  A band holds every base row whose exact distance can
 // still be <= the query's k-th; ctot bounds its size (more fails the query).
 struct BandLayout {
-  int nchunk, tiles_per_chunk, cap;
-  size_t bytes_per_query() const { return (size_t)nchunk * 2 * cap * 8 + nchunk * 8 + 64; }
+  int nchunk, tiles_per_chunk, cap, halves;
+  size_t bytes_per_query() const {
+    return (size_t)nchunk * halves * cap * 8 + (size_t)nchunk * halves * 4 + 64;
+  }
 };
 
-BandLayout band_layout(int nq, int nb, int k, int tile_m, int tile_n, int num_sms) {
+BandLayout band_layout(int nq, int nb, int k, int tile_m, int tile_n, int halves, int num_sms) {
   const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
   BandLayout L;
+  L.halves = halves;
   L.nchunk = imin(choose_chunks(nqt, ntb, num_sms, 1, 4), 1024);
   L.tiles_per_chunk = (int)ceil_div(ntb, L.nchunk);
   L.nchunk = (int)ceil_div(ntb, L.tiles_per_chunk);
   const int ctot = imin(kMaxCandidates / 2, imax(512, 4 * k));
-  L.cap = pow2_at_least(imax(8, 2 * ctot / (2 * L.nchunk)));
+  L.cap = pow2_at_least(imax(8, 2 * ctot / (halves * L.nchunk)));
   return L;
 }
 
@@ -226,6 +229,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     // with stride = k/3 the chance that fewer than k fall below it is the
     // chance that a Poisson(3) exceeds c-1 (c = 16: ~3e-7 per query).
     sel.mode = SCAN_THRESH;
+    sel.halves = 2;
     float *thr;
     YG_CHECK(ws_get(ws, WS_THR, nq, &thr));
     const int c = 16;
@@ -238,14 +242,14 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     const int nreg = sel.nregion();
     if (band) {
       // thresholds from the k-th exact distance an earlier pass found
-      const BandLayout L = band_layout(nq, nb, k, tile_m, tile_n, ctx->num_sms);
+      const BandLayout L = band_layout(nq, nb, k, tile_m, tile_n, sel.halves, ctx->num_sms);
       sel.nchunk = L.nchunk;
       sel.tiles_per_chunk = L.tiles_per_chunk;
       sel.cap = L.cap;
       YG_CHECK(band_thresholds(nq, job.metric, job.band_kth, qn64, eps, thr, st));
     } else if (nb <= kMaxCandidates || ns < 4 * c) {
-      // every base row is a candidate; each region holds at most half of its chunk
-      sel.cap = pow2_at_least(imax(1, sel.tiles_per_chunk * tile_n / 2));
+      // every base row is a candidate; a region holds at most its share of the chunk
+      sel.cap = pow2_at_least(imax(1, sel.tiles_per_chunk * tile_n / sel.halves));
       fill_f32<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(thr, nq, INFINITY);
       YG_LAUNCH_CHECK();
     } else {
@@ -385,7 +389,8 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
   if (job.band_kth) {
     qbatch = nq;
     while (qbatch > 256 &&
-           band_layout(qbatch, nb, k, tile_m, tile_n, ctx->num_sms).bytes_per_query() *
+           band_layout(qbatch, nb, k, tile_m, tile_n, 2, ctx->num_sms)
+                       .bytes_per_query() *
                    (size_t)qbatch > budget)
       qbatch = (qbatch + 1) / 2;
   } else {

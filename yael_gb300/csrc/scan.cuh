@@ -10,9 +10,11 @@
 //             lexicographic order (strict '<' over increasing j), written to
 //             topv/topi[(chunk * nq + q) * C + s], ascending.
 //   THRESH -- every (q, j) with v <= thr[q] is appended to a candidate
-//             region owned by one thread: region r = chunk * 2 + column half,
-//             slots candv/candi[(r * nq + q) * cap + s], count cnt[r * nq + q]
-//             (all hits, including those that did not fit in cap).  No atomics:
+//             region owned by one thread: region r = chunk * halves + column
+//             half (halves = 2 for the CUDA-core producer, whose two threads
+//             of a row split the columns; 1 for the tensor-core one), slots
+//             candv/candi[(r * nq + q) * cap + s], count cnt[r * nq + q] (all
+//             hits, including those that did not fit in cap).  No atomics:
 //             each (region, query) has exactly one writer.
 #pragma once
 #include "common.cuh"
@@ -36,7 +38,8 @@ struct ScanSel {
   float *candv = nullptr;
   int *candi = nullptr;
   int cap = 0;              // THRESH: slots per (region, query)
-  __host__ __device__ int nregion() const { return nchunk * 2; }
+  int halves = 2;           // THRESH: regions per chunk (column halves of a row)
+  __host__ __device__ int nregion() const { return nchunk * halves; }
 };
 
 // FP32 CUDA-core producer.  q: nq rows (stride ldq floats); b: nb rows (stride

@@ -1,6 +1,7 @@
 // The tcgen05 BF16 distance + selection kernel and its host launcher, as
-// templates instantiated by tc_scan.cu (query tile resident in shared memory)
-// and tc_scan_qs.cu (query tile streamed with every K block, any Kp).
+// templates instantiated by tc_scan.cu / tc_scan_r2.cu (query tile resident in
+// shared memory) and tc_scan_qs.cu / tc_scan_qs2.cu (query tile streamed with
+// every K block, any Kp).
 //
 // One CTA = one 128-row query tile x one chunk of 256-row base tiles.
 //   warp 0      TMA producer: a ring of S stages, each one 64-column K block of
@@ -14,8 +15,21 @@
 //               update the per-row list (TOPC / TOPV) or append candidates
 //               (THRESH).
 // The accumulators are double-buffered so the selection of tile t overlaps the
-// MMAs of tile t+1.  All waits are bounded (tc_ptx.cuh); on expiry the kernel
-// sets *err, every role leaves its loop and TMEM is freed.
+// MMAs of tile t+1.
+//
+// PAIR: the CTAs of a query-tile pair form a cluster and run one 256x256x16
+// MMA per K step over both SMs (tcgen05 cta_group::2): each CTA holds its own
+// 128 query rows and loads only half (128 rows) of every base block, and the
+// leader CTA's MMA warp drives both tensor cores.  Per SM this halves the
+// shared-memory traffic of the base operand (read by the MMA and written by
+// TMA), which bounds the single-CTA form.  Pair protocol: the stage-full and
+// query-full barriers of the leader collect both CTAs' TMA bytes; the leader's
+// commits arrive on the stage-empty / accumulator-full barriers of both CTAs;
+// the selection warps of both CTAs arrive on the leader's accumulator-empty
+// barriers.
+//
+// All waits are bounded (tc_ptx.cuh); on expiry the kernel sets *err, every
+// role leaves its loop and TMEM is freed.
 #pragma once
 #include <cudaTypedefs.h>
 #include <math.h>
@@ -27,8 +41,6 @@ namespace yg {
 namespace tck {
 using namespace ptx;
 
-using namespace ptx;
-
 constexpr int NT_TC = 320;
 constexpr int N_EPI = 256;               // selection threads
 constexpr int STAGE_BYTES = 256 * 128;   // 256 rows x 64 bf16
@@ -37,21 +49,22 @@ constexpr int QN_BYTES = 4096;           // 128 rows x 16 bf16 (padded to 4 KB)
 constexpr int BN_BYTES = 256 * 32;       // 256 rows x 16 bf16
 constexpr int TMEM_COLS = 512;
 
-
 struct Layout {
   int nkb, S, C, mode;
   size_t q_off, qn_off, stg_off, stage_bytes, list_off, bar_off, total;
 };
 
 // qs: the query tile is streamed with each K block (stage = B block + A block)
-// instead of staying resident for the whole chunk
-__host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C, bool qs) {
+// instead of staying resident for the whole chunk; pair: a stage holds this
+// CTA's half of the base block
+__host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C, bool qs,
+                                              bool pair) {
   Layout L;
   L.nkb = nkb; L.S = S; L.mode = mode; L.C = C;
   size_t off = 0;
   L.q_off = off;   off += qs ? 0 : (size_t)nkb * QBLK_BYTES;
   L.qn_off = off;  off += qs ? 0 : QN_BYTES;
-  L.stage_bytes = STAGE_BYTES + (qs ? QBLK_BYTES : 0);
+  L.stage_bytes = (pair ? STAGE_BYTES / 2 : STAGE_BYTES) + (qs ? QBLK_BYTES : 0);
   L.stg_off = off; off += (size_t)S * L.stage_bytes;
   L.list_off = off;
   if (mode != SCAN_THRESH) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
@@ -85,7 +98,7 @@ __device__ __forceinline__ void reg_insert(float (&L)[C], int (&I)[C], float x, 
   }
 }
 
-template <int MODE, int C, bool L2, bool QS>
+template <int MODE, int C, bool L2, bool QS, bool PAIR>
 __global__ void __launch_bounds__(NT_TC, 1)
     tc_scan_kernel(const __grid_constant__ CUtensorMap mapQ,
                    const __grid_constant__ CUtensorMap mapQn,
@@ -95,8 +108,10 @@ __global__ void __launch_bounds__(NT_TC, 1)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  const Layout lay = make_layout(nkb, S, MODE, C, QS);
+  const Layout lay = make_layout(nkb, S, MODE, C, QS, PAIR);
   const size_t SB = lay.stage_bytes;
+  constexpr int BHALF = PAIR ? STAGE_BYTES / 2 : STAGE_BYTES;  // base bytes per stage, this CTA
+  constexpr int BNHALF = PAIR ? BN_BYTES / 2 : BN_BYTES;
   uint8_t *Qs = base + lay.q_off;
   uint8_t *Qn = base + lay.qn_off;
   uint8_t *Stg = base + lay.stg_off;
@@ -113,6 +128,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
   const int t_begin = blockIdx.y * sel.tiles_per_chunk;
   const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
   const int nks = nkb + (L2 ? 1 : 0);
+  const uint32_t crank = PAIR ? cluster_ctarank() : 0;
+  const bool leader = crank == 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
@@ -121,57 +138,105 @@ __global__ void __launch_bounds__(NT_TC, 1)
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(&tfull[a], 1);
-      mbar_init(&tempty[a], N_EPI / 32);
+      // the leader's MMA waits for the selection warps of both CTAs
+      mbar_init(&tempty[a], (PAIR ? 2 : 1) * (N_EPI / 32));
     }
     mbar_init(qfull, 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
   if (warp == 1) {
-    tmem_alloc(tmem_holder, TMEM_COLS);
-    tmem_relinquish();
+    if (PAIR) {
+      tmem_alloc_pair(tmem_holder, TMEM_COLS);
+      tmem_relinquish_pair();
+    } else {
+      tmem_alloc(tmem_holder, TMEM_COLS);
+      tmem_relinquish();
+    }
   }
   tc_fence_before();
   __syncthreads();
+  if (PAIR) cluster_sync();  // both CTAs' barriers exist before any remote signal
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  // barriers of the leader, as shared::cluster addresses (PAIR)
+  const uint32_t full_l = PAIR ? mapa_shared(smem_u32(full), 0) : 0;
+  const uint32_t qfull_l = PAIR ? mapa_shared(smem_u32(qfull), 0) : 0;
+  const uint32_t tempty_l = PAIR ? mapa_shared(smem_u32(tempty), 0) : 0;
 
   if (warp == 0) {
-    // ---------------- TMA producer
+    // ---------------- TMA producer (every CTA loads its own query tile and
+    // its part of each base block)
     if (lane == 0) {
       if (!QS) {
-        mbar_arrive_expect_tx(qfull, (uint32_t)(nkb * QBLK_BYTES + (L2 ? 128 * 32 : 0)));
-        for (int kb = 0; kb < nkb; kb++)
-          tma_load_2d(&mapQ, qfull, Qs + kb * QBLK_BYTES, kb * 64, (int)q0);
-        if (L2) tma_load_2d(&mapQn, qfull, Qn, 0, (int)q0);
+        const uint32_t qbytes = (uint32_t)(nkb * QBLK_BYTES + (L2 ? 128 * 32 : 0));
+        if (PAIR) {
+          if (leader) mbar_arrive_expect_tx(qfull, 2 * qbytes);
+          for (int kb = 0; kb < nkb; kb++)
+            tma_load_2d_pair(&mapQ, qfull_l, Qs + kb * QBLK_BYTES, kb * 64, (int)q0);
+          if (L2) tma_load_2d_pair(&mapQn, qfull_l, Qn, 0, (int)q0);
+        } else {
+          mbar_arrive_expect_tx(qfull, qbytes);
+          for (int kb = 0; kb < nkb; kb++)
+            tma_load_2d(&mapQ, qfull, Qs + kb * QBLK_BYTES, kb * 64, (int)q0);
+          if (L2) tma_load_2d(&mapQn, qfull, Qn, 0, (int)q0);
+        }
       }
-      long g = 0;
+      // ring position: stage sn, phase parity phn (advanced at every use)
+      int sn = 0;
+      uint32_t phn = 0;
       bool ok = true;
       for (int t = t_begin; t < t_end && ok; t++) {
-        for (int ks = 0; ks < nks; ks++, g++) {
-          const int s = (int)(g % S);
-          const uint32_t use = (uint32_t)(g / S);
-          if (!mbar_wait(&empty[s], (use & 1) ^ 1, abort_flag)) { ok = false; break; }
+        const int brow = t * TC_TILE_N + (int)crank * (TC_TILE_N / 2) * (PAIR ? 1 : 0);
+        for (int ks = 0; ks < nks; ks++) {
+          const int s = sn;
+          const uint32_t ph = phn;
+          if (++sn == S) { sn = 0; phn ^= 1; }
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) { ok = false; break; }
           uint8_t *sp = Stg + (size_t)s * SB;
-          if (ks < nkb) {
-            mbar_arrive_expect_tx(&full[s], STAGE_BYTES + (QS ? QBLK_BYTES : 0));
-            tma_load_2d(&mapB, &full[s], sp, ks * 64, t * TC_TILE_N);
-            if (QS) tma_load_2d(&mapQ, &full[s], sp + STAGE_BYTES, ks * 64, (int)q0);
+          const uint32_t tx = ks < nkb ? (uint32_t)(BHALF + (QS ? QBLK_BYTES : 0))
+                                       : (uint32_t)(BNHALF + (QS ? 128 * 32 : 0));
+          if (PAIR) {
+            const uint32_t fb = full_l + (uint32_t)(s * 8);
+            if (leader) mbar_arrive_expect_tx(&full[s], 2 * tx);
+            if (ks < nkb) {
+              tma_load_2d_pair(&mapB, fb, sp, ks * 64, brow);
+              if (QS) tma_load_2d_pair(&mapQ, fb, sp + BHALF, ks * 64, (int)q0);
+            } else {
+              tma_load_2d_pair(&mapBn, fb, sp, 0, brow);
+              if (QS) tma_load_2d_pair(&mapQn, fb, sp + BHALF, 0, (int)q0);
+            }
           } else {
-            mbar_arrive_expect_tx(&full[s], BN_BYTES + (QS ? 128 * 32 : 0));
-            tma_load_2d(&mapBn, &full[s], sp, 0, t * TC_TILE_N);
-            if (QS) tma_load_2d(&mapQn, &full[s], sp + STAGE_BYTES, 0, (int)q0);
+            mbar_arrive_expect_tx(&full[s], tx);
+            if (ks < nkb) {
+              tma_load_2d(&mapB, &full[s], sp, ks * 64, brow);
+              if (QS) tma_load_2d(&mapQ, &full[s], sp + BHALF, ks * 64, (int)q0);
+            } else {
+              tma_load_2d(&mapBn, &full[s], sp, 0, brow);
+              if (QS) tma_load_2d(&mapQn, &full[s], sp + BHALF, 0, (int)q0);
+            }
           }
+        }
+      }
+      if (PAIR) {
+        // every stage released by the leader's MMAs: no commit is still on its
+        // way to this CTA when the pair exits
+        for (int e = 0; e < S && ok; e++) {
+          const int s = sn;
+          const uint32_t ph = phn;
+          if (++sn == S) { sn = 0; phn ^= 1; }
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) ok = false;
         }
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(TC_TILE_M, TC_TILE_N);
+    // ---------------- MMA issuer (the leader's, for a pair)
+    if (lane == 0 && leader) {
+      constexpr uint32_t idesc = idesc_bf16_f32(PAIR ? 2 * TC_TILE_M : TC_TILE_M, TC_TILE_N);
       bool ok = QS ? true : mbar_wait(qfull, 0, abort_flag);
       tc_fence_after();
-      long g = 0;
+      int sn = 0;
+      uint32_t phn = 0;
       int it = 0;
       for (int t = t_begin; t < t_end && ok; t++, it++) {
         const int a = it & 1;
@@ -179,26 +244,54 @@ __global__ void __launch_bounds__(NT_TC, 1)
         if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
         const uint32_t dt = tmem + (uint32_t)(a * TC_TILE_N);
-        for (int ks = 0; ks < nks; ks++, g++) {
-          const int s = (int)(g % S);
-          const uint32_t use = (uint32_t)(g / S);
-          if (!mbar_wait(&full[s], use & 1, abort_flag)) { ok = false; break; }
-          tc_fence_after();
+        for (int ks = 0; ks < nks; ks++) {
+          const int s = sn;
+          const uint32_t ph = phn;
+          if (++sn == S) { sn = 0; phn ^= 1; }
+          // TMA data: its arrival is tracked by the barrier's transaction
+          // count, no tcgen05 fence is needed (a fence here would stall the
+          // MMA pipe once per stage)
+          if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
           const uint32_t sb = smem_u32(Stg + (size_t)s * SB);
+          // a descriptor's start address field is addr >> 4 in its low 14 bits
+          // (shared addresses < 256 KB): offsets are added to a base descriptor
           if (ks < nkb) {
-            const uint32_t sa = QS ? sb + STAGE_BYTES : smem_u32(Qs + ks * QBLK_BYTES);
+            const uint32_t sa = QS ? sb + BHALF : smem_u32(Qs + ks * QBLK_BYTES);
+            const uint64_t da = desc_k_sw128(sa), db = desc_k_sw128(sb);
 #pragma unroll
-            for (int kk = 0; kk < 4; kk++)
-              umma_bf16(dt, desc_k_sw128(sa + kk * 32), desc_k_sw128(sb + kk * 32), idesc,
-                        (ks > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < 4; kk++) {
+              const uint32_t acc = (ks > 0 || kk > 0) ? 1u : 0u;
+              if (PAIR)
+                umma_bf16_pair(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, acc);
+              else
+                umma_bf16(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, acc);
+            }
           } else {
-            umma_bf16(dt, desc_k_sw32(QS ? sb + STAGE_BYTES : smem_u32(Qn)), desc_k_sw32(sb), idesc,
-                      1u);
+            const uint64_t dq = desc_k_sw32(QS ? sb + BHALF : smem_u32(Qn)), db = desc_k_sw32(sb);
+            if (PAIR)
+              umma_bf16_pair(dt, dq, db, idesc, 1u);
+            else
+              umma_bf16(dt, dq, db, idesc, 1u);
           }
-          umma_commit(&empty[s]);
+          if (PAIR)
+            umma_commit_pair_mc(&empty[s], 3);
+          else
+            umma_commit(&empty[s]);
         }
         if (!ok) break;
-        umma_commit(&tfull[a]);
+        if (PAIR)
+          umma_commit_pair_mc(&tfull[a], 3);
+        else
+          umma_commit(&tfull[a]);
+      }
+      if (PAIR) {
+        // the last two accumulators released by the selection warps of both
+        // CTAs: no remote arrival is still on its way when the pair exits
+        for (int e = it; e < it + 2 && ok; e++) {
+          const int a = e & 1;
+          const uint32_t u = (uint32_t)(e >> 1);
+          if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag)) ok = false;
+        }
       }
     }
   } else {
@@ -225,8 +318,52 @@ __global__ void __launch_bounds__(NT_TC, 1)
     const long rbase = (long)(blockIdx.y * 2 + half) * nq + qrow;
     const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
 
-    // one 32-column chunk already in registers: mask, cheap bound test, then
-    // (rarely) the per-element update; every index is static (no local memory)
+    // per-element update of one value (the rare path)
+    auto update = [&](float x, int j) {
+      if (MODE == SCAN_TOPV) {
+        if (x < lmax) {  // min/max bubble, values only
+#pragma unroll
+          for (int z = 0; z < CR; z++) {
+            const float lo = fminf(RL[z], x);
+            x = fmaxf(RL[z], x);
+            RL[z] = lo;
+          }
+          lmax = RL[CR - 1];
+        }
+      } else if (MODE == SCAN_TOPC) {
+        if (x < lmax) {
+          if (C <= 16) {
+            reg_insert<CR>(RL, RI, x, j);
+            lmax = RL[CR - 1];
+          } else {
+            int p = C - 1;
+            while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
+              Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
+              Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
+              p--;
+            }
+            Lv[p * N_EPI + tslot] = x;
+            Li[p * N_EPI + tslot] = j;
+            lmax = Lv[(C - 1) * N_EPI + tslot];
+          }
+        }
+      } else {
+        if (x <= thr) {
+          if (rcount < sel.cap) {
+            sel.candv[rbase * sel.cap + rcount] = x;
+            sel.candi[rbase * sel.cap + rcount] = j;
+          }
+          rcount++;
+        }
+      }
+    };
+
+    // One 32-column chunk already in registers.  The loop body must stay small
+    // (the selection warps run it from the instruction cache): a min tree and
+    // one warp vote per chunk; only when some lane's chunk minimum passes its
+    // bound (true when min < bound or min is NaN) does the warp build each
+    // lane's hit mask and walk its hits, extracting each value with a select
+    // tree instead of unrolled per-element code.
     auto process = [&](const uint32_t (&r)[32], int jc) {
       float v[32];
 #pragma unroll
@@ -236,67 +373,37 @@ __global__ void __launch_bounds__(NT_TC, 1)
         for (int i = 0; i < 32; i++)
           if (jc + i >= nb) v[i] = NAN;
       }
-      if (!rvalid) return;
-      // four 8-column groups: a group is scanned element by element only when
-      // its minimum passes the bound (true when min < bound or min is NaN)
+      float m8[4];
 #pragma unroll
-      for (int g = 0; g < 4; g++) {
-        const float mg = fmin3(fmin3(v[8 * g], v[8 * g + 1], v[8 * g + 2]),
-                               fmin3(v[8 * g + 3], v[8 * g + 4], v[8 * g + 5]),
-                               fminf(v[8 * g + 6], v[8 * g + 7]));
-        if (MODE == SCAN_TOPV) {
-          if (!(mg >= lmax)) {
+      for (int g = 0; g < 4; g++)
+        m8[g] = fmin3(fmin3(v[8 * g], v[8 * g + 1], v[8 * g + 2]),
+                      fmin3(v[8 * g + 3], v[8 * g + 4], v[8 * g + 5]),
+                      fminf(v[8 * g + 6], v[8 * g + 7]));
+      const float mc = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
+      const float bnd = MODE == SCAN_THRESH ? thr : lmax;
+      const bool pass = rvalid && (MODE == SCAN_THRESH ? !(mc > bnd) : !(mc >= bnd));
+      if (!__any_sync(0xffffffffu, pass)) return;
+      if (!pass) return;
+      uint32_t bits = 0;
 #pragma unroll
-            for (int i = 8 * g; i < 8 * g + 8; i++) {
-              float x = v[i];
-              if (x < lmax) {  // min/max bubble, values only
+      for (int i = 0; i < 32; i++) {
+        const bool h = MODE == SCAN_THRESH ? !(v[i] > bnd) : !(v[i] >= bnd);
+        bits |= h ? (1u << i) : 0u;
+      }
+#pragma unroll 1
+      while (bits) {
+        const int i = __ffs(bits) - 1;
+        bits &= bits - 1;
+        float t16[16], t8[8], t4[4], t2[2];
 #pragma unroll
-                for (int z = 0; z < CR; z++) {
-                  const float lo = fminf(RL[z], x);
-                  x = fmaxf(RL[z], x);
-                  RL[z] = lo;
-                }
-                lmax = RL[CR - 1];
-              }
-            }
-          }
-        } else if (MODE == SCAN_TOPC) {
-          if (!(mg >= lmax)) {
+        for (int z = 0; z < 16; z++) t16[z] = (i & 1) ? v[2 * z + 1] : v[2 * z];
 #pragma unroll
-            for (int i = 8 * g; i < 8 * g + 8; i++) {
-              const float x = v[i];
-              if (x < lmax) {
-                if (C <= 16) {
-                  reg_insert<CR>(RL, RI, x, jc + i);
-                  lmax = RL[CR - 1];
-                } else {
-                  int p = C - 1;
-                  while (p > 0 && Lv[(p - 1) * N_EPI + tslot] > x) {
-                    Lv[p * N_EPI + tslot] = Lv[(p - 1) * N_EPI + tslot];
-                    Li[p * N_EPI + tslot] = Li[(p - 1) * N_EPI + tslot];
-                    p--;
-                  }
-                  Lv[p * N_EPI + tslot] = x;
-                  Li[p * N_EPI + tslot] = jc + i;
-                  lmax = Lv[(C - 1) * N_EPI + tslot];
-                }
-              }
-            }
-          }
-        } else {
-          if (!(mg > thr)) {
+        for (int z = 0; z < 8; z++) t8[z] = (i & 2) ? t16[2 * z + 1] : t16[2 * z];
 #pragma unroll
-            for (int i = 8 * g; i < 8 * g + 8; i++) {
-              if (v[i] <= thr) {
-                if (rcount < sel.cap) {
-                  sel.candv[rbase * sel.cap + rcount] = v[i];
-                  sel.candi[rbase * sel.cap + rcount] = jc + i;
-                }
-                rcount++;
-              }
-            }
-          }
-        }
+        for (int z = 0; z < 4; z++) t4[z] = (i & 4) ? t8[2 * z + 1] : t8[2 * z];
+#pragma unroll
+        for (int z = 0; z < 2; z++) t2[z] = (i & 8) ? t4[2 * z + 1] : t4[2 * z];
+        update((i & 16) ? t2[1] : t2[0], jc + i);
       }
     };
 
@@ -327,7 +434,12 @@ __global__ void __launch_bounds__(NT_TC, 1)
           // every load of this accumulator is complete: hand it back to the MMA warp
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[a]);
+          if (lane == 0) {
+            if (PAIR)
+              mbar_arrive_cluster(tempty_l + (uint32_t)(a * 8));
+            else
+              mbar_arrive(&tempty[a]);
+          }
         }
         process(rb, j0 + 64 * cc + 32);
         if (cc == 0) tmem_ld_wait(ra);
@@ -375,11 +487,16 @@ __global__ void __launch_bounds__(NT_TC, 1)
 
   tc_fence_before();
   __syncthreads();
+  if (PAIR) cluster_sync();  // no peer signal is still on its way
   tc_fence_after();
   if (warp == 1) {
     __syncwarp();
-    tmem_dealloc(tmem, TMEM_COLS);
+    if (PAIR)
+      tmem_dealloc_pair(tmem, TMEM_COLS);
+    else
+      tmem_dealloc(tmem, TMEM_COLS);
   }
+  if (PAIR) cluster_sync();  // the pair's collective free is done before either CTA exits
   if (threadIdx.x == 0 && *abort_flag && err) atomicExch(err, 1);
 }
 
@@ -426,12 +543,12 @@ static int make_map(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t row
   return OK;
 }
 
-template <int MODE, int C, bool L2, bool QS>
+template <int MODE, int C, bool L2, bool QS, bool PAIR>
 int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
   const int nkb = op.Kp / 64;
-  int S = 6;
-  while (S > 2 && make_layout(nkb, S, MODE, C, QS).total > 227 * 1024) S--;
-  const Layout lay = make_layout(nkb, S, MODE, C, QS);
+  int S = 12;
+  while (S > 2 && make_layout(nkb, S, MODE, C, QS, PAIR).total > 227 * 1024) S--;
+  const Layout lay = make_layout(nkb, S, MODE, C, QS, PAIR);
   if (!QS && lay.q_off + (size_t)nkb * QBLK_BYTES > 227 * 1024) {
     set_error(E_UNSUPPORTED, "tc_scan: resident query tile too large (Kp=%d)", op.Kp);
     return E_UNSUPPORTED;
@@ -443,51 +560,80 @@ int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_
   }
   static bool attr = false;
   if (!attr) {
-    YG_CUDA(cudaFuncSetAttribute(tc_scan_kernel<MODE, C, L2, QS>,
+    YG_CUDA(cudaFuncSetAttribute(tc_scan_kernel<MODE, C, L2, QS, PAIR>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     attr = true;
   }
   CUtensorMap mq, mqn, mb, mbn;
   YG_CHECK(make_map(&mq, op.q, op.Kp, nq, (uint64_t)op.Kp * 2, 64, 128,
                     CU_TENSOR_MAP_SWIZZLE_128B));
-  YG_CHECK(make_map(&mb, op.b, op.Kp, nb, (uint64_t)op.Kp * 2 * op.b_step, 64, 256,
+  // a pair CTA loads 128 of the 256 rows of each base block
+  const uint32_t brows = PAIR ? TC_TILE_N / 2 : TC_TILE_N;
+  YG_CHECK(make_map(&mb, op.b, op.Kp, nb, (uint64_t)op.Kp * 2 * op.b_step, 64, brows,
                     CU_TENSOR_MAP_SWIZZLE_128B));
   if (L2) {
     YG_CHECK(make_map(&mqn, op.qn, 16, nq, 32, 16, 128, CU_TENSOR_MAP_SWIZZLE_32B));
-    YG_CHECK(make_map(&mbn, op.bn, 16, nb, (uint64_t)32 * op.b_step, 16, 256,
+    YG_CHECK(make_map(&mbn, op.bn, 16, nb, (uint64_t)32 * op.b_step, 16, brows,
                       CU_TENSOR_MAP_SWIZZLE_32B));
   } else {
     mqn = mq;
     mbn = mb;
   }
-  dim3 grid((unsigned)ceil_div(nq, TC_TILE_M), (unsigned)sel.nchunk);
-  tc_scan_kernel<MODE, C, L2, QS><<<grid, NT_TC, lay.total, st>>>(mq, mqn, mb, mbn, nq, nb, nkb,
-                                                                  S, sel, op.err);
+  if (!PAIR) {
+    dim3 grid((unsigned)ceil_div(nq, TC_TILE_M), (unsigned)sel.nchunk);
+    tc_scan_kernel<MODE, C, L2, QS, PAIR><<<grid, NT_TC, lay.total, st>>>(
+        mq, mqn, mb, mbn, nq, nb, nkb, S, sel, op.err);
+  } else {
+    // query tiles padded to whole pairs (a padding CTA has no valid rows)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(ceil_div(ceil_div(nq, TC_TILE_M), 2) * 2), (unsigned)sel.nchunk);
+    cfg.blockDim = dim3(NT_TC);
+    cfg.dynamicSmemBytes = lay.total;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    YG_CUDA(cudaLaunchKernelEx(&cfg, tc_scan_kernel<MODE, C, L2, QS, PAIR>, mq, mqn, mb, mbn, nq,
+                               nb, nkb, S, sel, op.err));
+  }
   YG_LAUNCH_CHECK();
   return OK;
 }
 
-template <bool L2, bool QS>
+template <bool L2, bool QS, bool PAIR>
 int dispatch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
-  if (sel.mode == SCAN_THRESH) return launch<SCAN_THRESH, 1, L2, QS>(op, nq, nb, sel, st);
+  if (sel.mode == SCAN_THRESH) return launch<SCAN_THRESH, 1, L2, QS, PAIR>(op, nq, nb, sel, st);
   switch (sel.C) {
-    case 1: return launch<SCAN_TOPC, 1, L2, QS>(op, nq, nb, sel, st);
-    case 2: return launch<SCAN_TOPC, 2, L2, QS>(op, nq, nb, sel, st);
-    case 4: return launch<SCAN_TOPC, 4, L2, QS>(op, nq, nb, sel, st);
-    case 8: return launch<SCAN_TOPC, 8, L2, QS>(op, nq, nb, sel, st);
+    case 1: return launch<SCAN_TOPC, 1, L2, QS, PAIR>(op, nq, nb, sel, st);
+    case 2: return launch<SCAN_TOPC, 2, L2, QS, PAIR>(op, nq, nb, sel, st);
+    case 4: return launch<SCAN_TOPC, 4, L2, QS, PAIR>(op, nq, nb, sel, st);
+    case 8: return launch<SCAN_TOPC, 8, L2, QS, PAIR>(op, nq, nb, sel, st);
     case 16:
-      if (sel.mode == SCAN_TOPV) return launch<SCAN_TOPV, 16, L2, QS>(op, nq, nb, sel, st);
-      return launch<SCAN_TOPC, 16, L2, QS>(op, nq, nb, sel, st);
+      if (sel.mode == SCAN_TOPV) return launch<SCAN_TOPV, 16, L2, QS, PAIR>(op, nq, nb, sel, st);
+      return launch<SCAN_TOPC, 16, L2, QS, PAIR>(op, nq, nb, sel, st);
   }
   set_error(E_ARG, "tc_scan: unsupported list length C=%d", sel.C);
   return E_ARG;
 }
 
+// one instantiation per translation unit (they compile in parallel)
+template <bool QS, bool PAIR>
+int dispatch_metric(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
+  if (op.metric == METRIC_L2) return dispatch<true, QS, PAIR>(op, nq, nb, sel, st);
+  return dispatch<false, QS, PAIR>(op, nq, nb, sel, st);
+}
 
 }  // namespace tck
 
-// streamed-query dispatch (tc_scan_qs.cu)
-int tc_dispatch_streaming(const TcOperands &op, int nq, int nb, const ScanSel &sel,
-                          cudaStream_t st);
+// the four instantiations: query tile resident (r) or streamed (s), single
+// CTAs (1) or CTA pairs (2)
+int tc_dispatch_r1(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
+int tc_dispatch_r2(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
+int tc_dispatch_s1(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
+int tc_dispatch_s2(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
 
 }  // namespace yg

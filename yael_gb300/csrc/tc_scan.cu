@@ -1,5 +1,8 @@
 // tcgen05 BF16 distance tiles with the fused selection (see tc_scan.cuh and
-// tc_kernel.cuh): operand packing and the resident-query-tile dispatch.
+// tc_kernel.cuh): operand packing, the choice of kernel variant, and the
+// resident-query-tile single-CTA instantiation.
+#include <stdlib.h>
+
 #include "tc_kernel.cuh"
 
 namespace yg {
@@ -65,11 +68,24 @@ int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out)
   return OK;
 }
 
+int tc_dispatch_r1(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
+  return tck::dispatch_metric<false, false>(op, nq, nb, sel, st);
+}
+
 int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
   if (nq <= 0 || nb <= 0) return OK;
-  if (op.Kp > 256) return tc_dispatch_streaming(op, nq, nb, sel, st);
-  if (op.metric == METRIC_L2) return tck::dispatch<true, false>(op, nq, nb, sel, st);
-  return tck::dispatch<false, false>(op, nq, nb, sel, st);
+  // CTA pairs (one 256-row MMA over two SMs) halve the per-SM base traffic
+  // but add a cross-SM handoff to every accumulator; measured on the 1M x 10k
+  // k-NN pass they are slower (3.98 ms vs 2.87 ms), so single CTAs are the
+  // default and YAEL_GPU_TC_PAIR=1 selects pairs
+  static const bool pair_env = [] {
+    const char *e = getenv("YAEL_GPU_TC_PAIR");
+    return e && e[0] == '1';
+  }();
+  const bool pair = pair_env && nq > TC_TILE_M;
+  if (op.Kp > 256)  // query tile too large to stay resident: streamed per K block
+    return pair ? tc_dispatch_s2(op, nq, nb, sel, st) : tc_dispatch_s1(op, nq, nb, sel, st);
+  return pair ? tc_dispatch_r2(op, nq, nb, sel, st) : tc_dispatch_r1(op, nq, nb, sel, st);
 }
 
 }  // namespace yg
