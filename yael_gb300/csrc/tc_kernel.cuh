@@ -64,7 +64,10 @@ __host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C, b
   size_t off = 0;
   L.q_off = off;   off += qs ? 0 : (size_t)nkb * QBLK_BYTES;
   L.qn_off = off;  off += qs ? 0 : QN_BYTES;
-  L.stage_bytes = (pair ? STAGE_BYTES / 2 : STAGE_BYTES) + (qs ? QBLK_BYTES : 0);
+  // a stage: this CTA's base block, the query block when streamed, and room
+  // for the norm blocks that travel with the last K block of a tile
+  L.stage_bytes = (pair ? STAGE_BYTES / 2 : STAGE_BYTES) + BN_BYTES +
+                  (qs ? QBLK_BYTES + QN_BYTES : 0);
   L.stg_off = off; off += (size_t)S * L.stage_bytes;
   L.list_off = off;
   if (mode != SCAN_THRESH) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
@@ -127,7 +130,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
   const int ntb = (int)ceil_div(nb, TC_TILE_N);
   const int t_begin = blockIdx.y * sel.tiles_per_chunk;
   const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
-  const int nks = nkb + (L2 ? 1 : 0);
+  const int nks = nkb;  // stages per base tile (the norm block rides with the last)
   const uint32_t crank = PAIR ? cluster_ctarank() : 0;
   const bool leader = crank == 0;
 
@@ -194,26 +197,28 @@ __global__ void __launch_bounds__(NT_TC, 1)
           if (++sn == S) { sn = 0; phn ^= 1; }
           if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) { ok = false; break; }
           uint8_t *sp = Stg + (size_t)s * SB;
-          const uint32_t tx = ks < nkb ? (uint32_t)(BHALF + (QS ? QBLK_BYTES : 0))
-                                       : (uint32_t)(BNHALF + (QS ? 128 * 32 : 0));
+          const bool lastk = L2 && ks == nkb - 1;
+          const uint32_t tx = (uint32_t)(BHALF + (QS ? QBLK_BYTES : 0)) +
+                              (lastk ? (uint32_t)(BNHALF + (QS ? 128 * 32 : 0)) : 0u);
+          // the norm blocks travel with the last K block (base norms first,
+          // then, when streamed, the query norms BN_BYTES further)
+          uint8_t *np_ = sp + BHALF + (QS ? QBLK_BYTES : 0);
           if (PAIR) {
             const uint32_t fb = full_l + (uint32_t)(s * 8);
             if (leader) mbar_arrive_expect_tx(&full[s], 2 * tx);
-            if (ks < nkb) {
-              tma_load_2d_pair(&mapB, fb, sp, ks * 64, brow);
-              if (QS) tma_load_2d_pair(&mapQ, fb, sp + BHALF, ks * 64, (int)q0);
-            } else {
-              tma_load_2d_pair(&mapBn, fb, sp, 0, brow);
-              if (QS) tma_load_2d_pair(&mapQn, fb, sp + BHALF, 0, (int)q0);
+            tma_load_2d_pair(&mapB, fb, sp, ks * 64, brow);
+            if (QS) tma_load_2d_pair(&mapQ, fb, sp + BHALF, ks * 64, (int)q0);
+            if (lastk) {
+              tma_load_2d_pair(&mapBn, fb, np_, 0, brow);
+              if (QS) tma_load_2d_pair(&mapQn, fb, np_ + BN_BYTES, 0, (int)q0);
             }
           } else {
             mbar_arrive_expect_tx(&full[s], tx);
-            if (ks < nkb) {
-              tma_load_2d(&mapB, &full[s], sp, ks * 64, brow);
-              if (QS) tma_load_2d(&mapQ, &full[s], sp + BHALF, ks * 64, (int)q0);
-            } else {
-              tma_load_2d(&mapBn, &full[s], sp, 0, brow);
-              if (QS) tma_load_2d(&mapQn, &full[s], sp + BHALF, 0, (int)q0);
+            tma_load_2d(&mapB, &full[s], sp, ks * 64, brow);
+            if (QS) tma_load_2d(&mapQ, &full[s], sp + BHALF, ks * 64, (int)q0);
+            if (lastk) {
+              tma_load_2d(&mapBn, &full[s], np_, 0, brow);
+              if (QS) tma_load_2d(&mapQn, &full[s], np_ + BN_BYTES, 0, (int)q0);
             }
           }
         }
@@ -255,7 +260,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           const uint32_t sb = smem_u32(Stg + (size_t)s * SB);
           // a descriptor's start address field is addr >> 4 in its low 14 bits
           // (shared addresses < 256 KB): offsets are added to a base descriptor
-          if (ks < nkb) {
+          {
             const uint32_t sa = QS ? sb + BHALF : smem_u32(Qs + ks * QBLK_BYTES);
             const uint64_t da = desc_k_sw128(sa), db = desc_k_sw128(sb);
 #pragma unroll
@@ -266,12 +271,15 @@ __global__ void __launch_bounds__(NT_TC, 1)
               else
                 umma_bf16(dt, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, acc);
             }
-          } else {
-            const uint64_t dq = desc_k_sw32(QS ? sb + BHALF : smem_u32(Qn)), db = desc_k_sw32(sb);
-            if (PAIR)
-              umma_bf16_pair(dt, dq, db, idesc, 1u);
-            else
-              umma_bf16(dt, dq, db, idesc, 1u);
+            if (L2 && ks == nkb - 1) {  // the norm fold: one more K=16 step
+              const uint32_t sn_ = sb + BHALF + (QS ? QBLK_BYTES : 0);
+              const uint64_t dq = desc_k_sw32(QS ? sn_ + BN_BYTES : smem_u32(Qn));
+              const uint64_t dbn = desc_k_sw32(sn_);
+              if (PAIR)
+                umma_bf16_pair(dt, dq, dbn, idesc, 1u);
+              else
+                umma_bf16(dt, dq, dbn, idesc, 1u);
+            }
           }
           if (PAIR)
             umma_commit_pair_mc(&empty[s], 3);
@@ -420,30 +428,27 @@ __global__ void __launch_bounds__(NT_TC, 1)
       const int j0 = t * TC_TILE_N + half * 128;
       // two register sets: the load of chunk c+1 is in flight while chunk c is
       // scanned; the loop keeps one copy of the chunk code per register set
-      uint32_t ra[32], rb[32];
-      tmem_ld32(tcol, ra);
-      tmem_ld_wait(ra);
-#pragma unroll 1
-      for (int cc = 0; cc < 2; cc++) {
-        tmem_ld32(tcol + (uint32_t)(64 * cc + 32), rb);
-        process(ra, j0 + 64 * cc);
-        tmem_ld_wait(rb);
-        if (cc == 0) {
-          tmem_ld32(tcol + 64, ra);
-        } else {
-          // every load of this accumulator is complete: hand it back to the MMA warp
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) {
-            if (PAIR)
-              mbar_arrive_cluster(tempty_l + (uint32_t)(a * 8));
-            else
-              mbar_arrive(&tempty[a]);
-          }
-        }
-        process(rb, j0 + 64 * cc + 32);
-        if (cc == 0) tmem_ld_wait(ra);
+      uint32_t r0[32], r1[32], r2[32], r3[32];
+      tmem_ld32(tcol, r0);
+      tmem_ld32(tcol + 32, r1);
+      tmem_ld32(tcol + 64, r2);
+      tmem_ld32(tcol + 96, r3);
+      tmem_ld_wait(r0);
+      tmem_ld_wait(r1);
+      tmem_ld_wait(r2);
+      tmem_ld_wait(r3);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        if (PAIR)
+          mbar_arrive_cluster(tempty_l + (uint32_t)(a * 8));
+        else
+          mbar_arrive(&tempty[a]);
       }
+      process(r0, j0);
+      process(r1, j0 + 32);
+      process(r2, j0 + 64);
+      process(r3, j0 + 96);
     }
     (void)ok;
     if (MODE == SCAN_THRESH && rvalid) sel.cnt[rbase] = rcount;
