@@ -152,6 +152,10 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes (read + write) of one main-pass launch at the default k-NN sizes,
+# from the ncu capture summarised in profiles/tc_scan_knn_main_nb1M_nq10k.md
+KNN_MAIN_TRAFFIC = 434.985984e6 + 48.504576e6
+
 CLUSTER_CFG = {
     # n, d, k, niter, seed, data
     "kmeans1": dict(n=100_000, d=128, k=256, niter=20, seed=0, comps=256, sigma=0.15, zipf=None),
@@ -175,6 +179,8 @@ def run_clustering(args, world, rank, local):
     c = dict(CLUSTER_CFG[args.workload])
     if args.niter:
         c["niter"] = args.niter
+    if args.n:
+        c["n"] = args.n
     w = synth.zipf_weights(c["comps"], c["zipf"]) if c.get("zipf") else None
     v_h, _, _ = synth.gaussian_mixture(c["n"], c["d"], c["comps"], c["sigma"], seed=11, weights=w)
     n, d = v_h.shape
@@ -304,6 +310,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the FP64 spot check")
     ap.add_argument("--niter", type=int, default=0, help="override the clustering iterations")
+    ap.add_argument("--n", type=int, default=0,
+                    help="override the clustering point count (smaller cases for profiling)")
     ap.add_argument("--workload", default="knn", choices=["knn", "kmeans1", "kmeans3", "hkm4"],
                     help="knn: the headline configuration; the others are the k-means / hkm "
                          "configurations, reported separately")
@@ -443,7 +451,12 @@ def main():
         "roofline": {"bound": "tensor", "kernel": "tc_scan_kernel (THRESH, main pass)",
                      "achieved": achieved, "peak": pk_tf, "unit": "TFLOP/s",
                      "frac": (achieved / pk_tf) if achieved else None,
-                     "peak_source": pk_src, "traffic": None,
+                     "peak_source": pk_src,
+                     # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this
+                     # kernel at the default sizes (profiles/tc_scan_knn_main_nb1M_nq10k.md)
+                     "traffic": KNN_MAIN_TRAFFIC if (args.nb, args.nq, args.d, args.k) ==
+                     (1_000_000, 10_000, 128, 100) else None,
+                     "traffic_unit": "bytes per launch",
                      "algorithmic": f"2*nq*nb*d = {flops:.4g} flop per launch"},
         "e2e": {"value": e2e_qps, "unit": "queries/s",
                 "h2d_bytes_per_step": 4 * (args.nb + args.nq) * args.d,
