@@ -284,6 +284,160 @@ def run_clustering(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def batch_sizes(npairs, seed):
+    """Pair sizes of the batched uneven k-NN configuration: queries log-uniform
+    in [1, 8192], base rows log-uniform in [10,000, 2,000,000]."""
+    rng = np.random.default_rng(seed)
+    nq = np.floor(np.exp(rng.uniform(np.log(1), np.log(8193), npairs))).astype(np.int64)
+    nb = np.floor(np.exp(rng.uniform(np.log(1e4), np.log(2e6 + 1), npairs))).astype(np.int64)
+    return np.clip(nq, 1, 8192), np.clip(nb, 10_000, 2_000_000)
+
+
+def run_knn_batch(args, world, rank, local):
+    """Batched uneven exact k-NN: 512 independent (queries, base) pairs, d = 128,
+    k = 32, unit-normalised Gaussian rows, L2 and inner product, through
+    yael_gpu_knn_batch; the plain FP32 per-pair loop beside it."""
+    import torch
+    import yael_gb300 as yg
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _util import knn_port
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = yg.lib()
+    npairs, d, k = args.pairs, 128, 32
+    nq, nb = batch_sizes(npairs, 5 + 1000 * rank)
+    gen = torch.Generator(device=dev)
+    qs, bs = [], []
+    for i in range(npairs):  # seeded per pair, generated and normalised in HBM
+        gen.manual_seed(1_000_003 * (rank + 1) + i)
+        b = torch.randn((int(nb[i]), d), device=dev, generator=gen)
+        b /= b.norm(dim=1, keepdim=True)
+        q = torch.randn((int(nq[i]), d), device=dev, generator=gen)
+        q /= q.norm(dim=1, keepdim=True)
+        bs.append(b)
+        qs.append(q)
+    idx = [torch.empty((int(n), k), dtype=torch.int32, device=dev) for n in nq]
+    dis = [torch.empty((int(n), k), device=dev) for n in nq]
+    descs = (yg.KnnPair * npairs)()
+    for i in range(npairs):
+        descs[i] = yg.KnnPair(int(nq[i]), int(nb[i]), qs[i].data_ptr(), bs[i].data_ptr(),
+                              idx[i].data_ptr(), dis[i].data_ptr())
+    torch.cuda.synchronize(dev)
+    flops = float(np.sum(2.0 * nq * nb * d))
+
+    def batch_call(prec, metric):
+        o = yg.KnnOpts(prec, metric, 1, None)
+        rc = L.yael_gpu_knn_batch(npairs, ctypes.cast(descs, ctypes.c_void_p), d, k,
+                                  ctypes.byref(o))
+        if rc != 0:
+            raise RuntimeError(yg.last_error())
+        return o
+
+    def timed(prec, metric, steps, warmup):
+        for _ in range(warmup):
+            batch_call(prec, metric)
+        torch.cuda.synchronize(dev)
+        l0 = L.yael_gpu_launch_count()
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                o = batch_call(prec, metric)
+            torch.cuda.synchronize(dev)
+            dt = time.perf_counter() - t0
+        return dt / steps, L.yael_gpu_launch_count() - l0, o, clk.summary()
+
+    steps = max(1, args.steps)
+    sec, launches, o, clocks = timed(yg.PREC_BF16, 2, steps, args.warmup)
+    sec_ip, _, o_ip, _ = timed(yg.PREC_BF16, 16, max(1, steps // 2), 1)
+    # exactness spot check: pair 0 and the largest pair's first 16 queries vs FP64
+    check = None
+    if not args.no_check:
+        from _util import knn_exact
+        ok = True
+        for i in (0, int(np.argmax(nq * nb))):
+            m = min(16, int(nq[i]))
+            ridx, _, _ = knn_exact(bs[i].cpu().numpy(), qs[i][:m].cpu().numpy(), k,
+                                   os.cpu_count() or 1)
+            batch_call(yg.PREC_BF16, 2)
+            ok = ok and bool((idx[i][:m].cpu().numpy() == ridx).all())
+        check = ok
+    # the plain FP32 path, one knn call per pair (the drop-in loop)
+    t0 = time.perf_counter()
+    for i in range(npairs):
+        o32 = yg.KnnOpts(yg.PREC_FP32, 2, 1, None)
+        L.yael_gpu_knn_ex(int(nq[i]), int(nb[i]), d, k, bs[i].data_ptr(), qs[i].data_ptr(),
+                          idx[i].data_ptr(), dis[i].data_ptr(), ctypes.byref(o32))
+    torch.cuda.synchronize(dev)
+    sec32 = time.perf_counter() - t0
+    # end to end with host buffers for the first pairs (pinned copies of the same data)
+    ne = min(npairs, args.e2e_pairs)
+    hq = [qs[i].cpu().pin_memory() for i in range(ne)]
+    hb = [bs[i].cpu().pin_memory() for i in range(ne)]
+    hi = [torch.empty((int(nq[i]), k), dtype=torch.int32).pin_memory() for i in range(ne)]
+    hd = [torch.empty((int(nq[i]), k)).pin_memory() for i in range(ne)]
+    hdesc = (yg.KnnPair * ne)()
+    for i in range(ne):
+        hdesc[i] = yg.KnnPair(int(nq[i]), int(nb[i]), hq[i].data_ptr(), hb[i].data_ptr(),
+                              hi[i].data_ptr(), hd[i].data_ptr())
+    oe = yg.KnnOpts(yg.PREC_BF16, 2, 0, None)
+    L.yael_gpu_knn_batch(ne, ctypes.cast(hdesc, ctypes.c_void_p), d, k, ctypes.byref(oe))
+    t0 = time.perf_counter()
+    rc = L.yael_gpu_knn_batch(ne, ctypes.cast(hdesc, ctypes.c_void_p), d, k, ctypes.byref(oe))
+    sec_e2e = time.perf_counter() - t0
+    if rc != 0:
+        raise RuntimeError(yg.last_error())
+    # CPU: the reference algorithm (oracle port) on a bounded sample
+    cpu = None
+    if not args.no_cpu:
+        sel = np.argsort(nb)[:4]
+        tq, tt = 0, 0.0
+        for i in sel:
+            m = min(int(nq[i]), 200)
+            bh = bs[i].cpu().numpy()
+            qh = qs[i][:m].cpu().numpy()
+            t1 = time.perf_counter()
+            knn_port(bh, qh, k, nt=os.cpu_count() or 1)
+            tt += time.perf_counter() - t1
+            tq += m
+        cpu = {"value": tq / tt, "unit": "queries/s", "cores": os.cpu_count() or 1,
+               "kind": "port",
+               "sample": f"<= 200 queries of each of the 4 pairs with the smallest bases "
+                         f"(nb {int(nb[sel].min())}..{int(nb[sel].max())}); the whole batch "
+                         f"averages nb = {int(nb.mean())}"}
+    pk = peaks()
+    tot_q = float(np.sum(nq))
+    line = {
+        "metric": METRIC, "value": world * tot_q / sec, "unit": "queries/s", "n_gpus": world,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic",
+        "config": {"workload": f"batched uneven exact k-NN, {npairs} pairs: nq log-uniform "
+                               f"[1, 8192], nb log-uniform [1e4, 2e6], d={d}, k={k}, "
+                               "unit-normalised Gaussian rows, L2",
+                   "pairs": npairs, "sum_nq": int(tot_q), "sum_nb": int(np.sum(nb)),
+                   "flop_per_step": flops, "l2": "inputs larger than L2"},
+        "inner_product": {"value": world * tot_q / sec_ip, "unit": "queries/s",
+                          "ms_per_step": 1e3 * sec_ip, "fallback_queries": o_ip.n_fallback},
+        "plain_fp32_per_pair_loop": {"value": tot_q / sec32, "unit": "queries/s",
+                                     "ms_per_step": 1e3 * sec32},
+        "exact_ids_vs_fp64_oracle_spot": check,
+        "fallback_queries": o.n_fallback, "band_queries": o.n_band,
+        "roofline": {"bound": "tensor", "kernel": "whole batch (all passes)",
+                     "achieved": flops / sec / 1e12, "unit": "TFLOP/s", "peak": pk[0],
+                     "frac": flops / sec / 1e12 / pk[0], "peak_source": pk[2],
+                     "traffic": None},
+        "e2e": {"value": float(np.sum(nq[:ne])) / sec_e2e, "unit": "queries/s",
+                "h2d_bytes_per_step": int(4 * d * (np.sum(nq[:ne]) + np.sum(nb[:ne]))),
+                "d2h_bytes_per_step": int(8 * k * np.sum(nq[:ne])),
+                "api": f"yael_gpu_knn_batch with pinned host buffers, first {ne} pairs"},
+        "gpu_launches": launches, "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def config_of(args):
     return {"workload": f"exact kNN L2, SIFT-like float32 (30% zeros, floor|N(0,40)| clipped "
                         f"to 255), nb={args.nb}, nq={args.nq}, d={args.d}, k={args.k}",
@@ -312,12 +466,19 @@ def main():
     ap.add_argument("--niter", type=int, default=0, help="override the clustering iterations")
     ap.add_argument("--n", type=int, default=0,
                     help="override the clustering point count (smaller cases for profiling)")
-    ap.add_argument("--workload", default="knn", choices=["knn", "kmeans1", "kmeans3", "hkm4"],
+    ap.add_argument("--pairs", type=int, default=512, help="knn_batch: number of pairs")
+    ap.add_argument("--e2e-pairs", type=int, default=64,
+                    help="knn_batch: pairs timed end to end from host buffers")
+    ap.add_argument("--workload", default="knn",
+                    choices=["knn", "kmeans1", "kmeans3", "hkm4", "knn_batch"],
                     help="knn: the headline configuration; the others are the k-means / hkm "
                          "configurations, reported separately")
     args = ap.parse_args()
     world, rank, local = dist_setup()
-    if args.workload != "knn":
+    if args.workload == "knn_batch" and args.impl != "reference":
+        run_knn_batch(args, world, rank, local)
+        return
+    if args.workload not in ("knn", "knn_batch"):
         run_clustering(args, world, rank, local)
         return
 

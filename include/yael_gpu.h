@@ -217,6 +217,28 @@ typedef struct {
 int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q,
                     int *assign, float *dis, yael_gpu_knn_opts *opts);
 
+/* One (queries, base) pair of a batched k-NN call. */
+typedef struct {
+  int nq, nb;          /* query rows and base rows of this pair (k <= nb) */
+  const float *q;      /* nq x d, row-major (yael layout) */
+  const float *b;      /* nb x d */
+  int *assign;         /* out: nq x k ids into this pair's base */
+  float *dis;          /* out: nq x k distances */
+} yael_gpu_knn_pair;
+
+/* knn_full over npairs independent pairs of uneven sizes, all with the same d,
+ * k, metric and precision (opts may be NULL: L2, YAEL_GPU_PRECISION).  No
+ * counterpart in the reference, whose callers loop over knn_full (per-cell
+ * searches, hkm / kmlsh children); results are those of that loop.  Pairs run
+ * concurrently, largest first, on a persistent pool of host workers each with
+ * its own stream and workspace (YAEL_GPU_BATCH_WORKERS, default 8).  With
+ * opts->device_ptrs every array is device memory and opts->stream (a
+ * cudaStream_t, NULL = default stream) is synchronised before the pairs start.
+ * Returns when every pair is done; opts' counters are summed over the pairs.
+ * Returns a status code (first error met; later pairs are skipped). */
+int yael_gpu_knn_batch(int npairs, const yael_gpu_knn_pair *pairs, int d, int k,
+                       yael_gpu_knn_opts *opts);
+
 typedef struct {
   int precision;   /* YAEL_GPU_PREC_*: distance pass of the assignment step */
   int device_ptrs; /* 1: v and the outputs are device pointers */

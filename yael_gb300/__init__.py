@@ -37,6 +37,10 @@ KMEANS_CHI2 = 0x400000
 PREC_ENV, PREC_FP32, PREC_BF16, PREC_BF16X3 = -1, 0, 1, 2
 
 
+class KnnPair(ctypes.Structure):
+    _fields_ = [("nq", c_int), ("nb", c_int), ("q", P), ("b", P), ("assign", P), ("dis", P)]
+
+
 class KmeansOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("device_ptrs", c_int), ("stream", P), ("status", c_int),
                 ("iterations", c_long), ("n_fallback", c_long), ("n_second", c_long),
@@ -78,6 +82,7 @@ SIGNATURES = {
     "compute_distances_1_thread": (None, [c_int, c_int, P, P, P, c_int]),
     "compute_distances_1_nonpacked_thread": (None, [c_int, c_int, P, P, c_int, P, c_int]),
     "yael_gpu_knn_ex": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, ctypes.POINTER(KnnOpts)]),
+    "yael_gpu_knn_batch": (c_int, [c_int, P, c_int, c_int, P]),
     "yael_gpu_last_error": (ctypes.c_char_p, []),
     "kmeans": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P]),
     "clustering_kmeans": (P, [c_int, c_int, P, c_int, c_int, c_double]),
@@ -160,6 +165,37 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
                           "exact_class": opts.exact_class, "n_second": opts.n_second,
                           "n_band": opts.n_band, "ms_second": opts.ms_second}
     return idx, dis
+
+
+def knn_batch(pairs, nnn=1, distance_type=2, precision=None, stats=False):
+    """Exact k-NN for many independent (queries, base) pairs in one call
+    (yael_gpu_knn_batch); pairs = [(queries, base), ...] float32 arrays with the
+    same d.  Returns [(idx, dis), ...] as knn() would for each pair."""
+    arrays = []
+    descs = (KnnPair * len(pairs))()
+    d = None
+    for i, (q, b) in enumerate(pairs):
+        q = np.ascontiguousarray(q, dtype=np.float32)
+        b = np.ascontiguousarray(b, dtype=np.float32)
+        if d is None:
+            d = q.shape[1]
+        if q.shape[1] != d or b.shape[1] != d:
+            raise ValueError("knn_batch: every pair must have the same d")
+        idx = np.empty((q.shape[0], nnn), dtype=np.int32)
+        dis = np.empty((q.shape[0], nnn), dtype=np.float32)
+        arrays.append((q, b, idx, dis))
+        descs[i] = KnnPair(q.shape[0], b.shape[0], _ptr(q), _ptr(b), _ptr(idx), _ptr(dis))
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3}[precision]
+    opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    rc = lib().yael_gpu_knn_batch(len(pairs), ctypes.cast(descs, P), d or 1, nnn,
+                                  ctypes.byref(opts))
+    if rc != 0:
+        raise RuntimeError(f"yael_gpu_knn_batch failed ({rc}): {last_error()}")
+    out = [(a[2], a[3]) for a in arrays]
+    if stats:
+        return out, {"n_fallback": opts.n_fallback, "n_band": opts.n_band,
+                     "n_second": opts.n_second, "exact_class": opts.exact_class}
+    return out
 
 
 def cross_distances(a, b, distance_type=12):

@@ -527,7 +527,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
 }
 
 // host-memory entry: copies in, runs, copies out
-static int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
+int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
                     const float *q, const float *w, int *assign, float *dis, int prec,
                     yael_gpu_knn_opts *opts) {
   Ctx *ctx;

@@ -2,6 +2,7 @@
 // k-means assignment step and the batched calls.
 #pragma once
 #include "select.cuh"
+#include "../../include/yael_gpu.h"
 
 namespace yg {
 
@@ -35,6 +36,12 @@ struct KnnJob {
 
 // Runs the whole pipeline on stream st using the calling thread's workspace.
 int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st);
+
+// One k-NN call on the calling thread's context: host arrays (copied in and
+// out) or, with opts->device_ptrs, device arrays on opts->stream (NULL = the
+// thread's stream); fills opts' counters.
+int knn_host(int metric, int nq, int nb, int d, int k, const float *b, const float *q,
+             const float *w, int *assign, float *dis, int prec, yael_gpu_knn_opts *opts);
 
 // workspace slots (each slot is one grow-only device buffer per host thread)
 enum WsSlot : int {
