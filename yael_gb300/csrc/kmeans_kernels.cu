@@ -9,32 +9,75 @@ namespace {
 
 constexpr float kU = 5.9604645e-08f;  // 2^-24
 
-template <int K>
+// Grouped exact nearest centroid for k <= 64: one block = a run of points of
+// one instance, its k x d centroids (and their norms) in shared memory.  The
+// scan uses the expanded form (||x||^2 + ||c||^2 - 2 x.c, one FMA per
+// coordinate and centroid, float4 loads).  Each value is within
+// eps = 2 (d + 8) u (||x||^2 + max ||c||^2) of the exact distance, so only the
+// centroids within 2 eps of the best (the band, usually one or two) can be the
+// nearest.  The band is re-evaluated by direct differences (relative error
+// (d + 4) u); when its best two are closer than that they are decided in FP64,
+// sequential over coordinates, lowest index on equality (yael/nn.c:404-435
+// semantics).  The reported distance is the direct-difference value.
+template <int K, bool VEC>
 __global__ void __launch_bounds__(256)
     assign_small_kernel(const KmWork *__restrict__ work, const float *__restrict__ v, int d,
                         const float *__restrict__ C, int k, const unsigned char *active,
                         int *assign, float *dis) {
-  extern __shared__ float cs[];  // the instance's k x d centroids
+  extern __shared__ __align__(16) float cs[];  // k x d centroids, then k norms
+  float *cn = cs + (((long)k * d + 3) & ~3L);
+  __shared__ float s_cmax;
   const KmWork w = work[blockIdx.x];
   if (!active[w.inst]) return;
   const float *Ci = C + (long)w.inst * k * d;
   for (int i = threadIdx.x; i < k * d; i += blockDim.x) cs[i] = Ci[i];
   __syncthreads();
-  const float rho = (float)(d + 4) * kU;
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    float sn = 0.f;
+    for (int c = 0; c < d; c++) sn = fmaf(cs[j * d + c], cs[j * d + c], sn);
+    cn[j] = sn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int j = 0; j < k; j++) m = fmaxf(m, cn[j]);
+    s_cmax = m;
+  }
+  __syncthreads();
+  const float cmax = s_cmax;
   for (int pi = threadIdx.x; pi < w.n; pi += blockDim.x) {
     const long p = w.p0 + pi;
     const float *x = v + p * d;
     float acc[K];
 #pragma unroll
     for (int j = 0; j < K; j++) acc[j] = 0.f;
-    for (int c = 0; c < d; c++) {
-      const float xv = __ldg(x + c);
+    float xn = 0.f;
+    if (VEC) {
+      const float4 *x4 = reinterpret_cast<const float4 *>(x);
+      for (int c4 = 0; c4 < (d >> 2); c4++) {
+        const float4 xv = __ldg(x4 + c4);
+        xn = fmaf(xv.x, xv.x, xn);
+        xn = fmaf(xv.y, xv.y, xn);
+        xn = fmaf(xv.z, xv.z, xn);
+        xn = fmaf(xv.w, xv.w, xn);
 #pragma unroll
-      for (int j = 0; j < K; j++) {
-        if (j < k) {
-          const float t = xv - cs[j * d + c];
-          acc[j] = fmaf(t, t, acc[j]);
+        for (int j = 0; j < K; j++) {
+          if (j < k) {
+            const float4 cv = *reinterpret_cast<const float4 *>(cs + j * d + 4 * c4);
+            acc[j] = fmaf(xv.x, cv.x, acc[j]);
+            acc[j] = fmaf(xv.y, cv.y, acc[j]);
+            acc[j] = fmaf(xv.z, cv.z, acc[j]);
+            acc[j] = fmaf(xv.w, cv.w, acc[j]);
+          }
         }
+      }
+    } else {
+      for (int c = 0; c < d; c++) {
+        const float xv = __ldg(x + c);
+        xn = fmaf(xv, xv, xn);
+#pragma unroll
+        for (int j = 0; j < K; j++)
+          if (j < k) acc[j] = fmaf(xv, cs[j * d + c], acc[j]);
       }
     }
     // strict '<' from 1e30 over increasing j (yael/nn.c:404-435)
@@ -43,7 +86,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int j = 0; j < K; j++) {
       if (j < k) {
-        const float a = acc[j];
+        const float a = (xn + cn[j]) - 2.f * acc[j];
         if (a < b1) {
           b2 = b1;
           b1 = a;
@@ -53,24 +96,61 @@ __global__ void __launch_bounds__(256)
         }
       }
     }
-    float out = b1;
-    if (i1 >= 0 && b2 < 1e30f && b2 - b1 <= rho * (b1 + b2)) {
-      // near tie: FP64, sequential over coordinates, lowest index on equality
-      double best = INFINITY;
-      int bi = -1;
-      for (int j = 0; j < k; j++) {
-        double s = 0;
+    // band: every centroid that can still be the nearest (its expanded value is
+    // within 2 eps of the best); non-band centroids are certified farther
+    const float tol = 4.f * (float)(d + 8) * kU * (xn + cmax);
+    unsigned long long band = 0;
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      if (j < k) {
+        const float a = (xn + cn[j]) - 2.f * acc[j];
+        if (!(a > b1 + tol)) band |= 1ull << j;
+      }
+    }
+    float out = 1e30f;
+    if (i1 >= 0) {
+      // direct differences for the band, sequential over coordinates; strict
+      // '<' over increasing j
+      const float rho = (float)(d + 4) * kU;
+      float e1 = INFINITY, e2 = INFINITY;
+      int j1 = -1;
+      for (unsigned long long bm = band; bm; bm &= bm - 1) {
+        const int j = __ffsll((long long)bm) - 1;
+        float sd = 0.f;
         for (int c = 0; c < d; c++) {
-          const double t = (double)x[c] - (double)cs[j * d + c];
-          s += t * t;
+          const float t = x[c] - cs[j * d + c];
+          sd = fmaf(t, t, sd);
         }
-        if (s < best) {
-          best = s;
-          bi = j;
+        if (sd < e1) {
+          e2 = e1;
+          e1 = sd;
+          j1 = j;
+        } else if (sd < e2) {
+          e2 = sd;
         }
       }
-      i1 = bi;
-      out = (float)best;
+      if (e2 < INFINITY && e2 - e1 <= rho * (e1 + e2)) {
+        // near tie: FP64, sequential over coordinates, lowest index on equality
+        double best = INFINITY;
+        int bi = -1;
+        for (unsigned long long bm = band; bm; bm &= bm - 1) {
+          const int j = __ffsll((long long)bm) - 1;
+          double sd = 0;
+          for (int c = 0; c < d; c++) {
+            const double t = (double)x[c] - (double)cs[j * d + c];
+            sd += t * t;
+          }
+          if (sd < best) {
+            best = sd;
+            bi = j;
+          }
+        }
+        i1 = bi;
+        out = bi >= 0 ? (float)best : 1e30f;
+      } else {
+        i1 = j1;
+        out = j1 >= 0 ? e1 : 1e30f;
+      }
     }
     assign[p] = i1;
     dis[p] = out;
@@ -137,6 +217,35 @@ __global__ void scatter_kernel(const int *assign, const int *pinst, long n, int 
   perm[base + __popc(peers & ((1u << lane) - 1))] = p;
 }
 
+// llrint(x * 2^S) (round to nearest, ties to even) of a float x, with integer
+// operations only (the FP64 pipe of this GPU is narrow).  The caller's shift
+// keeps |x| 2^S < 2^62; non-finite x gives 0.
+__device__ __forceinline__ long long fixed_of(float x, int S) {
+  const unsigned u = __float_as_uint(x);
+  const int ex = (int)((u >> 23) & 0xffu);
+  if (ex == 0xff) return 0;
+  unsigned long long m = u & 0x7fffffu;
+  int e = -149;  // x = +-m 2^e
+  if (ex != 0) {
+    m |= 0x800000u;
+    e = ex - 150;
+  }
+  const int sh = e + S;
+  unsigned long long r;
+  if (sh >= 0) {
+    r = m << sh;
+  } else if (-sh > 24) {
+    r = 0;  // m < 2^24 <= half of the unit in the last place kept
+  } else {
+    const int rs = -sh;
+    const unsigned long long q = m >> rs;
+    const unsigned long long rem = m & ((1ull << rs) - 1);
+    const unsigned long long half = 1ull << (rs - 1);
+    r = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+  }
+  return (u >> 31) ? -(long long)r : (long long)r;
+}
+
 // warps walk contiguous runs of the cluster-sorted point list, accumulating
 // exact integer sums in registers and flushing at cluster boundaries
 template <int NDR>
@@ -172,11 +281,11 @@ __global__ void __launch_bounds__(256)
       }
       gcur = g;
     }
-    const double sc = ldexp(1.0, shift[inst]);
+    const int sh = shift[inst];
 #pragma unroll
     for (int r = 0; r < NDR; r++) {
       const int c = dbase + r * 32 + lane;
-      if (c < d) part[r] += __double2ll_rn((double)__ldg(v + p * d + c) * sc);
+      if (c < d) part[r] += fixed_of(__ldg(v + p * d + c), sh);
     }
   }
   if (gcur >= 0) {
@@ -248,19 +357,30 @@ __global__ void gather_kernel(const float *v, int d, const long *rows, long nrow
   C[i] = v[rows[r] * d + (i - r * d)];
 }
 
-template <int K>
+template <int K, bool VEC>
 int launch_assign(const KmWork *work, int nwork, const float *v, int d, const float *C, int k,
                   const unsigned char *active, int *assign, float *dis, cudaStream_t st) {
-  const size_t smem = (size_t)k * d * sizeof(float);
+  const size_t smem = (size_t)((((long)k * d + 3) & ~3L) + k) * sizeof(float);
   static size_t attr = 48 * 1024;
   if (smem > attr) {
-    YG_CUDA(cudaFuncSetAttribute(assign_small_kernel<K>,
+    YG_CUDA(cudaFuncSetAttribute(assign_small_kernel<K, VEC>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = smem;
   }
-  assign_small_kernel<K><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign, dis);
+  assign_small_kernel<K, VEC><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign, dis);
   YG_LAUNCH_CHECK();
   return OK;
+}
+
+template <int K>
+int launch_assign_any(const KmWork *work, int nwork, const float *v, int d, const float *C,
+                      int k, const unsigned char *active, int *assign, float *dis,
+                      cudaStream_t st) {
+  // float4 rows need d % 4 == 0 and 16-byte aligned points and centroids
+  const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(v) & 15) == 0) &&
+                   ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+  if (vec) return launch_assign<K, true>(work, nwork, v, d, C, k, active, assign, dis, st);
+  return launch_assign<K, false>(work, nwork, v, d, C, k, active, assign, dis, st);
 }
 
 }  // namespace
@@ -269,14 +389,14 @@ int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const 
                     int k, const unsigned char *active, int *assign, float *dis,
                     cudaStream_t st) {
   if (nwork <= 0) return OK;
-  if ((size_t)k * d * 4 > 200 * 1024) {
+  if ((size_t)k * d * 4 + (size_t)k * 4 + 16 > 200 * 1024) {
     set_error(E_UNSUPPORTED, "grouped assignment: k*d=%ld too large for shared memory",
               (long)k * d);
     return E_UNSUPPORTED;
   }
-  if (k <= 16) return launch_assign<16>(work, nwork, v, d, C, k, active, assign, dis, st);
-  if (k <= 32) return launch_assign<32>(work, nwork, v, d, C, k, active, assign, dis, st);
-  if (k <= 64) return launch_assign<64>(work, nwork, v, d, C, k, active, assign, dis, st);
+  if (k <= 16) return launch_assign_any<16>(work, nwork, v, d, C, k, active, assign, dis, st);
+  if (k <= 32) return launch_assign_any<32>(work, nwork, v, d, C, k, active, assign, dis, st);
+  if (k <= 64) return launch_assign_any<64>(work, nwork, v, d, C, k, active, assign, dis, st);
   set_error(E_ARG, "grouped assignment: k=%d > %d", k, kSmallK);
   return E_ARG;
 }
