@@ -227,12 +227,14 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     // ---- THRESH: per-query thresholds from a strided sample of the base.
     // The c-th smallest of a 1/stride sample lies below ~c*stride base values;
     // with stride = k/3 the chance that fewer than k fall below it is the
-    // chance that a Poisson(3) exceeds c-1 (c = 16: ~3e-7 per query).
+    // chance that a Poisson(3) exceeds c-1 (c = 12: ~1.7e-4 per query; such a
+    // query fails its certificate and the band pass settles it).  The sample
+    // pass keeps 16 values per row; the c-th of them is the threshold.
     sel.mode = SCAN_THRESH;
     sel.halves = 2;
     float *thr;
     YG_CHECK(ws_get(ws, WS_THR, nq, &thr));
-    const int c = 16;
+    const int c = 12;
     int stride = k / 3;
     if (stride < 1) stride = 1;
     const int ns = nb / stride;
@@ -257,14 +259,14 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       sel.cap = pow2_at_least((int)(2.0 * er + 6.0 * sqrt(er) + 16.0));
       ScanSel ss;
       ss.mode = SCAN_TOPV;  // only the c-th value is needed
-      ss.C = c;
+      ss.C = 16;
       const int nts = (int)ceil_div(ns, tile_n);
       int nch = choose_chunks(nqt, nts, ctx->num_sms, ctas_per_sm, 2);
       nch = imin(nch, 64);
       ss.tiles_per_chunk = (int)ceil_div(nts, nch);
       ss.nchunk = (int)ceil_div(nts, ss.tiles_per_chunk);
-      YG_CHECK(ws_get(ws, WS_STOPV, (size_t)ss.nchunk * nq * c, &ss.topv));
-      YG_CHECK(ws_get(ws, WS_STOPI, (size_t)ss.nchunk * nq * c, &ss.topi));
+      YG_CHECK(ws_get(ws, WS_STOPV, (size_t)ss.nchunk * nq * ss.C, &ss.topv));
+      YG_CHECK(ws_get(ws, WS_STOPI, (size_t)ss.nchunk * nq * ss.C, &ss.topi));
       tm_sample.reset(new PassTimer(timed, st, &job.ms_sample));
       if (bf16) {
         TcOperands tcs = tcq;
@@ -275,7 +277,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
                            job.metric, ss, st));
       }
       tm_sample->stop(st);
-      YG_CHECK(thresh_from_sample(nq, ss.nchunk, c, c, ss.topv, eps, thr, st));
+      YG_CHECK(thresh_from_sample(nq, ss.nchunk, ss.C, c, ss.topv, eps, thr, st));
     }
     sel.thr = thr;
     const int nr = sel.nregion();

@@ -10,6 +10,7 @@ namespace yg {
 namespace {
 
 constexpr int RT = 256;  // threads per re-rank block
+constexpr int kMaxRegions = 2048;  // candidate regions per query (chunks x halves)
 constexpr float kU = 5.9604645e-08f;  // 2^-24
 
 __device__ __forceinline__ bool lex_less(unsigned long long ka, int ia,
@@ -18,9 +19,17 @@ __device__ __forceinline__ bool lex_less(unsigned long long ka, int ia,
 }
 
 // ascending bitonic sort of n (power of two) (key, id) pairs in shared memory
+// Ascending bitonic sort of n (a power of two) keys with ids, by the whole
+// block.  In a stage of stride s <= 32, thread i handles pairs inside elements
+// [64 (i/32 + r blockDim/32), +64) (r = 0, 1, ...): the same 64-element
+// segments for its warp in every such stage.  So a stage of stride <= 16 (its
+// predecessor has stride <= 32, hence was warp-local too) needs only a warp
+// barrier; stages of stride >= 32 follow a stage that may have crossed
+// segments and take a block barrier.
 __device__ void bitonic_sort(unsigned long long *K, int *I, int n) {
   for (int size = 2; size <= n; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride >= 32) __syncthreads();
       for (int i = threadIdx.x; i < (n >> 1); i += blockDim.x) {
         const int lo = 2 * i - (i & (stride - 1));
         const int hi = lo + stride;
@@ -33,9 +42,10 @@ __device__ void bitonic_sort(unsigned long long *K, int *I, int n) {
           I[lo] = ihi; I[hi] = ilo;
         }
       }
-      __syncthreads();
+      __syncwarp();
     }
   }
+  __syncthreads();
 }
 
 __device__ __forceinline__ int next_pow2(int x) {
@@ -121,19 +131,25 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
       }
     }
   } else {
-    // regions (chunk, half) of this query; any overflowing region fails the query
+    // regions (chunk, half) of this query; any overflowing region fails the
+    // query.  Offsets first (one thread), then one sweep over all regions.
     const int nreg = s.nregion();
-    for (int r = 0; r < nreg; r++) {
-      const int cnt = s.cnt[(long)r * a.nq + q];
-      if (cnt > s.cap) {
-        if (tid == 0) sfail = 1;
-        break;
+    __shared__ int s_off[kMaxRegions + 1];
+    if (tid == 0) {
+      int tot = 0;
+      for (int r = 0; r < nreg; r++) {
+        const int cnt = s.cnt[(long)r * a.nq + q];
+        if (cnt > s.cap) sfail = 1;
+        if (r < kMaxRegions) s_off[r] = tot;
+        tot += cnt;
       }
-      __shared__ int sbase;
-      if (tid == 0) { sbase = sM; sM += cnt; }
-      __syncthreads();
-      const int base = sbase;
-      if (base + cnt <= Mp_alloc) {
+      if (nreg <= kMaxRegions) s_off[nreg] = tot; else sfail = 1;
+      sM = tot;
+    }
+    __syncthreads();
+    if (!sfail && sM <= Mp_alloc) {
+      for (int r = 0; r < nreg; r++) {
+        const int base = s_off[r], cnt = s_off[r + 1] - base;
         const long o = ((long)r * a.nq + q) * s.cap;
         for (int idx = tid; idx < cnt; idx += RT) {
           const float v = s.candv[o + idx];
@@ -142,7 +158,6 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
           I[base + idx] = s.candi[o + idx];
         }
       }
-      __syncthreads();
     }
   }
   __syncthreads();
