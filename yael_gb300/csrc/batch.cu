@@ -15,6 +15,7 @@
 #include <thread>
 #include <vector>
 
+#include "autotune.cuh"
 #include "knn.cuh"
 
 namespace yg {
@@ -33,6 +34,7 @@ struct BatchTask {
 };
 
 void run_pairs(BatchTask *t) {
+  tune_set_thread_enabled(false);  // concurrent pairs: timings not comparable
   if (cudaSetDevice(t->device) != cudaSuccess) {
     std::lock_guard<std::mutex> g(t->m);
     if (t->err == OK) { t->err = E_CUDA; t->msg = "cudaSetDevice failed in a batch worker"; }

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <memory>
 
+#include "autotune.cuh"
 #include "knn.cuh"
 #include "tc_scan.cuh"
 #include "../../include/yael_gpu.h"
@@ -93,6 +94,7 @@ __global__ void fill_f32(float *p, long n, float v) {
 struct PassTimer {
   cudaEvent_t a = nullptr, b = nullptr;
   float *dst;
+  float last = 0.f;  // the elapsed time of this pass, after collect()
   PassTimer(bool enable, cudaStream_t st, float *out) : dst(enable ? out : nullptr) {
     if (dst) {
       cudaEventCreate(&a);
@@ -106,7 +108,10 @@ struct PassTimer {
   void collect() {  // call after the stream has been synchronized
     if (!dst) return;
     float ms = 0;
-    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) *dst += ms;
+    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) {
+      *dst += ms;
+      last = ms;
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     dst = nullptr;
@@ -208,18 +213,21 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   const int c_needed = list_length(k, bstats_exact);
 
   std::unique_ptr<PassTimer> tm_scan, tm_sample;
+  int scan_ticket = -1, sample_ticket = -1;  // autotuner trials (autotune.cuh)
   ScanSel sel;
   if (!band && c_needed <= 16) {
     // ---- TOPC over the full base (register lists)
     sel.mode = SCAN_TOPC;
     sel.C = pow2_at_least(c_needed);
-    int nchunk = choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4);
-    nchunk = imin(nchunk, kMaxCandidates / sel.C);
+    const int nchunk = tune_chunks(TuneKey{0, job.prec, nqt, ntb, sel.C},
+                                   choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4),
+                                   imin(1024, kMaxCandidates / sel.C),
+                                   ctx->num_sms * ctas_per_sm, &scan_ticket);
     sel.tiles_per_chunk = (int)ceil_div(ntb, nchunk);
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     YG_CHECK(ws_get(ws, WS_TOPV, (size_t)sel.nchunk * nq * sel.C, &sel.topv));
     YG_CHECK(ws_get(ws, WS_TOPI, (size_t)sel.nchunk * nq * sel.C, &sel.topi));
-    tm_scan.reset(new PassTimer(timed, st, &job.ms_scan));
+    tm_scan.reset(new PassTimer(timed || scan_ticket >= 0, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
     tm_scan->stop(st);
     job.scan_launches++;
@@ -238,7 +246,10 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     int stride = k / 3;
     if (stride < 1) stride = 1;
     const int ns = nb / stride;
-    sel.nchunk = imin(choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 1024);
+    sel.nchunk = band ? 1
+                      : tune_chunks(TuneKey{1, job.prec, nqt, ntb, 0},
+                                    choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 1024,
+                                    ctx->num_sms * ctas_per_sm, &scan_ticket);
     sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
     sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     const int nreg = sel.nregion();
@@ -255,19 +266,21 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       fill_f32<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(thr, nq, INFINITY);
       YG_LAUNCH_CHECK();
     } else {
+      ra.m_expect = c * stride;
       const double er = (double)c * stride / nreg;  // expected hits per region
       sel.cap = pow2_at_least((int)(2.0 * er + 6.0 * sqrt(er) + 16.0));
       ScanSel ss;
       ss.mode = SCAN_TOPV;  // only the c-th value is needed
       ss.C = 16;
       const int nts = (int)ceil_div(ns, tile_n);
-      int nch = choose_chunks(nqt, nts, ctx->num_sms, ctas_per_sm, 2);
-      nch = imin(nch, 64);
+      const int nch = tune_chunks(TuneKey{2, job.prec, nqt, nts, ss.C},
+                                  choose_chunks(nqt, nts, ctx->num_sms, ctas_per_sm, 2), 64,
+                                  ctx->num_sms * ctas_per_sm, &sample_ticket);
       ss.tiles_per_chunk = (int)ceil_div(nts, nch);
       ss.nchunk = (int)ceil_div(nts, ss.tiles_per_chunk);
       YG_CHECK(ws_get(ws, WS_STOPV, (size_t)ss.nchunk * nq * ss.C, &ss.topv));
       YG_CHECK(ws_get(ws, WS_STOPI, (size_t)ss.nchunk * nq * ss.C, &ss.topi));
-      tm_sample.reset(new PassTimer(timed, st, &job.ms_sample));
+      tm_sample.reset(new PassTimer(timed || sample_ticket >= 0, st, &job.ms_sample));
       if (bf16) {
         TcOperands tcs = tcq;
         YG_CHECK(tc_base_view(tcq, stride, ns, &tcs));
@@ -284,13 +297,13 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     YG_CHECK(ws_get(ws, WS_CNT, (size_t)nr * nq, &sel.cnt));
     YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nr * nq * sel.cap, &sel.candv));
     YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nr * nq * sel.cap, &sel.candi));
-    tm_scan.reset(new PassTimer(timed, st, &job.ms_scan));
+    tm_scan.reset(new PassTimer(timed || scan_ticket >= 0, st, &job.ms_scan));
     YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
     tm_scan->stop(st);
     job.scan_launches++;
   }
   ra.sel = sel;
-  PassTimer tr(timed, st, &job.ms_rerank);
+  PassTimer tr(timed || scan_ticket >= 0, st, &job.ms_rerank);
   YG_CHECK(rerank(ra, st));
   tr.stop(st);
 
@@ -298,9 +311,16 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   Small hs;
   YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
   YG_CUDA(cudaStreamSynchronize(st));
-  if (tm_scan) tm_scan->collect();
-  if (tm_sample) tm_sample->collect();
   tr.collect();
+  if (tm_scan) {
+    tm_scan->collect();
+    // a chunk count also sets the candidate lists the re-rank reads
+    tune_report(scan_ticket, tm_scan->last + tr.last);
+  }
+  if (tm_sample) {
+    tm_sample->collect();
+    tune_report(sample_ticket, tm_sample->last);
+  }
   job.n_cand = (long long)hs.n_cand;
   const int nf = hs.fail_cnt;
   if (trace_enabled())
@@ -401,7 +421,9 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
     const int C = pow2_at_least(cn);
     size_t per_query;
     if (cn <= 16) {
-      const int nch = imin(choose_chunks(nqt, ntb, ctx->num_sms, 1, 4), kMaxCandidates / C);
+      // the autotuner may try up to 3x the heuristic's chunk count
+      const int nch = imin(imin(1024, kMaxCandidates / C),
+                           3 * choose_chunks(nqt, ntb, ctx->num_sms, 1, 4) + 2);
       per_query = (size_t)nch * C * 8 + 64;
     } else {
       per_query = (size_t)2 * kMaxCandidates * 8 + 64;

@@ -135,28 +135,52 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
     // query.  Offsets first (one thread), then one sweep over all regions.
     const int nreg = s.nregion();
     __shared__ int s_off[kMaxRegions + 1];
-    if (tid == 0) {
-      int tot = 0;
-      for (int r = 0; r < nreg; r++) {
-        const int cnt = s.cnt[(long)r * a.nq + q];
+    __shared__ int s_wsum[RT / 32];
+    if (nreg > kMaxRegions) {
+      if (tid == 0) sfail = 1;
+    } else {
+      // exclusive scan of the region counts, RT regions per round
+      int run = 0;
+      for (int r0 = 0; r0 < nreg; r0 += RT) {
+        const int r = r0 + tid;
+        int cnt = r < nreg ? s.cnt[(long)r * a.nq + q] : 0;
         if (cnt > s.cap) sfail = 1;
-        if (r < kMaxRegions) s_off[r] = tot;
-        tot += cnt;
+        int x = cnt;  // inclusive scan within the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, x, o);
+          if ((tid & 31) >= o) x += y;
+        }
+        if ((tid & 31) == 31) s_wsum[tid >> 5] = x;
+        __syncthreads();
+        int wpre = 0;
+        for (int w = 0; w < (tid >> 5); w++) wpre += s_wsum[w];
+        int tot = 0;
+        for (int w = 0; w < RT / 32; w++) tot += s_wsum[w];
+        if (r < nreg) s_off[r] = run + wpre + x - cnt;
+        run += tot;
+        __syncthreads();
       }
-      if (nreg <= kMaxRegions) s_off[nreg] = tot; else sfail = 1;
-      sM = tot;
+      if (tid == 0) {
+        s_off[nreg] = run;
+        sM = run;
+      }
     }
     __syncthreads();
     if (!sfail && sM <= Mp_alloc) {
-      for (int r = 0; r < nreg; r++) {
-        const int base = s_off[r], cnt = s_off[r + 1] - base;
-        const long o = ((long)r * a.nq + q) * s.cap;
-        for (int idx = tid; idx < cnt; idx += RT) {
-          const float v = s.candv[o + idx];
-          const float av = L2 ? (float)((double)v + qn) : v;
-          K[base + idx] = f2ord(av);
-          I[base + idx] = s.candi[o + idx];
+      // every slot at once: slot e belongs to the last region r with s_off[r] <= e
+      const int M0 = sM;
+      for (int e = tid; e < M0; e += RT) {
+        int lo = 0, hi = nreg - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_off[mid] <= e) lo = mid; else hi = mid - 1;
         }
+        const long o = ((long)lo * a.nq + q) * s.cap + (e - s_off[lo]);
+        const float v = s.candv[o];
+        const float av = L2 ? (float)((double)v + qn) : v;
+        K[e] = f2ord(av);
+        I[e] = s.candi[o];
       }
     }
   }
@@ -666,6 +690,9 @@ int rerank(const RerankArgs &a, cudaStream_t st) {
     return OK;
   }
   int Mmax = a.sel.mode == SCAN_TOPC ? a.sel.nchunk * a.sel.C : a.sel.nregion() * a.sel.cap;
+  if (a.sel.mode == SCAN_THRESH && a.m_expect > 0 && Mmax > 4 * a.m_expect + 64)
+    Mmax = 4 * a.m_expect + 64;
+  if (Mmax < a.k) Mmax = a.k;
   if (Mmax > kMaxCandidates) Mmax = kMaxCandidates;  // more candidates than this fail the query
   int Mp = 1;
   while (Mp < Mmax) Mp <<= 1;

@@ -37,6 +37,10 @@ struct RerankArgs {
   // optional: for each rejected query, an upper bound of its k-th smallest
   // exact distance (INFINITY when none was found), for the band pass
   float *kth_out = nullptr;
+  // THRESH: expected candidates per query (0: unknown); shared memory is
+  // sized for a few times this rather than for every region's capacity, and a
+  // query with more candidates fails its certificate (the band pass follows)
+  int m_expect = 0;
 };
 
 int rerank(const RerankArgs &a, cudaStream_t st);
