@@ -50,6 +50,8 @@ const char *last_message();
   } while (0)
 
 void count_launch();
+void count_launches(long n);  // kernels replayed by a CUDA graph launch
+long launch_count();
 #define YG_LAUNCH_CHECK()          \
   do {                             \
     ::yg::count_launch();          \

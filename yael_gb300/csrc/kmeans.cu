@@ -5,8 +5,10 @@
 // lrand48 in the same order, so runs are reproducible against it.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <memory>
 #include <unordered_map>
 #include <vector>
@@ -158,6 +160,56 @@ struct Engine {
   long n_fallback = 0, n_second = 0, n_band = 0;
   float ms_assign = 0, ms_update = 0;
 
+  // CUDA graphs of one Lloyd iteration's device work (grouped small-k path):
+  // the assignment and the update are captured on the second iteration (the
+  // first runs eagerly and sets every kernel attribute) and replayed after.
+  // Their arguments never change within a run: the per-iteration state (active
+  // instances, split centroids) lives in device buffers written between
+  // replays.  YAEL_GPU_GRAPHS=0 runs every iteration eagerly.
+  cudaGraphExec_t g_assign = nullptr, g_update = nullptr;
+  bool eager_done = false;
+  long g_assign_n = 0, g_update_n = 0;  // kernels per replay
+  bool graphs_failed = false;
+  int *ph_counts = nullptr;     // pinned copies the update graph writes
+  double *ph_part = nullptr;
+
+  ~Engine() {
+    if (g_assign) cudaGraphExecDestroy(g_assign);
+    if (g_update) cudaGraphExecDestroy(g_update);
+    if (ph_counts) cudaFreeHost(ph_counts);
+    if (ph_part) cudaFreeHost(ph_part);
+  }
+
+  bool graphs_wanted() const {
+    static const bool on = [] {
+      const char *e = getenv("YAEL_GPU_GRAPHS");
+      return !(e && e[0] == '0');
+    }();
+    return on && !graphs_failed && !(in.size() == 1 && k > kSmallK);
+  }
+
+  // captures body() on st into *exec; false (and eager mode) on any failure
+  template <typename F>
+  bool capture(F body, cudaGraphExec_t *exec, long *nlaunch) {
+    const long l0 = launch_count();
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    const int rc = body();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    bool ok = rc == OK && e == cudaSuccess && g != nullptr &&
+              cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      (void)cudaGetLastError();
+      *exec = nullptr;
+    }
+    *nlaunch = launch_count() - l0;
+    return ok;
+  }
+
   int setup() {
     Workspace &ws = ctx->ws;
     const int ni = (int)in.size();
@@ -208,6 +260,8 @@ struct Engine {
     YG_CUDA(cudaMemcpyAsync(shift, hs.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, st));
     hcounts.resize(ncl);
     hpart.resize(nsl);
+    YG_CUDA(cudaMallocHost(&ph_counts, sizeof(int) * (size_t)ncl));
+    YG_CUDA(cudaMallocHost(&ph_part, sizeof(double) * (size_t)std::max(1, nsl)));
     YG_CUDA(cudaStreamSynchronize(st));
     return OK;
   }
@@ -273,21 +327,44 @@ struct Engine {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventCreate(&e2);
+    auto update_body = [&]() -> int {
+      YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
+      YG_CHECK(km_histogram(assign, pinst, ntot, k, active, counts, st));
+      YG_CHECK(km_scan(counts, ncl, offs, cursor, st));
+      YG_CHECK(km_scatter(assign, pinst, ntot, k, active, cursor, perm, st));
+      YG_CHECK(km_update(perm, offs + ncl, ntot, assign, pinst, counts, v, d, ncl, k, shift,
+                         active, acc, C, st));
+      if (flags & YAEL_KMEANS_NORMALIZE_CENTS) YG_CHECK(km_normalize(C, ncl, d, k, active, st));
+      YG_CHECK(km_slice_sums(slices, nsl, dis, part, st));
+      YG_CUDA(cudaMemcpyAsync(ph_counts, counts, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
+      YG_CUDA(cudaMemcpyAsync(ph_part, part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
+      return OK;
+    };
+    const bool use_graphs = graphs_wanted() && eager_done;
+    if (use_graphs && !g_assign) {
+      if (!capture([&] { return assign_step(); }, &g_assign, &g_assign_n) ||
+          !capture(update_body, &g_update, &g_update_n))
+        graphs_failed = true;
+    }
     cudaEventRecord(e0, st);
-    YG_CHECK(assign_step());
+    if (use_graphs && !graphs_failed) {
+      YG_CUDA(cudaGraphLaunch(g_assign, st));
+      count_launches(g_assign_n);
+    } else {
+      YG_CHECK(assign_step());
+    }
     cudaEventRecord(e1, st);
-    YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
-    YG_CHECK(km_histogram(assign, pinst, ntot, k, active, counts, st));
-    YG_CHECK(km_scan(counts, ncl, offs, cursor, st));
-    YG_CHECK(km_scatter(assign, pinst, ntot, k, active, cursor, perm, st));
-    YG_CHECK(km_update(perm, offs + ncl, ntot, assign, pinst, counts, v, d, ncl, k, shift, active,
-                       acc, C, st));
-    if (flags & YAEL_KMEANS_NORMALIZE_CENTS) YG_CHECK(km_normalize(C, ncl, d, k, active, st));
-    YG_CHECK(km_slice_sums(slices, nsl, dis, part, st));
-    YG_CUDA(cudaMemcpyAsync(hcounts.data(), counts, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
-    YG_CUDA(cudaMemcpyAsync(hpart.data(), part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
+    if (use_graphs && !graphs_failed) {
+      YG_CUDA(cudaGraphLaunch(g_update, st));
+      count_launches(g_update_n);
+    } else {
+      YG_CHECK(update_body());
+    }
+    eager_done = true;
     cudaEventRecord(e2, st);
     YG_CUDA(cudaStreamSynchronize(st));
+    std::copy(ph_counts, ph_counts + ncl, hcounts.begin());
+    std::copy(ph_part, ph_part + nsl, hpart.begin());
     float a = 0, b = 0;
     cudaEventElapsedTime(&a, e0, e1);
     cudaEventElapsedTime(&b, e1, e2);

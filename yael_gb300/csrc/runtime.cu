@@ -13,6 +13,7 @@ namespace yg {
 
 static std::atomic<long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(); }
 
 static thread_local int t_code = OK;
