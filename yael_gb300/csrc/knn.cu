@@ -75,12 +75,14 @@ __global__ void gather_kth_kernel(const float *in_kth, const float *out_kth, con
 }
 
 // per-thread list length of a TOPC pass: k when the distances are exact, else
-// an oversampled list whose extra entries give the certificate its margin (k = 1
-// keeps two: longer lists make the epilogue's insertions the bottleneck, and
-// the band pass settles what they would have)
-int list_length(int k, int exact) {
+// an oversampled list whose extra entries give the certificate its margin.
+// k = 1 (k-means assignment) does not depend on exactness: lists of two over
+// large bases (longer lists make the epilogue's insertions the bottleneck, and
+// the band pass settles what they would have), of eight over small ones (the
+// pass is cheap, a band pass would cost more than the longer list).
+int list_length(int k, int exact, int nb) {
+  if (k == 1) return nb <= 8192 ? 8 : 2;
   if (exact) return k;
-  if (k == 1) return 2;
   return k <= 4 ? 8 : 2 * k;
 }
 
@@ -210,7 +212,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   const int ctas_per_sm = 1;
   // oversampling for inexact distances: the certificate needs a margin between
   // the k-th exact value and the first excluded candidate
-  const int c_needed = list_length(k, bstats_exact);
+  const int c_needed = list_length(k, bstats_exact, nb);
 
   std::unique_ptr<PassTimer> tm_scan, tm_sample;
   int scan_ticket = -1, sample_ticket = -1;  // autotuner trials (autotune.cuh)
@@ -322,6 +324,11 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     tune_report(sample_ticket, tm_sample->last);
   }
   job.n_cand = (long long)hs.n_cand;
+  job.exact_class = hs.bs.all_exact;
+  if (hs.tc_err) {
+    set_error(E_TIMEOUT, "tensor-core pass gave up waiting (bounded wait expired)");
+    return E_TIMEOUT;
+  }
   const int nf = hs.fail_cnt;
   if (trace_enabled())
     fprintf(stderr,
@@ -416,7 +423,7 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
                    (size_t)qbatch > budget)
       qbatch = (qbatch + 1) / 2;
   } else {
-    const int cn = list_length(k, bexact);
+    const int cn = list_length(k, bexact, nb);
     const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
     const int C = pow2_at_least(cn);
     size_t per_query;
@@ -451,6 +458,7 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
     job.ms_rerank += sub.ms_rerank;
     job.ms_second += sub.ms_second;
     job.scan_launches += sub.scan_launches;
+    job.exact_class = sub.exact_class;
   }
   job.n_cand = ncand;
   return OK;
@@ -531,22 +539,18 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     YG_CHECK(prep_rows(job.b, job.ldb, nb, d, 1.f, nullptr, bn32, nullptr, bres, nullptr, 0,
                        nullptr, 0, &dsmall->bs, st));
   }
-  Small hs;
-  YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
-  YG_CUDA(cudaStreamSynchronize(st));
-  const int bexact = hs.bs.all_exact;
-  job.exact_class = bexact;
-  bops.plain.err = bops.split.err = &dsmall->tc_err;
-
-  YG_CHECK(knn_batches(job, ctx, st, dsmall, &bops, bexact));
-  if (job.prec != PREC_FP32) {
+  // the list length of k > 1 depends on whether the base is exact class (k = 1
+  // does not: no host round trip then); every later read of the small state
+  // also checks the tensor-core passes' error flag
+  int bexact = 0;
+  if (k > 1) {
+    Small hs;
     YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
     YG_CUDA(cudaStreamSynchronize(st));
-    if (hs.tc_err) {
-      set_error(E_TIMEOUT, "tensor-core pass gave up waiting (bounded wait expired)");
-      return E_TIMEOUT;
-    }
+    bexact = hs.bs.all_exact;
   }
+  bops.plain.err = bops.split.err = &dsmall->tc_err;
+  YG_CHECK(knn_batches(job, ctx, st, dsmall, &bops, bexact));
   return OK;
 }
 
