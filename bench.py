@@ -493,13 +493,13 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import yael_gb300 as yg
-    from yael_gb300 import synth
+    from yael_gb300 import replicas, synth
     L = yg.lib()
     dev = torch.device("cuda", local)
 
     # the same base on every rank, a different query set per rank (replicas: weak scaling)
     b_h = synth.sift_like(args.nb, args.d, seed=1)
-    q_h = synth.sift_like(args.nq, args.d, seed=2 + 1000 * rank)
+    q_h = synth.sift_like(args.nq, args.d, seed=replicas.query_seed(rank))
     b = torch.from_numpy(b_h).to(dev)
     q = torch.from_numpy(q_h).to(dev)
     idx = torch.empty((args.nq, args.k), dtype=torch.int32, device=dev)
@@ -538,14 +538,11 @@ def main():
             torch.cuda.synchronize(dev)
         ms = ev0.elapsed_time(ev1)
         launches = L.yael_gpu_launch_count() - l0
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(ms, dist, dev)
         return ms, launches, scan_ms / max(1, scan_n), fb, clk.summary(), sample_ms / steps, rr_ms / steps
 
     ms, launches, scan_ms, fb, clocks, sample_ms, rr_ms = timed(prec, args.steps, args.warmup)
-    qps = world * args.nq * args.steps / (ms / 1e3)
+    qps = replicas.whole_job_rate(args.nq * args.steps, ms / 1e3, world)
 
     # parity spot check of the timed configuration (first 64 queries, FP64 oracle)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -586,11 +583,8 @@ def main():
         for _ in range(args.e2e_steps):
             e2e_step()
         e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_qps = world * args.nq * args.e2e_steps / e2e_s if e2e_s > 0 else None
+    e2e_s = replicas.max_over_ranks(e2e_s, dist, dev)
+    e2e_qps = replicas.whole_job_rate(args.nq * args.e2e_steps, e2e_s, world) if e2e_s > 0 else None
 
     if rank != 0:
         if dist:
