@@ -266,3 +266,21 @@ def test_cta_pair_kernel_matches():
     r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
                        text=True, timeout=300)
     assert r.returncode == 0 and "pair ok" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("k", [1, 8, 100])
+def test_host_upload_in_parts(k):
+    """Host arrays with a large base go up in parts overlapped with the passes
+    (thresholds from the first part); ids are still exact, including a base
+    whose parts differ (sorted rows: part 0 is not representative)."""
+    rng = np.random.default_rng(91)
+    nb, nq, d = 300_000, 300, 64
+    b = rng.standard_normal((nb, d)).astype(np.float32)
+    b = b[np.argsort(b[:, 0])]  # ordered rows: a worst case for the first-part sample
+    q = rng.standard_normal((nq, d)).astype(np.float32)
+    idx, dis, st = gpu_knn(b, q, k, "bf16")
+    ridx, rdis, r64 = knn_exact(b, q, k, NT)
+    mism = np.nonzero((idx != ridx).any(1))[0]
+    if len(mism):
+        assert check_knn_ties(idx, exact_dist64(b, q, idx), ridx, r64) == 0
+    np.testing.assert_allclose(dis, rdis, rtol=2e-6, atol=1e-5)

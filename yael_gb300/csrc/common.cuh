@@ -81,6 +81,7 @@ struct Ctx {
   int cc_major = 0, cc_minor = 0;
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host uploads overlapped with passes (lazy)
   Workspace ws;
   Workspace host_ws;  // pinned host staging
 };

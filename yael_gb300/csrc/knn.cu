@@ -30,6 +30,7 @@ struct Small {
 struct BaseOps {
   TcOperands plain, split;
   bool has_plain = false, has_split = false;
+  float *bn32 = nullptr, *res = nullptr;  // plain packing: per-row norms and residuals
 };
 
 template <typename T>
@@ -97,12 +98,16 @@ struct PassTimer {
   cudaEvent_t a = nullptr, b = nullptr;
   float *dst;
   float last = 0.f;  // the elapsed time of this pass, after collect()
-  PassTimer(bool enable, cudaStream_t st, float *out) : dst(enable ? out : nullptr) {
+  PassTimer(bool enable, cudaStream_t st, float *out, bool start_now = true)
+      : dst(enable ? out : nullptr) {
     if (dst) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
-      cudaEventRecord(a, st);
+      if (start_now) cudaEventRecord(a, st);
     }
+  }
+  void start(cudaStream_t st) {
+    if (dst) cudaEventRecord(a, st);
   }
   void stop(cudaStream_t st) {
     if (dst) cudaEventRecord(b, st);
@@ -153,6 +158,65 @@ BandLayout band_layout(int nq, int nb, int k, int tile_m, int tile_n, int halves
 
 int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bops,
                 int bexact);
+
+// Chunk layout of a main pass over a base that arrives part by part: part i
+// gets nch[i] chunks of tpc[i] tiles, its lists / regions start at chunk
+// first[i]; the total is returned.
+int part_chunks(const BaseUpload &up, int kind, int prec, int C, int nqt, int tile_n, int slots,
+                int cmax, int *nch, int *tpc, int *first, int *ticket) {
+  int tot = 0;
+  for (int i = 0; i < up.nparts; i++) {
+    const int ntb = (int)ceil_div(up.row0[i + 1] - up.row0[i], tile_n);
+    // each part shape is tuned on its own pass time (the re-rank cost does
+    // not depend on the chunk count)
+    const int c = tune_chunks(TuneKey{kind, prec, nqt, ntb, C},
+                              imin(cmax, choose_chunks(nqt, ntb, slots, 1, 4)), cmax, slots,
+                              &ticket[i]);
+    tpc[i] = (int)ceil_div(ntb, c);
+    nch[i] = (int)ceil_div(ntb, tpc[i]);
+    first[i] = tot;
+    tot += nch[i];
+  }
+  return tot;
+}
+
+// the main pass over every part of an uploading base: each part is packed
+// once it has landed, then scanned into its own lists / regions with ids
+// offset by its first row
+int scan_parts(const KnnJob &job, BaseUpload &up, const BaseOps &bops, Small *dsmall,
+               const TcOperands &tcq, int nq, const ScanSel &sel, const int *nch,
+               const int *tpc, const int *first, std::unique_ptr<PassTimer> *ptm,
+               cudaStream_t st) {
+  for (int i = 0; i < up.nparts; i++) {
+    const long r0 = up.row0[i];
+    const int n = (int)(up.row0[i + 1] - r0);
+    if (!up.packed[i]) {
+      YG_CUDA(cudaStreamWaitEvent(st, up.ready[i], 0));
+      YG_CHECK(tc_prepare_base_range(job.b, job.ldb, r0, n, job.d, job.metric, bops.plain,
+                                     bops.bn32, bops.res, &dsmall->bs, st));
+      up.packed[i] = true;
+    }
+    ScanSel si = sel;
+    si.nchunk = nch[i];
+    si.tiles_per_chunk = tpc[i];
+    si.id_off = (int)r0;
+    if (sel.mode == SCAN_THRESH) {
+      const long reg = (long)first[i] * sel.halves;
+      si.cnt = sel.cnt + reg * nq;
+      si.candv = sel.candv + reg * nq * sel.cap;
+      si.candi = sel.candi + reg * nq * sel.cap;
+    } else {
+      si.topv = sel.topv + (long)first[i] * nq * sel.C;
+      si.topi = sel.topi + (long)first[i] * nq * sel.C;
+    }
+    TcOperands tp;
+    YG_CHECK(tc_base_slice(tcq, r0, n, &tp));
+    if (ptm[i]) ptm[i]->start(st);
+    YG_CHECK(tc_scan(tp, nq, n, si, st));
+    if (ptm[i]) ptm[i]->stop(st);
+  }
+  return OK;
+}
 
 // one batch of queries (all buffers sized for nq of this batch)
 int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bops,
@@ -217,7 +281,27 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   std::unique_ptr<PassTimer> tm_scan, tm_sample;
   int scan_ticket = -1, sample_ticket = -1;  // autotuner trials (autotune.cuh)
   ScanSel sel;
-  if (!band && c_needed <= 16) {
+  BaseUpload *up = (job.upload && !band && bf16 && !split) ? job.upload : nullptr;
+  int pnch[BaseUpload::kMaxParts], ptpc[BaseUpload::kMaxParts], pfirst[BaseUpload::kMaxParts];
+  int pticket[BaseUpload::kMaxParts];
+  float part_ms[BaseUpload::kMaxParts] = {};
+  std::unique_ptr<PassTimer> ptm[BaseUpload::kMaxParts];
+  if (up && !band && c_needed <= 16) {
+    // ---- TOPC, base arriving part by part
+    sel.mode = SCAN_TOPC;
+    sel.C = pow2_at_least(c_needed);
+    sel.nchunk = part_chunks(*up, 0, job.prec, sel.C, nqt, tile_n, ctx->num_sms * ctas_per_sm,
+                             imin(1024, kMaxCandidates / sel.C) / up->nparts, pnch, ptpc, pfirst,
+                             pticket);
+    YG_CHECK(ws_get(ws, WS_TOPV, (size_t)sel.nchunk * nq * sel.C, &sel.topv));
+    YG_CHECK(ws_get(ws, WS_TOPI, (size_t)sel.nchunk * nq * sel.C, &sel.topi));
+    for (int i = 0; i < up->nparts; i++)
+      if (pticket[i] >= 0) ptm[i].reset(new PassTimer(true, st, &part_ms[i], false));
+    tm_scan.reset(new PassTimer(timed, st, &job.ms_scan));
+    YG_CHECK(scan_parts(job, *up, *bops, dsmall, tcq, nq, sel, pnch, ptpc, pfirst, ptm, st));
+    tm_scan->stop(st);
+    job.scan_launches += up->nparts;
+  } else if (!band && c_needed <= 16) {
     // ---- TOPC over the full base (register lists)
     sel.mode = SCAN_TOPC;
     sel.C = pow2_at_least(c_needed);
@@ -248,13 +332,30 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     int stride = k / 3;
     if (stride < 1) stride = 1;
     const int ns = nb / stride;
-    sel.nchunk = band ? 1
-                      : tune_chunks(TuneKey{1, job.prec, nqt, ntb, 0},
-                                    choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4), 1024,
-                                    ctx->num_sms * ctas_per_sm, &scan_ticket);
-    sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
-    sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    if (up) {
+      sel.nchunk = part_chunks(*up, 1, job.prec, 0, nqt, tile_n, ctx->num_sms * ctas_per_sm,
+                               1024 / up->nparts, pnch, ptpc, pfirst, pticket);
+      for (int i = 0; i < up->nparts; i++)
+        if (pticket[i] >= 0) ptm[i].reset(new PassTimer(true, st, &part_ms[i], false));
+    } else {
+      sel.nchunk = band ? 1
+                        : tune_chunks(TuneKey{1, job.prec, nqt, ntb, 0},
+                                      choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4),
+                                      1024, ctx->num_sms * ctas_per_sm, &scan_ticket);
+      sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
+      sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
+    }
     const int nreg = sel.nregion();
+    // the threshold sample: every stride-th row of the base, or, while the base
+    // is still arriving, every stride0-th row of part 0 (same sample size, so
+    // the same expected rank if the rows are in no particular order; any
+    // other order only costs candidates or band passes, never exactness)
+    int sstride = stride, sns = ns;
+    if (up) {
+      const long n0 = up->row0[1] - up->row0[0];
+      sstride = (int)std::max<long>(1, (long)((double)stride * n0 / nb));
+      sns = (int)(n0 / sstride);
+    }
     if (band) {
       // thresholds from the k-th exact distance an earlier pass found
       const BandLayout L = band_layout(nq, nb, k, tile_m, tile_n, sel.halves, ctx->num_sms);
@@ -262,7 +363,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       sel.tiles_per_chunk = L.tiles_per_chunk;
       sel.cap = L.cap;
       YG_CHECK(band_thresholds(nq, job.metric, job.band_kth, qn64, eps, thr, st));
-    } else if (nb <= kMaxCandidates || ns < 4 * c) {
+    } else if (nb <= kMaxCandidates || sns < 4 * c) {
       // every base row is a candidate; a region holds at most its share of the chunk
       sel.cap = pow2_at_least(imax(1, sel.tiles_per_chunk * tile_n / sel.halves));
       fill_f32<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(thr, nq, INFINITY);
@@ -274,7 +375,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       ScanSel ss;
       ss.mode = SCAN_TOPV;  // only the c-th value is needed
       ss.C = 16;
-      const int nts = (int)ceil_div(ns, tile_n);
+      const int nts = (int)ceil_div(sns, tile_n);
       const int nch = tune_chunks(TuneKey{2, job.prec, nqt, nts, ss.C},
                                   choose_chunks(nqt, nts, ctx->num_sms, ctas_per_sm, 2), 64,
                                   ctx->num_sms * ctas_per_sm, &sample_ticket);
@@ -285,8 +386,8 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       tm_sample.reset(new PassTimer(timed || sample_ticket >= 0, st, &job.ms_sample));
       if (bf16) {
         TcOperands tcs = tcq;
-        YG_CHECK(tc_base_view(tcq, stride, ns, &tcs));
-        YG_CHECK(tc_scan(tcs, nq, ns, ss, st));
+        YG_CHECK(tc_base_view(tcq, sstride, sns, &tcs));
+        YG_CHECK(tc_scan(tcs, nq, sns, ss, st));
       } else {
         YG_CHECK(simt_scan(job.q, job.ldq, nq, job.b, job.ldb * stride, ns, d, bn32, stride,
                            job.metric, ss, st));
@@ -300,9 +401,19 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     YG_CHECK(ws_get(ws, WS_TOPV, (size_t)nr * nq * sel.cap, &sel.candv));
     YG_CHECK(ws_get(ws, WS_TOPI, (size_t)nr * nq * sel.cap, &sel.candi));
     tm_scan.reset(new PassTimer(timed || scan_ticket >= 0, st, &job.ms_scan));
-    YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
+    if (up) {
+      YG_CHECK(scan_parts(job, *up, *bops, dsmall, tcq, nq, sel, pnch, ptpc, pfirst, ptm, st));
+      job.scan_launches += up->nparts;
+    } else {
+      YG_CHECK(scan(job, job.q, nq, job.b, job.ldb, nb, bn32, 1, &tcq, sel, st));
+      job.scan_launches++;
+    }
     tm_scan->stop(st);
-    job.scan_launches++;
+  }
+  if (up) {
+    // the error bounds over the whole base (the thresholds used part 0's)
+    YG_CHECK(compute_eps(nq, d, job.prec, job.metric, qn64, qres, qflag, &dsmall->bs, eps,
+                         qexact, st));
   }
   ra.sel = sel;
   PassTimer tr(timed || scan_ticket >= 0, st, &job.ms_rerank);
@@ -322,6 +433,13 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   if (tm_sample) {
     tm_sample->collect();
     tune_report(sample_ticket, tm_sample->last);
+  }
+  if (up) {
+    for (int i = 0; i < up->nparts; i++) {
+      if (!ptm[i]) continue;
+      ptm[i]->collect();
+      tune_report(pticket[i], ptm[i]->last);
+    }
   }
   job.n_cand = (long long)hs.n_cand;
   job.exact_class = hs.bs.all_exact;
@@ -524,7 +642,18 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   float *bn32, *bres = nullptr;
   YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32));
   BaseOps bops;
-  if (job.prec == PREC_BF16) {
+  if (job.prec == PREC_BF16 && job.upload) {
+    // the base arrives part by part: buffers for all of it, part 0 packed now
+    BaseUpload &up = *job.upload;
+    YG_CHECK(tc_alloc_base(nb, d, job.metric, ws, WS_BPACK, WS_BNORMP, WS_BRES, &bops.plain,
+                           &bops.res));
+    bops.bn32 = bn32;
+    YG_CUDA(cudaStreamWaitEvent(st, up.ready[0], 0));
+    YG_CHECK(tc_prepare_base_range(job.b, job.ldb, up.row0[0], (int)(up.row0[1] - up.row0[0]),
+                                   d, job.metric, bops.plain, bn32, bops.res, &dsmall->bs, st));
+    up.packed[0] = true;
+    bops.has_plain = true;
+  } else if (job.prec == PREC_BF16) {
     YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK, WS_BNORMP,
                              WS_BRES, &bops.plain, bn32, &dsmall->bs, 0, st));
     bops.has_plain = true;
@@ -579,8 +708,54 @@ int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
     YG_CHECK(ws_get(ws, WS_H_Q, (size_t)nq * d, &dq));
     YG_CHECK(ws_get(ws, WS_H_IDX, (size_t)nq * k, &didx));
     YG_CHECK(ws_get(ws, WS_H_DIS, (size_t)nq * k, &ddis));
-    YG_CUDA(cudaMemcpyAsync(db, b, sizeof(float) * nb * (size_t)d, cudaMemcpyHostToDevice, st));
-    YG_CUDA(cudaMemcpyAsync(dq, q, sizeof(float) * nq * (size_t)d, cudaMemcpyHostToDevice, st));
+    // A large base goes up in parts on a second stream while the passes over
+    // the parts already there run (host -> device copies are ~25x slower than
+    // the packing of what they carry).  The guard drains the copies and frees
+    // the events on every exit path.
+    const bool stream_up = w == nullptr && prec == PREC_BF16 && nb >= (1 << 18);
+    BaseUpload up;
+    struct UploadGuard {
+      BaseUpload *u;
+      cudaStream_t cs;
+      ~UploadGuard() {
+        if (cs) cudaStreamSynchronize(cs);
+        for (int i = 0; i < u->nparts; i++)
+          if (u->ready[i]) cudaEventDestroy(u->ready[i]);
+      }
+    } guard{&up, nullptr};
+    if (stream_up) {
+      if (!ctx->copy_stream)
+        YG_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+      cudaStream_t cs = ctx->copy_stream;
+      guard.cs = cs;
+      // the queries first: a copy issued after the base parts would wait for them
+      YG_CUDA(cudaMemcpyAsync(dq, q, sizeof(float) * nq * (size_t)d, cudaMemcpyHostToDevice, st));
+      cudaEvent_t qdone;
+      YG_CUDA(cudaEventCreateWithFlags(&qdone, cudaEventDisableTiming));
+      YG_CUDA(cudaEventRecord(qdone, st));
+      YG_CUDA(cudaStreamWaitEvent(cs, qdone, 0));
+      YG_CUDA(cudaEventDestroy(qdone));
+      // parts of 1/8, 1/4, 1/4, 1/4, 1/8 of the base (whole 256-row tiles): a
+      // small first part starts the passes early, a small last one leaves
+      // little to do after the final copy
+      const int parts = 5;
+      const double frac[parts + 1] = {0.0, 0.125, 0.375, 0.625, 0.875, 1.0};
+      up.nparts = parts;
+      for (int i = 0; i <= parts; i++)
+        up.row0[i] = std::min<long>((long)nb, (long)(frac[i] * nb / 256) * 256);
+      up.row0[parts] = nb;
+      for (int i = 0; i < parts; i++) {
+        YG_CUDA(cudaEventCreateWithFlags(&up.ready[i], cudaEventDisableTiming));
+        const long r0 = up.row0[i], n = up.row0[i + 1] - r0;
+        YG_CUDA(cudaMemcpyAsync(db + r0 * d, b + r0 * d, sizeof(float) * n * (size_t)d,
+                                cudaMemcpyHostToDevice, cs));
+        YG_CUDA(cudaEventRecord(up.ready[i], cs));
+      }
+      job.upload = &up;
+    } else {
+      YG_CUDA(cudaMemcpyAsync(db, b, sizeof(float) * nb * (size_t)d, cudaMemcpyHostToDevice, st));
+      YG_CUDA(cudaMemcpyAsync(dq, q, sizeof(float) * nq * (size_t)d, cudaMemcpyHostToDevice, st));
+    }
     if (w) {
       YG_CHECK(ws_get(ws, WS_H_W, (size_t)nb, &dw));
       YG_CUDA(cudaMemcpyAsync(dw, w, sizeof(float) * nb, cudaMemcpyHostToDevice, st));

@@ -6,6 +6,19 @@
 
 namespace yg {
 
+// A base that arrives part by part (host -> device upload overlapped with the
+// passes): part i is rows [row0[i], row0[i+1]); ready[i] is recorded on the
+// copy stream once it has landed.  The pipeline packs each part after waiting
+// for it, samples the thresholds from part 0 and runs the main pass part by
+// part; error bounds for the re-rank are taken over the whole base.
+struct BaseUpload {
+  static constexpr int kMaxParts = 8;
+  int nparts = 0;
+  long row0[kMaxParts + 1] = {};
+  cudaEvent_t ready[kMaxParts] = {};
+  bool packed[kMaxParts] = {};
+};
+
 struct KnnJob {
   int nq = 0, nb = 0, d = 0, k = 1;
   int metric = METRIC_L2;
@@ -21,6 +34,7 @@ struct KnnJob {
   // from band_kth[q], an upper bound of the query's k-th exact distance
   const float *band_kth = nullptr;
   int level = 0;  // nesting depth of the later-chance passes (workspace slots)
+  BaseUpload *upload = nullptr;  // base arriving part by part (BF16 pass only)
   // CUDA-event timing of the passes (optional)
   int timing = 0;
   float ms_scan = 0, ms_sample = 0, ms_rerank = 0;

@@ -39,6 +39,7 @@ struct ScanSel {
   int *candi = nullptr;
   int cap = 0;              // THRESH: slots per (region, query)
   int halves = 2;           // THRESH: regions per chunk (column halves of a row)
+  int id_off = 0;           // added to every emitted base id (a pass over a base slice)
   __host__ __device__ int nregion() const { return nchunk * halves; }
 };
 

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(NT, 1)
           if (v <= thr) {
             if (rcount < sel.cap) {
               sel.candv[rbase * sel.cap + rcount] = v;
-              sel.candi[rbase * sel.cap + rcount] = jbase + c;
+              sel.candi[rbase * sel.cap + rcount] = jbase + c + sel.id_off;
             }
             rcount++;
           }
@@ -115,11 +115,11 @@ __global__ void __launch_bounds__(NT, 1)
             (ia < C) && (ib >= C || va < vb || (va == vb && (unsigned)xa <= (unsigned)xb));
         if (takeA) {
           sel.topv[o + s] = va;
-          sel.topi[o + s] = xa;
+          sel.topi[o + s] = xa < 0 ? xa : xa + sel.id_off;
           ia++;
         } else {
           sel.topv[o + s] = vb;
-          sel.topi[o + s] = xb;
+          sel.topi[o + s] = xb < 0 ? xb : xb + sel.id_off;
           ib++;
         }
       }

@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
         if (x <= thr) {
           if (rcount < sel.cap) {
             sel.candv[rbase * sel.cap + rcount] = x;
-            sel.candi[rbase * sel.cap + rcount] = j;
+            sel.candi[rbase * sel.cap + rcount] = j + sel.id_off;
           }
           rcount++;
         }
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           const float vo = takeA ? va : vb;
           const int xo = takeA ? xa : xb;
           sel.topv[o + s] = vo;
-          sel.topi[o + s] = (xo == 0x7fffffff) ? -1 : xo;
+          sel.topi[o + s] = (xo == 0x7fffffff) ? -1 : xo + sel.id_off;
           if (takeA) ia++; else ib++;
         }
       }

@@ -61,6 +61,44 @@ int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspa
   return OK;
 }
 
+int tc_prepare_base_range(const float *b, long ldb, long row0, int n, int d, int metric,
+                          const TcOperands &op, float *bn32, float *res, SetStats *bs,
+                          cudaStream_t st) {
+  if (n <= 0) return OK;
+  const int nmode = metric == METRIC_L2 ? 1 : 0;
+  __nv_bfloat16 *pack = const_cast<__nv_bfloat16 *>(op.b) + row0 * op.Kp;
+  __nv_bfloat16 *norm = op.bn ? const_cast<__nv_bfloat16 *>(op.bn) + row0 * 16 : nullptr;
+  return prep_rows(b + row0 * ldb, ldb, n, d, 1.f, nullptr, bn32 + row0, nullptr, res + row0,
+                   pack, op.Kp, norm, nmode, bs, st);
+}
+
+int tc_alloc_base(int nb, int d, int metric, Workspace &ws, int slot_pack, int slot_norm,
+                  int slot_res, TcOperands *op, float **res) {
+  const int Kp = ((d + 63) / 64) * 64;
+  void *pack, *norm = nullptr, *r;
+  YG_CHECK(ws.get(slot_pack, (size_t)nb * Kp * 2, &pack));
+  if (metric == METRIC_L2) YG_CHECK(ws.get(slot_norm, (size_t)nb * 32, &norm));
+  YG_CHECK(ws.get(slot_res, (size_t)nb * 4, &r));
+  op->d = d;
+  op->Kp = Kp;
+  op->metric = metric;
+  op->split = 0;
+  op->b = (const __nv_bfloat16 *)pack;
+  op->bn = (const __nv_bfloat16 *)norm;
+  op->b_rows = nb;
+  op->b_step = 1;
+  *res = (float *)r;
+  return OK;
+}
+
+int tc_base_slice(const TcOperands &full, long row0, int nrows, TcOperands *out) {
+  *out = full;
+  out->b = full.b + row0 * full.b_step * full.Kp;
+  if (full.bn) out->bn = full.bn + row0 * full.b_step * 16;
+  out->b_rows = nrows;
+  return OK;
+}
+
 int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out) {
   *out = full;
   out->b_step = full.b_step * stride;

@@ -47,6 +47,17 @@ int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspa
 // strided view of the packed base (every stride-th row, nrows rows)
 int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out);
 
+// Base rows [row0, row0 + n) uploaded part by part: the bf16 buffers of the
+// whole base are allocated first (tc_alloc_base, plain packing), each part is
+// packed when it has arrived (tc_prepare_base_range, its statistics folded
+// into bs), and a pass over one part reads a slice (tc_base_slice).
+int tc_alloc_base(int nb, int d, int metric, Workspace &ws, int slot_pack, int slot_norm,
+                  int slot_res, TcOperands *op, float **res);
+int tc_prepare_base_range(const float *b, long ldb, long row0, int n, int d, int metric,
+                          const TcOperands &op, float *bn32, float *res, SetStats *bs,
+                          cudaStream_t st);
+int tc_base_slice(const TcOperands &full, long row0, int nrows, TcOperands *out);
+
 int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st);
 
 }  // namespace yg
