@@ -121,7 +121,16 @@ int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream
     return e && e[0] == '1';
   }();
   const bool pair = pair_env && nq > TC_TILE_M;
-  if (op.Kp > 256)  // query tile too large to stay resident: streamed per K block
+  // the query tile stays resident in shared memory when a ring of at least
+  // three stages still fits beside it (always for K <= 256; for the 3xBF16
+  // split of d <= 128, K = 384, with short lists); else it is streamed with
+  // every K block
+  bool resident = op.Kp <= 256;
+  if (!resident && op.Kp <= 384) {
+    const int C = sel.mode == SCAN_THRESH ? 1 : sel.C;
+    resident = tck::make_layout(op.Kp / 64, 3, sel.mode, C, false, false).total <= 227 * 1024;
+  }
+  if (!resident)  // query tile too large to stay resident: streamed per K block
     return pair ? tc_dispatch_s2(op, nq, nb, sel, st) : tc_dispatch_s1(op, nq, nb, sel, st);
   return pair ? tc_dispatch_r2(op, nq, nb, sel, st) : tc_dispatch_r1(op, nq, nb, sel, st);
 }
