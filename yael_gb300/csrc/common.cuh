@@ -98,6 +98,10 @@ int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), def
 // and reported on stderr, one line per pass
 bool trace_enabled();
 
+// Raises kernel func's dynamic shared-memory limit to at least bytes on the
+// current device, once per (kernel, device, size); thread safe.
+int ensure_smem(const void *func, size_t bytes);
+
 // ---------------------------------------------------------------------------
 // device helpers
 __host__ __device__ inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }

@@ -110,12 +110,7 @@ int cross_host(int metric, int d, int na, int nb, const float *a, int lda, const
     YG_CUDA(cudaMemsetAsync(bn, 0, sizeof(double) * nb, st));
   }
   const size_t smem = sizeof(float) * (kOperandFloats + BM * ST_LD);
-  static bool attr = false;
-  if (!attr) {
-    YG_CUDA(cudaFuncSetAttribute(cross_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  YG_CHECK(ensure_smem((const void *)cross_kernel, smem));
   long jb = (long)(((size_t)1 << 30) / ((size_t)na * 4));
   jb = (jb / BN) * BN;
   if (jb < BN) jb = BN;
@@ -231,9 +226,7 @@ static int reorder_host(int n, int nb, int d, int k, const float *b, const float
     set_error(E_UNSUPPORTED, "knn_reorder_shortlist: k=%d too large", k);
     return E_UNSUPPORTED;
   }
-  if (smem > 48 * 1024)
-    YG_CUDA(cudaFuncSetAttribute(reorder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
+  YG_CHECK(ensure_smem((const void *)reorder_kernel, smem));
   reorder_kernel<<<n, 128, smem, st>>>(n, nb, d, k, db, dv, didx, ddis);
   YG_LAUNCH_CHECK();
   YG_CUDA(cudaMemcpyAsync(idx, didx, sizeof(int) * (size_t)n * k, cudaMemcpyDeviceToHost, st));

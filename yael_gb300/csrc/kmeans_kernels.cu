@@ -361,12 +361,7 @@ template <int K, bool VEC>
 int launch_assign(const KmWork *work, int nwork, const float *v, int d, const float *C, int k,
                   const unsigned char *active, int *assign, float *dis, cudaStream_t st) {
   const size_t smem = (size_t)((((long)k * d + 3) & ~3L) + k) * sizeof(float);
-  static size_t attr = 48 * 1024;
-  if (smem > attr) {
-    YG_CUDA(cudaFuncSetAttribute(assign_small_kernel<K, VEC>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = smem;
-  }
+  YG_CHECK(ensure_smem((const void *)assign_small_kernel<K, VEC>, smem));
   assign_small_kernel<K, VEC><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign, dis);
   YG_LAUNCH_CHECK();
   return OK;

@@ -4,7 +4,9 @@
 #include <string.h>
 
 #include <atomic>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "common.cuh"
 #include "../../include/yael_gpu.h"
@@ -115,6 +117,19 @@ int default_precision() {
   if (!strcmp(s, "bf16") || !strcmp(s, "BF16") || !strcmp(s, "1")) return PREC_BF16;
   if (!strcmp(s, "bf16x3") || !strcmp(s, "BF16X3") || !strcmp(s, "2")) return PREC_BF16X3;
   return PREC_FP32;
+}
+
+int ensure_smem(const void *func, size_t bytes) {
+  static std::mutex m;
+  static std::map<std::pair<const void *, int>, size_t> done;
+  int dev = 0;
+  YG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(m);
+  size_t &cur = done[std::make_pair(func, dev)];
+  if (bytes <= cur || bytes <= 48 * 1024) return OK;
+  YG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+  return OK;
 }
 
 bool trace_enabled() {

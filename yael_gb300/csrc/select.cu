@@ -698,12 +698,7 @@ int rerank(const RerankArgs &a, cudaStream_t st) {
   while (Mp < Mmax) Mp <<= 1;
   // K (8 B) + I (4 B) + E (4 B) per slot, then the query row
   const size_t smem = (size_t)Mp * 16 + (size_t)a.d * 4 + 16;
-  static size_t attr = 48 * 1024;
-  if (smem > attr) {
-    YG_CUDA(cudaFuncSetAttribute(rerank_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = smem;
-  }
+  YG_CHECK(ensure_smem((const void *)rerank_kernel, smem));
   rerank_kernel<<<a.nq, RT, smem, st>>>(a, Mp);
   YG_LAUNCH_CHECK();
   return OK;
@@ -768,12 +763,7 @@ int exhaustive(int nlist, const int *qlist_dev, int nb, int d, int k, int metric
   int kp = 1;
   while (kp < k) kp <<= 1;
   const size_t smem_sel = (size_t)kp * 12 + 16;
-  static size_t attr = 48 * 1024;
-  if (smem_sel > attr) {
-    YG_CUDA(cudaFuncSetAttribute(fb_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_sel));
-    attr = smem_sel;
-  }
+  YG_CHECK(ensure_smem((const void *)fb_select_kernel, smem_sel));
   unsigned long long *rows = reinterpret_cast<unsigned long long *>(scratch);
   for (int q0 = 0; q0 < nlist; q0 += batch) {
     const int nbt = imin(batch, nlist - q0);

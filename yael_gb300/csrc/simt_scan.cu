@@ -133,12 +133,7 @@ int launch(const float *q, long ldq, int nq, const float *b, long ldb, int nb, i
            cudaStream_t st) {
   const size_t smem = sizeof(float) * (kOperandFloats + BM * ST_LD) +
                       (MODE == SCAN_TOPC ? (size_t)C * NT * 8 : 0);
-  static bool attr_done = false;  // per instantiation
-  if (!attr_done) {
-    YG_CUDA(cudaFuncSetAttribute(simt_scan_kernel<MODE, C>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_done = true;
-  }
+  YG_CHECK(ensure_smem((const void *)simt_scan_kernel<MODE, C>, smem));
   dim3 grid((unsigned)ceil_div(nq, BM), (unsigned)sel.nchunk);
   simt_scan_kernel<MODE, C><<<grid, NT, smem, st>>>(q, ldq, nq, b, ldb, nb, d, bn,
                                                      bn_stride, metric, sel);

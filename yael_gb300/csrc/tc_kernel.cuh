@@ -563,12 +563,7 @@ int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_
               op.Kp, C);
     return E_UNSUPPORTED;
   }
-  static bool attr = false;
-  if (!attr) {
-    YG_CUDA(cudaFuncSetAttribute(tc_scan_kernel<MODE, C, L2, QS, PAIR>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr = true;
-  }
+  YG_CHECK(ensure_smem((const void *)tc_scan_kernel<MODE, C, L2, QS, PAIR>, lay.total));
   CUtensorMap mq, mqn, mb, mbn;
   YG_CHECK(make_map(&mq, op.q, op.Kp, nq, (uint64_t)op.Kp * 2, 64, 128,
                     CU_TENSOR_MAP_SWIZZLE_128B));
