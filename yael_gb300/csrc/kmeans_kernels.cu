@@ -157,6 +157,197 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The grouped assignment as a register-blocked GEMM (d % 4 == 0, aligned
+// rows): a block takes 128 points of one instance at a time; thread (pg, cg)
+// accumulates x.c for points 4 pg .. 4 pg + 3 and centroids cg TN .. cg TN +
+// TN - 1 (TN = K / 8) from 32-coordinate slices of the points staged
+// transposed in shared memory and the transposed centroids, i.e. 4 TN FMAs per
+// 1 + TN / 4 shared loads.  Each point's K values live in its 8 consecutive
+// lanes, which reduce the best value, the certified band (values within
+// 2 eps of the best, eps as assign_small_kernel), its direct-difference
+// re-check (sequential over coordinates, the same order as there, so the same
+// reported distance) and the FP64 decision of near ties, lowest index first.
+// FULL: whole rows are staged (d <= kFullD), so the band re-check reads shared
+// memory; else 32-coordinate slices and the re-check reads the rows again.
+constexpr int kFullD = 136;
+template <int K, bool FULL>
+__global__ void __launch_bounds__(256)
+    assign_gemm_kernel(const KmWork *__restrict__ work, const float *__restrict__ v, int d,
+                       const float *__restrict__ C, int k, const unsigned char *active,
+                       int *assign, float *dis) {
+  constexpr int TP = 128, TM = 4, TN = K / 8, XS = TP + 4;
+  const int DC = FULL ? d : 32;
+  extern __shared__ __align__(16) float sm[];
+  float *cst = sm;            // [d][K] transposed centroids (zero past k)
+  float *cn = cst + d * K;    // [K] norms
+  float *xs = cn + K;         // [DC][XS] transposed points (all of d when FULL)
+  __shared__ float s_cmax;
+  const KmWork w = work[blockIdx.x];
+  if (!active[w.inst]) return;
+  const int tid = threadIdx.x, pg = tid >> 3, cg = tid & 7;
+  const float *Ci = C + (long)w.inst * k * d;
+  for (int i = tid; i < d * K; i += blockDim.x) {
+    const int c = i / K, j = i - c * K;
+    cst[i] = j < k ? Ci[(long)j * d + c] : 0.f;
+  }
+  __syncthreads();
+  for (int j = tid; j < K; j += blockDim.x) {
+    float sn = 0.f;
+    for (int c = 0; c < d; c++) sn = fmaf(cst[c * K + j], cst[c * K + j], sn);
+    cn[j] = sn;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float m = 0.f;
+    for (int j = 0; j < k; j++) m = fmaxf(m, cn[j]);
+    s_cmax = m;
+  }
+  __syncthreads();
+  const float cmax = s_cmax;
+  const float rho = (float)(d + 4) * kU;
+  for (int t0 = 0; t0 < w.n; t0 += TP) {
+    const int np = min(TP, w.n - t0);
+    const float *vt = v + (w.p0 + t0) * (long)d;
+    float acc[TM][TN], xn[TM];
+#pragma unroll
+    for (int i = 0; i < TM; i++) {
+      xn[i] = 0.f;
+#pragma unroll
+      for (int t = 0; t < TN; t++) acc[i][t] = 0.f;
+    }
+    for (int c0 = 0; c0 < d; c0 += DC) {
+      const int n4 = min(DC, d - c0) >> 2, n4p = (n4 + 1) >> 1;
+      __syncthreads();  // the previous slice has been read
+      // a warp covers 16 consecutive points x one pair of float4 columns: each
+      // pair of lanes reads one 32-byte sector and the transposed stores of a
+      // warp hit 32 distinct banks (row pitch XS = 4 mod 32)
+      for (int idx = tid; idx < TP * 2 * n4p; idx += blockDim.x) {
+        const int ln = idx & 31, grp = idx >> 5;
+        const int p = (grp % (TP / 16)) * 16 + (ln >> 1);
+        const int c4 = 2 * (grp / (TP / 16)) + (ln & 1);
+        if (c4 >= n4) continue;
+        float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p < np) val = __ldg(reinterpret_cast<const float4 *>(vt + (long)p * d + c0) + c4);
+        xs[(4 * c4 + 0) * XS + p] = val.x;
+        xs[(4 * c4 + 1) * XS + p] = val.y;
+        xs[(4 * c4 + 2) * XS + p] = val.z;
+        xs[(4 * c4 + 3) * XS + p] = val.w;
+      }
+      __syncthreads();
+      for (int c = 0; c < 4 * n4; c++) {
+        const float4 xv = *reinterpret_cast<const float4 *>(xs + c * XS + pg * TM);
+        const float xa[TM] = {xv.x, xv.y, xv.z, xv.w};
+        float cv[TN];
+        const float *cr = cst + (c0 + c) * K + cg * TN;
+#pragma unroll
+        for (int t = 0; t < TN; t += 2) {
+          const float2 c2 = *reinterpret_cast<const float2 *>(cr + t);
+          cv[t] = c2.x;
+          cv[t + 1] = c2.y;
+        }
+#pragma unroll
+        for (int i = 0; i < TM; i++) {
+          xn[i] = fmaf(xa[i], xa[i], xn[i]);
+#pragma unroll
+          for (int t = 0; t < TN; t++) acc[i][t] = fmaf(xa[i], cv[t], acc[i][t]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < TM; i++) {
+      const int p = pg * TM + i;
+      // best approximate value, lowest index on equal values, over the 8 lanes
+      float a[TN];
+      float bv = 1e30f;
+      int bj = 0x7fffffff;
+#pragma unroll
+      for (int t = 0; t < TN; t++) {
+        const int j = cg * TN + t;
+        a[t] = (xn[i] + cn[j]) - 2.f * acc[i][t];
+        if (j < k && a[t] < bv) { bv = a[t]; bj = j; }
+      }
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (ov < bv || (ov == bv && oj < bj)) { bv = ov; bj = oj; }
+      }
+      const float b1 = bv;
+      const float *x = vt + (long)p * d;
+      const bool pv = p < np;
+      // band members of this lane: direct differences, strict '<' over j
+      const float tol = 4.f * (float)(d + 8) * kU * (xn[i] + cmax);
+      unsigned band = 0;
+      float e1 = INFINITY, e2 = INFINITY;
+      int j1 = 0x7fffffff;
+      if (pv && b1 < 1e30f) {
+#pragma unroll
+        for (int t = 0; t < TN; t++) {
+          const int j = cg * TN + t;
+          if (j < k && !(a[t] > b1 + tol)) band |= 1u << t;
+        }
+        for (unsigned bm = band; bm; bm &= bm - 1) {
+          const int j = cg * TN + __ffs(bm) - 1;
+          float sd = 0.f;
+          for (int c = 0; c < d; c++) {
+            const float tt = (FULL ? xs[c * XS + p] : __ldg(x + c)) - cst[c * K + j];
+            sd = fmaf(tt, tt, sd);
+          }
+          if (sd < e1) { e2 = e1; e1 = sd; j1 = j; } else if (sd < e2) { e2 = sd; }
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        const float oe1 = __shfl_xor_sync(0xffffffffu, e1, o);
+        const float oe2 = __shfl_xor_sync(0xffffffffu, e2, o);
+        const int oj1 = __shfl_xor_sync(0xffffffffu, j1, o);
+        if (oe1 < e1 || (oe1 == e1 && oj1 < j1)) {
+          e2 = fminf(oe2, e1);
+          e1 = oe1;
+          j1 = oj1;
+        } else {
+          e2 = fminf(e2, oe1);
+        }
+      }
+      int out_j = -1;
+      float out_d = 1e30f;
+      if (pv && b1 < 1e30f) {
+        if (e2 < INFINITY && e2 - e1 <= rho * (e1 + e2)) {
+          // near tie: FP64 over the band, sequential over coordinates
+          double best = INFINITY;
+          int bi = 0x7fffffff;
+          for (unsigned bm = band; bm; bm &= bm - 1) {
+            const int j = cg * TN + __ffs(bm) - 1;
+            double sd = 0;
+            for (int c = 0; c < d; c++) {
+              const double tt = (double)(FULL ? xs[c * XS + p] : x[c]) - (double)cst[c * K + j];
+              sd += tt * tt;
+            }
+            if (sd < best) { best = sd; bi = j; }
+          }
+          // only this point's 8 lanes take this branch (together: their
+          // conditions come from values they reduced jointly)
+          const unsigned gmask = 0xffu << ((threadIdx.x & 31) & ~7);
+#pragma unroll
+          for (int o = 1; o < 8; o <<= 1) {
+            const double ob = __shfl_xor_sync(gmask, best, o);
+            const int oi = __shfl_xor_sync(gmask, bi, o);
+            if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+          }
+          if (bi != 0x7fffffff) { out_j = bi; out_d = (float)best; }
+        } else if (j1 != 0x7fffffff) {
+          out_j = j1;
+          out_d = e1;
+        }
+      }
+      if (pv && cg == 0) {
+        assign[w.p0 + t0 + p] = out_j;
+        dis[w.p0 + t0 + p] = out_d;
+      }
+    }
+  }
+}
+
 __global__ void hist_kernel(const int *assign, const int *pinst, long n, int k,
                             const unsigned char *active, int *counts) {
   const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -374,6 +565,21 @@ int launch_assign_any(const KmWork *work, int nwork, const float *v, int d, cons
   // float4 rows need d % 4 == 0 and 16-byte aligned points and centroids
   const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(v) & 15) == 0) &&
                    ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+  if (vec && (size_t)d * K * 4 <= 120 * 1024) {
+    if (d <= kFullD) {
+      const size_t smem = ((size_t)d * K + K + (size_t)d * 132) * sizeof(float);
+      YG_CHECK(ensure_smem((const void *)assign_gemm_kernel<K, true>, smem));
+      assign_gemm_kernel<K, true><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign,
+                                                            dis);
+    } else {
+      const size_t smem = ((size_t)d * K + K + 32 * 132) * sizeof(float);
+      YG_CHECK(ensure_smem((const void *)assign_gemm_kernel<K, false>, smem));
+      assign_gemm_kernel<K, false><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign,
+                                                             dis);
+    }
+    YG_LAUNCH_CHECK();
+    return OK;
+  }
   if (vec) return launch_assign<K, true>(work, nwork, v, d, C, k, active, assign, dis, st);
   return launch_assign<K, false>(work, nwork, v, d, C, k, active, assign, dis, st);
 }
