@@ -315,18 +315,20 @@ failed:
   }
 }
 
-// ---- warp-per-query variant for short TOPC lists (nchunk * C <= 32) -------
+// ---- group-per-query variant for short TOPC lists (nchunk * C <= 32) ------
+// G lanes (8, 16 or 32) hold one query's candidates, one per lane.
 
-__device__ __forceinline__ void warp_sort(unsigned long long &key, int &id) {
-  const int lane = threadIdx.x & 31;
+template <int G>
+__device__ __forceinline__ void group_sort(unsigned long long &key, int &id, unsigned gm) {
+  const int gl = threadIdx.x & (G - 1);
 #pragma unroll
-  for (int size = 2; size <= 32; size <<= 1) {
+  for (int size = 2; size <= G; size <<= 1) {
 #pragma unroll
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      const unsigned long long pk = __shfl_xor_sync(0xffffffffu, key, stride);
-      const int pi = __shfl_xor_sync(0xffffffffu, id, stride);
-      const bool up = (lane & size) == 0 || size == 32;
-      const bool lower = (lane & stride) == 0;
+      const unsigned long long pk = __shfl_xor_sync(gm, key, stride);
+      const int pi = __shfl_xor_sync(gm, id, stride);
+      const bool up = (gl & size) == 0 || size == G;
+      const bool lower = (gl & stride) == 0;
       const bool pless = lex_less(pk, pi, key, id);
       const bool take = (lower == up) ? pless : (!pless && (pk != key || pi != id));
       if (take) { key = pk; id = pi; }
@@ -334,15 +336,43 @@ __device__ __forceinline__ void warp_sort(unsigned long long &key, int &id) {
   }
 }
 
+// FP32 distance of one base row, the group's lanes over strided coordinates
+template <int G>
+__device__ __forceinline__ float group_dist32(const float *qv, const float *brow, int d,
+                                              int metric, unsigned gm) {
+  const int gl = threadIdx.x & (G - 1);
+  float acc = 0.f;
+  for (int c = gl; c < d; c += G) {
+    const float bv = __ldg(brow + c);
+    if (metric == METRIC_L2) {
+      const float t = qv[c] - bv;
+      acc = fmaf(t, t, acc);
+    } else {
+      acc = fmaf(qv[c], bv, acc);
+    }
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gm, acc, o);
+  return acc;
+}
+
 __device__ __forceinline__ double ord2d(unsigned long long k) {
   const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
   return __longlong_as_double((long long)u);
 }
 
+template <int G>
 __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (q >= a.nq) return;  // uniform per warp
+  constexpr int QPB = 256 / G;  // queries per block
+  const int gl = threadIdx.x & (G - 1);
+  const int gbase = (threadIdx.x & 31) & ~(G - 1);  // first lane of the group in its warp
+  const unsigned gm = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+  const int q = blockIdx.x * QPB + (int)(threadIdx.x / G);
+  if (q >= a.nq) return;  // uniform per group
+  auto gballot = [&](bool p) -> unsigned {
+    const unsigned b = __ballot_sync(gm, p);
+    return G == 32 ? b : (b >> gbase) & ((1u << G) - 1u);
+  };
   const ScanSel &s = a.sel;
   const int M = s.nchunk * s.C, k = a.k, d = a.d;
   const bool L2 = a.metric == METRIC_L2;
@@ -353,8 +383,8 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
 
   unsigned long long key = ~0ull, tkey = ~0ull;
   int id = 0x7fffffff;
-  if (lane < M) {
-    const int ch = lane / s.C, sl = lane - ch * s.C;
+  if (gl < M) {
+    const int ch = gl / s.C, sl = gl - ch * s.C;
     const long o = ((long)ch * a.nq + q) * s.C + sl;
     const int j = s.topi[o];
     if (j >= 0) {
@@ -367,70 +397,74 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
   }
   // boundary: smallest (value, id) that closes a full chunk list
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(0xffffffffu, tkey, o);
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(gm, tkey, o);
     tkey = t < tkey ? t : tkey;
   }
-  const int nvalid = __popc(__ballot_sync(0xffffffffu, id != 0x7fffffff));
+  const int nvalid = __popc(gballot(id != 0x7fffffff));
   bool ok = nvalid >= k;
   float kth_hi = INFINITY;  // upper bound of the k-th exact distance, when found
   if (ok) {
-    if (a.n_cand && lane == 0) atomicAdd(a.n_cand, (unsigned long long)nvalid);
-    warp_sort(key, id);
+    if (a.n_cand) {  // one atomic per set of converged lanes, not per query
+      const unsigned am = __activemask();
+      const unsigned tot = __reduce_add_sync(am, gl == 0 ? (unsigned)nvalid : 0u);
+      if ((int)(threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(a.n_cand, (unsigned long long)tot);
+    }
+    group_sort<G>(key, id, gm);
     if (ex) {
       if (tkey != ~0ull) {
-        const unsigned long long kk = __shfl_sync(0xffffffffu, key, k - 1);
-        const int ik = __shfl_sync(0xffffffffu, id, k - 1);
+        const unsigned long long kk = __shfl_sync(gm, key, k - 1, G);
+        const int ik = __shfl_sync(gm, id, k - 1, G);
         const unsigned long long tk = tkey >> 32;
         const unsigned tid_b = (unsigned)(tkey & 0xffffffffu);
         ok = kk < tk || (kk == tk && (unsigned)ik <= tid_b);
         kth_hi = ord2f((unsigned)kk);  // exact values
       }
-      if (ok && lane < k) {
-        a.out_idx[(long)q * k + lane] = id;
-        a.out_dis[(long)q * k + lane] = ord2f((unsigned)key);
+      if (ok && gl < k) {
+        a.out_idx[(long)q * k + gl] = id;
+        a.out_dis[(long)q * k + gl] = ord2f((unsigned)key);
       }
     } else {
-      const float ak = ord2f((unsigned)__shfl_sync(0xffffffffu, key, k - 1));
+      const float ak = ord2f((unsigned)__shfl_sync(gm, key, k - 1, G));
       const double lim = (double)ak + 2.0 * (double)eps + 4e-7 * fabs((double)ak) + 1e-30;
       const bool inband = id != 0x7fffffff && (double)ord2f((unsigned)key) <= lim;
-      const int nband = __popc(__ballot_sync(0xffffffffu, inband));
-      // FP32 re-rank of the band, one candidate at a time across the warp
+      const int nband = __popc(gballot(inband));
+      // FP32 re-rank of the band, one candidate at a time across the group
       float e = INFINITY;
       for (int c = 0; c < nband; c++) {
-        const int cid = __shfl_sync(0xffffffffu, id, c);
-        const float ec = warp_dist32(qv, a.b + (long)cid * a.ldb, d, a.metric);
-        if (lane == c) e = ec;
+        const int cid = __shfl_sync(gm, id, c, G);
+        const float ec = group_dist32<G>(qv, a.b + (long)cid * a.ldb, d, a.metric, gm);
+        if (gl == c) e = ec;
       }
-      key = lane < nband ? (unsigned long long)f2ord(e) : ~0ull;
-      if (lane >= nband) id = 0x7fffffff;
-      warp_sort(key, id);
+      key = gl < nband ? (unsigned long long)f2ord(e) : ~0ull;
+      if (gl >= nband) id = 0x7fffffff;
+      group_sort<G>(key, id, gm);
       const float rho = (float)(d + 4) * kU;
       float eta = 0.f;
       if (!L2) eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64[q], 0.0)) *
                      __uint_as_float(a.bstats->max_norm_bits);
       const float e0 = ord2f((unsigned)key);
-      const float e1 = ord2f((unsigned)__shfl_down_sync(0xffffffffu, key, 1));
-      const bool tie = lane < imin(k, nband - 1) && (e1 - e0 <= rho * (fabsf(e0) + fabsf(e1)) + 2.f * eta);
+      const float e1 = ord2f((unsigned)__shfl_down_sync(gm, key, 1, G));
+      const bool tie = gl < imin(k, nband - 1) && (e1 - e0 <= rho * (fabsf(e0) + fabsf(e1)) + 2.f * eta);
       double ek_hi;
-      if (__any_sync(0xffffffffu, tie)) {
+      if (__any_sync(gm, tie)) {
         // FP64, sequential over coordinates, for the whole band
         unsigned long long k64 = ~0ull;
-        if (lane < nband) k64 = d2ord(dist64_seq(qv, a.b + (long)id * a.ldb, d, a.metric));
+        if (gl < nband) k64 = d2ord(dist64_seq(qv, a.b + (long)id * a.ldb, d, a.metric));
         key = k64;
-        warp_sort(key, id);
-        const double ek = ord2d(__shfl_sync(0xffffffffu, key, k - 1));
+        group_sort<G>(key, id, gm);
+        const double ek = ord2d(__shfl_sync(gm, key, k - 1, G));
         ek_hi = ek + 1e-12 * fabs(ek);
-        if (lane < k) {
-          a.out_idx[(long)q * k + lane] = id;
-          a.out_dis[(long)q * k + lane] = (float)ord2d(key);
+        if (gl < k) {
+          a.out_idx[(long)q * k + gl] = id;
+          a.out_dis[(long)q * k + gl] = (float)ord2d(key);
         }
       } else {
-        const float ek = ord2f((unsigned)__shfl_sync(0xffffffffu, key, k - 1));
+        const float ek = ord2f((unsigned)__shfl_sync(gm, key, k - 1, G));
         ek_hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
-        if (lane < k) {
-          a.out_idx[(long)q * k + lane] = id;
-          a.out_dis[(long)q * k + lane] = ord2f((unsigned)key);
+        if (gl < k) {
+          a.out_idx[(long)q * k + gl] = id;
+          a.out_dis[(long)q * k + gl] = ord2f((unsigned)key);
         }
       }
       const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
@@ -438,7 +472,7 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
       kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
     }
   }
-  if (!ok && lane == 0) {
+  if (!ok && gl == 0) {
     const int pos = atomicAdd(a.fail_cnt, 1);
     a.fail_list[pos] = q;
     if (a.kth_out) a.kth_out[q] = kth_hi;
@@ -685,7 +719,13 @@ __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0,
 int rerank(const RerankArgs &a, cudaStream_t st) {
   if (a.nq <= 0) return OK;
   if (a.sel.mode == SCAN_TOPC && a.sel.nchunk * a.sel.C <= 32) {
-    rerank_small_kernel<<<(unsigned)ceil_div(a.nq, 8), 256, 0, st>>>(a);
+    const int M = a.sel.nchunk * a.sel.C;
+    if (M <= 8)
+      rerank_small_kernel<8><<<(unsigned)ceil_div(a.nq, 32), 256, 0, st>>>(a);
+    else if (M <= 16)
+      rerank_small_kernel<16><<<(unsigned)ceil_div(a.nq, 16), 256, 0, st>>>(a);
+    else
+      rerank_small_kernel<32><<<(unsigned)ceil_div(a.nq, 8), 256, 0, st>>>(a);
     YG_LAUNCH_CHECK();
     return OK;
   }

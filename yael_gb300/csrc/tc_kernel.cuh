@@ -32,6 +32,7 @@
 // role leaves its loop and TMEM is freed.
 #pragma once
 #include <cudaTypedefs.h>
+#include <limits.h>
 #include <math.h>
 
 #include "tc_ptx.cuh"
@@ -126,11 +127,21 @@ __global__ void __launch_bounds__(NT_TC, 1)
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_holder + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long q0 = (long)blockIdx.x * TC_TILE_M;
   const int ntb = (int)ceil_div(nb, TC_TILE_N);
-  const int t_begin = blockIdx.y * sel.tiles_per_chunk;
-  const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
   const int nks = nkb;  // stages per base tile (the norm block rides with the last)
+  // Work units are (query tile, chunk of base tiles).  With streamed queries a
+  // CTA keeps no per-unit state in shared memory, so single CTAs run a 1D
+  // persistent grid that walks the units with stride gridDim.x (ring position,
+  // accumulator buffer and barrier phases carry over from unit to unit); else
+  // one unit per CTA from the 2D grid (query tile, chunk).
+  constexpr bool PERSIST = QS && !PAIR;
+  const int nqt = (int)ceil_div(nq, TC_TILE_M);
+  const int nunits = PERSIST ? nqt * sel.nchunk : 1;
+  const int w0 = PERSIST ? (int)blockIdx.x : 0, wstep = PERSIST ? (int)gridDim.x : 1;
+  auto unit_q0 = [&](int w) -> long {
+    return PERSIST ? (long)(w % nqt) * TC_TILE_M : (long)blockIdx.x * TC_TILE_M;
+  };
+  auto unit_chunk = [&](int w) -> int { return PERSIST ? w / nqt : (int)blockIdx.y; };
   const uint32_t crank = PAIR ? cluster_ctarank() : 0;
   const bool leader = crank == 0;
 
@@ -172,6 +183,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
     // its part of each base block)
     if (lane == 0) {
       if (!QS) {
+        const long q0 = unit_q0(0);
         const uint32_t qbytes = (uint32_t)(nkb * QBLK_BYTES + (L2 ? 128 * 32 : 0));
         if (PAIR) {
           if (leader) mbar_arrive_expect_tx(qfull, 2 * qbytes);
@@ -189,6 +201,10 @@ __global__ void __launch_bounds__(NT_TC, 1)
       int sn = 0;
       uint32_t phn = 0;
       bool ok = true;
+      for (int w = w0; w < nunits && ok; w += wstep) {
+      const long q0 = unit_q0(w);
+      const int t_begin = unit_chunk(w) * sel.tiles_per_chunk;
+      const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
       for (int t = t_begin; t < t_end && ok; t++) {
         const int brow = t * TC_TILE_N + (int)crank * (TC_TILE_N / 2) * (PAIR ? 1 : 0);
         for (int ks = 0; ks < nks; ks++) {
@@ -223,6 +239,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           }
         }
       }
+      }
       if (PAIR) {
         // every stage released by the leader's MMAs: no commit is still on its
         // way to this CTA when the pair exits
@@ -243,6 +260,9 @@ __global__ void __launch_bounds__(NT_TC, 1)
       int sn = 0;
       uint32_t phn = 0;
       int it = 0;
+      for (int w = w0; w < nunits && ok; w += wstep) {
+      const int t_begin = unit_chunk(w) * sel.tiles_per_chunk;
+      const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
       for (int t = t_begin; t < t_end && ok; t++, it++) {
         const int a = it & 1;
         const uint32_t u = (uint32_t)(it >> 1);
@@ -292,6 +312,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
         else
           umma_commit(&tfull[a]);
       }
+      }
       if (PAIR) {
         // the last two accumulators released by the selection warps of both
         // CTAs: no remote arrival is still on its way when the pair exits
@@ -308,9 +329,16 @@ __global__ void __launch_bounds__(NT_TC, 1)
     const int grp = warp & 3;              // TMEM lane group this warp may access
     const int half = ew >> 2;              // column half
     const int row = grp * 32 + lane;
-    const long qrow = q0 + row;
-    const bool rvalid = qrow < nq;
     const int tslot = ew * 32 + lane;      // 0..255
+    const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
+    int it = 0;
+    bool ok = true;
+    for (int w = w0; w < nunits && ok; w += wstep) {
+    const long qrow = unit_q0(w) + row;
+    const int chunk = unit_chunk(w);
+    const int t_begin = chunk * sel.tiles_per_chunk;
+    const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
+    const bool rvalid = qrow < nq;
     float lmax = INFINITY, thr = NAN;
     constexpr int CR = (C <= 16) ? C : 1;  // register lists up to 16 entries
     float RL[CR];
@@ -323,8 +351,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
     }
     if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
     int rcount = 0;  // THRESH: hits of this thread's region (chunk, half, query)
-    const long rbase = (long)(blockIdx.y * 2 + half) * nq + qrow;
-    const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
+    const long rbase = (long)(chunk * 2 + half) * nq + qrow;
 
     // per-element update of one value (the rare path)
     auto update = [&](float x, int j) {
@@ -415,8 +442,6 @@ __global__ void __launch_bounds__(NT_TC, 1)
       }
     };
 
-    int it = 0;
-    bool ok = true;
     for (int t = t_begin; t < t_end; t++, it++) {
       const int a = it & 1;
       const uint32_t u = (uint32_t)(it >> 1);
@@ -450,7 +475,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
       process(r2, j0 + 64);
       process(r3, j0 + 96);
     }
-    (void)ok;
+    // a failed wait ends this unit's scan; the merge below still runs, so that
+    // every selection warp reaches each named barrier
     if (MODE == SCAN_THRESH && rvalid) sel.cnt[rbase] = rcount;
     if (MODE != SCAN_THRESH) {
       // merge the two column halves of each row
@@ -461,7 +487,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
       }
       asm volatile("bar.sync 1, 256;" ::: "memory");
       if (half == 0 && rvalid) {
-        const long o = ((long)blockIdx.y * nq + qrow) * C;
+        const long o = ((long)chunk * nq + qrow) * C;
         int ia = 0, ib = 0;
         for (int s = 0; s < C; s++) {
           float va, vb;
@@ -487,6 +513,10 @@ __global__ void __launch_bounds__(NT_TC, 1)
           if (takeA) ia++; else ib++;
         }
       }
+    }
+    // the next unit's half 1 rewrites the rows only after they are merged, and
+    // all selection warps leave the unit loop together (any failed wait ends it)
+    if (PERSIST) ok = bar_red_and_256(ok);
     }
   }
 
@@ -579,7 +609,20 @@ int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_
     mqn = mq;
     mbn = mb;
   }
-  if (!PAIR) {
+  if (!PAIR && QS) {
+    // persistent: one CTA per SM (the ring fills shared memory), units strided
+    int dev = 0, nsm = 0;
+    YG_CUDA(cudaGetDevice(&dev));
+    YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const long nunits = ceil_div(nq, TC_TILE_M) * (long)sel.nchunk;
+    if (nunits > INT_MAX) {
+      set_error(E_UNSUPPORTED, "tc_scan: %ld work units", nunits);
+      return E_UNSUPPORTED;
+    }
+    const unsigned g = (unsigned)(nunits < nsm ? nunits : nsm);
+    tc_scan_kernel<MODE, C, L2, QS, PAIR><<<g, NT_TC, lay.total, st>>>(mq, mqn, mb, mbn, nq, nb,
+                                                                        nkb, S, sel, op.err);
+  } else if (!PAIR) {
     dim3 grid((unsigned)ceil_div(nq, TC_TILE_M), (unsigned)sel.nchunk);
     tc_scan_kernel<MODE, C, L2, QS, PAIR><<<grid, NT_TC, lay.total, st>>>(
         mq, mqn, mb, mbn, nq, nb, nkb, S, sel, op.err);

@@ -125,8 +125,12 @@ int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream
   // three stages still fits beside it (always for K <= 256; for the 3xBF16
   // split of d <= 128, K = 384, with short lists); else it is streamed with
   // every K block
-  bool resident = op.Kp <= 256;
-  if (!resident && op.Kp <= 384) {
+  // A unit of at most two base tiles reuses a resident tile at most twice: then
+  // the streamed form, whose persistent grid also saves a CTA start-up
+  // (barriers, TMEM allocation, first loads) per query tile, is faster.
+  const bool few_tiles = !pair && sel.tiles_per_chunk <= 2;
+  bool resident = op.Kp <= 256 && !few_tiles;
+  if (!resident && !few_tiles && op.Kp <= 384) {
     const int C = sel.mode == SCAN_THRESH ? 1 : sel.C;
     resident = tck::make_layout(op.Kp / 64, 3, sel.mode, C, false, false).total <= 227 * 1024;
   }

@@ -1,5 +1,6 @@
-// Streamed-query instantiation of the tcgen05 distance kernel, single CTAs
-// (any Kp; used by the split 3xBF16 packing, whose K is three times d).
+// Streamed-query instantiation of the tcgen05 distance kernel, single CTAs on
+// a persistent grid (any Kp; used when the query tile is too large to stay
+// resident, and when a work unit holds at most two base tiles).
 #include "tc_kernel.cuh"
 
 namespace yg {
