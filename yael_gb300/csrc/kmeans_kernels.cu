@@ -363,31 +363,39 @@ __global__ void hist_kernel(const int *assign, const int *pinst, long n, int k,
 
 __global__ void scan_kernel(const int *counts, long ncl, long *offs, long *cursor) {
   // offs has ncl + 1 entries: offs[ncl] = total
-  // one block: contiguous chunks per thread, then a scan of the chunk sums
-  __shared__ long part[1024];
-  const int t = threadIdx.x, nt = blockDim.x;
+  // one block of 1024: contiguous chunks per thread, then a shuffle scan of
+  // the chunk sums (within warps, then over the 32 warp totals)
+  __shared__ long wsum[32];
+  const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, w = t >> 5;
   const long per = (ncl + nt - 1) / nt;
   const long a = (long)t * per, b = a + per < ncl ? a + per : ncl;
   long s = 0;
   for (long i = a; i < b; i++) s += counts[i];
-  part[t] = s;
+  long x = s;  // inclusive scan within the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
   __syncthreads();
-  if (t == 0) {
-    long run = 0;
-    for (int i = 0; i < nt; i++) {
-      const long x = part[i];
-      part[i] = run;
-      run += x;
+  if (w == 0) {
+    long z = lane < (nt >> 5) ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
     }
+    wsum[lane] = z;  // inclusive over warps
   }
   __syncthreads();
-  long run = part[t];
+  long run = x - s + (w > 0 ? wsum[w - 1] : 0);
   for (long i = a; i < b; i++) {
     offs[i] = run;
     cursor[i] = run;
     run += counts[i];
   }
-  if (t == nt - 1) offs[ncl] = part[nt - 1] + s;
+  if (t == nt - 1) offs[ncl] = run;
 }
 
 __global__ void scatter_kernel(const int *assign, const int *pinst, long n, int k,
@@ -444,39 +452,62 @@ __global__ void __launch_bounds__(256)
     segsum_kernel(const long *perm, const long *total, const int *assign, const int *pinst,
                   const float *__restrict__ v, int d, int k, const int *shift,
                   long long *acc) {
-  constexpr int RUN = 32;
+  constexpr int RUN = 32, PF = 4;  // points per warp; rows in flight
   const int lane = threadIdx.x & 31;
   const long wglob = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long nsorted = *total;
   const long s0 = wglob * RUN;
   if (s0 >= nsorted) return;
-  const long s1 = s0 + RUN < nsorted ? s0 + RUN : nsorted;
+  const int n = (int)(nsorted - s0 < RUN ? nsorted - s0 : RUN);
   const int dbase = blockIdx.y * NDR * 32;
+  // lane i holds the row, cluster and shift of the run's i-th point
+  long p_l = 0, g_l = -1;
+  int sh_l = 0;
+  if (lane < n) {
+    p_l = perm[s0 + lane];
+    const int inst = pinst ? pinst[p_l] : 0;
+    g_l = (long)inst * k + assign[p_l];
+    sh_l = shift[inst];
+  }
   long long part[NDR];
 #pragma unroll
   for (int r = 0; r < NDR; r++) part[r] = 0;
   long gcur = -1;
-  for (long s = s0; s < s1; s++) {
-    const long p = perm[s];
-    const int inst = pinst ? pinst[p] : 0;
-    const long g = (long)inst * k + assign[p];
-    if (g != gcur) {
-      if (gcur >= 0) {
+  for (int i0 = 0; i0 < n; i0 += PF) {
+    float xv[PF][NDR];
 #pragma unroll
-        for (int r = 0; r < NDR; r++) {
-          const int c = dbase + r * 32 + lane;
-          if (c < d && part[r])
-            atomicAdd((unsigned long long *)(acc + gcur * d + c), (unsigned long long)part[r]);
-          part[r] = 0;
-        }
+    for (int u = 0; u < PF; u++) {
+      const int i = i0 + u;  // < RUN + PF: the shuffle index wraps, the value is unused
+      const long p = __shfl_sync(0xffffffffu, p_l, i & 31);
+#pragma unroll
+      for (int r = 0; r < NDR; r++) {
+        const int c = dbase + r * 32 + lane;
+        xv[u][r] = (i < n && c < d) ? __ldg(v + p * d + c) : 0.f;
       }
-      gcur = g;
     }
-    const int sh = shift[inst];
 #pragma unroll
-    for (int r = 0; r < NDR; r++) {
-      const int c = dbase + r * 32 + lane;
-      if (c < d) part[r] += fixed_of(__ldg(v + p * d + c), sh);
+    for (int u = 0; u < PF; u++) {
+      const int i = i0 + u;
+      if (i >= n) break;  // uniform over the warp
+      const long g = __shfl_sync(0xffffffffu, g_l, i);
+      const int sh = __shfl_sync(0xffffffffu, sh_l, i);
+      if (g != gcur) {
+        if (gcur >= 0) {
+#pragma unroll
+          for (int r = 0; r < NDR; r++) {
+            const int c = dbase + r * 32 + lane;
+            if (c < d && part[r])
+              atomicAdd((unsigned long long *)(acc + gcur * d + c), (unsigned long long)part[r]);
+            part[r] = 0;
+          }
+        }
+        gcur = g;
+      }
+#pragma unroll
+      for (int r = 0; r < NDR; r++) {
+        const int c = dbase + r * 32 + lane;
+        if (c < d) part[r] += fixed_of(xv[u][r], sh);
+      }
     }
   }
   if (gcur >= 0) {

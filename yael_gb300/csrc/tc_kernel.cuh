@@ -85,6 +85,37 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 }
 
 // sorted insertion of (x, j) into an ascending register list; the caller has
+// Upper bound of the C-th smallest value of a thread's 128 columns (four
+// 32-column register sets): the largest of the minima of C equal column
+// blocks, each block holding a value <= it.  A block without a number (all
+// NaN) or holding +inf gives +inf, i.e. no bound.
+template <int C>
+__device__ __forceinline__ float cth_bound(const uint32_t (&r0)[32], const uint32_t (&r1)[32],
+                                           const uint32_t (&r2)[32], const uint32_t (&r3)[32]) {
+  constexpr int BS = 128 / C;  // block width in columns, a multiple of 8
+  float B = -INFINITY, run = INFINITY;
+  auto chunk = [&](const uint32_t (&r)[32], int c) {
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      const uint32_t *x = r + 8 * g;
+      run = fminf(run, fmin3(fmin3(__uint_as_float(x[0]), __uint_as_float(x[1]),
+                                   __uint_as_float(x[2])),
+                             fmin3(__uint_as_float(x[3]), __uint_as_float(x[4]),
+                                   __uint_as_float(x[5])),
+                             fminf(__uint_as_float(x[6]), __uint_as_float(x[7]))));
+      if ((c * 32 + 8 * g + 8) % BS == 0) {
+        B = fmaxf(B, run);
+        run = INFINITY;
+      }
+    }
+  };
+  chunk(r0, 0);
+  chunk(r1, 1);
+  chunk(r2, 2);
+  chunk(r3, 3);
+  return B;
+}
+
 // checked x < L[C-1].  Equal values keep their earlier (smaller) ids first.
 template <int C>
 __device__ __forceinline__ void reg_insert(float (&L)[C], int (&I)[C], float x, int j) {
@@ -351,6 +382,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
     }
     if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
     int rcount = 0;  // THRESH: hits of this thread's region (chunk, half, query)
+    float tb = INFINITY;  // lists: bound of the current half tile's C-th smallest
     const long rbase = (long)(chunk * 2 + half) * nq + qrow;
 
     // per-element update of one value (the rare path)
@@ -415,15 +447,15 @@ __global__ void __launch_bounds__(NT_TC, 1)
                       fmin3(v[8 * g + 3], v[8 * g + 4], v[8 * g + 5]),
                       fminf(v[8 * g + 6], v[8 * g + 7]));
       const float mc = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
-      const float bnd = MODE == SCAN_THRESH ? thr : lmax;
-      const bool pass = rvalid && (MODE == SCAN_THRESH ? !(mc > bnd) : !(mc >= bnd));
+      // lists: a superset filter (update() keeps the strict x < lmax)
+      const float bnd = MODE == SCAN_THRESH ? thr : fminf(lmax, tb);
+      const bool pass = rvalid && !(mc > bnd);
       if (!__any_sync(0xffffffffu, pass)) return;
       if (!pass) return;
       uint32_t bits = 0;
 #pragma unroll
       for (int i = 0; i < 32; i++) {
-        const bool h = MODE == SCAN_THRESH ? !(v[i] > bnd) : !(v[i] >= bnd);
-        bits |= h ? (1u << i) : 0u;
+        bits |= !(v[i] > bnd) ? (1u << i) : 0u;
       }
 #pragma unroll 1
       while (bits) {
@@ -469,6 +501,12 @@ __global__ void __launch_bounds__(NT_TC, 1)
           mbar_arrive_cluster(tempty_l + (uint32_t)(a * 8));
         else
           mbar_arrive(&tempty[a]);
+      }
+      // first tile of a unit: the lists are empty and every value would be a
+      // hit; a bound of this half tile's C-th smallest filters them instead
+      if (MODE != SCAN_THRESH && C <= 16) {
+        tb = INFINITY;
+        if (t == t_begin && j0 + 128 <= nb) tb = cth_bound<C>(r0, r1, r2, r3);
       }
       process(r0, j0);
       process(r1, j0 + 32);
