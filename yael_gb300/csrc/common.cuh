@@ -83,8 +83,12 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // host uploads overlapped with passes (lazy)
   Workspace ws;
-  Workspace host_ws;  // pinned host staging
+  void *pinned_status = nullptr;  // kPinnedStatusBytes of pinned host memory (lazy)
 };
+
+constexpr size_t kPinnedStatusBytes = 4096;
+// the context's pinned status buffer: small device -> host reads stay async
+int ctx_pinned_status(Ctx *c, void **out);
 
 // returns the calling thread's context (created on first use)
 int ctx_get(Ctx **out);

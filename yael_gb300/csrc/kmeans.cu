@@ -160,9 +160,11 @@ struct Engine {
   long n_fallback = 0, n_second = 0, n_band = 0;
   float ms_assign = 0, ms_update = 0;
 
-  // CUDA graphs of one Lloyd iteration's device work (grouped small-k path):
-  // the assignment and the update are captured on the second iteration (the
-  // first runs eagerly and sets every kernel attribute) and replayed after.
+  // CUDA graphs of one Lloyd iteration's device work: the update always, the
+  // assignment on the grouped small-k path (the k-NN path reads its
+  // certificate results on the host).  Both are captured on the second
+  // iteration (the first runs eagerly and sets every kernel attribute) and
+  // replayed after.
   // Their arguments never change within a run: the per-iteration state (active
   // instances, split centroids) lives in device buffers written between
   // replays.  YAEL_GPU_GRAPHS=0 runs every iteration eagerly.
@@ -185,8 +187,9 @@ struct Engine {
       const char *e = getenv("YAEL_GPU_GRAPHS");
       return !(e && e[0] == '0');
     }();
-    return on && !graphs_failed && !(in.size() == 1 && k > kSmallK);
+    return on && !graphs_failed;
   }
+  bool assign_graph_wanted() const { return graphs_wanted() && !(in.size() == 1 && k > kSmallK); }
 
   // captures body() on st into *exec; false (and eager mode) on any failure
   template <typename F>
@@ -285,11 +288,15 @@ struct Engine {
     return OK;
   }
 
+  std::vector<unsigned char> hactive;  // the flags last written to the device
+
   int set_active() {
     std::vector<unsigned char> h(in.size());
     for (size_t i = 0; i < in.size(); i++) h[i] = !in[i].done;
+    if (h == hactive) return OK;
     YG_CUDA(cudaMemcpyAsync(active, h.data(), h.size(), cudaMemcpyHostToDevice, st));
     YG_CUDA(cudaStreamSynchronize(st));  // h is a stack buffer
+    hactive = h;
     return OK;
   }
 
@@ -341,13 +348,14 @@ struct Engine {
       return OK;
     };
     const bool use_graphs = graphs_wanted() && eager_done;
-    if (use_graphs && !g_assign) {
-      if (!capture([&] { return assign_step(); }, &g_assign, &g_assign_n) ||
+    const bool graph_assign = use_graphs && assign_graph_wanted();
+    if (use_graphs && !g_update) {
+      if ((graph_assign && !capture([&] { return assign_step(); }, &g_assign, &g_assign_n)) ||
           !capture(update_body, &g_update, &g_update_n))
         graphs_failed = true;
     }
     cudaEventRecord(e0, st);
-    if (use_graphs && !graphs_failed) {
+    if (graph_assign && !graphs_failed) {
       YG_CUDA(cudaGraphLaunch(g_assign, st));
       count_launches(g_assign_n);
     } else {

@@ -25,6 +25,24 @@ struct Small {
   unsigned long long n_cand;
 };
 
+static_assert(sizeof(Small) <= kPinnedStatusBytes, "status block larger than its pinned copy");
+
+__global__ void small_init_kernel(Small *s) {
+  memset(s, 0, sizeof(Small));
+  s->bs.all_exact = 1;
+  s->bs3.all_exact = 1;
+}
+
+// the device status block, read through the context's pinned buffer
+int read_small(Ctx *ctx, const Small *dsmall, cudaStream_t st, Small *out) {
+  void *pin;
+  YG_CHECK(ctx_pinned_status(ctx, &pin));
+  YG_CUDA(cudaMemcpyAsync(pin, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
+  YG_CUDA(cudaStreamSynchronize(st));
+  memcpy(out, pin, sizeof(Small));
+  return OK;
+}
+
 // packed base operands of the tensor-core passes (the split one is built on
 // first use by the second-chance pass)
 struct BaseOps {
@@ -422,8 +440,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
 
   // ---- later chances for the queries the certificate rejected
   Small hs;
-  YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
-  YG_CUDA(cudaStreamSynchronize(st));
+  YG_CHECK(read_small(ctx, dsmall, st, &hs));
   tr.collect();
   if (tm_scan) {
     tm_scan->collect();
@@ -616,13 +633,8 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
 
   Small *dsmall;
   YG_CHECK(ws_get(ws, WS_SMALL, 1, &dsmall));
-  {
-    Small h;
-    memset(&h, 0, sizeof(h));
-    h.bs.all_exact = 1;
-    h.bs3.all_exact = 1;
-    YG_CUDA(cudaMemcpyAsync(dsmall, &h, sizeof(h), cudaMemcpyHostToDevice, st));
-  }
+  small_init_kernel<<<1, 1, 0, st>>>(dsmall);
+  YG_LAUNCH_CHECK();
 
   if (job.w) {
     // weighted distances reorder per base row: exhaustive exact path
@@ -674,8 +686,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   int bexact = 0;
   if (k > 1) {
     Small hs;
-    YG_CUDA(cudaMemcpyAsync(&hs, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
-    YG_CUDA(cudaStreamSynchronize(st));
+    YG_CHECK(read_small(ctx, dsmall, st, &hs));
     bexact = hs.bs.all_exact;
   }
   bops.plain.err = bops.split.err = &dsmall->tc_err;

@@ -111,6 +111,20 @@ int ctx_get(Ctx **out) {
   return OK;
 }
 
+int ctx_pinned_status(Ctx *c, void **out) {
+  if (!c->pinned_status) {
+    cudaError_t e = cudaMallocHost(&c->pinned_status, kPinnedStatusBytes);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      c->pinned_status = nullptr;
+      set_error(E_NOMEM, "cudaMallocHost(%zu): %s", kPinnedStatusBytes, cudaGetErrorString(e));
+      return E_NOMEM;
+    }
+  }
+  *out = c->pinned_status;
+  return OK;
+}
+
 int default_precision() {
   const char *s = getenv("YAEL_GPU_PRECISION");
   if (!s || !*s) return PREC_FP32;
