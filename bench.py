@@ -154,7 +154,7 @@ def run_reference(args, world, rank):
 
 # DRAM bytes (read + write) of one main-pass launch at the default k-NN sizes,
 # from the ncu capture summarised in profiles/tc_scan_knn_main_nb1M_nq10k.md
-KNN_MAIN_TRAFFIC = 434.985984e6 + 48.504576e6
+KNN_MAIN_TRAFFIC = 325.835776e6 + 44.952832e6
 
 CLUSTER_CFG = {
     # n, d, k, niter, seed, data
