@@ -84,3 +84,68 @@ def test_batch_device_pointers():
     assert rc == 0, yg.last_error()
     for (q, b), i in zip(pairs, di):
         np.testing.assert_array_equal(i.cpu().numpy(), knn_exact(b, q, k)[0])
+
+
+def _device_batch(pairs, k, metric, torch):
+    dq = [torch.from_numpy(q).cuda() for q, _ in pairs]
+    db = [torch.from_numpy(b).cuda() for _, b in pairs]
+    di = [torch.full((q.shape[0], k), -7, dtype=torch.int32, device="cuda") for q, _ in pairs]
+    dd = [torch.empty((q.shape[0], k), device="cuda") for q, _ in pairs]
+    descs = (yg.KnnPair * len(pairs))()
+    for i in range(len(pairs)):
+        descs[i] = yg.KnnPair(pairs[i][0].shape[0], pairs[i][1].shape[0], dq[i].data_ptr(),
+                              db[i].data_ptr(), di[i].data_ptr(), dd[i].data_ptr())
+    stream = torch.cuda.current_stream()
+    o = yg.KnnOpts(1, metric, 1, ctypes.c_void_p(stream.cuda_stream))
+    d = pairs[0][0].shape[1]
+    rc = yg.lib().yael_gpu_knn_batch(len(pairs), ctypes.cast(descs, ctypes.c_void_p), d, k,
+                                     ctypes.byref(o))
+    assert rc == 0, yg.last_error()
+    torch.cuda.synchronize()
+    return [(i.cpu().numpy(), x.cpu().numpy()) for i, x in zip(di, dd)], o
+
+
+@pytest.mark.parametrize("metric", [2, 16])
+@pytest.mark.parametrize("d", [64, 128])
+def test_grouped_batch_uneven(metric, d):
+    """Device arrays, BF16, k = 32: the grouped pipeline (one launch per pass).
+    Pairs cover empty and single queries, bases of exactly k rows, bases where
+    every row is a candidate and bases with a threshold sample, and query
+    counts that are not multiples of the 128-row tile."""
+    torch = pytest.importorskip("torch")
+    k = 32
+    sizes = [(0, 40), (1, 32), (5, 3000), (130, 700), (300, 9000), (257, 64), (64, 20000),
+             (1, 33), (700, 2500), (33, 50000), (129, 12000)]
+    pairs = unit_pairs(11 + d + metric, sizes, d)
+    out, o = _device_batch(pairs, k, metric, torch)
+    for (q, b), (idx, dis) in zip(pairs, out):
+        if q.shape[0] == 0:
+            continue
+        if metric == 2:
+            ridx, rdis, _ = knn_exact(b, q, k, NT)
+        else:
+            ridx, rdis = dot_order(q, b, k)
+        np.testing.assert_array_equal(idx, ridx)
+        np.testing.assert_allclose(dis, rdis, rtol=2e-6, atol=2e-6)
+
+
+def test_grouped_batch_rejections_rerun():
+    """A base with hundreds of copies of one row next to the queries overflows
+    the candidate regions: those queries fail the certificate in the grouped
+    pass and are settled by the single-pair pipeline; the others stay."""
+    torch = pytest.importorskip("torch")
+    k = 32
+    rng = np.random.default_rng(21)
+    d = 64
+    pairs = unit_pairs(22, [(200, 30000), (50, 15000)], d)
+    q, b = pairs[0]
+    b = b.copy()
+    b[1000:1600] = q[7]  # 600 exact copies of query 7
+    b[5000:5400] = q[9] + 1e-4 * rng.standard_normal(d).astype(np.float32)
+    pairs[0] = (q, b)
+    out, o = _device_batch(pairs, k, 2, torch)
+    assert o.n_band > 0  # the rejected queries were re-run
+    for (q, b), (idx, dis) in zip(pairs, out):
+        ridx, rdis, _ = knn_exact(b, q, k, NT)
+        np.testing.assert_array_equal(idx, ridx)
+        np.testing.assert_allclose(dis, rdis, rtol=2e-6, atol=2e-6)

@@ -1,6 +1,8 @@
 // Batched exact k-NN over many independent (queries, base) pairs of uneven
-// sizes (yael_gpu_knn_batch).  The pairs run concurrently on a persistent pool
-// of host workers; each worker owns a context (stream + grow-only workspace,
+// sizes (yael_gpu_knn_batch).  Device arrays with the BF16 pass and k >= 9 go
+// through the grouped pipeline (group.cu: one launch per pass over all the
+// pairs).  Otherwise the pairs run concurrently on a persistent pool of host
+// workers; each worker owns a context (stream + grow-only workspace,
 // runtime.cu) that lives as long as the process, so repeated batches reuse
 // their buffers.  Pairs are handed out largest first (nq * nb) from an atomic
 // cursor, which balances the uneven sizes; the calling thread works too.
@@ -174,6 +176,24 @@ extern "C" int yael_gpu_knn_batch(int npairs, const yael_gpu_knn_pair *pairs, in
       set_error(E_CUDA, "knn_batch: cudaStreamSynchronize: %s", cudaGetErrorString(e));
       return E_CUDA;
     }
+  }
+  if (npairs > 0 && knn_grouped_eligible(d, k, t.prec, t.device_ptrs)) {
+    Ctx *ctx;
+    YG_CHECK(ctx_get(&ctx));
+    GroupCounters gc;
+    const int rc = knn_grouped(npairs, pairs, d, k, t.metric, ctx->stream, &gc);
+    if (rc == OK) {
+      if (opts) {
+        opts->n_fallback = (int)std::min<long long>(gc.n_fallback, 0x7fffffff);
+        opts->n_band = (int)std::min<long long>(gc.n_band, 0x7fffffff);
+        opts->n_second = (int)std::min<long long>(gc.n_second, 0x7fffffff);
+        opts->n_candidates = (int)std::min<long long>(gc.n_cand, 0x7fffffff);
+        opts->exact_class = gc.all_exact;
+      }
+      return OK;
+    }
+    if (rc != E_NOMEM) return rc;  // out of memory: the per-pair pool below
+    (void)cudaGetLastError();
   }
   t.order.resize(npairs);
   for (int i = 0; i < npairs; i++) t.order[i] = i;

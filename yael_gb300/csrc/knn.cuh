@@ -57,6 +57,17 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st);
 int knn_host(int metric, int nq, int nb, int d, int k, const float *b, const float *q,
              const float *w, int *assign, float *dis, int prec, yael_gpu_knn_opts *opts);
 
+// Grouped batched k-NN (group.cu): every pair of a batch through one launch
+// per pass.  Eligible: device arrays, the BF16 pass, k >= 9 (the threshold
+// form of the selection); YAEL_GPU_BATCH_GROUPED=0 turns it off.
+struct GroupCounters {
+  long long n_band = 0, n_second = 0, n_fallback = 0, n_cand = 0;
+  int all_exact = 1;
+};
+bool knn_grouped_eligible(int d, int k, int prec, int device_ptrs);
+int knn_grouped(int npairs, const yael_gpu_knn_pair *pairs, int d, int k, int metric,
+                cudaStream_t st, GroupCounters *gc);
+
 // workspace slots (each slot is one grow-only device buffer per host thread)
 enum WsSlot : int {
   WS_QN64 = 0, WS_QFLAG, WS_QRES, WS_BN32, WS_SMALL, WS_EPS, WS_QEXACT,

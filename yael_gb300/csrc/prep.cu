@@ -152,9 +152,21 @@ __global__ void __launch_bounds__(PW * 32)
     const float *xr = x + row * ld;
     float s = 0.f, r = 0.f;
     int exact = 1, bad = 0;
-    for (int c = sl * 4; c < cols; c += 4 * LPR) {
-      float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (rv && c < d) q4 = __ldg(reinterpret_cast<const float4 *>(xr + c));
+    // every load of the row first (cols <= 128, the launch condition), then
+    // the conversions: NIT float4 loads of each lane in flight at once
+    constexpr int NIT = 128 / (4 * LPR);
+    float4 q4s[NIT];
+#pragma unroll
+    for (int it = 0; it < NIT; it++) {
+      const int c = sl * 4 + it * 4 * LPR;
+      q4s[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (rv && c < d) q4s[it] = __ldg(reinterpret_cast<const float4 *>(xr + c));
+    }
+#pragma unroll
+    for (int it = 0; it < NIT; it++) {
+      const int c = sl * 4 + it * 4 * LPR;
+      if (c >= cols) break;
+      const float4 q4 = q4s[it];
       const float e[4] = {q4.x, q4.y, q4.z, q4.w};
       __nv_bfloat16 hb[4];
 #pragma unroll

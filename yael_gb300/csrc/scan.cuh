@@ -21,6 +21,39 @@
 
 namespace yg {
 
+struct SetStats;
+
+// Grouped passes (tc_scan only): many (queries, base) pairs in one persistent
+// launch.  The pairs' packed queries are concatenated, and so are their packed
+// bases, each pair's base padded so that its tiles (in the view the pass
+// reads) start at a tile boundary.  A unit is one query tile of one pair
+// against a range of that pair's base tiles.
+struct GroupUnit {
+  int q0;              // first query row of the tile (concatenated rows)
+  int qend;            // end of the pair's query rows
+  int t_begin, t_end;  // base tiles of this view of the concatenated base
+  int bend;            // end of the pair's valid columns in this view
+  int pair;            // index into the pair table
+  int chunk;           // chunk of the pair's base (THRESH region; 0 for lists)
+  int pad_;
+};
+
+// Per pair: where its candidates go (THRESH) and what the re-rank needs.
+struct GroupPair {
+  long cnt_off;   // region counters: cnt[cnt_off + r * nq + (row - qoff)]
+  long cand_off;  // slots: candv/candi[cand_off + (r * nq + (row - qoff)) * cap + s]
+  int qoff, nq;   // the pair's rows in the concatenated queries
+  int boff;       // first row of the pair in the concatenated base (ids are relative)
+  int nb;
+  int nreg;       // THRESH regions per query (chunks * halves)
+  int cap;        // THRESH slots per region
+  const float *q;           // the pair's query rows (FP32, stride d): exact re-rank
+  const float *b;           // the pair's base rows (FP32, stride d)
+  int *out_idx;             // the pair's outputs, nq x k
+  float *out_dis;
+  const SetStats *bs;       // the pair's base statistics
+};
+
 // SCAN_TOPV is SCAN_TOPC without ids (only the values are kept and written;
 // used where a rank statistic of the distances is all that is needed).
 enum ScanMode : int { SCAN_TOPC = 0, SCAN_THRESH = 1, SCAN_TOPV = 2 };
@@ -40,6 +73,11 @@ struct ScanSel {
   int cap = 0;              // THRESH: slots per (region, query)
   int halves = 2;           // THRESH: regions per chunk (column halves of a row)
   int id_off = 0;           // added to every emitted base id (a pass over a base slice)
+  // grouped pass (units != null): the work units, in launch order, and the
+  // pair table; the pass's nq / nb are those of the concatenated operands
+  const GroupUnit *units = nullptr;
+  int nunits = 0;
+  const GroupPair *gpairs = nullptr;
   __host__ __device__ int nregion() const { return nchunk * halves; }
 };
 

@@ -103,12 +103,25 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
   const double qn = L2 ? a.qn64[q] : 0.0;
   const float eps = a.eps ? a.eps[q] : 0.f;
   const bool ex = a.qexact ? a.qexact[q] != 0 : false;
+  // a grouped row reads its pair's candidate regions, base, statistics and
+  // outputs; otherwise the pass-wide ones
+  const GroupPair *gp = a.qpair ? &a.gpairs[a.qpair[q]] : nullptr;
+  const long qloc = gp ? (long)(q - gp->qoff) : (long)q;
+  const long nqv = gp ? (long)gp->nq : (long)a.nq;
+  const long cnt_base = gp ? gp->cnt_off : 0, cand_base = gp ? gp->cand_off : 0;
+  const int cap = gp ? gp->cap : a.sel.cap;
+  const float *B = gp ? gp->b : a.b;
+  const long ldb = gp ? (long)d : a.ldb;
+  int *oidx = gp ? gp->out_idx : a.out_idx;
+  float *odis = gp ? gp->out_dis : a.out_dis;
+  const SetStats *bst = gp ? gp->bs : a.bstats;
 
   if (tid == 0) {
     sM = 0; sfail = 0; sneed64 = 0;
     sT = ~0ull;
   }
-  for (int c = tid; c < d; c += RT) qv[c] = a.q[(long)q * a.ldq + c];
+  const float *qrow = gp ? gp->q + qloc * d : a.q + (long)q * a.ldq;
+  for (int c = tid; c < d; c += RT) qv[c] = qrow[c];
   __syncthreads();
 
   // ---- 1. gather candidates as (approx dist, id)
@@ -133,7 +146,7 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
   } else {
     // regions (chunk, half) of this query; any overflowing region fails the
     // query.  Offsets first (one thread), then one sweep over all regions.
-    const int nreg = s.nregion();
+    const int nreg = gp ? gp->nreg : s.nregion();
     __shared__ int s_off[kMaxRegions + 1];
     __shared__ int s_wsum[RT / 32];
     if (nreg > kMaxRegions) {
@@ -143,8 +156,8 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
       int run = 0;
       for (int r0 = 0; r0 < nreg; r0 += RT) {
         const int r = r0 + tid;
-        int cnt = r < nreg ? s.cnt[(long)r * a.nq + q] : 0;
-        if (cnt > s.cap) sfail = 1;
+        int cnt = r < nreg ? s.cnt[cnt_base + (long)r * nqv + qloc] : 0;
+        if (cnt > cap) sfail = 1;
         int x = cnt;  // inclusive scan within the warp
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -176,7 +189,7 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
           const int mid = (lo + hi + 1) >> 1;
           if (s_off[mid] <= e) lo = mid; else hi = mid - 1;
         }
-        const long o = ((long)lo * a.nq + q) * s.cap + (e - s_off[lo]);
+        const long o = cand_base + ((long)lo * nqv + qloc) * cap + (e - s_off[lo]);
         const float v = s.candv[o];
         const float av = L2 ? (float)((double)v + qn) : v;
         K[e] = f2ord(av);
@@ -220,8 +233,8 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
         }
       }
       for (int r = tid; r < k; r += RT) {
-        a.out_idx[(long)q * k + r] = I[r];
-        a.out_dis[(long)q * k + r] = ord2f((unsigned)K[r]);
+        oidx[qloc * k + r] = I[r];
+        odis[qloc * k + r] = ord2f((unsigned)K[r]);
       }
       return;
     }
@@ -244,7 +257,7 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
     // ---- 3. FP32 re-rank of the band
     const int warp = tid >> 5, nw = RT / 32;
     for (int i = warp; i < nband; i += nw) {
-      const float e = warp_dist32(qv, a.b + (long)I[i] * a.ldb, d, a.metric);
+      const float e = warp_dist32(qv, B + (long)I[i] * ldb, d, a.metric);
       if ((tid & 31) == 0) E[i] = e;
     }
     __syncthreads();
@@ -260,7 +273,7 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
     const float rho = (float)(d + 4) * kU;
     float eta = 0.f;
     if (!L2) {
-      const float B = __uint_as_float(a.bstats->max_norm_bits);
+      const float B = __uint_as_float(bst->max_norm_bits);
       eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64 ? a.qn64[q] : 0.0, 0.0)) * B;
     }
     // near ties anywhere up to position k -> FP64 for the whole band
@@ -275,7 +288,7 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
     if (sneed64) {
       // one thread per candidate, sequential FP64 sum
       for (int i = tid; i < nband; i += RT) {
-        const double e = dist64_seq(qv, a.b + (long)I[i] * a.ldb, d, a.metric);
+        const double e = dist64_seq(qv, B + (long)I[i] * ldb, d, a.metric);
         K[i] = d2ord(e);
       }
       __syncthreads();
@@ -287,15 +300,15 @@ __global__ void __launch_bounds__(RT) rerank_kernel(RerankArgs a, int Mp_alloc) 
       for (int r = tid; r < k; r += RT) {
         const unsigned long long kr = K[r];
         const unsigned long long ur = (kr & 0x8000000000000000ull) ? (kr & 0x7fffffffffffffffull) : ~kr;
-        a.out_idx[(long)q * k + r] = I[r];
-        a.out_dis[(long)q * k + r] = (float)__longlong_as_double((long long)ur);
+        oidx[qloc * k + r] = I[r];
+        odis[qloc * k + r] = (float)__longlong_as_double((long long)ur);
       }
     } else {
       const float ek = ord2f((unsigned)K[k - 1]);
       ek_hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
       for (int r = tid; r < k; r += RT) {
-        a.out_idx[(long)q * k + r] = I[r];
-        a.out_dis[(long)q * k + r] = ord2f((unsigned)K[r]);
+        oidx[qloc * k + r] = I[r];
+        odis[qloc * k + r] = ord2f((unsigned)K[r]);
       }
     }
     // ---- 4. certificate: every non-candidate is provably worse than the k-th
@@ -481,9 +494,11 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
 
 __global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn64,
                            const float *qres, const unsigned char *qflag,
-                           const SetStats *bs, float *eps, unsigned char *qexact) {
+                           const SetStats *bs, float *eps, unsigned char *qexact,
+                           const int *qpair, const GroupPair *gpairs) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq) return;
+  if (qpair) bs = gpairs[qpair[q]].bs;  // grouped: the query's own pair
   const bool ex = qflag[q] && bs->all_exact;
   qexact[q] = ex;
   if (ex) { eps[q] = 0.f; return; }
@@ -732,6 +747,7 @@ int rerank(const RerankArgs &a, cudaStream_t st) {
   int Mmax = a.sel.mode == SCAN_TOPC ? a.sel.nchunk * a.sel.C : a.sel.nregion() * a.sel.cap;
   if (a.sel.mode == SCAN_THRESH && a.m_expect > 0 && Mmax > 4 * a.m_expect + 64)
     Mmax = 4 * a.m_expect + 64;
+  if (a.gpairs) Mmax = a.max_candidates;  // grouped: sized by the caller over all pairs
   if (Mmax < a.k) Mmax = a.k;
   if (Mmax > kMaxCandidates) Mmax = kMaxCandidates;  // more candidates than this fail the query
   int Mp = 1;
@@ -746,10 +762,12 @@ int rerank(const RerankArgs &a, cudaStream_t st) {
 
 int compute_eps(int nq, int d, int prec, int metric, const double *qn64,
                 const float *qres, const unsigned char *qflag, const SetStats *bstats,
-                float *eps, unsigned char *qexact, cudaStream_t st) {
+                float *eps, unsigned char *qexact, cudaStream_t st, const int *qpair,
+                const GroupPair *gpairs) {
   if (nq <= 0) return OK;
   eps_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(nq, d, prec, metric, qn64, qres,
-                                                          qflag, bstats, eps, qexact);
+                                                          qflag, bstats, eps, qexact, qpair,
+                                                          gpairs);
   YG_LAUNCH_CHECK();
   return OK;
 }

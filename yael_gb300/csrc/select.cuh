@@ -41,16 +41,24 @@ struct RerankArgs {
   // sized for a few times this rather than for every region's capacity, and a
   // query with more candidates fails its certificate (the band pass follows)
   int m_expect = 0;
+  // grouped re-rank (many pairs, THRESH): row q belongs to pair qpair[q], whose
+  // table entry gives its candidate regions, base rows, statistics and outputs
+  // (q, qn64, eps, qexact, thr, fail_list and kth_out stay indexed by q)
+  const int *qpair = nullptr;
+  const GroupPair *gpairs = nullptr;
+  int max_candidates = 0;        // grouped: shared memory is sized for this many
 };
 
 int rerank(const RerankArgs &a, cudaStream_t st);
 
 // eps[q] in dist space for the FP32 path (prec 0) or the BF16 path (prec 1),
-// computed from the query's norm / residual and the base set statistics.
+// computed from the query's norm / residual and the base set statistics
+// (grouped: those of the query's pair, gpairs[qpair[q]].bs).
 // qexact[q] = query exact class and every base row exact class.
 int compute_eps(int nq, int d, int prec, int metric, const double *qn64,
                 const float *qres, const unsigned char *qflag, const SetStats *bstats,
-                float *eps, unsigned char *qexact, cudaStream_t st);
+                float *eps, unsigned char *qexact, cudaStream_t st,
+                const int *qpair = nullptr, const GroupPair *gpairs = nullptr);
 
 // eps[q] for the 3xBF16 split pass: the left-out q_lo.b_lo and residual
 // terms plus the FP32 accumulation of 3*Kp1 + 16 products.

@@ -73,7 +73,7 @@ __host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C, b
   L.list_off = off;
   if (mode != SCAN_THRESH) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
   off = (off + 15) & ~(size_t)15;
-  L.bar_off = off; off += (size_t)(2 * S + 5) * 8 + 16;
+  L.bar_off = off; off += (size_t)(2 * S + 6) * 8 + 16;
   L.total = off + 1024;  // alignment slack for the 1024-byte aligned base
   return L;
 }
@@ -154,7 +154,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
   uint64_t *bars = reinterpret_cast<uint64_t *>(base + lay.bar_off);
   uint64_t *full = bars, *empty = bars + S, *tfull = bars + 2 * S, *tempty = bars + 2 * S + 2;
   uint64_t *qfull = bars + 2 * S + 4;
-  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * S + 5);
+  uint64_t *qempty = bars + 2 * S + 5;  // resident query tile released (grouped)
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * S + 6);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_holder + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -165,14 +166,36 @@ __global__ void __launch_bounds__(NT_TC, 1)
   // persistent grid that walks the units with stride gridDim.x (ring position,
   // accumulator buffer and barrier phases carry over from unit to unit); else
   // one unit per CTA from the 2D grid (query tile, chunk).
-  constexpr bool PERSIST = QS && !PAIR;
+  // A grouped pass (sel.units) takes its units from the table: query rows and
+  // valid columns end at the unit's pair, and ids are relative to its base.
+  // A grouped pass with a resident query tile is persistent too: the tile is
+  // reloaded per unit once the previous unit's MMAs have released it (qempty).
+  const bool grouped = !PAIR && sel.units != nullptr;
+  const bool PERSIST = !PAIR && (QS || grouped);
   const int nqt = (int)ceil_div(nq, TC_TILE_M);
-  const int nunits = PERSIST ? nqt * sel.nchunk : 1;
+  const int nunits = grouped ? sel.nunits : PERSIST ? nqt * sel.nchunk : 1;
   const int w0 = PERSIST ? (int)blockIdx.x : 0, wstep = PERSIST ? (int)gridDim.x : 1;
-  auto unit_q0 = [&](int w) -> long {
-    return PERSIST ? (long)(w % nqt) * TC_TILE_M : (long)blockIdx.x * TC_TILE_M;
+  struct UnitInfo {
+    long q0, qend;
+    int t_begin, t_end, bend, chunk, pair;
   };
-  auto unit_chunk = [&](int w) -> int { return PERSIST ? w / nqt : (int)blockIdx.y; };
+  auto unit_info = [&](int w) -> UnitInfo {
+    UnitInfo u;
+    if (grouped) {
+      const GroupUnit g = sel.units[w];
+      u.q0 = g.q0; u.qend = g.qend; u.t_begin = g.t_begin; u.t_end = g.t_end;
+      u.bend = g.bend; u.chunk = g.chunk; u.pair = g.pair;
+      return u;
+    }
+    u.q0 = PERSIST ? (long)(w % nqt) * TC_TILE_M : (long)blockIdx.x * TC_TILE_M;
+    u.qend = nq;
+    u.chunk = PERSIST ? w / nqt : (int)blockIdx.y;
+    u.t_begin = u.chunk * sel.tiles_per_chunk;
+    u.t_end = imin(ntb, u.t_begin + sel.tiles_per_chunk);
+    u.bend = nb;
+    u.pair = -1;
+    return u;
+  };
   const uint32_t crank = PAIR ? cluster_ctarank() : 0;
   const bool leader = crank == 0;
 
@@ -187,6 +210,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
       mbar_init(&tempty[a], (PAIR ? 2 : 1) * (N_EPI / 32));
     }
     mbar_init(qfull, 1);
+    mbar_init(qempty, 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -213,8 +237,20 @@ __global__ void __launch_bounds__(NT_TC, 1)
     // ---------------- TMA producer (every CTA loads its own query tile and
     // its part of each base block)
     if (lane == 0) {
+      // ring position: stage sn, phase parity phn (advanced at every use)
+      int sn = 0;
+      uint32_t phn = 0;
+      bool ok = true;
+      int ui = 0;  // units done by this CTA
+      for (int w = w0; w < nunits && ok; w += wstep, ui++) {
+      const UnitInfo un = unit_info(w);
+      const long q0 = un.q0;
       if (!QS) {
-        const long q0 = unit_q0(0);
+        // the resident tile of the previous unit is free once its MMAs are done
+        if (ui > 0 && !mbar_wait(qempty, (uint32_t)((ui - 1) & 1), abort_flag)) {
+          ok = false;
+          break;
+        }
         const uint32_t qbytes = (uint32_t)(nkb * QBLK_BYTES + (L2 ? 128 * 32 : 0));
         if (PAIR) {
           if (leader) mbar_arrive_expect_tx(qfull, 2 * qbytes);
@@ -228,15 +264,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           if (L2) tma_load_2d(&mapQn, qfull, Qn, 0, (int)q0);
         }
       }
-      // ring position: stage sn, phase parity phn (advanced at every use)
-      int sn = 0;
-      uint32_t phn = 0;
-      bool ok = true;
-      for (int w = w0; w < nunits && ok; w += wstep) {
-      const long q0 = unit_q0(w);
-      const int t_begin = unit_chunk(w) * sel.tiles_per_chunk;
-      const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
-      for (int t = t_begin; t < t_end && ok; t++) {
+      for (int t = un.t_begin; t < un.t_end && ok; t++) {
         const int brow = t * TC_TILE_N + (int)crank * (TC_TILE_N / 2) * (PAIR ? 1 : 0);
         for (int ks = 0; ks < nks; ks++) {
           const int s = sn;
@@ -271,6 +299,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
         }
       }
       }
+      // the last unit's tile release has landed before the CTA exits
+      if (!QS && PERSIST && ok && ui > 0) ok = mbar_wait(qempty, (uint32_t)((ui - 1) & 1), abort_flag);
       if (PAIR) {
         // every stage released by the leader's MMAs: no commit is still on its
         // way to this CTA when the pair exits
@@ -286,15 +316,17 @@ __global__ void __launch_bounds__(NT_TC, 1)
     // ---------------- MMA issuer (the leader's, for a pair)
     if (lane == 0 && leader) {
       constexpr uint32_t idesc = idesc_bf16_f32(PAIR ? 2 * TC_TILE_M : TC_TILE_M, TC_TILE_N);
-      bool ok = QS ? true : mbar_wait(qfull, 0, abort_flag);
-      tc_fence_after();
+      bool ok = true;
       int sn = 0;
       uint32_t phn = 0;
-      int it = 0;
-      for (int w = w0; w < nunits && ok; w += wstep) {
-      const int t_begin = unit_chunk(w) * sel.tiles_per_chunk;
-      const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
-      for (int t = t_begin; t < t_end && ok; t++, it++) {
+      int it = 0, ui = 0;
+      for (int w = w0; w < nunits && ok; w += wstep, ui++) {
+      const UnitInfo un = unit_info(w);
+      if (!QS) {
+        if (!mbar_wait(qfull, (uint32_t)(ui & 1), abort_flag)) { ok = false; break; }
+        tc_fence_after();
+      }
+      for (int t = un.t_begin; t < un.t_end && ok; t++, it++) {
         const int a = it & 1;
         const uint32_t u = (uint32_t)(it >> 1);
         if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag)) { ok = false; break; }
@@ -343,6 +375,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
         else
           umma_commit(&tfull[a]);
       }
+      // release the resident query tile once this unit's MMAs are done
+      if (!QS && PERSIST && ok) umma_commit(qempty);
       }
       if (PAIR) {
         // the last two accumulators released by the selection warps of both
@@ -365,11 +399,12 @@ __global__ void __launch_bounds__(NT_TC, 1)
     int it = 0;
     bool ok = true;
     for (int w = w0; w < nunits && ok; w += wstep) {
-    const long qrow = unit_q0(w) + row;
-    const int chunk = unit_chunk(w);
-    const int t_begin = chunk * sel.tiles_per_chunk;
-    const int t_end = imin(ntb, t_begin + sel.tiles_per_chunk);
-    const bool rvalid = qrow < nq;
+    const UnitInfo un = unit_info(w);
+    const long qrow = un.q0 + row;
+    const int chunk = un.chunk;
+    const int t_begin = un.t_begin, t_end = un.t_end;
+    const int nbv = un.bend;  // columns at or past nbv are not the unit's
+    const bool rvalid = qrow < un.qend;
     float lmax = INFINITY, thr = NAN;
     constexpr int CR = (C <= 16) ? C : 1;  // register lists up to 16 entries
     float RL[CR];
@@ -383,7 +418,19 @@ __global__ void __launch_bounds__(NT_TC, 1)
     if (MODE == SCAN_THRESH && rvalid) thr = sel.thr[qrow];
     int rcount = 0;  // THRESH: hits of this thread's region (chunk, half, query)
     float tb = INFINITY;  // lists: bound of the current half tile's C-th smallest
-    const long rbase = (long)(chunk * 2 + half) * nq + qrow;
+    // THRESH region of this thread: counter index and first slot
+    long rbase = (long)(chunk * 2 + half) * nq + qrow, cbase;
+    int cap = sel.cap, id_off = sel.id_off;
+    if (grouped && MODE == SCAN_THRESH) {
+      const GroupPair &gp = sel.gpairs[un.pair];
+      const long rl = (long)(chunk * 2 + half) * gp.nq + (qrow - gp.qoff);
+      rbase = gp.cnt_off + rl;
+      cbase = gp.cand_off + rl * gp.cap;
+      cap = gp.cap;
+      id_off = -gp.boff;
+    } else {
+      cbase = rbase * cap;
+    }
 
     // per-element update of one value (the rare path)
     auto update = [&](float x, int j) {
@@ -416,9 +463,9 @@ __global__ void __launch_bounds__(NT_TC, 1)
         }
       } else {
         if (x <= thr) {
-          if (rcount < sel.cap) {
-            sel.candv[rbase * sel.cap + rcount] = x;
-            sel.candi[rbase * sel.cap + rcount] = j + sel.id_off;
+          if (rcount < cap) {
+            sel.candv[cbase + rcount] = x;
+            sel.candi[cbase + rcount] = j + id_off;
           }
           rcount++;
         }
@@ -435,10 +482,10 @@ __global__ void __launch_bounds__(NT_TC, 1)
       float v[32];
 #pragma unroll
       for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-      if (jc + 32 > nb) {
+      if (jc + 32 > nbv) {
 #pragma unroll
         for (int i = 0; i < 32; i++)
-          if (jc + i >= nb) v[i] = NAN;
+          if (jc + i >= nbv) v[i] = NAN;
       }
       float m8[4];
 #pragma unroll
@@ -506,7 +553,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
       // hit; a bound of this half tile's C-th smallest filters them instead
       if (MODE != SCAN_THRESH && C <= 16) {
         tb = INFINITY;
-        if (t == t_begin && j0 + 128 <= nb) tb = cth_bound<C>(r0, r1, r2, r3);
+        if (t == t_begin && j0 + 128 <= nbv) tb = cth_bound<C>(r0, r1, r2, r3);
       }
       process(r0, j0);
       process(r1, j0 + 32);
@@ -547,7 +594,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           const float vo = takeA ? va : vb;
           const int xo = takeA ? xa : xb;
           sel.topv[o + s] = vo;
-          sel.topi[o + s] = (xo == 0x7fffffff) ? -1 : xo + sel.id_off;
+          sel.topi[o + s] = (xo == 0x7fffffff) ? -1 : xo + id_off;
           if (takeA) ia++; else ib++;
         }
       }
@@ -647,12 +694,12 @@ int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_
     mqn = mq;
     mbn = mb;
   }
-  if (!PAIR && QS) {
+  if (!PAIR && (QS || sel.units)) {
     // persistent: one CTA per SM (the ring fills shared memory), units strided
     int dev = 0, nsm = 0;
     YG_CUDA(cudaGetDevice(&dev));
     YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const long nunits = ceil_div(nq, TC_TILE_M) * (long)sel.nchunk;
+    const long nunits = sel.units ? (long)sel.nunits : ceil_div(nq, TC_TILE_M) * (long)sel.nchunk;
     if (nunits > INT_MAX) {
       set_error(E_UNSUPPORTED, "tc_scan: %ld work units", nunits);
       return E_UNSUPPORTED;

@@ -112,6 +112,20 @@ int tc_dispatch_r1(const TcOperands &op, int nq, int nb, const ScanSel &sel, cud
 
 int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
   if (nq <= 0 || nb <= 0) return OK;
+  if (sel.units) {
+    // grouped pass: the streamed-query persistent form walks the unit table;
+    // ids of list passes would not be relative to their pair
+    if (sel.mode == SCAN_TOPC) {
+      set_error(E_UNSUPPORTED, "tc_scan: grouped pass with id lists");
+      return E_UNSUPPORTED;
+    }
+    // the query tile stays resident when it fits beside a ring of 3 stages
+    const bool res = op.Kp <= 256 || (op.Kp <= 384 && tck::make_layout(op.Kp / 64, 3, sel.mode,
+                                                                       sel.mode == SCAN_THRESH ? 1 : sel.C,
+                                                                       false, false)
+                                                          .total <= 227 * 1024);
+    return res ? tc_dispatch_r1(op, nq, nb, sel, st) : tc_dispatch_s1(op, nq, nb, sel, st);
+  }
   // CTA pairs (one 256-row MMA over two SMs) halve the per-SM base traffic
   // but add a cross-SM handoff to every accumulator; measured on the 1M x 10k
   // k-NN pass they are slower (3.98 ms vs 2.87 ms), so single CTAs are the
