@@ -123,20 +123,47 @@ struct Wave {
   std::vector<int> pairs;  // indices into the caller's pair array
 };
 
-// One wave: every pair of w through the grouped passes; results in the pairs'
-// output arrays, counters added to *gc.
-int run_wave(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int metric, Ctx *ctx,
-             cudaStream_t st, GroupCounters *gc) {
+// Everything a wave's passes need, on the device, plus the host copy of its
+// pair table for the final checks.  Two sets of buffers alternate between
+// consecutive waves, so wave i + 1 is packed while wave i's passes run.
+struct WaveState {
+  int np = 0, nq_all = 0, stride = 1, max_cand = 0;
+  long brows = 0;
+  std::vector<GroupPair> hp;
+  size_t n_mu = 0, n_su = 0;
+  __nv_bfloat16 *bpack = nullptr, *bnorm = nullptr, *qpack = nullptr, *qnorm = nullptr;
+  double *qn64 = nullptr;
+  unsigned char *qflag = nullptr, *qexact = nullptr, *dinf = nullptr;
+  float *qres = nullptr, *eps = nullptr, *thr = nullptr, *kth = nullptr, *stopv = nullptr;
+  float *candv = nullptr;
+  int *qpair = nullptr, *fail = nullptr, *cnt = nullptr, *candi = nullptr, *stopi = nullptr;
+  SetStats *stats = nullptr;
+  GroupPair *dpairs = nullptr;
+  GroupUnit *dmu = nullptr, *dsu = nullptr;
+  GroupStatus *status = nullptr;
+  cudaEvent_t ev[5] = {};  // trace: pack | sample | main | rerank
+};
+
+constexpr int kSetSlots = 32;  // slot distance between the two buffer sets
+
+// Phase 1 (stream sp): layout, buffers of set `set`, packing, unit tables,
+// error bounds.
+int wave_prepare(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int metric,
+                 Ctx *ctx, int set, cudaStream_t sp, WaveState &S) {
   Workspace &ws = ctx->ws;
+  const int o = set * kSetSlots;
   const int np = (int)w.pairs.size();
   const int Kp = ((d + 63) / 64) * 64;
   const bool L2 = metric == METRIC_L2;
   const int stride = std::max(1, k / 3);
   const long P = (long)TC_TILE_N * stride;
+  S.np = np;
+  S.stride = stride;
   // ---- layout
-  std::vector<GroupPair> hp(np);
+  std::vector<GroupPair> &hp = S.hp;
+  hp.assign(np, GroupPair());
   std::vector<unsigned char> hinf(np);
-  long nqt_all = 0, brows = 0;
+  long brows = 0;
   int nq_all = 0;
   for (int i = 0; i < np; i++) {
     const yael_gpu_knn_pair &x = pairs[w.pairs[i]];
@@ -151,64 +178,56 @@ int run_wave(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int me
     g.out_dis = x.dis;
     nq_all += x.nq;
     brows += round_up(x.nb, P);
-    nqt_all += ceil_div(x.nq, TC_TILE_M);
     hinf[i] = pair_inf(x.nb, stride) ? 1 : 0;
   }
+  S.nq_all = nq_all;
+  S.brows = brows;
   if (nq_all == 0) return OK;
   if (brows > 0x7fffffffL) {
     set_error(E_UNSUPPORTED, "knn_batch: %ld padded base rows in one group", brows);
     return E_UNSUPPORTED;
   }
   // ---- buffers
-  __nv_bfloat16 *bpack, *bnorm = nullptr, *qpack, *qnorm = nullptr;
-  double *qn64;
-  unsigned char *qflag, *qexact, *dinf;
-  float *qres, *eps, *thr, *kth;
-  SetStats *stats;
-  GroupPair *dpairs;
-  int *qpair, *fail;
-  GroupStatus *status;
-  YG_CHECK(gs_get(ws, GS_BPACK, (size_t)brows * Kp, &bpack));
-  if (L2) YG_CHECK(gs_get(ws, GS_BNORM, (size_t)brows * 16, &bnorm));
-  YG_CHECK(gs_get(ws, GS_QPACK, (size_t)nq_all * Kp, &qpack));
-  if (L2) YG_CHECK(gs_get(ws, GS_QNORM, (size_t)nq_all * 16, &qnorm));
-  YG_CHECK(gs_get(ws, GS_QN64, nq_all, &qn64));
-  YG_CHECK(gs_get(ws, GS_QFLAG, nq_all, &qflag));
-  YG_CHECK(gs_get(ws, GS_QRES, nq_all, &qres));
-  YG_CHECK(gs_get(ws, GS_EPS, nq_all, &eps));
-  YG_CHECK(gs_get(ws, GS_QEXACT, nq_all, &qexact));
-  YG_CHECK(gs_get(ws, GS_THR, nq_all, &thr));
-  YG_CHECK(gs_get(ws, GS_KTH, nq_all, &kth));
-  YG_CHECK(gs_get(ws, GS_FAIL, nq_all, &fail));
-  YG_CHECK(gs_get(ws, GS_QPAIR, nq_all, &qpair));
-  YG_CHECK(gs_get(ws, GS_STATS, np, &stats));
-  YG_CHECK(gs_get(ws, GS_INF, np, &dinf));
-  YG_CHECK(gs_get(ws, GS_STATUS, 1, &status));
-  for (int i = 0; i < np; i++) hp[i].bs = stats + i;
+  YG_CHECK(gs_get(ws, o + GS_BPACK, (size_t)brows * Kp, &S.bpack));
+  if (L2) YG_CHECK(gs_get(ws, o + GS_BNORM, (size_t)brows * 16, &S.bnorm));
+  YG_CHECK(gs_get(ws, o + GS_QPACK, (size_t)nq_all * Kp, &S.qpack));
+  if (L2) YG_CHECK(gs_get(ws, o + GS_QNORM, (size_t)nq_all * 16, &S.qnorm));
+  YG_CHECK(gs_get(ws, o + GS_QN64, nq_all, &S.qn64));
+  YG_CHECK(gs_get(ws, o + GS_QFLAG, nq_all, &S.qflag));
+  YG_CHECK(gs_get(ws, o + GS_QRES, nq_all, &S.qres));
+  YG_CHECK(gs_get(ws, o + GS_EPS, nq_all, &S.eps));
+  YG_CHECK(gs_get(ws, o + GS_QEXACT, nq_all, &S.qexact));
+  YG_CHECK(gs_get(ws, o + GS_THR, nq_all, &S.thr));
+  YG_CHECK(gs_get(ws, o + GS_KTH, nq_all, &S.kth));
+  YG_CHECK(gs_get(ws, o + GS_FAIL, nq_all, &S.fail));
+  YG_CHECK(gs_get(ws, o + GS_QPAIR, nq_all, &S.qpair));
+  YG_CHECK(gs_get(ws, o + GS_STATS, np, &S.stats));
+  YG_CHECK(gs_get(ws, o + GS_INF, np, &S.dinf));
+  YG_CHECK(gs_get(ws, o + GS_STATUS, 1, &S.status));
+  for (int i = 0; i < np; i++) hp[i].bs = S.stats + i;
 
   // trace: events between the passes (YAEL_GPU_TRACE)
-  const bool tr = trace_enabled();
-  cudaEvent_t ev[5] = {};
-  if (tr)
-    for (auto &e : ev) cudaEventCreate(&e);
-  if (tr) cudaEventRecord(ev[0], st);
+  if (trace_enabled()) {
+    for (auto &e : S.ev) cudaEventCreate(&e);
+    cudaEventRecord(S.ev[0], sp);
+  }
 
   // ---- packing: every pair's base and queries into the concatenated buffers
-  stats_init_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, st>>>(stats, np);
+  stats_init_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, sp>>>(S.stats, np);
   YG_LAUNCH_CHECK();
-  YG_CUDA(cudaMemsetAsync(status, 0, sizeof(GroupStatus), st));
+  YG_CUDA(cudaMemsetAsync(S.status, 0, sizeof(GroupStatus), sp));
   const float qscale = L2 ? -2.f : 1.f;
   for (int i = 0; i < np; i++) {
     const GroupPair &g = hp[i];
     YG_CHECK(prep_rows(g.b, d, g.nb, d, 1.f, nullptr, nullptr, nullptr, nullptr,
-                       bpack + (size_t)g.boff * Kp, Kp, L2 ? bnorm + (size_t)g.boff * 16 : nullptr,
-                       L2 ? 1 : 0, stats + i, st));
+                       S.bpack + (size_t)g.boff * Kp, Kp,
+                       L2 ? S.bnorm + (size_t)g.boff * 16 : nullptr, L2 ? 1 : 0, S.stats + i,
+                       sp));
     if (g.nq == 0) continue;
-    const float *q = pairs[w.pairs[i]].q;
-    YG_CHECK(prep_rows(q, d, g.nq, d, qscale, qn64 + g.qoff, nullptr, qflag + g.qoff,
-                       qres + g.qoff, qpack + (size_t)g.qoff * Kp, Kp,
-                       L2 ? qnorm + (size_t)g.qoff * 16 : nullptr, L2 ? 2 : 0, nullptr, st));
-    qpair_kernel<<<(unsigned)ceil_div(g.nq, 256), 256, 0, st>>>(qpair, i, g.qoff, g.nq);
+    YG_CHECK(prep_rows(g.q, d, g.nq, d, qscale, S.qn64 + g.qoff, nullptr, S.qflag + g.qoff,
+                       S.qres + g.qoff, S.qpack + (size_t)g.qoff * Kp, Kp,
+                       L2 ? S.qnorm + (size_t)g.qoff * 16 : nullptr, L2 ? 2 : 0, nullptr, sp));
+    qpair_kernel<<<(unsigned)ceil_div(g.nq, 256), 256, 0, sp>>>(S.qpair, i, g.qoff, g.nq);
     YG_LAUNCH_CHECK();
   }
 
@@ -261,7 +280,7 @@ int run_wave(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int me
       }
     }
   }
-  max_cand = std::min(max_cand, kMaxCandidates);
+  S.max_cand = std::min(max_cand, kMaxCandidates);
   // longest units first: the persistent CTAs take units round robin
   auto by_len = [](const GroupUnit &a, const GroupUnit &b) {
     return a.t_end - a.t_begin > b.t_end - b.t_begin;
@@ -272,115 +291,138 @@ int run_wave(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int me
     set_error(E_UNSUPPORTED, "knn_batch: too many work units");
     return E_UNSUPPORTED;
   }
-
-  GroupUnit *dmu, *dsu = nullptr;
-  float *stopv = nullptr, *candv;
-  int *cnt, *candi, *stopi = nullptr;
-  YG_CHECK(gs_get(ws, GS_PAIRS, np, &dpairs));
-  YG_CHECK(gs_get(ws, GS_MUNITS, mu.size(), &dmu));
+  S.n_mu = mu.size();
+  S.n_su = su.size();
+  YG_CHECK(gs_get(ws, o + GS_PAIRS, np, &S.dpairs));
+  YG_CHECK(gs_get(ws, o + GS_MUNITS, mu.size(), &S.dmu));
   if (!su.empty()) {
-    YG_CHECK(gs_get(ws, GS_SUNITS, su.size(), &dsu));
-    YG_CHECK(gs_get(ws, GS_STOPV, (size_t)nq_all * 16, &stopv));
-    YG_CHECK(gs_get(ws, GS_STOPI, (size_t)nq_all * 16, &stopi));
+    YG_CHECK(gs_get(ws, o + GS_SUNITS, su.size(), &S.dsu));
+    YG_CHECK(gs_get(ws, o + GS_STOPV, (size_t)nq_all * 16, &S.stopv));
+    YG_CHECK(gs_get(ws, o + GS_STOPI, (size_t)nq_all * 16, &S.stopi));
   }
-  YG_CHECK(gs_get(ws, GS_CNT, cnt_tot, &cnt));
-  YG_CHECK(gs_get(ws, GS_CANDV, cand_tot, &candv));
-  YG_CHECK(gs_get(ws, GS_CANDI, cand_tot, &candi));
+  YG_CHECK(gs_get(ws, o + GS_CNT, cnt_tot, &S.cnt));
+  YG_CHECK(gs_get(ws, o + GS_CANDV, cand_tot, &S.candv));
+  YG_CHECK(gs_get(ws, o + GS_CANDI, cand_tot, &S.candi));
   // the host tables are copied before they go out of scope: pageable copies
   // are staged before cudaMemcpyAsync returns
-  YG_CUDA(cudaMemcpyAsync(dpairs, hp.data(), sizeof(GroupPair) * np, cudaMemcpyHostToDevice, st));
-  YG_CUDA(cudaMemcpyAsync(dinf, hinf.data(), np, cudaMemcpyHostToDevice, st));
-  YG_CUDA(cudaMemcpyAsync(dmu, mu.data(), sizeof(GroupUnit) * mu.size(), cudaMemcpyHostToDevice,
-                          st));
+  YG_CUDA(cudaMemcpyAsync(S.dpairs, hp.data(), sizeof(GroupPair) * np, cudaMemcpyHostToDevice,
+                          sp));
+  YG_CUDA(cudaMemcpyAsync(S.dinf, hinf.data(), np, cudaMemcpyHostToDevice, sp));
+  YG_CUDA(cudaMemcpyAsync(S.dmu, mu.data(), sizeof(GroupUnit) * mu.size(),
+                          cudaMemcpyHostToDevice, sp));
   if (!su.empty())
-    YG_CUDA(cudaMemcpyAsync(dsu, su.data(), sizeof(GroupUnit) * su.size(),
-                            cudaMemcpyHostToDevice, st));
+    YG_CUDA(cudaMemcpyAsync(S.dsu, su.data(), sizeof(GroupUnit) * su.size(),
+                            cudaMemcpyHostToDevice, sp));
 
   // ---- error bounds, per query against its own pair's statistics
-  YG_CHECK(compute_eps(nq_all, d, PREC_BF16, metric, qn64, qres, qflag, nullptr, eps, qexact, st,
-                       qpair, dpairs));
+  YG_CHECK(compute_eps(nq_all, d, PREC_BF16, metric, S.qn64, S.qres, S.qflag, nullptr, S.eps,
+                       S.qexact, sp, S.qpair, S.dpairs));
+  return OK;
+}
 
+// Phase 2 (stream st): the sample pass, thresholds, main pass and re-rank.
+// max_ctas > 0 leaves SMs free for the next wave's packing.
+int wave_execute(WaveState &S, int d, int k, int metric, int max_ctas, cudaStream_t st) {
+  if (S.nq_all == 0) return OK;
+  const int Kp = ((d + 63) / 64) * 64;
   TcOperands op;
   op.d = d;
   op.Kp = Kp;
   op.metric = metric;
   op.split = 0;
-  op.q = qpack;
-  op.qn = qnorm;
-  op.b = bpack;
-  op.bn = bnorm;
-  op.b_rows = brows;
+  op.q = S.qpack;
+  op.qn = S.qnorm;
+  op.b = S.bpack;
+  op.bn = S.bnorm;
+  op.b_rows = S.brows;
   op.b_step = 1;
-  op.err = &status->tc_err;
-
-  // ---- threshold sample pass and thresholds
-  if (tr) cudaEventRecord(ev[1], st);
-  if (!su.empty()) {
+  op.err = &S.status->tc_err;
+  if (S.ev[1]) cudaEventRecord(S.ev[1], st);
+  if (S.n_su) {
     ScanSel ss;
     ss.mode = SCAN_TOPV;
     ss.C = 16;
     ss.nchunk = 1;
-    ss.topv = stopv;
-    ss.topi = stopi;
-    ss.units = dsu;
-    ss.nunits = (int)su.size();
-    ss.gpairs = dpairs;
+    ss.topv = S.stopv;
+    ss.topi = S.stopi;
+    ss.units = S.dsu;
+    ss.nunits = (int)S.n_su;
+    ss.gpairs = S.dpairs;
+    ss.max_ctas = max_ctas;
     TcOperands ops;
-    YG_CHECK(tc_base_view(op, stride, (int)(brows / stride), &ops));
-    YG_CHECK(tc_scan(ops, nq_all, (int)(brows / stride), ss, st));
-    YG_CHECK(thresh_from_sample(nq_all, 1, 16, kSampleC, stopv, eps, thr, st));
+    YG_CHECK(tc_base_view(op, S.stride, (int)(S.brows / S.stride), &ops));
+    YG_CHECK(tc_scan(ops, S.nq_all, (int)(S.brows / S.stride), ss, st));
+    YG_CHECK(thresh_from_sample(S.nq_all, 1, 16, kSampleC, S.stopv, S.eps, S.thr, st));
   }
-  thr_inf_kernel<<<(unsigned)ceil_div(nq_all, 256), 256, 0, st>>>(qpair, dpairs, dinf, nq_all,
-                                                                  thr);
+  thr_inf_kernel<<<(unsigned)ceil_div(S.nq_all, 256), 256, 0, st>>>(S.qpair, S.dpairs, S.dinf,
+                                                                    S.nq_all, S.thr);
   YG_LAUNCH_CHECK();
-
-  // ---- main pass
-  if (tr) cudaEventRecord(ev[2], st);
+  if (S.ev[2]) cudaEventRecord(S.ev[2], st);
   ScanSel sel;
   sel.mode = SCAN_THRESH;
   sel.halves = 2;
-  sel.thr = thr;
-  sel.cnt = cnt;
-  sel.candv = candv;
-  sel.candi = candi;
-  sel.units = dmu;
-  sel.nunits = (int)mu.size();
-  sel.gpairs = dpairs;
-  YG_CHECK(tc_scan(op, nq_all, (int)brows, sel, st));
-
-  // ---- re-rank every query against its pair
+  sel.thr = S.thr;
+  sel.cnt = S.cnt;
+  sel.candv = S.candv;
+  sel.candi = S.candi;
+  sel.units = S.dmu;
+  sel.nunits = (int)S.n_mu;
+  sel.gpairs = S.dpairs;
+  sel.max_ctas = max_ctas;
+  YG_CHECK(tc_scan(op, S.nq_all, (int)S.brows, sel, st));
+  if (S.ev[3]) cudaEventRecord(S.ev[3], st);
   RerankArgs ra;
-  ra.nq = nq_all;
+  ra.nq = S.nq_all;
   ra.nb = 0;
   ra.d = d;
   ra.k = k;
   ra.metric = metric;
-  ra.qn64 = qn64;
-  ra.eps = eps;
-  ra.qexact = qexact;
+  ra.qn64 = S.qn64;
+  ra.eps = S.eps;
+  ra.qexact = S.qexact;
   ra.sel = sel;
-  ra.fail_list = fail;
-  ra.fail_cnt = &status->fail_cnt;
-  ra.n_cand = &status->n_cand;
-  ra.kth_out = kth;
-  ra.m_expect = kSampleC * stride;
-  ra.qpair = qpair;
-  ra.gpairs = dpairs;
-  ra.max_candidates = max_cand;
-  if (tr) cudaEventRecord(ev[3], st);
+  ra.fail_list = S.fail;
+  ra.fail_cnt = &S.status->fail_cnt;
+  ra.n_cand = &S.status->n_cand;
+  ra.kth_out = S.kth;
+  ra.m_expect = kSampleC * S.stride;
+  ra.qpair = S.qpair;
+  ra.gpairs = S.dpairs;
+  ra.max_candidates = S.max_cand;
   YG_CHECK(rerank(ra, st));
-  if (tr) cudaEventRecord(ev[4], st);
+  if (S.ev[4]) cudaEventRecord(S.ev[4], st);
+  return OK;
+}
 
-  // ---- status, base statistics; queries the certificate rejected go
-  // through the single-pair pipeline of their pair
+// Phase 3 (stream st, host sync): status, base statistics; the queries the
+// certificate rejected go through the single-pair pipeline of their pair.
+int wave_finish(WaveState &S, int d, int k, int metric, Ctx *ctx, int set, cudaStream_t st,
+                GroupCounters *gc) {
+  if (S.nq_all == 0) return OK;
+  Workspace &ws = ctx->ws;
+  const int o = set * kSetSlots;
+  const int np = S.np;
   void *pin;
   YG_CHECK(ctx_pinned_status(ctx, &pin));
-  YG_CUDA(cudaMemcpyAsync(pin, status, sizeof(GroupStatus), cudaMemcpyDeviceToHost, st));
+  YG_CUDA(cudaMemcpyAsync(pin, S.status, sizeof(GroupStatus), cudaMemcpyDeviceToHost, st));
   std::vector<SetStats> hs(np);
-  YG_CUDA(cudaMemcpyAsync(hs.data(), stats, sizeof(SetStats) * np, cudaMemcpyDeviceToHost, st));
+  YG_CUDA(cudaMemcpyAsync(hs.data(), S.stats, sizeof(SetStats) * np, cudaMemcpyDeviceToHost, st));
   YG_CUDA(cudaStreamSynchronize(st));
   GroupStatus gst;
   memcpy(&gst, pin, sizeof(gst));
+  if (S.ev[0]) {
+    float t[4];
+    for (int i = 0; i < 4; i++) cudaEventElapsedTime(&t[i], S.ev[i], S.ev[i + 1]);
+    fprintf(stderr,
+            "[yael_gpu] grouped wave: %d pairs, %d queries, %ld base rows, %zu + %zu units: "
+            "pack %.3f ms (to the passes' start), sample %.3f ms, main %.3f ms, rerank %.3f ms, "
+            "rejected %d\n",
+            np, S.nq_all, S.brows, S.n_su, S.n_mu, t[0], t[1], t[2], t[3], gst.fail_cnt);
+    for (auto &e : S.ev) {
+      cudaEventDestroy(e);
+      e = nullptr;
+    }
+  }
   if (gst.tc_err) {
     set_error(E_TIMEOUT, "tensor-core pass gave up waiting (bounded wait expired)");
     return E_TIMEOUT;
@@ -389,20 +431,12 @@ int run_wave(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int me
   for (int i = 0; i < np; i++)
     if (!hs[i].all_exact) gc->all_exact = 0;
   const int nf = gst.fail_cnt;
-  if (tr) {
-    float t[4];
-    for (int i = 0; i < 4; i++) cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]);
-    fprintf(stderr,
-            "[yael_gpu] grouped wave: %d pairs, %d queries, %ld base rows, %zu + %zu units: "
-            "pack %.3f ms, sample %.3f ms, main %.3f ms, rerank %.3f ms, rejected %d\n",
-            np, nq_all, brows, su.size(), mu.size(), t[0], t[1], t[2], t[3], nf);
-    for (auto &e : ev) cudaEventDestroy(e);
-  }
   if (nf == 0) return OK;
-  std::vector<int> hf(nf), hqp(nf);
-  YG_CUDA(cudaMemcpyAsync(hf.data(), fail, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
+  std::vector<int> hf(nf);
+  YG_CUDA(cudaMemcpyAsync(hf.data(), S.fail, sizeof(int) * nf, cudaMemcpyDeviceToHost, st));
   YG_CUDA(cudaStreamSynchronize(st));
   std::sort(hf.begin(), hf.end());
+  const std::vector<GroupPair> &hp = S.hp;
   size_t a0 = 0;
   while (a0 < hf.size()) {
     // the failed rows of one pair (rows are concatenated pair by pair)
@@ -418,10 +452,10 @@ int run_wave(const yael_gpu_knn_pair *pairs, const Wave &w, int d, int k, int me
     for (int r = 0; r < m; r++) rows[r] = hf[a0 + r] - g.qoff;
     int *drows, *fidx;
     float *fq, *fdis;
-    YG_CHECK(gs_get(ws, GS_FROWS, m, &drows));
-    YG_CHECK(gs_get(ws, GS_FQ, (size_t)m * d, &fq));
-    YG_CHECK(gs_get(ws, GS_FIDX, (size_t)m * k, &fidx));
-    YG_CHECK(gs_get(ws, GS_FDIS, (size_t)m * k, &fdis));
+    YG_CHECK(gs_get(ws, o + GS_FROWS, m, &drows));
+    YG_CHECK(gs_get(ws, o + GS_FQ, (size_t)m * d, &fq));
+    YG_CHECK(gs_get(ws, o + GS_FIDX, (size_t)m * k, &fidx));
+    YG_CHECK(gs_get(ws, o + GS_FDIS, (size_t)m * k, &fdis));
     YG_CUDA(cudaMemcpyAsync(drows, rows.data(), sizeof(int) * m, cudaMemcpyHostToDevice, st));
     gather_rows_k<<<(unsigned)ceil_div((long)m * d, 256), 256, 0, st>>>(g.q, d, drows, m, fq);
     YG_LAUNCH_CHECK();
@@ -459,8 +493,13 @@ int knn_grouped(int npairs, const yael_gpu_knn_pair *pairs, int d, int k, int me
   const int Kp = ((d + 63) / 64) * 64;
   const int stride = std::max(1, k / 3);
   const long P = (long)TC_TILE_N * stride;
-  // waves of pairs whose buffers stay within a budget (YAEL_GPU_GROUP_BYTES)
-  size_t budget = (size_t)24 << 30;
+  // waves of pairs whose buffers stay within a budget (YAEL_GPU_GROUP_BYTES;
+  // two waves' buffers are live at a time)
+  static const bool pipeline = [] {
+    const char *e = getenv("YAEL_GPU_GROUP_PIPELINE");
+    return !(e && e[0] == '0');
+  }();
+  size_t budget = (size_t)(pipeline ? 16 : 24) << 30;
   if (const char *e = getenv("YAEL_GPU_GROUP_BYTES")) {
     const double v = atof(e);
     if (v > 0) budget = (size_t)v;
@@ -481,7 +520,48 @@ int knn_grouped(int npairs, const yael_gpu_knn_pair *pairs, int d, int k, int me
     waves.back().pairs.push_back(i);
     used += bytes;
   }
-  for (const Wave &w : waves) YG_CHECK(run_wave(pairs, w, d, k, metric, ctx, st, gc));
+  // Pipeline (YAEL_GPU_GROUP_PIPELINE=0 turns it off): wave i + 1 is packed on
+  // a side stream while wave i's passes run on st with a grid that leaves
+  // YAEL_GPU_GROUP_PACK_SMS (default 24) SMs to the packing, whose blocks do
+  // not fit beside a distance-pass CTA.  512-pair batch: 93.7 ms pipelined,
+  // 97.4 ms one wave after the other (8 to 48 reserved SMs: 93.9-95.7 ms).
+  int pack_sms = 24;
+  if (const char *e = getenv("YAEL_GPU_GROUP_PACK_SMS")) pack_sms = std::max(0, atoi(e));
+  const int pass_ctas = std::max(1, ctx->num_sms - pack_sms);
+  cudaStream_t sp = nullptr;
+  YG_CUDA(cudaStreamCreateWithFlags(&sp, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } guard{sp};
+  cudaEvent_t packed[2];
+  YG_CUDA(cudaEventCreateWithFlags(&packed[0], cudaEventDisableTiming));
+  YG_CUDA(cudaEventCreateWithFlags(&packed[1], cudaEventDisableTiming));
+  struct EventGuard {
+    cudaEvent_t *e;
+    ~EventGuard() { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+  } eguard{packed};
+  const int nw = (int)waves.size();
+  WaveState S[2];
+  // the first wave packs alone: full-size blocks
+  YG_CHECK(wave_prepare(pairs, waves[0], d, k, metric, ctx, 0, sp, S[0]));
+  YG_CUDA(cudaEventRecord(packed[0], sp));
+  for (int i = 0; i < nw; i++) {
+    const int cur = i & 1, nxt = cur ^ 1;
+    YG_CUDA(cudaStreamWaitEvent(st, packed[cur], 0));
+    YG_CHECK(wave_execute(S[cur], d, k, metric, pipeline && i + 1 < nw ? pass_ctas : 0, st));
+    if (pipeline && i + 1 < nw) {
+      // set nxt was last used by wave i - 1, finished before this iteration
+      YG_CHECK(wave_prepare(pairs, waves[i + 1], d, k, metric, ctx, nxt, sp, S[nxt]));
+      YG_CUDA(cudaEventRecord(packed[nxt], sp));
+    }
+    YG_CHECK(wave_finish(S[cur], d, k, metric, ctx, cur, st, gc));
+    if (!pipeline && i + 1 < nw) {
+      YG_CHECK(wave_prepare(pairs, waves[i + 1], d, k, metric, ctx, nxt, sp, S[nxt]));
+      YG_CUDA(cudaEventRecord(packed[nxt], sp));
+    }
+  }
+  YG_CUDA(cudaStreamSynchronize(sp));
   return OK;
 }
 

@@ -142,11 +142,12 @@ __global__ void __launch_bounds__(PW * 32)
   constexpr int RPW = 32 / LPR;  // rows per warp step
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int sub = lane / LPR, sl = lane % LPR;
-  const long nwarps = (long)gridDim.x * PW;
+  const int wpb = (int)(blockDim.x >> 5);  // warps per block (<= PW)
+  const long nwarps = (long)gridDim.x * wpb;
   float w_maxnorm = 0.f, w_maxres = 0.f;
   int w_exact = 1, w_nan = 0;
   const int cols = packed ? (Kp > d ? Kp : d) : d;
-  for (long rbase = ((long)blockIdx.x * PW + wid) * RPW; rbase < n; rbase += nwarps * RPW) {
+  for (long rbase = ((long)blockIdx.x * wpb + wid) * RPW; rbase < n; rbase += nwarps * RPW) {
     const long row = rbase + sub;
     const bool rv = row < n;
     const float *xr = x + row * ld;
@@ -263,7 +264,7 @@ __global__ void __launch_bounds__(PW * 32)
   if (threadIdx.x == 0) {
     float mn = 0.f, mr = 0.f;
     int ex = 1, nn = 0;
-    for (int w = 0; w < PW; w++) {
+    for (int w = 0; w < wpb; w++) {
       mn = fmaxf(mn, s_norm[w]);
       mr = fmaxf(mr, s_res[w]);
       ex &= s_exact[w];
@@ -391,7 +392,7 @@ int stats_reset(SetStats *stats, cudaStream_t st) {
 int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64,
               float *norm32, unsigned char *flags, float *resid,
               __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
-              int normpart_mode, SetStats *stats, cudaStream_t st) {
+              int normpart_mode, SetStats *stats, cudaStream_t st, int warps) {
   if (n <= 0) return OK;
   static int sms = 0;
   if (!sms) {
@@ -407,9 +408,10 @@ int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64
                    ((reinterpret_cast<uintptr_t>(x) & 15) == 0) && (!packed || Kp % 4 == 0) &&
                    (!normpart || (reinterpret_cast<uintptr_t>(normpart) & 15) == 0);
   if (vec && cols <= 128) {
-    long blocks = ceil_div(n, PW * 4);
-    if (blocks > cap) blocks = cap;
-    prep_rows_vec_kernel<8><<<(unsigned)blocks, PW * 32, 0, st>>>(
+    const int wpb = warps >= 1 && warps <= PW ? warps : PW;
+    long blocks = ceil_div(n, wpb * 4);
+    if (blocks > cap * PW / wpb) blocks = cap * PW / wpb;
+    prep_rows_vec_kernel<8><<<(unsigned)blocks, wpb * 32, 0, st>>>(
         x, ld, n, d, scale, norm64, norm32, flags, resid, packed, Kp, normpart, normpart_mode,
         stats);
   } else {

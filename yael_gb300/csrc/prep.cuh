@@ -32,10 +32,12 @@ constexpr double kExactNorm2Max = 4194304.0;  // 2^22
 //   normpart[i] = when base_parts: bf16 parts (hi, mid, lo) of (float)norm64 in
 //                 columns 0..2, zero in 3..15; when query_ones: 1,1,1,0...
 // and folds max norm / max residual / all-exact / NaN counts into *stats.
+// warps: warps per block of the row-vector form (1..8): small blocks fit on an
+// SM beside a running distance pass, so packing can overlap one
 int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64,
               float *norm32, unsigned char *flags, float *resid,
               __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
-              int normpart_mode, SetStats *stats, cudaStream_t st);
+              int normpart_mode, SetStats *stats, cudaStream_t st, int warps = 8);
 
 // Split ("3xBF16") packing: x = hi + lo + r with hi = bf16(x), lo = bf16(x - hi),
 // written as three K segments of Kp1 = 64*ceil(d/64) columns each:

@@ -78,6 +78,7 @@ struct ScanSel {
   const GroupUnit *units = nullptr;
   int nunits = 0;
   const GroupPair *gpairs = nullptr;
+  int max_ctas = 0;         // persistent passes: grid limit (0 = one CTA per SM)
   __host__ __device__ int nregion() const { return nchunk * halves; }
 };
 

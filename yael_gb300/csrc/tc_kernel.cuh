@@ -704,6 +704,7 @@ int launch(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_
       set_error(E_UNSUPPORTED, "tc_scan: %ld work units", nunits);
       return E_UNSUPPORTED;
     }
+    if (sel.max_ctas > 0 && sel.max_ctas < nsm) nsm = sel.max_ctas;
     const unsigned g = (unsigned)(nunits < nsm ? nunits : nsm);
     tc_scan_kernel<MODE, C, L2, QS, PAIR><<<g, NT_TC, lay.total, st>>>(mq, mqn, mb, mbn, nq, nb,
                                                                         nkb, S, sel, op.err);
