@@ -229,7 +229,9 @@ typedef struct {
 /* knn_full over npairs independent pairs of uneven sizes, all with the same d,
  * k, metric and precision (opts may be NULL: L2, YAEL_GPU_PRECISION).  No
  * counterpart in the reference, whose callers loop over knn_full (per-cell
- * searches, hkm / kmlsh children); results are those of that loop.  Pairs run
+ * searches, hkm / kmlsh children); results are those of that loop.  With
+ * device arrays, the BF16 pass and k >= 9 every pass is one persistent launch
+ * over all the pairs (YAEL_GPU_BATCH_GROUPED=0: off); otherwise pairs run
  * concurrently, largest first, on a persistent pool of host workers each with
  * its own stream and workspace (YAEL_GPU_BATCH_WORKERS, default 8).  With
  * opts->device_ptrs every array is device memory and opts->stream (a
