@@ -422,6 +422,9 @@ def run_knn_batch(args, world, rank, local):
                                      "ms_per_step": 1e3 * sec32},
         "exact_ids_vs_fp64_oracle_spot": check,
         "fallback_queries": o.n_fallback, "band_queries": o.n_band,
+        "path": ("grouped: one persistent launch per pass over all pairs, waves pipelined"
+                 if os.environ.get("YAEL_GPU_BATCH_GROUPED", "1") != "0"
+                 else "worker pool, one pipeline per pair"),
         "roofline": {"bound": "tensor", "kernel": "whole batch (all passes)",
                      "achieved": flops / sec / 1e12, "unit": "TFLOP/s", "peak": pk[0],
                      "frac": flops / sec / 1e12 / pk[0], "peak_source": pk[2],
@@ -429,7 +432,8 @@ def run_knn_batch(args, world, rank, local):
         "e2e": {"value": float(np.sum(nq[:ne])) / sec_e2e, "unit": "queries/s",
                 "h2d_bytes_per_step": int(4 * d * (np.sum(nq[:ne]) + np.sum(nb[:ne]))),
                 "d2h_bytes_per_step": int(8 * k * np.sum(nq[:ne])),
-                "api": f"yael_gpu_knn_batch with pinned host buffers, first {ne} pairs"},
+                "api": f"yael_gpu_knn_batch with pinned host buffers, first {ne} pairs "
+                       "(host arrays: the worker pool)"},
         "gpu_launches": launches, "clocks": clocks,
     }
     if cpu:
