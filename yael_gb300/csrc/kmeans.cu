@@ -305,6 +305,22 @@ struct Engine {
   // assignment on the 3xBF16 split operands; later iterations see similar
   // centroid geometry, so the switch is kept for the rest of the run.
   bool split_assign = false;
+  // The k-NN assignment defers its certificate check to the end of the
+  // iteration (the update is queued right behind it); rejected points are
+  // settled then and the update is run again.  Only after an iteration that
+  // rejected under 1% of the points: a pass that rejects many (BF16 on close
+  // centroids) does better with the in-line band passes.
+  KnnJob pend;
+  long last_rejected = -1;  // rejected points of the previous assignment
+
+  void count_assign(const KnnJob &job) {
+    last_rejected = (long)job.n_band + job.n_fallback;
+    n_fallback += job.n_fallback;
+    n_second += job.n_second;
+    n_band += job.n_band;
+    if (job.prec == PREC_BF16 && 4L * (job.n_band + job.n_fallback) > (long)job.nq)
+      split_assign = true;
+  }
 
   int assign_step() {
     if (in.size() == 1 && k > kSmallK) {
@@ -313,12 +329,10 @@ struct Engine {
       job.prec = (prec == PREC_BF16 && split_assign) ? PREC_BF16X3 : prec;
       job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
       job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
+      job.defer = last_rejected >= 0 && 100 * last_rejected < (long)job.nq;
       YG_CHECK(knn_device(job, ctx, st));
-      n_fallback += job.n_fallback;
-      n_second += job.n_second;
-      n_band += job.n_band;
-      if (job.prec == PREC_BF16 && 4L * (job.n_band + job.n_fallback) > (long)job.nq)
-        split_assign = true;
+      if (job.pending) pend = job;
+      else count_assign(job);
       return OK;
     }
     return km_assign_small(work, nwork, v, d, C, k, active, assign, dis, st);
@@ -371,6 +385,19 @@ struct Engine {
     eager_done = true;
     cudaEventRecord(e2, st);
     YG_CUDA(cudaStreamSynchronize(st));
+    if (pend.pending) {
+      YG_CHECK(knn_resolve(pend, ctx, st));
+      count_assign(pend);
+      if (pend.n_band > 0) {  // some points were re-run: their clusters changed
+        if (use_graphs && !graphs_failed) {
+          YG_CUDA(cudaGraphLaunch(g_update, st));
+          count_launches(g_update_n);
+        } else {
+          YG_CHECK(update_body());
+        }
+        YG_CUDA(cudaStreamSynchronize(st));
+      }
+    }
     std::copy(ph_counts, ph_counts + ncl, hcounts.begin());
     std::copy(ph_part, ph_part + nsl, hpart.begin());
     float a = 0, b = 0;

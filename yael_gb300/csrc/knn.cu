@@ -438,6 +438,17 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   YG_CHECK(rerank(ra, st));
   tr.stop(st);
 
+  // ---- deferred check: the status goes to the pinned buffer, the caller
+  // synchronises later and calls knn_resolve
+  if (job.defer && job.level == 0 && !timed && scan_ticket < 0 && sample_ticket < 0 && !up) {
+    void *pin;
+    YG_CHECK(ctx_pinned_status(ctx, &pin));
+    YG_CUDA(cudaMemcpyAsync(pin, dsmall, sizeof(Small), cudaMemcpyDeviceToHost, st));
+    job.pending = 1;
+    job.fail_dev = fail_list;
+    return OK;
+  }
+
   // ---- later chances for the queries the certificate rejected
   Small hs;
   YG_CHECK(read_small(ctx, dsmall, st, &hs));
@@ -583,7 +594,12 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
     sub.n_fallback = sub.n_band = sub.n_second = 0;
     sub.ms_scan = sub.ms_sample = sub.ms_rerank = sub.ms_second = 0;
     sub.scan_launches = 0;
+    sub.defer = job.defer && qbatch >= nq;  // a single batch only
     YG_CHECK(knn_batch(sub, ctx, st, dsmall, bops, bexact));
+    if (sub.pending) {
+      job.pending = 1;
+      job.fail_dev = sub.fail_dev;
+    }
     job.n_fallback += sub.n_fallback;
     job.n_band += sub.n_band;
     job.n_second += sub.n_second;
@@ -691,6 +707,49 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   }
   bops.plain.err = bops.split.err = &dsmall->tc_err;
   YG_CHECK(knn_batches(job, ctx, st, dsmall, &bops, bexact));
+  return OK;
+}
+
+int knn_resolve(KnnJob &job, Ctx *ctx, cudaStream_t st) {
+  if (!job.pending) return OK;
+  job.pending = 0;
+  void *pin;
+  YG_CHECK(ctx_pinned_status(ctx, &pin));
+  Small hs;
+  memcpy(&hs, pin, sizeof(Small));
+  job.n_cand = (long long)hs.n_cand;
+  job.exact_class = hs.bs.all_exact;
+  if (hs.tc_err) {
+    set_error(E_TIMEOUT, "tensor-core pass gave up waiting (bounded wait expired)");
+    return E_TIMEOUT;
+  }
+  const int nf = hs.fail_cnt, d = job.d, k = job.k;
+  if (nf == 0) return OK;
+  Workspace &ws = ctx->ws;
+  int *map, *cidx;
+  float *cq, *cdis;
+  YG_CHECK(ws_get(ws, WS_DEF0 + 0, nf, &map));
+  YG_CHECK(ws_get(ws, WS_DEF0 + 1, (size_t)nf * d, &cq));
+  YG_CHECK(ws_get(ws, WS_DEF0 + 2, (size_t)nf * k, &cidx));
+  YG_CHECK(ws_get(ws, WS_DEF0 + 3, (size_t)nf * k, &cdis));
+  // the list is copied first: the pipeline below reuses its workspace slot
+  YG_CUDA(cudaMemcpyAsync(map, job.fail_dev, sizeof(int) * nf, cudaMemcpyDeviceToDevice, st));
+  gather_rows_kernel<<<(unsigned)ceil_div((long)nf * d, 256), 256, 0, st>>>(job.q, job.ldq, map, nf,
+                                                                          d, cq);
+  YG_LAUNCH_CHECK();
+  KnnJob sub;
+  sub.nq = nf; sub.nb = job.nb; sub.d = d; sub.k = k; sub.metric = job.metric;
+  sub.prec = job.prec;
+  sub.q = cq; sub.ldq = d; sub.b = job.b; sub.ldb = job.ldb; sub.w = job.w;
+  sub.out_idx = cidx; sub.out_dis = cdis;
+  YG_CHECK(knn_device(sub, ctx, st));
+  scatter_rows_kernel<<<(unsigned)ceil_div((long)nf * k, 256), 256, 0, st>>>(cidx, cdis, map, nf, k,
+                                                                           job.out_idx, job.out_dis);
+  YG_LAUNCH_CHECK();
+  YG_CUDA(cudaStreamSynchronize(st));
+  job.n_band += nf + sub.n_band;
+  job.n_second += sub.n_second;
+  job.n_fallback += sub.n_fallback;
   return OK;
 }
 

@@ -46,10 +46,23 @@ struct KnnJob {
   int n_second = 0;     // queries re-run through the 3xBF16 split pass
   long long n_cand = 0;
   int exact_class = 0;
+  // Deferred certificate check (the k-means assignment): with defer = 1 a call
+  // whose queries fit one batch (and that runs no autotuner trial) returns
+  // right after the re-rank with pending = 1, its status block on its way to
+  // the context's pinned buffer; knn_resolve() settles the rejected queries
+  // once the caller has synchronised the stream.
+  int defer = 0;
+  int pending = 0;
+  int *fail_dev = nullptr;  // device list of the rejected queries (pending)
 };
 
 // Runs the whole pipeline on stream st using the calling thread's workspace.
 int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st);
+
+// For a pending job (defer): reads its status (st must have been synchronised
+// since the call), runs the rejected queries through the whole pipeline and
+// writes their results; n_band counts them.  No-op when nothing is pending.
+int knn_resolve(KnnJob &job, Ctx *ctx, cudaStream_t st);
 
 // One k-NN call on the calling thread's context: host arrays (copied in and
 // out) or, with opts->device_ptrs, device arrays on opts->stream (NULL = the
@@ -79,6 +92,7 @@ enum WsSlot : int {
   // compacted queries of a later-chance pass, per nesting level
   WS_SC0 = 100,
   WS_SC_PER_LEVEL = 5,  // + 0 map, 1 rows, 2 ids, 3 distances, 4 k-th bounds
+  WS_DEF0 = 130,        // knn_resolve: + 0 map, 1 rows, 2 ids, 3 distances
 };
 
 }  // namespace yg
