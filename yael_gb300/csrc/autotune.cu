@@ -1,4 +1,5 @@
 // Online chunk-count tuner (autotune.cuh).
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -100,6 +101,47 @@ int tune_chunks(const TuneKey &key, int c0, int cmax, int slots, int *ticket) {
   return e.cand[0];  // every trial is running: the heuristic's choice
 }
 
+int tune_variant(const TuneKey &key, int n, bool trial_ok, int *ticket, bool *settled) {
+  *ticket = -1;
+  *settled = true;
+  n = n < 1 ? 1 : (n > 3 ? 3 : n);
+  if (!enabled() || n == 1) return 0;
+  std::lock_guard<std::mutex> g(g_m);
+  auto it = g_index.find(key);
+  if (!trial_ok) {
+    if (it == g_index.end() || g_entries[it->second].best < 0) {
+      *settled = false;
+      return 0;
+    }
+    const Entry &e = g_entries[it->second];
+    return e.cand[e.best];
+  }
+  *settled = false;
+  if (it == g_index.end()) {
+    Entry e;
+    for (int i = 0; i < n; i++) e.cand[e.n++] = i;
+    g_entries.push_back(e);
+    it = g_index.emplace(key, (int)g_entries.size() - 1).first;
+  }
+  Entry &e = g_entries[it->second];
+  if (e.best >= 0) {
+    *settled = true;
+    return e.cand[e.best];
+  }
+  if (!e.warm) {
+    e.warm = true;
+    return e.cand[0];
+  }
+  for (int i = 0; i < e.n; i++) {
+    if (e.ms[i] < 0.f) {
+      e.ms[i] = 0.f;
+      *ticket = it->second * 4 + i;
+      return e.cand[i];
+    }
+  }
+  return e.cand[0];
+}
+
 void tune_report(int ticket, float ms) {
   if (ticket < 0) return;
   std::lock_guard<std::mutex> g(g_m);
@@ -111,6 +153,15 @@ void tune_report(int ticket, float ms) {
     if (e.ms[i] < e.ms[b]) b = i;
   }
   e.best = b;
+  if (trace_enabled()) {
+    for (const auto &kv : g_index) {
+      if (kv.second != ticket / 4) continue;
+      fprintf(stderr, "[yael_gpu] autotune kind=%d key=(%d,%d,%d): candidate %d (", kv.first.kind,
+              kv.first.nqt, kv.first.ntb, kv.first.C, e.cand[b]);
+      for (int i = 0; i < e.n; i++) fprintf(stderr, "%s%d: %.3f ms", i ? ", " : "", e.cand[i], e.ms[i]);
+      fprintf(stderr, ")\n");
+    }
+  }
 }
 
 }  // namespace yg

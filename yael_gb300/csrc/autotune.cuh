@@ -14,7 +14,7 @@
 namespace yg {
 
 struct TuneKey {
-  int kind;   // pass: 0 TOPC main, 1 THRESH main, 2 threshold sample
+  int kind;   // pass: 0 TOPC main, 1 THRESH main, 2 threshold sample, 3 grouped assignment
   int prec;   // distance precision
   int nqt;    // query tiles
   int ntb;    // base tiles
@@ -26,6 +26,12 @@ struct TuneKey {
 // whose pass time must be reported with tune_report().
 int tune_chunks(const TuneKey &key, int c0, int cmax, int slots, int *ticket);
 void tune_report(int ticket, float ms);
+
+// The same scheme over n <= 3 kernel variants (index 0: the default): the
+// variant for this call; *ticket >= 0 marks a trial to report.  trial_ok =
+// false (a launch being captured into a CUDA graph) returns the best variant
+// found so far without taking part; *settled tells whether the choice is final.
+int tune_variant(const TuneKey &key, int n, bool trial_ok, int *ticket, bool *settled);
 
 // Per host thread: calls made while it is off use the heuristic (the batched
 // k-NN workers share the GPU, so their timings would not be comparable).

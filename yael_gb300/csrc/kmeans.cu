@@ -170,6 +170,7 @@ struct Engine {
   // replays.  YAEL_GPU_GRAPHS=0 runs every iteration eagerly.
   cudaGraphExec_t g_assign = nullptr, g_update = nullptr;
   bool eager_done = false;
+  bool assign_settled = false;  // the grouped assignment's variant is tuned
   long g_assign_n = 0, g_update_n = 0;  // kernels per replay
   bool graphs_failed = false;
   int *ph_counts = nullptr;     // pinned copies the update graph writes
@@ -362,12 +363,14 @@ struct Engine {
       return OK;
     };
     const bool use_graphs = graphs_wanted() && eager_done;
-    const bool graph_assign = use_graphs && assign_graph_wanted();
-    if (use_graphs && !g_update) {
-      if ((graph_assign && !capture([&] { return assign_step(); }, &g_assign, &g_assign_n)) ||
-          !capture(update_body, &g_update, &g_update_n))
-        graphs_failed = true;
-    }
+    // the assignment is captured once its kernel variant is tuned (the
+    // tuner's trials run eagerly)
+    const bool graph_assign = use_graphs && assign_graph_wanted() && assign_settled;
+    if (use_graphs && !g_update && !capture(update_body, &g_update, &g_update_n))
+      graphs_failed = true;
+    if (graph_assign && !g_assign && !graphs_failed &&
+        !capture([&] { return assign_step(); }, &g_assign, &g_assign_n))
+      graphs_failed = true;
     cudaEventRecord(e0, st);
     if (graph_assign && !graphs_failed) {
       YG_CUDA(cudaGraphLaunch(g_assign, st));
@@ -385,6 +388,7 @@ struct Engine {
     eager_done = true;
     cudaEventRecord(e2, st);
     YG_CUDA(cudaStreamSynchronize(st));
+    if (!g_assign) assign_settled = km_assign_tune_collect();
     if (pend.pending) {
       YG_CHECK(knn_resolve(pend, ctx, st));
       count_assign(pend);

@@ -25,6 +25,11 @@ int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const 
                     int k, const unsigned char *active, int *assign, float *dis,
                     cudaStream_t st);
 
+// After the caller's synchronisation: reports a timed trial of the grouped
+// assignment's variant tuner (autotune.cuh); true once the variant choice of
+// the last call is final, so that a CUDA graph may capture the assignment.
+bool km_assign_tune_collect();
+
 // counts[inst*k + assign[p]]++ over points of active instances
 int km_histogram(const int *assign, const int *pinst, long n, int k,
                  const unsigned char *active, int *counts, cudaStream_t st);

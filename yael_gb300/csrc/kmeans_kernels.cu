@@ -1,6 +1,7 @@
 // Device kernels of the k-means Lloyd step (see kmeans.cuh).
 #include <math.h>
 
+#include "autotune.cuh"
 #include "kmeans.cuh"
 
 namespace yg {
@@ -589,6 +590,14 @@ int launch_assign(const KmWork *work, int nwork, const float *v, int d, const fl
   return OK;
 }
 
+// The variant of the grouped assignment is tuned per shape (autotune.cuh):
+// 0 the GEMM form with whole rows staged (d <= kFullD), 1 the GEMM form over
+// 32-coordinate slices, 2 one point per thread.  A trial is timed with events
+// around its launch and reported after the caller's next synchronisation.
+thread_local int t_trial = -1;
+thread_local cudaEvent_t t_trial_ev[2] = {nullptr, nullptr};
+thread_local bool t_settled = true;
+
 template <int K>
 int launch_assign_any(const KmWork *work, int nwork, const float *v, int d, const float *C,
                       int k, const unsigned char *active, int *assign, float *dis,
@@ -596,23 +605,48 @@ int launch_assign_any(const KmWork *work, int nwork, const float *v, int d, cons
   // float4 rows need d % 4 == 0 and 16-byte aligned points and centroids
   const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(v) & 15) == 0) &&
                    ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
-  if (vec && (size_t)d * K * 4 <= 120 * 1024) {
-    if (d <= kFullD) {
+  const bool gemm = vec && (size_t)d * K * 4 <= 120 * 1024;
+  int var[3], nv = 0;
+  if (gemm && d <= kFullD) var[nv++] = 0;
+  if (gemm) var[nv++] = 1;
+  var[nv++] = 2;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  YG_CUDA(cudaStreamIsCapturing(st, &cs));
+  int ticket = -1;
+  const int pick = tune_variant(TuneKey{3, 0, d, K, vec ? 1 : 0}, nv,
+                                cs == cudaStreamCaptureStatusNone && t_trial < 0, &ticket,
+                                &t_settled);
+  if (ticket >= 0) {
+    for (auto &e : t_trial_ev)
+      if (!e) YG_CUDA(cudaEventCreate(&e));
+    YG_CUDA(cudaEventRecord(t_trial_ev[0], st));
+  }
+  switch (var[pick < nv ? pick : 0]) {
+    case 0: {
       const size_t smem = ((size_t)d * K + K + (size_t)d * 132) * sizeof(float);
       YG_CHECK(ensure_smem((const void *)assign_gemm_kernel<K, true>, smem));
       assign_gemm_kernel<K, true><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign,
                                                             dis);
-    } else {
+      YG_LAUNCH_CHECK();
+      break;
+    }
+    case 1: {
       const size_t smem = ((size_t)d * K + K + 32 * 132) * sizeof(float);
       YG_CHECK(ensure_smem((const void *)assign_gemm_kernel<K, false>, smem));
       assign_gemm_kernel<K, false><<<nwork, 256, smem, st>>>(work, v, d, C, k, active, assign,
                                                              dis);
+      YG_LAUNCH_CHECK();
+      break;
     }
-    YG_LAUNCH_CHECK();
-    return OK;
+    default:
+      if (vec) YG_CHECK((launch_assign<K, true>(work, nwork, v, d, C, k, active, assign, dis, st)));
+      else YG_CHECK((launch_assign<K, false>(work, nwork, v, d, C, k, active, assign, dis, st)));
   }
-  if (vec) return launch_assign<K, true>(work, nwork, v, d, C, k, active, assign, dis, st);
-  return launch_assign<K, false>(work, nwork, v, d, C, k, active, assign, dis, st);
+  if (ticket >= 0) {
+    YG_CUDA(cudaEventRecord(t_trial_ev[1], st));
+    t_trial = ticket;
+  }
+  return OK;
 }
 
 }  // namespace
@@ -631,6 +665,18 @@ int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const 
   if (k <= 64) return launch_assign_any<64>(work, nwork, v, d, C, k, active, assign, dis, st);
   set_error(E_ARG, "grouped assignment: k=%d > %d", k, kSmallK);
   return E_ARG;
+}
+
+bool km_assign_tune_collect() {
+  if (t_trial < 0) return t_settled;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, t_trial_ev[0], t_trial_ev[1]) != cudaSuccess) {
+    (void)cudaGetLastError();
+    ms = 0.f;
+  }
+  tune_report(t_trial, ms);
+  t_trial = -1;
+  return false;  // the next call may still be a trial
 }
 
 int km_histogram(const int *assign, const int *pinst, long n, int k,
