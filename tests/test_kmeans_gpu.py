@@ -42,7 +42,8 @@ def gpu_kmeans(v, k, niter, flags, seed, redo, prec, C0=None):
     q = yg.lib().yael_gpu_kmeans_ex(d, n, k, niter, ptr(v), flags, seed, redo, ptr(C), ptr(dis),
                                     ptr(assign), ptr(nassign), ctypes.byref(o))
     assert o.status == 0, yg.last_error()
-    return dict(C=C, dis=dis, assign=assign, nassign=nassign, qerr=q, iters=o.iterations)
+    return dict(C=C, dis=dis, assign=assign, nassign=nassign, qerr=q, iters=o.iterations,
+                n_band=o.n_band)
 
 
 def same(g, o, rtol=2e-6):
@@ -64,6 +65,51 @@ def test_kmeans_small_k(prec):
 def test_kmeans_large_k_knn_path(prec):
     v, _, _ = synth.gaussian_mixture(20000, 32, 128, 0.15, seed=5)
     same(gpu_kmeans(v, 100, 10, QUIET, 777, 1, prec), oracle_kmeans(v, 100, 10, QUIET, 777, 1))
+
+
+def duplicate_heavy(seed):
+    """40% of the points are one vector: random init picks ~40 identical
+    centroids, so the 8-entry candidate lists of those points tie and the
+    certificate rejects them (band passes settle them)."""
+    v, _, _ = synth.gaussian_mixture(20000, 32, 50, 0.2, seed=seed)
+    v[::5] = v[1]
+    v[1::5] = v[1]
+    return v
+
+
+def test_kmeans_deferred_check_rejections():
+    """The k-NN assignment with its certificate check deferred to the end of
+    the iteration (YAEL_GPU_KMEANS_DEFER=1, read once per process: child
+    process): rejected points are re-run and the update repeated; results
+    bit-identical to the oracle."""
+    import subprocess
+    import sys
+    import tempfile
+    v = duplicate_heavy(31)
+    with tempfile.TemporaryDirectory() as tmp:
+        np.save(os.path.join(tmp, "v.npy"), v)
+        code = (
+            "import sys, numpy as np; sys.path.insert(0, 'tests');"
+            "import test_kmeans_gpu as T;"
+            f"v = np.load('{tmp}/v.npy');"
+            "r = T.gpu_kmeans(v, 100, 8, T.QUIET, 5, 1, 'bf16');"
+            f"np.savez('{tmp}/r.npz', **r); print('ran')")
+        env = dict(os.environ, YAEL_GPU_KMEANS_DEFER="1")
+        root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        p = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                           text=True, timeout=300)
+        assert p.returncode == 0 and "ran" in p.stdout, p.stdout + p.stderr
+        g = dict(np.load(os.path.join(tmp, "r.npz")))
+    assert g["n_band"] > 0  # rejected points went through the re-run
+    same(g, oracle_kmeans(v, 100, 8, QUIET, 5, 1))
+
+
+def test_kmeans_inline_check_rejections():
+    """The same data with the check in line (first iteration: adaptive mode)."""
+    v = duplicate_heavy(31)
+    g = gpu_kmeans(v, 100, 8, QUIET, 5, 1, "bf16")
+    assert g["n_band"] > 0
+    same(g, oracle_kmeans(v, 100, 8, QUIET, 5, 1))
 
 
 def test_kmeans_empty_cluster_splits():

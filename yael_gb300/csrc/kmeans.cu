@@ -32,7 +32,7 @@ int ws_get(Workspace &ws, int slot, size_t count, T **p) {
 enum KmSlot : int {
   KS_V = WS_KM0, KS_C, KS_ASSIGN, KS_DIS, KS_COUNTS, KS_OFFS, KS_CURSOR, KS_PERM, KS_ACC,
   KS_SHIFT, KS_ACTIVE, KS_PINST, KS_WORK, KS_SLICES, KS_PART, KS_ROWS, KS_AMAX,
-  KS_BEST_C, KS_BEST_DIS, KS_BEST_ASSIGN, KS_NODE, KS_VSORT, KS_TMP,
+  KS_BEST_C, KS_BEST_DIS, KS_BEST_ASSIGN, KS_NODE, KS_VSORT, KS_TMP, KS_CPREV,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -330,10 +330,26 @@ struct Engine {
       job.prec = (prec == PREC_BF16 && split_assign) ? PREC_BF16X3 : prec;
       job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
       job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
-      job.defer = last_rejected >= 0 && 100 * last_rejected < (long)job.nq;
+      // YAEL_GPU_KMEANS_DEFER=0 / 1: never / always defer (default: adaptive)
+      static const int defer_mode = [] {
+        const char *e = getenv("YAEL_GPU_KMEANS_DEFER");
+        return e && *e ? atoi(e) : -1;
+      }();
+      job.defer = defer_mode == 1 ||
+                  (defer_mode != 0 && last_rejected >= 0 && 100 * last_rejected < (long)job.nq);
       YG_CHECK(knn_device(job, ctx, st));
-      if (job.pending) pend = job;
-      else count_assign(job);
+      if (job.pending) {
+        // the update queued next overwrites C: the rejected points are settled
+        // against a copy of this iteration's centroids
+        float *cprev;
+        YG_CHECK(ws_get(ctx->ws, KS_CPREV, (size_t)k * d, &cprev));
+        YG_CUDA(cudaMemcpyAsync(cprev, C, sizeof(float) * (size_t)k * d, cudaMemcpyDeviceToDevice,
+                                st));
+        job.b = cprev;
+        pend = job;
+      } else {
+        count_assign(job);
+      }
       return OK;
     }
     return km_assign_small(work, nwork, v, d, C, k, active, assign, dis, st);

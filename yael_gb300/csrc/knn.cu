@@ -793,11 +793,16 @@ int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
           if (u->ready[i]) cudaEventDestroy(u->ready[i]);
       }
     } guard{&up, nullptr};
+    cudaEvent_t tl[3] = {nullptr, nullptr, nullptr};  // trace timeline (streamed upload)
     if (stream_up) {
       if (!ctx->copy_stream)
         YG_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
       cudaStream_t cs = ctx->copy_stream;
       guard.cs = cs;
+      if (trace_enabled()) {
+        YG_CUDA(cudaEventCreate(&tl[0]));
+        YG_CUDA(cudaEventRecord(tl[0], st));
+      }
       // the queries first: a copy issued after the base parts would wait for them
       YG_CUDA(cudaMemcpyAsync(dq, q, sizeof(float) * nq * (size_t)d, cudaMemcpyHostToDevice, st));
       cudaEvent_t qdone;
@@ -815,7 +820,8 @@ int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
         up.row0[i] = std::min<long>((long)nb, (long)(frac[i] * nb / 256) * 256);
       up.row0[parts] = nb;
       for (int i = 0; i < parts; i++) {
-        YG_CUDA(cudaEventCreateWithFlags(&up.ready[i], cudaEventDisableTiming));
+        YG_CUDA(cudaEventCreateWithFlags(&up.ready[i],
+                                         tl[0] ? cudaEventDefault : cudaEventDisableTiming));
         const long r0 = up.row0[i], n = up.row0[i + 1] - r0;
         YG_CUDA(cudaMemcpyAsync(db + r0 * d, b + r0 * d, sizeof(float) * n * (size_t)d,
                                 cudaMemcpyHostToDevice, cs));
@@ -832,9 +838,34 @@ int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
     }
     job.q = dq; job.b = db; job.w = dw; job.out_idx = didx; job.out_dis = ddis;
     YG_CHECK(knn_device(job, ctx, st));
+    if (tl[0]) {
+      YG_CUDA(cudaEventCreate(&tl[1]));
+      YG_CUDA(cudaEventRecord(tl[1], st));
+    }
     YG_CUDA(cudaMemcpyAsync(assign, didx, sizeof(int) * nq * (size_t)k, cudaMemcpyDeviceToHost, st));
     YG_CUDA(cudaMemcpyAsync(dis, ddis, sizeof(float) * nq * (size_t)k, cudaMemcpyDeviceToHost, st));
+    if (tl[0]) {
+      YG_CUDA(cudaEventCreate(&tl[2]));
+      YG_CUDA(cudaEventRecord(tl[2], st));
+    }
     YG_CUDA(cudaStreamSynchronize(st));
+    if (tl[0]) {
+      // trace: the host call's timeline (base parts landed, passes done, results back)
+      float t;
+      fprintf(stderr, "[yael_gpu] knn host call timeline (ms):");
+      for (int i = 0; i < up.nparts; i++) {
+        cudaEventElapsedTime(&t, tl[0], up.ready[i]);
+        fprintf(stderr, " part%d %.3f", i, t);
+      }
+      cudaEventElapsedTime(&t, tl[0], tl[1]);
+      fprintf(stderr, " | passes %.3f", t);
+      cudaEventElapsedTime(&t, tl[0], tl[2]);
+      fprintf(stderr, " | results %.3f\n", t);
+      for (auto &e : tl) {
+        cudaEventDestroy(e);
+        e = nullptr;
+      }
+    }
   }
   if (opts) {
     opts->n_fallback = job.n_fallback;
