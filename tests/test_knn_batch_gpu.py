@@ -149,3 +149,26 @@ def test_grouped_batch_rejections_rerun():
         ridx, rdis, _ = knn_exact(b, q, k, NT)
         np.testing.assert_array_equal(idx, ridx)
         np.testing.assert_allclose(dis, rdis, rtol=2e-6, atol=2e-6)
+
+
+@pytest.mark.parametrize("pipeline", ["1", "0"])
+def test_grouped_batch_many_waves(pipeline):
+    """A 3 MB wave budget splits the batch into many waves: the two buffer sets
+    alternate, and with the pipeline on each wave is packed on a side stream
+    while the previous wave's passes run (child process: the switches are
+    read once per process)."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, ctypes, numpy as np, torch; sys.path.insert(0, 'tests');"
+        "import test_knn_batch_gpu as T; from _util import knn_exact;"
+        "sizes = [(40, 9000), (3, 12000), (129, 20000), (1, 33), (77, 15000), (0, 50), (200, 10000)];"
+        "pairs = T.unit_pairs(41, sizes, 64);"
+        "out, o = T._device_batch(pairs, 16, 2, torch);"
+        "ok = all((idx == knn_exact(b, q, 16)[0]).all() for (q, b), (idx, _) in zip(pairs, out) if q.shape[0]);"
+        "print('waves ok' if ok else 'MISMATCH')")
+    env = dict(os.environ, YAEL_GPU_GROUP_BYTES="3e6", YAEL_GPU_GROUP_PIPELINE=pipeline)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0 and "waves ok" in r.stdout, r.stdout + r.stderr
