@@ -18,6 +18,8 @@
 #ifndef YAEL_GPU_H
 #define YAEL_GPU_H
 
+#include <stdio.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -176,6 +178,46 @@ hkm_t *hkm_read(const char *filename);
 
 /* yael/hkm.h:35 (yael/hkm.c:154-157) */
 float *hkm_get_centroids(const hkm_t *hkm, int l, int no);
+
+/* Vector files (host code, doc/file_format.rst): records of an int32
+ * dimension d followed by d floats (.fvecs), int32 (.ivecs) or uint8
+ * (.bvecs).  Same return values as the reference; where it asserts on a
+ * dimension / count mismatch (b2fvecs_read) these print and return -1.
+ * Arrays from the *_new_* readers are malloc'd. */
+/* yael/vector.h:190-212 (yael/vector.c:1369-1580; bvec_fwrite and
+ * bvecs_fwrite are defined at yael/vector.c:1540, 1559): 0 / count written */
+int fvec_fwrite(FILE *f, const float *v, int d);
+int ivec_fwrite(FILE *f, const int *v, int d);
+int bvec_fwrite(FILE *f, const unsigned char *v, int d);
+int fvecs_fwrite(FILE *f, int d, int n, const float *v);
+int ivecs_fwrite(FILE *f, int d, int n, const int *v);
+int bvecs_fwrite(FILE *f, int d, int n, const unsigned char *v);
+int fvecs_write(const char *fname, int d, int n, const float *v);
+int ivecs_write(const char *fname, int d, int n, const int *v);
+int bvecs_write(const char *fname, int d, int n, const unsigned char *v);
+/* yael/vector.h:183-185 (yael/vector.c:593-640): file bytes, *d_out, *n_out */
+long fvecs_fsize(const char *fname, int *d_out, int *n_out);
+long ivecs_fsize(const char *fname, int *d_out, int *n_out);
+long bvecs_fsize(const char *fname, int *d_out, int *n_out);
+/* yael/vector.h:217-248, 325-328 (yael/vector.c:651-720, 1121-1150,
+ * 1298-1320): number of vectors read, -1 on error */
+int fvecs_new_read(const char *fname, int *d_out, float **vf);
+int fvecs_new_fread_max(FILE *f, int *d_out, float **vf, long nmax);
+int ivecs_new_read(const char *fname, int *d_out, int **vi);
+int ivecs_new_fread_max(FILE *f, int *d_out, int **vi, long nmax);
+int bvecs_new_read(const char *fname, int *d_out, unsigned char **v_out);
+int b2fvecs_new_read(const char *fname, int *d_out, float **v_out);
+/* yael/vector.h:263-266 (yael/vector.c:882-935): the first n vectors */
+int fvecs_read(const char *fname, int d, int n, float *v);
+int b2fvecs_read(const char *fname, int d, int n, float *v);
+/* yael/vector.h:280-317 (yael/vector.c:966-1090): one record (its d, 0 at
+ * end of file, -1 on error); n records (the count, 0 on error) */
+int fvec_fread(FILE *f, float *v, int d_alloc);
+int ivec_fread(FILE *f, int *v, int d_alloc);
+int bvec_fread(FILE *f, unsigned char *v, int d_alloc);
+long fvecs_fread(FILE *f, float *v, long n, int d_alloc);
+long ivecs_fread(FILE *f, int *v, long n, int d_alloc);
+long bvecs_fread(FILE *f, unsigned char *v, long n, int d_alloc);
 
 /* ------------------------------------------------------------------ */
 /* extension API                                                       */

@@ -1,0 +1,85 @@
+"""yael_knn, the command-line program of yael's progs/knn.c: options and
+formats (CPU), and its results against the FP64 oracle (GPU)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from _util import knn_exact
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "yael_gb300", "bin", "yael_knn")
+
+
+@pytest.fixture(scope="module")
+def cli():
+    from yael_gb300 import build
+    build.build()
+    assert os.path.exists(CLI)
+    return CLI
+
+
+def write_vecs(path, a, dtype):
+    with open(path, "wb") as f:
+        for row in a:
+            f.write(np.int32(row.shape[0]).tobytes() + row.astype(dtype).tobytes())
+
+
+def read_vecs(path, dtype):
+    raw = open(path, "rb").read()
+    out, pos = [], 0
+    while pos < len(raw):
+        d = int(np.frombuffer(raw, np.int32, 1, pos)[0])
+        out.append(np.frombuffer(raw, dtype, d, pos + 4))
+        pos += 4 + d * np.dtype(dtype).itemsize
+    return np.stack(out)
+
+
+def test_usage_and_argument_errors(cli):
+    r = subprocess.run([cli, "-h"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "-onn idxfile" in r.stdout
+    r = subprocess.run([cli, "-k", "5"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "are needed" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fmt", ["fvec", "bvec", "text"])
+def test_knn_program_matches_oracle(cli, tmp_path, fmt):
+    rng = np.random.default_rng(17)
+    nb, nq, d, k = 3000, 40, 32, 10
+    if fmt == "bvec":
+        b = rng.integers(0, 256, (nb, d)).astype(np.float32)
+        q = rng.integers(0, 256, (nq, d)).astype(np.float32)
+    else:
+        b = rng.standard_normal((nb, d)).astype(np.float32)
+        q = rng.standard_normal((nq, d)).astype(np.float32)
+    args = [cli, "-k", str(k), "-silence"]
+    if fmt == "fvec":
+        write_vecs(tmp_path / "b.fvecs", b, np.float32)
+        write_vecs(tmp_path / "q.fvecs", q, np.float32)
+        args += ["-b", str(tmp_path / "b.fvecs"), "-q", str(tmp_path / "q.fvecs")]
+    elif fmt == "bvec":
+        write_vecs(tmp_path / "b.bvecs", b, np.uint8)
+        write_vecs(tmp_path / "q.bvecs", q, np.uint8)
+        args += ["-bb", str(tmp_path / "b.bvecs"), "-qb", str(tmp_path / "q.bvecs")]
+    else:
+        np.savetxt(tmp_path / "b.txt", b, fmt="%.9g")
+        np.savetxt(tmp_path / "q.txt", q, fmt="%.9g")
+        args += ["-bt", str(tmp_path / "b.txt"), "-qt", str(tmp_path / "q.txt"), "-nb", str(nb),
+                 "-nq", str(nq), "-d", str(d)]
+    if fmt == "text":
+        args += ["-onnt", str(tmp_path / "nn.txt"), "-odist", str(tmp_path / "dis.txt")]
+    else:
+        args += ["-onn", str(tmp_path / "nn.ivecs"), "-odis", str(tmp_path / "dis.fvecs")]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    if fmt == "text":
+        idx = np.loadtxt(tmp_path / "nn.txt", dtype=np.int64).reshape(nq, k)
+        dis = np.loadtxt(tmp_path / "dis.txt").reshape(nq, k)
+    else:
+        idx = read_vecs(tmp_path / "nn.ivecs", np.int32)
+        dis = read_vecs(tmp_path / "dis.fvecs", np.float32)
+    ridx, rdis, _ = knn_exact(b, q, k)
+    np.testing.assert_array_equal(idx, ridx)
+    np.testing.assert_allclose(dis, rdis, rtol=1e-5, atol=1e-4)

@@ -1,0 +1,181 @@
+"""Vector file I/O (.fvecs / .ivecs / .bvecs): the record format, round trips,
+edge cases, and -- where the reference library compiled from its own sources
+is present -- byte-identical files and identical reads against it.  Host code
+only: no GPU."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import yael_gb300 as yg
+from _util import reference
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+L = ctypes.c_long
+libc = ctypes.CDLL(None)
+libc.fopen.restype = P
+libc.fopen.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+libc.fclose.argtypes = [P]
+libc.free.argtypes = [P]
+
+
+def ptr(a):
+    return a.ctypes.data_as(P)
+
+
+def records(path, dtype):
+    """numpy restatement of the record format: int32 d, then d elements."""
+    raw = open(path, "rb").read()
+    out, pos, item = [], 0, np.dtype(dtype).itemsize
+    while pos < len(raw):
+        d = int(np.frombuffer(raw, np.int32, 1, pos)[0])
+        out.append(np.frombuffer(raw, dtype, d, pos + 4))
+        pos += 4 + d * item
+    return out
+
+
+def ref_lib():
+    r = reference()
+    if r is None:
+        return None
+    for name, (res, args) in yg.SIGNATURES.items():
+        if name.endswith(("vec_fwrite", "vecs_fwrite", "vecs_write", "vecs_fsize", "vecs_new_read",
+                          "vecs_new_fread_max", "vecs_read", "vec_fread", "vecs_fread")) \
+                and hasattr(r, name):
+            getattr(r, name).restype = res
+            getattr(r, name).argtypes = args
+    return r
+
+
+@pytest.fixture(scope="module")
+def data():
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal((37, 24)).astype(np.float32)
+    i = rng.integers(-1000, 1000, (37, 24)).astype(np.int32)
+    b = rng.integers(0, 256, (37, 24)).astype(np.uint8)
+    return f, i, b
+
+
+def test_writers_follow_the_record_format(tmp_path, data):
+    f, i, b = data
+    L_ = yg.lib()
+    for name, arr, dt, w in (("a.fvecs", f, np.float32, L_.fvecs_write),
+                             ("a.ivecs", i, np.int32, L_.ivecs_write),
+                             ("a.bvecs", b, np.uint8, L_.bvecs_write)):
+        path = str(tmp_path / name)
+        assert w(path.encode(), arr.shape[1], arr.shape[0], ptr(arr)) == arr.shape[0]
+        recs = records(path, dt)
+        assert len(recs) == arr.shape[0]
+        np.testing.assert_array_equal(np.stack(recs), arr)
+
+
+def test_readers_round_trip(tmp_path, data):
+    f, i, b = data
+    L_ = yg.lib()
+    fp, ip, bp = (str(tmp_path / n).encode() for n in ("r.fvecs", "r.ivecs", "r.bvecs"))
+    L_.fvecs_write(fp, 24, 37, ptr(f))
+    L_.ivecs_write(ip, 24, 37, ptr(i))
+    L_.bvecs_write(bp, 24, 37, ptr(b))
+    d, n = I(), I()
+    assert L_.fvecs_fsize(fp, ctypes.byref(d), ctypes.byref(n)) == 37 * (4 + 24 * 4)
+    assert (d.value, n.value) == (24, 37)
+    assert L_.bvecs_fsize(bp, ctypes.byref(d), ctypes.byref(n)) == 37 * (4 + 24)
+    for fn, dt, arr, path in ((L_.fvecs_new_read, np.float32, f, fp),
+                              (L_.ivecs_new_read, np.int32, i, ip),
+                              (L_.bvecs_new_read, np.uint8, b, bp),
+                              (L_.b2fvecs_new_read, np.float32, b.astype(np.float32), bp)):
+        out = P()
+        cnt = fn(path, ctypes.byref(d), ctypes.byref(out))
+        assert (cnt, d.value) == (37, 24)
+        got = np.ctypeslib.as_array(ctypes.cast(out, ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                    shape=(37 * 24,)).reshape(37, 24).copy()
+        libc.free(out)
+        np.testing.assert_array_equal(got, arr)
+    # the first n records; asking for more than the file holds reads what is there
+    buf = np.zeros((40, 24), np.float32)
+    assert L_.fvecs_read(fp, 24, 10, ptr(buf)) == 10
+    np.testing.assert_array_equal(buf[:10], f[:10])
+    assert L_.fvecs_read(fp, 24, 40, ptr(buf)) == 37
+    assert L_.fvecs_read(fp, 23, 5, ptr(buf)) == -1  # wrong dimension
+    assert L_.b2fvecs_read(bp, 24, 5, ptr(buf)) == 5
+    np.testing.assert_array_equal(buf[:5], b[:5].astype(np.float32))
+    # streams: at most nmax records, then one record at a time
+    fh = libc.fopen(fp, b"r")
+    out = P()
+    assert L_.fvecs_new_fread_max(fh, ctypes.byref(d), ctypes.byref(out), 5) == 5
+    got = np.ctypeslib.as_array(ctypes.cast(out, ctypes.POINTER(ctypes.c_float)), shape=(5 * 24,))
+    np.testing.assert_array_equal(got.reshape(5, 24), f[:5])
+    libc.free(out)
+    row = np.zeros(24, np.float32)
+    assert L_.fvec_fread(fh, ptr(row), 24) == 24
+    np.testing.assert_array_equal(row, f[5])
+    rest = np.zeros((40, 24), np.float32)
+    assert L_.fvecs_fread(fh, ptr(rest), 40, 24) == 31
+    np.testing.assert_array_equal(rest[:31], f[6:])
+    assert L_.fvec_fread(fh, ptr(row), 24) == 0  # end of file
+    libc.fclose(fh)
+
+
+def test_edge_cases(tmp_path):
+    L_ = yg.lib()
+    d, n, out = I(), I(), P()
+    empty = str(tmp_path / "e.fvecs").encode()
+    open(empty, "wb").close()
+    assert L_.fvecs_fsize(empty, ctypes.byref(d), ctypes.byref(n)) == 0 and n.value == 0
+    assert L_.fvecs_new_read(empty, ctypes.byref(d), ctypes.byref(out)) == 0
+    assert d.value == -1
+    missing = str(tmp_path / "none.fvecs").encode()
+    assert L_.fvecs_new_read(missing, ctypes.byref(d), ctypes.byref(out)) == -1
+    assert L_.fvecs_fsize(missing, ctypes.byref(d), ctypes.byref(n)) == -1
+    # records of different dimensions
+    mixed = str(tmp_path / "m.fvecs").encode()
+    with open(mixed, "wb") as fh:
+        fh.write(np.int32(3).tobytes() + np.ones(3, np.float32).tobytes())
+        fh.write(np.int32(2).tobytes() + np.ones(2, np.float32).tobytes())
+    assert L_.fvecs_new_read(mixed, ctypes.byref(d), ctypes.byref(out)) == -1
+    assert L_.fvecs_fsize(mixed, ctypes.byref(d), ctypes.byref(n)) == -1  # 20 bytes, records of 16
+    # truncated last record
+    trunc = str(tmp_path / "t.fvecs").encode()
+    with open(trunc, "wb") as fh:
+        fh.write(np.int32(4).tobytes() + np.ones(4, np.float32).tobytes())
+        fh.write(np.int32(4).tobytes() + np.ones(2, np.float32).tobytes())
+    assert L_.fvecs_new_read(trunc, ctypes.byref(d), ctypes.byref(out)) == -1
+    # zero vectors written
+    z = str(tmp_path / "z.ivecs").encode()
+    assert L_.ivecs_write(z, 5, 0, None) == 0 and os.path.getsize(z) == 0
+
+
+def test_against_the_reference(tmp_path, data):
+    """Same bytes written and same values read as the reference library."""
+    R = ref_lib()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    f, i, b = data
+    L_ = yg.lib()
+    for ext, arr, ours, theirs in (("fvecs", f, L_.fvecs_write, R.fvecs_write),
+                                   ("ivecs", i, L_.ivecs_write, R.ivecs_write),
+                                   ("bvecs", b, L_.bvecs_write, R.bvecs_write)):
+        p1, p2 = (str(tmp_path / f"{w}.{ext}").encode() for w in ("ours", "ref"))
+        assert ours(p1, 24, 37, ptr(arr)) == theirs(p2, 24, 37, ptr(arr)) == 37
+        assert open(p1, "rb").read() == open(p2, "rb").read()
+    d1, d2, o1, o2 = I(), I(), P(), P()
+    for name in ("fvecs_new_read", "ivecs_new_read", "bvecs_new_read", "b2fvecs_new_read"):
+        ext = "bvecs" if name.startswith(("bvecs", "b2f")) else name[:5]
+        path = str(tmp_path / f"ref.{ext}").encode()
+        n1 = getattr(L_, name)(path, ctypes.byref(d1), ctypes.byref(o1))
+        n2 = getattr(R, name)(path, ctypes.byref(d2), ctypes.byref(o2))
+        assert (n1, d1.value) == (n2, d2.value) == (37, 24)
+        nbytes = 37 * 24 * (1 if name == "bvecs_new_read" else 4)
+        assert ctypes.string_at(o1, nbytes) == ctypes.string_at(o2, nbytes)
+        libc.free(o1)
+        libc.free(o2)
+    path = str(tmp_path / "ref.fvecs").encode()
+    for nread in (5, 37, 50):
+        a1, a2 = np.zeros((50, 24), np.float32), np.zeros((50, 24), np.float32)
+        assert L_.fvecs_read(path, 24, nread, ptr(a1)) == R.fvecs_read(path, 24, nread, ptr(a2))
+        np.testing.assert_array_equal(a1, a2)
+    s1, s2 = (I(), I()), (I(), I())
+    assert L_.fvecs_fsize(path, *map(ctypes.byref, s1)) == R.fvecs_fsize(path, *map(ctypes.byref, s2))
+    assert [x.value for x in s1] == [x.value for x in s2]

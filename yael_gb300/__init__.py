@@ -93,6 +93,32 @@ SIGNATURES = {
     "hkm_quantize": (None, [P, c_int, P, P]),
     "hkm_write": (None, [ctypes.c_char_p, P]),
     "hkm_read": (P, [ctypes.c_char_p]),
+    "fvec_fwrite": (c_int, [P, P, c_int]),
+    "ivec_fwrite": (c_int, [P, P, c_int]),
+    "bvec_fwrite": (c_int, [P, P, c_int]),
+    "fvecs_fwrite": (c_int, [P, c_int, c_int, P]),
+    "ivecs_fwrite": (c_int, [P, c_int, c_int, P]),
+    "bvecs_fwrite": (c_int, [P, c_int, c_int, P]),
+    "fvecs_write": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "ivecs_write": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "bvecs_write": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "fvecs_fsize": (ctypes.c_long, [ctypes.c_char_p, P, P]),
+    "ivecs_fsize": (ctypes.c_long, [ctypes.c_char_p, P, P]),
+    "bvecs_fsize": (ctypes.c_long, [ctypes.c_char_p, P, P]),
+    "fvecs_new_read": (c_int, [ctypes.c_char_p, P, P]),
+    "fvecs_new_fread_max": (c_int, [P, P, P, ctypes.c_long]),
+    "ivecs_new_read": (c_int, [ctypes.c_char_p, P, P]),
+    "ivecs_new_fread_max": (c_int, [P, P, P, ctypes.c_long]),
+    "bvecs_new_read": (c_int, [ctypes.c_char_p, P, P]),
+    "b2fvecs_new_read": (c_int, [ctypes.c_char_p, P, P]),
+    "fvecs_read": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "b2fvecs_read": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "fvec_fread": (c_int, [P, P, c_int]),
+    "ivec_fread": (c_int, [P, P, c_int]),
+    "bvec_fread": (c_int, [P, P, c_int]),
+    "fvecs_fread": (ctypes.c_long, [P, P, ctypes.c_long, c_int]),
+    "ivecs_fread": (ctypes.c_long, [P, P, ctypes.c_long, c_int]),
+    "bvecs_fread": (ctypes.c_long, [P, P, ctypes.c_long, c_int]),
     "hkm_get_centroids": (P, [P, c_int, c_int]),
     "yael_gpu_kmeans_ex": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P, ctypes.c_void_p]),
     "yael_gpu_hkm_learn_ex": (c_int, [c_int, c_int, c_int, c_int, P, c_int, c_int, P, P, P, P]),
