@@ -1,6 +1,7 @@
 """Multi-GPU runs of this path are replicas: one process per GPU, each with its
 own query set against the same base (the path has no exchange step on one
-node: a sharded search would merge per-shard top-k lists).
+node: a sharded search would merge per-shard top-k lists, whose ids the
+kernels already offset by the shard's first row).
 These helpers hold the host-side logic of such a run: per-rank inputs, the
 slowest rank's time, and the whole-job rate."""
 from __future__ import annotations
