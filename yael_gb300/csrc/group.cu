@@ -71,8 +71,7 @@ __global__ void qpair_kernel(int *qpair, int p, int q0, int n) {
 }
 
 // thresholds of the queries of pairs without a sample (every row a candidate)
-__global__ void thr_inf_kernel(const int *qpair, const GroupPair *gp, const unsigned char *inf,
-                               int nq, float *thr) {
+__global__ void thr_inf_kernel(const int *qpair, const unsigned char *inf, int nq, float *thr) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < nq && inf[qpair[q]]) thr[q] = INFINITY;
 }
@@ -354,8 +353,8 @@ int wave_execute(WaveState &S, int d, int k, int metric, int max_ctas, cudaStrea
     YG_CHECK(tc_scan(ops, S.nq_all, (int)(S.brows / S.stride), ss, st));
     YG_CHECK(thresh_from_sample(S.nq_all, 1, 16, kSampleC, S.stopv, S.eps, S.thr, st));
   }
-  thr_inf_kernel<<<(unsigned)ceil_div(S.nq_all, 256), 256, 0, st>>>(S.qpair, S.dpairs, S.dinf,
-                                                                    S.nq_all, S.thr);
+  thr_inf_kernel<<<(unsigned)ceil_div(S.nq_all, 256), 256, 0, st>>>(S.qpair, S.dinf, S.nq_all,
+                                                                    S.thr);
   YG_LAUNCH_CHECK();
   if (S.ev[2]) cudaEventRecord(S.ev[2], st);
   ScanSel sel;
