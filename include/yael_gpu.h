@@ -179,6 +179,23 @@ hkm_t *hkm_read(const char *filename);
 /* yael/hkm.h:35 (yael/hkm.c:154-157) */
 float *hkm_get_centroids(const hkm_t *hkm, int l, int no);
 
+/* Image descriptors on the exact nearest-centroid assignment
+ * (yael/vlad.h:17-76, yael/vlad.c:10-139): VLAD sums are the reference's own
+ * float additions in point (or list) order; bag-of-features counts exact.
+ * Points without a nearest centroid (all-NaN rows) are left out. */
+void vlad_compute(int k, int d, const float *centroids, int n, const float *v, float *desc);
+void vlad_compute_weighted(int k, int d, const float *centroids, int n, const float *v,
+                           const float *weights, float *desc);
+void vlad_compute_subsets(int k, int d, const float *centroids, int n, const float *v,
+                          int n_subset, const int *subset_indexes, const int *subset_ends,
+                          float *desc);
+void bof_compute(int k, int d, const float *centroids, int n, const float *v, int *desc);
+void bof_compute_ma(int k, int d, const float *centroids, int n, const float *v, int *desc,
+                    int ma, float alpha, int nt);
+void bof_compute_subsets(int k, int d, const float *centroids, int n, const float *v,
+                         int n_subset, const int *subset_indexes, const int *subset_ends,
+                         float *desc);
+
 /* Vector files (host code, doc/file_format.rst): records of an int32
  * dimension d followed by d floats (.fvecs), int32 (.ivecs) or uint8
  * (.bvecs).  Same return values as the reference; where it asserts on a

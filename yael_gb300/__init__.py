@@ -93,6 +93,12 @@ SIGNATURES = {
     "hkm_quantize": (None, [P, c_int, P, P]),
     "hkm_write": (None, [ctypes.c_char_p, P]),
     "hkm_read": (P, [ctypes.c_char_p]),
+    "vlad_compute": (None, [c_int, c_int, P, c_int, P, P]),
+    "vlad_compute_weighted": (None, [c_int, c_int, P, c_int, P, P, P]),
+    "vlad_compute_subsets": (None, [c_int, c_int, P, c_int, P, c_int, P, P, P]),
+    "bof_compute": (None, [c_int, c_int, P, c_int, P, P]),
+    "bof_compute_ma": (None, [c_int, c_int, P, c_int, P, P, c_int, c_float, c_int]),
+    "bof_compute_subsets": (None, [c_int, c_int, P, c_int, P, c_int, P, P, P]),
     "fvec_fwrite": (c_int, [P, P, c_int]),
     "ivec_fwrite": (c_int, [P, P, c_int]),
     "bvec_fwrite": (c_int, [P, P, c_int]),
