@@ -78,8 +78,12 @@ void compute_cross_distances_nonpacked(int d, int na, int nb, const float *a,
 void compute_cross_distances_thread(int d, int na, int nb, const float *a,
                                     const float *b, float *dist2, int nt);
 
-/* yael/nn.h:174-176 (yael/nn.c:352-356).  Types 2/12 (L2) and 16 (dot
- * product) run on the GPU; other types abort with a message. */
+/* yael/nn.h:174-176 (yael/nn.c:352-356).  Every type runs on the GPU: 12
+ * (expanded-form L2) and 16 (dot product) as GEMMs; 1 (L1), 2 (L2), 3 / 4
+ * (chi2 forms), 5 (histogram intersection), 6 (dot) as the reference's
+ * per-coordinate sums (float lanes for 1 / 3 when d % 4 == 0, else double
+ * sums of float terms), bit-identical to its x86 build; other types abort
+ * with a message. */
 void compute_cross_distances_alt(int distance_type, int d, int na, int nb,
                                  const float *a, const float *b, float *dist2);
 

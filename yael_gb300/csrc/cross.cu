@@ -3,6 +3,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "knn.cuh"
 #include "simt_tile.cuh"
 #include "../../include/yael_gpu.h"
@@ -271,6 +273,128 @@ static int recompute_host(int n, int nb, int d, int k, const float *b, const flo
   return OK;
 }
 
+// ---- the other distance types of compute_cross_distances_alt
+// (yael/nn.c:164-350), as the reference computes them on x86: L1 (type 1) and
+// chi2 (type 3) with d % 4 == 0 in four float lanes (SSE2 form: lane l sums
+// the coordinates c = l mod 4, the lanes are then added left to right), every
+// other case as a double sum over the coordinates in order of float terms,
+// rounded to float.  One thread per output (a_i, b_j); the coordinates are
+// walked in order through 32-wide slices staged in shared memory, so each
+// output is the reference's own sequence of operations.
+constexpr int AT = 16, AC = 32;  // pairs per block side, coordinates per slice
+
+template <int TYPE, bool SSE>
+__global__ void __launch_bounds__(AT * AT)
+    alt_kernel(const float *__restrict__ a, int lda, int na, const float *__restrict__ b, int ldb,
+               int nb, int d, float *out, int ldo) {
+  __shared__ float sa[AT][AC + 1], sb[AT][AC + 1];
+  const int ti = threadIdx.x % AT, tj = threadIdx.x / AT;
+  const int i = blockIdx.x * AT + ti, j = blockIdx.y * AT + tj;
+  double sum = 0.0;
+  float lane[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int c0 = 0; c0 < d; c0 += AC) {
+    const int w = min(AC, d - c0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < AT * AC; e += AT * AT) {
+      const int r = e / AC, c = e % AC;
+      const long ia = (long)blockIdx.x * AT + r, jb = (long)blockIdx.y * AT + r;
+      sa[r][c] = (c < w && ia < na) ? a[ia * lda + c0 + c] : 0.f;
+      sb[r][c] = (c < w && jb < nb) ? b[jb * ldb + c0 + c] : 0.f;
+    }
+    __syncthreads();
+    for (int c = 0; c < w; c++) {
+      const float av = sa[ti][c], bv = sb[tj][c];
+      if (SSE) {
+        float t;
+        if (TYPE == 1) {
+          t = fabsf(__fsub_rn(av, bv));
+        } else {  // chi2: (a - b)^2 / (a + b) where a != b, else 0
+          const float df = __fsub_rn(av, bv);
+          t = av != bv ? __fdiv_rn(__fmul_rn(df, df), __fadd_rn(av, bv)) : 0.f;
+        }
+        lane[(c0 + c) & 3] = __fadd_rn(lane[(c0 + c) & 3], t);
+      } else if (TYPE == 1) {
+        sum = __dadd_rn(sum, (double)fabsf(__fsub_rn(av, bv)));
+      } else if (TYPE == 2) {
+        const double df = (double)__fsub_rn(av, bv);
+        sum = __dadd_rn(sum, __dmul_rn(df, df));
+      } else if (TYPE == 3) {
+        const float s = __fadd_rn(av, bv);
+        if (s != 0.f) {
+          const double df = (double)__fsub_rn(av, bv);
+          sum = __dadd_rn(sum, __ddiv_rn(__dmul_rn(df, df), (double)s));
+        }
+      } else if (TYPE == 4) {
+        const float den = fabsf(__fadd_rn(av, bv));
+        if (den != 0.f) {
+          const double df = (double)__fsub_rn(av, bv);
+          sum = __dadd_rn(sum, __ddiv_rn(__dmul_rn(df, df), (double)den));
+        }
+      } else if (TYPE == 5) {
+        sum = __dadd_rn(sum, (double)(av < bv ? av : bv));
+      } else {  // 6
+        sum = __dadd_rn(sum, (double)__fmul_rn(av, bv));
+      }
+    }
+  }
+  if (i >= na || j >= nb) return;
+  out[(long)j * ldo + i] =
+      SSE ? __fadd_rn(__fadd_rn(__fadd_rn(lane[0], lane[1]), lane[2]), lane[3]) : (float)sum;
+}
+
+template <int TYPE, bool SSE>
+void alt_launch(const float *a, int na, const float *b, int nb, int d, float *out, int ldo,
+                cudaStream_t st) {
+  dim3 grid((unsigned)ceil_div(na, AT), (unsigned)ceil_div(nb, AT));
+  alt_kernel<TYPE, SSE><<<grid, AT * AT, 0, st>>>(a, d, na, b, d, nb, d, out, ldo);
+}
+
+// host arrays in, host matrix out (pitch ldd), chunked over b
+int alt_host(int type, int d, int na, int nb, const float *a, int lda, const float *b, int ldb,
+             float *dist2, int ldd) {
+  if (na <= 0 || nb <= 0) return OK;
+  if (d < 0 || lda < d || ldb < d || ldd < na) {
+    set_error(E_ARG, "cross distances: bad leading dimensions");
+    return E_ARG;
+  }
+  Ctx *ctx;
+  YG_CHECK(ctx_get(&ctx));
+  cudaStream_t st = ctx->stream;
+  Workspace &ws = ctx->ws;
+  float *da, *db, *dout;
+  YG_CHECK(ws_get(ws, WS_H_Q, (size_t)na * d + 1, &da));
+  YG_CHECK(ws_get(ws, WS_H_B, (size_t)nb * d + 1, &db));
+  if (d > 0) {
+    YG_CUDA(cudaMemcpy2DAsync(da, sizeof(float) * d, a, sizeof(float) * lda, sizeof(float) * d,
+                              na, cudaMemcpyHostToDevice, st));
+    YG_CUDA(cudaMemcpy2DAsync(db, sizeof(float) * d, b, sizeof(float) * ldb, sizeof(float) * d,
+                              nb, cudaMemcpyHostToDevice, st));
+  }
+  const bool sse = (type == 1 || type == 3) && d % 4 == 0;
+  long jb = (long)(((size_t)1 << 30) / ((size_t)na * 4));
+  jb = std::max<long>(AT, jb / AT * AT);
+  YG_CHECK(ws_get(ws, WS_H_DIS, (size_t)na * (size_t)imin(nb, (int)std::min<long>(jb, nb)), &dout));
+  for (long j0 = 0; j0 < nb; j0 += jb) {
+    const int nbc = (int)std::min<long>(jb, nb - j0);
+    const float *bj = db + j0 * d;
+    switch (type * 2 + (sse ? 1 : 0)) {
+      case 2: alt_launch<1, false>(da, na, bj, nbc, d, dout, na, st); break;
+      case 3: alt_launch<1, true>(da, na, bj, nbc, d, dout, na, st); break;
+      case 4: alt_launch<2, false>(da, na, bj, nbc, d, dout, na, st); break;
+      case 6: alt_launch<3, false>(da, na, bj, nbc, d, dout, na, st); break;
+      case 7: alt_launch<3, true>(da, na, bj, nbc, d, dout, na, st); break;
+      case 8: alt_launch<4, false>(da, na, bj, nbc, d, dout, na, st); break;
+      case 10: alt_launch<5, false>(da, na, bj, nbc, d, dout, na, st); break;
+      default: alt_launch<6, false>(da, na, bj, nbc, d, dout, na, st); break;
+    }
+    YG_LAUNCH_CHECK();
+    YG_CUDA(cudaMemcpy2DAsync(dist2 + j0 * ldd, sizeof(float) * ldd, dout, sizeof(float) * na,
+                              sizeof(float) * na, nbc, cudaMemcpyDeviceToHost, st));
+  }
+  YG_CUDA(cudaStreamSynchronize(st));
+  return OK;
+}
+
 }  // namespace yg
 
 using namespace yg;
@@ -303,13 +427,19 @@ void compute_cross_distances_thread(int d, int na, int nb, const float *a, const
 void compute_cross_distances_alt_nonpacked(int distance_type, int d, int na, int nb,
                                            const float *a, int lda, const float *b, int ldb,
                                            float *dist2, int ldd) {
-  const int m = alt_metric(distance_type);
-  if (m < 0) {
-    set_error(E_UNSUPPORTED, "distance_type %d has no GPU implementation (supported: 2, 12, 16)",
-              distance_type);
+  // types 12 / 16: the expanded form and the plain product (yael/nn.c:321-328);
+  // 1-6: per-coordinate sums (yael/nn.c:311-350, SSE forms at 164-259)
+  if (distance_type == 12 || distance_type == 16) {
+    if (cross_distances_host(alt_metric(distance_type), d, na, nb, a, lda, b, ldb, dist2, ldd) !=
+        OK)
+      fatal_last("compute_cross_distances_alt");
+    return;
+  }
+  if (distance_type < 1 || distance_type > 6) {
+    set_error(E_UNSUPPORTED, "distance_type %d is not one of 1-6, 12, 16", distance_type);
     fatal_last("compute_cross_distances_alt");
   }
-  if (cross_distances_host(m, d, na, nb, a, lda, b, ldb, dist2, ldd) != OK)
+  if (alt_host(distance_type, d, na, nb, a, lda, b, ldb, dist2, ldd) != OK)
     fatal_last("compute_cross_distances_alt");
 }
 
