@@ -30,9 +30,11 @@ extern "C" {
 /* drop-in: exact k-NN (yael/nn.h)                                     */
 
 /* yael/nn.h:41-45 (yael/nn.c:451-525).  distance_type 2 or 12 = squared L2,
- * 16 = dot product (k smallest, like the reference's min-heap).  k <= nb.
- * Neighbours are ordered by increasing distance, ties by increasing base
- * index.  b_weights (may be NULL) multiplies each base vector's distance. */
+ * 16 = dot product (k smallest, like the reference's min-heap); 1, 3, 4, 5, 6
+ * = the per-coordinate types of compute_cross_distances_alt, computed in the
+ * reference's arithmetic and searched exhaustively.  k <= nb.  Neighbours are
+ * ordered by increasing distance, ties by increasing base index.  b_weights
+ * (may be NULL) multiplies each base vector's distance. */
 void knn_full(int distance_type, int nq, int nb, int d, int k, const float *b,
               const float *q, const float *b_weights, int *assign, float *dis);
 

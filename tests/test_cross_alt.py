@@ -99,3 +99,62 @@ def test_restatement_pinned_to_reference():
 def test_gpu_alt_types_bit_identical(t, d):
     a, b = operands(t * 100 + d + 1, 70, 45, d)
     np.testing.assert_array_equal(run(yg.lib(), t, a, b, ldd_extra=3), restate(t, a, b))
+
+
+def knn_restate(t, base, queries, k):
+    """k smallest (value, index) of the reference's distances (base as the
+    first operand); NaN never taken; k = 1 takes only values below 1e30."""
+    dist = restate(t, base, queries)  # [query, base row]
+    nq, nb = dist.shape
+    idx = np.full((nq, k), -1, np.int32)
+    dis = np.full((nq, k), np.nan, f32)
+    for q in range(nq):
+        row = dist[q]
+        ok = ~np.isnan(row)
+        if k == 1:
+            ok &= row < f32(1e30)
+        cand = np.nonzero(ok)[0]
+        order = cand[np.lexsort((cand, row[cand]))][:k]
+        idx[q, :len(order)] = order
+        dis[q, :len(order)] = row[order]
+        if k == 1 and len(order) == 0:
+            dis[q, 0] = f32(1e30)
+    return idx, dis
+
+
+KNN_CASES = [(t, d, k) for t in (1, 3, 4, 5, 6) for d in (16, 13) for k in (1, 5)]
+
+
+def knn_call(L, t, base, queries, k):
+    nq, d = queries.shape
+    idx = np.zeros((nq, k), np.int32)
+    dis = np.zeros((nq, k), f32)
+    L.knn_full_thread(t, nq, base.shape[0], d, k, ptr(base), ptr(queries), None, ptr(idx),
+                      ptr(dis), 1)
+    return idx, dis
+
+
+def test_knn_restatement_pinned_to_reference():
+    R = reference()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    for t, d, k in KNN_CASES:
+        rng = np.random.default_rng(t * 1000 + d * 10 + k)
+        base = rng.standard_normal((300, d)).astype(f32)
+        queries = rng.standard_normal((20, d)).astype(f32)
+        gi, gd = knn_call(R, t, base, queries, k)
+        ei, ed = knn_restate(t, base, queries, k)
+        np.testing.assert_array_equal(gi, ei, err_msg=f"type {t} d {d} k {k}")
+        np.testing.assert_array_equal(gd, ed, err_msg=f"type {t} d {d} k {k}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("t,d,k", KNN_CASES)
+def test_gpu_knn_alt_types(t, d, k):
+    rng = np.random.default_rng(t * 1000 + d * 10 + k + 1)
+    base = rng.standard_normal((2000, d)).astype(f32)
+    queries = rng.standard_normal((50, d)).astype(f32)
+    gi, gd = knn_call(yg.lib(), t, base, queries, k)
+    ei, ed = knn_restate(t, base, queries, k)
+    np.testing.assert_array_equal(gi, ei)
+    np.testing.assert_array_equal(gd, ed)

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 
+#include "alt.cuh"
 #include "knn.cuh"
 #include "simt_tile.cuh"
 #include "../../include/yael_gpu.h"
@@ -273,14 +274,9 @@ static int recompute_host(int n, int nb, int d, int k, const float *b, const flo
   return OK;
 }
 
-// ---- the other distance types of compute_cross_distances_alt
-// (yael/nn.c:164-350), as the reference computes them on x86: L1 (type 1) and
-// chi2 (type 3) with d % 4 == 0 in four float lanes (SSE2 form: lane l sums
-// the coordinates c = l mod 4, the lanes are then added left to right), every
-// other case as a double sum over the coordinates in order of float terms,
-// rounded to float.  One thread per output (a_i, b_j); the coordinates are
-// walked in order through 32-wide slices staged in shared memory, so each
-// output is the reference's own sequence of operations.
+// ---- the other distance types of compute_cross_distances_alt (alt.cuh):
+// one thread per output (a_i, b_j); the coordinates are walked in order
+// through 32-wide slices staged in shared memory.
 constexpr int AT = 16, AC = 32;  // pairs per block side, coordinates per slice
 
 template <int TYPE, bool SSE>
@@ -290,8 +286,7 @@ __global__ void __launch_bounds__(AT * AT)
   __shared__ float sa[AT][AC + 1], sb[AT][AC + 1];
   const int ti = threadIdx.x % AT, tj = threadIdx.x / AT;
   const int i = blockIdx.x * AT + ti, j = blockIdx.y * AT + tj;
-  double sum = 0.0;
-  float lane[4] = {0.f, 0.f, 0.f, 0.f};
+  AltAcc acc;
   for (int c0 = 0; c0 < d; c0 += AC) {
     const int w = min(AC, d - c0);
     __syncthreads();
@@ -302,44 +297,10 @@ __global__ void __launch_bounds__(AT * AT)
       sb[r][c] = (c < w && jb < nb) ? b[jb * ldb + c0 + c] : 0.f;
     }
     __syncthreads();
-    for (int c = 0; c < w; c++) {
-      const float av = sa[ti][c], bv = sb[tj][c];
-      if (SSE) {
-        float t;
-        if (TYPE == 1) {
-          t = fabsf(__fsub_rn(av, bv));
-        } else {  // chi2: (a - b)^2 / (a + b) where a != b, else 0
-          const float df = __fsub_rn(av, bv);
-          t = av != bv ? __fdiv_rn(__fmul_rn(df, df), __fadd_rn(av, bv)) : 0.f;
-        }
-        lane[(c0 + c) & 3] = __fadd_rn(lane[(c0 + c) & 3], t);
-      } else if (TYPE == 1) {
-        sum = __dadd_rn(sum, (double)fabsf(__fsub_rn(av, bv)));
-      } else if (TYPE == 2) {
-        const double df = (double)__fsub_rn(av, bv);
-        sum = __dadd_rn(sum, __dmul_rn(df, df));
-      } else if (TYPE == 3) {
-        const float s = __fadd_rn(av, bv);
-        if (s != 0.f) {
-          const double df = (double)__fsub_rn(av, bv);
-          sum = __dadd_rn(sum, __ddiv_rn(__dmul_rn(df, df), (double)s));
-        }
-      } else if (TYPE == 4) {
-        const float den = fabsf(__fadd_rn(av, bv));
-        if (den != 0.f) {
-          const double df = (double)__fsub_rn(av, bv);
-          sum = __dadd_rn(sum, __ddiv_rn(__dmul_rn(df, df), (double)den));
-        }
-      } else if (TYPE == 5) {
-        sum = __dadd_rn(sum, (double)(av < bv ? av : bv));
-      } else {  // 6
-        sum = __dadd_rn(sum, (double)__fmul_rn(av, bv));
-      }
-    }
+    for (int c = 0; c < w; c++) alt_step<TYPE, SSE>(acc, sa[ti][c], sb[tj][c], c0 + c);
   }
   if (i >= na || j >= nb) return;
-  out[(long)j * ldo + i] =
-      SSE ? __fadd_rn(__fadd_rn(__fadd_rn(lane[0], lane[1]), lane[2]), lane[3]) : (float)sum;
+  out[(long)j * ldo + i] = alt_finish<SSE>(acc);
 }
 
 template <int TYPE, bool SSE>

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <memory>
 
+#include "alt.cuh"
 #include "autotune.cuh"
 #include "knn.cuh"
 #include "tc_scan.cuh"
@@ -640,7 +641,9 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
     set_error(E_UNSUPPORTED, "knn: k=%d above the supported maximum %d", k, kMaxK);
     return E_UNSUPPORTED;
   }
-  if (job.metric != METRIC_L2 && job.metric != METRIC_DOT) {
+  const bool alt = job.metric > METRIC_ALT0 && job.metric <= METRIC_ALT0 + 6 &&
+                   job.metric != METRIC_ALT0 + 2;
+  if (job.metric != METRIC_L2 && job.metric != METRIC_DOT && !alt) {
     set_error(E_UNSUPPORTED, "knn: distance_type %d not supported on the GPU", job.metric);
     return E_UNSUPPORTED;
   }
@@ -652,8 +655,10 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   small_init_kernel<<<1, 1, 0, st>>>(dsmall);
   YG_LAUNCH_CHECK();
 
-  if (job.w) {
-    // weighted distances reorder per base row: exhaustive exact path
+  if (job.w || alt) {
+    // weighted distances reorder per base row, and the per-coordinate types
+    // (L1, chi2, ...) have no GEMM form: the exhaustive path, which computes
+    // every distance in the reference's arithmetic and keeps the k smallest
     size_t per = exhaustive_bytes_per_query(nb);
     size_t want = per * (size_t)nq;
     const size_t cap_bytes = (size_t)1 << 30;
@@ -782,7 +787,8 @@ int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
     // the parts already there run (host -> device copies are ~25x slower than
     // the packing of what they carry).  The guard drains the copies and frees
     // the events on every exit path.
-    const bool stream_up = w == nullptr && prec == PREC_BF16 && nb >= (1 << 18);
+    const bool stream_up =
+        w == nullptr && prec == PREC_BF16 && metric < METRIC_ALT0 && nb >= (1 << 18);
     BaseUpload up;
     struct UploadGuard {
       BaseUpload *u;
@@ -885,6 +891,9 @@ int knn_host(int metric, int nq, int nb, int d, int k, const float *b,
 static int metric_of(int distance_type) {
   if (distance_type == 2 || distance_type == 12) return METRIC_L2;
   if (distance_type == 16) return METRIC_DOT;
+  // L1, the chi2 forms, histogram intersection, float dot (yael/nn.c:311-350)
+  if (distance_type == 1 || (distance_type >= 3 && distance_type <= 6))
+    return METRIC_ALT0 + distance_type;
   return -1;
 }
 
@@ -916,7 +925,7 @@ void knn_full(int distance_type, int nq, int nb, int d, int k, const float *b,
   const int metric = metric_of(distance_type);
   if (metric < 0) {
     set_error(E_UNSUPPORTED,
-              "distance_type %d has no GPU implementation (supported: 2, 12, 16)",
+              "distance_type %d has no GPU implementation (supported: 1-6, 12, 16)",
               distance_type);
     fatal_last("knn_full");
   }

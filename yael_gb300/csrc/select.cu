@@ -3,6 +3,7 @@
 #include <float.h>
 #include <math.h>
 
+#include "alt.cuh"
 #include "select.cuh"
 
 namespace yg {
@@ -616,6 +617,40 @@ __global__ void fb_rows_kernel(const int *qlist, int q0, int nb, int d, int metr
   rows[(long)r * nb + j] = isnan(e) ? ~0ull : d2ord(e);
 }
 
+// the per-coordinate distance types (alt.cuh) of one query against every base
+// row: the reference's float value (base row as the first operand, as its
+// knn_full passes it), times the weight in float; NaN is never selected, and
+// for k = 1 neither is a value >= 1e30 (the reference's argmin starts there,
+// yael/nn.c:404-435)
+template <int TYPE, bool SSE>
+__global__ void fb_rows_alt_kernel(const int *qlist, int q0, int nb, int d,
+                                   const float *__restrict__ Q, long ldq,
+                                   const float *__restrict__ B, long ldb,
+                                   const float *__restrict__ w, int k1,
+                                   unsigned long long *rows) {
+  extern __shared__ float qs[];
+  const int r = blockIdx.y;
+  const int qi = qlist ? qlist[q0 + r] : q0 + r;
+  for (int c = threadIdx.x; c < d; c += blockDim.x) qs[c] = Q[(long)qi * ldq + c];
+  __syncthreads();
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nb) return;
+  const float *br = B + j * ldb;
+  AltAcc acc;
+  for (int c = 0; c < d; c++) alt_step<TYPE, SSE>(acc, __ldg(br + c), qs[c], c);
+  float e = alt_finish<SSE>(acc);
+  if (w) e = __fmul_rn(e, w[j]);
+  rows[(long)r * nb + j] = (isnan(e) || (k1 && !(e < 1e30f))) ? ~0ull : d2ord((double)e);
+}
+
+template <int TYPE, bool SSE>
+void fb_rows_alt(dim3 g, cudaStream_t st, const int *qlist, int q0, int nb, int d, const float *q,
+                 long ldq, const float *b, long ldb, const float *w, int k1,
+                 unsigned long long *rows) {
+  fb_rows_alt_kernel<TYPE, SSE><<<g, 256, (size_t)d * 4, st>>>(qlist, q0, nb, d, q, ldq, b, ldb,
+                                                                 w, k1, rows);
+}
+
 __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0, int nb, int k,
                                                        const unsigned long long *rows,
                                                        int *out_idx, float *out_dis) {
@@ -826,8 +861,25 @@ int exhaustive(int nlist, const int *qlist_dev, int nb, int d, int k, int metric
   for (int q0 = 0; q0 < nlist; q0 += batch) {
     const int nbt = imin(batch, nlist - q0);
     dim3 g1((unsigned)ceil_div(nb, 256), (unsigned)nbt);
-    fb_rows_kernel<<<g1, 256, (size_t)d * 4, st>>>(qlist_dev, q0, nb, d, metric, q, ldq, b,
-                                                    ldb, w, rows);
+    if (metric >= METRIC_ALT0) {
+      const int t = metric - METRIC_ALT0, k1 = k == 1;
+      const bool sse = (t == 1 || t == 3) && d % 4 == 0;
+      switch (t * 2 + (sse ? 1 : 0)) {
+        case 2: fb_rows_alt<1, false>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        case 3: fb_rows_alt<1, true>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        case 6: fb_rows_alt<3, false>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        case 7: fb_rows_alt<3, true>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        case 8: fb_rows_alt<4, false>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        case 10: fb_rows_alt<5, false>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        case 12: fb_rows_alt<6, false>(g1, st, qlist_dev, q0, nb, d, q, ldq, b, ldb, w, k1, rows); break;
+        default:
+          set_error(E_UNSUPPORTED, "exhaustive: distance type %d", t);
+          return E_UNSUPPORTED;
+      }
+    } else {
+      fb_rows_kernel<<<g1, 256, (size_t)d * 4, st>>>(qlist_dev, q0, nb, d, metric, q, ldq, b,
+                                                      ldb, w, rows);
+    }
     YG_LAUNCH_CHECK();
     fb_select_kernel<<<nbt, RT, smem_sel, st>>>(qlist_dev, q0, nb, k, rows, out_idx, out_dis);
     YG_LAUNCH_CHECK();
