@@ -134,7 +134,8 @@ void compute_distances_1_nonpacked_thread(int d, int nb, const float *a,
  * nearest centroid by FP64 distance, ties to the lowest index.  Centroids are
  * exact integer sums (2^-S fixed point, S chosen from the data so nothing
  * overflows) divided by the count.  flags & 0xffff (threads) is ignored;
- * KMEANS_L1 / KMEANS_CHI2 abort with a message (not implemented). */
+ * KMEANS_L1 / KMEANS_CHI2: assignment by the L1 / chi2 distance (type 1 / 3),
+ * centroids the per-coordinate medians / chi2 minimisers, as the reference. */
 float kmeans(int d, int n, int k, int niter, const float *v, int flags, long seed,
              int redo, float *centroids, float *dis, int *assign, int *nassign);
 

@@ -202,3 +202,18 @@ def test_hkm_golden_and_quantize(gpu_lib):
     np.testing.assert_array_equal(q, oq)
     gpu_lib.hkm_delete(h)
     ctypes.CDLL(None).free(ctypes.cast(ap, ctypes.c_void_p))
+
+
+@pytest.mark.parametrize("name", ["kmeans_l1", "kmeans_chi2"])
+def test_kmeans_l1_chi2_golden(name):
+    """KMEANS_L1 (medians) and KMEANS_CHI2 (chi2 minimisers) against the
+    reference's own outputs (tests/golden/make_golden_alt.py): assignments,
+    counts, centroids and distances bit-identical, objective to 1e-6."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    v = g["v"]
+    r = gpu_kmeans(v, int(g["k"]), int(g["niter"]), int(g["flags"]), int(g["seed"]), 1, "fp32")
+    np.testing.assert_array_equal(r["assign"], g["assign"])
+    np.testing.assert_array_equal(r["nassign"], g["nassign"])
+    np.testing.assert_array_equal(r["C"], g["C"])
+    np.testing.assert_array_equal(r["dis"], g["dis"])
+    assert abs(r["qerr"] - float(g["qerr"])) <= 1e-6 * abs(float(g["qerr"]))

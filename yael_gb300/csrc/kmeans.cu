@@ -13,6 +13,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "alt.cuh"
 #include "kmeans.cuh"
 #include "knn.cuh"
 #include "../../include/yael_gpu.h"
@@ -33,6 +34,7 @@ enum KmSlot : int {
   KS_V = WS_KM0, KS_C, KS_ASSIGN, KS_DIS, KS_COUNTS, KS_OFFS, KS_CURSOR, KS_PERM, KS_ACC,
   KS_SHIFT, KS_ACTIVE, KS_PINST, KS_WORK, KS_SLICES, KS_PART, KS_ROWS, KS_AMAX,
   KS_BEST_C, KS_BEST_DIS, KS_BEST_ASSIGN, KS_NODE, KS_VSORT, KS_TMP, KS_CPREV,
+  KS_AKEYS, KS_AKEYS2, KS_AVALS, KS_AVALS2, KS_AOFFS, KS_ATMP, KS_ASORT,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -183,12 +185,16 @@ struct Engine {
     if (ph_part) cudaFreeHost(ph_part);
   }
 
+  // L1 / chi2 k-means (one instance): per-coordinate distances searched
+  // exhaustively, medians / chi2 minimisers as centroids
+  bool alt_mode() const { return (flags & (YAEL_KMEANS_L1 | YAEL_KMEANS_CHI2)) != 0; }
+
   bool graphs_wanted() const {
     static const bool on = [] {
       const char *e = getenv("YAEL_GPU_GRAPHS");
       return !(e && e[0] == '0');
     }();
-    return on && !graphs_failed;
+    return on && !graphs_failed && !alt_mode();
   }
   bool assign_graph_wanted() const { return graphs_wanted() && !(in.size() == 1 && k > kSmallK); }
 
@@ -324,6 +330,16 @@ struct Engine {
   }
 
   int assign_step() {
+    if (alt_mode()) {
+      // yael/kmeans.c:242-244: knn_full with distance type 1 (L1) or 3 (chi2)
+      KnnJob job;
+      job.nq = in[0].n; job.nb = k; job.d = d; job.k = 1;
+      job.metric = METRIC_ALT0 + ((flags & YAEL_KMEANS_L1) ? 1 : 3);
+      job.prec = PREC_FP32;
+      job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
+      job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
+      return knn_device(job, ctx, st);
+    }
     if (in.size() == 1 && k > kSmallK) {
       KnnJob job;
       job.nq = in[0].n; job.nb = k; job.d = d; job.k = 1; job.metric = METRIC_L2;
@@ -368,6 +384,30 @@ struct Engine {
     auto update_body = [&]() -> int {
       YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
       YG_CHECK(km_histogram(assign, pinst, ntot, k, active, counts, st));
+      if (alt_mode()) {
+        Workspace &ws = ctx->ws;
+        int *keys, *keys2, *vals, *vals2, *offs2;
+        float *tmp;
+        void *sort_tmp;
+        const size_t sb = km_alt_sort_bytes(ntot);
+        YG_CHECK(ws_get(ws, KS_AKEYS, (size_t)ntot, &keys));
+        YG_CHECK(ws_get(ws, KS_AKEYS2, (size_t)ntot, &keys2));
+        YG_CHECK(ws_get(ws, KS_AVALS, (size_t)ntot, &vals));
+        YG_CHECK(ws_get(ws, KS_AVALS2, (size_t)ntot, &vals2));
+        YG_CHECK(ws_get(ws, KS_AOFFS, (size_t)k + 1, &offs2));
+        YG_CHECK(ws_get(ws, KS_ATMP, (size_t)ntot * d, &tmp));
+        YG_CHECK(ctx->ws.get(KS_ASORT, sb ? sb : 1, &sort_tmp));
+        YG_CHECK(km_alt_update(assign, ntot, v, d, k, (flags & YAEL_KMEANS_L1) != 0, keys, keys2,
+                               vals, vals2, offs2, tmp, sort_tmp, sb, C, st));
+        if (flags & YAEL_KMEANS_NORMALIZE_CENTS) {
+          if (flags & YAEL_KMEANS_L1) YG_CHECK(km_normalize_l1(C, ncl, d, st));
+          else YG_CHECK(km_normalize(C, ncl, d, k, active, st));
+        }
+        YG_CHECK(km_slice_sums(slices, nsl, dis, part, st));
+        YG_CUDA(cudaMemcpyAsync(ph_counts, counts, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
+        YG_CUDA(cudaMemcpyAsync(ph_part, part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
+        return OK;
+      }
       YG_CHECK(km_scan(counts, ncl, offs, cursor, st));
       YG_CHECK(km_scatter(assign, pinst, ntot, k, active, cursor, perm, st));
       YG_CHECK(km_update(perm, offs + ncl, ntot, assign, pinst, counts, v, d, ncl, k, shift,
@@ -569,10 +609,6 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
   if (k > n || k < 1 || d < 1) {
     set_error(E_ARG, "kmeans: k=%d n=%d d=%d (the reference asserts k <= n)", k, n, d);
     return E_ARG;
-  }
-  if (flags & (YAEL_KMEANS_L1 | YAEL_KMEANS_CHI2)) {
-    set_error(E_UNSUPPORTED, "kmeans: L1 / chi2 k-means are not implemented on the GPU");
-    return E_UNSUPPORTED;
   }
   const float *v = v_in;
   if (!dev) {

@@ -30,6 +30,17 @@ int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const 
 // the last call is final, so that a CUDA graph may capture the assignment.
 bool km_assign_tune_collect();
 
+// L1 / chi2 k-means centroids (yael/kmeans.c:253-275): per cluster and
+// coordinate the median (l1) or the minimiser of the summed chi2 distance of
+// the cluster's points, which are first sorted by cluster (keys / vals:
+// n-element scratch pairs, offs: k + 1, tmp: n x d, sort_tmp:
+// km_alt_sort_bytes(n)).
+size_t km_alt_sort_bytes(long n);
+int km_alt_update(const int *assign, long n, const float *v, int d, int k, bool l1, int *keys,
+                  int *keys2, int *vals, int *vals2, int *offs, float *tmp, void *sort_tmp,
+                  size_t sort_bytes, float *C, cudaStream_t st);
+int km_normalize_l1(float *C, long ncl, int d, cudaStream_t st);
+
 // counts[inst*k + assign[p]]++ over points of active instances
 int km_histogram(const int *assign, const int *pinst, long n, int k,
                  const unsigned char *active, int *counts, cudaStream_t st);

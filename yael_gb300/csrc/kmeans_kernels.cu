@@ -1,5 +1,8 @@
 // Device kernels of the k-means Lloyd step (see kmeans.cuh).
+#include <limits.h>
 #include <math.h>
+
+#include <cub/device/device_radix_sort.cuh>
 
 #include "autotune.cuh"
 #include "kmeans.cuh"
@@ -544,6 +547,141 @@ __global__ void normalize_kernel(float *C, long ncl, int d, int k, const unsigne
   for (int c = 0; c < d; c++) row[c] = (float)((double)row[c] * inv);
 }
 
+// L1 normalisation of the centroids (yael/vector.c:2016-2026, 2180-2191)
+__global__ void normalize_l1_kernel(float *C, long ncl, int d) {
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ncl) return;
+  float *row = C + g * d;
+  double s = 0;
+  for (int c = 0; c < d; c++) s += (double)fabsf(row[c]);
+  const double inv = 1. / s;
+  for (int c = 0; c < d; c++) row[c] = (float)((double)row[c] * inv);
+}
+
+// ---- L1 / chi2 centroids (yael/kmeans.c:253-275) ------------------------
+// perm: point indices sorted by cluster, increasing within a cluster; offs:
+// the cluster segments; tmp: n x d scratch, the values of one coordinate
+// contiguous (the reference's tmp_v layout).
+
+// in place: a[kth] becomes the kth smallest (0-based), a[0..kth) <= a[kth] <=
+// a[kth+1..n) (Hoare partitions around a middle pivot; each round shrinks the
+// range, so it ends)
+__device__ void select_kth(float *a, int n, int kth) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const float p = a[(lo + hi) >> 1];
+    int i = lo, j = hi;
+    while (i <= j) {
+      while (a[i] < p) i++;
+      while (a[j] > p) j--;
+      if (i <= j) {
+        const float t = a[i];
+        a[i] = a[j];
+        a[j] = t;
+        i++;
+        j--;
+      }
+    }
+    if (kth <= j) hi = j;
+    else if (kth >= i) lo = i;
+    else break;
+  }
+}
+
+// the median of each cluster's values per coordinate (yael/sorting.c:676-703):
+// the (m/2)-th smallest for odd m, half the float sum of the two middle values
+// for even m; NaN for an empty cluster
+__global__ void median_kernel(const int *perm, const int *offs, const float *v, int d, int k,
+                              long n, float *tmp, float *C) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)k * d) return;
+  const int c = (int)(t / d), j = (int)(t - (long)c * d);
+  const int o0 = offs[c], m = offs[c + 1] - o0;
+  float out;
+  if (m == 0) {
+    out = __int_as_float(0x7fc00000);
+  } else if (m == 1) {
+    out = v[(long)perm[o0] * d + j];
+  } else {
+    float *seg = tmp + (long)j * n + o0;
+    for (int e = 0; e < m; e++) seg[e] = v[(long)perm[o0 + e] * d + j];
+    const int half = m / 2;
+    select_kth(seg, m, half);
+    const float upper = seg[half];
+    if (m & 1) {
+      out = upper;
+    } else {
+      float lower = seg[0];
+      for (int e = 1; e < half; e++) lower = seg[e] > lower ? seg[e] : lower;
+      out = (float)(0.5 * (double)__fadd_rn(upper, lower));
+    }
+  }
+  C[t] = out;
+}
+
+// the minimiser of sum_i (x - a_i)^2 / (x + a_i) over x >= 0 (Newton steps,
+// yael/kmeans.c:95-158), the cluster's values taken in decreasing point order
+// as the reference's scratch holds them; float arithmetic, unfused
+__global__ void chi2_kernel(const int *perm, const int *offs, const float *v, int d, int k, long n,
+                            float *tmp, float *C) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)k * d) return;
+  const int c = (int)(t / d), j = (int)(t - (long)c * d);
+  const int o0 = offs[c], m = offs[c + 1] - o0;
+  float x;
+  if (m == 0) {
+    x = __int_as_float(0x7fc00000);
+  } else if (m == 1) {
+    x = v[(long)perm[o0] * d + j];
+  } else {
+    float *a = tmp + (long)j * n + o0;
+    for (int e = 0; e < m; e++) a[e] = v[(long)perm[o0 + m - 1 - e] * d + j];
+    float mag = 0.f;
+    for (int e = 0; e < m; e++) mag = __fadd_rn(mag, a[e]);
+    mag = __fdiv_rn(mag, (float)m);
+    x = 0.f;
+    float prev = 0.f;
+    int niter = 0;
+    for (;;) {
+      float dv = 0.f, ddv = 0.f;
+      for (int e = 0; e < m; e++) {
+        const float s1 = __fadd_rn(x, a[e]);
+        const float s2 = __fmul_rn(s1, s1);
+        const float s3 = __fmul_rn(s1, s2);
+        if (s2 == 0.f) continue;
+        dv = __fadd_rn(dv, __fdiv_rn(__fmul_rn(__fsub_rn(x, a[e]), __fadd_rn(x, __fmul_rn(3.f, a[e]))),
+                                     s2));
+        ddv = __fadd_rn(ddv, __fdiv_rn(__fmul_rn(__fmul_rn(8.f, a[e]), a[e]), s3));
+      }
+      if (dv == 0.f) break;
+      prev = x;
+      x = __fsub_rn(x, __fdiv_rn(dv, ddv));
+      if (x < 0.f) x = (float)((double)prev / 2.0);
+      if (++niter == 1000) break;
+      if (!(fabs((double)__fsub_rn(x, prev)) > 1e-4 * (double)mag)) break;
+    }
+  }
+  C[t] = x;
+}
+
+__global__ void cluster_keys_kernel(const int *assign, long n, int *keys, int *vals) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keys[i] = assign[i] < 0 ? INT_MAX : assign[i];
+  vals[i] = (int)i;
+}
+
+__global__ void cluster_offsets_kernel(const int *sorted, long n, int k, int *offs) {
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g > k) return;
+  long lo = 0, hi = n;
+  while (lo < hi) {
+    const long mid = (lo + hi) / 2;
+    if (sorted[mid] < g) lo = mid + 1; else hi = mid;
+  }
+  offs[g] = (int)lo;
+}
+
 __global__ void absmax_kernel(const KmSlice *sl, const float *v, int d, float *out) {
   const KmSlice s = sl[blockIdx.x];
   float m = 0.f;
@@ -665,6 +803,40 @@ int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const 
   if (k <= 64) return launch_assign_any<64>(work, nwork, v, d, C, k, active, assign, dis, st);
   set_error(E_ARG, "grouped assignment: k=%d > %d", k, kSmallK);
   return E_ARG;
+}
+
+size_t km_alt_sort_bytes(long n) {
+  size_t tb = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tb, (const int *)nullptr, (int *)nullptr,
+                                  (const int *)nullptr, (int *)nullptr, (int)n, 0, 32);
+  return tb;
+}
+
+int km_alt_update(const int *assign, long n, const float *v, int d, int k, bool l1, int *keys,
+                  int *keys2, int *vals, int *vals2, int *offs, float *tmp, void *sort_tmp,
+                  size_t sort_bytes, float *C, cudaStream_t st) {
+  if (n > INT_MAX) {
+    set_error(E_UNSUPPORTED, "L1 / chi2 k-means: %ld points", n);
+    return E_UNSUPPORTED;
+  }
+  cluster_keys_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(assign, n, keys, vals);
+  YG_LAUNCH_CHECK();
+  size_t tb = sort_bytes;
+  YG_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp, tb, keys, keys2, vals, vals2, (int)n, 0, 32,
+                                          st));
+  cluster_offsets_kernel<<<(unsigned)ceil_div((long)k + 1, 256), 256, 0, st>>>(keys2, n, k, offs);
+  YG_LAUNCH_CHECK();
+  const unsigned g = (unsigned)ceil_div((long)k * d, 128);
+  if (l1) median_kernel<<<g, 128, 0, st>>>(vals2, offs, v, d, k, n, tmp, C);
+  else chi2_kernel<<<g, 128, 0, st>>>(vals2, offs, v, d, k, n, tmp, C);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int km_normalize_l1(float *C, long ncl, int d, cudaStream_t st) {
+  normalize_l1_kernel<<<(unsigned)ceil_div(ncl, 128), 128, 0, st>>>(C, ncl, d);
+  YG_LAUNCH_CHECK();
+  return OK;
 }
 
 bool km_assign_tune_collect() {
