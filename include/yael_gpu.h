@@ -242,6 +242,32 @@ int bvec_fread(FILE *f, unsigned char *v, int d_alloc);
 long fvecs_fread(FILE *f, float *v, long n, int d_alloc);
 long ivecs_fread(FILE *f, int *v, long n, int d_alloc);
 long bvecs_fread(FILE *f, unsigned char *v, long n, int d_alloc);
+/* yael/vector.h:193-200 (yael/vector.c:1386-1445): d elements without the
+ * dimension header; 0, -1 on error */
+int fvec_fwrite_raw(FILE *f, const float *v, long d);
+int ivec_fwrite_raw(FILE *f, const int *v, long d);
+int bvec_fwrite_raw(FILE *f, const unsigned char *v, long d);
+int fvec_write_raw(const char *fname, const float *v, long d);
+int ivec_write_raw(const char *fname, const int *v, long d);
+int bvec_write_raw(const char *fname, const unsigned char *v, long d);
+/* yael/vector.h:282-295 (yael/vector.c:1149-1250): n headerless elements
+ * (n, -1 on a short read: the caller's buffer is left allocated, where the
+ * reference frees it); the *_new_* forms return a malloc'd array or NULL */
+int fvec_fread_raw(FILE *f, float *v, long n);
+int ivec_fread_raw(FILE *f, int *v, long n);
+int bvec_fread_raw(FILE *f, unsigned char *v, long n);
+float *fvec_new_fread_raw(FILE *f, long d);
+int *ivec_new_fread_raw(FILE *f, long d);
+unsigned char *bvec_new_fread_raw(FILE *f, long d);
+float *fvec_new_read_raw(const char *fname, long d);
+int *ivec_new_read_raw(const char *fname, long d);
+unsigned char *bvec_new_read_raw(const char *fname, long d);
+/* yael/vector.h:207-210, 270 (yael/vector.c:939-964, 1279-1294, 1475-1491):
+ * one text line per vector, "%d " / "%f " per element; the writers return n
+ * (-1 if the file cannot be opened), the reader the whole vectors read */
+int ivecs_write_txt(const char *fname, int d, int n, const int *v);
+int fvecs_write_txt(const char *fname, int d, int n, const float *v);
+int fvecs_read_txt(const char *fname, int d, int n, float *v);
 
 /* ------------------------------------------------------------------ */
 /* extension API                                                       */

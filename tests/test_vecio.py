@@ -19,6 +19,7 @@ libc.fopen.restype = P
 libc.fopen.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
 libc.fclose.argtypes = [P]
 libc.free.argtypes = [P]
+libc.fflush.argtypes = [P]
 
 
 def ptr(a):
@@ -42,7 +43,8 @@ def ref_lib():
         return None
     for name, (res, args) in yg.SIGNATURES.items():
         if name.endswith(("vec_fwrite", "vecs_fwrite", "vecs_write", "vecs_fsize", "vecs_new_read",
-                          "vecs_new_fread_max", "vecs_read", "vec_fread", "vecs_fread")) \
+                          "vecs_new_fread_max", "vecs_read", "vec_fread", "vecs_fread", "_raw",
+                          "_txt")) \
                 and hasattr(r, name):
             getattr(r, name).restype = res
             getattr(r, name).argtypes = args
@@ -179,3 +181,80 @@ def test_against_the_reference(tmp_path, data):
     s1, s2 = (I(), I()), (I(), I())
     assert L_.fvecs_fsize(path, *map(ctypes.byref, s1)) == R.fvecs_fsize(path, *map(ctypes.byref, s2))
     assert [x.value for x in s1] == [x.value for x in s2]
+
+
+def as_array(p, n, dtype):
+    return np.ctypeslib.as_array(
+        ctypes.cast(p, ctypes.POINTER(np.ctypeslib.as_ctypes_type(dtype))), shape=(n,)).copy()
+
+
+def test_raw_and_text(tmp_path, data):
+    """Headerless files hold exactly the elements; text files one line per
+    vector with a space after each element; both read back."""
+    f, i, b = data
+    L_ = yg.lib()
+    for name, arr, w, rd, nf in (("r.f", f, L_.fvec_write_raw, L_.fvec_new_read_raw, L_.fvec_fread_raw),
+                                 ("r.i", i, L_.ivec_write_raw, L_.ivec_new_read_raw, L_.ivec_fread_raw),
+                                 ("r.b", b, L_.bvec_write_raw, L_.bvec_new_read_raw, L_.bvec_fread_raw)):
+        path = str(tmp_path / name).encode()
+        assert w(path, ptr(arr), arr.size) == 0
+        assert open(path, "rb").read() == arr.tobytes()
+        out = rd(path, arr.size)
+        np.testing.assert_array_equal(as_array(out, arr.size, arr.dtype), arr.ravel())
+        libc.free(out)
+        assert rd(path, arr.size + 1) is None          # short file
+        fh = libc.fopen(path, b"r")
+        half = np.zeros(arr.size // 2, arr.dtype)
+        assert nf(fh, ptr(half), half.size) == half.size
+        np.testing.assert_array_equal(half, arr.ravel()[:half.size])
+        rest = np.zeros(arr.size, arr.dtype)
+        assert nf(fh, ptr(rest), rest.size) == -1      # past the end
+        libc.fclose(fh)
+    assert L_.fvec_new_read_raw(str(tmp_path / "none").encode(), 4) is None
+    ft, it = str(tmp_path / "f.txt").encode(), str(tmp_path / "i.txt").encode()
+    assert L_.fvecs_write_txt(ft, 24, 37, ptr(f)) == 37
+    assert L_.ivecs_write_txt(it, 24, 37, ptr(i)) == 37
+    lines = open(it).read().split("\n")
+    assert lines[-1] == "" and len(lines) == 38
+    assert lines[0] == "".join(f"{x} " for x in i[0])
+    assert open(ft).read().split("\n")[1] == "".join(f"{x:f} " for x in f[1])
+    got = np.zeros((40, 24), np.float32)
+    assert L_.fvecs_read_txt(ft, 24, 40, ptr(got)) == 37  # fewer vectors than asked
+    np.testing.assert_array_equal(got[:37], np.array([[float(f"{x:f}") for x in r] for r in f],
+                                                     np.float32))
+    assert L_.fvecs_read_txt(ft, 24, 3, ptr(got)) == 3
+    bad = str(tmp_path / "bad.txt").encode()
+    open(bad, "w").write("1 2 x 4\n")
+    assert L_.fvecs_read_txt(bad, 2, 2, ptr(got)) == -1
+
+
+def test_raw_and_text_against_the_reference(tmp_path, data):
+    """Same bytes written and same values read as the reference library (its
+    success paths only: on a short raw read it frees the caller's buffer)."""
+    R = ref_lib()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    f, i, b = data
+    L_ = yg.lib()
+    for ext, arr, fn in (("f", f, "fvec"), ("i", i, "ivec"), ("b", b, "bvec")):
+        p1, p2 = (str(tmp_path / f"{w}.raw{ext}").encode() for w in ("ours", "ref"))
+        assert getattr(L_, fn + "_write_raw")(p1, ptr(arr), arr.size) == 0
+        assert getattr(R, fn + "_write_raw")(p2, ptr(arr), arr.size) == 0
+        assert open(p1, "rb").read() == open(p2, "rb").read()
+        o1 = getattr(L_, fn + "_new_read_raw")(p2, arr.size - 5)
+        o2 = getattr(R, fn + "_new_read_raw")(p2, arr.size - 5)
+        nbytes = (arr.size - 5) * arr.itemsize
+        assert ctypes.string_at(o1, nbytes) == ctypes.string_at(o2, nbytes)
+        libc.free(o1)
+        libc.free(o2)
+    for fn, arr in (("fvecs_write_txt", f), ("ivecs_write_txt", i)):
+        p1, p2 = (str(tmp_path / f"{w}.{fn}").encode() for w in ("ours", "ref"))
+        assert getattr(L_, fn)(p1, 24, 37, ptr(arr)) == getattr(R, fn)(p2, 24, 37, ptr(arr)) == 37
+        libc.fflush(None)  # the reference leaves its text file open
+        assert open(p1, "rb").read() == open(p2, "rb").read()
+    path = str(tmp_path / "ours.fvecs_write_txt").encode()
+    for nread in (5, 37, 50):
+        a1, a2 = np.zeros((50, 24), np.float32), np.zeros((50, 24), np.float32)
+        assert L_.fvecs_read_txt(path, 24, nread, ptr(a1)) == R.fvecs_read_txt(path, 24, nread,
+                                                                              ptr(a2))
+        np.testing.assert_array_equal(a1, a2)

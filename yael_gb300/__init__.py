@@ -125,6 +125,24 @@ SIGNATURES = {
     "fvecs_fread": (ctypes.c_long, [P, P, ctypes.c_long, c_int]),
     "ivecs_fread": (ctypes.c_long, [P, P, ctypes.c_long, c_int]),
     "bvecs_fread": (ctypes.c_long, [P, P, ctypes.c_long, c_int]),
+    "fvec_fwrite_raw": (c_int, [P, P, ctypes.c_long]),
+    "ivec_fwrite_raw": (c_int, [P, P, ctypes.c_long]),
+    "bvec_fwrite_raw": (c_int, [P, P, ctypes.c_long]),
+    "fvec_write_raw": (c_int, [ctypes.c_char_p, P, ctypes.c_long]),
+    "ivec_write_raw": (c_int, [ctypes.c_char_p, P, ctypes.c_long]),
+    "bvec_write_raw": (c_int, [ctypes.c_char_p, P, ctypes.c_long]),
+    "fvec_fread_raw": (c_int, [P, P, ctypes.c_long]),
+    "ivec_fread_raw": (c_int, [P, P, ctypes.c_long]),
+    "bvec_fread_raw": (c_int, [P, P, ctypes.c_long]),
+    "fvec_new_fread_raw": (P, [P, ctypes.c_long]),
+    "ivec_new_fread_raw": (P, [P, ctypes.c_long]),
+    "bvec_new_fread_raw": (P, [P, ctypes.c_long]),
+    "fvec_new_read_raw": (P, [ctypes.c_char_p, ctypes.c_long]),
+    "ivec_new_read_raw": (P, [ctypes.c_char_p, ctypes.c_long]),
+    "bvec_new_read_raw": (P, [ctypes.c_char_p, ctypes.c_long]),
+    "ivecs_write_txt": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "fvecs_write_txt": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
+    "fvecs_read_txt": (c_int, [ctypes.c_char_p, c_int, c_int, P]),
     "hkm_get_centroids": (P, [P, c_int, c_int]),
     "yael_gpu_kmeans_ex": (c_float, [c_int, c_int, c_int, c_int, P, c_int, c_long, c_int, P, P, P, P, ctypes.c_void_p]),
     "yael_gpu_hkm_learn_ex": (c_int, [c_int, c_int, c_int, c_int, P, c_int, c_int, P, P, P, P]),

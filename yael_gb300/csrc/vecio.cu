@@ -362,4 +362,156 @@ int b2fvecs_new_read(const char *fname, int *d_out, float **v_out) {
   return n;
 }
 
+// Raw vectors (yael/vector.c:1149-1250, 1386-1445): d elements with no
+// dimension header.  Where the reference frees the caller's buffer on a short
+// read (fvec_fread_raw & co.) these leave it alone; where it asserts or hands a
+// null FILE to fread on an unopenable file these print and return -1 / NULL.
+static int raw_fwrite(FILE *f, const void *v, long d, size_t unit, const char *who) {
+  if (fwrite(v, unit, (size_t)d, f) != (size_t)d) {
+    perror(who);
+    return -1;
+  }
+  return 0;
+}
+
+static int raw_fread(FILE *f, void *v, long n, size_t unit, const char *who) {
+  if (fread(v, unit, (size_t)n, f) != (size_t)n) {
+    perror(who);
+    return -1;
+  }
+  return (int)n;
+}
+
+static void *raw_new_fread(FILE *f, long d, size_t unit, const char *who) {
+  void *v = malloc(unit * (size_t)(d > 0 ? d : 0) + 1);
+  if (raw_fread(f, v, d, unit, who) < 0) {
+    free(v);
+    return nullptr;
+  }
+  return v;
+}
+
+static void *raw_new_read(const char *fname, long d, size_t unit, const char *who) {
+  FILE *f = fopen(fname, "r");
+  if (!f) {
+    fprintf(stderr, "%s: cannot open %s: %s\n", who, fname, strerror(errno));
+    return nullptr;
+  }
+  void *v = raw_new_fread(f, d, unit, who);
+  fclose(f);
+  return v;
+}
+
+static int raw_write(const char *fname, const void *v, long d, size_t unit, const char *who) {
+  FILE *f = fopen(fname, "w");
+  if (!f) {
+    fprintf(stderr, "%s: cannot open %s: %s\n", who, fname, strerror(errno));
+    return -1;
+  }
+  const int r = raw_fwrite(f, v, d, unit, who);
+  fclose(f);
+  return r;
+}
+
+int fvec_fwrite_raw(FILE *f, const float *v, long d) {
+  return raw_fwrite(f, v, d, 4, "fvec_fwrite_raw");
+}
+int ivec_fwrite_raw(FILE *f, const int *v, long d) {
+  return raw_fwrite(f, v, d, 4, "ivec_fwrite_raw");
+}
+int bvec_fwrite_raw(FILE *f, const unsigned char *v, long d) {
+  return raw_fwrite(f, v, d, 1, "bvec_fwrite_raw");
+}
+int fvec_write_raw(const char *fname, const float *v, long d) {
+  return raw_write(fname, v, d, 4, "fvec_write_raw");
+}
+int ivec_write_raw(const char *fname, const int *v, long d) {
+  return raw_write(fname, v, d, 4, "ivec_write_raw");
+}
+int bvec_write_raw(const char *fname, const unsigned char *v, long d) {
+  return raw_write(fname, v, d, 1, "bvec_write_raw");
+}
+int fvec_fread_raw(FILE *f, float *v, long n) { return raw_fread(f, v, n, 4, "fvec_fread_raw"); }
+int ivec_fread_raw(FILE *f, int *v, long n) { return raw_fread(f, v, n, 4, "ivec_fread_raw"); }
+int bvec_fread_raw(FILE *f, unsigned char *v, long n) {
+  return raw_fread(f, v, n, 1, "bvec_fread_raw");
+}
+float *fvec_new_fread_raw(FILE *f, long d) {
+  return (float *)raw_new_fread(f, d, 4, "fvec_new_fread_raw");
+}
+int *ivec_new_fread_raw(FILE *f, long d) {
+  return (int *)raw_new_fread(f, d, 4, "ivec_new_fread_raw");
+}
+unsigned char *bvec_new_fread_raw(FILE *f, long d) {
+  return (unsigned char *)raw_new_fread(f, d, 1, "bvec_new_fread_raw");
+}
+float *fvec_new_read_raw(const char *fname, long d) {
+  return (float *)raw_new_read(fname, d, 4, "fvec_new_read_raw");
+}
+int *ivec_new_read_raw(const char *fname, long d) {
+  return (int *)raw_new_read(fname, d, 4, "ivec_new_read_raw");
+}
+unsigned char *bvec_new_read_raw(const char *fname, long d) {
+  return (unsigned char *)raw_new_read(fname, d, 1, "bvec_new_read_raw");
+}
+
+// Text vectors (yael/vector.c:939-964, 1279-1294, 1475-1491): one line per
+// vector, each element followed by a space ("%d " / "%f "); the writers return
+// the characters of the line ends written (n), the reader the number of whole
+// vectors read (elements read / d).  The writers close their file (the
+// reference leaves it open until exit).
+int ivecs_write_txt(const char *fname, int d, int n, const int *v) {
+  FILE *f = fopen(fname, "w");
+  if (!f) {
+    perror("ivecs_write_txt: cannot open file");
+    return -1;
+  }
+  int ret = 0;
+  for (long i = 0; i < n; i++) {
+    for (long j = 0; j < d; j++) fprintf(f, "%d ", v[i * d + j]);
+    ret += fprintf(f, "\n");
+  }
+  fclose(f);
+  return ret;
+}
+
+int fvecs_write_txt(const char *fname, int d, int n, const float *v) {
+  FILE *f = fopen(fname, "w");
+  if (!f) {
+    perror("fvecs_write_txt: cannot open file");
+    return -1;
+  }
+  int ret = 0;
+  for (long i = 0; i < n; i++) {
+    for (long j = 0; j < d; j++) fprintf(f, "%f ", (double)v[i * d + j]);
+    ret += fprintf(f, "\n");
+  }
+  fclose(f);
+  return ret;
+}
+
+int fvecs_read_txt(const char *fname, int d, int n, float *v) {
+  FILE *f = fopen(fname, "r");
+  if (!f) {
+    fprintf(stderr, "fvecs_read_txt: could not open %s: %s\n", fname, strerror(errno));
+    return -1;
+  }
+  if (d <= 0) {
+    fclose(f);
+    return 0;
+  }
+  long i;
+  const long total = (long)n * d;
+  for (i = 0; i < total; i++) {
+    if (fscanf(f, "%f", v + i) != 1) {
+      if (feof(f)) break;
+      perror("fvecs_read_txt");
+      fclose(f);
+      return -1;
+    }
+  }
+  fclose(f);
+  return (int)(i / d);
+}
+
 }  // extern "C"
