@@ -203,6 +203,112 @@ void bof_compute_subsets(int k, int d, const float *centroids, int n, const floa
                          int n_subset, const int *subset_indexes, const int *subset_ends,
                          float *desc);
 
+/* ------------------------------------------------------------------ */
+/* drop-in: k-means LSH (yael/kmlsh.h)                                 */
+
+/* same layouts as yael/kmlsh.h:24-29, 62-67, 74-80 */
+typedef struct nnlist_s {
+  long n;     /* number of lists */
+  long k;     /* entries per list */
+  int *idx;   /* n x k ids (-1: empty) */
+  float *dis; /* n x k distances (1e30: empty) */
+} nnlist_t;
+
+typedef struct kmlsh_s {
+  int nhash;         /* number of partitions (hash functions) */
+  int d;             /* dimension */
+  int nclust;        /* cells per partition */
+  float **centroids; /* nhash arrays of nclust x d */
+} kmlsh_t;
+
+typedef struct kmlsh_idx_s {
+  int nhash;
+  int n;           /* vectors indexed */
+  int nclust;
+  int *perm;       /* per partition: the n ids ordered by cell */
+  int *boundaries; /* per partition: the nclust + 1 cell starts in perm */
+} kmlsh_idx_t;
+
+/* flag bits and constants, same values as yael/kmlsh.h:49-58 */
+#define YAEL_KMLSH_NT 0x000000ff
+#define YAEL_KMLSH_QUIET 0x00010000
+#define YAEL_KMLSH_WRITE_INTER_NHASH 0x00020000
+#define YAEL_KMLSH_BLOCK_SIZE 256
+#define YAEL_KMLSH_NB_ITER_MAX 8
+#define YAEL_KMLSH_VECTYPE_FVEC 0
+#define YAEL_KMLSH_VECTYPE_BVEC 1
+
+/* yael/kmlsh.h:31-44 (yael/kmlsh.c:31-92): n lists of k (id, distance);
+ * nnlist_addn keeps each list's k smallest distinct ids, the largest in
+ * slot 0, in the reference's slot order.  _noalloc leaves idx / dis NULL. */
+nnlist_t *nnlist_new(int n, int k);
+nnlist_t *nnlist_new_noalloc(int n, int k);
+void nnlist_delete(nnlist_t *l);
+void nnlist_addn(nnlist_t *l, int lno, int n, int *idx, float *dis);
+
+/* yael/kmlsh.h:86-104 (yael/kmlsh.c:99-206): each partition is the drop-in
+ * kmeans (8 iterations, random init, seed drawn by lrand48()) of nlearn
+ * vectors sampled with ivec_new_random_idx, as the reference */
+kmlsh_t *kmlsh_new(int nhash, int nclust, int d);
+void kmlsh_delete(kmlsh_t *lsh);
+void kmlsh_learn_xvec(kmlsh_t *lsh, int n, int nlearn, const void *v, int flags,
+                      int vec_type);
+kmlsh_t *kmlsh_new_learn_bvec(int nhash, int nclust, int d, int n, int nlearn,
+                              const unsigned char *v, int flags);
+kmlsh_t *kmlsh_new_learn_fvec(int nhash, int nclust, int d, int n, int nlearn,
+                              const float *v, int flags);
+
+/* yael/kmlsh.h:106-119 (yael/kmlsh.c:376-476): per partition, the exact
+ * k-NN of every cell's queries among the cell's base vectors (one batched
+ * GPU call over the occupied cells), merged into one list of k per query
+ * in the reference's order.  nt is ignored. */
+nnlist_t *kmlsh_match_xvec(const kmlsh_t *lsh, const kmlsh_idx_t *lshidx_b, const void *vb,
+                           int nb, const kmlsh_idx_t *lshidx_q, const void *vq, int nq, int k,
+                           int nt, int vec_type);
+nnlist_t *kmlsh_match_bvec(const kmlsh_t *lsh, const kmlsh_idx_t *lshidx_b,
+                           const unsigned char *vb, int nb, const kmlsh_idx_t *lshidx_q,
+                           const unsigned char *vq, int nq, int k, int nt);
+nnlist_t *kmlsh_match_fvec(const kmlsh_t *lsh, const kmlsh_idx_t *lshidx_b, const float *vb,
+                           int nb, const kmlsh_idx_t *lshidx_q, const float *vq, int nq, int k,
+                           int nt);
+
+/* yael/kmlsh.h:124-135 (yael/kmlsh.c:479-520): nclust = sqrt(nb), 100 *
+ * nclust learning vectors, then learn, index and match as above */
+nnlist_t *kmlsh_ann_xvec(const void *vb, int nb, const void *vq, int nq, int d, int k,
+                         int nhash, int flags, int vec_type);
+nnlist_t *kmlsh_ann_bvec(const unsigned char *vb, int nb, const unsigned char *vq, int nq,
+                         int d, int k, int nhash, int flags);
+nnlist_t *kmlsh_ann_fvec(const float *vb, int nb, const float *vq, int nq, int d, int k,
+                         int nhash, int flags);
+
+/* yael/kmlsh.h:138-169 (yael/kmlsh.c:210-372): per partition the
+ * nearest centroid of each vector (one k = 1 GPU search), then the ids
+ * ordered by cell (stable) and the cell starts */
+kmlsh_idx_t *kmlsh_idx_new(const kmlsh_t *lsh, int n);
+void kmlsh_idx_delete(kmlsh_idx_t *lshidx);
+kmlsh_idx_t *kmlsh_idx_new_compile_xvec(const kmlsh_t *lsh, const void *v, int n, int flags,
+                                        int vec_type);
+kmlsh_idx_t *kmlsh_idx_new_compile_bvec(const kmlsh_t *lsh, const unsigned char *v, int n,
+                                        int flags);
+kmlsh_idx_t *kmlsh_idx_new_compile_fvec(const kmlsh_t *lsh, const float *v, int n, int flags);
+int kmlsh_idx_get_nvec(const kmlsh_idx_t *lshidx, int h, int c);
+int kmlsh_idx_get_maxincell(const kmlsh_idx_t *lshidx, int h);
+int *kmlsh_idx_get_vecids(const kmlsh_idx_t *lshidx, int h, int c);
+void kmeans_cohash_xvec(const kmlsh_t *lsh, int h, const void *v, int n, int *perm,
+                        int *boundaries, int flags, int vec_type);
+void kmeans_cohash_bvec(const kmlsh_t *lsh, int h, const unsigned char *v, int n, int *perm,
+                        int *boundaries, int flags);
+void kmeans_cohash_fvec(const kmlsh_t *lsh, int h, const float *v, int n, int *perm,
+                        int *boundaries, int flags);
+
+/* yael/kmlsh.h:175-184 (yael/kmlsh.c:526-611): same files; an I/O error
+ * prints and exits(1).  kmlsh_idx_write checks each record's write status
+ * (the reference compares the second one with nclust + 1 and so exits). */
+void kmlsh_write(const char *filename, const kmlsh_t *lsh);
+void kmlsh_read(const char *filename, const kmlsh_t *lsh);
+void kmlsh_idx_write(const char *filename, const kmlsh_idx_t *lshidx);
+void kmlsh_idx_read(const char *filename, kmlsh_idx_t *lshidx);
+
 /* Vector files (host code, doc/file_format.rst): records of an int32
  * dimension d followed by d floats (.fvecs), int32 (.ivecs) or uint8
  * (.bvecs).  Same return values as the reference; where it asserts on a

@@ -705,3 +705,123 @@ void orc_hkm_quantize(int nlevel, int bf, int d, const float *centroids, int npt
     idx[i] = (int)vw;
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* k-means LSH (yael/kmlsh.c)                                           */
+
+/* nnlist_add (yael/kmlsh.c:60-84) on one list of k */
+static void orc_nnlist_add(int *idx, float *dis, int k, int elidx, float eldis)
+{
+  if (eldis > dis[0]) return;
+  for (int i = 0; i < k; i++)
+    if (idx[i] == elidx) return;
+  idx[0] = elidx;
+  dis[0] = eldis;
+  int posmax = 0; /* fvec_arg_max (yael/sorting.c:764-775) */
+  float m = dis[0];
+  for (int i = 1; i < k; i++)
+    if (dis[i] > m) { m = dis[i]; posmax = i; }
+  if (posmax == 0) return;
+  idx[0] = idx[posmax];
+  dis[0] = dis[posmax];
+  idx[posmax] = elidx;
+  dis[posmax] = eldis;
+}
+
+/* fvec_cpy_subvectors / b2fvec_cpy_subvectors (yael/vector.c:2478-2497) */
+static void orc_rows(const void *v, int vec_type, const int *ids, long m, int d, float *out)
+{
+  for (long i = 0; i < m; i++)
+    for (int j = 0; j < d; j++)
+      out[i * d + j] = vec_type == 0 ? ((const float *)v)[(long)ids[i] * d + j]
+                                     : (float)((const unsigned char *)v)[(long)ids[i] * d + j];
+}
+
+/* kmeans_cohash_xvec (yael/kmlsh.c:210-279): nearest centroid of every vector
+ * in blocks of KMLSH_BLOCK_SIZE, then the ids ordered by cell and the cell
+ * starts */
+static void orc_cohash(const float *C, int nclust, int d, const void *v, int n, int vec_type,
+                       int mode, int *perm, int *bnd)
+{
+  int *idx = malloc(sizeof(int) * (size_t)(n + 1));
+  float *dis = malloc(sizeof(float) * (size_t)(n + 1));
+  float *buf = malloc(sizeof(float) * 256 * (size_t)d);
+  int *ids = malloc(sizeof(int) * 256);
+  for (long i = 0; i < n; i += 256) {
+    int m = n - i < 256 ? (int)(n - i) : 256;
+    for (int j = 0; j < m; j++) ids[j] = (int)(i + j);
+    orc_rows(v, vec_type, ids, m, d, buf);
+    if (mode == ORC_PORT)
+      knn_full_port(2, m, nclust, d, 1, C, buf, NULL, idx + i, dis + i);
+    else
+      orc_knn_exact(m, nclust, d, 1, C, buf, idx + i, dis + i, NULL, 1);
+  }
+  int *nocc = calloc((size_t)nclust + 1, sizeof(int));
+  for (int c = 0; c <= nclust; c++) bnd[c] = 0;
+  for (long i = 0; i < n; i++) bnd[idx[i] + 1]++;
+  for (int c = 0; c < nclust; c++) bnd[c + 1] += bnd[c];
+  for (long i = 0; i < n; i++) perm[bnd[idx[i]] + nocc[idx[i]]++] = (int)i;
+  free(nocc); free(ids); free(buf); free(dis); free(idx);
+}
+
+void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k, int nhash,
+                   int vec_type, int mode, int *idx_out, float *dis_out)
+{
+  /* kmlsh_ann_xvec (yael/kmlsh.c:479-500) with one thread */
+  int nclust = (int)sqrt(nb);
+  int nlearn = nclust * 100;
+  if (nlearn > nb) nlearn = nb;
+  long cs = (long)nclust * d;
+  float *C = malloc(sizeof(float) * (size_t)(cs * nhash + 1));
+  /* kmlsh_learn_xvec (yael/kmlsh.c:133-185) */
+  float *vlearn = malloc(sizeof(float) * ((size_t)nlearn * d + 1));
+  int *sel = malloc(sizeof(int) * (size_t)(nlearn + 1));
+  for (int h = 0; h < nhash; h++) {
+    orc_random_init(nb, nlearn, (unsigned int)lrand48(), sel);
+    orc_rows(vb, vec_type, sel, nlearn, d, vlearn);
+    orc_kmeans(d, nlearn, nclust, 8, vlearn, 1 | ORC_KMEANS_INIT_RANDOM, 0, 1, C + h * cs,
+               NULL, NULL, NULL, mode, NULL);
+  }
+  free(sel);
+  free(vlearn);
+  /* kmlsh_idx_new_compile_xvec (yael/kmlsh.c:319-338) for base and queries */
+  int *pb = malloc(sizeof(int) * ((size_t)nb * nhash + 1));
+  int *pq = malloc(sizeof(int) * ((size_t)nq * nhash + 1));
+  int *bb = malloc(sizeof(int) * (size_t)(nclust + 1) * nhash);
+  int *bq = malloc(sizeof(int) * (size_t)(nclust + 1) * nhash);
+  for (int h = 0; h < nhash; h++) {
+    orc_cohash(C + h * cs, nclust, d, vb, nb, vec_type, mode, pb + (long)h * nb,
+               bb + (long)h * (nclust + 1));
+    orc_cohash(C + h * cs, nclust, d, vq, nq, vec_type, mode, pq + (long)h * nq,
+               bq + (long)h * (nclust + 1));
+  }
+  /* kmlsh_match_xvec (yael/kmlsh.c:376-456) */
+  for (long i = 0; i < (long)nq * k; i++) { idx_out[i] = -1; dis_out[i] = 1e30f; }
+  float *vbuf_b = malloc(sizeof(float) * ((size_t)nb * d + 1));
+  float *vbuf_q = malloc(sizeof(float) * ((size_t)nq * d + 1));
+  int *it = malloc(sizeof(int) * ((size_t)nq * k + 1));
+  float *dt = malloc(sizeof(float) * ((size_t)nq * k + 1));
+  for (int h = 0; h < nhash; h++) {
+    const int *hb = bb + (long)h * (nclust + 1), *hq = bq + (long)h * (nclust + 1);
+    for (int c = 0; c < nclust; c++) {
+      int nbc = hb[c + 1] - hb[c], nqc = hq[c + 1] - hq[c];
+      if (nbc == 0 || nqc == 0) continue;
+      const int *vidx_b = pb + (long)h * nb + hb[c];
+      const int *vidx_q = pq + (long)h * nq + hq[c];
+      orc_rows(vb, vec_type, vidx_b, nbc, d, vbuf_b);
+      orc_rows(vq, vec_type, vidx_q, nqc, d, vbuf_q);
+      int k2 = k < nbc ? k : nbc;
+      if (mode == ORC_PORT)
+        knn_full_port(2, nqc, nbc, d, k2, vbuf_b, vbuf_q, NULL, it, dt);
+      else
+        orc_knn_exact(nqc, nbc, d, k2, vbuf_b, vbuf_q, it, dt, NULL, 1);
+      for (long i = 0; i < (long)k2 * nqc; i++) it[i] = vidx_b[it[i]];
+      for (int i = 0; i < nqc; i++)
+        for (int j = 0; j < k2; j++)
+          orc_nnlist_add(idx_out + (long)vidx_q[i] * k, dis_out + (long)vidx_q[i] * k, k,
+                         it[(long)i * k2 + j], dt[(long)i * k2 + j]);
+    }
+  }
+  free(dt); free(it); free(vbuf_q); free(vbuf_b);
+  free(bq); free(bb); free(pq); free(pb); free(C);
+}

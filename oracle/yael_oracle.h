@@ -89,6 +89,14 @@ int orc_hkm_learn(int n, int d, int nlevel, int bf, const float *points,
 void orc_hkm_quantize(int nlevel, int bf, int d, const float *centroids, int npt,
                       const float *v, int *idx, int mode);
 
+/* k-means LSH search (yael/kmlsh.c:479-500: learn 133-185, cell assignment
+ * 210-279, per-cell search and merge 376-456) with one thread.  vec_type 0:
+ * float rows, 1: byte rows.  idx_out / dis_out (nq x k) receive the merged
+ * lists in the reference's slot order.  The RNG stream (lrand48 per
+ * partition, then the kmeans seed) is the reference's. */
+void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k, int nhash,
+                   int vec_type, int mode, int *idx_out, float *dis_out);
+
 /* RNG pieces, exposed so the tests can compare them with the GPU library's. */
 double orc_gaussrand_r(unsigned int *seed);
 void orc_random_init(int n, int k, unsigned int seed, int *sel);

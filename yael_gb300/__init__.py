@@ -99,6 +99,36 @@ SIGNATURES = {
     "bof_compute": (None, [c_int, c_int, P, c_int, P, P]),
     "bof_compute_ma": (None, [c_int, c_int, P, c_int, P, P, c_int, c_float, c_int]),
     "bof_compute_subsets": (None, [c_int, c_int, P, c_int, P, c_int, P, P, P]),
+    "nnlist_new": (P, [c_int, c_int]),
+    "nnlist_new_noalloc": (P, [c_int, c_int]),
+    "nnlist_delete": (None, [P]),
+    "nnlist_addn": (None, [P, c_int, c_int, P, P]),
+    "kmlsh_new": (P, [c_int, c_int, c_int]),
+    "kmlsh_delete": (None, [P]),
+    "kmlsh_learn_xvec": (None, [P, c_int, c_int, P, c_int, c_int]),
+    "kmlsh_new_learn_bvec": (P, [c_int, c_int, c_int, c_int, c_int, P, c_int]),
+    "kmlsh_new_learn_fvec": (P, [c_int, c_int, c_int, c_int, c_int, P, c_int]),
+    "kmlsh_match_xvec": (P, [P, P, P, c_int, P, P, c_int, c_int, c_int, c_int]),
+    "kmlsh_match_bvec": (P, [P, P, P, c_int, P, P, c_int, c_int, c_int]),
+    "kmlsh_match_fvec": (P, [P, P, P, c_int, P, P, c_int, c_int, c_int]),
+    "kmlsh_ann_xvec": (P, [P, c_int, P, c_int, c_int, c_int, c_int, c_int, c_int]),
+    "kmlsh_ann_bvec": (P, [P, c_int, P, c_int, c_int, c_int, c_int, c_int]),
+    "kmlsh_ann_fvec": (P, [P, c_int, P, c_int, c_int, c_int, c_int, c_int]),
+    "kmlsh_idx_new": (P, [P, c_int]),
+    "kmlsh_idx_delete": (None, [P]),
+    "kmlsh_idx_new_compile_xvec": (P, [P, P, c_int, c_int, c_int]),
+    "kmlsh_idx_new_compile_bvec": (P, [P, P, c_int, c_int]),
+    "kmlsh_idx_new_compile_fvec": (P, [P, P, c_int, c_int]),
+    "kmlsh_idx_get_nvec": (c_int, [P, c_int, c_int]),
+    "kmlsh_idx_get_maxincell": (c_int, [P, c_int]),
+    "kmlsh_idx_get_vecids": (P, [P, c_int, c_int]),
+    "kmeans_cohash_xvec": (None, [P, c_int, P, c_int, P, P, c_int, c_int]),
+    "kmeans_cohash_bvec": (None, [P, c_int, P, c_int, P, P, c_int]),
+    "kmeans_cohash_fvec": (None, [P, c_int, P, c_int, P, P, c_int]),
+    "kmlsh_write": (None, [ctypes.c_char_p, P]),
+    "kmlsh_read": (None, [ctypes.c_char_p, P]),
+    "kmlsh_idx_write": (None, [ctypes.c_char_p, P]),
+    "kmlsh_idx_read": (None, [ctypes.c_char_p, P]),
     "fvec_fwrite": (c_int, [P, P, c_int]),
     "ivec_fwrite": (c_int, [P, P, c_int]),
     "bvec_fwrite": (c_int, [P, P, c_int]),
