@@ -204,6 +204,57 @@ void bof_compute_subsets(int k, int d, const float *centroids, int n, const floa
                          float *desc);
 
 /* ------------------------------------------------------------------ */
+/* drop-in: Gaussian mixtures and Fisher vectors (yael/gmm.h)          */
+
+/* same layout as yael/gmm.h:19-25 */
+typedef struct gmm_s {
+  int d;        /* dimension */
+  int k;        /* components */
+  float *w;     /* k weights */
+  float *mu;    /* k x d means */
+  float *sigma; /* k x d diagonal variances */
+} gmm_t;
+
+/* flag bits, same values as yael/gmm.h:28-41 */
+#define YAEL_GMM_FLAGS_W 1
+#define YAEL_GMM_FLAGS_NO_NORM 2
+#define YAEL_GMM_FLAGS_1SIGMA 4
+#define YAEL_GMM_FLAGS_SIGMA 8
+#define YAEL_GMM_FLAGS_MU 16
+#define YAEL_GMM_FLAGS_PURE_KMEANS 32
+
+/* yael/gmm.h:57-59 (yael/gmm.c:436-502): the drop-in kmeans, then EM on the
+ * GPU (posteriors and posterior-weighted moments per iteration, parameters on
+ * the host) until the sum of the means repeats or niter iterations.  Returns
+ * a malloc'd mixture (gmm_delete). */
+gmm_t *gmm_learn(int d, int n, int k, int niter, const float *v, int nt, int seed, int nredo,
+                 int flags);
+/* yael/gmm.h:63-66 (yael/gmm.c:794-807, 43-49) */
+void gmm_print(const gmm_t *g);
+void gmm_delete(gmm_t *g);
+/* yael/gmm.h:74-77, 135-140 (yael/gmm.c:305-362, 862-870): p (n x k) =
+ * p(component | vector); squared Mahalanobis distances in direct form;
+ * n_thread is ignored */
+void gmm_compute_p(int n, const float *v, const gmm_t *g, float *p, int flags);
+void gmm_compute_p_thread(int n, const float *v, const gmm_t *g, float *p, int flags,
+                          int n_thread);
+/* yael/gmm.h:95-107 (yael/gmm.c:505-725): Fisher vectors from the
+ * posterior-weighted moments (FP64 sums on the GPU) */
+void gmm_fisher(int n, const float *v, const gmm_t *g, int flags, float *fisher_vector_out);
+void gmm_fisher_from_posteriors(int n, const float *v, const gmm_t *g, int flags,
+                                const float *p, float *fisher_vector_out);
+size_t gmm_fisher_sizeof(const gmm_t *g, int flags);
+/* yael/gmm.h:121-124 (yael/gmm.c:728-791): Q (K x N posteriors), sgmm (mean
+ * then variance, D each), ll (D x N: coordinate d of vector i at ll[d*N+i]);
+ * sdesc = D x K mean terms then D x K variance terms */
+void gmm_fisher_spatial(int N, int K, int D, const float *Q, const float *sgmm,
+                        const float *ll, float *sdesc);
+/* yael/gmm.h:128-131 (yael/gmm.c:810-850): d, k, w, mu, sigma as raw int32 /
+ * float32; an I/O error prints and aborts */
+void gmm_write(const gmm_t *g, FILE *f);
+gmm_t *gmm_read(FILE *f);
+
+/* ------------------------------------------------------------------ */
 /* drop-in: k-means LSH (yael/kmlsh.h)                                 */
 
 /* same layouts as yael/kmlsh.h:24-29, 62-67, 74-80 */

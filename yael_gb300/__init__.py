@@ -99,6 +99,17 @@ SIGNATURES = {
     "bof_compute": (None, [c_int, c_int, P, c_int, P, P]),
     "bof_compute_ma": (None, [c_int, c_int, P, c_int, P, P, c_int, c_float, c_int]),
     "bof_compute_subsets": (None, [c_int, c_int, P, c_int, P, c_int, P, P, P]),
+    "gmm_learn": (P, [c_int, c_int, c_int, c_int, P, c_int, c_int, c_int, c_int]),
+    "gmm_print": (None, [P]),
+    "gmm_delete": (None, [P]),
+    "gmm_compute_p": (None, [c_int, P, P, P, c_int]),
+    "gmm_compute_p_thread": (None, [c_int, P, P, P, c_int, c_int]),
+    "gmm_fisher": (None, [c_int, P, P, c_int, P]),
+    "gmm_fisher_from_posteriors": (None, [c_int, P, P, c_int, P, P]),
+    "gmm_fisher_sizeof": (ctypes.c_size_t, [P, c_int]),
+    "gmm_fisher_spatial": (None, [c_int, c_int, c_int, P, P, P, P]),
+    "gmm_write": (None, [P, P]),
+    "gmm_read": (P, [P]),
     "nnlist_new": (P, [c_int, c_int]),
     "nnlist_new_noalloc": (P, [c_int, c_int]),
     "nnlist_delete": (None, [P]),
