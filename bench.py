@@ -284,6 +284,152 @@ def run_clustering(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+class _quiet_stdout:
+    """Silences the C library's progress lines on file descriptor 1 (the
+    reference's k-means / EM / LSH chatter) so that the JSON line stays alone."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        self.null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.null, 1)
+
+    def __exit__(self, *exc):
+        ctypes.CDLL(None).fflush(None)
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        os.close(self.null)
+
+
+def run_callers(args, world, rank, local):
+    """The path's callers, timed through their drop-in calls with host buffers
+    (host <-> device copies included): gmm_learn / gmm_compute_p / gmm_fisher,
+    and kmlsh_ann_fvec.  The CPU figure is the oracle's restatement on a
+    bounded sample, one thread."""
+    import torch
+    import yael_gb300 as yg
+    from yael_gb300 import synth
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from _util import oracle, ptr
+    torch.cuda.set_device(local)
+    L = yg.lib()
+    for name, (res, argt) in yg.SIGNATURES.items():
+        if name.startswith(("gmm_", "kmlsh_", "nnlist_")):
+            getattr(L, name).restype = res
+            getattr(L, name).argtypes = argt
+    os.environ["YAEL_GPU_PRECISION"] = args.prec
+    line = {"n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic", "dtype": "f32" if args.workload == "gmm" else args.prec,
+            "steps": 1, "warmup": 1}
+    if args.workload == "gmm":
+        import gmm_oracle as go
+        n = args.n or 1_000_000
+        d, k, niter = 128, 256, args.niter or 10
+        v, _, _ = synth.gaussian_mixture(n, d, k, 0.5, seed=21)
+        flags = go.FLAGS_W
+
+        def learn():
+            t0 = time.perf_counter()
+            with _quiet_stdout():
+                gp = L.gmm_learn(d, n, k, niter, ptr(v), 1, 1, 1, flags)
+            return gp, time.perf_counter() - t0
+
+        gp, _ = learn()  # warm-up
+        L.gmm_delete(gp)
+        C = np.zeros((k, d), np.float32)
+        t0 = time.perf_counter()
+        with _quiet_stdout():
+            L.kmeans(d, n, k, niter, ptr(v), 1 | yg.KMEANS_QUIET, 1, 1, ptr(C), None, None, None)
+        t_seed = time.perf_counter() - t0
+        gp, t_learn = learn()
+        p = np.empty((n, k), np.float32)
+        t0 = time.perf_counter()
+        L.gmm_compute_p(n, ptr(v), gp, ptr(p), flags)
+        t_p = time.perf_counter() - t0
+        fl = go.FLAGS_W | go.FLAGS_MU | go.FLAGS_SIGMA
+        fv = np.empty(L.gmm_fisher_sizeof(gp, fl), np.float32)
+        t0 = time.perf_counter()
+        L.gmm_fisher(n, ptr(v), gp, fl, ptr(fv))
+        t_f = time.perf_counter() - t0
+        t_em = max(t_learn - t_seed, 1e-9)
+        line.update({"metric": "GMM EM iterations/s (gmm_learn, k-means seeding excluded)",
+                     "unit": "EM iterations/s", "value": niter / t_em,
+                     "ms_per_step": 1e3 * t_em / niter,
+                     "config": {"workload": f"gmm_learn n={n} d={d} k={k} niter={niter} "
+                                            f"flags=GMM_FLAGS_W, Gaussian mixture (k comps, "
+                                            f"sigma 0.5)", "n": n, "d": d, "k": k},
+                     "gmm_learn_seconds": t_learn, "kmeans_seeding_seconds": t_seed,
+                     "e2e": {"gmm_compute_p_vectors_per_s": n / t_p,
+                             "gmm_fisher_w_mu_sigma_vectors_per_s": n / t_f,
+                             "h2d_bytes_per_step": 4 * n * d, "d2h_bytes_per_step": 4 * n * k}})
+        L.gmm_delete(gp)
+        if not args.no_cpu:
+            # one EM iteration of the FP64 restatement on n / 100 vectors, scaled to n
+            sub = np.ascontiguousarray(v[: n // 100])
+            rng = np.random.default_rng(0)
+            mu0 = sub[rng.choice(sub.shape[0], k, replace=False)]
+            w0 = np.full(k, 1.0 / k, np.float32)
+            s0 = np.ones((k, d), np.float32)
+            t0 = time.perf_counter()
+            pp = go.compute_p(sub, w0, mu0, s0, flags)
+            go.compute_params(sub, pp, mu0, flags)
+            cdt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": (sub.shape[0] / n) / cdt, "unit": "EM iterations/s",
+                                    "cores": 1, "kind": "port",
+                                    "sample": f"one EM iteration (posteriors + parameters) of "
+                                              f"the FP64 numpy restatement on {sub.shape[0]} "
+                                              f"vectors, scaled to n"}
+    else:
+        nb, nq, d, k, nhash = (args.n or 1_000_000), 10_000, 128, 100, 4
+        b = synth.sift_like(nb, d, seed=1)
+        q = synth.sift_like(nq, d, seed=2)
+
+        def ann(bb, qq):
+            t0 = time.perf_counter()
+            with _quiet_stdout():
+                lp = L.kmlsh_ann_fvec(ptr(bb), bb.shape[0], ptr(qq), qq.shape[0], d, k, nhash, 1)
+            dt = time.perf_counter() - t0
+            nl = ctypes.cast(lp, ctypes.POINTER(ctypes.c_long))
+            idx = np.ctypeslib.as_array(ctypes.cast(nl[2], ctypes.POINTER(ctypes.c_int)),
+                                        shape=(qq.shape[0] * k,)).reshape(-1, k).copy()
+            L.nnlist_delete(lp)
+            return idx, dt
+
+        ann(b[:100_000], q[:1000])  # warm-up
+        idx, dt = ann(b, q)
+        exact = np.empty((nq, k), np.int32)
+        dis = np.empty((nq, k), np.float32)
+        L.knn_full_thread(2, nq, nb, d, k, ptr(b), ptr(q), None, ptr(exact), ptr(dis), 1)
+        recall = float(np.mean([len(np.intersect1d(idx[i], exact[i])) for i in range(nq)]) / k)
+        line.update({"metric": "k-means LSH queries/s (kmlsh_ann_fvec: learn, index, search)",
+                     "unit": "queries/s", "value": nq / dt, "ms_per_step": 1e3 * dt,
+                     "config": {"workload": f"kmlsh_ann_fvec nb={nb} nq={nq} d={d} k={k} "
+                                            f"nhash={nhash} (nclust={int(np.sqrt(nb))}), "
+                                            f"SIFT-like data", "nb": nb, "nq": nq, "d": d,
+                                "k": k},
+                     "recall_at_k_vs_exact": recall})
+        if not args.no_cpu:
+            sb, sq = np.ascontiguousarray(b[:100_000]), np.ascontiguousarray(q[:1000])
+            _, gdt = ann(sb, sq)
+            o = oracle()
+            o.orc_kmlsh_ann.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_int] + [ctypes.c_int] * 5 + [ctypes.c_void_p] * 2
+            oi = np.empty((1000, k), np.int32)
+            od = np.empty((1000, k), np.float32)
+            t0 = time.perf_counter()
+            o.orc_kmlsh_ann(ptr(sb), 100_000, ptr(sq), 1000, d, k, nhash, 0, 0, ptr(oi), ptr(od))
+            cdt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": 1000 / cdt, "unit": "queries/s", "cores": 1,
+                                    "kind": "port",
+                                    "sample": "the reference's algorithm in its own arithmetic "
+                                              "(oracle port) at nb=100000 nq=1000; the GPU on "
+                                              "the same sample: "
+                                              f"{1000 / gdt:.1f} queries/s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def batch_sizes(npairs, seed):
     """Pair sizes of the batched uneven k-NN configuration: queries log-uniform
     in [1, 8192], base rows log-uniform in [10,000, 2,000,000]."""
@@ -474,11 +620,21 @@ def main():
     ap.add_argument("--e2e-pairs", type=int, default=64,
                     help="knn_batch: pairs timed end to end from host buffers")
     ap.add_argument("--workload", default="knn",
-                    choices=["knn", "kmeans1", "kmeans3", "hkm4", "knn_batch"],
+                    choices=["knn", "kmeans1", "kmeans3", "hkm4", "knn_batch", "gmm", "kmlsh"],
                     help="knn: the headline configuration; the others are the k-means / hkm "
-                         "configurations, reported separately")
+                         "configurations and the path's callers (gmm, kmlsh), reported "
+                         "separately")
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.workload in ("gmm", "kmlsh"):
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable":
+                                  "the reference's CPU figure for this workload is the "
+                                  "cpu_baseline of the ours line"}), flush=True)
+            return
+        run_callers(args, world, rank, local)
+        return
     if args.workload == "knn_batch" and args.impl != "reference":
         run_knn_batch(args, world, rank, local)
         return

@@ -102,6 +102,38 @@ int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), def
 // and reported on stderr, one line per pass
 bool trace_enabled();
 
+// A device array owned by the host scope that holds it (freed on
+// destruction).  get() grows it to at least `want` elements, dropping the
+// contents; an allocation failure records E_NOMEM and aborts through
+// fatal_last(where), the convention of the drop-in entry points.
+template <typename T>
+struct DevArray {
+  T *p = nullptr;
+  long n = 0;
+  DevArray() = default;
+  DevArray(const DevArray &) = delete;
+  DevArray &operator=(const DevArray &) = delete;
+  ~DevArray() {
+    if (p) cudaFree(p);
+  }
+  T *get(const char *where, long want) {
+    if (want > n) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      n = 0;
+      const size_t bytes = sizeof(T) * (size_t)(want > 1 ? want : 1);
+      const cudaError_t e = cudaMalloc((void **)&p, bytes);
+      if (e != cudaSuccess) {
+        p = nullptr;
+        set_error(E_NOMEM, "cudaMalloc of %zu bytes: %s", bytes, cudaGetErrorString(e));
+        fatal_last(where);
+      }
+      n = want;
+    }
+    return p;
+  }
+};
+
 // Raises kernel func's dynamic shared-memory limit to at least bytes on the
 // current device, once per (kernel, device, size); thread safe.
 int ensure_smem(const void *func, size_t bytes);

@@ -240,33 +240,6 @@ void launched(const char *where) {
   ok(where, cudaGetLastError());
 }
 
-template <typename T>
-struct DevArray {
-  T *p = nullptr;
-  long n = 0;
-  DevArray() = default;
-  DevArray(const DevArray &) = delete;
-  DevArray &operator=(const DevArray &) = delete;
-  ~DevArray() {
-    if (p) cudaFree(p);
-  }
-  T *get(const char *where, long want) {
-    if (want > n) {
-      if (p) cudaFree(p);
-      p = nullptr;
-      n = 0;
-      const cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * (size_t)std::max(want, 1L));
-      if (e != cudaSuccess) {
-        set_error(E_NOMEM, "cudaMalloc of %ld bytes: %s", (long)sizeof(T) * want,
-                  cudaGetErrorString(e));
-        die(where);
-      }
-      n = want;
-    }
-    return p;
-  }
-};
-
 // The moments of a posterior matrix against a set of vectors, as FP64:
 // s0[j] = sum_i p_ij, s1[j*d + l] = sum_i p_ij x_il, s2[j*d + l] = sum_i p_ij x_il^2
 struct Moments {

@@ -97,22 +97,6 @@ struct Cell {
   long boff, qoff, ooff;
 };
 
-template <typename T>
-struct DevBuf {
-  T *p = nullptr;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  void alloc(const char *where, long n) {
-    const cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * (size_t)(n > 0 ? n : 1));
-    if (e != cudaSuccess) {
-      yg::set_error(yg::E_NOMEM, "cudaMalloc of %ld bytes: %s", (long)(sizeof(T) * n),
-                    cudaGetErrorString(e));
-      yg::fatal_last(where);
-    }
-  }
-};
-
 void cuda_ok(const char *where, cudaError_t e) {
   if (e != cudaSuccess) {
     yg::set_error(yg::E_CUDA, "%s", cudaGetErrorString(e));
@@ -123,12 +107,12 @@ void cuda_ok(const char *where, cudaError_t e) {
 void search_cells(const std::vector<Cell> &cells, int d, const float *hb, long bt,
                   const float *hq, long qt, int *hi, float *hd, long ot) {
   const char *where = "kmlsh_match_xvec";
-  DevBuf<float> db, dq, dd;
-  DevBuf<int> di;
-  db.alloc(where, bt);
-  dq.alloc(where, qt);
-  di.alloc(where, ot);
-  dd.alloc(where, ot);
+  yg::DevArray<float> db, dq, dd;
+  yg::DevArray<int> di;
+  db.get(where, bt);
+  dq.get(where, qt);
+  di.get(where, ot);
+  dd.get(where, ot);
   cuda_ok(where, cudaMemcpy(db.p, hb, sizeof(float) * (size_t)bt, cudaMemcpyHostToDevice));
   cuda_ok(where, cudaMemcpy(dq.p, hq, sizeof(float) * (size_t)qt, cudaMemcpyHostToDevice));
   std::vector<int> ks;
