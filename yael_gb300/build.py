@@ -16,9 +16,10 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libyael_gb300.so")
-# the command-line program of yael's progs/knn.c, linked against the library
-CLI_SRC = os.path.join(HERE, "cli", "yael_knn.cpp")
-CLI = os.path.join(HERE, "bin", "yael_knn")
+# the command-line programs of yael's progs/knn.c and progs/kmeans.c, linked
+# against the library
+CLIS = [(os.path.join(HERE, "cli", name + ".cpp"), os.path.join(HERE, "bin", name))
+        for name in ("yael_knn", "yael_kmeans")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -81,17 +82,19 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         os.replace(tmp, LIB)
         if verbose:
             print(f"[yael_gb300] linked {LIB}", file=sys.stderr)
-    if _stale(CLI, [CLI_SRC, LIB] + hdrs):
-        os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    for cli_src, cli in CLIS:
+        if not _stale(cli, [cli_src, LIB] + hdrs):
+            continue
+        os.makedirs(os.path.dirname(cli), exist_ok=True)
         cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
-        cmd = [cxx, "-O2", "-std=c++17", "-o", CLI + ".tmp", CLI_SRC, "-L" + HERE, "-lyael_gb300",
+        cmd = [cxx, "-O2", "-std=c++17", "-o", cli + ".tmp", cli_src, "-L" + HERE, "-lyael_gb300",
                "-Wl,-rpath,$ORIGIN/.."]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"building yael_knn failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(CLI + ".tmp", CLI)
+            raise RuntimeError(f"building {os.path.basename(cli)} failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(cli + ".tmp", cli)
         if verbose:
-            print(f"[yael_gb300] built {CLI}", file=sys.stderr)
+            print(f"[yael_gb300] built {cli}", file=sys.stderr)
     return LIB
 
 
