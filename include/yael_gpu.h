@@ -1,7 +1,9 @@
 /*
  * yael_gpu.h -- C ABI of the GB300 (sm_103a) implementation of yael's
  * distance-GEMM path: exact k-NN, cross distances, k-means, hierarchical
- * k-means.
+ * k-means; and of the path's callers and data formats: VLAD /
+ * bag-of-features, Gaussian mixtures and Fisher vectors, k-means LSH, the
+ * vector files.
  *
  * The first group of functions are drop-in replacements: same symbol names,
  * argument order, meaning, ownership and error convention as the reference
