@@ -176,7 +176,8 @@ def test_spatial_restatement_pinned_to_reference():
     close(run_spatial(R, Q, sgmm, ll), go.fisher_spatial(Q, sgmm, ll), FV_RTOL, FV_ATOL)
 
 
-@pytest.mark.parametrize("flags", [go.FLAGS_W, go.FLAGS_W | go.FLAGS_1SIGMA, 0])
+@pytest.mark.parametrize("flags", [go.FLAGS_W, go.FLAGS_W | go.FLAGS_1SIGMA, 0,
+                                   go.FLAGS_W | go.FLAGS_PURE_KMEANS])
 def test_learn_restatement_pinned_to_reference(flags):
     """k-means seeding in the reference's arithmetic (identical centroids and
     distances), then EM: the reference's float32 parameters against the FP64

@@ -108,6 +108,25 @@ def test_restatement_pinned_to_reference():
             assert (got[0] >= 0).all()
 
 
+def test_restatement_small_cells_pinned_to_reference():
+    """400 base vectors in 20 cells per partition and k = 30: most cells hold
+    fewer than k vectors (k2 = cell size), and the lists keep empty slots
+    (-1, 1e30) where the partitions found fewer than k distinct neighbours."""
+    R = reference()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    bind(R)
+    vb, vq = clustered(3, 400, 60, 8, ncl=10)
+    for nhash in (1, 3):
+        srand48(300 + nhash)
+        got = lib_ann(R, vb, vq, 30, nhash)
+        srand48(300 + nhash)
+        exp = orc_ann(vb, vq, 30, nhash, 0, ORC_PORT)
+        np.testing.assert_array_equal(got[0], exp[0])
+        np.testing.assert_array_equal(got[1], exp[1])
+        assert (got[0] == -1).any() and (got[0] >= 0).any()
+
+
 def test_nnlist_merge_against_the_reference():
     """Repeated ids, equal distances and values above the current largest, in
     the same sequence: the same lists, slot for slot."""
