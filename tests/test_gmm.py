@@ -265,3 +265,32 @@ def test_gpu_learn(flags):
     got = run_learn(L_, v, k, niter, seed, flags)
     mu0, dis0 = seeded_kmeans(v, k, niter, seed, ORC_EXACT)
     check_learn(got, go.learn(v, k, niter, mu0, dis0, flags))
+
+
+def test_numpy_front_end_plumbing(monkeypatch, tmp_path):
+    """ynumpy's gmm_learn / gmm_read / fisher (yael/ynumpy.py:268-353): the
+    module's wrappers, run over the reference library (same C ABI), return
+    what direct calls into it return -- the argument and result handling
+    checked without a GPU.  The GPU library behind them is checked above."""
+    R = ref_lib()
+    v, _, _ = synth.gaussian_mixture(1500, 6, 4, 0.9, seed=12)
+    n, d = v.shape
+    srand48_ = ctypes.CDLL(None).srand48
+    srand48_(5)
+    exp = run_learn(R, v, 4, 5, 3, go.FLAGS_W)
+    monkeypatch.setattr(yg, "_lib", R)
+    srand48_(5)
+    got = yg.gmm_learn(v, 4, nt=1, niter=5, seed=3, use_weights=True)
+    for a, b in zip(got, exp):
+        np.testing.assert_array_equal(a, b)
+    g, keep = make_gmm(*exp)
+    for include, flags in (("mu", go.FLAGS_MU), ("mu sigma w", go.FLAGS_MU | go.FLAGS_SIGMA |
+                                                   go.FLAGS_W), ("sigma", go.FLAGS_SIGMA)):
+        np.testing.assert_array_equal(yg.fisher(exp, v, include=include),
+                                      run_fisher(R, v, g, flags))
+    fn = str(tmp_path / "g.gmm").encode()
+    fh = libc.fopen(fn, b"w")
+    R.gmm_write(ctypes.byref(g), fh)
+    libc.fclose(fh)
+    for a, b in zip(yg.gmm_read(fn.decode()), exp):
+        np.testing.assert_array_equal(a, b)

@@ -258,3 +258,34 @@ def test_raw_and_text_against_the_reference(tmp_path, data):
         assert L_.fvecs_read_txt(path, 24, nread, ptr(a1)) == R.fvecs_read_txt(path, 24, nread,
                                                                               ptr(a2))
         np.testing.assert_array_equal(a1, a2)
+
+
+def test_numpy_front_end(tmp_path, data):
+    """The ynumpy file helpers (yael/ynumpy.py:158-226) over the library's
+    readers and writers: round trips, nmax, appends to an open file, errors."""
+    f, i, b = data
+    fp, ip, bp = (str(tmp_path / n) for n in ("a.fvecs", "a.ivecs", "a.bvecs"))
+    yg.fvecs_write(fp, f)
+    yg.ivecs_write(ip, i)
+    yg.bvecs_write(bp, b)
+    assert yg.fvecs_fsize(fp) == (37, 24)
+    np.testing.assert_array_equal(yg.fvecs_read(fp), f)
+    np.testing.assert_array_equal(yg.fvecs_read(fp, nmax=5), f[:5])
+    np.testing.assert_array_equal(yg.fvecs_read(fp, nmax=100), f)
+    np.testing.assert_array_equal(yg.ivecs_read(ip), i)
+    np.testing.assert_array_equal(np.stack(records(bp, np.uint8)), b)
+    with open(str(tmp_path / "app.fvecs"), "wb") as fh:
+        fh.write(np.int32(24).tobytes() + f[0].tobytes())
+        yg.fvecs_fwrite(fh, f[1:4])
+        yg.fvecs_fwrite(fh, f[4:6])
+    np.testing.assert_array_equal(yg.fvecs_read(str(tmp_path / "app.fvecs")), f[:6])
+    empty = str(tmp_path / "e.fvecs")
+    open(empty, "wb").close()
+    assert yg.fvecs_read(empty).shape == (0, 0)
+    assert yg.fvecs_read(empty, nmax=3).shape == (0, 0)
+    with pytest.raises(IOError):
+        yg.fvecs_read(str(tmp_path / "none.fvecs"), nmax=3)
+    with pytest.raises(IOError):
+        yg.ivecs_read(str(tmp_path / "none.ivecs"))
+    with pytest.raises(IOError):
+        yg.fvecs_fsize(str(tmp_path / "none.fvecs"))

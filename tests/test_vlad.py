@@ -107,3 +107,20 @@ def test_gpu_descriptors_bit_identical(seed):
     got = run_all(yg.lib(), C, v, w, si, se)
     for g, e in zip(got, expected(C, v, w, si, se)):
         np.testing.assert_array_equal(g, e)
+
+
+def test_numpy_front_end_plumbing(monkeypatch):
+    """ynumpy.vlad (yael/ynumpy.py:356-369) over the reference library (same C
+    ABI) returns what a direct vlad_compute call into it returns."""
+    R = reference()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    res, args = yg.SIGNATURES["vlad_compute"]
+    R.vlad_compute.restype = res
+    R.vlad_compute.argtypes = args
+    C, v, w, si, se = data(7)
+    k, d = C.shape
+    exp = np.zeros((k, d), np.float32)
+    R.vlad_compute(k, d, ptr(C), v.shape[0], ptr(v), ptr(exp))
+    monkeypatch.setattr(yg, "_lib", R)
+    np.testing.assert_array_equal(yg.vlad(C, v), exp)

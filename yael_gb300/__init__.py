@@ -2,9 +2,12 @@
 
 The product is the C-ABI library ``libyael_gb300.so`` (declared in
 ``include/yael_gpu.h``): exact k-NN, cross distances, k-means and hierarchical
-k-means with yael's own symbol names and conventions.  This module loads it
-with ctypes and mirrors the reference's numpy front end (yael/ynumpy.py:46-130:
-``knn``, ``cross_distances``, ``kmeans``) on top of it.
+k-means, and their callers (VLAD / bag-of-features, Gaussian mixtures and
+Fisher vectors, k-means LSH) and vector files, with yael's own symbol names
+and conventions.  This module loads it with ctypes and mirrors the reference's
+numpy front end on top of it (yael/ynumpy.py:46-130, 158-369: ``knn``,
+``cross_distances``, ``kmeans``, the ``fvecs`` / ``ivecs`` / ``bvecs``
+helpers, ``gmm_learn``, ``gmm_read``, ``fisher``, ``vlad``).
 
 There is no CPU fallback: if the library (or a GPU) is missing, calls raise.
 """
@@ -339,6 +342,214 @@ def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
                      "n_second": opts.n_second, "n_band": opts.n_band,
                      "ms_assign": opts.ms_assign, "ms_update": opts.ms_update}
     return res
+
+
+class Gmm(ctypes.Structure):
+    """gmm_t (yael/gmm.h:19-25)."""
+    _fields_ = [("d", c_int), ("k", c_int), ("w", ctypes.POINTER(c_float)),
+                ("mu", ctypes.POINTER(c_float)), ("sigma", ctypes.POINTER(c_float))]
+
+
+GMM_FLAGS_W, GMM_FLAGS_NO_NORM, GMM_FLAGS_1SIGMA = 1, 2, 4
+GMM_FLAGS_SIGMA, GMM_FLAGS_MU, GMM_FLAGS_PURE_KMEANS = 8, 16, 32
+
+_libc_handle = None
+
+
+def _libc():
+    global _libc_handle
+    if _libc_handle is None:
+        c = ctypes.CDLL(None)
+        c.fopen.restype = P
+        c.fopen.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        c.fdopen.restype = P
+        c.fdopen.argtypes = [c_int, ctypes.c_char_p]
+        c.fclose.argtypes = [P]
+        c.free.argtypes = [P]
+        _libc_handle = c
+    return _libc_handle
+
+
+def _fopen(filename, mode):
+    fh = _libc().fopen(os.fsencode(filename), mode.encode())
+    if not fh:
+        raise IOError(f"cannot open {filename}")
+    return fh
+
+
+def _take(p, n, ctype, dtype):
+    """copy n elements of a malloc'd C array into numpy, then free it"""
+    a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctype)), shape=(n,)).astype(dtype) \
+        if n > 0 else np.zeros(0, dtype)
+    _libc().free(p)
+    return a
+
+
+def _rows(a, dtype, name):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    if a.ndim != 2:
+        raise ValueError(f"{name}: expected a 2-D array")
+    return a
+
+
+def fvecs_fsize(filename):
+    """(n, d) of a .fvecs file (yael/ynumpy.py:158-163)."""
+    d, n = c_int(), c_int()
+    lib().fvecs_fsize(os.fsencode(filename), ctypes.byref(d), ctypes.byref(n))
+    if n.value < 0 and d.value < 0:
+        raise IOError("fvecs_fsize: cannot read " + str(filename))
+    return n.value, d.value
+
+
+def fvecs_read(filename, nmax=-1, c_contiguous=True):
+    """The vectors of a .fvecs file as an (n, d) float32 array
+    (yael/ynumpy.py:165-186): all of them, or at most nmax."""
+    if nmax < 0:
+        fv = np.fromfile(filename, dtype=np.float32)
+        if fv.size == 0:
+            return np.zeros((0, 0))
+        dim = int(fv.view(np.int32)[0])
+        assert dim > 0
+        fv = fv.reshape(-1, 1 + dim)
+        if not (fv.view(np.int32)[:, 0] == dim).all():
+            raise IOError("non-uniform vector sizes in " + str(filename))
+        fv = fv[:, 1:]
+        return fv.copy() if c_contiguous else fv
+    fh = _fopen(filename, "r")
+    d, out = c_int(), P()
+    n = lib().fvecs_new_fread_max(fh, ctypes.byref(d), ctypes.byref(out), nmax)
+    _libc().fclose(fh)
+    if n == -1:
+        raise IOError("could not read " + str(filename))
+    dd = d.value if n > 0 else 0
+    return _take(out, n * dd, c_float, np.float32).reshape(n, dd)
+
+
+def ivecs_read(filename):
+    """The vectors of a .ivecs file as an (n, d) int32 array
+    (yael/ynumpy.py:188-196)."""
+    d, out = c_int(), P()
+    n = lib().ivecs_new_read(os.fsencode(filename), ctypes.byref(d), ctypes.byref(out))
+    if n == -1:
+        raise IOError("could not read " + str(filename))
+    dd = d.value if n > 0 else 0
+    return _take(out, n * dd, c_int, np.int32).reshape(n, dd)
+
+
+def fvecs_write(filename, matrix):
+    """yael/ynumpy.py:200-205"""
+    m = _rows(matrix, np.float32, "fvecs_write")
+    n, d = m.shape
+    if lib().fvecs_write(os.fsencode(filename), d, n, _ptr(m)) != n:
+        raise IOError("write error " + str(filename))
+
+
+def fvecs_fwrite(f, matrix):
+    """Append the rows of matrix to the open binary file f (yael/ynumpy.py:208-213)."""
+    m = _rows(matrix, np.float32, "fvecs_fwrite")
+    n, d = m.shape
+    f.flush()
+    fh = _libc().fdopen(os.dup(f.fileno()), b"ab")
+    if not fh:
+        raise IOError("fvecs_fwrite: cannot write to the file")
+    ret = lib().fvecs_fwrite(fh, d, n, _ptr(m))
+    _libc().fclose(fh)
+    if ret != n:
+        raise IOError("write error")
+
+
+def bvecs_write(filename, matrix):
+    """yael/ynumpy.py:216-221"""
+    m = _rows(matrix, np.uint8, "bvecs_write")
+    n, d = m.shape
+    if lib().bvecs_write(os.fsencode(filename), d, n, _ptr(m)) != n:
+        raise IOError("write error " + str(filename))
+
+
+def ivecs_write(filename, matrix):
+    """The rows of an int32 matrix as an .ivecs file (yael/ynumpy.py:225-226
+    leaves this unimplemented; yael/vector.c:1524-1535 writes the format)."""
+    m = _rows(matrix, np.int32, "ivecs_write")
+    n, d = m.shape
+    if lib().ivecs_write(os.fsencode(filename), d, n, _ptr(m)) != n:
+        raise IOError("write error " + str(filename))
+
+
+def _gmm_to_numpy(gp):
+    """(w, mu, sigma) copies of a gmm_t (yael/ynumpy.py:268-275)."""
+    g = ctypes.cast(gp, ctypes.POINTER(Gmm)).contents
+    k, d = g.k, g.d
+    w = np.ctypeslib.as_array(g.w, shape=(k,)).copy()
+    mu = np.ctypeslib.as_array(g.mu, shape=(k * d,)).reshape(k, d).copy()
+    sigma = np.ctypeslib.as_array(g.sigma, shape=(k * d,)).reshape(k, d).copy()
+    return w, mu, sigma
+
+
+def _numpy_to_gmm(gmm_npy):
+    """A gmm_t over the arrays of (w, mu, sigma) (yael/ynumpy.py:283-300);
+    returns it with the float32 arrays it points into (keep them alive)."""
+    w, mu, sigma = (np.ascontiguousarray(a, dtype=np.float32) for a in gmm_npy)
+    k, d = mu.shape
+    assert sigma.shape == mu.shape and w.shape == (k,)
+    fp = ctypes.POINTER(c_float)
+    g = Gmm(d, k, w.ctypes.data_as(fp), mu.ctypes.data_as(fp), sigma.ctypes.data_as(fp))
+    return g, (w, mu, sigma)
+
+
+def gmm_learn(v, k, nt=1, niter=30, seed=0, redo=1, use_weights=True):
+    """A diagonal Gaussian mixture of k components: (w, mu, sigma)
+    (yael/ynumpy.py:303-320)."""
+    v = _f32(v)
+    n, d = v.shape
+    flags = GMM_FLAGS_W if use_weights else 0
+    gp = lib().gmm_learn(d, n, k, niter, _ptr(v), nt, seed, redo, flags)
+    try:
+        return _gmm_to_numpy(gp)
+    finally:
+        lib().gmm_delete(gp)
+
+
+def gmm_read(filename):
+    """(w, mu, sigma) of a file written by gmm_write (yael/ynumpy.py:323-329)."""
+    fh = _fopen(filename, "r")
+    gp = lib().gmm_read(fh)
+    _libc().fclose(fh)
+    try:
+        return _gmm_to_numpy(gp)
+    finally:
+        lib().gmm_delete(gp)
+
+
+def fisher(gmm_npy, v, include="mu"):
+    """The Fisher vector of the rows of v under the mixture (w, mu, sigma),
+    with the gradients named in include ('mu', 'sigma', 'w')
+    (yael/ynumpy.py:332-353)."""
+    v = _f32(v)
+    n, d = v.shape
+    g, keep = _numpy_to_gmm(gmm_npy)
+    assert d == g.d
+    flags = 0
+    if "mu" in include:
+        flags |= GMM_FLAGS_MU
+    if "sigma" in include:
+        flags |= GMM_FLAGS_SIGMA
+    if "w" in include:
+        flags |= GMM_FLAGS_W
+    out = np.zeros(lib().gmm_fisher_sizeof(ctypes.byref(g), flags), dtype=np.float32)
+    lib().gmm_fisher(n, _ptr(v), ctypes.byref(g), flags, _ptr(out))
+    return out
+
+
+def vlad(centroids, v):
+    """The VLAD descriptor (k, d) of the rows of v (yael/ynumpy.py:356-369)."""
+    v = _f32(v)
+    n, d = v.shape
+    c = _f32(centroids)
+    k, d2 = c.shape
+    assert d2 == d
+    out = np.zeros((k, d), dtype=np.float32)
+    lib().vlad_compute(k, d, _ptr(c), n, _ptr(v), _ptr(out))
+    return out
 
 
 def hkm(v, nlevel, bf, niter=15, small_nodes=False):
