@@ -39,3 +39,40 @@ def test_hkm_file_roundtrip(tmp_path):
     assert open(out, "rb").read() == open(path, "rb").read()
     L.hkm_delete(h)
     assert not L.hkm_read(str(tmp_path / "missing.hkm").encode())
+
+
+def test_hkm_files_against_the_reference(tmp_path):
+    """The reference library reads what this one writes and writes the same
+    bytes back; get_centroids agrees."""
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from _util import reference
+    R = reference()
+    if R is None:
+        import pytest
+        pytest.skip("reference library not built here (oracle/_ref)")
+    for name in ("hkm_read", "hkm_write", "hkm_delete", "hkm_get_centroids"):
+        res, args = yg.SIGNATURES[name]
+        getattr(R, name).restype = res
+        getattr(R, name).argtypes = args
+    L = yg.lib()
+    nlevel, bf, d = 3, 2, 5
+    rng = np.random.default_rng(1)
+    path = str(tmp_path / "a.hkm")
+    with open(path, "wb") as f:
+        f.write(struct.pack("iii", nlevel, bf, d))
+        for l in range(nlevel):
+            a = rng.standard_normal(bf ** (l + 1) * d).astype(np.float32)
+            f.write(struct.pack("i", a.size) + a.tobytes())
+    ours, theirs = L.hkm_read(path.encode()), R.hkm_read(path.encode())
+    o1, o2 = str(tmp_path / "o.hkm"), str(tmp_path / "r.hkm")
+    L.hkm_write(o1.encode(), theirs)
+    R.hkm_write(o2.encode(), ours)
+    assert open(o1, "rb").read() == open(o2, "rb").read() == open(path, "rb").read()
+    for l in range(nlevel):
+        for node in range(bf ** l):
+            a = ctypes.string_at(L.hkm_get_centroids(ours, l, node), 4 * bf * d)
+            b = ctypes.string_at(R.hkm_get_centroids(theirs, l, node), 4 * bf * d)
+            assert a == b
+    L.hkm_delete(ours)
+    R.hkm_delete(theirs)
