@@ -30,6 +30,22 @@ def srand48(seed):
     _libc.srand48(seed)
 
 
+def read_bytes(path):
+    """The contents of a file (path as str, bytes or PathLike), closed after reading."""
+    with open(path, "rb") as f:
+        return f.read()
+
+
+def read_text(path):
+    with open(path) as f:
+        return f.read()
+
+
+def write_text(path, text):
+    with open(path, "w") as f:
+        f.write(text)
+
+
 def build_oracle():
     if not os.path.exists(ORACLE_LIB) or any(
             os.path.getmtime(os.path.join(ORACLE_DIR, f)) > os.path.getmtime(ORACLE_LIB)

@@ -11,7 +11,8 @@ HEADER = os.path.join(ROOT, "include", "yael_gpu.h")
 
 
 def declared_functions():
-    src = open(HEADER).read()
+    with open(HEADER) as f:
+        src = f.read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     src = re.sub(r"//[^\n]*", "", src)
     src = re.sub(r"typedef\s+struct\s*\{.*?\}\s*\w+\s*;", "", src, flags=re.S)

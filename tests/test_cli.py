@@ -6,7 +6,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from _util import knn_exact
+from _util import knn_exact, read_bytes, read_text
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CLI = os.path.join(ROOT, "yael_gb300", "bin", "yael_knn")
@@ -27,7 +27,7 @@ def write_vecs(path, a, dtype):
 
 
 def read_vecs(path, dtype):
-    raw = open(path, "rb").read()
+    raw = read_bytes(path)
     out, pos = [], 0
     while pos < len(raw):
         d = int(np.frombuffer(raw, np.int32, 1, pos)[0])
@@ -135,4 +135,4 @@ def test_kmeans_program_matches_oracle(cli, tmp_path, fmt):
         np.testing.assert_array_equal(read_vecs(tmp_path / "c.fvecs", np.float32), C)
     else:
         want = "".join("".join(f"{x:f} " for x in row) + "\n" for row in C)
-        assert open(tmp_path / "c.txt").read() == want
+        assert read_text(tmp_path / "c.txt") == want

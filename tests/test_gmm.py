@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import yael_gb300 as yg
-from _util import ORACLE_DIR, oracle, reference
+from _util import ORACLE_DIR, oracle, read_bytes, reference
 from yael_gb300 import synth
 
 sys.path.insert(0, ORACLE_DIR)
@@ -199,7 +199,7 @@ def test_files(tmp_path):
     fh = libc.fopen(f1, b"w")
     L_.gmm_write(ctypes.byref(g), fh)
     libc.fclose(fh)
-    raw = open(f1, "rb").read()
+    raw = read_bytes(f1)
     assert raw == (np.array([5, 4], np.int32).tobytes() + w.tobytes() + mu.tobytes() +
                    sigma.tobytes())
     fh = libc.fopen(f1, b"r")
@@ -215,7 +215,7 @@ def test_files(tmp_path):
         fh = libc.fopen(f2, b"w")
         R.gmm_write(ctypes.byref(g), fh)
         libc.fclose(fh)
-        assert open(f2, "rb").read() == raw
+        assert read_bytes(f2) == raw
 
 
 # ---------------------------------------------------------------- GPU

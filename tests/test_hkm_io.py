@@ -2,12 +2,12 @@
 format of yael/hkm.c:181-232 -- int nlevel, bf, d, then one fvec record
 (int count, count floats) per level."""
 import ctypes
-import os
 import struct
 
 import numpy as np
 
 import yael_gb300 as yg
+from _util import read_bytes, reference
 
 
 def test_hkm_file_roundtrip(tmp_path):
@@ -36,7 +36,7 @@ def test_hkm_file_roundtrip(tmp_path):
         lv[1][2 * bf * d:3 * bf * d])
     out = str(tmp_path / "u.hkm")
     L.hkm_write(out.encode(), h)
-    assert open(out, "rb").read() == open(path, "rb").read()
+    assert read_bytes(out) == read_bytes(path)
     L.hkm_delete(h)
     assert not L.hkm_read(str(tmp_path / "missing.hkm").encode())
 
@@ -44,9 +44,6 @@ def test_hkm_file_roundtrip(tmp_path):
 def test_hkm_files_against_the_reference(tmp_path):
     """The reference library reads what this one writes and writes the same
     bytes back; get_centroids agrees."""
-    import sys
-    sys.path.insert(0, os.path.dirname(__file__))
-    from _util import reference
     R = reference()
     if R is None:
         import pytest
@@ -68,7 +65,7 @@ def test_hkm_files_against_the_reference(tmp_path):
     o1, o2 = str(tmp_path / "o.hkm"), str(tmp_path / "r.hkm")
     L.hkm_write(o1.encode(), theirs)
     R.hkm_write(o2.encode(), ours)
-    assert open(o1, "rb").read() == open(o2, "rb").read() == open(path, "rb").read()
+    assert read_bytes(o1) == read_bytes(o2) == read_bytes(path)
     for l in range(nlevel):
         for node in range(bf ** l):
             a = ctypes.string_at(L.hkm_get_centroids(ours, l, node), 4 * bf * d)

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import yael_gb300 as yg
-from _util import oracle, reference, srand48
+from _util import oracle, read_bytes, reference, srand48
 
 P = ctypes.c_void_p
 I = ctypes.c_int
@@ -169,7 +169,7 @@ def test_index_accessors_and_files(tmp_path):
         bind(R)
         f2 = str(tmp_path / "b.kmlsh").encode()
         R.kmlsh_write(f2, lp)
-        assert open(f1, "rb").read() == open(f2, "rb").read()
+        assert read_bytes(f1) == read_bytes(f2)
     lp2 = L_.kmlsh_new(nhash, nclust, d)
     L_.kmlsh_read(f1, lp2)
     lsh2 = ctypes.cast(lp2, ctypes.POINTER(KmLsh)).contents

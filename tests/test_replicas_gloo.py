@@ -34,7 +34,7 @@ def _rank_main(rank, world, port, out):
 
 def test_two_rank_replica_aggregation():
     world = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of this (threaded) process
     out = mgr.dict()
     mp.spawn(_rank_main, args=(world, _free_port(), out), nprocs=world, join=True)
     assert out[0][0] == out[1][0] == 2.5          # both ranks see the slowest time

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import yael_gb300 as yg
-from _util import reference
+from _util import read_bytes, read_text, reference, write_text
 
 P = ctypes.c_void_p
 I = ctypes.c_int
@@ -28,7 +28,7 @@ def ptr(a):
 
 def records(path, dtype):
     """numpy restatement of the record format: int32 d, then d elements."""
-    raw = open(path, "rb").read()
+    raw = read_bytes(path)
     out, pos, item = [], 0, np.dtype(dtype).itemsize
     while pos < len(raw):
         d = int(np.frombuffer(raw, np.int32, 1, pos)[0])
@@ -161,7 +161,7 @@ def test_against_the_reference(tmp_path, data):
                                    ("bvecs", b, L_.bvecs_write, R.bvecs_write)):
         p1, p2 = (str(tmp_path / f"{w}.{ext}").encode() for w in ("ours", "ref"))
         assert ours(p1, 24, 37, ptr(arr)) == theirs(p2, 24, 37, ptr(arr)) == 37
-        assert open(p1, "rb").read() == open(p2, "rb").read()
+        assert read_bytes(p1) == read_bytes(p2)
     d1, d2, o1, o2 = I(), I(), P(), P()
     for name in ("fvecs_new_read", "ivecs_new_read", "bvecs_new_read", "b2fvecs_new_read"):
         ext = "bvecs" if name.startswith(("bvecs", "b2f")) else name[:5]
@@ -198,7 +198,7 @@ def test_raw_and_text(tmp_path, data):
                                  ("r.b", b, L_.bvec_write_raw, L_.bvec_new_read_raw, L_.bvec_fread_raw)):
         path = str(tmp_path / name).encode()
         assert w(path, ptr(arr), arr.size) == 0
-        assert open(path, "rb").read() == arr.tobytes()
+        assert read_bytes(path) == arr.tobytes()
         out = rd(path, arr.size)
         np.testing.assert_array_equal(as_array(out, arr.size, arr.dtype), arr.ravel())
         libc.free(out)
@@ -214,17 +214,17 @@ def test_raw_and_text(tmp_path, data):
     ft, it = str(tmp_path / "f.txt").encode(), str(tmp_path / "i.txt").encode()
     assert L_.fvecs_write_txt(ft, 24, 37, ptr(f)) == 37
     assert L_.ivecs_write_txt(it, 24, 37, ptr(i)) == 37
-    lines = open(it).read().split("\n")
+    lines = read_text(it).split("\n")
     assert lines[-1] == "" and len(lines) == 38
     assert lines[0] == "".join(f"{x} " for x in i[0])
-    assert open(ft).read().split("\n")[1] == "".join(f"{x:f} " for x in f[1])
+    assert read_text(ft).split("\n")[1] == "".join(f"{x:f} " for x in f[1])
     got = np.zeros((40, 24), np.float32)
     assert L_.fvecs_read_txt(ft, 24, 40, ptr(got)) == 37  # fewer vectors than asked
     np.testing.assert_array_equal(got[:37], np.array([[float(f"{x:f}") for x in r] for r in f],
                                                      np.float32))
     assert L_.fvecs_read_txt(ft, 24, 3, ptr(got)) == 3
     bad = str(tmp_path / "bad.txt").encode()
-    open(bad, "w").write("1 2 x 4\n")
+    write_text(bad, "1 2 x 4\n")
     assert L_.fvecs_read_txt(bad, 2, 2, ptr(got)) == -1
 
 
@@ -240,7 +240,7 @@ def test_raw_and_text_against_the_reference(tmp_path, data):
         p1, p2 = (str(tmp_path / f"{w}.raw{ext}").encode() for w in ("ours", "ref"))
         assert getattr(L_, fn + "_write_raw")(p1, ptr(arr), arr.size) == 0
         assert getattr(R, fn + "_write_raw")(p2, ptr(arr), arr.size) == 0
-        assert open(p1, "rb").read() == open(p2, "rb").read()
+        assert read_bytes(p1) == read_bytes(p2)
         o1 = getattr(L_, fn + "_new_read_raw")(p2, arr.size - 5)
         o2 = getattr(R, fn + "_new_read_raw")(p2, arr.size - 5)
         nbytes = (arr.size - 5) * arr.itemsize
@@ -251,7 +251,7 @@ def test_raw_and_text_against_the_reference(tmp_path, data):
         p1, p2 = (str(tmp_path / f"{w}.{fn}").encode() for w in ("ours", "ref"))
         assert getattr(L_, fn)(p1, 24, 37, ptr(arr)) == getattr(R, fn)(p2, 24, 37, ptr(arr)) == 37
         libc.fflush(None)  # the reference leaves its text file open
-        assert open(p1, "rb").read() == open(p2, "rb").read()
+        assert read_bytes(p1) == read_bytes(p2)
     path = str(tmp_path / "ours.fvecs_write_txt").encode()
     for nread in (5, 37, 50):
         a1, a2 = np.zeros((50, 24), np.float32), np.zeros((50, 24), np.float32)
