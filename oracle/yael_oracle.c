@@ -825,3 +825,244 @@ void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k,
   free(dt); free(it); free(vbuf_q); free(vbuf_b);
   free(bq); free(bb); free(pq); free(pb); free(C);
 }
+
+/* ------------------------------------------------------------------ */
+/* Gaussian mixtures (yael/gmm.c) in the reference's arithmetic: the   */
+/* expanded sgemm forms, float / double roundings and slice order      */
+
+/* softmax_ref (yael/gmm.c:262-300), in place on k x n */
+static void gmm_softmax_port(int k, long n, float *p)
+{
+  const float norm_to_0 = 16.636f;
+  for (long i = 0; i < n; i++) {
+    float *f = p + i * k;
+    float maxval = -1e30f;
+    for (int l = 0; l < k; l++)
+      if (f[l] > maxval) maxval = f[l];
+    float s = 0.0f;
+    for (int l = 0; l < k; l++) {
+      if (f[l] >= maxval - norm_to_0) {
+        f[l] = (float)exp(f[l] - maxval);
+        s += f[l];
+      } else {
+        f[l] = 0;
+      }
+    }
+    if (s != 0) {
+      float is = (float)(1.0 / s);
+      for (int l = 0; l < k; l++) f[l] *= is;
+    }
+  }
+}
+
+/* gmm_compute_p (yael/gmm.c:305-362) with compute_mahalanobis_sqr (212-259) */
+static void gmm_compute_p_port(int ni, const float *v, int di, int ki, const float *w,
+                               const float *mu, const float *sigma, float *p, int flags)
+{
+  if (ni == 0) return;
+  long n = ni, d = di, k = ki;
+  float *logdetnr = malloc(sizeof(float) * k);
+  for (long j = 0; j < k; j++) {
+    logdetnr[j] = (float)(-d / 2.0 * log(2 * M_PI));
+    for (long i = 0; i < d; i++) logdetnr[j] = (float)(logdetnr[j] - 0.5 * log(sigma[j * d + i]));
+  }
+  for (long j = 0; j < k; j++) {
+    double dtmp = 0;
+    for (long l = 0; l < d; l++) {
+      double m = mu[j * d + l];
+      dtmp += m * m / sigma[j * d + l];
+    }
+    float m2 = (float)dtmp;
+    for (long i = 0; i < n; i++) p[i * k + j] = m2;
+  }
+  float *v2 = malloc(sizeof(float) * (size_t)(n * d));
+  for (long i = 0; i < n * d; i++) v2[i] = v[i] * v[i];
+  float *tmp = malloc(sizeof(float) * (size_t)(k * d));
+  for (long i = 0; i < k * d; i++) tmp[i] = (float)(1.0 / sigma[i]);
+  float one = 1, minus_two = -2;
+  sgemm_("Transposed", "Not transposed", &ki, &ni, &di, &one, tmp, &di, v2, &di, &one, p, &ki);
+  free(v2);
+  for (long i = 0; i < k * d; i++) tmp[i] = mu[i] / sigma[i];
+  sgemm_("Transposed", "Not transposed", &ki, &ni, &di, &minus_two, tmp, &di, v, &di, &one, p,
+         &ki);
+  free(tmp);
+  float *lg = malloc(sizeof(float) * k);
+  for (long j = 0; j < k; j++) lg[j] = (flags & 1) ? (float)log(w[j]) : 0.0f;
+  for (long i = 0; i < n; i++)
+    for (long j = 0; j < k; j++)
+      p[i * k + j] = (float)(logdetnr[j] - 0.5 * p[i * k + j] + lg[j]);
+  free(lg);
+  gmm_softmax_port(ki, n, p);
+  free(logdetnr);
+}
+
+void orc_gmm_compute_p(int n, const float *v, int d, int k, const float *w, const float *mu,
+                       const float *sigma, float *p, int flags, int nt)
+{
+  /* gmm_compute_p_thread (yael/gmm.c:854-870): nt slices of the vectors */
+  if (nt < 1) nt = 1;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int t = 0; t < nt; t++) {
+    long n0 = (long)t * n / nt, n1 = (long)(t + 1) * n / nt;
+    gmm_compute_p_port((int)(n1 - n0), v + n0 * d, d, k, w, mu, sigma, p + n0 * k, flags);
+  }
+}
+
+/* compute_sum_dcov (yael/gmm.c:72-103) */
+static void gmm_sum_dcov_port(int ni, int ki, int di, const float *v, const float *mu_old,
+                              const float *p, float *mu, float *sigma, float *w)
+{
+  long n = ni, k = ki, d = di;
+  for (long j = 0; j < k; j++) {
+    double dtmp = 0;
+    for (long i = 0; i < n; i++) dtmp += p[i * k + j];
+    w[j] = (float)dtmp;
+  }
+  float zero = 0, one = 1;
+  sgemm_("Not transposed", "Transposed", &di, &ki, &ni, &one, v, &di, p, &ki, &zero, mu, &di);
+  float *v2 = malloc(sizeof(float) * (size_t)(n * d + 1));
+  for (long i = 0; i < n * d; i++) v2[i] = v[i] * v[i];
+  sgemm_("Not transposed", "Transposed", &di, &ki, &ni, &one, v2, &di, p, &ki, &zero, sigma,
+         &di);
+  free(v2);
+  for (long j = 0; j < k; j++)
+    for (long l = 0; l < d; l++) {
+      float mo = mu_old[j * d + l];
+      sigma[j * d + l] += mo * (mo * w[j] - 2 * mu[j * d + l]);
+    }
+}
+
+/* gmm_compute_params (yael/gmm.c:114-199) with compute_sum_dcov_thread
+ * (880-930) for nt > 1 */
+static void gmm_compute_params_port(int n, const float *v, const float *p, int d, int k,
+                                    float *w, float *mu, float *sigma, int flags, int nt)
+{
+  long kd = (long)k * d;
+  float *mu_old = malloc(sizeof(float) * (size_t)kd);
+  memcpy(mu_old, mu, sizeof(float) * (size_t)kd);
+  if (nt <= 1) {
+    gmm_sum_dcov_port(n, k, d, v, mu_old, p, mu, sigma, w);
+  } else {
+    float *tm = malloc(sizeof(float) * (size_t)(nt * kd));
+    float *ts = malloc(sizeof(float) * (size_t)(nt * kd));
+    float *tw = malloc(sizeof(float) * (size_t)(nt * k));
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int t = 0; t < nt; t++) {
+      long n0 = (long)t * n / nt, n1 = (long)(t + 1) * n / nt;
+      gmm_sum_dcov_port((int)(n1 - n0), k, d, v + d * n0, mu_old, p + n0 * k, tm + t * kd,
+                        ts + t * kd, tw + (long)t * k);
+    }
+    memcpy(mu, tm, sizeof(float) * (size_t)kd);
+    memcpy(sigma, ts, sizeof(float) * (size_t)kd);
+    memcpy(w, tw, sizeof(float) * (size_t)k);
+    for (int t = 1; t < nt; t++) {
+      for (long i = 0; i < kd; i++) mu[i] += tm[t * kd + i];
+      for (long i = 0; i < kd; i++) sigma[i] += ts[t * kd + i];
+      for (long i = 0; i < k; i++) w[i] += tw[(long)t * k + i];
+    }
+    free(tm); free(ts); free(tw);
+  }
+  if (flags & 4) { /* GMM_FLAGS_1SIGMA */
+    for (long j = 0; j < k; j++) {
+      double s = 0;
+      for (long l = 0; l < d; l++) s += sigma[j * d + l];
+      float var = (float)(s / d);
+      for (long l = 0; l < d; l++) sigma[j * d + l] = var;
+    }
+  }
+  for (long i = 0; i < kd; i++)
+    if (sigma[i] < 1e-10f) sigma[i] = 1e-10f;
+  for (long j = 0; j < k; j++) { /* fvec_div_by: times 1. / w in double */
+    double inv = 1. / w[j];
+    for (long l = 0; l < d; l++) {
+      mu[j * d + l] = (float)(mu[j * d + l] * inv);
+      sigma[j * d + l] = (float)(sigma[j * d + l] * inv);
+    }
+  }
+  double nr = 0; /* fvec_normalize(w, k, 1) */
+  for (long j = 0; j < k; j++) nr += fabs(w[j]);
+  for (long j = 0; j < k; j++) w[j] = (float)(w[j] * (1. / nr));
+  free(mu_old);
+}
+
+/* gmm_handle_empty (yael/gmm.c:366-433); returns -1 where the reference
+ * asserts or loops for ever */
+static int gmm_handle_empty_port(long n, const float *v, int d, int k, const float *mu,
+                                 const float *sigma, float *p)
+{
+  float *w = calloc((size_t)k, sizeof(float));
+  for (long i = 0; i < n; i++)
+    for (int j = 0; j < k; j++) w[j] += p[j + i * k];
+  const int bigprime = 1000003;
+  for (int j = 0; j < k; j++) {
+    if (w[j] != 0) continue;
+    int j2 = j, tries = 0, nnz;
+    for (;;) {
+      int i;
+      for (i = 0; i < k; i++) {
+        j2 = (j2 + bigprime) % k;
+        if (w[j2] > 0) break;
+      }
+      if (i == k || ++tries > k) { free(w); return -1; }
+      nnz = 0;
+      for (long t = 0; t < n; t++)
+        if (p[j2 + t * k] > 0) nnz++;
+      if (nnz < n / k) continue;
+      break;
+    }
+    int sd = 0;
+    for (int l = 1; l < d; l++)
+      if (sigma[(long)d * j2 + l] > sigma[(long)d * j2 + sd]) sd = l;
+    for (long t = 0; t < n; t++)
+      if (p[j2 + t * k] > 0 && v[t * d + sd] < mu[(long)j2 * d + sd]) {
+        p[j + t * k] = p[j2 + t * k];
+        p[j2 + t * k] = 0;
+      }
+    w[j2] = -1;
+  }
+  free(w);
+  return 0;
+}
+
+int orc_gmm_em_step(int n, const float *v, int d, int k, float *w, float *mu, float *sigma,
+                    int flags, int nt)
+{
+  /* one iteration of gmm_learn's loop (yael/gmm.c:472-484) */
+  float *p = malloc(sizeof(float) * ((size_t)n * k + 1));
+  orc_gmm_compute_p(n, v, d, k, w, mu, sigma, p, flags, nt);
+  int ret = gmm_handle_empty_port(n, v, d, k, mu, sigma, p);
+  if (ret == 0) gmm_compute_params_port(n, v, p, d, k, w, mu, sigma, flags, nt);
+  free(p);
+  return ret;
+}
+
+int orc_gmm_learn(int d, int n, int k, int niter, const float *v, int nt, int seed, int nredo,
+                  int flags, float *w, float *mu, float *sigma, int *iters_out)
+{
+  /* gmm_learn (yael/gmm.c:436-502): the reference's k-means, then EM */
+  niter = niter == 0 ? 10000 : niter;
+  float *dis = malloc(sizeof(float) * (size_t)(n + 1));
+  orc_kmeans(d, n, k, niter, v, nt, seed, nredo, mu, dis, NULL, NULL, ORC_PORT, NULL);
+  for (int j = 0; j < k; j++) w[j] = (float)(1.0 / k);
+  double sig = 0;
+  for (long i = 0; i < n; i++) sig += dis[i];
+  sig /= n;
+  for (long t = 0; t < (long)k * d; t++) sigma[t] = (float)sig;
+  free(dis);
+  if (flags & 32) niter = 0; /* GMM_FLAGS_PURE_KMEANS */
+  float *p = malloc(sizeof(float) * ((size_t)n * k + 1));
+  double key = 666, old_key;
+  int iter, ret = 0;
+  for (iter = 1; iter <= niter; iter++) {
+    orc_gmm_compute_p(n, v, d, k, w, mu, sigma, p, flags, nt);
+    if (gmm_handle_empty_port(n, v, d, k, mu, sigma, p) < 0) { ret = -1; break; }
+    gmm_compute_params_port(n, v, p, d, k, w, mu, sigma, flags, nt);
+    old_key = key;
+    key = 0;
+    for (long t = 0; t < (long)k * d; t++) key += mu[t];
+    if (key == old_key) break;
+  }
+  if (iters_out) *iters_out = iter > niter ? niter : iter;
+  free(p);
+  return ret;
+}

@@ -97,6 +97,19 @@ void orc_hkm_quantize(int nlevel, int bf, int d, const float *centroids, int npt
 void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k, int nhash,
                    int vec_type, int mode, int *idx_out, float *dis_out);
 
+/* Gaussian mixtures in the reference's arithmetic (yael/gmm.c): expanded
+ * sgemm forms, its float / double roundings and its slice order for nt > 1.
+ * orc_gmm_compute_p follows gmm_compute_p_thread (854-870); orc_gmm_learn
+ * follows gmm_learn (436-502) with the port-mode k-means; returns -1 where
+ * the reference would assert or loop for ever in gmm_handle_empty. */
+void orc_gmm_compute_p(int n, const float *v, int d, int k, const float *w, const float *mu,
+                       const float *sigma, float *p, int flags, int nt);
+int orc_gmm_learn(int d, int n, int k, int niter, const float *v, int nt, int seed, int nredo,
+                  int flags, float *w, float *mu, float *sigma, int *iters_out);
+/* one EM iteration of orc_gmm_learn on the given mixture, in place */
+int orc_gmm_em_step(int n, const float *v, int d, int k, float *w, float *mu, float *sigma,
+                    int flags, int nt);
+
 /* RNG pieces, exposed so the tests can compare them with the GPU library's. */
 double orc_gaussrand_r(unsigned int *seed);
 void orc_random_init(int n, int k, unsigned int seed, int *sel);

@@ -294,3 +294,38 @@ def test_numpy_front_end_plumbing(monkeypatch, tmp_path):
     libc.fclose(fh)
     for a, b in zip(yg.gmm_read(fn.decode()), exp):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("nt", [1, 3])
+def test_port_restatement_bit_identical_to_reference(nt):
+    """The oracle's restatement in the reference's own arithmetic (expanded
+    sgemm forms, float roundings, slice order for nt > 1) equals the reference
+    library bit for bit: posteriors and learned mixtures.  It is the timed CPU
+    baseline of the mixture workload."""
+    R = ref_lib()
+    o = oracle()
+    o.orc_gmm_compute_p.argtypes = [ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P, P, P, P,
+                                    ctypes.c_int, ctypes.c_int]
+    o.orc_gmm_learn.argtypes = [ctypes.c_int] * 4 + [P] + [ctypes.c_int] * 4 + [P, P, P, P]
+    v, w, mu, sigma = mixture(3)
+    n, d = v.shape
+    k = mu.shape[0]
+    g, keep = make_gmm(w, mu, sigma)
+    for flags in (0, go.FLAGS_W):
+        exp = np.empty((n, k), np.float32)
+        R.gmm_compute_p_thread(n, ptr(v), ctypes.byref(g), ptr(exp), flags, nt)
+        got = np.empty((n, k), np.float32)
+        o.orc_gmm_compute_p(n, ptr(v), d, k, ptr(w), ptr(mu), ptr(sigma), ptr(got), flags, nt)
+        np.testing.assert_array_equal(got, exp)
+    v, _, _ = synth.gaussian_mixture(3000, 10, 6, 0.9, seed=11)
+    n, d = v.shape
+    for flags in (go.FLAGS_W, go.FLAGS_W | go.FLAGS_1SIGMA):
+        gp = R.gmm_learn(d, n, 6, 8, ptr(v), nt, 5, 1, flags)
+        exp = read_gmm(gp)
+        R.gmm_delete(gp)
+        gw, gm, gs = np.empty(6, np.float32), np.empty((6, d), np.float32), np.empty((6, d), np.float32)
+        it = ctypes.c_int(0)
+        assert o.orc_gmm_learn(d, n, 6, 8, ptr(v), nt, 5, 1, flags, ptr(gw), ptr(gm), ptr(gs),
+                               ctypes.byref(it)) == 0
+        for a, b in zip((gw, gm, gs), exp):
+            np.testing.assert_array_equal(a, b)
