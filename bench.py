@@ -419,13 +419,15 @@ def run_callers(args, world, rank, local):
             _, gdt = ann(sb, sq)
             o = oracle()
             o.orc_kmlsh_ann.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
-                                        ctypes.c_int] + [ctypes.c_int] * 5 + [ctypes.c_void_p] * 2
+                                        ctypes.c_int] + [ctypes.c_int] * 6 + [ctypes.c_void_p] * 2
             oi = np.empty((1000, k), np.int32)
             od = np.empty((1000, k), np.float32)
+            nt = min(os.cpu_count() or 1, 255)  # KMLSH_NT holds 8 bits
             t0 = time.perf_counter()
-            o.orc_kmlsh_ann(ptr(sb), 100_000, ptr(sq), 1000, d, k, nhash, 0, 0, ptr(oi), ptr(od))
+            o.orc_kmlsh_ann(ptr(sb), 100_000, ptr(sq), 1000, d, k, nhash, 0, 0, nt, ptr(oi),
+                            ptr(od))
             cdt = time.perf_counter() - t0
-            line["cpu_baseline"] = {"value": 1000 / cdt, "unit": "queries/s", "cores": 1,
+            line["cpu_baseline"] = {"value": 1000 / cdt, "unit": "queries/s", "cores": nt,
                                     "kind": "port",
                                     "sample": "the reference's algorithm in its own arithmetic "
                                               "(oracle port) at nb=100000 nq=1000; the GPU on "

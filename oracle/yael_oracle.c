@@ -741,7 +741,7 @@ static void orc_rows(const void *v, int vec_type, const int *ids, long m, int d,
  * in blocks of KMLSH_BLOCK_SIZE, then the ids ordered by cell and the cell
  * starts */
 static void orc_cohash(const float *C, int nclust, int d, const void *v, int n, int vec_type,
-                       int mode, int *perm, int *bnd)
+                       int mode, int nt, int *perm, int *bnd)
 {
   int *idx = malloc(sizeof(int) * (size_t)(n + 1));
   float *dis = malloc(sizeof(float) * (size_t)(n + 1));
@@ -752,9 +752,9 @@ static void orc_cohash(const float *C, int nclust, int d, const void *v, int n, 
     for (int j = 0; j < m; j++) ids[j] = (int)(i + j);
     orc_rows(v, vec_type, ids, m, d, buf);
     if (mode == ORC_PORT)
-      knn_full_port(2, m, nclust, d, 1, C, buf, NULL, idx + i, dis + i);
+      orc_knn_port(2, m, nclust, d, 1, C, buf, NULL, idx + i, dis + i, nt);
     else
-      orc_knn_exact(m, nclust, d, 1, C, buf, idx + i, dis + i, NULL, 1);
+      orc_knn_exact(m, nclust, d, 1, C, buf, idx + i, dis + i, NULL, nt);
   }
   int *nocc = calloc((size_t)nclust + 1, sizeof(int));
   for (int c = 0; c <= nclust; c++) bnd[c] = 0;
@@ -765,9 +765,11 @@ static void orc_cohash(const float *C, int nclust, int d, const void *v, int n, 
 }
 
 void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k, int nhash,
-                   int vec_type, int mode, int *idx_out, float *dis_out)
+                   int vec_type, int mode, int nt, int *idx_out, float *dis_out)
 {
-  /* kmlsh_ann_xvec (yael/kmlsh.c:479-500) with one thread */
+  /* kmlsh_ann_xvec (yael/kmlsh.c:479-500); nt threads as its knn_full_thread
+   * and kmeans calls use them */
+  if (nt < 1) nt = 1;
   int nclust = (int)sqrt(nb);
   int nlearn = nclust * 100;
   if (nlearn > nb) nlearn = nb;
@@ -779,7 +781,7 @@ void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k,
   for (int h = 0; h < nhash; h++) {
     orc_random_init(nb, nlearn, (unsigned int)lrand48(), sel);
     orc_rows(vb, vec_type, sel, nlearn, d, vlearn);
-    orc_kmeans(d, nlearn, nclust, 8, vlearn, 1 | ORC_KMEANS_INIT_RANDOM, 0, 1, C + h * cs,
+    orc_kmeans(d, nlearn, nclust, 8, vlearn, nt | ORC_KMEANS_INIT_RANDOM, 0, 1, C + h * cs,
                NULL, NULL, NULL, mode, NULL);
   }
   free(sel);
@@ -790,9 +792,9 @@ void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k,
   int *bb = malloc(sizeof(int) * (size_t)(nclust + 1) * nhash);
   int *bq = malloc(sizeof(int) * (size_t)(nclust + 1) * nhash);
   for (int h = 0; h < nhash; h++) {
-    orc_cohash(C + h * cs, nclust, d, vb, nb, vec_type, mode, pb + (long)h * nb,
+    orc_cohash(C + h * cs, nclust, d, vb, nb, vec_type, mode, nt, pb + (long)h * nb,
                bb + (long)h * (nclust + 1));
-    orc_cohash(C + h * cs, nclust, d, vq, nq, vec_type, mode, pq + (long)h * nq,
+    orc_cohash(C + h * cs, nclust, d, vq, nq, vec_type, mode, nt, pq + (long)h * nq,
                bq + (long)h * (nclust + 1));
   }
   /* kmlsh_match_xvec (yael/kmlsh.c:376-456) */
@@ -812,9 +814,9 @@ void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k,
       orc_rows(vq, vec_type, vidx_q, nqc, d, vbuf_q);
       int k2 = k < nbc ? k : nbc;
       if (mode == ORC_PORT)
-        knn_full_port(2, nqc, nbc, d, k2, vbuf_b, vbuf_q, NULL, it, dt);
+        orc_knn_port(2, nqc, nbc, d, k2, vbuf_b, vbuf_q, NULL, it, dt, nt);
       else
-        orc_knn_exact(nqc, nbc, d, k2, vbuf_b, vbuf_q, it, dt, NULL, 1);
+        orc_knn_exact(nqc, nbc, d, k2, vbuf_b, vbuf_q, it, dt, NULL, nt);
       for (long i = 0; i < (long)k2 * nqc; i++) it[i] = vidx_b[it[i]];
       for (int i = 0; i < nqc; i++)
         for (int j = 0; j < k2; j++)

@@ -90,12 +90,13 @@ void orc_hkm_quantize(int nlevel, int bf, int d, const float *centroids, int npt
                       const float *v, int *idx, int mode);
 
 /* k-means LSH search (yael/kmlsh.c:479-500: learn 133-185, cell assignment
- * 210-279, per-cell search and merge 376-456) with one thread.  vec_type 0:
- * float rows, 1: byte rows.  idx_out / dis_out (nq x k) receive the merged
- * lists in the reference's slot order.  The RNG stream (lrand48 per
- * partition, then the kmeans seed) is the reference's. */
+ * 210-279, per-cell search and merge 376-456) with nt threads, split as the
+ * reference splits them.  vec_type 0: float rows, 1: byte rows.  idx_out /
+ * dis_out (nq x k) receive the merged lists in the reference's slot order.
+ * The RNG stream (lrand48 per partition, then the kmeans seed) is the
+ * reference's. */
 void orc_kmlsh_ann(const void *vb, int nb, const void *vq, int nq, int d, int k, int nhash,
-                   int vec_type, int mode, int *idx_out, float *dis_out);
+                   int vec_type, int mode, int nt, int *idx_out, float *dis_out);
 
 /* Gaussian mixtures in the reference's arithmetic (yael/gmm.c): expanded
  * sgemm forms, its float / double roundings and its slice order for nt > 1.

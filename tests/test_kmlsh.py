@@ -52,21 +52,21 @@ def lists(lp):
     return idx, dis
 
 
-def orc_ann(vb, vq, k, nhash, vec_type, mode):
+def orc_ann(vb, vq, k, nhash, vec_type, mode, nt=1):
     o = oracle()
-    o.orc_kmlsh_ann.argtypes = [P, I, P, I, I, I, I, I, I, P, P]
+    o.orc_kmlsh_ann.argtypes = [P, I, P, I, I, I, I, I, I, I, P, P]
     nq, d = vq.shape
     idx = np.empty((nq, k), np.int32)
     dis = np.empty((nq, k), np.float32)
-    o.orc_kmlsh_ann(ptr(vb), vb.shape[0], ptr(vq), nq, d, k, nhash, vec_type, mode, ptr(idx),
-                    ptr(dis))
+    o.orc_kmlsh_ann(ptr(vb), vb.shape[0], ptr(vq), nq, d, k, nhash, vec_type, mode, nt,
+                    ptr(idx), ptr(dis))
     return idx, dis
 
 
-def lib_ann(lib, vb, vq, k, nhash):
+def lib_ann(lib, vb, vq, k, nhash, nt=1):
     nq, d = vq.shape
     fn = lib.kmlsh_ann_bvec if vb.dtype == np.uint8 else lib.kmlsh_ann_fvec
-    lp = fn(ptr(vb), vb.shape[0], ptr(vq), nq, d, k, nhash, 1)
+    lp = fn(ptr(vb), vb.shape[0], ptr(vq), nq, d, k, nhash, nt)
     out = lists(lp)
     lib.nnlist_delete(lp)
     return out
@@ -106,6 +106,22 @@ def test_restatement_pinned_to_reference():
             np.testing.assert_array_equal(got[0], exp[0], err_msg=f"seed {seed} k {k}")
             np.testing.assert_array_equal(got[1], exp[1], err_msg=f"seed {seed} k {k}")
             assert (got[0] >= 0).all()
+
+
+def test_threaded_restatement_pinned_to_reference():
+    """Three threads in the reference (its k-means and knn_full_thread calls
+    split the work) and in the restatement: the same lists."""
+    R = reference()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    bind(R)
+    vb, vq = clustered(4, 3000, 200, 24)
+    srand48(104)
+    got = lib_ann(R, vb, vq, 10, 2, nt=3)
+    srand48(104)
+    exp = orc_ann(vb, vq, 10, 2, 0, ORC_PORT, nt=3)
+    np.testing.assert_array_equal(got[0], exp[0])
+    np.testing.assert_array_equal(got[1], exp[1])
 
 
 def test_restatement_small_cells_pinned_to_reference():
