@@ -2,8 +2,9 @@
  * yael_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * A CPU restatement of yael's distance-GEMM path (exact k-NN, k-means Lloyd loop,
- * hierarchical k-means), used as the checker for the GPU library and as the timed
- * CPU baseline.  Nothing in the product library links, loads or calls this code;
+ * hierarchical k-means) and of two of its callers (k-means LSH, Gaussian
+ * mixtures), used as the checker for the GPU library and as the timed CPU
+ * baseline.  Nothing in the product library links, loads or calls this code;
  * only tests/, __graft_entry__.smoke() and bench.py's CPU legs do.
  *
  * Two arithmetic modes:
