@@ -153,17 +153,92 @@ static void dot_products_port(int d, int na, int nb, const float *a, const float
   sgemm_("Trans", "Not", &na, &nb, &d, &one, a, &d, b, &d, &zero, dist2, &na);
 }
 
+/* the SSE2 forms of yael/nn.c:172-210 (used when d % 4 == 0 in builds with
+ * SSE2): four float lanes, lane l adding the terms of coordinates l, l+4, ...,
+ * then lane0 + lane1 + lane2 + lane3; chi2 terms where the coordinates differ */
+static float alt_lanes(int dt, const float *a, const float *b, int d)
+{
+  float acc[4] = {0, 0, 0, 0};
+  for (int i = 0; i < d; i += 4)
+    for (int l = 0; l < 4; l++) {
+      float ai = a[i + l], bi = b[i + l];
+      float diff = ai - bi;
+      if (dt == 1) {
+        acc[l] += fabsf(diff);
+      } else if (ai != bi) {
+        float sum = ai + bi;
+        acc[l] += (diff * diff) / sum;
+      }
+    }
+  return acc[0] + acc[1] + acc[2] + acc[3];
+}
+
+/* compute_cross_distances_alt_nonpacked (yael/nn.c:280-350):
+ * dist2[i + ldd*j] = distance(a_i, b_j) */
+void orc_cross_distances_alt(int dt, int d, int na, int nb, const float *a, int lda,
+                             const float *b, int ldb, float *dist2, int ldd)
+{
+#ifdef __SSE2__
+  if (d % 4 == 0 && (dt == 1 || dt == 3)) {
+    for (long j = 0; j < nb; j++)
+      for (long i = 0; i < na; i++)
+        dist2[j * ldd + i] = alt_lanes(dt, a + i * lda, b + j * ldb, d);
+    return;
+  }
+#endif
+  if (dt == 12) {
+    orc_cross_distances_port(d, na, nb, a, lda, b, ldb, dist2, ldd);
+    return;
+  }
+  if (dt == 16) {
+    float one = 1, zero = 0;
+    sgemm_("Trans", "Not", &na, &nb, &d, &one, a, &lda, b, &ldb, &zero, dist2, &ldd);
+    return;
+  }
+  for (long j = 0; j < nb; j++) {
+    const float *bl = b + (long)ldb * j;
+    for (long i = 0; i < na; i++) {
+      const float *al = a + (long)lda * i;
+      double sum = 0;
+      for (int c = 0; c < d; c++) {
+        float av = al[c], bv = bl[c];
+        if (dt == 1) {
+          sum += fabs(av - bv);
+        } else if (dt == 2) {
+          double t = av - bv;
+          sum += t * t;
+        } else if (dt == 3) {
+          double t = av - bv;
+          sum += av + bv == 0 ? 0 : t * t / (av + bv);
+        } else if (dt == 4) {
+          float den = fabs(av + bv);
+          double t = av - bv;
+          sum += den == 0 ? 0 : t * t / den;
+        } else if (dt == 5) {
+          sum += av < bv ? av : bv;
+        } else if (dt == 6) {
+          sum += av * bv;
+        } else {
+          fprintf(stderr, "oracle: distance_type %d not restated\n", dt);
+          abort();
+        }
+      }
+      dist2[j * ldd + i] = (float)sum;
+    }
+  }
+}
+
 static void tile_distances(int dt, int d, int na, int nb, const float *a,
                            const float *b, float *out)
 {
+  /* knn_full / nn_single_full (yael/nn.c:414-417, 491-496): type 2 through
+   * compute_cross_distances, every other through the _alt dispatch */
   if (dt == 2 || dt == 12)
     orc_cross_distances_port(d, na, nb, a, d, b, d, out, na);
   else if (dt == 16)
     dot_products_port(d, na, nb, a, b, out);
-  else {
-    fprintf(stderr, "oracle: distance_type %d not restated\n", dt);
-    abort();
-  }
+  else
+    orc_cross_distances_alt(dt, d, na, nb, a, d, b, d, out, na);
 }
 
 /* nn_single_full (yael/nn.c:383-446): blocked argmin, strict '<' */
@@ -1067,4 +1142,22 @@ int orc_gmm_learn(int d, int n, int k, int niter, const float *v, int nt, int se
   if (iters_out) *iters_out = iter > niter ? niter : iter;
   free(p);
   return ret;
+}
+
+/* vlad_compute (yael/vlad.c:10-27): nearest centroid by nn (the blocked
+ * argmin of knn_full, split over nt query slices as knn_full_thread does;
+ * each vector's result is its own), then the residuals added in float, in
+ * vector order */
+void orc_vlad_compute(int k, int d, const float *centroids, int n, const float *v, float *desc,
+                      int nt)
+{
+  int *assign = malloc(sizeof(int) * (size_t)(n + 1));
+  float *dis = malloc(sizeof(float) * (size_t)(n + 1));
+  orc_knn_port(2, n, k, d, 1, centroids, v, NULL, assign, dis, nt);
+  memset(desc, 0, sizeof(float) * (size_t)k * d);
+  for (long i = 0; i < n; i++)
+    for (long j = 0; j < d; j++)
+      desc[(long)assign[i] * d + j] += v[i * d + j] - centroids[(long)assign[i] * d + j];
+  free(dis);
+  free(assign);
 }

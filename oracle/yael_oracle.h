@@ -55,6 +55,17 @@ void orc_knn_port(int distance_type, int nq, int nb, int d, int k, const float *
                   const float *q, const float *b_weights, int *assign, float *dis,
                   int nt);
 
+/* Restatement of compute_cross_distances_alt_nonpacked (yael/nn.c:164-350):
+ * every distance type, with the SSE2 lane form for L1 / chi2 when d % 4 == 0
+ * in builds with SSE2 (as the reference's x86 build), double sums otherwise.
+ * orc_knn_port takes these types as well (knn_full's _alt dispatch). */
+void orc_cross_distances_alt(int dt, int d, int na, int nb, const float *a, int lda,
+                             const float *b, int ldb, float *dist2, int ldd);
+
+/* vlad_compute (yael/vlad.c:10-27) with the nearest centroids of the port */
+void orc_vlad_compute(int k, int d, const float *centroids, int n, const float *v, float *desc,
+                      int nt);
+
 /* Restatement of compute_cross_distances_nonpacked (yael/nn.c:100-129). */
 void orc_cross_distances_port(int d, int na, int nb, const float *a, int lda,
                               const float *b, int ldb, float *dist2, int ldd);

@@ -125,12 +125,12 @@ def knn_restate(t, base, queries, k):
 KNN_CASES = [(t, d, k) for t in (1, 3, 4, 5, 6) for d in (16, 13) for k in (1, 5)]
 
 
-def knn_call(L, t, base, queries, k):
+def knn_call(L, t, base, queries, k, nt=1):
     nq, d = queries.shape
     idx = np.zeros((nq, k), np.int32)
     dis = np.zeros((nq, k), f32)
     L.knn_full_thread(t, nq, base.shape[0], d, k, ptr(base), ptr(queries), None, ptr(idx),
-                      ptr(dis), 1)
+                      ptr(dis), nt)
     return idx, dis
 
 
@@ -158,3 +158,38 @@ def test_gpu_knn_alt_types(t, d, k):
     ei, ed = knn_restate(t, base, queries, k)
     np.testing.assert_array_equal(gi, ei)
     np.testing.assert_array_equal(gd, ed)
+
+
+def test_oracle_port_bit_identical_to_reference():
+    """The oracle's C restatement of the _alt dispatch, and of knn_full_thread
+    over it (blocked, heap, nt query slices), equal the reference library bit
+    for bit for every distance type; they are the timed CPU baselines."""
+    from _util import oracle
+    R = reference()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    res, args = yg.SIGNATURES["compute_cross_distances_alt_nonpacked"]
+    R.compute_cross_distances_alt_nonpacked.restype = res
+    R.compute_cross_distances_alt_nonpacked.argtypes = args
+    o = oracle()
+    o.orc_cross_distances_alt.argtypes = [I, I, I, I, P, I, P, I, P, I]
+    for t in (1, 2, 3, 4, 5, 6, 12, 16):
+        for d in (16, 13):
+            a, b = operands(t * 10 + d, 300, 270, d)  # more than one 256-row block
+            exp = np.full((270, 300), -1.0, f32)
+            R.compute_cross_distances_alt_nonpacked(t, d, 300, 270, ptr(a), d, ptr(b), d,
+                                                    ptr(exp), 300)
+            got = np.full((270, 300), -1.0, f32)
+            o.orc_cross_distances_alt(t, d, 300, 270, ptr(a), d, ptr(b), d, ptr(got), 300)
+            np.testing.assert_array_equal(got, exp, err_msg=f"type {t} d {d}")
+    for t in (1, 3, 4, 5, 6):
+        for k, nt in ((1, 1), (5, 1), (5, 3)):
+            rng = np.random.default_rng(t * 100 + k + nt)
+            base = rng.standard_normal((600, 16)).astype(f32)
+            queries = rng.standard_normal((40, 16)).astype(f32)
+            gi, gd = knn_call(R, t, base, queries, k, nt)
+            ei = np.zeros((40, k), np.int32)
+            ed = np.zeros((40, k), f32)
+            o.orc_knn_port(t, 40, 600, 16, k, ptr(base), ptr(queries), None, ptr(ei), ptr(ed), nt)
+            np.testing.assert_array_equal(ei, gi, err_msg=f"type {t} k {k} nt {nt}")
+            np.testing.assert_array_equal(ed, gd, err_msg=f"type {t} k {k} nt {nt}")

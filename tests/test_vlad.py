@@ -124,3 +124,26 @@ def test_numpy_front_end_plumbing(monkeypatch):
     R.vlad_compute(k, d, ptr(C), v.shape[0], ptr(v), ptr(exp))
     monkeypatch.setattr(yg, "_lib", R)
     np.testing.assert_array_equal(yg.vlad(C, v), exp)
+
+
+@pytest.mark.parametrize("nt", [1, 3])
+def test_oracle_port_bit_identical_to_reference(nt):
+    """The oracle's C restatement of vlad_compute (the reference's sgemm-based
+    nearest centroid, float sums in vector order) equals the reference library
+    bit for bit; it is the timed CPU baseline."""
+    from _util import oracle
+    R = reference()
+    if R is None:
+        pytest.skip("reference library not built here (oracle/_ref)")
+    res, args = yg.SIGNATURES["vlad_compute"]
+    R.vlad_compute.restype = res
+    R.vlad_compute.argtypes = args
+    o = oracle()
+    o.orc_vlad_compute.argtypes = [I, I, P, I, P, P, I]
+    C, v, w, si, se = data(9)
+    k, d = C.shape
+    exp = np.zeros((k, d), np.float32)
+    R.vlad_compute(k, d, ptr(C), v.shape[0], ptr(v), ptr(exp))
+    got = np.zeros((k, d), np.float32)
+    o.orc_vlad_compute(k, d, ptr(C), v.shape[0], ptr(v), ptr(got), nt)
+    np.testing.assert_array_equal(got, exp)
