@@ -304,8 +304,9 @@ class _quiet_stdout:
 def run_callers(args, world, rank, local):
     """The path's callers, timed through their drop-in calls with host buffers
     (host <-> device copies included): gmm_learn / gmm_compute_p / gmm_fisher,
-    and kmlsh_ann_fvec.  The CPU figure is the oracle's restatement on a
-    bounded sample, one thread."""
+    kmlsh_ann_fvec, vlad_compute, knn_full_thread with the L1 / chi2 distances.
+    The CPU figure is the oracle's restatement in the reference's arithmetic on
+    a bounded sample, on the host's threads."""
     import torch
     import yael_gb300 as yg
     from yael_gb300 import synth
@@ -320,7 +321,7 @@ def run_callers(args, world, rank, local):
             getattr(L, name).argtypes = argt
     os.environ["YAEL_GPU_PRECISION"] = args.prec
     line = {"n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "data": "synthetic", "dtype": "f32" if args.workload == "gmm" else args.prec,
+            "data": "synthetic", "dtype": "f32" if args.workload in ("gmm", "alt") else args.prec,
             "steps": 1, "warmup": 1}
     if args.workload == "gmm":
         import gmm_oracle as go
@@ -385,6 +386,71 @@ def run_callers(args, world, rank, local):
                                     "sample": f"one EM iteration (posteriors, splits, parameters) "
                                               f"in the reference's arithmetic (BLAS sgemm, {nt} "
                                               f"slices) on {sub.shape[0]} vectors, scaled to n"}
+    elif args.workload == "vlad":
+        n, d, k = (args.n or 1_000_000), 128, 256
+        v = synth.sift_like(n, d, seed=31)
+        C = synth.sift_like(k, d, seed=32)
+        desc = np.empty((k, d), np.float32)
+        L.vlad_compute(k, d, ptr(C), 10_000, ptr(v), ptr(desc))  # warm-up
+        t0 = time.perf_counter()
+        L.vlad_compute(k, d, ptr(C), n, ptr(v), ptr(desc))
+        dt = time.perf_counter() - t0
+        line.update({"metric": "VLAD descriptors/s (vlad_compute, host buffers)",
+                     "unit": "vectors/s", "value": n / dt, "ms_per_step": 1e3 * dt,
+                     "config": {"workload": f"vlad_compute n={n} d={d} k={k}, SIFT-like vectors "
+                                            f"and centroids", "n": n, "d": d, "k": k},
+                     "e2e": {"value": n / dt, "unit": "vectors/s", "h2d_bytes_per_step": 4 * n * d,
+                             "d2h_bytes_per_step": 4 * k * d}})
+        if not args.no_cpu:
+            nt = os.cpu_count() or 1
+            sub = v  # the whole workload: a fraction of a second per million vectors
+            o = oracle()
+            o.orc_vlad_compute.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_int]
+            od = np.empty((k, d), np.float32)
+            t0 = time.perf_counter()
+            o.orc_vlad_compute(k, d, ptr(C), sub.shape[0], ptr(sub), ptr(od), nt)
+            cdt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": sub.shape[0] / cdt, "unit": "vectors/s",
+                                    "cores": nt, "kind": "port",
+                                    "sample": f"vlad_compute in the reference's arithmetic "
+                                              f"(bit-identical to it) on {sub.shape[0]} vectors"}
+    elif args.workload == "alt":
+        nb, nq, d, k = (args.n or 100_000), 1000, 128, 10
+        b = synth.sift_like(nb, d, seed=1)
+        q = synth.sift_like(nq, d, seed=2)
+        idx = np.empty((nq, k), np.int32)
+        dis = np.empty((nq, k), np.float32)
+        rates = {}
+        for t in (1, 3):  # L1, chi2
+            L.knn_full_thread(t, 10, nb, d, k, ptr(b), ptr(q), None, ptr(idx), ptr(dis), 1)
+            t0 = time.perf_counter()
+            L.knn_full_thread(t, nq, nb, d, k, ptr(b), ptr(q), None, ptr(idx), ptr(dis), 1)
+            rates[t] = nq / (time.perf_counter() - t0)
+        line.update({"metric": "k-NN queries/s with the per-coordinate distances "
+                               "(knn_full_thread, L1; chi2 beside it)",
+                     "unit": "queries/s", "value": rates[1], "ms_per_step": 1e3 * nq / rates[1],
+                     "config": {"workload": f"knn_full_thread distance_type 1 (L1) nb={nb} "
+                                            f"nq={nq} d={d} k={k}, SIFT-like", "nb": nb, "nq": nq,
+                                "d": d, "k": k},
+                     "chi2_queries_per_s": rates[3],
+                     "e2e": {"value": rates[1], "unit": "queries/s",
+                             "h2d_bytes_per_step": 4 * (nb + nq) * d,
+                             "d2h_bytes_per_step": 8 * nq * k}})
+        if not args.no_cpu:
+            nt = os.cpu_count() or 1
+            nqs = nq
+            qs = np.ascontiguousarray(q[:nqs])
+            oi = np.empty((nqs, k), np.int32)
+            od = np.empty((nqs, k), np.float32)
+            t0 = time.perf_counter()
+            oracle().orc_knn_port(1, nqs, nb, d, k, ptr(b), ptr(qs), None, ptr(oi), ptr(od), nt)
+            cdt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": nqs / cdt, "unit": "queries/s", "cores": nt,
+                                    "kind": "port",
+                                    "sample": f"knn_full_thread L1 in the reference's arithmetic "
+                                              f"(bit-identical to it) for {nqs} queries"}
     else:
         nb, nq, d, k, nhash = (args.n or 1_000_000), 10_000, 128, 100, 4
         b = synth.sift_like(nb, d, seed=1)
@@ -627,13 +693,14 @@ def main():
     ap.add_argument("--e2e-pairs", type=int, default=64,
                     help="knn_batch: pairs timed end to end from host buffers")
     ap.add_argument("--workload", default="knn",
-                    choices=["knn", "kmeans1", "kmeans3", "hkm4", "knn_batch", "gmm", "kmlsh"],
+                    choices=["knn", "kmeans1", "kmeans3", "hkm4", "knn_batch", "gmm", "kmlsh",
+                             "vlad", "alt"],
                     help="knn: the headline configuration; the others are the k-means / hkm "
-                         "configurations and the path's callers (gmm, kmlsh), reported "
+                         "configurations and the path's callers (gmm, kmlsh, vlad, alt), reported "
                          "separately")
     args = ap.parse_args()
     world, rank, local = dist_setup()
-    if args.workload in ("gmm", "kmlsh"):
+    if args.workload in ("gmm", "kmlsh", "vlad", "alt"):
         if args.impl == "reference":
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable":
