@@ -308,7 +308,8 @@ class _quiet_stdout:
 def run_callers(args, world, rank, local):
     """The path's callers, timed through their drop-in calls with host buffers
     (host <-> device copies included): gmm_learn / gmm_compute_p / gmm_fisher,
-    kmlsh_ann_fvec, vlad_compute, knn_full_thread with the L1 / chi2 distances.
+    kmlsh_ann_fvec, vlad_compute, knn_full_thread with the L1 / chi2 distances,
+    kmeans with KMEANS_L1.
     The CPU figure is the oracle's restatement in the reference's arithmetic on
     a bounded sample, on the host's threads."""
     import torch
@@ -325,7 +326,8 @@ def run_callers(args, world, rank, local):
             getattr(L, name).argtypes = argt
     os.environ["YAEL_GPU_PRECISION"] = args.prec
     line = {"n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "data": "synthetic", "dtype": "f32" if args.workload in ("gmm", "alt") else args.prec,
+            "data": "synthetic",
+            "dtype": "f32" if args.workload in ("gmm", "alt", "kmeans_l1") else args.prec,
             "steps": 1, "warmup": 1}
     if args.workload == "gmm":
         import gmm_oracle as go
@@ -420,6 +422,38 @@ def run_callers(args, world, rank, local):
                                     "cores": nt, "kind": "port",
                                     "sample": f"vlad_compute in the reference's arithmetic "
                                               f"(bit-identical to it) on {sub.shape[0]} vectors"}
+    elif args.workload == "kmeans_l1":
+        n, d, k, niter, seed = (args.n or 100_000), 128, 256, (args.niter or 5), 3
+        v = synth.sift_like(n, d, seed=41)
+        C = np.zeros((k, d), np.float32)
+        flags = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM | yg.KMEANS_L1
+        with _quiet_stdout():
+            L.kmeans(d, 5000, k, 1, ptr(v), flags, seed, 1, ptr(C), None, None, None)  # warm-up
+        t0 = time.perf_counter()
+        with _quiet_stdout():
+            L.kmeans(d, n, k, niter, ptr(v), flags, seed, 1, ptr(C), None, None, None)
+        dt = time.perf_counter() - t0
+        line.update({"metric": "L1 k-means iterations/s (kmeans with KMEANS_L1: exhaustive L1 "
+                               "assignment, per-coordinate medians)",
+                     "unit": "iterations/s", "value": niter / dt, "ms_per_step": 1e3 * dt / niter,
+                     "config": {"workload": f"kmeans KMEANS_L1 n={n} d={d} k={k} niter={niter} "
+                                            f"seed={seed}, SIFT-like", "n": n, "d": d, "k": k},
+                     "e2e": {"value": niter / dt, "unit": "iterations/s",
+                             "h2d_bytes_per_step": 4 * n * d // niter,
+                             "d2h_bytes_per_step": 4 * k * d // niter}})
+        if not args.no_cpu:
+            nt = os.cpu_count() or 1
+            sub = np.ascontiguousarray(v[: n // 10])
+            Cc = np.zeros((k, d), np.float32)
+            t0 = time.perf_counter()
+            oracle().orc_kmeans(d, sub.shape[0], k, 2, ptr(sub), nt | (flags & ~0xffff), seed, 1,
+                                ptr(Cc), None, None, None, 0, None)
+            cdt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": 2 * (sub.shape[0] / n) / cdt,
+                                    "unit": "iterations/s", "cores": nt, "kind": "port",
+                                    "sample": f"2 iterations of KMEANS_L1 in the reference's "
+                                              f"arithmetic (bit-identical to it) on "
+                                              f"{sub.shape[0]} points, scaled to n"}
     elif args.workload == "alt":
         nb, nq, d, k = (args.n or 100_000), 1000, 128, 10
         b = synth.sift_like(nb, d, seed=1)
@@ -698,13 +732,14 @@ def main():
                     help="knn_batch: pairs timed end to end from host buffers")
     ap.add_argument("--workload", default="knn",
                     choices=["knn", "kmeans1", "kmeans3", "hkm4", "knn_batch", "gmm", "kmlsh",
-                             "vlad", "alt"],
+                             "vlad", "alt", "kmeans_l1"],
                     help="knn: the headline configuration; the others are the k-means / hkm "
-                         "configurations and the path's callers (gmm, kmlsh, vlad, alt), reported "
+                         "configurations and the path's callers (gmm, kmlsh, vlad, alt, "
+                         "kmeans_l1), reported "
                          "separately")
     args = ap.parse_args()
     world, rank, local = dist_setup()
-    if args.workload in ("gmm", "kmlsh", "vlad", "alt"):
+    if args.workload in ("gmm", "kmlsh", "vlad", "alt", "kmeans_l1"):
         if args.impl == "reference":
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable":

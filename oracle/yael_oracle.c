@@ -622,21 +622,100 @@ static void kmeanspp_init(int d, int n, int k, const float *v, int *sel, unsigne
 /* ------------------------------------------------------------------ */
 /* kmeans (yael/kmeans.c:213-447), L2 only                              */
 
+static int cmp_float(const void *a, const void *b)
+{
+  float x = *(const float *)a, y = *(const float *)b;
+  return x < y ? -1 : x > y;
+}
+
+/* fvec_median (yael/sorting.c:676-703): an order statistic, so the value of
+ * a sorted copy equals the reference's in-place selection (non-NaN data) */
+static float median_port(const float *f, int n, float *work)
+{
+  if (n == 0) return 0.0f / 0.0f;
+  if (n == 1) return f[0];
+  memcpy(work, f, sizeof(float) * (size_t)n);
+  qsort(work, (size_t)n, sizeof(float), cmp_float);
+  int halfn = n / 2;
+  if (n % 2 == 1) return work[halfn];
+  return (float)(0.5 * (work[halfn] + work[halfn - 1]));
+}
+
+/* minimize_sum_chi2 (yael/kmeans.c:95-158): Newton steps in float over a[]
+ * in the order given */
+static float chi2_port(const float *a, int n)
+{
+  if (n == 0) return 0.0f / 0.0f;
+  if (n == 1) return a[0];
+  float x, prev_x = 0, mag = 0;
+  for (int i = 0; i < n; i++) mag += a[i];
+  mag /= n;
+  x = 0;
+  int niter = 0;
+  do {
+    float dv = 0, dd = 0;
+    for (int i = 0; i < n; i++) {
+      float sum2 = (x + a[i]) * (x + a[i]);
+      float sum3 = (x + a[i]) * sum2;
+      if (sum2 == 0) continue;
+      dv += (x - a[i]) * (x + 3 * a[i]) / sum2;
+      dd += 8 * a[i] * a[i] / sum3;
+    }
+    if (dv == 0) break;
+    prev_x = x;
+    x -= dv / dd;
+    if (x < 0) x = (float)(prev_x / 2.0);
+    if (++niter == 1000) break;
+  } while (fabs(x - prev_x) > 1e-4 * mag);
+  return x;
+}
+
+/* the L1 / chi2 centroid update of kmeans_core (yael/kmeans.c:253-275): each
+ * cluster's coordinates gathered column by column, the cluster's points in
+ * decreasing index order, then the median / the chi2 minimiser of each */
+static void update_alt_port(int d, int n, int k, const float *v, const int *assign,
+                            const int *nassign, int l1, float *C)
+{
+  float *tmp_v = malloc(sizeof(float) * ((size_t)n * d + 1));
+  float *work = malloc(sizeof(float) * ((size_t)n + 1));
+  int *cum = malloc(sizeof(int) * (size_t)k);
+  int run = 0;
+  for (int c = 0; c < k; c++) { run += nassign[c]; cum[c] = run; }
+  for (long i = 0; i < n; i++) {
+    int w = --cum[assign[i]];
+    for (long j = 0; j < d; j++) tmp_v[w + j * n] = v[i * d + j];
+  }
+  for (long c = 0; c < k; c++)
+    for (long j = 0; j < d; j++) {
+      const float *col = tmp_v + cum[c] + j * n;
+      C[c * d + j] = l1 ? median_port(col, nassign[c], work) : chi2_port(col, nassign[c]);
+    }
+  free(cum); free(work); free(tmp_v);
+}
+
 static int kmeans_core(int d, int n, int k, int niter, int nt, int flags, float *C,
                        const float *v, unsigned int seed, int *assign, int *nassign,
                        float *dis, double *qerr_out, long *iter_tot, int mode, int S)
 {
+  const int alt = (flags & (ORC_KMEANS_L1 | ORC_KMEANS_CHI2)) != 0;
+  const int l1 = (flags & ORC_KMEANS_L1) != 0;
+  if (alt && mode != ORC_PORT) {
+    fprintf(stderr, "oracle: L1 / chi2 k-means is restated in port mode only\n");
+    abort();
+  }
   double qerr = HUGE_VAL, qerr_old;
   int tot_re = 0;
   for (int iter = 1; iter <= niter; iter++) {
     (*iter_tot)++;
     if (mode == ORC_PORT)
-      orc_knn_port(2, n, k, d, 1, C, v, NULL, assign, dis, nt);
+      orc_knn_port(alt ? (l1 ? 1 : 3) : 2, n, k, d, 1, C, v, NULL, assign, dis, nt);
     else
       assign_exact(d, n, k, v, C, assign, dis, nt);
     memset(nassign, 0, sizeof(int) * k);
     for (int i = 0; i < n; i++) nassign[assign[i]]++;
-    if (mode == ORC_PORT) {
+    if (alt) {
+      update_alt_port(d, n, k, v, assign, nassign, l1, C);
+    } else if (mode == ORC_PORT) {
       memset(C, 0, sizeof(float) * (size_t)k * d);
       for (long i = 0; i < n; i++) {
         float *c = C + (long)assign[i] * d;
@@ -647,7 +726,8 @@ static int kmeans_core(int d, int n, int k, int niter, int nt, int flags, float 
       update_exact(d, n, k, v, assign, nassign, C, S);
     }
     if (flags & ORC_KMEANS_NORMALIZE_CENTS)
-      for (long c = 0; c < k; c++) mul_by(C + c * d, d, 1. / norm_l2(C + c * d, d));
+      for (long c = 0; c < k; c++)
+        mul_by(C + c * d, d, 1. / (l1 ? norm_l1(C + c * d, d) : norm_l2(C + c * d, d)));
     int nre = reassign_empty(d, k, C, nassign, rand_r(&seed));
     tot_re += nre;
     if (tot_re > n / 100 && tot_re > 1000) return -1;

@@ -1,13 +1,14 @@
 """The oracle (C restatement) pinned against the reference's own outputs
 (tests/golden, generated by running the compiled reference) and against a
 numpy FP64 brute force.  CPU only."""
+import ctypes
 import os
 
 import numpy as np
 import pytest
 
 from _util import (GOLDEN, check_knn_ties, exact_dist64, knn_exact, knn_port, oracle, ptr,
-                   srand48)
+                   reference, srand48)
 
 
 def load(name):
@@ -62,6 +63,10 @@ def test_reference_equals_exact_modulo_ties():
         assert check_knn_ties(ridx, exact_dist64(g["b"], g["q"], ridx), idx, d64) == 0
         if k == 1:  # the k=1 path is strict '<' over increasing ids: lowest id wins
             np.testing.assert_array_equal(ridx, idx)
+
+
+I = ctypes.c_int
+P = ctypes.c_void_p
 
 
 def run_kmeans(v, k, niter, flags, seed, redo, mode):
@@ -168,3 +173,34 @@ def test_random_init_is_partial_fisher_yates():
     sel = np.empty(5, np.int32)
     oracle().orc_random_init(10, 5, 123, ptr(sel))
     assert len(set(sel.tolist())) == 5 and sel.min() >= 0 and sel.max() < 10
+
+
+@pytest.mark.parametrize("name", ["kmeans_l1", "kmeans_chi2"])
+def test_port_kmeans_l1_chi2_matches_reference(name):
+    """The oracle's port of KMEANS_L1 / KMEANS_CHI2 (L1 / chi2 assignment
+    through its knn_full port, medians / chi2 minimisers over the cluster
+    columns in the reference's order) reproduces the reference's own outputs
+    bit for bit; with three threads it equals the reference library called
+    directly."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    v = g["v"]
+    k, niter, flags, seed = int(g["k"]), int(g["niter"]), int(g["flags"]), int(g["seed"])
+    r = run_kmeans(v, k, niter, flags, seed, 1, 0)
+    for key in ("C", "dis", "assign", "nassign"):
+        np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+    assert r["qerr"] == g["qerr"]
+    R = reference()
+    if R is None:
+        return
+    R.kmeans.restype = ctypes.c_float
+    R.kmeans.argtypes = [I, I, I, I, P, I, ctypes.c_long, I, P, P, P, P]
+    n, d = v.shape
+    flags3 = (flags & ~0xffff) | 3
+    C = np.zeros((k, d), np.float32)
+    dis = np.empty(n, np.float32)
+    assign = np.empty(n, np.int32)
+    nassign = np.empty(k, np.int32)
+    R.kmeans(d, n, k, niter, ptr(v), flags3, seed, 1, ptr(C), ptr(dis), ptr(assign), ptr(nassign))
+    r3 = run_kmeans(v, k, niter, flags3, seed, 1, 0)
+    for key, val in (("C", C), ("dis", dis), ("assign", assign), ("nassign", nassign)):
+        np.testing.assert_array_equal(r3[key], val, err_msg=key)
