@@ -204,3 +204,49 @@ def test_port_kmeans_l1_chi2_matches_reference(name):
     r3 = run_kmeans(v, k, niter, flags3, seed, 1, 0)
     for key, val in (("C", C), ("dis", dis), ("assign", assign), ("nassign", nassign)):
         np.testing.assert_array_equal(r3[key], val, err_msg=key)
+
+
+def test_callers_port_matches_reference_fixtures():
+    """The oracle's C restatements of the callers reproduce the reference's own
+    outputs stored in tests/golden (make_golden_callers.py): k-means LSH lists
+    slot for slot, the learned mixture and its posteriors, the VLAD descriptor
+    -- bit for bit under the BLAS the fixtures were made with."""
+    o = oracle()
+    g = load("kmlsh.npz")
+    vb, vq, k, nhash = g["vb"], g["vq"], int(g["k"]), int(g["nhash"])
+    o.orc_kmlsh_ann.argtypes = [P, I, P, I, I, I, I, I, I, I, P, P]
+    idx = np.empty((vq.shape[0], k), np.int32)
+    dis = np.empty((vq.shape[0], k), np.float32)
+    srand48(int(g["srand48"]))
+    o.orc_kmlsh_ann(ptr(vb), vb.shape[0], ptr(vq), vq.shape[0], vb.shape[1], k, nhash, 0, 0, 1,
+                    ptr(idx), ptr(dis))
+    exact = same_blas(g)
+    if exact:
+        np.testing.assert_array_equal(idx, g["idx"])
+        np.testing.assert_array_equal(dis, g["dis"])
+    else:
+        assert (idx == g["idx"]).mean() > 0.99
+    g = load("gmm.npz")
+    v, k = g["v"], int(g["k"])
+    n, d = v.shape
+    o.orc_gmm_learn.argtypes = [I] * 4 + [P] + [I] * 4 + [P, P, P, P]
+    o.orc_gmm_compute_p.argtypes = [I, P, I, I, P, P, P, P, I, I]
+    w, mu, sg = np.empty(k, np.float32), np.empty((k, d), np.float32), np.empty((k, d), np.float32)
+    assert o.orc_gmm_learn(d, n, k, int(g["niter"]), ptr(v), 1, int(g["seed"]), 1, int(g["flags"]),
+                           ptr(w), ptr(mu), ptr(sg), None) == 0
+    p = np.empty((n, k), np.float32)
+    o.orc_gmm_compute_p(n, ptr(v), d, k, ptr(w), ptr(mu), ptr(sg), ptr(p), 1, 1)
+    for got, key in ((w, "w"), (mu, "mu"), (sg, "sigma"), (p, "p")):
+        if exact:
+            np.testing.assert_array_equal(got, g[key], err_msg=key)
+        else:
+            np.testing.assert_allclose(got, g[key], rtol=1e-4, atol=1e-5, err_msg=key)
+    g = load("vlad.npz")
+    C, v = g["C"], g["v"]
+    o.orc_vlad_compute.argtypes = [I, I, P, I, P, P, I]
+    desc = np.empty_like(g["desc"])
+    o.orc_vlad_compute(C.shape[0], C.shape[1], ptr(C), v.shape[0], ptr(v), ptr(desc), 1)
+    if exact:
+        np.testing.assert_array_equal(desc, g["desc"])
+    else:
+        np.testing.assert_allclose(desc, g["desc"], rtol=1e-5, atol=1e-4)
