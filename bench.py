@@ -152,8 +152,8 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes (read + write) of one main-pass launch at the default k-NN sizes,
-# from the ncu capture summarised in profiles/tc_scan_knn_main_nb1M_nq10k.md
+# dram__bytes_read.sum + dram__bytes_write.sum of one main-pass launch at the
+# default k-NN sizes (one ncu capture of tc_scan_kernel, THRESH mode)
 KNN_MAIN_TRAFFIC = 325.835776e6 + 44.952832e6
 
 CLUSTER_CFG = {
@@ -165,127 +165,350 @@ CLUSTER_CFG = {
 }
 
 
-def run_clustering(args, world, rank, local):
-    """k-means / hkm configurations: iterations per second on GB300, the plain
-    FP32 assignment beside the BF16+re-rank one, the reference algorithm
-    (oracle port) on the host cores for a bounded sample."""
+def flush_l2(dev, nbytes=256 << 20):
+    """Writes a buffer larger than the L2 (129 MB) so the next run starts cold."""
+    import torch
+    buf = getattr(flush_l2, "buf", None)
+    if buf is None or buf.device != dev:
+        buf = flush_l2.buf = torch.empty(nbytes // 4, dtype=torch.float32, device=dev)
+    buf.fill_(1.0)
+
+
+def cluster_data(name, c, dev):
+    """The configuration's points: a seeded Gaussian mixture.  The large one is
+    drawn on the device (5 GB; the host copy only of the CPU sample)."""
+    import torch
+    from yael_gb300 import synth
+    w = synth.zipf_weights(c["comps"], c["zipf"]) if c.get("zipf") else None
+    if c["n"] <= 2_000_000:
+        v_h, _, _ = synth.gaussian_mixture(c["n"], c["d"], c["comps"], c["sigma"], seed=11,
+                                           weights=w)
+        return torch.from_numpy(v_h).to(dev), v_h
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    centres = torch.randn((c["comps"], c["d"]), device=dev, generator=g)
+    p = torch.ones(c["comps"], device=dev) if w is None else torch.from_numpy(w).to(dev)
+    lab = torch.multinomial(p, c["n"], replacement=True, generator=g)
+    v = torch.empty((c["n"], c["d"]), device=dev)
+    step = 1 << 20
+    for s0 in range(0, c["n"], step):
+        e = min(c["n"], s0 + step)
+        v[s0:e] = centres[lab[s0:e]] + c["sigma"] * torch.randn((e - s0, c["d"]), device=dev,
+                                                                generator=g)
+    return v, None
+
+
+def kmeans_record(name, args, local):
+    """One k-means configuration (kmeans1 / kmeans3) on GB300: Lloyd iterations
+    per second of the chosen form (16-bit tensor-core pass + exact re-rank)
+    with the points resident in HBM, the plain FP32 path beside it, the
+    drop-in kmeans() end to end from host buffers, the oracle's FP64 check of
+    the assignment of every iteration, and the reference algorithm (the
+    oracle's port) on the host cores."""
+    import torch
+    import yael_gb300 as yg
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _util import assign_mismatches, objective64, oracle, ptr
+    dev = torch.device("cuda", local)
+    L = yg.lib()
+    c = dict(CLUSTER_CFG[name])
+    if args.niter:
+        c["niter"] = args.niter
+    if args.n:
+        c["n"] = args.n
+    dv, v_h = cluster_data(name, c, dev)
+    n, d = dv.shape
+    k, niter, seed = c["k"], c["niter"], c["seed"]
+    C = torch.empty((k, d), device=dev)
+    dis = torch.empty(n, device=dev)
+    assign = torch.empty(n, dtype=torch.int32, device=dev)
+    flags = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
+    stream = torch.cuda.current_stream(dev)
+    libc = ctypes.CDLL(None)
+    libc.srand48.argtypes = [ctypes.c_long]
+    nt = os.cpu_count() or 1
+
+    def run(prec, it=niter, probe=None):
+        # seed 0 draws the k-means seed from lrand48(): the same state for every run
+        libc.srand48(0)
+        o = yg.KmeansOpts(prec, 1, ctypes.c_void_p(stream.cuda_stream))
+        if probe:
+            for key, val in probe.items():
+                setattr(o, key, val)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        q = L.yael_gpu_kmeans_ex(d, n, k, it, dv.data_ptr(), flags, seed, 1, C.data_ptr(),
+                                 dis.data_ptr(), assign.data_ptr(), None, ctypes.byref(o))
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if o.status != 0:
+            raise RuntimeError(yg.last_error())
+        return q, e0.elapsed_time(e1), o
+
+    prec = yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32
+    run(prec)  # warm-up: kernel attributes, the chunk tuner's trials
+    runs = max(1, args.cluster_runs if n <= 200_000 else 1)
+    ms_tot, iters, ms_assign = 0.0, 0, 0.0
+    l0 = L.yael_gpu_launch_count()
+    with ClockSampler(local) as clk:
+        for _ in range(runs):
+            flush_l2(dev)
+            q, ms, o = run(prec)
+            ms_tot += ms
+            iters += o.iterations
+            ms_assign += o.ms_assign
+    launches = L.yael_gpu_launch_count() - l0
+    prec_used = {0: "f32", 1: "bf16", 2: "bf16x3", 3: "f16"}.get(o.prec_used, "?")
+    a_ch = assign.cpu().numpy().copy()
+    rec = {"metric": METRIC, "value": 1e3 * iters / ms_tot, "unit": "iterations/s",
+           "ms_per_step": ms_tot / iters, "steps": iters, "warmup": 1, "runs": runs,
+           "higher_is_better": True, "dtype": prec_used,
+           "config": {"workload": f"k-means n={n} d={d} k={k} niter={niter} seed={seed}, "
+                                  f"Gaussian mixture ({c['comps']} comps, sigma={c['sigma']}"
+                                  + (f", Zipf({c['zipf']}) weights" if c.get('zipf') else "")
+                                  + "), random init", "n": n, "d": d, "k": k,
+                      "l2": ("flushed between runs (256 MB written); the 51 MB of points "
+                             "stay in L2 across one run's iterations" if 4 * n * d < 100e6
+                             else "inputs larger than L2")},
+           "qerr": q, "assign_ms_per_iter": ms_assign / iters,
+           "update_ms_per_iter": (ms_tot - ms_assign) / iters,
+           "band_pass_points": int(o.n_band), "split_pass_points": int(o.n_second),
+           "fallback_points": int(o.n_fallback), "gpu_launches": launches,
+           "clocks": clk.summary()}
+    pk_tf, pk_hbm, pk_src = peaks()
+    flop = 2.0 * n * k * d
+    rec["roofline"] = {"bound": "tensor",
+                       "kernel": "assignment step (packing, 16-bit tensor-core pass, exact "
+                                 "re-rank), CUDA events per iteration",
+                       "achieved": flop / (ms_assign / iters / 1e3) / 1e12, "unit": "TFLOP/s",
+                       "peak": pk_tf, "peak_source": pk_src,
+                       "algorithmic": f"2*n*k*d = {flop:.4g} flop per iteration",
+                       "traffic": None}
+    rec["roofline"]["frac"] = rec["roofline"]["achieved"] / pk_tf
+    bytes_it = 2.0 * 4 * n * d  # the points read by the assignment and the update
+    rec["hbm_view"] = {"achieved_gbs": bytes_it / (ms_tot / iters / 1e3) / 1e9,
+                       "peak_gbs": pk_hbm, "frac": bytes_it / (ms_tot / iters / 1e3) / 1e9 / pk_hbm,
+                       "algorithmic": "2 x 4*n*d bytes per iteration (assignment + update)"}
+    # the plain FP32 path (the drop-in default): the whole run where it takes
+    # seconds, its first iteration on the large configuration
+    it32 = niter if n <= 200_000 else 1
+    flush_l2(dev)
+    q32, ms32, o32 = run(yg.PREC_FP32, it32)
+    rec["plain_fp32"] = {"value": 1e3 * o32.iterations / ms32, "unit": "iterations/s",
+                         "iterations_timed": int(o32.iterations),
+                         "assign_ms_per_iter": o32.ms_assign / max(1, o32.iterations)}
+    if it32 == niter:
+        rec["plain_fp32"]["same_assignments"] = bool((assign.cpu().numpy() == a_ch).all())
+    rec["speedup_vs_plain_fp32"] = rec["value"] / rec["plain_fp32"]["value"]
+    # parity: the assignment of every iteration against the oracle's FP64
+    # nearest centroid (all points on the small configuration, a fixed sample
+    # of 100k on the large one), the objective against the FP64 sum
+    if not args.no_check:
+        nprobe = n if n <= 200_000 else min(n, 100_000)
+        rows = (np.arange(n, dtype=np.int64) if nprobe == n else
+                np.sort(np.random.default_rng(0).choice(n, nprobe, replace=False)))
+        pa = np.empty((niter, nprobe), np.int32)
+        pc = np.empty((niter, k, d), np.float32)
+        pq = np.zeros(niter, np.float64)
+        probe = {"n_probe": nprobe, "probe_rows": rows.ctypes.data, "probe_iters": niter,
+                 "probe_assign": pa.ctypes.data, "probe_centroids": pc.ctypes.data,
+                 "probe_qerr": pq.ctypes.data}
+        _, _, op = run(prec, niter, probe)
+        T = int(op.iterations)
+        a_fin = assign.cpu().numpy()
+        xs = (v_h if v_h is not None else None)
+        if xs is None or nprobe != n:
+            xs = np.ascontiguousarray(dv[torch.from_numpy(rows).to(dev)].cpu().numpy())
+        t0 = time.perf_counter()
+        bad = [assign_mismatches(xs, pc[t], pa[t], nt)[0] for t in range(T)]
+        vh = v_h if v_h is not None else None
+        if vh is None:
+            vh = dv.cpu().numpy()
+        q64 = objective64(vh, pc[T - 1], a_fin, nt)
+        rec["parity"] = {
+            "checked_points_per_iteration": nprobe, "iterations_checked": T,
+            "assignment_mismatches_vs_fp64_oracle": int(sum(bad)),
+            "same_run_as_timed": bool((a_fin == a_ch).all()),
+            "objective_last_iteration": float(pq[T - 1]), "objective_fp64": q64,
+            "objective_rel_err_vs_fp64": abs(float(pq[T - 1]) - q64) / q64,
+            "check_seconds": time.perf_counter() - t0}
+        if n <= 200_000:
+            # the whole run against the oracle's exact-mode k-means
+            Co = np.zeros((k, d), np.float32)
+            ao = np.empty(n, np.int32)
+            libc.srand48(0)
+            qo = oracle().orc_kmeans(d, n, k, niter, ptr(v_h), nt | flags, seed, 1, ptr(Co),
+                                     None, ptr(ao), None, 1, None)
+            rec["parity"]["oracle_exact_kmeans"] = {
+                "assignments_identical": bool((ao == a_fin).all()),
+                "centroids_bit_identical": bool((Co == C.cpu().numpy()).all()),
+                "qerr_rel_diff": abs(float(qo) - float(q)) / abs(float(qo))}
+        del pc
+    # end to end: the drop-in kmeans() with host buffers (copies included)
+    vh = v_h if v_h is not None else dv.cpu().numpy()
+    vp = torch.from_numpy(vh).pin_memory()
+    Ch = torch.empty((k, d)).pin_memory()
+    dh = torch.empty(n).pin_memory()
+    ah = torch.empty(n, dtype=torch.int32).pin_memory()
+    nh = torch.empty(k, dtype=torch.int32).pin_memory()
+    os.environ["YAEL_GPU_PRECISION"] = args.prec
+    libc.srand48(0)
+    t0 = time.perf_counter()
+    L.kmeans(d, n, k, niter, vp.data_ptr(), flags, seed, 1, Ch.data_ptr(), dh.data_ptr(),
+             ah.data_ptr(), nh.data_ptr())
+    te = time.perf_counter() - t0
+    rec["e2e"] = {"value": (iters / runs) / te, "unit": "iterations/s",
+                  "h2d_bytes_per_step": 4 * n * d, "d2h_bytes_per_step": 4 * (k * d + 2 * n + k),
+                  "api": "kmeans (drop-in C ABI), pinned host buffers, one whole run per step"}
+    del vp
+    # the reference algorithm (oracle port) on the host cores: the whole run on
+    # the small configuration, one iteration on 1% of the points on the large one
+    if not args.no_cpu:
+        sub = vh if n <= 200_000 else np.ascontiguousarray(vh[: n // 100])
+        it = niter if n <= 200_000 else 1
+        Cc = np.zeros((k, d), np.float32)
+        libc.srand48(0)
+        t0 = time.perf_counter()
+        oracle().orc_kmeans(d, sub.shape[0], k, it, ptr(sub), nt | flags, seed, 1, ptr(Cc),
+                            None, None, None, 0, None)
+        cdt = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": it * (sub.shape[0] / n) / cdt, "unit": "iterations/s",
+                               "cores": nt, "kind": "port",
+                               "sample": f"{it} iteration(s) on {sub.shape[0]} points, seed "
+                                         f"{seed}, value scaled to the full n"}
+    del dv
+    torch.cuda.empty_cache()
+    return rec
+
+
+def hkm_record(args, local):
+    """Hierarchical k-means (n = 2M, d = 96, bf = 32, 3 levels, 15 iterations)
+    through yael_gpu_hkm_learn_ex and the drop-in hkm_learn (both from host
+    buffers; the tree is a host-array API), parity on a tenth of the points
+    against the oracle's exact-mode tree, the reference algorithm on the host."""
     import torch
     import yael_gb300 as yg
     from yael_gb300 import synth
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from _util import oracle, ptr
-    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
     L = yg.lib()
-    c = dict(CLUSTER_CFG[args.workload])
+    c = dict(CLUSTER_CFG["hkm4"])
     if args.niter:
         c["niter"] = args.niter
     if args.n:
         c["n"] = args.n
-    w = synth.zipf_weights(c["comps"], c["zipf"]) if c.get("zipf") else None
-    v_h, _, _ = synth.gaussian_mixture(c["n"], c["d"], c["comps"], c["sigma"], seed=11, weights=w)
+    v_h, _, _ = synth.gaussian_mixture(c["n"], c["d"], c["comps"], c["sigma"], seed=11)
     n, d = v_h.shape
-    line = {"metric": METRIC, "unit": "iterations/s", "n_gpus": world, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "data": "synthetic", "dtype": args.prec}
-    if args.workload.startswith("kmeans"):
-        k, niter, seed = c["k"], c["niter"], c["seed"]
-        dv = torch.from_numpy(v_h).cuda()
-        C = torch.empty((k, d), device="cuda")
-        dis = torch.empty(n, device="cuda")
-        assign = torch.empty(n, dtype=torch.int32, device="cuda")
-        flags = yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
+    nl, bf, niter = c["nlevel"], c["bf"], c["niter"]
+    ncent = sum(bf ** (l + 1) for l in range(nl))
+    cent = np.empty(ncent * d, np.float32)
+    assign = np.empty(n, np.int32)
+    it, ms = ctypes.c_long(0), ctypes.c_float(0)
+    vp = torch.from_numpy(v_h).pin_memory()
 
+    def learn(x, nn):
         libc = ctypes.CDLL(None)
-
-        def run(prec):
-            # seed 0 draws the k-means seed from lrand48(): reset its state so
-            # every form clusters from the same seed
-            libc.srand48(ctypes.c_long(0))
-            o = yg.KmeansOpts(prec, 1, None, 0, 0, 0, 0, 0, 0)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            q = L.yael_gpu_kmeans_ex(d, n, k, niter, dv.data_ptr(), flags, seed, 1, C.data_ptr(),
-                                     dis.data_ptr(), assign.data_ptr(), None, ctypes.byref(o))
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
-            assert o.status == 0, yg.last_error()
-            return q, dt, o
-
-        run(yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32)  # warm-up
-        prec = yg.PREC_BF16 if args.prec == "bf16" else yg.PREC_FP32
-        l0 = L.yael_gpu_launch_count()
-        q, dt, o = run(prec)
-        launches = L.yael_gpu_launch_count() - l0
-        a_bf = assign.cpu().numpy().copy()
-        q32, dt32, o32 = run(yg.PREC_FP32)
-        same_assign = bool((assign.cpu().numpy() == a_bf).all())
-        line.update({
-            "value": o.iterations / dt, "ms_per_step": 1e3 * dt / max(1, o.iterations),
-            "steps": int(o.iterations), "warmup": 1,
-            "config": {"workload": f"k-means n={n} d={d} k={k} niter={niter} seed={seed}, "
-                                   f"Gaussian mixture ({c['comps']} comps, sigma={c['sigma']}"
-                                   + (f", Zipf({c['zipf']}) weights" if c.get('zipf') else "")
-                                   + "), random init", "n": n, "d": d, "k": k},
-            "qerr": q, "assign_ms_per_iter": o.ms_assign / max(1, o.iterations),
-            "update_ms_per_iter": o.ms_update / max(1, o.iterations),
-            "fallback_points": int(o.n_fallback), "band_pass_points": int(o.n_band),
-            "split_pass_points": int(o.n_second),
-            "gpu_launches": launches,
-            "plain_fp32": {"value": o32.iterations / dt32, "qerr": q32,
-                           "assign_ms_per_iter": o32.ms_assign / max(1, o32.iterations),
-                           "same_assignments_as_bf16": same_assign},
-            "roofline": {"bound": "tensor", "kernel": "assignment pass",
-                         "achieved": 2.0 * n * k * d / (o.ms_assign / max(1, o.iterations) / 1e3) / 1e12,
-                         "unit": "TFLOP/s", "peak": peaks()[0], "peak_source": peaks()[2]},
-        })
-        line["roofline"]["frac"] = line["roofline"]["achieved"] / line["roofline"]["peak"]
-        if not args.no_cpu:
-            # reference algorithm (oracle port) on the host: whole run for the small
-            # configuration, one iteration on 1/100 of the points for the large one
-            nt = os.cpu_count() or 1
-            sub = v_h if n <= 200_000 else np.ascontiguousarray(v_h[: n // 100])
-            it = niter if n <= 200_000 else 1
-            Cc = np.zeros((k, d), np.float32)
-            t0 = time.perf_counter()
-            oracle().orc_kmeans(d, sub.shape[0], k, it, ptr(sub), nt | flags, 1234, 1, ptr(Cc),
-                                None, None, None, 0, None)
-            cdt = time.perf_counter() - t0
-            scale = sub.shape[0] / n
-            line["cpu_baseline"] = {"value": it * scale / cdt, "unit": "iterations/s",
-                                    "cores": nt, "kind": "port",
-                                    "sample": f"{it} iteration(s) on {sub.shape[0]} points "
-                                              f"(value scaled to the full n)"}
-    else:
-        nl, bf, niter = c["nlevel"], c["bf"], c["niter"]
-        cent = np.empty(sum(bf ** (l + 1) for l in range(nl)) * d, np.float32)
-        assign = np.empty(n, np.int32)
-        it, ms = ctypes.c_long(0), ctypes.c_float(0)
-        L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, 1, ptr(cent), ptr(assign), None,
-                                None)
-        t0 = time.perf_counter()
-        rc = L.yael_gpu_hkm_learn_ex(n, d, nl, bf, ptr(v_h), niter, 1, ptr(cent), ptr(assign),
+        libc.srand48(ctypes.c_long(0))
+        st = yg.CallStats()
+        rc = L.yael_gpu_hkm_learn_ex(nn, d, nl, bf, x, niter, 1, ptr(cent), ptr(assign),
                                      ctypes.byref(it), ctypes.byref(ms))
-        dt = time.perf_counter() - t0
         assert rc == 0, yg.last_error()
-        line.update({"value": it.value / dt, "unit": "instance-iterations/s",
-                     "ms_per_step": 1e3 * dt, "steps": 1, "warmup": 1,
-                     "config": {"workload": f"hierarchical k-means n={n} d={d} bf={bf} "
-                                            f"nlevel={nl} niter={niter}", "n": n, "d": d},
-                     "hkm_seconds": dt, "gpu_ms": ms.value, "instance_iterations": it.value})
-        if not args.no_cpu:
-            nt = os.cpu_count() or 1
-            sub = np.ascontiguousarray(v_h[: n // 10])
-            oc = np.empty_like(cent)
-            t0 = time.perf_counter()
-            oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(oc), None, 0)
-            cdt = time.perf_counter() - t0
-            # the tree has the same instances and iterations at n / 10; each
-            # instance's work is linear in its points: time x 10 for the full n
-            line["cpu_baseline"] = {"value": it.value / (10 * cdt),
-                                    "unit": "instance-iterations/s", "seconds_on_tenth": cdt,
-                                    "cores": nt, "kind": "port",
-                                    "sample": f"hkm_learn on n/10 = {sub.shape[0]} points, time "
-                                              f"x 10, the GPU run's instance-iteration count"}
-    print(json.dumps(line), flush=True)
+        L.yael_gpu_last_stats(ctypes.byref(st))
+        return st
+
+    # the plain FP32 form first (the drop-in default), then the chosen form
+    os.environ["YAEL_GPU_PRECISION"] = "fp32"
+    learn(vp.data_ptr(), n)
+    t0 = time.perf_counter()
+    learn(vp.data_ptr(), n)
+    dt32 = time.perf_counter() - t0
+    os.environ["YAEL_GPU_PRECISION"] = args.prec
+    learn(vp.data_ptr(), n)  # warm-up (kernel attributes, packing buffers)
+    l0 = L.yael_gpu_launch_count()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        st = learn(vp.data_ptr(), n)
+        dt = time.perf_counter() - t0
+    launches = L.yael_gpu_launch_count() - l0
+    pk_tf, pk_hbm, pk_src = peaks()
+    # algorithmic bytes: one read of every active instance's points per
+    # iteration (the fused pass reads them once; 4*d bytes a point)
+    alg = 4.0 * d * st.point_iterations
+    rec = {"metric": METRIC, "value": it.value / dt, "unit": "instance-iterations/s",
+           "ms_per_step": 1e3 * dt, "steps": 1, "warmup": 1, "higher_is_better": True,
+           "dtype": {0: "f32", 1: "bf16", 3: "f16"}.get(st.prec_used, "?"),
+           "config": {"workload": f"hierarchical k-means n={n} d={d} bf={bf} nlevel={nl} "
+                                  f"niter={niter}, Gaussian mixture ({c['comps']} comps, "
+                                  f"sigma={c['sigma']})", "n": n, "d": d,
+                      "l2": "inputs larger than L2"},
+           "tree_ms": 1e3 * dt, "gpu_ms": ms.value, "instance_iterations": it.value,
+           "level_iterations": int(st.level_iterations), "gpu_launches": launches,
+           "assign_ms": st.ms_assign, "update_ms": st.ms_update, "clocks": clk.summary(),
+           "roofline": {"bound": "hbm", "kernel": "assignment passes (all levels), CUDA events",
+                        "achieved": alg / (st.ms_assign / 1e3) / 1e9 if st.ms_assign > 0 else None,
+                        "unit": "GB/s", "peak": pk_hbm, "peak_source": pk_src,
+                        "algorithmic": "4*d bytes per point per iteration of its instance "
+                                       f"({alg:.4g} bytes in the tree)", "traffic": None}}
+    if rec["roofline"]["achieved"]:
+        rec["roofline"]["frac"] = rec["roofline"]["achieved"] / pk_hbm
+    rec["whole_tree_hbm_frac"] = alg / dt / 1e9 / pk_hbm
+    rec["plain_fp32"] = {"value": it.value / dt32, "unit": "instance-iterations/s",
+                         "tree_ms": 1e3 * dt32}
+    rec["speedup_vs_plain_fp32"] = dt32 / dt
+    # end to end: the call above takes the points from (pinned) host memory and
+    # returns the tree there; the device time excludes the upload.  (The
+    # drop-in hkm_learn stops on this data, as the reference's kmeans assert
+    # would: a level-1 child gets fewer points than bf, and small_nodes = 1
+    # gives such a node one child per point instead.)
+    rec["value"] = it.value / (ms.value / 1e3)
+    rec["e2e"] = {"value": it.value / dt, "unit": "instance-iterations/s",
+                  "h2d_bytes_per_step": 4 * n * d, "d2h_bytes_per_step": 4 * (ncent * d + n),
+                  "api": "yael_gpu_hkm_learn_ex (small_nodes = 1), pinned host buffer"}
+    nt = os.cpu_count() or 1
+    sub = np.ascontiguousarray(v_h[: n // 10])
+    if not args.no_check:
+        # the tree of a tenth of the points, GPU against the oracle's exact mode
+        cg = np.empty_like(cent)
+        ag = np.empty(sub.shape[0], np.int32)
+        libc.srand48(ctypes.c_long(0))
+        rc = L.yael_gpu_hkm_learn_ex(sub.shape[0], d, nl, bf, ptr(sub), niter, 1, ptr(cg),
+                                     ptr(ag), None, None)
+        co = np.empty_like(cent)
+        ao = np.empty(sub.shape[0], np.int32)
+        libc.srand48(ctypes.c_long(0))
+        t0 = time.perf_counter()
+        ro = oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(co), ptr(ao), 1)
+        rec["parity"] = {"points": sub.shape[0], "status": [rc, ro],
+                         "assignments_identical_to_oracle_exact": bool((ag == ao).all()),
+                         "centroids_bit_identical": bool((cg == co).all()),
+                         "check_seconds": time.perf_counter() - t0}
+    if not args.no_cpu:
+        oc = np.empty_like(cent)
+        libc.srand48(ctypes.c_long(0))
+        t0 = time.perf_counter()
+        oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(oc), None, 0)
+        cdt = time.perf_counter() - t0
+        # the tree has the same instances and iterations at n / 10; each
+        # instance's work is linear in its points: time x 10 for the full n
+        rec["cpu_baseline"] = {"value": it.value / (10 * cdt), "unit": "instance-iterations/s",
+                               "seconds_on_tenth": cdt, "cores": nt, "kind": "port",
+                               "sample": f"hkm_learn on n/10 = {sub.shape[0]} points, time x 10, "
+                                         "the GPU run's instance-iteration count"}
+    del vp
+    return rec
+
+
+def run_clustering(args, world, rank, local):
+    """--workload kmeans1 | kmeans3 | hkm4: the configuration's record as the line."""
+    import torch
+    torch.cuda.set_device(local)
+    rec = hkm_record(args, local) if args.workload == "hkm4" else kmeans_record(args.workload,
+                                                                               args, local)
+    rec.update({"n_gpus": world, "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
+    if rank == 0:
+        print(json.dumps(rec), flush=True)
 
 
 class _quiet_stdout:
@@ -551,14 +774,23 @@ def batch_sizes(npairs, seed):
 
 
 def run_knn_batch(args, world, rank, local):
+    """--workload knn_batch: the batch record as the line."""
+    import torch
+    torch.cuda.set_device(local)
+    line = knn_batch_record(args, local, world, rank)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def knn_batch_record(args, local, world=1, rank=0):
     """Batched uneven exact k-NN: 512 independent (queries, base) pairs, d = 128,
     k = 32, unit-normalised Gaussian rows, L2 and inner product, through
-    yael_gpu_knn_batch; the plain FP32 per-pair loop beside it."""
+    yael_gpu_knn_batch; the plain FP32 per-pair loop beside it; ids of a
+    sample of queries from eight pairs against the oracle's FP64 brute force."""
     import torch
     import yael_gb300 as yg
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from _util import knn_port
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     L = yg.lib()
     npairs, d, k = args.pairs, 128, 32
@@ -606,18 +838,23 @@ def run_knn_batch(args, world, rank, local):
     steps = max(1, args.steps)
     sec, launches, o, clocks = timed(yg.PREC_BF16, 2, steps, args.warmup)
     sec_ip, _, o_ip, _ = timed(yg.PREC_BF16, 16, max(1, steps // 2), 1)
-    # exactness spot check: pair 0 and the largest pair's first 16 queries vs FP64
+    # parity: up to 32 queries of each of eight pairs (the largest and smallest
+    # bases and queries, and four drawn at random) against the FP64 oracle
     check = None
     if not args.no_check:
-        from _util import knn_exact
-        ok = True
-        for i in (0, int(np.argmax(nq * nb))):
-            m = min(16, int(nq[i]))
-            ridx, _, _ = knn_exact(bs[i].cpu().numpy(), qs[i][:m].cpu().numpy(), k,
-                                   os.cpu_count() or 1)
-            batch_call(yg.PREC_BF16, 2)
-            ok = ok and bool((idx[i][:m].cpu().numpy() == ridx).all())
-        check = ok
+        from _util import knn_mismatches
+        batch_call(yg.PREC_BF16, 2)
+        torch.cuda.synchronize(dev)
+        sel = {0, int(np.argmax(nb)), int(np.argmin(nb)), int(np.argmax(nq)),
+               int(np.argmax(nq * nb))}
+        sel |= set(int(x) for x in np.random.default_rng(1).choice(npairs, 4, replace=False))
+        nbad, nchk = 0, 0
+        for i in sorted(sel):
+            m = min(32, int(nq[i]))
+            nbad += knn_mismatches(bs[i].cpu().numpy(), qs[i][:m].cpu().numpy(),
+                                   idx[i][:m].cpu().numpy(), os.cpu_count() or 1)[0]
+            nchk += m
+        check = {"pairs": len(sel), "queries": nchk, "queries_with_id_mismatch": nbad}
     # the plain FP32 path, one knn call per pair (the drop-in loop)
     t0 = time.perf_counter()
     for i in range(npairs):
@@ -677,7 +914,7 @@ def run_knn_batch(args, world, rank, local):
                           "ms_per_step": 1e3 * sec_ip, "fallback_queries": o_ip.n_fallback},
         "plain_fp32_per_pair_loop": {"value": tot_q / sec32, "unit": "queries/s",
                                      "ms_per_step": 1e3 * sec32},
-        "exact_ids_vs_fp64_oracle_spot": check,
+        "parity": check,
         "fallback_queries": o.n_fallback, "band_queries": o.n_band,
         "path": ("grouped: one persistent launch per pass over all pairs, waves pipelined"
                  if os.environ.get("YAEL_GPU_BATCH_GROUPED", "1") != "0"
@@ -695,8 +932,9 @@ def run_knn_batch(args, world, rank, local):
     }
     if cpu:
         line["cpu_baseline"] = cpu
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    del bs, qs, idx, dis
+    torch.cuda.empty_cache()
+    return line
 
 
 def config_of(args):
@@ -727,6 +965,11 @@ def main():
     ap.add_argument("--niter", type=int, default=0, help="override the clustering iterations")
     ap.add_argument("--n", type=int, default=0,
                     help="override the clustering point count (smaller cases for profiling)")
+    ap.add_argument("--cluster-runs", type=int, default=5,
+                    help="kmeans1: whole k-means runs timed (L2 flushed between runs)")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="default run: only the k-NN line, without the clustering and "
+                         "batch records")
     ap.add_argument("--pairs", type=int, default=512, help="knn_batch: number of pairs")
     ap.add_argument("--e2e-pairs", type=int, default=64,
                     help="knn_batch: pairs timed end to end from host buffers")
@@ -817,13 +1060,22 @@ def main():
     ms, launches, scan_ms, fb, clocks, sample_ms, rr_ms = timed(prec, args.steps, args.warmup)
     qps = replicas.whole_job_rate(args.nq * args.steps, ms / 1e3, world)
 
-    # parity spot check of the timed configuration (first 64 queries, FP64 oracle)
+    # parity of the timed configuration: every query's ids against the oracle's
+    # FP64 brute force (outside the timed region)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from _util import knn_exact
-    exact_ids = None
+    from _util import exact_dist64, knn_mismatches
+    parity = None
     if not args.no_check:
-        ridx, _, _ = knn_exact(b_h, q_h[:64], args.k, os.cpu_count() or 1)
-        exact_ids = bool((idx[:64].cpu().numpy() == ridx).all())
+        t0 = time.perf_counter()
+        gi, gd = idx.cpu().numpy(), dis.cpu().numpy()
+        nbad, first = knn_mismatches(b_h, q_h, gi, os.cpu_count() or 1)
+        m = min(256, args.nq)
+        d64 = exact_dist64(b_h, q_h[:m], gi[:m])
+        parity = {"queries_checked": int(args.nq), "queries_with_id_mismatch": nbad,
+                  "first_mismatch": first,
+                  "distance_max_rel_err_first256": float(
+                      np.max(np.abs(gd[:m] - d64) / np.maximum(d64, 1e-30))),
+                  "check_seconds": time.perf_counter() - t0}
 
     # plain FP32 path (the drop-in default) for the speed-up of the chosen form
     fp32 = None
@@ -874,15 +1126,13 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16" if args.prec == "bf16" else "f32", "data": "synthetic",
         "config": config_of(args),
-        "exact_ids_vs_fp64_oracle_first64": exact_ids,
+        "parity": parity,
         "fallback_queries_per_step": fb / args.steps,
         "phase_ms": {"threshold_sample_pass": sample_ms, "main_pass": scan_ms, "rerank": rr_ms},
         "roofline": {"bound": "tensor", "kernel": "tc_scan_kernel (THRESH, main pass)",
                      "achieved": achieved, "peak": pk_tf, "unit": "TFLOP/s",
                      "frac": (achieved / pk_tf) if achieved else None,
                      "peak_source": pk_src,
-                     # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this
-                     # kernel at the default sizes (profiles/tc_scan_knn_main_nb1M_nq10k.md)
                      "traffic": KNN_MAIN_TRAFFIC if (args.nb, args.nq, args.d, args.k) ==
                      (1_000_000, 10_000, 128, 100) else None,
                      "traffic_unit": "bytes per launch",
@@ -902,6 +1152,26 @@ def main():
         line["cpu_baseline"] = {"value": cqps, "unit": "queries/s", "cores": nt, "kind": "port",
                                 "sample": f"{nq_done} queries vs the full {args.nb}-row base, "
                                           f"knn_full_thread restated (BLAS {os.path.basename(blas)})"}
+    if world == 1 and not args.no_workloads:
+        # the other configurations of the metric, each a record of its own:
+        # k-means (small and large), hierarchical k-means, the batched k-NN
+        del b, q, idx, dis, bp, qp, ip, dp
+        torch.cuda.empty_cache()
+        wl = {}
+        for name in ("kmeans1", "kmeans3", "hkm4", "knn_batch"):
+            t0 = time.perf_counter()
+            try:
+                if name == "hkm4":
+                    r = hkm_record(args, local)
+                elif name == "knn_batch":
+                    r = knn_batch_record(args, local)
+                else:
+                    r = kmeans_record(name, args, local)
+            except Exception as e:  # a failed record is reported, not hidden
+                r = {"error": f"{type(e).__name__}: {e}"}
+            r["record_seconds"] = time.perf_counter() - t0
+            wl[name] = r
+        line["workloads"] = wl
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

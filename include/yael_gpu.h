@@ -431,10 +431,13 @@ int fvecs_read_txt(const char *fname, int d, int n, float *v);
 /* ------------------------------------------------------------------ */
 /* extension API                                                       */
 
-#define YAEL_GPU_PREC_ENV (-1) /* take YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), default fp32 */
+#define YAEL_GPU_PREC_ENV (-1) /* take YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3 | fp16), default fp32 */
 #define YAEL_GPU_PREC_FP32 0   /* FP32 CUDA-core distances (the plain drop-in path) */
 #define YAEL_GPU_PREC_BF16 1   /* BF16 tensor-core distances + exact FP32 re-rank */
 #define YAEL_GPU_PREC_BF16X3 2 /* tensor cores on a 3xBF16 split (x = hi + lo) + re-rank */
+#define YAEL_GPU_PREC_FP16 3   /* FP16 tensor-core distances + exact FP32 re-rank: the bf16
+                                  rate with 2^-11 rounding, for data fp16 holds (|x| < 16384,
+                                  base ||x||^2 < 2^15; other rows are settled by later passes) */
 
 /* status codes of the yael_gpu_* functions */
 #define YAEL_GPU_OK 0
@@ -462,6 +465,8 @@ typedef struct {
   int n_band;       /* rejected queries re-run through a band pass (thresholds from the
                        k-th exact distance the first re-rank found) */
   float ms_second;  /* band, split and exhaustive passes together */
+  int wait_limit_us; /* every wait inside the tensor-core passes gives up after this many
+                        microseconds (0: 2 s), and the call then returns YAEL_GPU_ETIMEOUT */
 } yael_gpu_knn_opts;
 
 /* k-NN with explicit options.  Same result contract as knn_full. */
@@ -504,6 +509,21 @@ typedef struct {
   float ms_assign; /* GPU time of the assignment steps */
   float ms_update; /* GPU time of counts, sums, splits' uploads and objective */
   long n_band;     /* points re-run through a band pass */
+  int prec_used;   /* filled: the distance pass of the last assignment (YAEL_GPU_PREC_*;
+                      the chosen form runs fp16 operands where the data range allows) */
+  /* Optional record of every iteration, for checkers of the assignment step
+   * (host memory; n_probe = 0 turns it off).  Iteration t (0-based, over all
+   * runs, t < probe_iters) stores the assignment of the n_probe points
+   * probe_rows, the centroids that assignment was made against (when
+   * probe_centroids is not NULL) and the iteration's objective (sum of the
+   * points' distances).  Recording synchronises the stream every iteration. */
+  int n_probe;
+  const long *probe_rows;
+  int probe_iters;
+  int *probe_assign;      /* probe_iters x n_probe */
+  float *probe_centroids; /* probe_iters x k x d, or NULL */
+  double *probe_qerr;     /* probe_iters, or NULL */
+  int wait_limit_us;      /* as in yael_gpu_knn_opts */
 } yael_gpu_kmeans_opts;
 
 /* kmeans() with options; returns -2 on error (message: yael_gpu_last_error). */
@@ -522,6 +542,19 @@ int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v,
                           int nb_iter_max, int small_nodes, float *centroids, int *assign,
                           long *iterations, float *ms);
 
+/* Work counters of the calling thread's last kmeans / hkm call (the drop-in
+ * symbols and the _ex functions).  No counterpart in the reference. */
+typedef struct {
+  long instance_iterations; /* Lloyd iterations summed over the clusterings run */
+  long point_iterations;    /* points assigned, summed over iterations: the rows the
+                               assignment passes had to read */
+  long level_iterations;    /* iterations of the batched loop (hkm: over all levels) */
+  float ms_assign;          /* GPU time of the assignment steps */
+  float ms_update;          /* GPU time of the updates */
+  int prec_used;            /* distance pass of the last assignment (YAEL_GPU_PREC_*) */
+} yael_gpu_call_stats;
+int yael_gpu_last_stats(yael_gpu_call_stats *out);
+
 /* Exact k-NN that allocates no GPU memory.  No counterpart in the reference:
  * it exists for callers that cannot let a library call cudaMalloc -- a
  * process whose device memory is all handed to its own pool allocator, or a
@@ -535,10 +568,11 @@ int yael_gpu_hkm_learn_ex(int n, int d, int nlevel, int bf, const float *v,
  * 12 bytes per base row plus 8 C + 24 bytes per query, C the smallest power
  * of two >= 2k; e.g. nb = 1M with nq = 20k at k = 10); larger requests
  * return YAEL_GPU_EARG with the size in yael_gpu_last_error() -- use
- * yael_gpu_knn_ex for them.  The first call on a device looks up the array's
- * device address (make that first call before any stream capture).  All
- * calls share the array: calls whose GPU work overlaps race and must be
- * serialised by the caller. */
+ * yael_gpu_knn_ex for them.  Each call looks up the array's device address
+ * (a lookup, no allocation) and synchronises the stream before it returns,
+ * error returns included: never call it on a stream that is being captured
+ * into a CUDA graph.  All calls share the array: calls whose GPU work
+ * overlaps race and must be serialised by the caller. */
 int yael_gpu_knn_noalloc(int nq, int nb, int d, int k, const float *b, const float *q,
                          int *assign, float *dis, void *stream);
 

@@ -429,6 +429,223 @@ static void assign_exact(int d, int n, int k, const float *v, const float *c,
   }
 }
 
+/* FP64 argmin of point x over all k centroids (assign_exact's rule) */
+static int argmin64(int d, int k, const float *x, const float *c)
+{
+  double best = INFINITY;
+  int bi = -1;
+  for (int j = 0; j < k; j++) {
+    double t = dist64(x, c + (long)j * d, d);
+    if (t < best) { best = t; bi = j; }
+  }
+  return bi;
+}
+
+long orc_assign_check(int d, int n, int k, const float *v, const float *c, const int *assign,
+                      int nt, long *first_bad)
+{
+  enum { PB = 64, CB = 2048, CAP = 32 };
+  double *cn = malloc(sizeof(double) * (size_t)k);
+  for (long j = 0; j < k; j++) {
+    double s = 0;
+    for (int i = 0; i < d; i++) s += (double)c[j * d + i] * c[j * d + i];
+    cn[j] = s;
+  }
+  const double rel = (d + 4) * 5.9604644775390625e-08;
+  long bad = 0, first = -1;
+#pragma omp parallel num_threads(nt > 0 ? nt : 1)
+  {
+    float *dot = malloc(sizeof(float) * PB * CB);
+    int *cj = malloc(sizeof(int) * PB * CAP);
+    double *clo = malloc(sizeof(double) * PB * CAP);
+    long my_bad = 0, my_first = -1;
+#pragma omp for schedule(dynamic)
+    for (long p0 = 0; p0 < n; p0 += PB) {
+      const int np = (int)(n - p0 < PB ? n - p0 : PB);
+      double xn2[PB], xn[PB], m[PB];
+      int cnt[PB];
+      for (int i = 0; i < np; i++) {
+        double s = 0;
+        for (int t = 0; t < d; t++) s += (double)v[(p0 + i) * d + t] * v[(p0 + i) * d + t];
+        xn2[i] = s;
+        xn[i] = sqrt(s);
+        m[i] = INFINITY;
+        cnt[i] = 0;
+      }
+      for (int j0 = 0; j0 < k; j0 += CB) {
+        const int nc = k - j0 < CB ? k - j0 : CB;
+        float one = 1, zero = 0;
+        sgemm_("Trans", "Not", &np, &nc, &d, &one, v + p0 * d, &d, c + (long)j0 * d, &d, &zero,
+               dot, &np);
+        for (int jj = 0; jj < nc; jj++) {
+          const long j = j0 + jj;
+          const double cnj = sqrt(cn[j]);
+          for (int i = 0; i < np; i++) {
+            if (cnt[i] < 0) continue;  /* overflowed: full FP64 scan later */
+            const double a = xn2[i] + cn[j] - 2.0 * (double)dot[i + (long)np * jj];
+            const double b = rel * (xn[i] + cnj) * (xn[i] + cnj);
+            if (!(a - b <= m[i])) continue;  /* NaN never enters */
+            if (a + b < m[i]) {
+              m[i] = a + b;
+              int w = 0; /* drop the listed ones now above the new bound */
+              for (int t = 0; t < cnt[i]; t++)
+                if (clo[i * CAP + t] <= m[i]) {
+                  clo[i * CAP + w] = clo[i * CAP + t];
+                  cj[i * CAP + w] = cj[i * CAP + t];
+                  w++;
+                }
+              cnt[i] = w;
+            }
+            if (cnt[i] == CAP) { cnt[i] = -1; continue; }
+            clo[i * CAP + cnt[i]] = a - b;
+            cj[i * CAP + cnt[i]] = (int)j;
+            cnt[i]++;
+          }
+        }
+      }
+      for (int i = 0; i < np; i++) {
+        const float *x = v + (p0 + i) * d;
+        int bi = -1;
+        if (cnt[i] <= 0) {
+          bi = argmin64(d, k, x, c);
+        } else {
+          double best = INFINITY;
+          for (int t = 0; t < cnt[i]; t++) {
+            const int j = cj[i * CAP + t];
+            const double e = dist64(x, c + (long)j * d, d);
+            if (e < best || (e == best && j < bi)) { best = e; bi = j; }
+          }
+        }
+        if (assign[p0 + i] != bi) {
+          my_bad++;
+          if (my_first < 0 || p0 + i < my_first) my_first = p0 + i;
+        }
+      }
+    }
+#pragma omp critical
+    {
+      bad += my_bad;
+      if (my_first >= 0 && (first < 0 || my_first < first)) first = my_first;
+    }
+    free(dot); free(cj); free(clo);
+  }
+  free(cn);
+  if (first_bad) *first_bad = first;
+  return bad;
+}
+
+/* k-th smallest (0-based) of a[0..n) in place (Hoare partitions) */
+static double select_kth(double *a, long n, long kth)
+{
+  long lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const double piv = a[lo + (hi - lo) / 2];
+    long i = lo, j = hi;
+    while (i <= j) {
+      while (a[i] < piv) i++;
+      while (a[j] > piv) j--;
+      if (i <= j) { double t = a[i]; a[i] = a[j]; a[j] = t; i++; j--; }
+    }
+    if (kth <= j) hi = j;
+    else if (kth >= i) lo = i;
+    else break;
+  }
+  return a[kth];
+}
+
+typedef struct { double d; int j; } dist_id;
+
+static int cmp_dist_id(const void *x, const void *y)
+{
+  const dist_id *a = x, *b = y;
+  if (a->d < b->d) return -1;
+  if (a->d > b->d) return 1;
+  return (a->j > b->j) - (a->j < b->j);
+}
+
+long orc_knn_check(int d, int nq, int nb, int k, const float *b, const float *q, const int *idx,
+                   int nt, long *first_bad)
+{
+  enum { QB = 8 };
+  double *bn = malloc(sizeof(double) * (size_t)nb);
+  int bfinite = 1;
+  for (long j = 0; j < nb; j++) {
+    double s = 0;
+    for (int i = 0; i < d; i++) s += (double)b[j * d + i] * b[j * d + i];
+    bn[j] = sqrt(s);
+    if (!isfinite(s)) bfinite = 0;
+  }
+  const double rel = (d + 4) * 5.9604644775390625e-08;
+  long bad = 0, first = -1;
+#pragma omp parallel num_threads(nt > 0 ? nt : 1)
+  {
+    float *dot = malloc(sizeof(float) * (size_t)QB * nb);
+    double *up = malloc(sizeof(double) * (size_t)nb);
+    dist_id *cand = malloc(sizeof(dist_id) * (size_t)nb);
+    int *ei = malloc(sizeof(int) * (size_t)k);
+    float *ed = malloc(sizeof(float) * (size_t)k);
+    long my_bad = 0, my_first = -1;
+#pragma omp for schedule(dynamic)
+    for (long q0 = 0; q0 < nq; q0 += QB) {
+      const int nqb = (int)(nq - q0 < QB ? nq - q0 : QB);
+      float one = 1, zero = 0;
+      sgemm_("Trans", "Not", &nqb, &nb, &d, &one, q + q0 * d, &d, b, &d, &zero, dot, &nqb);
+      for (int i = 0; i < nqb; i++) {
+        const float *x = q + (q0 + i) * d;
+        double qs = 0;
+        for (int t = 0; t < d; t++) qs += (double)x[t] * x[t];
+        const double qn = sqrt(qs);
+        int ok = 1;
+        if (!bfinite || !isfinite(qs)) {
+          /* non-finite values: the exact brute force itself */
+          orc_knn_exact(1, nb, d, k, b, x, ei, ed, NULL, 1);
+          for (int t = 0; t < k; t++) ok &= ei[t] == idx[(q0 + i) * (long)k + t];
+        } else {
+          for (long j = 0; j < nb; j++) {
+            const double a = qs + bn[j] * bn[j] - 2.0 * (double)dot[i + (long)nqb * j];
+            up[j] = a + rel * (qn + bn[j]) * (qn + bn[j]);
+          }
+          const double U = select_kth(up, nb, k - 1);
+          long nc = 0;
+          for (long j = 0; j < nb; j++) {
+            const double a = qs + bn[j] * bn[j] - 2.0 * (double)dot[i + (long)nqb * j];
+            if (a - rel * (qn + bn[j]) * (qn + bn[j]) <= U) {
+              cand[nc].d = dist64(x, b + j * d, d);
+              cand[nc].j = (int)j;
+              nc++;
+            }
+          }
+          qsort(cand, (size_t)nc, sizeof(dist_id), cmp_dist_id);
+          for (int t = 0; t < k; t++)
+            ok &= t < nc && cand[t].j == idx[(q0 + i) * (long)k + t];
+        }
+        if (!ok) {
+          my_bad++;
+          if (my_first < 0 || q0 + i < my_first) my_first = q0 + i;
+        }
+      }
+    }
+#pragma omp critical
+    {
+      bad += my_bad;
+      if (my_first >= 0 && (first < 0 || my_first < first)) first = my_first;
+    }
+    free(dot); free(up); free(cand); free(ei); free(ed);
+  }
+  free(bn);
+  if (first_bad) *first_bad = first;
+  return bad;
+}
+
+double orc_objective64(int d, int n, const float *v, const float *c, const int *assign, int nt)
+{
+  double tot = 0;
+#pragma omp parallel for schedule(static) reduction(+ : tot) num_threads(nt > 0 ? nt : 1)
+  for (long i = 0; i < n; i++)
+    if (assign[i] >= 0) tot += dist64(v + i * d, c + (long)assign[i] * d, d);
+  return tot;
+}
+
 /* ------------------------------------------------------------------ */
 /* RNG replay (yael/vector.c:134-155, 184-189, 226-253; kmeans.c:15-24) */
 

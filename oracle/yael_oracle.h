@@ -87,6 +87,35 @@ void orc_kmeans_step_exact(int d, int n, int k, const float *v, const float *c_i
                            int *assign, float *dis, int *nassign, float *c_out,
                            int fixed_shift);
 
+/* Checker of one assignment step at any size: the number of the n points
+ * whose assign[i] is not the ORC_EXACT nearest of the k centroids c (FP64
+ * distances in the dist64 form, ties to the lowest index; a point with no
+ * finite distance must have -1).  The k distances of a point are screened in
+ * FP32 through BLAS sgemm; every centroid whose FP32 value can be within the
+ * screen's rounding bound of the smallest, (d + 4) 2^-24 (||x|| + ||c||)^2
+ * each, is then recomputed in FP64, so the answer is the FP64 argmin's.
+ * first_bad (may be NULL) receives the first disagreeing point or -1.
+ * Not part of the reference: a test utility for sizes where the FP64 brute
+ * force of assign_exact would take minutes. */
+long orc_assign_check(int d, int n, int k, const float *v, const float *c, const int *assign,
+                      int nt, long *first_bad);
+
+/* Checker of k-NN results at any size: the number of the nq queries whose
+ * row of idx (k ids) is not the ORC_EXACT result (the k smallest dist64
+ * distances in (distance, id) order).  Distances are screened in FP32 through
+ * BLAS sgemm; every base row whose FP32 value can be within the screen's
+ * rounding bound ((d + 4) 2^-24 (||q|| + ||b||)^2) of the k-th smallest is
+ * recomputed in FP64.  Queries or rows with non-finite values are compared
+ * with orc_knn_exact's answer directly.  first_bad (may be NULL) receives the
+ * first disagreeing query or -1.  Test utility, not part of the reference. */
+long orc_knn_check(int d, int nq, int nb, int k, const float *b, const float *q, const int *idx,
+                   int nt, long *first_bad);
+
+/* The FP64 objective of an assignment: the sum over the n points of the
+ * dist64 distance to centroid assign[i] (points with assign -1 add nothing),
+ * summed per thread slice then across slices in FP64.  Test utility. */
+double orc_objective64(int d, int n, const float *v, const float *c, const int *assign, int nt);
+
 /* The fixed-point shift used by ORC_EXACT centroid sums for this data. */
 int orc_fixed_shift(long n, long d, const float *v);
 

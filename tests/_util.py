@@ -75,6 +75,12 @@ def oracle():
         o.orc_gaussrand_r.restype = D
         o.orc_random_init.argtypes = [I, I, ctypes.c_uint, P]
         o.oracle_blas_name.restype = ctypes.c_char_p
+        o.orc_assign_check.argtypes = [I, I, I, P, P, P, I, P]
+        o.orc_assign_check.restype = L
+        o.orc_objective64.argtypes = [I, I, P, P, P, I]
+        o.orc_knn_check.argtypes = [I, I, I, I, P, P, P, I, P]
+        o.orc_knn_check.restype = L
+        o.orc_objective64.restype = D
         _oracle = o
     return _oracle
 
@@ -119,6 +125,33 @@ def knn_port(b, q, k, nt=8, distance_type=2, w=None):
     dis = np.empty((nq, k), np.float32)
     oracle().orc_knn_port(distance_type, nq, nb, d, k, ptr(b), ptr(q), ptr(w), ptr(idx), ptr(dis), nt)
     return idx, dis
+
+
+def assign_mismatches(v, C, assign, nt=8):
+    """Points whose assignment is not the oracle's FP64 nearest centroid (ties
+    to the lowest index), and the first of them (-1 if none)."""
+    n, d = v.shape
+    first = ctypes.c_long(-1)
+    bad = oracle().orc_assign_check(d, n, C.shape[0], ptr(v), ptr(C), ptr(assign), nt,
+                                    ctypes.byref(first))
+    return int(bad), int(first.value)
+
+
+def knn_mismatches(b, q, idx, nt=8):
+    """Queries whose k ids differ from the oracle's FP64 (distance, id) order,
+    and the first of them (-1 if none)."""
+    nb, d = b.shape
+    nq, k = idx.shape
+    first = ctypes.c_long(-1)
+    bad = oracle().orc_knn_check(d, nq, nb, k, ptr(b), ptr(q), ptr(np.ascontiguousarray(idx)),
+                                 nt, ctypes.byref(first))
+    return int(bad), int(first.value)
+
+
+def objective64(v, C, assign, nt=8):
+    """FP64 sum of the points' distances to their assigned centroids."""
+    n, d = v.shape
+    return float(oracle().orc_objective64(d, n, ptr(v), ptr(C), ptr(assign), nt))
 
 
 def exact_dist64(b, q, idx):

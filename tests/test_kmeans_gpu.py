@@ -38,12 +38,13 @@ def gpu_kmeans(v, k, niter, flags, seed, redo, prec, C0=None):
     dis = np.empty(n, np.float32)
     assign = np.empty(n, np.int32)
     nassign = np.empty(k, np.int32)
-    o = yg.KmeansOpts({"fp32": 0, "bf16": 1, "bf16x3": 2}[prec], 0, None, 0, 0, 0, 0, 0, 0)
+    o = yg.KmeansOpts({"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3}[prec], 0, None, 0, 0, 0,
+                      0, 0, 0)
     q = yg.lib().yael_gpu_kmeans_ex(d, n, k, niter, ptr(v), flags, seed, redo, ptr(C), ptr(dis),
                                     ptr(assign), ptr(nassign), ctypes.byref(o))
     assert o.status == 0, yg.last_error()
     return dict(C=C, dis=dis, assign=assign, nassign=nassign, qerr=q, iters=o.iterations,
-                n_band=o.n_band)
+                n_band=o.n_band, prec_used=o.prec_used)
 
 
 def same(g, o, rtol=2e-6):
@@ -61,16 +62,30 @@ def test_kmeans_small_k(prec):
     same(gpu_kmeans(v, 20, 12, QUIET, 1234, 1, prec), oracle_kmeans(v, 20, 12, QUIET, 1234, 1))
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3", "fp16"])
 def test_kmeans_large_k_knn_path(prec):
     v, _, _ = synth.gaussian_mixture(20000, 32, 128, 0.15, seed=5)
-    same(gpu_kmeans(v, 100, 10, QUIET, 777, 1, prec), oracle_kmeans(v, 100, 10, QUIET, 777, 1))
+    g = gpu_kmeans(v, 100, 10, QUIET, 777, 1, prec)
+    same(g, oracle_kmeans(v, 100, 10, QUIET, 777, 1))
+    # the chosen form runs fp16 operands on data whose range fp16 holds
+    assert g["prec_used"] == {"fp32": 0, "bf16": 3, "bf16x3": 2, "fp16": 3}[prec]
+
+
+def test_kmeans_large_k_bf16_operands():
+    """Values up to 255 (norms far above fp16's range): the chosen form keeps
+    bf16 operands, with the same exact assignments."""
+    v = synth.sift_like(12000, 64, seed=8)
+    g = gpu_kmeans(v, 80, 6, QUIET, 99, 1, "bf16")
+    same(g, oracle_kmeans(v, 80, 6, QUIET, 99, 1))
+    assert g["prec_used"] == 1
 
 
 def duplicate_heavy(seed):
-    """40% of the points are one vector: random init picks ~40 identical
-    centroids, so the 8-entry candidate lists of those points tie and the
-    certificate rejects them (band passes settle them)."""
+    """40% of the points are one vector: random init picks many identical
+    centroids.  On the k-NN assignment (k > 256) the candidate lists of those
+    points tie and the certificate rejects them (band passes settle them); on
+    the small-k tensor-core assignment their error bands overflow the band
+    lists (every centroid is then re-checked) and the ties go to FP64."""
     v, _, _ = synth.gaussian_mixture(20000, 32, 50, 0.2, seed=seed)
     v[::5] = v[1]
     v[1::5] = v[1]
@@ -92,7 +107,7 @@ def test_kmeans_deferred_check_rejections():
             "import sys, numpy as np; sys.path.insert(0, 'tests');"
             "import test_kmeans_gpu as T;"
             f"v = np.load('{tmp}/v.npy');"
-            "r = T.gpu_kmeans(v, 100, 8, T.QUIET, 5, 1, 'bf16');"
+            "r = T.gpu_kmeans(v, 300, 8, T.QUIET, 5, 1, 'bf16');"
             f"np.savez('{tmp}/r.npz', **r); print('ran')")
         env = dict(os.environ, YAEL_GPU_KMEANS_DEFER="1")
         root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -101,15 +116,40 @@ def test_kmeans_deferred_check_rejections():
         assert p.returncode == 0 and "ran" in p.stdout, p.stdout + p.stderr
         g = dict(np.load(os.path.join(tmp, "r.npz")))
     assert g["n_band"] > 0  # rejected points went through the re-run
-    same(g, oracle_kmeans(v, 100, 8, QUIET, 5, 1))
+    same(g, oracle_kmeans(v, 300, 8, QUIET, 5, 1))
 
 
 def test_kmeans_inline_check_rejections():
     """The same data with the check in line (first iteration: adaptive mode)."""
     v = duplicate_heavy(31)
-    g = gpu_kmeans(v, 100, 8, QUIET, 5, 1, "bf16")
+    g = gpu_kmeans(v, 300, 8, QUIET, 5, 1, "bf16")
     assert g["n_band"] > 0
-    same(g, oracle_kmeans(v, 100, 8, QUIET, 5, 1))
+    same(g, oracle_kmeans(v, 300, 8, QUIET, 5, 1))
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("k", [100, 256])
+def test_kmeans_tensor_core_assignment_ties(prec, k):
+    """The small-k tensor-core assignment on duplicate-heavy data (bands wider
+    than their lists, exact FP32 ties decided in FP64): bit-identical to the
+    oracle.  k = 100 fuses the centroid sums into the pass (k * d * 8 bytes fit
+    shared memory); k = 256 keeps the sorted update."""
+    v = duplicate_heavy(31)
+    g = gpu_kmeans(v, k, 8, QUIET, 5, 1, prec)
+    assert g["prec_used"] == 3  # fp16 holds this data's range
+    same(g, oracle_kmeans(v, k, 8, QUIET, 5, 1))
+
+
+@pytest.mark.parametrize("d,k", [(4, 7), (20, 33), (96, 32), (128, 200), (256, 16)])
+def test_kmeans_tensor_core_assignment_shapes(d, k):
+    """Dimensions from 4 to 256 (one to four 64-column K blocks, partial
+    blocks zero padded) and k not a multiple of 32 (masked accumulator
+    columns), bf16 operands (values far outside fp16's range)."""
+    rng = np.random.default_rng(d * 100 + k)
+    v = (rng.standard_normal((6000, d)) * 300).astype(np.float32)
+    g = gpu_kmeans(v, k, 5, QUIET, 11, 1, "bf16")
+    assert g["prec_used"] == 1
+    same(g, oracle_kmeans(v, k, 5, QUIET, 11, 1))
 
 
 def test_kmeans_empty_cluster_splits():
@@ -177,6 +217,25 @@ def test_hkm_exact_vs_oracle():
     levels, ga = yg.hkm(v, 3, 5, 10)
     np.testing.assert_array_equal(ga, oa)
     np.testing.assert_array_equal(np.concatenate([l.ravel() for l in levels]), oc)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp32"])
+def test_hkm_chosen_form_vs_oracle(prec, monkeypatch):
+    """hkm with the tensor-core assignment and fused centroid sums (bf16
+    requested; fp16 operands for this data) and the plain FP32 form: the
+    same tree as the oracle's exact mode, bit for bit."""
+    monkeypatch.setenv("YAEL_GPU_PRECISION", prec)
+    v, _, _ = synth.gaussian_mixture(40000, 96, 300, 0.1, seed=19)
+    srand48(7)
+    oc, oa = oracle_hkm(v, 3, 8, 6)
+    srand48(7)
+    levels, ga = yg.hkm(v, 3, 8, 6)
+    np.testing.assert_array_equal(ga, oa)
+    np.testing.assert_array_equal(np.concatenate([l.ravel() for l in levels]), oc)
+    st = yg.CallStats()
+    yg.lib().yael_gpu_last_stats(ctypes.byref(st))
+    assert st.prec_used == (3 if prec == "bf16" else 0)
+    assert st.point_iterations >= st.instance_iterations > 0
 
 
 def test_hkm_golden_and_quantize(gpu_lib):

@@ -2,8 +2,9 @@
 
 The oracle is the FP64 brute force (canonical order: distance, then base id);
 the reference's own outputs (tests/golden) are checked modulo its
-heap-history tie order.  Both distance passes are covered: the plain FP32
-CUDA-core path and the BF16 tensor-core path with exact re-rank.
+heap-history tie order.  Every distance pass is covered: the plain FP32
+CUDA-core path, the BF16 and FP16 tensor-core paths with exact re-rank and
+the 3xBF16 split.
 """
 import ctypes
 import os
@@ -52,7 +53,7 @@ def test_golden_integer_ties(prec, k):
     assert st["exact_class"] == 1
 
 
-@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("prec", PRECS + ["fp16"])
 def test_golden_float(prec):
     g = np.load(os.path.join(GOLDEN, "knn_float.npz"))
     assert_exact(g["b"], g["q"], 10, prec)
@@ -60,7 +61,7 @@ def test_golden_float(prec):
     np.testing.assert_array_equal(idx, g["idx_k1"])
 
 
-@pytest.mark.parametrize("prec", PRECS + ["bf16x3"])
+@pytest.mark.parametrize("prec", PRECS + ["bf16x3", "fp16"])
 @pytest.mark.parametrize("nq,nb,d,k", [(1, 1, 1, 1), (7, 5, 3, 5), (33, 300, 129, 17),
                                         (130, 2000, 64, 100), (300, 9000, 96, 33),
                                         (257, 1000, 7, 1), (64, 3000, 200, 250),
@@ -84,7 +85,7 @@ def test_sift_like_medium(prec, k):
     assert st["exact_class"] == 1 and st["n_fallback"] == 0
 
 
-@pytest.mark.parametrize("prec", PRECS + ["bf16x3"])
+@pytest.mark.parametrize("prec", PRECS + ["bf16x3", "fp16"])
 def test_unit_vectors_oversampled(prec):
     b = synth.unit_gaussian(50_000, 128, seed=3)
     q = synth.unit_gaussian(200, 128, seed=4)
@@ -104,6 +105,21 @@ def test_k_equals_nb_and_duplicates(prec):
         np.testing.assert_array_equal(dis, rdis)
 
 
+@pytest.mark.parametrize("k", [1, 10])
+def test_fp16_rows_out_of_range_still_exact(k):
+    """Rows fp16 cannot hold (here ||b||^2 up to ~6e6 > 2^15, and query values
+    of 4e4 whose -2q overflows) get an infinite error bound: their queries
+    fail the certificate and the later passes (3xBF16 band, FP64) settle them."""
+    b = synth.sift_like(6000, 64, seed=21)
+    q = synth.sift_like(50, 64, seed=22)
+    q[::7, 3] = 4.0e4
+    idx, dis, st = gpu_knn(b, q, k, "fp16")
+    ridx, rdis, _ = knn_exact(b, q, k)
+    np.testing.assert_array_equal(idx, ridx)
+    np.testing.assert_array_equal(dis, rdis)
+    assert st["n_band"] + st["n_second"] + st["n_fallback"] > 0
+
+
 def test_nan_rows_follow_reference_padding():
     rng = np.random.default_rng(5)
     b = rng.standard_normal((400, 16)).astype(np.float32)
@@ -118,7 +134,7 @@ def test_nan_rows_follow_reference_padding():
         np.testing.assert_array_equal(idx[ok], knn_exact(b, q[ok], k)[0])
 
 
-@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("prec", PRECS + ["fp16"])
 def test_dot_product_metric(prec):
     rng = np.random.default_rng(6)
     b = rng.standard_normal((3000, 40)).astype(np.float32)
@@ -235,7 +251,7 @@ def shell_data(nb=4000, nq=64, d=64, seed=41):
     return b, q
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3", "fp16"])
 @pytest.mark.parametrize("k", [1, 5])
 def test_later_chance_chain(prec, k):
     b, q = shell_data()

@@ -9,6 +9,7 @@ import pytest
 
 from _util import (GOLDEN, check_knn_ties, exact_dist64, knn_exact, knn_port, oracle, ptr,
                    reference, srand48)
+from yael_gb300 import synth
 
 
 def load(name):
@@ -250,3 +251,50 @@ def test_callers_port_matches_reference_fixtures():
         np.testing.assert_array_equal(desc, g["desc"])
     else:
         np.testing.assert_allclose(desc, g["desc"], rtol=1e-5, atol=1e-4)
+
+
+def test_assign_check_and_objective_vs_numpy():
+    """The sampled FP64 checker used at the benchmarked sizes agrees with a
+    numpy FP64 brute force: no false alarms on the exact argmin (duplicate
+    centroids tie to the lowest index, a NaN row maps to -1), every planted
+    error found, and the FP64 objective equal to numpy's sum."""
+    from _util import assign_mismatches, objective64
+    v, _, _ = synth.gaussian_mixture(6000, 24, 40, 0.2, seed=13)
+    C = np.ascontiguousarray(v[::37][:120]).copy()
+    C[9] = C[4]
+    v[17] = np.nan
+    d64 = ((v.astype(np.float64)[:, None, :] - C.astype(np.float64)[None]) ** 2).sum(-1)
+    a = np.where(np.isnan(d64).all(1), -1, np.argmin(np.nan_to_num(d64, nan=np.inf), 1))
+    a = a.astype(np.int32)
+    assert assign_mismatches(v, C, a) == (0, -1)
+    planted = a.copy()
+    planted[[5, 2000, 5999]] = (planted[[5, 2000, 5999]] + 1) % C.shape[0]
+    assert assign_mismatches(v, C, planted) == (3, 5)
+    ok = a >= 0
+    ref = float(d64[np.nonzero(ok)[0], a[ok]].sum())
+    assert abs(objective64(v, C, a) - ref) <= 1e-12 * ref
+
+
+def test_knn_check_vs_exact():
+    """The screened k-NN checker used at the benchmarked sizes agrees with the
+    FP64 brute force (float data with exact duplicate rows, integer ties, a
+    NaN base row) and finds planted errors."""
+    from _util import knn_mismatches
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal((3000, 40)).astype(np.float32)
+    b[100:110] = b[7]
+    q = rng.standard_normal((60, 40)).astype(np.float32)
+    q[5] = b[7]
+    for k in (1, 12):
+        idx, _, _ = knn_exact(b, q, k)
+        assert knn_mismatches(b, q, idx) == (0, -1)
+        bad = idx.copy()
+        bad[[4, 33], -1] = (bad[[4, 33], -1] + 1) % 3000
+        assert knn_mismatches(b, q, bad) == (2, 4)
+    bi = rng.integers(0, 4, (500, 8)).astype(np.float32)
+    qi = rng.integers(0, 4, (30, 8)).astype(np.float32)
+    idx, _, _ = knn_exact(bi, qi, 20)
+    assert knn_mismatches(bi, qi, idx) == (0, -1)
+    bi[3, 2] = np.nan
+    idx, _, _ = knn_exact(bi, qi, 20)
+    assert knn_mismatches(bi, qi, idx) == (0, -1)

@@ -30,20 +30,60 @@ def noalloc_call(L, torch, b, q, k):
     return idx.cpu().numpy(), dis.cpu().numpy()
 
 
+def tie_heavy(seed):
+    """40 exact copies of one float row in the base and queries equal to it:
+    the k-th and the list's last entries tie, the FP32 certificate rejects
+    those queries and the exhaustive FP64 path (batched in the static
+    scratch) settles them."""
+    rng = np.random.default_rng(seed)
+    b = rng.standard_normal((5000, 24)).astype(np.float32)
+    b[1000:1040] = b[7]
+    q = rng.standard_normal((64, 24)).astype(np.float32)
+    q[::2] = b[7]
+    return b, q, 4
+
+
 def test_noalloc_matches_regular_entry_point_twice():
     torch = pytest.importorskip("torch")
+    from _util import knn_exact
     L = yg.lib()
     cases = [
         (synth.gaussian_mixture(20000, 48, 64, 0.3, seed=21)[0],
          synth.gaussian_mixture(300, 48, 64, 0.3, seed=22)[0], 10),
         (synth.sift_like(30000, 128, seed=23), synth.sift_like(200, 128, seed=24), 16),
+        tie_heavy(25),
     ]
     for b, q, k in cases:
         ridx, rdis = reference_call(b, q, k)
+        oidx, odis, _ = knn_exact(b, q, k)  # the oracle's FP64 (distance, id) order
+        np.testing.assert_array_equal(ridx, oidx)
         for _ in range(2):  # two calls in a row share (and must reset) the scratch
             idx, dis = noalloc_call(L, torch, b, q, k)
             np.testing.assert_array_equal(idx, ridx)
+            np.testing.assert_array_equal(idx, oidx)
             np.testing.assert_allclose(dis, rdis, rtol=2e-6, atol=1e-6)
+            np.testing.assert_allclose(dis, odis, rtol=2e-6, atol=1e-6)
+
+
+def test_noalloc_allocates_no_device_memory():
+    """After a first call (which may load the library's kernels), further
+    calls leave the device's free memory exactly as it was."""
+    torch = pytest.importorskip("torch")
+    L = yg.lib()
+    b, q, k = tie_heavy(26)
+    db, dq = torch.from_numpy(b).cuda(), torch.from_numpy(q).cuda()
+    idx = torch.empty((q.shape[0], k), dtype=torch.int32, device="cuda")
+    dis = torch.empty((q.shape[0], k), dtype=torch.float32, device="cuda")
+    args = (q.shape[0], b.shape[0], b.shape[1], k, db.data_ptr(), dq.data_ptr(), idx.data_ptr(),
+            dis.data_ptr(), None)
+    assert L.yael_gpu_knn_noalloc(*args) == 0, yg.last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert L.yael_gpu_knn_noalloc(*args) == 0, yg.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():

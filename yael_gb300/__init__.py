@@ -37,7 +37,7 @@ KMEANS_INIT_USER = 0x100000
 KMEANS_L1 = 0x200000
 KMEANS_CHI2 = 0x400000
 
-PREC_ENV, PREC_FP32, PREC_BF16, PREC_BF16X3 = -1, 0, 1, 2
+PREC_ENV, PREC_FP32, PREC_BF16, PREC_BF16X3, PREC_FP16 = -1, 0, 1, 2, 3
 
 
 class KnnPair(ctypes.Structure):
@@ -48,7 +48,16 @@ class KmeansOpts(ctypes.Structure):
     _fields_ = [("precision", c_int), ("device_ptrs", c_int), ("stream", P), ("status", c_int),
                 ("iterations", c_long), ("n_fallback", c_long), ("n_second", c_long),
                 ("ms_assign", c_float),
-                ("ms_update", c_float), ("n_band", c_long)]
+                ("ms_update", c_float), ("n_band", c_long), ("prec_used", c_int),
+                ("n_probe", c_int), ("probe_rows", P), ("probe_iters", c_int),
+                ("probe_assign", P), ("probe_centroids", P), ("probe_qerr", P),
+                ("wait_limit_us", c_int)]
+
+
+class CallStats(ctypes.Structure):
+    _fields_ = [("instance_iterations", c_long), ("point_iterations", c_long),
+                ("level_iterations", c_long), ("ms_assign", c_float), ("ms_update", c_float),
+                ("prec_used", c_int)]
 
 
 class Hkm(ctypes.Structure):
@@ -61,7 +70,8 @@ class KnnOpts(ctypes.Structure):
                 ("stream", P), ("n_fallback", c_int), ("n_candidates", c_int),
                 ("exact_class", c_int), ("timing", c_int), ("ms_scan", c_float),
                 ("ms_sample", c_float), ("ms_rerank", c_float), ("scan_launches", c_int),
-                ("n_second", c_int), ("n_band", c_int), ("ms_second", c_float)]
+                ("n_second", c_int), ("n_band", c_int), ("ms_second", c_float),
+                ("wait_limit_us", c_int)]
 
 
 # name -> (restype, argtypes); every symbol of include/yael_gpu.h
@@ -193,6 +203,7 @@ SIGNATURES = {
     "yael_gpu_knn_noalloc": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, P]),
     "yael_gpu_version": (c_int, []),
     "yael_gpu_launch_count": (c_long, []),
+    "yael_gpu_last_stats": (c_int, [P]),
 }
 
 
@@ -248,7 +259,8 @@ def knn(queries, base, nnn=1, distance_type=2, nt=1, precision=None, stats=False
     assert d == d2, "base and queries must have the same dimension"
     idx = np.empty((nq, nnn), dtype=np.int32)
     dis = np.empty((nq, nnn), dtype=np.float32)
-    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3}[precision]
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3,
+            "fp16": PREC_FP16}[precision]
     opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     rc = lib().yael_gpu_knn_ex(nq, nb, d, nnn, _ptr(base), _ptr(queries), _ptr(idx), _ptr(dis),
                                ctypes.byref(opts))
@@ -279,7 +291,8 @@ def knn_batch(pairs, nnn=1, distance_type=2, precision=None, stats=False):
         dis = np.empty((q.shape[0], nnn), dtype=np.float32)
         arrays.append((q, b, idx, dis))
         descs[i] = KnnPair(q.shape[0], b.shape[0], _ptr(q), _ptr(b), _ptr(idx), _ptr(dis))
-    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3}[precision]
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3,
+            "fp16": PREC_FP16}[precision]
     opts = KnnOpts(prec, distance_type, 0, None, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     rc = lib().yael_gpu_knn_batch(len(pairs), ctypes.cast(descs, P), d or 1, nnn,
                                   ctypes.byref(opts))
@@ -328,7 +341,8 @@ def kmeans(v, k, distance_type=2, nt=1, niter=30, seed=0, redo=1, verbose=True,
         flags |= KMEANS_INIT_BERKELEY
     if normalize:
         flags |= KMEANS_NORMALIZE_CENTS
-    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3}[precision]
+    prec = {None: PREC_ENV, "fp32": PREC_FP32, "bf16": PREC_BF16, "bf16x3": PREC_BF16X3,
+            "fp16": PREC_FP16}[precision]
     opts = KmeansOpts(prec, 0, None, 0, 0, 0, 0, 0, 0)
     qerr = lib().yael_gpu_kmeans_ex(d, n, k, niter, _ptr(v), flags, seed, redo, _ptr(centroids),
                                     _ptr(dis), _ptr(assign), _ptr(nassign), ctypes.byref(opts))

@@ -148,8 +148,7 @@ extern "C" int yael_gpu_knn_batch(int npairs, const yael_gpu_knn_pair *pairs, in
   t.k = k;
   t.prec = default_precision();
   if (opts) {
-    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16 ||
-        opts->precision == YAEL_GPU_PREC_BF16X3)
+    if (explicit_precision(opts->precision))
       t.prec = opts->precision;
     if (opts->metric == 16) t.metric = METRIC_DOT;
     else if (opts->metric && opts->metric != 2 && opts->metric != 12) {

@@ -3,6 +3,7 @@
 // workspace, small device helpers.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -96,11 +97,41 @@ int ctx_get(Ctx **out);
 // precision of the distance pass
 // PREC_BF16X3: the tensor cores on a 3xBF16 split of the operands
 // (x = hi + lo), about 2^-16 relative error instead of 2^-8
-enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1, PREC_BF16X3 = 2 };
-int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3), default fp32
+// PREC_FP16: the tensor cores on fp16 operands (2^-11 relative rounding at the
+// bf16 rate), for data fp16 can hold (|x| < 16384, ||x||^2 < 2^15 for base
+// rows); rows it cannot hold get an infinite error bound and are settled by
+// the later passes
+enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1, PREC_BF16X3 = 2, PREC_FP16 = 3 };
+int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3 | fp16), default fp32
+// p is one of the YAEL_GPU_PREC_* values a caller may pass explicitly
+inline bool explicit_precision(int p) { return p >= PREC_FP32 && p <= PREC_FP16; }
+// Bound of the waits inside the tensor-core kernels launched by the calling
+// thread, in ns (0: the kernels' own 2 s); set for the duration of a call by
+// WaitLimitScope from a caller's wait_limit_us option.
+unsigned long long wait_limit_ns();
+struct WaitLimitScope {
+  unsigned long long saved;
+  explicit WaitLimitScope(int limit_us);
+  ~WaitLimitScope();
+};
+// YAEL_GPU_TEST_WITHHOLD_LOADS=1 (read at every launch): the tensor-core
+// kernels' producers issue no load, so the consumers' bounded waits expire
+// and the call returns YAEL_GPU_ETIMEOUT with the context still usable.  A
+// test hook for that path; nothing is faulted and nothing hangs.
+bool test_withhold_loads();
 // YAEL_GPU_TRACE set (and not "0"): every k-NN pass is timed with CUDA events
 // and reported on stderr, one line per pass
 bool trace_enabled();
+
+// An NVTX range over a host scope: the phases of the pipeline (packing,
+// distance pass, re-rank, later passes, update, split) appear by name on a
+// profiler's timeline; without a tool attached a push / pop costs nothing.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // A device array owned by the host scope that holds it (freed on
 // destruction).  get() grows it to at least `want` elements, dropping the

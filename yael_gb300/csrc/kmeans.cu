@@ -35,6 +35,9 @@ enum KmSlot : int {
   KS_SHIFT, KS_ACTIVE, KS_PINST, KS_WORK, KS_SLICES, KS_PART, KS_ROWS, KS_AMAX,
   KS_BEST_C, KS_BEST_DIS, KS_BEST_ASSIGN, KS_NODE, KS_VSORT, KS_TMP, KS_CPREV,
   KS_AKEYS, KS_AKEYS2, KS_AVALS, KS_AVALS2, KS_AOFFS, KS_ATMP, KS_ASORT,
+  // the small-k tensor-core assignment
+  KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
+  KS_TCERR,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -128,6 +131,9 @@ int fixed_shift(long n, float maxabs) {
 
 // ---- the batched Lloyd engine --------------------------------------------
 
+// statistics of the calling thread's last kmeans / hkm call (yael_gpu_last_stats)
+thread_local yael_gpu_call_stats g_last_stats = {};
+
 struct Instance {
   long p0 = 0;
   int n = 0;
@@ -161,6 +167,7 @@ struct Engine {
   std::vector<double> hpart;
   long n_fallback = 0, n_second = 0, n_band = 0;
   float ms_assign = 0, ms_update = 0;
+  long point_iters = 0, engine_iters = 0;  // sum of active points per iteration; iterations
 
   // CUDA graphs of one Lloyd iteration's device work: the update always, the
   // assignment on the grouped small-k path (the k-NN path reads its
@@ -172,6 +179,17 @@ struct Engine {
   // replays.  YAEL_GPU_GRAPHS=0 runs every iteration eagerly.
   cudaGraphExec_t g_assign = nullptr, g_update = nullptr;
   bool eager_done = false;
+  // The chosen form's assignment for k <= 256 (km_tc.cu): the 16-bit tensor
+  // cores with an exact band re-check, and, when k * d fits shared memory, the
+  // centroid sums fused into it (no second pass over the points).
+  bool tc = false, tc_fuse = false;
+  KmTcUnit *tc_units = nullptr;
+  int tc_nunits = 0;
+  KmTcPoints tcP;
+  void *tc_cpk = nullptr, *tc_cside = nullptr;
+  SetStats *tc_cstats = nullptr;
+  int *tc_err = nullptr;
+  int *ph_err = nullptr;  // pinned copy of tc_err the update graph writes
   bool assign_settled = false;  // the grouped assignment's variant is tuned
   long g_assign_n = 0, g_update_n = 0;  // kernels per replay
   bool graphs_failed = false;
@@ -183,6 +201,7 @@ struct Engine {
     if (g_update) cudaGraphExecDestroy(g_update);
     if (ph_counts) cudaFreeHost(ph_counts);
     if (ph_part) cudaFreeHost(ph_part);
+    if (ph_err) cudaFreeHost(ph_err);
   }
 
   // L1 / chi2 k-means (one instance): per-coordinate distances searched
@@ -196,7 +215,9 @@ struct Engine {
     }();
     return on && !graphs_failed && !alt_mode();
   }
-  bool assign_graph_wanted() const { return graphs_wanted() && !(in.size() == 1 && k > kSmallK); }
+  bool assign_graph_wanted() const {
+    return graphs_wanted() && (tc || !(in.size() == 1 && k > kSmallK));
+  }
 
   // captures body() on st into *exec; false (and eager mode) on any failure
   template <typename F>
@@ -267,12 +288,65 @@ struct Engine {
     YG_CUDA(cudaStreamSynchronize(st));
     std::vector<int> hs(ni);
     for (int i = 0; i < ni; i++) hs[i] = fixed_shift(in[i].n, ha[i]);
+    // every centroid is a mean of points (or a split of one, 1e-7 apart), so
+    // |c| <= max |v| and ||c|| <= sqrt(d) max |v|: fp16 holds both operands of
+    // the assignment when that norm stays below 128 (||c||^2 < 2^14)
+    f16_fits = ni == 1 && ha[0] >= 0.f && ha[0] * sqrtf((float)d) < 128.f;
     YG_CUDA(cudaMemcpyAsync(shift, hs.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, st));
     hcounts.resize(ncl);
     hpart.resize(nsl);
     YG_CUDA(cudaMallocHost(&ph_counts, sizeof(int) * (size_t)ncl));
     YG_CUDA(cudaMallocHost(&ph_part, sizeof(double) * (size_t)std::max(1, nsl)));
+    YG_CUDA(cudaMallocHost(&ph_err, sizeof(int)));
+    *ph_err = 0;
+    float hmax = 0.f;
+    for (int i = 0; i < ni; i++) hmax = ha[i] > hmax ? ha[i] : (ha[i] >= 0.f ? hmax : NAN);
+    YG_CHECK(setup_tc(hmax));
     YG_CUDA(cudaStreamSynchronize(st));
+    return OK;
+  }
+
+  // The small-k tensor-core assignment: the chosen form (a 16-bit pass) for
+  // k <= 256 and aligned rows with d % 4 == 0.  Its unit table (tiles of up
+  // to 128 points of one instance) and the points' 16-bit packing are built
+  // once; the centroids are packed at every assignment.
+  int setup_tc(float hmax) {
+    tc = (prec == PREC_BF16 || prec == PREC_FP16) && !alt_mode() && km_tc_supported(d, k, v, C);
+    if (!tc) return OK;
+    tc_fuse = km_tc_fuses(d, k);
+    Workspace &ws = ctx->ws;
+    const int ni = (int)in.size();
+    const long ncl = (long)ni * k;
+    std::vector<KmTcUnit> hu;
+    for (int i = 0; i < ni; i++)
+      for (long o = 0; o < in[i].n; o += 128)
+        hu.push_back({i, (int)std::min<long>(128, in[i].n - o), in[i].p0 + o});
+    tc_nunits = (int)hu.size();
+    YG_CHECK(ws_get(ws, KS_TCU, hu.size(), &tc_units));
+    YG_CUDA(cudaMemcpyAsync(tc_units, hu.data(), sizeof(KmTcUnit) * hu.size(),
+                            cudaMemcpyHostToDevice, st));
+    // fp16 operands when every value and every centroid norm fits (see f16_fits)
+    tcP.f16 = hmax >= 0.f && hmax * sqrtf((float)d) < 128.f;
+    tcP.Kp = ((d + 63) / 64) * 64;
+    tcP.n = ntot;
+    uint16_t *pk, *side, *cpk, *cside;
+    YG_CHECK(ws_get(ws, KS_TCPK, (size_t)ntot * tcP.Kp, &pk));
+    YG_CHECK(ws_get(ws, KS_TCSIDE, (size_t)ntot * 16, &side));
+    YG_CHECK(ws_get(ws, KS_TCXN, (size_t)ntot, &tcP.xn64));
+    YG_CHECK(ws_get(ws, KS_TCXRES, (size_t)ntot, &tcP.xres));
+    YG_CHECK(ws_get(ws, KS_TCCPK, (size_t)ncl * tcP.Kp, &cpk));
+    YG_CHECK(ws_get(ws, KS_TCCSIDE, (size_t)ncl * 16, &cside));
+    YG_CHECK(ws_get(ws, KS_TCSTATS, 1, &tc_cstats));
+    YG_CHECK(ws_get(ws, KS_TCERR, 1, &tc_err));
+    YG_CUDA(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
+    tcP.pk = pk;
+    tcP.side = side;
+    tc_cpk = cpk;
+    tc_cside = cside;
+    YG_CHECK(prep_rows(v, d, (int)ntot, d, -2.f, tcP.xn64, nullptr, nullptr, tcP.xres,
+                       (__nv_bfloat16 *)pk, tcP.Kp, (__nv_bfloat16 *)side, 2, nullptr, st, 8,
+                       tcP.f16));
+    assign_settled = true;  // no variant tuner on this path
     return OK;
   }
 
@@ -307,11 +381,22 @@ struct Engine {
     return OK;
   }
 
-  // When the BF16 certificate rejects more than a quarter of the points, the
-  // band and split passes that settle them cost more than running the whole
-  // assignment on the 3xBF16 split operands; later iterations see similar
+  // When the 16-bit certificate rejects more than 60% of the points, the band
+  // passes that settle them cost more than running the whole assignment on
+  // the 3xBF16 split operands (measured on the large configuration: band
+  // passes ~32 ns per rejected point on bf16 crowding, the split pass ~19 ns
+  // more per point than the 16-bit one); later iterations see similar
   // centroid geometry, so the switch is kept for the rest of the run.
   bool split_assign = false;
+  // The 16-bit tensor-core pass of the chosen form runs on fp16 operands when
+  // the data range allows (the same tensor rate as bf16, 8x finer rounding,
+  // so an 8x narrower error band and far fewer points sent to later passes)
+  bool f16_fits = false;
+  int prec_used = -1;  // the distance pass of the last assignment
+  // per-iteration record (yael_gpu_kmeans_opts' probe fields), single instance
+  const yael_gpu_kmeans_opts *probe = nullptr;
+  long probe_t = 0;
+  std::vector<int> probe_all;
   // The k-NN assignment defers its certificate check to the end of the
   // iteration (the update is queued right behind it); rejected points are
   // settled then and the update is run again.  Only after an iteration that
@@ -325,17 +410,30 @@ struct Engine {
     n_fallback += job.n_fallback;
     n_second += job.n_second;
     n_band += job.n_band;
-    if (job.prec == PREC_BF16 && 4L * (job.n_band + job.n_fallback) > (long)job.nq)
+    if ((job.prec == PREC_BF16 || job.prec == PREC_FP16) &&
+        10L * (job.n_band + job.n_fallback) > 6L * (long)job.nq)
       split_assign = true;
   }
 
   int assign_step() {
+    if (tc) {
+      const long ncl = (long)in.size() * k;
+      if (tc_fuse) {
+        YG_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * ncl * d, st));
+        YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
+      }
+      prec_used = tcP.f16 ? PREC_FP16 : PREC_BF16;
+      return km_tc_assign(tc_units, tc_nunits, tcP, v, d, C, (int)in.size(), k, tc_cpk,
+                          tc_cside, nullptr, tc_cstats, active, assign, dis,
+                          tc_fuse ? acc : nullptr, tc_fuse ? counts : nullptr, shift, tc_err, st);
+    }
     if (alt_mode()) {
       // yael/kmeans.c:242-244: knn_full with distance type 1 (L1) or 3 (chi2)
       KnnJob job;
       job.nq = in[0].n; job.nb = k; job.d = d; job.k = 1;
       job.metric = METRIC_ALT0 + ((flags & YAEL_KMEANS_L1) ? 1 : 3);
       job.prec = PREC_FP32;
+      prec_used = PREC_FP32;
       job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
       job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
       return knn_device(job, ctx, st);
@@ -343,7 +441,9 @@ struct Engine {
     if (in.size() == 1 && k > kSmallK) {
       KnnJob job;
       job.nq = in[0].n; job.nb = k; job.d = d; job.k = 1; job.metric = METRIC_L2;
-      job.prec = (prec == PREC_BF16 && split_assign) ? PREC_BF16X3 : prec;
+      job.prec = prec == PREC_BF16 ? (split_assign ? PREC_BF16X3 : f16_fits ? PREC_FP16 : prec)
+                                   : prec;
+      prec_used = job.prec;
       job.q = v + in[0].p0 * d; job.ldq = d; job.b = C; job.ldb = d;
       job.out_idx = assign + in[0].p0; job.out_dis = dis + in[0].p0;
       // YAEL_GPU_KMEANS_DEFER=0 / 1: never / always defer (default: adaptive)
@@ -368,6 +468,7 @@ struct Engine {
       }
       return OK;
     }
+    prec_used = PREC_FP32;
     return km_assign_small(work, nwork, v, d, C, k, active, assign, dis, st);
   }
 
@@ -376,12 +477,27 @@ struct Engine {
     const int ni = (int)in.size();
     const long ncl = (long)ni * k;
     for (auto &x : in)
-      if (!x.done) x.iters++;
+      if (!x.done) {
+        x.iters++;
+        point_iters += x.n;
+      }
+    engine_iters++;
     cudaEvent_t e0, e1, e2;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventCreate(&e2);
     auto update_body = [&]() -> int {
+      if (tc_fuse) {
+        // the sums and counts came with the assignment
+        YG_CHECK(km_finalize(acc, counts, ncl, d, k, shift, active, C, st));
+        if (flags & YAEL_KMEANS_NORMALIZE_CENTS) YG_CHECK(km_normalize(C, ncl, d, k, active, st));
+        YG_CHECK(km_slice_sums(slices, nsl, dis, part, st));
+        YG_CUDA(cudaMemcpyAsync(ph_counts, counts, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
+        YG_CUDA(cudaMemcpyAsync(ph_part, part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
+        YG_CUDA(cudaMemcpyAsync(ph_err, tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        return OK;
+      }
+      if (tc) YG_CUDA(cudaMemcpyAsync(ph_err, tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
       YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
       YG_CHECK(km_histogram(assign, pinst, ntot, k, active, counts, st));
       if (alt_mode()) {
@@ -418,6 +534,12 @@ struct Engine {
       YG_CUDA(cudaMemcpyAsync(ph_part, part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
       return OK;
     };
+    const bool probing = probe && probe->n_probe > 0 && ni == 1 && probe_t < probe->probe_iters;
+    if (probing && probe->probe_centroids) {
+      YG_CUDA(cudaMemcpyAsync(probe->probe_centroids + (size_t)probe_t * k * d, C,
+                              sizeof(float) * (size_t)k * d, cudaMemcpyDeviceToHost, st));
+      YG_CUDA(cudaStreamSynchronize(st));
+    }
     const bool use_graphs = graphs_wanted() && eager_done;
     // the assignment is captured once its kernel variant is tuned (the
     // tuner's trials run eagerly)
@@ -428,6 +550,7 @@ struct Engine {
         !capture([&] { return assign_step(); }, &g_assign, &g_assign_n))
       graphs_failed = true;
     cudaEventRecord(e0, st);
+    std::unique_ptr<NvtxRange> nv(new NvtxRange("kmeans.assign"));
     if (graph_assign && !graphs_failed) {
       YG_CUDA(cudaGraphLaunch(g_assign, st));
       count_launches(g_assign_n);
@@ -435,6 +558,7 @@ struct Engine {
       YG_CHECK(assign_step());
     }
     cudaEventRecord(e1, st);
+    nv.reset(new NvtxRange("kmeans.update"));
     if (use_graphs && !graphs_failed) {
       YG_CUDA(cudaGraphLaunch(g_update, st));
       count_launches(g_update_n);
@@ -458,6 +582,10 @@ struct Engine {
         YG_CUDA(cudaStreamSynchronize(st));
       }
     }
+    if (tc && *ph_err) {
+      set_error(E_TIMEOUT, "k-means tensor-core assignment gave up waiting (bounded wait expired)");
+      return E_TIMEOUT;
+    }
     std::copy(ph_counts, ph_counts + ncl, hcounts.begin());
     std::copy(ph_part, ph_part + nsl, hpart.begin());
     float a = 0, b = 0;
@@ -472,7 +600,21 @@ struct Engine {
     // objective per instance: slice sums in point order
     std::vector<double> q(ni, 0.0);
     for (int s = 0; s < nsl; s++) q[hsl[s].inst] += hpart[s];
+    if (probing) {
+      probe_all.resize(ntot);
+      YG_CUDA(cudaMemcpyAsync(probe_all.data(), assign, sizeof(int) * ntot,
+                              cudaMemcpyDeviceToHost, st));
+      YG_CUDA(cudaStreamSynchronize(st));
+      int *dst = probe->probe_assign + (size_t)probe_t * probe->n_probe;
+      for (int i = 0; i < probe->n_probe; i++) {
+        const long r = probe->probe_rows[i];
+        dst[i] = r >= 0 && r < ntot ? probe_all[r] : -1;
+      }
+      if (probe->probe_qerr) probe->probe_qerr[probe_t] = q[0];
+      probe_t++;
+    }
 
+    nv.reset(new NvtxRange("kmeans.split_and_stop"));
     std::vector<float> hc;
     bool any_split = false;
     for (int i = 0; i < ni; i++) {
@@ -592,7 +734,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
                int redo, float *C_out, float *dis_out, int *assign_out, int *nassign_out,
                int prec, bool dev, cudaStream_t st_in, float *ret_out, long *iters_out,
                long *fallback_out, long *second_out, float *ms_assign, float *ms_update,
-               long *band_out = nullptr) {
+               long *band_out = nullptr, yael_gpu_kmeans_opts *xo = nullptr) {
   Ctx *ctx;
   YG_CHECK(ctx_get(&ctx));
   cudaStream_t st = st_in ? st_in : ctx->stream;
@@ -624,6 +766,13 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
   E.in.resize(1);
   E.in[0].n = n;
   E.in[0].seed = (unsigned)seed_in;
+  if (xo && xo->n_probe > 0) {
+    if (!xo->probe_rows || !xo->probe_assign || xo->probe_iters < 0) {
+      set_error(E_ARG, "kmeans: probe_rows and probe_assign are needed with n_probe > 0");
+      return E_ARG;
+    }
+    E.probe = xo;
+  }
   YG_CHECK(E.setup());
   double best = HUGE_VAL;
   long iter_tot = 0;
@@ -702,6 +851,9 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
   if (fallback_out) *fallback_out = E.n_fallback;
   if (second_out) *second_out = E.n_second;
   if (band_out) *band_out = E.n_band;
+  if (xo) xo->prec_used = E.prec_used;
+  g_last_stats = yael_gpu_call_stats{iter_tot, E.point_iters, E.engine_iters, E.ms_assign,
+                                     E.ms_update, E.prec_used};
   if (ms_assign) *ms_assign = E.ms_assign;
   if (ms_update) *ms_update = E.ms_update;
   *ret_out = core_ret < 0 ? -1.f : (float)(best / n);
@@ -736,11 +888,13 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   std::vector<int> hnode(n, 0);
   std::vector<long> hperm(n);
   long k = 1, iters = 0;
+  yael_gpu_call_stats stats = {};
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   cudaEventRecord(t0, st);
   for (int l = 0; l < nlevel; l++) {
+    NvtxRange nv_level("hkm.level");
     // points grouped by parent, stable in point index (ivec_sort_index, hkm.c:56-62)
     std::vector<long> start(k + 1, 0);
     for (int i = 0; i < n; i++) start[hnode[i] + 1]++;
@@ -789,6 +943,11 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
     YG_CHECK(E.set_active());
     while (!E.all_done()) YG_CHECK(E.iterate());
     for (auto &x : E.in) iters += x.iters;
+    stats.point_iterations += E.point_iters;
+    stats.level_iterations += E.engine_iters;
+    stats.ms_assign += E.ms_assign;
+    stats.ms_update += E.ms_update;
+    stats.prec_used = E.prec_used;
     // centroids of this level, then node = node * bf + child
     YG_CUDA(cudaMemcpyAsync(levels_out[l], E.C, sizeof(float) * (size_t)k * bf * d,
                             cudaMemcpyDeviceToHost, st));
@@ -805,6 +964,8 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   cudaEventDestroy(t1);
   if (assign_out) memcpy(assign_out, hnode.data(), sizeof(int) * n);
   if (iters_out) *iters_out = iters;
+  stats.instance_iterations = iters;
+  g_last_stats = stats;
   return OK;
 }
 
@@ -894,6 +1055,12 @@ static hkm_t *hkm_alloc(int d, int nlevel, int bf) {
 
 extern "C" {
 
+int yael_gpu_last_stats(yael_gpu_call_stats *out) {
+  if (!out) return YAEL_GPU_EARG;
+  *out = g_last_stats;
+  return YAEL_GPU_OK;
+}
+
 float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int flags, long seed,
                          int redo, float *centroids, float *dis, int *assign, int *nassign,
                          yael_gpu_kmeans_opts *opts) {
@@ -901,8 +1068,7 @@ float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int fla
   bool dev = false;
   cudaStream_t st = nullptr;
   if (opts) {
-    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16 ||
-        opts->precision == YAEL_GPU_PREC_BF16X3)
+    if (explicit_precision(opts->precision))
       prec = opts->precision;
     dev = opts->device_ptrs != 0;
     st = (cudaStream_t)opts->stream;
@@ -910,8 +1076,10 @@ float yael_gpu_kmeans_ex(int d, int n, int k, int niter, const float *v, int fla
   float ret = -1;
   long iters = 0, fb = 0, sec = 0, bd = 0;
   float ma = 0, mu = 0;
+  WaitLimitScope wls(opts ? opts->wait_limit_us : 0);
   const int rc = kmeans_run(d, n, k, niter, v, flags, seed, redo, centroids, dis, assign,
-                            nassign, prec, dev, st, &ret, &iters, &fb, &sec, &ma, &mu, &bd);
+                            nassign, prec, dev, st, &ret, &iters, &fb, &sec, &ma, &mu, &bd,
+                            opts);
   if (opts) {
     opts->status = rc;
     opts->iterations = iters;

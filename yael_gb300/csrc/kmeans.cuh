@@ -5,8 +5,38 @@
 // array; global cluster id = i*k + local id.
 #pragma once
 #include "common.cuh"
+#include "prep.cuh"
 
 namespace yg {
+
+// llrint(x * 2^S) (round to nearest, ties to even) of a float x, with integer
+// operations only (the FP64 pipe of this GPU is narrow).  The caller's shift
+// keeps |x| 2^S < 2^62; non-finite x gives 0.
+__device__ __forceinline__ long long fixed_of(float x, int S) {
+  const unsigned u = __float_as_uint(x);
+  const int ex = (int)((u >> 23) & 0xffu);
+  if (ex == 0xff) return 0;
+  unsigned long long m = u & 0x7fffffu;
+  int e = -149;  // x = +-m 2^e
+  if (ex != 0) {
+    m |= 0x800000u;
+    e = ex - 150;
+  }
+  const int sh = e + S;
+  unsigned long long r;
+  if (sh >= 0) {
+    r = m << sh;
+  } else if (-sh > 24) {
+    r = 0;  // m < 2^24 <= half of the unit in the last place kept
+  } else {
+    const int rs = -sh;
+    const unsigned long long q = m >> rs;
+    const unsigned long long rem = m & ((1ull << rs) - 1);
+    const unsigned long long half = 1ull << (rs - 1);
+    r = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+  }
+  return (u >> 31) ? -(long long)r : (long long)r;
+}
 
 struct KmWork {      // one block of the grouped assignment kernel
   int inst;          // instance
@@ -24,6 +54,46 @@ constexpr int kSmallK = 64;  // largest k of the direct grouped assignment
 int km_assign_small(const KmWork *work, int nwork, const float *v, int d, const float *C,
                     int k, const unsigned char *active, int *assign, float *dis,
                     cudaStream_t st);
+
+// ---- the 16-bit tensor-core assignment for k <= 256 (km_tc.cu) -------------
+// A unit is one tile of up to 128 consecutive points of one instance.
+struct KmTcUnit {
+  int inst;
+  int np;   // points in the tile
+  long p0;  // first point (global index)
+};
+constexpr int kTcMaxK = 256;
+
+// The points of a run (or of an hkm level) packed once: 16-bit -2x in
+// [n][Kp] with a [n][16] side block of ones (the norm fold), ||x||^2 in FP64
+// and the packing's error norm ||x - 16(x)|| per point.
+struct KmTcPoints {
+  void *pk = nullptr, *side = nullptr;
+  double *xn64 = nullptr;
+  float *xres = nullptr;
+  long n = 0;
+  int Kp = 0, f16 = 0;
+};
+
+// shapes the kernel takes: d % 4 == 0, d <= 256, k <= 256, 16-byte aligned rows
+bool km_tc_supported(int d, int k, const float *v, const float *C);
+
+// Nearest centroid of every point of the listed units, exact: the tensor
+// cores give every centroid's distance within a rigorous bound eps of the
+// point (the certificate bound of the k-NN pass); every centroid within 2 eps
+// of the smallest is re-evaluated by FP32 direct differences, and by FP64 when
+// the best two are closer than their rounding bound (ties to the lowest
+// index).  Points whose distances are all NaN get -1 / 1e30.  The centroids
+// are packed here (cpk, cside: [ninst*k][Kp] and [ninst*k][16], cstats reset
+// and filled).  With acc != null the exact fixed-point sums of the points and
+// the counts are added to acc[g][d] / counts[g] (g = inst*k + j; both zeroed
+// by the caller), accumulated in shared memory first (needs k*d*8 bytes of it:
+// km_tc_fuses).  Units of instances with active[inst] == 0 are skipped.
+bool km_tc_fuses(int d, int k);
+int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const float *v, int d,
+                 const float *C, int ninst, int k, void *cpk, void *cside, float *cres,
+                 SetStats *cstats, const unsigned char *active, int *assign, float *dis,
+                 long long *acc, int *counts, const int *shift, int *err, cudaStream_t st);
 
 // After the caller's synchronisation: reports a timed trial of the grouped
 // assignment's variant tuner (autotune.cuh); true once the variant choice of
@@ -62,6 +132,10 @@ int km_update(const long *perm, const long *total, long nmax, const int *assign,
               const int *pinst, const int *counts, const float *v, int d, long ncl, int k,
               const int *shift, const unsigned char *active, long long *acc, float *C,
               cudaStream_t st);
+
+// the readout of km_update alone, for sums accumulated elsewhere (km_tc_assign)
+int km_finalize(const long long *acc, const int *counts, long ncl, int d, int k,
+                const int *shift, const unsigned char *active, float *C, cudaStream_t st);
 
 // rows of C scaled to unit L2 norm (yael/vector.c:2016-2025 arithmetic)
 int km_normalize(float *C, long ncl, int d, int k, const unsigned char *active,

@@ -420,35 +420,6 @@ __global__ void scatter_kernel(const int *assign, const int *pinst, long n, int 
   perm[base + __popc(peers & ((1u << lane) - 1))] = p;
 }
 
-// llrint(x * 2^S) (round to nearest, ties to even) of a float x, with integer
-// operations only (the FP64 pipe of this GPU is narrow).  The caller's shift
-// keeps |x| 2^S < 2^62; non-finite x gives 0.
-__device__ __forceinline__ long long fixed_of(float x, int S) {
-  const unsigned u = __float_as_uint(x);
-  const int ex = (int)((u >> 23) & 0xffu);
-  if (ex == 0xff) return 0;
-  unsigned long long m = u & 0x7fffffu;
-  int e = -149;  // x = +-m 2^e
-  if (ex != 0) {
-    m |= 0x800000u;
-    e = ex - 150;
-  }
-  const int sh = e + S;
-  unsigned long long r;
-  if (sh >= 0) {
-    r = m << sh;
-  } else if (-sh > 24) {
-    r = 0;  // m < 2^24 <= half of the unit in the last place kept
-  } else {
-    const int rs = -sh;
-    const unsigned long long q = m >> rs;
-    const unsigned long long rem = m & ((1ull << rs) - 1);
-    const unsigned long long half = 1ull << (rs - 1);
-    r = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
-  }
-  return (u >> 31) ? -(long long)r : (long long)r;
-}
-
 // warps walk contiguous runs of the cluster-sorted point list, accumulating
 // exact integer sums in registers and flushing at cluster boundaries
 template <int NDR>
@@ -891,6 +862,14 @@ int km_update(const long *perm, const long *total, long nmax, const int *assign,
     }
     YG_LAUNCH_CHECK();
   }
+  finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(acc, counts, ncl, d, k, shift,
+                                                                     active, C);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int km_finalize(const long long *acc, const int *counts, long ncl, int d, int k,
+                const int *shift, const unsigned char *active, float *C, cudaStream_t st) {
   finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(acc, counts, ncl, d, k, shift,
                                                                      active, C);
   YG_LAUNCH_CHECK();

@@ -96,12 +96,15 @@ __global__ void gather_kth_kernel(const float *in_kth, const float *out_kth, con
 
 // per-thread list length of a TOPC pass: k when the distances are exact, else
 // an oversampled list whose extra entries give the certificate its margin.
-// k = 1 (k-means assignment) does not depend on exactness: lists of two over
-// large bases (longer lists make the epilogue's insertions the bottleneck, and
-// the band pass settles what they would have), of eight over small ones (the
-// pass is cheap, a band pass would cost more than the longer list).
+// k = 1 (k-means assignment) does not depend on exactness: lists of eight.
+// Measured on the large k-means configuration (10M points, 65,536 crowded
+// centroids, fp16 operands): lists of two reject 35-61% of the points (their
+// second entry sits inside the error band), lists of eight 0.2-16%, and the
+// band pass then costs a few ms instead of ~100; the longer lists slow the
+// distance pass by 1.35x, a net 1.5x per iteration (369 -> 243 ms).
 int list_length(int k, int exact, int nb) {
-  if (k == 1) return nb <= 8192 ? 8 : 2;
+  (void)nb;
+  if (k == 1) return 8;
   if (exact) return k;
   return k <= 4 ? 8 : 2 * k;
 }
@@ -256,11 +259,13 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
 
   TcOperands tcq;
   float *qlo = nullptr;
+  std::unique_ptr<NvtxRange> nv(new NvtxRange("knn.pack_queries"));
   if (bf16) {
     tcq = split ? bops->split : bops->plain;
     if (split) YG_CHECK(ws_get(ws, WS_QLO, nq, &qlo));
     YG_CHECK(tc_prepare_queries(job.q, job.ldq, nq, d, job.metric, ws, WS_QPACK, WS_QNORMP,
-                                &tcq, qn64, qflag, qres, split ? 1 : 0, qlo, st));
+                                &tcq, qn64, qflag, qres, split ? 1 : 0, qlo, st,
+                                job.prec == PREC_FP16));
   } else {
     YG_CHECK(prep_rows(job.q, job.ldq, nq, d, 1.f, qn64, nullptr, qflag, qres, nullptr, 0,
                        nullptr, 0, nullptr, st));
@@ -272,6 +277,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     YG_CHECK(compute_eps(nq, d, job.prec, job.metric, qn64, qres, qflag, &dsmall->bs, eps,
                          qexact, st));
 
+  nv.reset(new NvtxRange(job.band_kth ? "knn.band_pass" : "knn.distance_pass"));
   int *fail_list;
   YG_CHECK(ws_get(ws, WS_FAIL, nq, &fail_list));
   YG_CUDA(cudaMemsetAsync(&dsmall->fail_cnt, 0, sizeof(int), st));
@@ -435,6 +441,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
                          qexact, st));
   }
   ra.sel = sel;
+  nv.reset(new NvtxRange("knn.rerank"));
   PassTimer tr(timed || scan_ticket >= 0, st, &job.ms_rerank);
   YG_CHECK(rerank(ra, st));
   tr.stop(st);
@@ -486,12 +493,14 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   if (nf == 0) return OK;
   // A regular pass's rejections go to a band pass at the same precision: its
   // thresholds come from the k-th exact distance the re-rank found, so it
-  // collects every row that can still be in the top k.  A BF16 band pass's
+  // collects every row that can still be in the top k.  A BF16 / FP16 band pass's
   // rejections (bands too wide for its candidate buffers) go to a band pass on
   // the 3xBF16 split operands, whose error bound and so whose band is ~2^-8 of
   // the BF16 one; everything else to the exhaustive FP64 path.
   const bool to_band = !band && job.w == nullptr;
-  const bool to_split = band && job.prec == PREC_BF16 && job.w == nullptr;
+  const bool to_split =
+      band && (job.prec == PREC_BF16 || job.prec == PREC_FP16) && job.w == nullptr;
+  nv.reset(new NvtxRange("knn.later_passes"));
   PassTimer t2(timed, st, &job.ms_second);
   if ((to_band || to_split) && job.level < 4) {
     const int base = WS_SC0 + job.level * WS_SC_PER_LEVEL;
@@ -672,6 +681,7 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
   }
 
   // base preparation (once for all query batches)
+  NvtxRange nv_base("knn.pack_base");
   float *bn32, *bres = nullptr;
   YG_CHECK(ws_get(ws, WS_BN32, nb, &bn32));
   BaseOps bops;
@@ -686,9 +696,10 @@ int knn_device(KnnJob &job, Ctx *ctx, cudaStream_t st) {
                                    d, job.metric, bops.plain, bn32, bops.res, &dsmall->bs, st));
     up.packed[0] = true;
     bops.has_plain = true;
-  } else if (job.prec == PREC_BF16) {
+  } else if (job.prec == PREC_BF16 || job.prec == PREC_FP16) {
     YG_CHECK(tc_prepare_base(job.b, job.ldb, nb, d, job.metric, ws, WS_BPACK, WS_BNORMP,
-                             WS_BRES, &bops.plain, bn32, &dsmall->bs, 0, st));
+                             WS_BRES, &bops.plain, bn32, &dsmall->bs, 0, st,
+                             job.prec == PREC_FP16));
     bops.has_plain = true;
   } else if (job.prec == PREC_BF16X3) {
     // the plain statistics (max norm) are needed too: dot-product bounds read them
@@ -908,8 +919,7 @@ int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q
   int prec = default_precision();
   int metric = METRIC_L2;
   if (opts) {
-    if (opts->precision == YAEL_GPU_PREC_FP32 || opts->precision == YAEL_GPU_PREC_BF16 ||
-        opts->precision == YAEL_GPU_PREC_BF16X3)
+    if (explicit_precision(opts->precision))
       prec = opts->precision;
     if (opts->metric) metric = metric_of(opts->metric);
   }
@@ -917,6 +927,7 @@ int yael_gpu_knn_ex(int nq, int nb, int d, int k, const float *b, const float *q
     set_error(E_UNSUPPORTED, "distance_type %d not supported", opts ? opts->metric : 0);
     return E_UNSUPPORTED;
   }
+  WaitLimitScope wls(opts ? opts->wait_limit_us : 0);
   return knn_host(metric, nq, nb, d, k, b, q, nullptr, assign, dis, prec, opts);
 }
 

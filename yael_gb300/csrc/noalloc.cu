@@ -15,8 +15,6 @@
 // each call clears what must start at zero.  Calls whose GPU work overlaps
 // (other host threads, other streams) race on it and must be serialised by
 // the caller.
-#include <mutex>
-
 #include "knn.cuh"
 #include "../../include/yael_gpu.h"
 
@@ -34,31 +32,19 @@ struct NoAllocSmall {
   unsigned long long n_cand;
 };
 
-// device address of the array, resolved once per device (the name is only a
-// host-side stand-in for it)
-constexpr int kMaxDevices = 64;
-std::mutex g_sym_mu;
-unsigned char *g_sym_addr[kMaxDevices] = {nullptr};
-
+// device address of the array on the current device.  The array's name is
+// only a host-side stand-in for it; the lookup allocates nothing and is done
+// on every call, so a context that was reset and reloaded is never handed a
+// stale address.
 int scratch_address(unsigned char **out) {
-  int dev = 0;
-  YG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_error(E_ARG, "yael_gpu_knn_noalloc: device %d beyond %d", dev, kMaxDevices);
-    return E_ARG;
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    set_error(E_CUDA, "yael_gpu_knn_noalloc: cudaGetSymbolAddress failed: %s",
+              cudaGetErrorString(e));
+    return E_CUDA;
   }
-  std::lock_guard<std::mutex> lk(g_sym_mu);
-  if (!g_sym_addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error(E_CUDA, "yael_gpu_knn_noalloc: cudaGetSymbolAddress failed: %s",
-                cudaGetErrorString(e));
-      return E_CUDA;
-    }
-    g_sym_addr[dev] = static_cast<unsigned char *>(p);
-  }
-  *out = g_sym_addr[dev];
+  *out = static_cast<unsigned char *>(p);
   return OK;
 }
 
@@ -113,7 +99,6 @@ int knn_noalloc(int nq, int nb, int d, int k, const float *b, const float *q, in
   unsigned char *qexact = take((size_t)nq);
   float *eps = reinterpret_cast<float *>(take((size_t)nq * 4));
   int *fail_list = reinterpret_cast<int *>(take((size_t)nq * 4));
-  void *rows = take(exhaustive_bytes_per_query(nb));
   ScanSel sel;
   sel.mode = SCAN_TOPC;
   sel.C = C;
@@ -121,34 +106,45 @@ int knn_noalloc(int nq, int nb, int d, int k, const float *b, const float *q, in
   sel.tiles_per_chunk = tpc;
   sel.topv = reinterpret_cast<float *>(take((size_t)nchunk * nq * C * 4));
   sel.topi = reinterpret_cast<int *>(take((size_t)nchunk * nq * C * 4));
+  // the exhaustive fallback gets the rest of the array (at least one query's
+  // worth, by the size check above), so rejected queries are batched
+  void *rows = base + off;
+  const size_t rows_bytes = kNoAllocScratchBytes - off;
 
-  // everything that must start at zero: the statistics and counters
-  NoAllocSmall h{};
-  h.bs.all_exact = 1;
-  YG_CUDA(cudaMemcpyAsync(small, &h, sizeof(h), cudaMemcpyHostToDevice, st));
-  YG_CHECK(prep_rows(b, d, nb, d, 1.f, nullptr, bn32, nullptr, nullptr, nullptr, 0, nullptr, 0,
-                     &small->bs, st));
-  YG_CHECK(prep_rows(q, d, nq, d, 1.f, qn64, nullptr, qflag, nullptr, nullptr, 0, nullptr, 0,
-                     nullptr, st));
-  YG_CHECK(compute_eps(nq, d, PREC_FP32, METRIC_L2, qn64, nullptr, qflag, &small->bs, eps,
-                       qexact, st));
-  YG_CHECK(simt_scan(q, d, nq, b, d, nb, d, bn32, 1, METRIC_L2, sel, st));
-  RerankArgs ra;
-  ra.nq = nq; ra.nb = nb; ra.d = d; ra.k = k; ra.metric = METRIC_L2;
-  ra.q = q; ra.ldq = d; ra.b = b; ra.ldb = d;
-  ra.qn64 = qn64; ra.eps = eps; ra.qexact = qexact; ra.bstats = &small->bs;
-  ra.sel = sel;
-  ra.out_idx = assign; ra.out_dis = dis;
-  ra.fail_list = fail_list; ra.fail_cnt = &small->fail_cnt; ra.n_cand = &small->n_cand;
-  YG_CHECK(rerank(ra, st));
-  int nfail = 0;
-  YG_CUDA(cudaMemcpyAsync(&nfail, &small->fail_cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
-  YG_CUDA(cudaStreamSynchronize(st));
-  if (nfail > 0)
-    YG_CHECK(exhaustive(nfail, fail_list, nb, d, k, METRIC_L2, q, d, b, d, nullptr, assign, dis,
-                        rows, exhaustive_bytes_per_query(nb), st));
-  YG_CUDA(cudaStreamSynchronize(st));
-  return OK;
+  // once work is queued, every return waits for it: the next call reuses the
+  // array and must not race with kernels of this one
+  auto queued = [&]() -> int {
+    // everything that must start at zero: the statistics and counters
+    NoAllocSmall h{};
+    h.bs.all_exact = 1;
+    YG_CUDA(cudaMemcpyAsync(small, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+    YG_CHECK(prep_rows(b, d, nb, d, 1.f, nullptr, bn32, nullptr, nullptr, nullptr, 0, nullptr, 0,
+                       &small->bs, st));
+    YG_CHECK(prep_rows(q, d, nq, d, 1.f, qn64, nullptr, qflag, nullptr, nullptr, 0, nullptr, 0,
+                       nullptr, st));
+    YG_CHECK(compute_eps(nq, d, PREC_FP32, METRIC_L2, qn64, nullptr, qflag, &small->bs, eps,
+                         qexact, st));
+    YG_CHECK(simt_scan(q, d, nq, b, d, nb, d, bn32, 1, METRIC_L2, sel, st));
+    RerankArgs ra;
+    ra.nq = nq; ra.nb = nb; ra.d = d; ra.k = k; ra.metric = METRIC_L2;
+    ra.q = q; ra.ldq = d; ra.b = b; ra.ldb = d;
+    ra.qn64 = qn64; ra.eps = eps; ra.qexact = qexact; ra.bstats = &small->bs;
+    ra.sel = sel;
+    ra.out_idx = assign; ra.out_dis = dis;
+    ra.fail_list = fail_list; ra.fail_cnt = &small->fail_cnt; ra.n_cand = &small->n_cand;
+    YG_CHECK(rerank(ra, st));
+    int nfail = 0;
+    YG_CUDA(cudaMemcpyAsync(&nfail, &small->fail_cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    if (nfail > 0)
+      YG_CHECK(exhaustive(nfail, fail_list, nb, d, k, METRIC_L2, q, d, b, d, nullptr, assign, dis,
+                          rows, rows_bytes, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    return OK;
+  };
+  const int rc = queued();
+  if (rc != OK) (void)cudaStreamSynchronize(st);
+  return rc;
 }
 
 }  // namespace

@@ -6,10 +6,47 @@ namespace yg {
 namespace {
 constexpr int PW = 8;  // warps per block
 
+// 16-bit operand encoding of the tensor-core passes: bf16 (F16 = false) or
+// IEEE fp16 (F16 = true), both round to nearest even
+template <bool F16>
+__device__ __forceinline__ uint16_t to16(float v) {
+  if (F16) return __half_as_ushort(__float2half_rn(v));
+  return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+template <bool F16>
+__device__ __forceinline__ float from16(uint16_t h) {
+  if (F16) return __half2float(__ushort_as_half(h));
+  return __bfloat162float(__ushort_as_bfloat16(h));
+}
+
+// the rounding error of the packed value of v: bf16 shares float's exponent
+// range, so bf16(scale * v) = scale * bf16(v) for the power-of-two scales
+// used (1, -2); fp16 does not (overflow above 65504, subnormals below 2^-14),
+// so its error is taken from the packed value itself (an overflow gives an
+// infinite error, which rejects the row's every result)
+template <bool F16>
+__device__ __forceinline__ float pack_err(float v, float scale, uint16_t packed) {
+  if (F16) return v - from16<true>(packed) / scale;
+  return v - __bfloat162float(__float2bfloat16_rn(v));
+}
+
+// the float norm as three 16-bit parts whose exact sum is n32 (11 + 11 + 11
+// or 8 + 8 + 8 significant bits); *ok = false when fp16 cannot hold it
+template <bool F16>
+__device__ __forceinline__ void norm_parts(float n32, uint16_t *p, bool *ok) {
+  p[0] = to16<F16>(n32);
+  const float r1 = n32 - from16<F16>(p[0]);
+  p[1] = to16<F16>(r1);
+  const float r2 = r1 - from16<F16>(p[1]);
+  p[2] = to16<F16>(r2);
+  *ok = !F16 || (n32 < 32768.f && r2 - from16<F16>(p[2]) == 0.f);
+}
+
+template <bool F16>
 __global__ void __launch_bounds__(PW * 32)
     prep_rows_kernel(const float *__restrict__ x, long ld, int n, int d, float scale,
                      double *norm64, float *norm32, unsigned char *flags, float *resid,
-                     __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
+                     uint16_t *packed, int Kp, uint16_t *normpart,
                      int normpart_mode, SetStats *stats) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long nwarps = (long)gridDim.x * PW;
@@ -31,37 +68,38 @@ __global__ void __launch_bounds__(PW * 32)
         float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (c < d) q4 = __ldg(reinterpret_cast<const float4 *>(xr + c));
         const float e[4] = {q4.x, q4.y, q4.z, q4.w};
-        __nv_bfloat16 hb[4];
+        uint16_t hb[4];
 #pragma unroll
         for (int t = 0; t < 4; t++) {
           const float v = e[t];
+          hb[t] = to16<F16>(scale * v);
           if (c + t < d) {
             s = fmaf(v, v, s);
             exact &= (v == rintf(v)) && (fabsf(v) <= 256.f);
             bad |= !isfinite(v);
-            const float dv = v - __bfloat162float(__float2bfloat16_rn(v));  // exact
+            const float dv = pack_err<F16>(v, scale, hb[t]);  // exact
             r = fmaf(dv, dv, r);
           }
-          hb[t] = __float2bfloat16_rn(scale * v);
         }
         if (packed && c < Kp) {
           uint2 w;
-          w.x = (uint32_t)__bfloat16_as_ushort(hb[0]) | ((uint32_t)__bfloat16_as_ushort(hb[1]) << 16);
-          w.y = (uint32_t)__bfloat16_as_ushort(hb[2]) | ((uint32_t)__bfloat16_as_ushort(hb[3]) << 16);
+          w.x = (uint32_t)hb[0] | ((uint32_t)hb[1] << 16);
+          w.y = (uint32_t)hb[2] | ((uint32_t)hb[3] << 16);
           *reinterpret_cast<uint2 *>(packed + row * Kp + c) = w;
         }
       }
     } else {
       for (int c = lane; c < cols; c += 32) {
         const float v = c < d ? __ldg(xr + c) : 0.f;
+        const uint16_t h = to16<F16>(scale * v);
         if (c < d) {
           s = fmaf(v, v, s);
           exact &= (v == rintf(v)) && (fabsf(v) <= 256.f);
           bad |= !isfinite(v);
-          const float dv = v - __bfloat162float(__float2bfloat16_rn(v));
+          const float dv = pack_err<F16>(v, scale, h);
           r = fmaf(dv, dv, r);
         }
-        if (packed && c < Kp) packed[row * Kp + c] = __float2bfloat16_rn(scale * v);
+        if (packed && c < Kp) packed[row * Kp + c] = h;
       }
     }
 #pragma unroll
@@ -72,23 +110,22 @@ __global__ void __launch_bounds__(PW * 32)
       bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     exact &= (s <= kExactNorm2Max) && !bad;
+    bool nok = true;
     if (normpart && lane < 16) {
-      __nv_bfloat16 val = __float2bfloat16_rn(0.f);
+      uint16_t val = to16<F16>(0.f);
       if (normpart_mode == 1) {
-        // three bf16 parts whose exact sum is the float norm
-        const float n32 = (float)s;
-        const __nv_bfloat16 hi = __float2bfloat16_rn(n32);
-        const float r1 = n32 - __bfloat162float(hi);
-        const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
-        const float r2 = r1 - __bfloat162float(mid);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
-        val = lane == 0 ? hi : lane == 1 ? mid : lane == 2 ? lo : val;
+        uint16_t p[3];
+        norm_parts<F16>((float)s, p, &nok);
+        val = lane < 3 ? p[lane] : val;
       } else if (normpart_mode == 2) {
-        val = __float2bfloat16_rn(lane < 3 ? 1.f : 0.f);
+        val = to16<F16>(lane < 3 ? 1.f : 0.f);
       }
       normpart[row * 16 + lane] = val;
     }
-    const float rr = sqrtf(r) * (1.f + 1e-5f);
+    const float rr = nok ? sqrtf(r) * (1.f + 1e-5f) : INFINITY;
+    // exact class also needs every packed value and norm part to be exact,
+    // which fp16 cannot promise for large values and norms
+    if (F16) exact &= nok && r == 0.f;
     if (lane == 0) {
       if (norm64) norm64[row] = (double)s;
       if (norm32) norm32[row] = (float)s;
@@ -133,11 +170,11 @@ __global__ void __launch_bounds__(PW * 32)
 // 32 / LPR rows per warp step, each lane four consecutive coordinates per
 // float4 (several independent loads in flight), reductions over LPR lanes.
 // Same outputs as prep_rows_kernel.
-template <int LPR>
+template <int LPR, bool F16>
 __global__ void __launch_bounds__(PW * 32)
     prep_rows_vec_kernel(const float *__restrict__ x, long ld, int n, int d, float scale,
                          double *norm64, float *norm32, unsigned char *flags, float *resid,
-                         __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
+                         uint16_t *packed, int Kp, uint16_t *normpart,
                          int normpart_mode, SetStats *stats) {
   constexpr int RPW = 32 / LPR;  // rows per warp step
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -169,23 +206,23 @@ __global__ void __launch_bounds__(PW * 32)
       if (c >= cols) break;
       const float4 q4 = q4s[it];
       const float e[4] = {q4.x, q4.y, q4.z, q4.w};
-      __nv_bfloat16 hb[4];
+      uint16_t hb[4];
 #pragma unroll
       for (int t = 0; t < 4; t++) {
         const float v = e[t];
+        hb[t] = to16<F16>(scale * v);
         if (c + t < d) {
           s = fmaf(v, v, s);
           exact &= (v == rintf(v)) && (fabsf(v) <= 256.f);
           bad |= !isfinite(v);
-          const float dv = v - __bfloat162float(__float2bfloat16_rn(v));  // exact
+          const float dv = pack_err<F16>(v, scale, hb[t]);  // exact
           r = fmaf(dv, dv, r);
         }
-        hb[t] = __float2bfloat16_rn(scale * v);
       }
       if (rv && packed && c < Kp) {
         uint2 w;
-        w.x = (uint32_t)__bfloat16_as_ushort(hb[0]) | ((uint32_t)__bfloat16_as_ushort(hb[1]) << 16);
-        w.y = (uint32_t)__bfloat16_as_ushort(hb[2]) | ((uint32_t)__bfloat16_as_ushort(hb[3]) << 16);
+        w.x = (uint32_t)hb[0] | ((uint32_t)hb[1] << 16);
+        w.y = (uint32_t)hb[2] | ((uint32_t)hb[3] << 16);
         *reinterpret_cast<uint2 *>(packed + row * Kp + c) = w;
       }
     }
@@ -197,33 +234,25 @@ __global__ void __launch_bounds__(PW * 32)
       bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     exact &= (s <= kExactNorm2Max) && !bad;
-    const float rr = sqrtf(r) * (1.f + 1e-5f);
+    bool nok = true;
+    uint16_t part[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) part[i] = to16<F16>(0.f);
+    if (normpart_mode == 1) {
+      norm_parts<F16>(s, part, &nok);
+    } else if (normpart_mode == 2) {
+      part[0] = part[1] = part[2] = to16<F16>(1.f);
+    }
+    const float rr = nok ? sqrtf(r) * (1.f + 1e-5f) : INFINITY;
+    if (F16) exact &= nok && r == 0.f;
     if (rv && sl == 0) {
       if (normpart) {
-        __nv_bfloat16 part[16];
-#pragma unroll
-        for (int i = 0; i < 16; i++) part[i] = __float2bfloat16_rn(0.f);
-        if (normpart_mode == 1) {
-          // three bf16 parts whose exact sum is the float norm
-          const float n32 = s;
-          const __nv_bfloat16 hi = __float2bfloat16_rn(n32);
-          const float r1 = n32 - __bfloat162float(hi);
-          const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
-          const float r2 = r1 - __bfloat162float(mid);
-          part[0] = hi;
-          part[1] = mid;
-          part[2] = __float2bfloat16_rn(r2);
-        } else if (normpart_mode == 2) {
-          part[0] = part[1] = part[2] = __float2bfloat16_rn(1.f);
-        }
         uint4 w0, w1;
         uint32_t *u0 = reinterpret_cast<uint32_t *>(&w0), *u1 = reinterpret_cast<uint32_t *>(&w1);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          u0[i] = (uint32_t)__bfloat16_as_ushort(part[2 * i]) |
-                  ((uint32_t)__bfloat16_as_ushort(part[2 * i + 1]) << 16);
-          u1[i] = (uint32_t)__bfloat16_as_ushort(part[8 + 2 * i]) |
-                  ((uint32_t)__bfloat16_as_ushort(part[8 + 2 * i + 1]) << 16);
+          u0[i] = (uint32_t)part[2 * i] | ((uint32_t)part[2 * i + 1] << 16);
+          u1[i] = (uint32_t)part[8 + 2 * i] | ((uint32_t)part[8 + 2 * i + 1] << 16);
         }
         uint4 *dst = reinterpret_cast<uint4 *>(normpart + row * 16);
         dst[0] = w0;
@@ -383,16 +412,21 @@ __global__ void __launch_bounds__(PW * 32)
 }
 }  // namespace
 
+__global__ void stats_reset_kernel(SetStats *stats) { *stats = SetStats{0u, 0u, 1, 0, 0u}; }
+
+// a kernel, not a copy from a host variable: it may be captured in a CUDA graph
 int stats_reset(SetStats *stats, cudaStream_t st) {
-  SetStats h{0u, 0u, 1, 0, 0u};
-  YG_CUDA(cudaMemcpyAsync(stats, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  stats_reset_kernel<<<1, 1, 0, st>>>(stats);
+  YG_LAUNCH_CHECK();
   return OK;
 }
 
 int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64,
               float *norm32, unsigned char *flags, float *resid,
-              __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
-              int normpart_mode, SetStats *stats, cudaStream_t st, int warps) {
+              __nv_bfloat16 *packed_bf, int Kp, __nv_bfloat16 *normpart_bf,
+              int normpart_mode, SetStats *stats, cudaStream_t st, int warps, int f16) {
+  uint16_t *packed = reinterpret_cast<uint16_t *>(packed_bf);
+  uint16_t *normpart = reinterpret_cast<uint16_t *>(normpart_bf);
   if (n <= 0) return OK;
   static int sms = 0;
   if (!sms) {
@@ -411,15 +445,15 @@ int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64
     const int wpb = warps >= 1 && warps <= PW ? warps : PW;
     long blocks = ceil_div(n, wpb * 4);
     if (blocks > cap * PW / wpb) blocks = cap * PW / wpb;
-    prep_rows_vec_kernel<8><<<(unsigned)blocks, wpb * 32, 0, st>>>(
-        x, ld, n, d, scale, norm64, norm32, flags, resid, packed, Kp, normpart, normpart_mode,
-        stats);
+    auto kern = f16 ? prep_rows_vec_kernel<8, true> : prep_rows_vec_kernel<8, false>;
+    kern<<<(unsigned)blocks, wpb * 32, 0, st>>>(x, ld, n, d, scale, norm64, norm32, flags, resid,
+                                              packed, Kp, normpart, normpart_mode, stats);
   } else {
     long blocks = ceil_div(n, PW);
     if (blocks > cap) blocks = cap;
-    prep_rows_kernel<<<(unsigned)blocks, PW * 32, 0, st>>>(x, ld, n, d, scale, norm64, norm32,
-                                                           flags, resid, packed, Kp, normpart,
-                                                           normpart_mode, stats);
+    auto kern = f16 ? prep_rows_kernel<true> : prep_rows_kernel<false>;
+    kern<<<(unsigned)blocks, PW * 32, 0, st>>>(x, ld, n, d, scale, norm64, norm32, flags, resid,
+                                               packed, Kp, normpart, normpart_mode, stats);
   }
   YG_LAUNCH_CHECK();
   return OK;

@@ -2,6 +2,7 @@
 // device-side statistics the selection certificate needs.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "common.cuh"
 
@@ -10,7 +11,7 @@ namespace yg {
 // statistics of one vector set, kept in device memory
 struct SetStats {
   unsigned int max_norm_bits;   // max ||x|| (float bits; non-negative floats order as ints)
-  unsigned int max_resid_bits;  // max ||x - bf16(x)||
+  unsigned int max_resid_bits;  // max ||x - bf16(x)|| (fp16(x) for an fp16 packing)
   int all_exact;                // 1 iff every row is "exact class" (see row_exact below)
   int n_nan;                    // rows with a NaN/Inf coordinate
   unsigned int max_lo_bits;     // split packing: max ||lo||, lo = bf16(x - bf16(x))
@@ -34,10 +35,14 @@ constexpr double kExactNorm2Max = 4194304.0;  // 2^22
 // and folds max norm / max residual / all-exact / NaN counts into *stats.
 // warps: warps per block of the row-vector form (1..8): small blocks fit on an
 // SM beside a running distance pass, so packing can overlap one
+// f16 = 1: the packed row and the norm parts are IEEE fp16 instead of bf16
+// (same layout; resid is then the error of the fp16 packing, infinite for a
+// row that fp16 cannot hold: |scale x| > 65504 or ||x||^2 >= 2^15)
 int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64,
               float *norm32, unsigned char *flags, float *resid,
               __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
-              int normpart_mode, SetStats *stats, cudaStream_t st, int warps = 8);
+              int normpart_mode, SetStats *stats, cudaStream_t st, int warps = 8,
+              int f16 = 0);
 
 // Split ("3xBF16") packing: x = hi + lo + r with hi = bf16(x), lo = bf16(x - hi),
 // written as three K segments of Kp1 = 64*ceil(d/64) columns each:

@@ -130,6 +130,7 @@ int default_precision() {
   if (!s || !*s) return PREC_FP32;
   if (!strcmp(s, "bf16") || !strcmp(s, "BF16") || !strcmp(s, "1")) return PREC_BF16;
   if (!strcmp(s, "bf16x3") || !strcmp(s, "BF16X3") || !strcmp(s, "2")) return PREC_BF16X3;
+  if (!strcmp(s, "fp16") || !strcmp(s, "FP16") || !strcmp(s, "3")) return PREC_FP16;
   return PREC_FP32;
 }
 
@@ -144,6 +145,18 @@ int ensure_smem(const void *func, size_t bytes) {
   YG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   cur = bytes;
   return OK;
+}
+
+static thread_local unsigned long long t_wait_ns = 0;
+unsigned long long wait_limit_ns() { return t_wait_ns; }
+WaitLimitScope::WaitLimitScope(int limit_us) : saved(t_wait_ns) {
+  if (limit_us > 0) t_wait_ns = (unsigned long long)limit_us * 1000ull;
+}
+WaitLimitScope::~WaitLimitScope() { t_wait_ns = saved; }
+
+bool test_withhold_loads() {
+  const char *s = getenv("YAEL_GPU_TEST_WITHHOLD_LOADS");
+  return s && s[0] == '1';
 }
 
 bool trace_enabled() {

@@ -79,6 +79,12 @@ struct ScanSel {
   int nunits = 0;
   const GroupPair *gpairs = nullptr;
   int max_ctas = 0;         // persistent passes: grid limit (0 = one CTA per SM)
+  int f16 = 0;              // tensor-core passes: fp16 operands (else bf16)
+  // tensor-core passes: bound of every wait (0: kWaitLimitNs), and a test
+  // switch under which the producer issues no load, so that the consumers'
+  // bounded waits expire (wait_limit_ns / test_withhold_loads in common.cuh)
+  unsigned long long wait_ns = 0;
+  int withhold = 0;
   __host__ __device__ int nregion() const { return nchunk * halves; }
 };
 

@@ -1,4 +1,4 @@
-// The tcgen05 BF16 distance + selection kernel and its host launcher, as
+// The tcgen05 16-bit (bf16 or fp16) distance + selection kernel and its host launcher, as
 // templates instantiated by tc_scan.cu / tc_scan_r2.cu (query tile resident in
 // shared memory) and tc_scan_qs.cu / tc_scan_qs2.cu (query tile streamed with
 // every K block, any Kp).
@@ -73,7 +73,7 @@ __host__ __device__ inline Layout make_layout(int nkb, int S, int mode, int C, b
   L.list_off = off;
   if (mode != SCAN_THRESH) off += (size_t)(C > 16 ? N_EPI : 128) * C * 8;
   off = (off + 15) & ~(size_t)15;
-  L.bar_off = off; off += (size_t)(2 * S + 6) * 8 + 16;
+  L.bar_off = off; off += (size_t)(2 * S + 8) * 8 + 16;
   L.total = off + 1024;  // alignment slack for the 1024-byte aligned base
   return L;
 }
@@ -157,6 +157,8 @@ __global__ void __launch_bounds__(NT_TC, 1)
   uint64_t *qempty = bars + 2 * S + 5;  // resident query tile released (grouped)
   uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * S + 6);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_holder + 1);
+  uint64_t *mdone = bars + 2 * S + 7;  // the MMAs issued have finished (exit)
+  const uint64_t wl = sel.wait_ns ? (uint64_t)sel.wait_ns : kWaitLimitNs;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntb = (int)ceil_div(nb, TC_TILE_N);
@@ -211,6 +213,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
     }
     mbar_init(qfull, 1);
     mbar_init(qempty, 1);
+    mbar_init(mdone, 1);
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -236,18 +239,20 @@ __global__ void __launch_bounds__(NT_TC, 1)
   if (warp == 0) {
     // ---------------- TMA producer (every CTA loads its own query tile and
     // its part of each base block)
-    if (lane == 0) {
+    if (lane == 0 && !(sel.withhold && !PAIR)) {
       // ring position: stage sn, phase parity phn (advanced at every use)
       int sn = 0;
       uint32_t phn = 0;
       bool ok = true;
       int ui = 0;  // units done by this CTA
+      uint32_t issued = 0, last_par = 0;  // per stage: loaded at least once, last parity
+      int qloads = 0;
       for (int w = w0; w < nunits && ok; w += wstep, ui++) {
       const UnitInfo un = unit_info(w);
       const long q0 = un.q0;
       if (!QS) {
         // the resident tile of the previous unit is free once its MMAs are done
-        if (ui > 0 && !mbar_wait(qempty, (uint32_t)((ui - 1) & 1), abort_flag)) {
+        if (ui > 0 && !mbar_wait(qempty, (uint32_t)((ui - 1) & 1), abort_flag, wl)) {
           ok = false;
           break;
         }
@@ -263,6 +268,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
             tma_load_2d(&mapQ, qfull, Qs + kb * QBLK_BYTES, kb * 64, (int)q0);
           if (L2) tma_load_2d(&mapQn, qfull, Qn, 0, (int)q0);
         }
+        qloads++;
       }
       for (int t = un.t_begin; t < un.t_end && ok; t++) {
         const int brow = t * TC_TILE_N + (int)crank * (TC_TILE_N / 2) * (PAIR ? 1 : 0);
@@ -270,7 +276,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           const int s = sn;
           const uint32_t ph = phn;
           if (++sn == S) { sn = 0; phn ^= 1; }
-          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) { ok = false; break; }
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, wl)) { ok = false; break; }
           uint8_t *sp = Stg + (size_t)s * SB;
           const bool lastk = L2 && ks == nkb - 1;
           const uint32_t tx = (uint32_t)(BHALF + (QS ? QBLK_BYTES : 0)) +
@@ -295,12 +301,21 @@ __global__ void __launch_bounds__(NT_TC, 1)
               tma_load_2d(&mapBn, &full[s], np_, 0, brow);
               if (QS) tma_load_2d(&mapQn, &full[s], np_ + BN_BYTES, 0, (int)q0);
             }
+            issued |= 1u << s;
+            last_par = (last_par & ~(1u << s)) | (ph << s);
           }
         }
       }
       }
       // the last unit's tile release has landed before the CTA exits
-      if (!QS && PERSIST && ok && ui > 0) ok = mbar_wait(qempty, (uint32_t)((ui - 1) & 1), abort_flag);
+      if (!QS && PERSIST && ok && ui > 0) ok = mbar_wait(qempty, (uint32_t)((ui - 1) & 1), abort_flag, wl);
+      if (!PAIR) {
+        // every copy this CTA issued has landed before its shared memory is
+        // released (immediate unless a bounded wait gave up)
+        for (int s = 0; s < S; s++)
+          if (issued >> s & 1) mbar_wait_drain(&full[s], last_par >> s & 1);
+        if (qloads > 0) mbar_wait_drain(qfull, (uint32_t)((qloads - 1) & 1));
+      }
       if (PAIR) {
         // every stage released by the leader's MMAs: no commit is still on its
         // way to this CTA when the pair exits
@@ -308,28 +323,28 @@ __global__ void __launch_bounds__(NT_TC, 1)
           const int s = sn;
           const uint32_t ph = phn;
           if (++sn == S) { sn = 0; phn ^= 1; }
-          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) ok = false;
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, wl)) ok = false;
         }
       }
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer (the leader's, for a pair)
     if (lane == 0 && leader) {
-      constexpr uint32_t idesc = idesc_bf16_f32(PAIR ? 2 * TC_TILE_M : TC_TILE_M, TC_TILE_N);
-      bool ok = true;
+      const uint32_t idesc = idesc_16_f32(PAIR ? 2 * TC_TILE_M : TC_TILE_M, TC_TILE_N, sel.f16 != 0);
+      bool ok = true, any = false;
       int sn = 0;
       uint32_t phn = 0;
       int it = 0, ui = 0;
       for (int w = w0; w < nunits && ok; w += wstep, ui++) {
       const UnitInfo un = unit_info(w);
       if (!QS) {
-        if (!mbar_wait(qfull, (uint32_t)(ui & 1), abort_flag)) { ok = false; break; }
+        if (!mbar_wait(qfull, (uint32_t)(ui & 1), abort_flag, wl)) { ok = false; break; }
         tc_fence_after();
       }
       for (int t = un.t_begin; t < un.t_end && ok; t++, it++) {
         const int a = it & 1;
         const uint32_t u = (uint32_t)(it >> 1);
-        if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag)) { ok = false; break; }
+        if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag, wl)) { ok = false; break; }
         tc_fence_after();
         const uint32_t dt = tmem + (uint32_t)(a * TC_TILE_N);
         for (int ks = 0; ks < nks; ks++) {
@@ -339,7 +354,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
           // TMA data: its arrival is tracked by the barrier's transaction
           // count, no tcgen05 fence is needed (a fence here would stall the
           // MMA pipe once per stage)
-          if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
+          if (!mbar_wait(&full[s], ph, abort_flag, wl)) { ok = false; break; }
           const uint32_t sb = smem_u32(Stg + (size_t)s * SB);
           // a descriptor's start address field is addr >> 4 in its low 14 bits
           // (shared addresses < 256 KB): offsets are added to a base descriptor
@@ -364,6 +379,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
                 umma_bf16(dt, dq, dbn, idesc, 1u);
             }
           }
+          any = true;
           if (PAIR)
             umma_commit_pair_mc(&empty[s], 3);
           else
@@ -378,13 +394,18 @@ __global__ void __launch_bounds__(NT_TC, 1)
       // release the resident query tile once this unit's MMAs are done
       if (!QS && PERSIST && ok) umma_commit(qempty);
       }
+      if (!PAIR && any) {
+        // every MMA issued has finished with TMEM and shared memory
+        umma_commit(mdone);
+        mbar_wait_drain(mdone, 0);
+      }
       if (PAIR) {
         // the last two accumulators released by the selection warps of both
         // CTAs: no remote arrival is still on its way when the pair exits
         for (int e = it; e < it + 2 && ok; e++) {
           const int a = e & 1;
           const uint32_t u = (uint32_t)(e >> 1);
-          if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag)) ok = false;
+          if (!mbar_wait(&tempty[a], (u & 1) ^ 1, abort_flag, wl)) ok = false;
         }
       }
     }
@@ -524,7 +545,7 @@ __global__ void __launch_bounds__(NT_TC, 1)
     for (int t = t_begin; t < t_end; t++, it++) {
       const int a = it & 1;
       const uint32_t u = (uint32_t)(it >> 1);
-      ok = mbar_wait(&tfull[a], u & 1, abort_flag);
+      ok = mbar_wait(&tfull[a], u & 1, abort_flag, wl);
       __syncwarp();
       if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
       tc_fence_after();

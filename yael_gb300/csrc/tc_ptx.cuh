@@ -74,17 +74,28 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitim
 // aborted.  Waiting threads sleep in the barrier instead of polling, so they
 // take no issue slots from the selection warps sharing their SM sub-partition.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          volatile int *abort_flag) {
+                                          volatile int *abort_flag,
+                                          uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   for (;;) {
     if (mbar_try_wait_sleep(bar, parity, 200000u)) return true;
     if (*abort_flag) return false;
-    if (globaltimer_ns() - t0 > kWaitLimitNs) {
+    if (globaltimer_ns() - t0 > limit_ns) {
       *abort_flag = 1;
       return false;
     }
   }
+}
+
+// waits (bounded by time alone, whatever the abort flag says) for a phase of
+// an mbarrier that tracks this CTA's own bulk copies: a CTA that gives up
+// still lets the copies it issued land before its shared memory is released
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait_sleep(bar, parity, 200000u))
+    if (globaltimer_ns() - t0 > kWaitLimitNs / 2) return false;
+  return true;
 }
 
 // named barrier 1 over the 256 selection threads, with the AND of their flags
@@ -105,17 +116,6 @@ __device__ __forceinline__ void tma_load_2d(const CUtensorMap *map, uint64_t *ba
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
       "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
-      : "memory");
-}
-
-// the same box into every CTA of ctamask (same shared-memory offset); each
-// destination's mbarrier at the offset of bar receives the complete_tx
-__device__ __forceinline__ void tma_load_2d_mc(const CUtensorMap *map, uint64_t *bar, void *dst,
-                                               int c0, int c1, uint16_t ctamask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      ".multicast::cluster [%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "h"(ctamask)
       : "memory");
 }
 
@@ -166,16 +166,6 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(bar))
-      : "memory");
-}
-
-// arrive on bar (same offset) in every CTA of ctamask once all previously
-// issued tcgen05.mma of this thread completed
-__device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t ctamask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
-      " [%0], %1;" ::"r"(smem_u32(bar)),
-      "h"(ctamask)
       : "memory");
 }
 
@@ -299,6 +289,10 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
          | (1u << 7)          // A format: bf16
          | (1u << 10)         // B format: bf16
          | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// the same with A and B both fp16 (format code 0) when f16, else both bf16
+__host__ __device__ constexpr uint32_t idesc_16_f32(int M, int N, bool f16) {
+  return f16 ? (idesc_bf16_f32(M, N) & ~((7u << 7) | (7u << 10))) : idesc_bf16_f32(M, N);
 }
 
 }  // namespace ptx

@@ -12,7 +12,11 @@ bool tc_supported(int d) { return d >= 1; }
 int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Workspace &ws,
                        int slot_pack, int slot_norm, TcOperands *op, double *qn64,
                        unsigned char *qflag, float *qres, int split, float *lonorm,
-                       cudaStream_t st) {
+                       cudaStream_t st, int f16) {
+  if (split && f16) {
+    set_error(E_ARG, "tc_prepare_queries: the split packing is bf16 only");
+    return E_ARG;
+  }
   const int Kp1 = ((d + 63) / 64) * 64, Kp = split ? 3 * Kp1 : Kp1;
   void *pack, *norm = nullptr;
   YG_CHECK(ws.get(slot_pack, (size_t)nq * Kp * 2, &pack));
@@ -25,11 +29,12 @@ int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Work
                              st));
   else
     YG_CHECK(prep_rows(q, ldq, nq, d, scale, qn64, nullptr, qflag, qres, (__nv_bfloat16 *)pack,
-                       Kp, (__nv_bfloat16 *)norm, nmode, nullptr, st));
+                       Kp, (__nv_bfloat16 *)norm, nmode, nullptr, st, 8, f16));
   op->d = d;
   op->Kp = Kp;
   op->metric = metric;
   op->split = split;
+  op->f16 = f16;
   op->q = (const __nv_bfloat16 *)pack;
   op->qn = (const __nv_bfloat16 *)norm;
   return OK;
@@ -37,7 +42,11 @@ int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Work
 
 int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspace &ws,
                     int slot_pack, int slot_norm, int slot_res, TcOperands *op, float *bn32,
-                    SetStats *bs, int split, cudaStream_t st) {
+                    SetStats *bs, int split, cudaStream_t st, int f16) {
+  if (split && f16) {
+    set_error(E_ARG, "tc_prepare_base: the split packing is bf16 only");
+    return E_ARG;
+  }
   const int Kp1 = ((d + 63) / 64) * 64, Kp = split ? 3 * Kp1 : Kp1;
   void *pack, *norm = nullptr, *res;
   YG_CHECK(ws.get(slot_pack, (size_t)nb * Kp * 2, &pack));
@@ -49,11 +58,12 @@ int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspa
                              (__nv_bfloat16 *)pack, Kp1, (__nv_bfloat16 *)norm, nmode, bs, st));
   else
     YG_CHECK(prep_rows(b, ldb, nb, d, 1.f, nullptr, bn32, nullptr, (float *)res,
-                       (__nv_bfloat16 *)pack, Kp, (__nv_bfloat16 *)norm, nmode, bs, st));
+                       (__nv_bfloat16 *)pack, Kp, (__nv_bfloat16 *)norm, nmode, bs, st, 8, f16));
   op->d = d;
   op->Kp = Kp;
   op->metric = metric;
   op->split = split;
+  op->f16 = f16;
   op->b = (const __nv_bfloat16 *)pack;
   op->bn = (const __nv_bfloat16 *)norm;
   op->b_rows = nb;
@@ -69,7 +79,7 @@ int tc_prepare_base_range(const float *b, long ldb, long row0, int n, int d, int
   __nv_bfloat16 *pack = const_cast<__nv_bfloat16 *>(op.b) + row0 * op.Kp;
   __nv_bfloat16 *norm = op.bn ? const_cast<__nv_bfloat16 *>(op.bn) + row0 * 16 : nullptr;
   return prep_rows(b + row0 * ldb, ldb, n, d, 1.f, nullptr, bn32 + row0, nullptr, res + row0,
-                   pack, op.Kp, norm, nmode, bs, st);
+                   pack, op.Kp, norm, nmode, bs, st, 8, op.f16);
 }
 
 int tc_alloc_base(int nb, int d, int metric, Workspace &ws, int slot_pack, int slot_norm,
@@ -110,8 +120,12 @@ int tc_dispatch_r1(const TcOperands &op, int nq, int nb, const ScanSel &sel, cud
   return tck::dispatch_metric<false, false>(op, nq, nb, sel, st);
 }
 
-int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel, cudaStream_t st) {
+int tc_scan(const TcOperands &op, int nq, int nb, const ScanSel &sel_in, cudaStream_t st) {
   if (nq <= 0 || nb <= 0) return OK;
+  ScanSel sel = sel_in;
+  sel.f16 = op.f16;  // the MMA's operand format
+  sel.wait_ns = wait_limit_ns();
+  sel.withhold = test_withhold_loads() ? 1 : 0;
   if (sel.units) {
     // grouped pass: the streamed-query persistent form walks the unit table;
     // ids of list passes would not be relative to their pair

@@ -1,5 +1,6 @@
-// BF16 tensor-core (tcgen05) producer of distance tiles with the fused
-// selection of scan.cuh.
+// 16-bit tensor-core (tcgen05 kind::f16) producer of distance tiles with the
+// fused selection of scan.cuh: bf16 operands, or fp16 ones (same layout, 8x
+// finer rounding, the same tensor rate) where the data range allows.
 //
 // Operands are packed once per call: queries as bf16(-2 q) (L2) or bf16(q)
 // (dot), base rows as bf16(b); both padded to Kp = 64*ceil(d/64) columns.  For
@@ -26,6 +27,7 @@ struct TcOperands {
   long b_rows = 0;                    // packed base rows
   long b_step = 1;                    // scan row j reads packed row j*b_step
   int split = 0;                      // 1: 3xBF16 split packing (Kp = 3 * Kp1)
+  int f16 = 0;                        // 1: IEEE fp16 operands (the same layout as bf16)
   int *err = nullptr;                 // device flag set when a bounded wait expires
 };
 
@@ -34,15 +36,17 @@ struct TcOperands {
 bool tc_supported(int d);
 
 // split = 0: bf16 packing; split = 1: 3xBF16 split packing (prep.cuh); lonorm
-// (split only) receives ||lo|| per row
+// (split only) receives ||lo|| per row.  f16 = 1 (not with split): fp16 packing
+// (prep_rows), for data whose range fp16 holds; both operands of a pass must
+// use the same encoding.
 int tc_prepare_queries(const float *q, long ldq, int nq, int d, int metric, Workspace &ws,
                        int slot_pack, int slot_norm, TcOperands *op, double *qn64,
                        unsigned char *qflag, float *qres, int split, float *lonorm,
-                       cudaStream_t st);
+                       cudaStream_t st, int f16 = 0);
 
 int tc_prepare_base(const float *b, long ldb, int nb, int d, int metric, Workspace &ws,
                     int slot_pack, int slot_norm, int slot_res, TcOperands *op, float *bn32,
-                    SetStats *bs, int split, cudaStream_t st);
+                    SetStats *bs, int split, cudaStream_t st, int f16 = 0);
 
 // strided view of the packed base (every stride-th row, nrows rows)
 int tc_base_view(const TcOperands &full, int stride, int nrows, TcOperands *out);
