@@ -407,10 +407,11 @@ def hkm_record(args, local):
     assign = np.empty(n, np.int32)
     it, ms = ctypes.c_long(0), ctypes.c_float(0)
     vp = torch.from_numpy(v_h).pin_memory()
+    libc = ctypes.CDLL(None)
+    libc.srand48.argtypes = [ctypes.c_long]
 
     def learn(x, nn):
-        libc = ctypes.CDLL(None)
-        libc.srand48(ctypes.c_long(0))
+        libc.srand48(0)
         st = yg.CallStats()
         rc = L.yael_gpu_hkm_learn_ex(nn, d, nl, bf, x, niter, 1, ptr(cent), ptr(assign),
                                      ctypes.byref(it), ctypes.byref(ms))
@@ -472,23 +473,26 @@ def hkm_record(args, local):
         # the tree of a tenth of the points, GPU against the oracle's exact mode
         cg = np.empty_like(cent)
         ag = np.empty(sub.shape[0], np.int32)
-        libc.srand48(ctypes.c_long(0))
+        libc.srand48(0)
         rc = L.yael_gpu_hkm_learn_ex(sub.shape[0], d, nl, bf, ptr(sub), niter, 1, ptr(cg),
                                      ptr(ag), None, None)
         co = np.empty_like(cent)
         ao = np.empty(sub.shape[0], np.int32)
-        libc.srand48(ctypes.c_long(0))
+        libc.srand48(0)
         t0 = time.perf_counter()
-        ro = oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(co), ptr(ao), 1)
+        # exact mode (1) with the small-node rule of the GPU call (0x100)
+        ro = oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(co), ptr(ao),
+                                    1 | 0x100)
         rec["parity"] = {"points": sub.shape[0], "status": [rc, ro],
                          "assignments_identical_to_oracle_exact": bool((ag == ao).all()),
                          "centroids_bit_identical": bool((cg == co).all()),
                          "check_seconds": time.perf_counter() - t0}
     if not args.no_cpu:
         oc = np.empty_like(cent)
-        libc.srand48(ctypes.c_long(0))
+        libc.srand48(0)
         t0 = time.perf_counter()
-        oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(oc), None, 0)
+        # port mode (the reference's arithmetic) with the same small-node rule
+        oracle().orc_hkm_learn(sub.shape[0], d, nl, bf, ptr(sub), niter, ptr(oc), None, 0x100)
         cdt = time.perf_counter() - t0
         # the tree has the same instances and iterations at n / 10; each
         # instance's work is linear in its points: time x 10 for the full n

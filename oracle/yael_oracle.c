@@ -1034,12 +1034,22 @@ int orc_hkm_learn(int n, int d, int nlevel, int bf, const float *points,
     for (long parent = 0; parent < k; parent++) {
       int na = 0;
       while (pos + na < n && node[perm[pos + na]] == parent) na++;
-      if (na == 0 || na < bf) { rc = -1; break; }
+      const int small = na < bf && (mode & ORC_HKM_SMALL_NODES);
+      if (na == 0 || (na < bf && !small)) { rc = -1; break; }
       int *ca = malloc(sizeof(int) * (size_t)na);
       float *C = malloc(sizeof(float) * (size_t)bf * d);
-      orc_kmeans(d, na, bf, nb_iter_max, v + pos * d,
-                 8 | ORC_KMEANS_INIT_RANDOM | ORC_KMEANS_QUIET, 0, 1, C, NULL, ca,
-                 NULL, mode, NULL);
+      if (small) {
+        /* one child per point (later children repeat the last point); the
+         * kmeans() seed draw is still made, so later seeds stay in step */
+        (void)lrand48();
+        for (int j = 0; j < bf; j++)
+          memcpy(C + (long)j * d, v + (pos + (j < na ? j : na - 1)) * d, sizeof(float) * d);
+        for (int i = 0; i < na; i++) ca[i] = i;
+      } else {
+        orc_kmeans(d, na, bf, nb_iter_max, v + pos * d,
+                   8 | ORC_KMEANS_INIT_RANDOM | ORC_KMEANS_QUIET, 0, 1, C, NULL, ca,
+                   NULL, mode & 1, NULL);
+      }
       memcpy(centroids_out + off + parent * bf * d, C, sizeof(float) * (size_t)bf * d);
       for (int i = 0; i < na; i++) {
         int t = perm[pos + i];

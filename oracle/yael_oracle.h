@@ -122,7 +122,11 @@ int orc_fixed_shift(long n, long d, const float *v);
 /* hierarchical k-means (yael/hkm.c:36-116).  centroids_out receives the
  * levels concatenated (level l holds bf^(l+1) rows of d floats).  assign_out
  * (n ints, may be NULL).  Returns 0, or -1 when a node is empty (where the
- * reference exits, yael/hkm.c:77-80) or too small for bf clusters. */
+ * reference exits, yael/hkm.c:77-80) or too small for bf clusters.  With
+ * ORC_HKM_SMALL_NODES or'ed into mode, a node with 0 < n < bf points gets one
+ * child per point instead (the GPU library's small_nodes = 1 rule, not the
+ * reference's). */
+#define ORC_HKM_SMALL_NODES 0x100
 int orc_hkm_learn(int n, int d, int nlevel, int bf, const float *points,
                   int nb_iter_max, float *centroids_out, int *assign_out, int mode);
 

@@ -80,6 +80,17 @@ def test_kmeans_large_k_bf16_operands():
     assert g["prec_used"] == 1
 
 
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "fp16"])
+def test_kmeans_k_above_256_prior_bound_pass(prec):
+    """k > 256: the k-NN assignment.  From the second iteration on the chosen
+    form runs a threshold pass from each point's distance to its previous
+    centroid (no sample pass); iteration counts, assignments and centroids
+    equal the oracle's."""
+    v, _, _ = synth.gaussian_mixture(30000, 32, 500, 0.2, seed=15)
+    g = gpu_kmeans(v, 400, 8, QUIET, 21, 1, prec)
+    same(g, oracle_kmeans(v, 400, 8, QUIET, 21, 1))
+
+
 def duplicate_heavy(seed):
     """40% of the points are one vector: random init picks many identical
     centroids.  On the k-NN assignment (k > 256) the candidate lists of those
@@ -132,8 +143,8 @@ def test_kmeans_inline_check_rejections():
 def test_kmeans_tensor_core_assignment_ties(prec, k):
     """The small-k tensor-core assignment on duplicate-heavy data (bands wider
     than their lists, exact FP32 ties decided in FP64): bit-identical to the
-    oracle.  k = 100 fuses the centroid sums into the pass (k * d * 8 bytes fit
-    shared memory); k = 256 keeps the sorted update."""
+    oracle.  The centroid sums come with the pass: through shared memory for
+    k = 100 (k * d * 8 bytes fit), straight into the global sums for k = 256."""
     v = duplicate_heavy(31)
     g = gpu_kmeans(v, k, 8, QUIET, 5, 1, prec)
     assert g["prec_used"] == 3  # fp16 holds this data's range
@@ -236,6 +247,26 @@ def test_hkm_chosen_form_vs_oracle(prec, monkeypatch):
     yg.lib().yael_gpu_last_stats(ctypes.byref(st))
     assert st.prec_used == (3 if prec == "bf16" else 0)
     assert st.point_iterations >= st.instance_iterations > 0
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp32"])
+def test_hkm_small_nodes_vs_oracle(prec, monkeypatch):
+    """Nodes with fewer points than bf (small_nodes = 1: one child per point,
+    the seed draw still made): the oracle's restatement of that rule gives
+    the same tree, bit for bit, in both forms (and the tensor-core assignment
+    runs with many small instances)."""
+    monkeypatch.setenv("YAEL_GPU_PRECISION", prec)
+    v, _, _ = synth.gaussian_mixture(6000, 32, 60, 0.15, seed=23)
+    n, d = v.shape
+    nl, bf = 3, 16
+    cent = np.zeros(sum(bf ** (l + 1) for l in range(nl)) * d, np.float32)
+    oa = np.empty(n, np.int32)
+    srand48(3)
+    assert oracle().orc_hkm_learn(n, d, nl, bf, ptr(v), 5, ptr(cent), ptr(oa), 1 | 0x100) == 0
+    srand48(3)
+    levels, ga = yg.hkm(v, nl, bf, 5, small_nodes=True)
+    np.testing.assert_array_equal(ga, oa)
+    np.testing.assert_array_equal(np.concatenate([l.ravel() for l in levels]), cent)
 
 
 def test_hkm_golden_and_quantize(gpu_lib):

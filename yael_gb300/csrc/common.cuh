@@ -119,6 +119,9 @@ struct WaitLimitScope {
 // and the call returns YAEL_GPU_ETIMEOUT with the context still usable.  A
 // test hook for that path; nothing is faulted and nothing hangs.
 bool test_withhold_loads();
+// YAEL_GPU_TEST_FAIL_ALLOC=n: the n-th workspace growth after the variable
+// was set fails as an out-of-memory cudaMalloc (host-side test hook)
+bool test_fail_alloc();
 // YAEL_GPU_TRACE set (and not "0"): every k-NN pass is timed with CUDA events
 // and reported on stderr, one line per pass
 bool trace_enabled();

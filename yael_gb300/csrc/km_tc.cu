@@ -43,18 +43,20 @@ constexpr int A_BLK = 128 * 128;  // 128 rows x 64 16-bit columns
 constexpr int A_SIDE = 128 * 32;  // 128 rows x 16 16-bit columns
 
 struct Lay {
-  int nkb, N, S, fuse;
-  size_t stage_bytes, b_off, bside_off, band_off, acc_off, cnt_off, bar_off, total;
+  int nkb, N, S, fuse, csm;
+  size_t stage_bytes, b_off, bside_off, cf_off, band_off, acc_off, cnt_off, bar_off, total;
 };
 
-__host__ __device__ inline Lay make_lay(int nkb, int N, int S, int fuse, int k, int d) {
+__host__ __device__ inline Lay make_lay(int nkb, int N, int S, int fuse, int k, int d,
+                                       int csm) {
   Lay L;
-  L.nkb = nkb; L.N = N; L.S = S; L.fuse = fuse;
+  L.nkb = nkb; L.N = N; L.S = S; L.fuse = fuse; L.csm = csm;
   size_t off = 0;
   L.stage_bytes = (size_t)nkb * A_BLK + A_SIDE;  // a multiple of 1024
   off += (size_t)S * L.stage_bytes;
   L.b_off = off;     off += (size_t)nkb * N * 128;  // N % 32 == 0: 1024-aligned blocks
   L.bside_off = off; off += (size_t)N * 32;
+  L.cf_off = off;    off += csm ? (size_t)N * d * 4 : 0;  // FP32 centroid rows (d % 4 == 0)
   L.band_off = off;  off += (size_t)2 * 128 * (BMAX + 1) * 4;
   off = (off + 15) & ~(size_t)15;
   L.acc_off = off;   off += fuse ? (size_t)k * d * 8 : 0;
@@ -80,6 +82,9 @@ struct Params {
   int *counts;
   const int *shift;
   int *err;
+  int acc_global;              // sums added straight to acc / counts (k * d too large
+                               // for shared memory)
+  int csm;                     // the instance's FP32 centroid rows staged in shared memory
   unsigned long long wait_ns;  // bound of every wait (0: kWaitLimitNs)
   int withhold;                // test switch: the producer issues no load
 };
@@ -90,25 +95,147 @@ __device__ __forceinline__ float warp_sum(float x) {
   return x;
 }
 
+constexpr int G = 8;  // rows a warp of the epilogue takes at once in phase B
+
+// a float4 of a centroid row: shared memory (staged) or global (read-only path)
+__device__ __forceinline__ float4 cload(const float *p, bool sm) {
+  return sm ? *reinterpret_cast<const float4 *>(p) : __ldg(reinterpret_cast<const float4 *>(p));
+}
+
+template <int ND4>
+__device__ __forceinline__ float row_dist(const float4 (&x)[ND4], const float4 (&c)[ND4],
+                                          int lane, int d4) {
+  float s = 0.f;
+#pragma unroll
+  for (int q = 0; q < ND4; q++) {
+    if (lane + 32 * q < d4) {
+      float t = x[q].x - c[q].x;
+      s = fmaf(t, t, s);
+      t = x[q].y - c[q].y;
+      s = fmaf(t, t, s);
+      t = x[q].z - c[q].z;
+      s = fmaf(t, t, s);
+      t = x[q].w - c[q].w;
+      s = fmaf(t, t, s);
+    }
+  }
+  return warp_sum(s);
+}
+
+// Phase B for one point (the whole warp): the band's exact decision, the
+// outputs, and the point's fixed-point row added to its centroid's sums.  c0
+// holds the first band member's row (or centroid 0's when the band
+// overflowed its list); Ci the instance's centroid rows (staged or global).
+template <int ND4>
+__device__ __forceinline__ void finish_row(const Params &P, const int *bl, int r0, long p,
+                                           const float *Ci, const float4 (&x)[ND4],
+                                           const float4 (&c0)[ND4], int lane, int d, int d4,
+                                           int k, float rho, bool fuse,
+                                           unsigned long long *sacc, int *scnt, int sh,
+                                           int inst) {
+  const int cnt = bl[r0 * (BMAX + 1)];
+  const int nm = cnt > BMAX ? k : cnt;  // an overflowing band: every centroid
+  float e1 = INFINITY, e2 = INFINITY;
+  int j1 = -1;
+  for (int m = 0; m < nm; m++) {
+    const int j = cnt > BMAX ? m : bl[r0 * (BMAX + 1) + 1 + m];
+    float e;
+    if (m == 0) {
+      e = row_dist<ND4>(x, c0, lane, d4);
+    } else {
+      float4 c[ND4];
+#pragma unroll
+      for (int q = 0; q < ND4; q++) {
+        const int c4 = lane + 32 * q;
+        c[q] = c4 < d4 ? cload(Ci + (long)j * d + 4 * c4, P.csm != 0)
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      e = row_dist<ND4>(x, c, lane, d4);
+    }
+    // members come in increasing index order: strict '<' keeps the lower
+    // index on equal values
+    if (e < e1) { e2 = e1; e1 = e; j1 = j; } else if (e < e2) { e2 = e; }
+  }
+  int oj = -1;
+  float od = 1e30f;
+  if (j1 >= 0 && e1 < 1e30f) {
+    oj = j1;
+    od = e1;
+    if (e2 < INFINITY && e2 - e1 <= rho * (e1 + e2)) {
+      // near tie: FP64 over the members, sequential over coordinates, a lane
+      // per member; lowest index on equal values
+      double best = INFINITY;
+      int bj = INT_MAX;
+      for (int m = lane; m < nm; m += 32) {
+        const int j = cnt > BMAX ? m : bl[r0 * (BMAX + 1) + 1 + m];
+        const float *cr = Ci + (long)j * d, *xr = P.v + p * d;
+        double s = 0;
+        for (int c = 0; c < d; c++) {
+          const double t = (double)xr[c] - (double)cr[c];
+          s += t * t;
+        }
+        if (s < best || (s == best && j < bj)) { best = s; bj = j; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oj2 = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (ob < best || (ob == best && oj2 < bj)) { best = ob; bj = oj2; }
+      }
+      if (bj != INT_MAX && best < 1e30) { oj = bj; od = (float)best; }
+      else { oj = -1; od = 1e30f; }
+    }
+  }
+  if (lane == 0) {
+    P.assign[p] = oj;
+    P.dis[p] = od;
+  }
+  if (fuse && oj >= 0) {
+    // the instance's shared-memory sums, or the global ones directly
+    const long g = (long)inst * k + oj;
+    unsigned long long *row_acc =
+        P.acc_global ? reinterpret_cast<unsigned long long *>(P.acc) + g * d
+                     : sacc + (long)oj * d;
+#pragma unroll
+    for (int q = 0; q < ND4; q++) {
+      const int c4 = lane + 32 * q;
+      if (c4 < d4) {
+        atomicAdd(row_acc + 4 * c4 + 0, (unsigned long long)fixed_of(x[q].x, sh));
+        atomicAdd(row_acc + 4 * c4 + 1, (unsigned long long)fixed_of(x[q].y, sh));
+        atomicAdd(row_acc + 4 * c4 + 2, (unsigned long long)fixed_of(x[q].z, sh));
+        atomicAdd(row_acc + 4 * c4 + 3, (unsigned long long)fixed_of(x[q].w, sh));
+      }
+    }
+    if (lane == 0) {
+      if (P.acc_global) atomicAdd(P.counts + g, 1);
+      else atomicAdd(scnt + oj, 1);
+    }
+  }
+}
+
+template <int ND4>
 __global__ void __launch_bounds__(NT, 1)
     km_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAs,
                  const __grid_constant__ CUtensorMap mapB, const __grid_constant__ CUtensorMap mapBs,
-                 int S, Params P) {
+                 const __grid_constant__ CUtensorMap mapC, int S, Params P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int nkb = P.Kp / 64, N = P.N, k = P.k, d = P.d;
   const bool fuse = P.acc != nullptr;
-  const Lay lay = make_lay(nkb, N, S, fuse ? 1 : 0, k, d);
+  const bool sfuse = fuse && !P.acc_global;  // shared-memory sums
+  const Lay lay = make_lay(nkb, N, S, sfuse ? 1 : 0, k, d, P.csm);
   uint8_t *Stg = base;
   uint8_t *Bs = base + lay.b_off;
   uint8_t *Bside = base + lay.bside_off;
+  float *Cf = reinterpret_cast<float *>(base + lay.cf_off);
   int *band = reinterpret_cast<int *>(base + lay.band_off);  // [2][128][BMAX + 1]
   unsigned long long *sacc = reinterpret_cast<unsigned long long *>(base + lay.acc_off);
   int *scnt = reinterpret_cast<int *>(base + lay.cnt_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(base + lay.bar_off);
   uint64_t *full = bars, *empty = bars + S, *tfull = bars + 2 * S, *tempty = bars + 2 * S + 2;
   uint64_t *bfull = bars + 2 * S + 4, *bempty = bars + 2 * S + 5, *mdone = bars + 2 * S + 6;
+  uint64_t *cempty = bars + 2 * S + 7;  // the staged FP32 centroids read by the epilogue
   uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * S + 8);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_holder + 1);
   const uint64_t wl = P.wait_ns ? (uint64_t)P.wait_ns : kWaitLimitNs;
@@ -132,6 +259,7 @@ __global__ void __launch_bounds__(NT, 1)
     mbar_init(bfull, 1);
     mbar_init(bempty, 1);
     mbar_init(mdone, 1);
+    mbar_init(cempty, 8);  // the eight epilogue warps
     *abort_flag = 0;
     fence_mbar_init();
   }
@@ -139,7 +267,7 @@ __global__ void __launch_bounds__(NT, 1)
     tmem_alloc(tmem_holder, tcols);
     tmem_relinquish();
   }
-  if (fuse && warp >= 2) {
+  if (sfuse && warp >= 2) {
     for (int i = threadIdx.x - 64; i < k * d; i += 256) sacc[i] = 0ull;
     for (int i = threadIdx.x - 64; i < k; i += 256) scnt[i] = 0;
   }
@@ -157,7 +285,7 @@ __global__ void __launch_bounds__(NT, 1)
       int cur = -1, nbl = 0;
       bool ok = true;
       const uint32_t abytes = (uint32_t)(nkb * A_BLK + A_SIDE);
-      const uint32_t bbytes = (uint32_t)(nkb * N * 128 + N * 32);
+      const uint32_t bbytes = (uint32_t)(nkb * N * 128 + N * 32 + (P.csm ? N * d * 4 : 0));
       for (int w = w0; w < w1 && ok; w++) {
         const KmTcUnit u = P.units[w];
         if (!P.active[u.inst]) continue;
@@ -167,10 +295,16 @@ __global__ void __launch_bounds__(NT, 1)
             ok = false;
             break;
           }
+          // and the staged FP32 rows once the epilogue is done with them
+          if (nbl > 0 && P.csm && !mbar_wait(cempty, (uint32_t)((nbl - 1) & 1), abort_flag, wl)) {
+            ok = false;
+            break;
+          }
           mbar_arrive_expect_tx(bfull, bbytes);
           for (int kb = 0; kb < nkb; kb++)
             tma_load_2d(&mapB, bfull, Bs + (size_t)kb * N * 128, kb * 64, u.inst * k);
           tma_load_2d(&mapBs, bfull, Bside, 0, u.inst * k);
+          if (P.csm) tma_load_2d(&mapC, bfull, Cf, 0, u.inst * k);
           nbl++;
           cur = u.inst;
         }
@@ -269,19 +403,29 @@ __global__ void __launch_bounds__(NT, 1)
       }
       asm volatile("bar.sync 1, 256;" ::: "memory");
     };
+    int nbl = 0;  // centroid tiles seen (the staged FP32 rows' bfull phases)
     for (int w = w0; w < w1 && ok; w++) {
       const KmTcUnit u = P.units[w];
       if (!P.active[u.inst]) continue;
-      if (fuse && u.inst != cur) {
-        if (cur >= 0) flush(cur);
+      if (u.inst != cur) {
+        if (sfuse && cur >= 0) flush(cur);
+        // the previous instance's staged rows are no longer read by this warp
+        if (P.csm && cur >= 0 && lane == 0) mbar_arrive(cempty);
+        if (P.csm) {
+          // the new instance's rows have landed (the MMA warp waits on the same
+          // phase of bfull before its first MMA of the instance)
+          ok = mbar_wait(bfull, (uint32_t)(nbl & 1), abort_flag, wl);
+          __syncwarp();
+          ok = __all_sync(0xffffffffu, ok);
+        }
+        nbl++;
         cur = u.inst;
       }
-      cur = u.inst;
       const int a = it & 1;
       int *bl = band + a * 128 * (BMAX + 1);
       if (ew < 4) {
         const uint32_t uu = (uint32_t)(it >> 1);
-        ok = mbar_wait(&tfull[a], uu & 1, abort_flag, wl);
+        ok = ok && mbar_wait(&tfull[a], uu & 1, abort_flag, wl);
         __syncwarp();
         ok = __all_sync(0xffffffffu, ok);
         if (ok) {
@@ -329,94 +473,43 @@ __global__ void __launch_bounds__(NT, 1)
       // read by every warp before it): one barrier per tile, all warps agree
       ok = bar_red_and_256(ok);
       if (!ok) break;
+      // phase B: a warp takes rows ew, ew + 8, ..., eight at a time, with the
+      // point rows and each point's first band member loaded for all eight
+      // before any is used (the loads are the latency of this phase)
       const int sh = fuse ? P.shift[u.inst] : 0;
-      for (int r0 = ew; r0 < u.np; r0 += 8) {
-        const long p = u.p0 + r0;
-        const int cnt = bl[r0 * (BMAX + 1)];
-        float4 x4[2];
+      const float *Ci = P.csm ? Cf : P.C + (long)u.inst * k * d;
+#pragma unroll 1
+      for (int i0 = 0; i0 < 128 / 8; i0 += G) {
+        if (ew + 8 * i0 >= u.np) break;  // uniform over the warp
+        float4 xb[G][ND4], cb[G][ND4];
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-          const int c4 = lane + 32 * q;
-          x4[q] = c4 < d4 ? __ldg(reinterpret_cast<const float4 *>(P.v + p * d) + c4)
+        for (int g = 0; g < G; g++) {
+          const int r0 = ew + 8 * (i0 + g);
+          const bool val = r0 < u.np;
+          const int cnt = val ? bl[r0 * (BMAX + 1)] : 0;
+          const int j0 = cnt > BMAX ? 0 : cnt > 0 ? bl[r0 * (BMAX + 1) + 1] : 0;
+          const long p = u.p0 + r0;
+#pragma unroll
+          for (int q = 0; q < ND4; q++) {
+            const int c4 = lane + 32 * q;
+            const bool in = val && c4 < d4;
+            xb[g][q] = in ? __ldg(reinterpret_cast<const float4 *>(P.v + p * d) + c4)
                           : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        const int nm = cnt > BMAX ? k : cnt;  // an overflowing band: every centroid
-        const float *Ci = P.C + (long)u.inst * k * d;
-        float e1 = INFINITY, e2 = INFINITY;
-        int j1 = -1;
-        for (int m = 0; m < nm; m++) {
-          const int j = cnt > BMAX ? m : bl[r0 * (BMAX + 1) + 1 + m];
-          float sacc_ = 0.f;
-#pragma unroll
-          for (int q = 0; q < 2; q++) {
-            const int c4 = lane + 32 * q;
-            if (c4 < d4) {
-              const float4 cv = __ldg(reinterpret_cast<const float4 *>(Ci + (long)j * d) + c4);
-              float t = x4[q].x - cv.x;
-              sacc_ = fmaf(t, t, sacc_);
-              t = x4[q].y - cv.y;
-              sacc_ = fmaf(t, t, sacc_);
-              t = x4[q].z - cv.z;
-              sacc_ = fmaf(t, t, sacc_);
-              t = x4[q].w - cv.w;
-              sacc_ = fmaf(t, t, sacc_);
-            }
-          }
-          const float e = warp_sum(sacc_);
-          if (e < e1) { e2 = e1; e1 = e; j1 = j; } else if (e < e2) { e2 = e; }
-        }
-        int oj = -1;
-        float od = 1e30f;
-        if (j1 >= 0 && e1 < 1e30f) {
-          oj = j1;
-          od = e1;
-          if (e2 < INFINITY && e2 - e1 <= rho * (e1 + e2)) {
-            // near tie: FP64 over the members, sequential over coordinates, a
-            // lane per member; lowest index on equal values
-            double best = INFINITY;
-            int bj = INT_MAX;
-            for (int m = lane; m < nm; m += 32) {
-              const int j = cnt > BMAX ? m : bl[r0 * (BMAX + 1) + 1 + m];
-              const float *cr = Ci + (long)j * d, *xr = P.v + p * d;
-              double s = 0;
-              for (int c = 0; c < d; c++) {
-                const double t = (double)xr[c] - (double)cr[c];
-                s += t * t;
-              }
-              if (s < best || (s == best && j < bj)) { best = s; bj = j; }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-              const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-              const int oj2 = __shfl_xor_sync(0xffffffffu, bj, o);
-              if (ob < best || (ob == best && oj2 < bj)) { best = ob; bj = oj2; }
-            }
-            if (bj != INT_MAX && best < 1e30) { oj = bj; od = (float)best; }
-            else { oj = -1; od = 1e30f; }
+            cb[g][q] = in && cnt > 0 ? cload(Ci + (long)j0 * d + 4 * c4, P.csm != 0)
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         }
-        if (lane == 0) {
-          P.assign[p] = oj;
-          P.dis[p] = od;
-        }
-        if (fuse && oj >= 0) {
-          unsigned long long *row_acc = sacc + (long)oj * d;
 #pragma unroll
-          for (int q = 0; q < 2; q++) {
-            const int c4 = lane + 32 * q;
-            if (c4 < d4) {
-              atomicAdd(row_acc + 4 * c4 + 0, (unsigned long long)fixed_of(x4[q].x, sh));
-              atomicAdd(row_acc + 4 * c4 + 1, (unsigned long long)fixed_of(x4[q].y, sh));
-              atomicAdd(row_acc + 4 * c4 + 2, (unsigned long long)fixed_of(x4[q].z, sh));
-              atomicAdd(row_acc + 4 * c4 + 3, (unsigned long long)fixed_of(x4[q].w, sh));
-            }
-          }
-          if (lane == 0) atomicAdd(scnt + oj, 1);
+        for (int g = 0; g < G; g++) {
+          const int r0 = ew + 8 * (i0 + g);
+          if (r0 < u.np)
+            finish_row<ND4>(P, bl, r0, u.p0 + r0, Ci, xb[g], cb[g], lane, d, d4, k, rho, fuse,
+                            sacc, scnt, sh, u.inst);
         }
       }
       it++;
     }
-    if (fuse && ok && cur >= 0) flush(cur);
+    if (sfuse && ok && cur >= 0) flush(cur);
   }
 
   tc_fence_before();
@@ -430,6 +523,31 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 }  // namespace kmtc
+
+namespace {
+// a tensor map over FP32 rows, no swizzle (box: cols x rows)
+int make_map_f32(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t rows, uint32_t box_cols,
+                 uint32_t box_rows) {
+  YG_CHECK(tck::get_encode());
+  if (!ptr || (reinterpret_cast<uintptr_t>(ptr) & 15) || ((cols * 4) & 15) || rows == 0) {
+    set_error(E_ARG, "tensor map (f32): null / misaligned operand");
+    return E_ARG;
+  }
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 4};
+  cuuint32_t box[2] = {box_cols, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = tck::g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(ptr), dims,
+                             strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error(E_CUDA, "cuTensorMapEncodeTiled (f32) failed (%d)", (int)r);
+    return E_CUDA;
+  }
+  return OK;
+}
+}  // namespace
 
 bool km_tc_supported(int d, int k, const float *v, const float *C) {
   return d >= 4 && d % 4 == 0 && d <= 256 && k >= 1 && k <= kTcMaxK &&
@@ -454,28 +572,31 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   YG_CHECK(stats_reset(cstats, st));
   YG_CHECK(prep_rows(C, d, (int)ncl, d, 1.f, nullptr, nullptr, nullptr, cres,
                      (__nv_bfloat16 *)cpk, P.Kp, (__nv_bfloat16 *)cside, 1, cstats, st, 8, P.f16));
-  const int fuse = acc != nullptr;
-  if (fuse && !km_tc_fuses(d, k)) {
-    set_error(E_UNSUPPORTED, "km_tc_assign: fused sums of k*d=%ld need too much shared memory",
-              (long)k * d);
-    return E_UNSUPPORTED;
-  }
+  // the sums go through shared memory when an instance's k x d fit, else
+  // straight to the global accumulators
+  const int acc_global = acc != nullptr && !km_tc_fuses(d, k);
+  const int fuse = acc != nullptr && !acc_global;
+  // the instance's FP32 centroid rows are staged when they are few
+  const int csm = (size_t)N * d * 4 <= 32 * 1024;
   int S = 6;
-  while (S > 2 && make_lay(nkb, N, S, fuse, k, d).total > 227 * 1024) S--;
-  const Lay lay = make_lay(nkb, N, S, fuse, k, d);
+  while (S > 2 && make_lay(nkb, N, S, fuse, k, d, csm).total > 227 * 1024) S--;
+  const Lay lay = make_lay(nkb, N, S, fuse, k, d, csm);
   if (lay.total > 227 * 1024) {
     set_error(E_UNSUPPORTED, "km_tc_assign: shared memory %zu too large (d=%d k=%d)", lay.total,
               d, k);
     return E_UNSUPPORTED;
   }
-  YG_CHECK(ensure_smem((const void *)km_tc_kernel, lay.total));
-  CUtensorMap mA, mAs, mB, mBs;
+  auto kern = d <= 128 ? km_tc_kernel<1> : km_tc_kernel<2>;
+  YG_CHECK(ensure_smem((const void *)kern, lay.total));
+  CUtensorMap mA, mAs, mB, mBs, mC;
   YG_CHECK(tck::make_map(&mA, P.pk, P.Kp, P.n, (uint64_t)P.Kp * 2, 64, 128,
                          CU_TENSOR_MAP_SWIZZLE_128B));
   YG_CHECK(tck::make_map(&mAs, P.side, 16, P.n, 32, 16, 128, CU_TENSOR_MAP_SWIZZLE_32B));
   YG_CHECK(tck::make_map(&mB, cpk, P.Kp, ncl, (uint64_t)P.Kp * 2, 64, (uint32_t)N,
                          CU_TENSOR_MAP_SWIZZLE_128B));
   YG_CHECK(tck::make_map(&mBs, cside, 16, ncl, 32, 16, (uint32_t)N, CU_TENSOR_MAP_SWIZZLE_32B));
+  if (csm) YG_CHECK(make_map_f32(&mC, C, d, ncl, (uint32_t)d, (uint32_t)N));
+  else mC = mBs;
   int dev = 0, nsm = 0;
   YG_CUDA(cudaGetDevice(&dev));
   YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -483,10 +604,12 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   p.units = units; p.nunits = nunits; p.d = d; p.k = k; p.N = N; p.Kp = P.Kp; p.f16 = P.f16;
   p.v = v; p.C = C; p.xn64 = P.xn64; p.xres = P.xres; p.cs = cstats; p.active = active;
   p.assign = assign; p.dis = dis; p.acc = acc; p.counts = counts; p.shift = shift; p.err = err;
+  p.acc_global = acc_global;
+  p.csm = csm;
   p.wait_ns = wait_limit_ns();
   p.withhold = test_withhold_loads() ? 1 : 0;
   const unsigned g = (unsigned)(nunits < nsm ? nunits : nsm);
-  km_tc_kernel<<<g, NT, lay.total, st>>>(mA, mAs, mB, mBs, S, p);
+  kern<<<g, NT, lay.total, st>>>(mA, mAs, mB, mBs, mC, S, p);
   YG_LAUNCH_CHECK();
   return OK;
 }

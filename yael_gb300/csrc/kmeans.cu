@@ -37,7 +37,7 @@ enum KmSlot : int {
   KS_AKEYS, KS_AKEYS2, KS_AVALS, KS_AVALS2, KS_AOFFS, KS_ATMP, KS_ASORT,
   // the small-k tensor-core assignment
   KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
-  KS_TCERR,
+  KS_TCERR, KS_PRIOR,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -313,7 +313,7 @@ struct Engine {
   int setup_tc(float hmax) {
     tc = (prec == PREC_BF16 || prec == PREC_FP16) && !alt_mode() && km_tc_supported(d, k, v, C);
     if (!tc) return OK;
-    tc_fuse = km_tc_fuses(d, k);
+    tc_fuse = true;  // the sums come with the assignment (shared memory or global atomics)
     Workspace &ws = ctx->ws;
     const int ni = (int)in.size();
     const long ncl = (long)ni * k;
@@ -404,6 +404,13 @@ struct Engine {
   // centroids) does better with the in-line band passes.
   KnnJob pend;
   long last_rejected = -1;  // rejected points of the previous assignment
+  // From the second iteration of a run on, the chosen form's k-NN assignment
+  // starts from each point's distance to its previous centroid's new
+  // position, an upper bound of its nearest distance: a THRESH pass with those
+  // thresholds finds every possible winner with the cheapest selection, and no
+  // sample pass.  (The plain FP32 path keeps its list pass: its CUDA-core
+  // scan does not gain from the cheaper selection.)
+  bool have_prev = false;
 
   void count_assign(const KnnJob &job) {
     last_rejected = (long)job.n_band + job.n_fallback;
@@ -453,7 +460,14 @@ struct Engine {
       }();
       job.defer = defer_mode == 1 ||
                   (defer_mode != 0 && last_rejected >= 0 && 100 * last_rejected < (long)job.nq);
+      if (have_prev && job.prec != PREC_FP32) {
+        float *kth;
+        YG_CHECK(ws_get(ctx->ws, KS_PRIOR, (size_t)in[0].n, &kth));
+        YG_CHECK(km_prior_bound(job.q, d, in[0].n, job.out_idx, C, kth, st));
+        job.prior_kth = kth;
+      }
       YG_CHECK(knn_device(job, ctx, st));
+      have_prev = true;
       if (job.pending) {
         // the update queued next overwrites C: the rejected points are settled
         // against a copy of this iteration's centroids
@@ -804,6 +818,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
     }
     x.core = rand_r(&x.seed);
     x.tot_re = 0; x.iters = 0; x.ret = 0; x.done = false;
+    E.have_prev = false;
     x.qerr = HUGE_VAL; x.qerr_old = HUGE_VAL;
     YG_CHECK(E.set_active());
     while (!E.all_done()) YG_CHECK(E.iterate());
@@ -827,6 +842,12 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
       bnassign.assign(E.hcounts.begin(), E.hcounts.begin() + k);
     }
   }
+  if (trace_enabled())
+    fprintf(stderr,
+            "[yael_gpu] kmeans n=%d k=%d d=%d iterations=%ld assign=%.3fms update=%.3fms "
+            "graphs(assign=%d update=%d failed=%d) tc=%d fused=%d prec=%d\n",
+            n, k, d, iter_tot, E.ms_assign, E.ms_update, E.g_assign != nullptr,
+            E.g_update != nullptr, (int)E.graphs_failed, (int)E.tc, (int)E.tc_fuse, E.prec_used);
   if (verbose && core_ret >= 0) {
     printf("Total number of iterations: %ld\n", iter_tot);
     // unbalanced factor of the last iteration's counts (yael/vector.c:2301-2314)

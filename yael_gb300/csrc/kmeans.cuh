@@ -87,8 +87,10 @@ bool km_tc_supported(int d, int k, const float *v, const float *C);
 // are packed here (cpk, cside: [ninst*k][Kp] and [ninst*k][16], cstats reset
 // and filled).  With acc != null the exact fixed-point sums of the points and
 // the counts are added to acc[g][d] / counts[g] (g = inst*k + j; both zeroed
-// by the caller), accumulated in shared memory first (needs k*d*8 bytes of it:
-// km_tc_fuses).  Units of instances with active[inst] == 0 are skipped.
+// by the caller), accumulated in shared memory first when an instance's
+// k*d*8 bytes fit (km_tc_fuses), else added to them directly (integer
+// atomics: the result does not depend on their order).  Units of instances
+// with active[inst] == 0 are skipped.
 bool km_tc_fuses(int d, int k);
 int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const float *v, int d,
                  const float *C, int ninst, int k, void *cpk, void *cside, float *cres,
@@ -132,6 +134,12 @@ int km_update(const long *perm, const long *total, long nmax, const int *assign,
               const int *pinst, const int *counts, const float *v, int d, long ncl, int k,
               const int *shift, const unsigned char *active, long long *acc, float *C,
               cudaStream_t st);
+
+// kth[p] >= the exact squared distance from point p to centroid assign[p]
+// (FP32 direct differences widened by their rounding bound; +inf for -1): an
+// upper bound of p's nearest distance for the next assignment
+int km_prior_bound(const float *v, int d, long n, const int *assign, const float *C, float *kth,
+                   cudaStream_t st);
 
 // the readout of km_update alone, for sums accumulated elsewhere (km_tc_assign)
 int km_finalize(const long long *acc, const int *counts, long ncl, int d, int k,

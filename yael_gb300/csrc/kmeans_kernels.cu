@@ -868,6 +868,42 @@ int km_update(const long *perm, const long *total, long nmax, const int *assign,
   return OK;
 }
 
+// a warp per point: FP32 direct differences to centroid assign[p] (any
+// summation order), widened by their rounding bound (d + 4) 2^-24 relative,
+// so that the result is >= the exact distance; +inf without a centroid
+__global__ void prior_bound_kernel(const float *__restrict__ v, int d, long n,
+                                   const int *__restrict__ assign, const float *__restrict__ C,
+                                   float *kth) {
+  const long p = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (p >= n) return;
+  const int j = assign[p];
+  if (j < 0) {
+    if (lane == 0) kth[p] = INFINITY;
+    return;
+  }
+  const float *x = v + p * d, *c = C + (long)j * d;
+  float s = 0.f;
+  for (int i = lane; i < d; i += 32) {
+    const float t = __ldg(x + i) - __ldg(c + i);
+    s = fmaf(t, t, s);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const float w = (float)(d + 4) * 5.9604645e-08f * 1.01f;
+    kth[p] = isfinite(s) ? __fmul_ru(s, 1.f + w) + 1e-30f : INFINITY;
+  }
+}
+
+int km_prior_bound(const float *v, int d, long n, const int *assign, const float *C, float *kth,
+                   cudaStream_t st) {
+  if (n <= 0) return OK;
+  prior_bound_kernel<<<(unsigned)ceil_div(n * 32, 256), 256, 0, st>>>(v, d, n, assign, C, kth);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
 int km_finalize(const long long *acc, const int *counts, long ncl, int d, int k,
                 const int *shift, const unsigned char *active, float *C, cudaStream_t st) {
   finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(acc, counts, ncl, d, k, shift,

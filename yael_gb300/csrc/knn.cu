@@ -102,6 +102,11 @@ __global__ void gather_kth_kernel(const float *in_kth, const float *out_kth, con
 // second entry sits inside the error band), lists of eight 0.2-16%, and the
 // band pass then costs a few ms instead of ~100; the longer lists slow the
 // distance pass by 1.35x, a net 1.5x per iteration (369 -> 243 ms).
+// candidate slots per THRESH region of a pass with prior thresholds: the
+// nearest centroid and the few others within the error band of the bound,
+// as many as the short re-rank's 32 slots hold (two regions per chunk)
+int prior_cap(int nchunk) { return imax(8, 32 / (2 * nchunk)); }
+
 int list_length(int k, int exact, int nb) {
   (void)nb;
   if (k == 1) return 8;
@@ -292,6 +297,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   YG_CHECK(ws_get(ws, WS_KTH, nq, &kth));
   ra.kth_out = kth;
   const bool band = job.band_kth != nullptr;
+  const bool prior = !band && job.prior_kth != nullptr;
 
   const bool timed = job.timing || trace_enabled();
   const int tile_n = bf16 ? TC_TILE_N : SIMT_TILE_N;
@@ -311,7 +317,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
   int pticket[BaseUpload::kMaxParts];
   float part_ms[BaseUpload::kMaxParts] = {};
   std::unique_ptr<PassTimer> ptm[BaseUpload::kMaxParts];
-  if (up && !band && c_needed <= 16) {
+  if (up && !band && !prior && c_needed <= 16) {
     // ---- TOPC, base arriving part by part
     sel.mode = SCAN_TOPC;
     sel.C = pow2_at_least(c_needed);
@@ -326,7 +332,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     YG_CHECK(scan_parts(job, *up, *bops, dsmall, tcq, nq, sel, pnch, ptpc, pfirst, ptm, st));
     tm_scan->stop(st);
     job.scan_launches += up->nparts;
-  } else if (!band && c_needed <= 16) {
+  } else if (!band && !prior && c_needed <= 16) {
     // ---- TOPC over the full base (register lists)
     sel.mode = SCAN_TOPC;
     sel.C = pow2_at_least(c_needed);
@@ -363,10 +369,11 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       for (int i = 0; i < up->nparts; i++)
         if (pticket[i] >= 0) ptm[i].reset(new PassTimer(true, st, &part_ms[i], false));
     } else {
-      sel.nchunk = band ? 1
-                        : tune_chunks(TuneKey{1, job.prec, nqt, ntb, 0},
-                                      choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4),
-                                      1024, ctx->num_sms * ctas_per_sm, &scan_ticket);
+      sel.nchunk = band    ? 1
+                   : prior ? choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4)
+                           : tune_chunks(TuneKey{1, job.prec, nqt, ntb, 0},
+                                         choose_chunks(nqt, ntb, ctx->num_sms, ctas_per_sm, 4),
+                                         1024, ctx->num_sms * ctas_per_sm, &scan_ticket);
       sel.tiles_per_chunk = (int)ceil_div(ntb, sel.nchunk);
       sel.nchunk = (int)ceil_div(ntb, sel.tiles_per_chunk);
     }
@@ -388,6 +395,10 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
       sel.tiles_per_chunk = L.tiles_per_chunk;
       sel.cap = L.cap;
       YG_CHECK(band_thresholds(nq, job.metric, job.band_kth, qn64, eps, thr, st));
+    } else if (prior) {
+      // every row whose exact distance can be <= the known bound
+      sel.cap = prior_cap(sel.nchunk);
+      YG_CHECK(band_thresholds(nq, job.metric, job.prior_kth, qn64, eps, thr, st));
     } else if (nb <= kMaxCandidates || sns < 4 * c) {
       // every base row is a candidate; a region holds at most its share of the chunk
       sel.cap = pow2_at_least(imax(1, sel.tiles_per_chunk * tile_n / sel.halves));
@@ -488,7 +499,8 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     fprintf(stderr,
             "[yael_gpu] knn level=%d prec=%d pass=%s nq=%d nb=%d d=%d k=%d chunks=%d "
             "scan=%.3fms sample=%.3fms rerank=%.3fms rejected=%d\n",
-            job.level, job.prec, band ? "band" : (sel.mode == SCAN_TOPC ? "topc" : "thresh"), nq,
+            job.level, job.prec,
+            band ? "band" : prior ? "prior" : (sel.mode == SCAN_TOPC ? "topc" : "thresh"), nq,
             nb, d, k, sel.nchunk, job.ms_scan, job.ms_sample, job.ms_rerank, nf);
   if (nf == 0) return OK;
   // A regular pass's rejections go to a band pass at the same precision: its
@@ -515,8 +527,8 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
                                                                             nf, d, cq);
     YG_LAUNCH_CHECK();
     YG_CHECK(ws_get(ws, base + 4, nf, &ckth));
-    gather_kth_kernel<<<(unsigned)ceil_div(nf, 256), 256, 0, st>>>(job.band_kth, kth, map, nf,
-                                                                  ckth);
+    gather_kth_kernel<<<(unsigned)ceil_div(nf, 256), 256, 0, st>>>(
+        job.band_kth ? job.band_kth : job.prior_kth, kth, map, nf, ckth);
     YG_LAUNCH_CHECK();
     if (to_split && !bops->has_split) {
       float *bn32s;
@@ -529,6 +541,7 @@ int knn_batch(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *bo
     KnnJob sub = job;
     sub.prec = to_split ? PREC_BF16X3 : job.prec;
     sub.band_kth = ckth;
+    sub.prior_kth = nullptr;
     sub.level = job.level + 1;
     sub.nq = nf;
     sub.q = cq;
@@ -578,6 +591,11 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
                        .bytes_per_query() *
                    (size_t)qbatch > budget)
       qbatch = (qbatch + 1) / 2;
+  } else if (job.prior_kth) {
+    const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
+    const int nch = choose_chunks(nqt, ntb, ctx->num_sms, 1, 4);
+    const size_t per_query = (size_t)nch * 2 * (prior_cap(nch) * 8 + 4) + 64;
+    qbatch = (int)std::min<size_t>((size_t)nq, std::max<size_t>(256, budget / per_query));
   } else {
     const int cn = list_length(k, bexact, nb);
     const int nqt = (int)ceil_div(nq, tile_m), ntb = (int)ceil_div(nb, tile_n);
@@ -601,6 +619,7 @@ int knn_batches(KnnJob &job, Ctx *ctx, cudaStream_t st, Small *dsmall, BaseOps *
     sub.out_idx = job.out_idx + (long)q0 * k;
     sub.out_dis = job.out_dis + (long)q0 * k;
     if (job.band_kth) sub.band_kth = job.band_kth + q0;
+    if (job.prior_kth) sub.prior_kth = job.prior_kth + q0;
     sub.n_fallback = sub.n_band = sub.n_second = 0;
     sub.ms_scan = sub.ms_sample = sub.ms_rerank = sub.ms_second = 0;
     sub.scan_launches = 0;

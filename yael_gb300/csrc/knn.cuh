@@ -33,6 +33,12 @@ struct KnnJob {
   // band pass (internal): when set, a THRESH pass with per-query thresholds
   // from band_kth[q], an upper bound of the query's k-th exact distance
   const float *band_kth = nullptr;
+  // Known before the pass (the k-means assignment from its second iteration
+  // on): per query an upper bound of its k-th exact distance, here its exact
+  // distance to its previous centroid, which has moved.  The pass is then a
+  // THRESH pass with thresholds from these bounds (no sample pass; short
+  // candidate regions, whose overflow sends the query to the band pass).
+  const float *prior_kth = nullptr;
   int level = 0;  // nesting depth of the later-chance passes (workspace slots)
   BaseUpload *upload = nullptr;  // base arriving part by part (BF16 pass only)
   // CUDA-event timing of the passes (optional)

@@ -6,6 +6,7 @@
 #include <atomic>
 #include <map>
 #include <mutex>
+#include <string>
 #include <utility>
 
 #include "common.cuh"
@@ -53,7 +54,7 @@ int Workspace::get(int slot, size_t bytes, void **out) {
     }
     size_t n = bytes + bytes / 8;  // headroom so slowly growing sizes do not thrash
     n = (n + 255) & ~(size_t)255;
-    cudaError_t e = cudaMalloc(&b.p, n);
+    cudaError_t e = test_fail_alloc() ? cudaErrorMemoryAllocation : cudaMalloc(&b.p, n);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
       b.p = nullptr;
@@ -145,6 +146,24 @@ int ensure_smem(const void *func, size_t bytes) {
   YG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   cur = bytes;
   return OK;
+}
+
+// YAEL_GPU_TEST_FAIL_ALLOC=n (n >= 1, read at every workspace growth): the
+// n-th growth of the calling thread counted from the moment the variable
+// changed value fails as an out-of-memory cudaMalloc would (the call is not
+// made).  A host-side test hook for the E_NOMEM path.
+static thread_local long t_fail_seen = 0;
+static thread_local std::string t_fail_env;
+bool test_fail_alloc() {
+  const char *s = getenv("YAEL_GPU_TEST_FAIL_ALLOC");
+  const std::string cur = s ? s : "";
+  if (cur != t_fail_env) {
+    t_fail_env = cur;
+    t_fail_seen = 0;
+  }
+  const long n = cur.empty() ? 0 : atol(cur.c_str());
+  if (n <= 0) return false;
+  return ++t_fail_seen == n;
 }
 
 static thread_local unsigned long long t_wait_ns = 0;

@@ -388,7 +388,8 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
     return G == 32 ? b : (b >> gbase) & ((1u << G) - 1u);
   };
   const ScanSel &s = a.sel;
-  const int M = s.nchunk * s.C, k = a.k, d = a.d;
+  const bool thresh = s.mode == SCAN_THRESH;
+  const int k = a.k, d = a.d;
   const bool L2 = a.metric == METRIC_L2;
   const double qn = L2 ? a.qn64[q] : 0.0;
   const float eps = a.eps ? a.eps[q] : 0.f;
@@ -397,26 +398,44 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
 
   unsigned long long key = ~0ull, tkey = ~0ull;
   int id = 0x7fffffff;
-  if (gl < M) {
-    const int ch = gl / s.C, sl = gl - ch * s.C;
-    const long o = ((long)ch * a.nq + q) * s.C + sl;
-    const int j = s.topi[o];
-    if (j >= 0) {
-      const float v = s.topv[o];
-      const float av = L2 ? (float)((double)v + qn) : v;
-      key = f2ord(av);
-      id = j;
-      if (sl == s.C - 1) tkey = ((unsigned long long)f2ord(av) << 32) | (unsigned)j;
+  bool overflow = false;
+  if (thresh) {
+    // THRESH regions of cap slots (regions * cap <= G): every row with
+    // approx <= thr[q]; a region that had more hits than slots fails the query
+    if (gl < s.nregion() * s.cap) {
+      const int r = gl / s.cap, sl = gl - r * s.cap;
+      const int cnt = s.cnt[(long)r * a.nq + q];
+      overflow = cnt > s.cap;
+      if (sl < cnt && sl < s.cap) {
+        const long o = ((long)r * a.nq + q) * s.cap + sl;
+        const float v = s.candv[o];
+        key = f2ord(L2 ? (float)((double)v + qn) : v);
+        id = s.candi[o];
+      }
+    }
+  } else {
+    const int M = s.nchunk * s.C;
+    if (gl < M) {
+      const int ch = gl / s.C, sl = gl - ch * s.C;
+      const long o = ((long)ch * a.nq + q) * s.C + sl;
+      const int j = s.topi[o];
+      if (j >= 0) {
+        const float v = s.topv[o];
+        const float av = L2 ? (float)((double)v + qn) : v;
+        key = f2ord(av);
+        id = j;
+        if (sl == s.C - 1) tkey = ((unsigned long long)f2ord(av) << 32) | (unsigned)j;
+      }
+    }
+    // boundary: smallest (value, id) that closes a full chunk list
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(gm, tkey, o);
+      tkey = t < tkey ? t : tkey;
     }
   }
-  // boundary: smallest (value, id) that closes a full chunk list
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(gm, tkey, o);
-    tkey = t < tkey ? t : tkey;
-  }
   const int nvalid = __popc(gballot(id != 0x7fffffff));
-  bool ok = nvalid >= k;
+  bool ok = nvalid >= k && gballot(overflow) == 0u;
   float kth_hi = INFINITY;  // upper bound of the k-th exact distance, when found
   if (ok) {
     if (a.n_cand) {  // one atomic per set of converged lanes, not per query
@@ -426,7 +445,8 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
     }
     group_sort<G>(key, id, gm);
     if (ex) {
-      if (tkey != ~0ull) {
+      // THRESH: non-candidates are above thr, so the sorted prefix is the answer
+      if (!thresh && tkey != ~0ull) {
         const unsigned long long kk = __shfl_sync(gm, key, k - 1, G);
         const int ik = __shfl_sync(gm, id, k - 1, G);
         const unsigned long long tk = tkey >> 32;
@@ -481,8 +501,15 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
           a.out_dis[(long)q * k + gl] = ord2f((unsigned)key);
         }
       }
-      const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
-      ok = ek_hi < bound - (double)eps - 4e-7 * fabs(bound);
+      if (thresh) {
+        // every non-candidate has approx > thr, so exact > thr + ||q||^2 - eps
+        const float t = s.thr[q];
+        const double bound = L2 ? (double)t + qn : (double)t;
+        ok = ek_hi <= bound - (double)eps - 4e-7 * fabs(bound);
+      } else {
+        const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
+        ok = ek_hi < bound - (double)eps - 4e-7 * fabs(bound);
+      }
       kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
     }
   }
@@ -768,8 +795,12 @@ __global__ void __launch_bounds__(RT) fb_select_kernel(const int *qlist, int q0,
 
 int rerank(const RerankArgs &a, cudaStream_t st) {
   if (a.nq <= 0) return OK;
-  if (a.sel.mode == SCAN_TOPC && a.sel.nchunk * a.sel.C <= 32) {
-    const int M = a.sel.nchunk * a.sel.C;
+  // short candidate sets: a group of 8 to 32 lanes per query
+  const bool small_topc = a.sel.mode == SCAN_TOPC && a.sel.nchunk * a.sel.C <= 32;
+  const bool small_thresh = a.sel.mode == SCAN_THRESH && !a.gpairs && a.sel.cap > 0 &&
+                            a.sel.nregion() * a.sel.cap <= 32;
+  if (small_topc || small_thresh) {
+    const int M = small_topc ? a.sel.nchunk * a.sel.C : a.sel.nregion() * a.sel.cap;
     if (M <= 8)
       rerank_small_kernel<8><<<(unsigned)ceil_div(a.nq, 32), 256, 0, st>>>(a);
     else if (M <= 16)
