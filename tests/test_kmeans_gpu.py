@@ -151,11 +151,15 @@ def test_kmeans_tensor_core_assignment_ties(prec, k):
     same(g, oracle_kmeans(v, k, 8, QUIET, 5, 1))
 
 
-@pytest.mark.parametrize("d,k", [(4, 7), (20, 33), (96, 32), (128, 200), (256, 16)])
+@pytest.mark.parametrize("d,k", [(4, 7), (20, 33), (96, 32), (128, 200), (256, 16), (128, 256),
+                                 (256, 256)])
 def test_kmeans_tensor_core_assignment_shapes(d, k):
     """Dimensions from 4 to 256 (one to four 64-column K blocks, partial
     blocks zero padded) and k not a multiple of 32 (masked accumulator
-    columns), bf16 operands (values far outside fp16's range)."""
+    columns), bf16 operands (values far outside fp16's range); the shared
+    memory layout gives up staging and shared-memory sums where they do not
+    fit, and d = 256 with k = 256 (no room for two stages) takes the k-NN
+    assignment instead."""
     rng = np.random.default_rng(d * 100 + k)
     v = (rng.standard_normal((6000, d)) * 300).astype(np.float32)
     g = gpu_kmeans(v, k, 5, QUIET, 11, 1, "bf16")

@@ -550,8 +550,13 @@ int make_map_f32(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t rows, 
 }  // namespace
 
 bool km_tc_supported(int d, int k, const float *v, const float *C) {
-  return d >= 4 && d % 4 == 0 && d <= 256 && k >= 1 && k <= kTcMaxK &&
-         (reinterpret_cast<uintptr_t>(v) & 15) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0;
+  if (!(d >= 4 && d % 4 == 0 && d <= 256 && k >= 1 && k <= kTcMaxK &&
+        (reinterpret_cast<uintptr_t>(v) & 15) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0))
+    return false;
+  // a ring of two stages beside the centroid tile, without staging or
+  // shared-memory sums, must fit (not so for d > 128 with k > 224)
+  const int Kp = ((d + 63) / 64) * 64, N = ((k + 31) / 32) * 32;
+  return kmtc::make_lay(Kp / 64, N, 2, 0, k, d, 0).total <= 227 * 1024;
 }
 
 bool km_tc_fuses(int d, int k) { return (size_t)k * d * 8 <= 48 * 1024; }
@@ -573,13 +578,22 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   YG_CHECK(prep_rows(C, d, (int)ncl, d, 1.f, nullptr, nullptr, nullptr, cres,
                      (__nv_bfloat16 *)cpk, P.Kp, (__nv_bfloat16 *)cside, 1, cstats, st, 8, P.f16));
   // the sums go through shared memory when an instance's k x d fit, else
-  // straight to the global accumulators
-  const int acc_global = acc != nullptr && !km_tc_fuses(d, k);
-  const int fuse = acc != nullptr && !acc_global;
-  // the instance's FP32 centroid rows are staged when they are few
-  const int csm = (size_t)N * d * 4 <= 32 * 1024;
+  // straight to the global accumulators; the instance's FP32 centroid rows
+  // are staged when they are few.  Both give way, staging first, when a ring
+  // of two stages would not fit beside them.
+  int acc_global = acc != nullptr && !km_tc_fuses(d, k);
+  int fuse = acc != nullptr && !acc_global;
+  int csm = (size_t)N * d * 4 <= 32 * 1024;
+  auto fits = [&](int S_) {
+    return make_lay(nkb, N, S_, fuse, k, d, csm).total <= 227 * 1024;
+  };
+  if (!fits(2)) csm = 0;
+  if (!fits(2) && fuse) {
+    fuse = 0;
+    acc_global = 1;
+  }
   int S = 6;
-  while (S > 2 && make_lay(nkb, N, S, fuse, k, d, csm).total > 227 * 1024) S--;
+  while (S > 2 && !fits(S)) S--;
   const Lay lay = make_lay(nkb, N, S, fuse, k, d, csm);
   if (lay.total > 227 * 1024) {
     set_error(E_UNSUPPORTED, "km_tc_assign: shared memory %zu too large (d=%d k=%d)", lay.total,
