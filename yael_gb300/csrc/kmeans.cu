@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include <algorithm>
 #include <memory>
@@ -130,6 +131,12 @@ int fixed_shift(long n, float maxabs) {
 }
 
 // ---- the batched Lloyd engine --------------------------------------------
+
+double wall_ms() {
+  timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
 
 // statistics of the calling thread's last kmeans / hkm call (yael_gpu_last_stats)
 thread_local yael_gpu_call_stats g_last_stats = {};
@@ -490,6 +497,7 @@ struct Engine {
   int iterate() {
     const int ni = (int)in.size();
     const long ncl = (long)ni * k;
+    const double t_host0 = trace_enabled() ? wall_ms() : 0.0;
     for (auto &x : in)
       if (!x.done) {
         x.iters++;
@@ -607,6 +615,9 @@ struct Engine {
     cudaEventElapsedTime(&b, e1, e2);
     ms_assign += a;
     ms_update += b;
+    if (trace_enabled())
+      fprintf(stderr, "[yael_gpu] kmeans iteration %ld: assign %.3f ms, update %.3f ms (events), "
+              "%.3f ms on the host clock\n", engine_iters, a, b, wall_ms() - t_host0);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaEventDestroy(e2);
