@@ -22,7 +22,8 @@ CLIS = [(os.path.join(HERE, "cli", name + ".cpp"), os.path.join(HERE, "bin", nam
         for name in ("yael_knn", "yael_kmeans")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-ffp-contract=off",
               "-Xcompiler", "-fvisibility=default", "--expt-relaxed-constexpr"]
 
 

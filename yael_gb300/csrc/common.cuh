@@ -101,6 +101,16 @@ int ctx_get(Ctx **out);
 // bf16 rate), for data fp16 can hold (|x| < 16384, ||x||^2 < 2^15 for base
 // rows); rows it cannot hold get an infinite error bound and are settled by
 // the later passes
+// s + t * t and s + a * b with the product rounded before the sum, as C
+// without floating-point contraction computes them (the oracle is built with
+// -ffp-contract=off): FP64 distances agree with it bit for bit on any host
+__device__ __forceinline__ double add_sq64(double s, double t) {
+  return __dadd_rn(s, __dmul_rn(t, t));
+}
+__device__ __forceinline__ double add_mul64(double s, double a, double b) {
+  return __dadd_rn(s, __dmul_rn(a, b));
+}
+
 enum Precision : int { PREC_FP32 = 0, PREC_BF16 = 1, PREC_BF16X3 = 2, PREC_FP16 = 3 };
 int default_precision();  // from YAEL_GPU_PRECISION (fp32 | bf16 | bf16x3 | fp16), default fp32
 // p is one of the YAEL_GPU_PREC_* values a caller may pass explicitly

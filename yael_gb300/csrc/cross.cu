@@ -164,7 +164,7 @@ __global__ void reorder_kernel(int nq, int nb, int d, int k, const float *b, con
     double s = 0;
     for (int c = 0; c < d; c++) {
       const double t = (double)qv[c] - (double)bv[c];
-      s += t * t;
+      s = add_sq64(s, t);
     }
     key[i] = s;
     pos[i] = i;
@@ -193,7 +193,7 @@ __global__ void recompute_kernel(int nq, int nb, int d, int k, const float *b,
     double s = 0;
     for (int c = 0; c < d; c++) {
       const double t = (double)v[(long)q * d + c] - (double)b[j * d + c];
-      s += t * t;
+      s = add_sq64(s, t);
     }
     dis[(long)q * k + i] = (float)s;
   }

@@ -38,26 +38,30 @@ namespace kmtc {
 using namespace ptx;
 
 constexpr int NT = 320;
-constexpr int BMAX = 8;  // band entries kept per point; more: every centroid is re-checked
+constexpr int BW = 9;  // band mask words per point (k <= 256: 8 used; odd: no bank conflicts)
 constexpr int A_BLK = 128 * 128;  // 128 rows x 64 16-bit columns
 constexpr int A_SIDE = 128 * 32;  // 128 rows x 16 16-bit columns
 
 struct Lay {
-  int nkb, N, S, fuse, csm;
-  size_t stage_bytes, b_off, bside_off, cf_off, band_off, acc_off, cnt_off, bar_off, total;
+  int nkb, N, S, fuse, csm, xs;
+  size_t stage_bytes, x_off, b_off, bside_off, cf_off, band_off, lst_off, acc_off, cnt_off, bar_off,
+      total;
 };
 
+// xs: every stage also holds the tile's FP32 point rows (128 x d floats)
 __host__ __device__ inline Lay make_lay(int nkb, int N, int S, int fuse, int k, int d,
-                                       int csm) {
+                                       int csm, int xs) {
   Lay L;
-  L.nkb = nkb; L.N = N; L.S = S; L.fuse = fuse; L.csm = csm;
+  L.nkb = nkb; L.N = N; L.S = S; L.fuse = fuse; L.csm = csm; L.xs = xs;
   size_t off = 0;
-  L.stage_bytes = (size_t)nkb * A_BLK + A_SIDE;  // a multiple of 1024
+  L.x_off = (size_t)nkb * A_BLK + A_SIDE;
+  L.stage_bytes = L.x_off + (xs ? (((size_t)128 * d * 4 + 1023) & ~(size_t)1023) : 0);
   off += (size_t)S * L.stage_bytes;
   L.b_off = off;     off += (size_t)nkb * N * 128;  // N % 32 == 0: 1024-aligned blocks
   L.bside_off = off; off += (size_t)N * 32;
   L.cf_off = off;    off += csm ? (size_t)N * d * 4 : 0;  // FP32 centroid rows (d % 4 == 0)
-  L.band_off = off;  off += (size_t)2 * 128 * (BMAX + 1) * 4;
+  L.band_off = off;  off += (size_t)2 * 128 * BW * 4;
+  L.lst_off = off;   off += (size_t)256 * 4;  // the tile's moves: new and old centroids
   off = (off + 15) & ~(size_t)15;
   L.acc_off = off;   off += fuse ? (size_t)k * d * 8 : 0;
   L.cnt_off = off;   off += fuse ? (size_t)k * 4 : 0;
@@ -85,6 +89,9 @@ struct Params {
   int acc_global;              // sums added straight to acc / counts (k * d too large
                                // for shared memory)
   int csm;                     // the instance's FP32 centroid rows staged in shared memory
+  int xs;                      // the tile's FP32 point rows staged with it
+  int centered;                // the packed rows are translated by the instance's mean
+  int delta;                   // the sums hold the previous assignment's: only moves are added
   unsigned long long wait_ns;  // bound of every wait (0: kWaitLimitNs)
   int withhold;                // test switch: the producer issues no load
 };
@@ -95,141 +102,230 @@ __device__ __forceinline__ float warp_sum(float x) {
   return x;
 }
 
-constexpr int G = 8;  // rows a warp of the epilogue takes at once in phase B
-
-// a float4 of a centroid row: shared memory (staged) or global (read-only path)
-__device__ __forceinline__ float4 cload(const float *p, bool sm) {
-  return sm ? *reinterpret_cast<const float4 *>(p) : __ldg(reinterpret_cast<const float4 *>(p));
+// fixed_of without branches (the same value): integral x 2^S by a shift,
+// otherwise rounded to nearest even from the 24-bit mantissa
+__device__ __forceinline__ long long fixed_of_nb(float x, int S) {
+  const unsigned u = __float_as_uint(x);
+  const int ex = (int)((u >> 23) & 0xffu);
+  const unsigned m = (u & 0x7fffffu) | (ex ? 0x800000u : 0u);
+  const int sh = (ex ? ex - 150 : -149) + S;
+  const int rs = max(1, min(-sh, 31));  // the rounding form's shift (unused for sh >= 0)
+  const unsigned q = rs >= 25 ? 0u : m >> rs;
+  const unsigned rem = rs >= 25 ? m : m & ((1u << rs) - 1u);
+  const unsigned half = rs >= 25 ? 0xffffffffu : 1u << (rs - 1);
+  const unsigned rq = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+  const long long r = sh >= 0 ? (long long)((unsigned long long)m << min(sh, 63)) : (long long)rq;
+  return ex == 0xff ? 0 : (u >> 31) ? -r : r;
 }
 
-template <int ND4>
-__device__ __forceinline__ float row_dist(const float4 (&x)[ND4], const float4 (&c)[ND4],
-                                          int lane, int d4) {
-  float s = 0.f;
-#pragma unroll
-  for (int q = 0; q < ND4; q++) {
-    if (lane + 32 * q < d4) {
-      float t = x[q].x - c[q].x;
-      s = fmaf(t, t, s);
-      t = x[q].y - c[q].y;
-      s = fmaf(t, t, s);
-      t = x[q].z - c[q].z;
-      s = fmaf(t, t, s);
-      t = x[q].w - c[q].w;
-      s = fmaf(t, t, s);
-    }
-  }
-  return warp_sum(s);
-}
-
-// Phase B for one point (the whole warp): the band's exact decision, the
-// outputs, and the point's fixed-point row added to its centroid's sums.  c0
-// holds the first band member's row (or centroid 0's when the band
-// overflowed its list); Ci the instance's centroid rows (staged or global).
-template <int ND4>
-__device__ __forceinline__ void finish_row(const Params &P, const int *bl, int r0, long p,
-                                           const float *Ci, const float4 (&x)[ND4],
-                                           const float4 (&c0)[ND4], int lane, int d, int d4,
-                                           int k, float rho, bool fuse,
-                                           unsigned long long *sacc, int *scnt, int sh,
-                                           int inst) {
-  const int cnt = bl[r0 * (BMAX + 1)];
-  const int nm = cnt > BMAX ? k : cnt;  // an overflowing band: every centroid
+// The exact decision for the sixteen points r0 .. r0 + 15 of a warp, two
+// lanes per point (lanes 2 p and 2 p + 1 for point p; h = lane & 1 takes the
+// float4 columns q = 2 i + h).  The lanes of point p start at i = p and wrap
+// around, so that any eight consecutive lanes (four points, both halves) read
+// eight different bank groups when the rows are a multiple of 128 bytes.  Per band member the FP32 distance
+// sum_c (x_c - c_c)^2 is summed in that order (four partial sums, the two
+// halves added last: deterministic); members come in increasing index order
+// and strict '<' keeps the lower index on equal values; when the best two are
+// closer than their rounding bound the members are compared in FP64 (lowest
+// index on equal values).  Writes assign / dis and, for the fused sums, the
+// point's move: the centroid it joins to toj and the one it leaves to toa
+// (-1 for none; with P.delta == 0 every point joins and none leaves, else
+// only a point whose centroid changed moves).
+// X: the tile's rows (staged, or global from the tile's first point);
+// Ci: the instance's centroid rows (staged or global).
+template <bool CSM>
+__device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *bm, int r0,
+                                               int np, long p0, const float *X, const float *Ci,
+                                               int lane, int d, int k, float rho, int *toj) {
+  const int r = r0 + (lane >> 1), h = lane & 1;
+  const bool val = r < np;
+  // the previous assignment, loaded first (its latency under the distances)
+  const int oa = (P.delta && val && h == 0) ? P.assign[p0 + r] : -1;
+  const int d4 = d >> 2;
+  const int nh = (d4 + 1 - h) >> 1;  // this half's float4 columns
+  // the band: a bit per centroid, words of 32
+  const int nw = (k + 31) >> 5;
+  const unsigned *bw = bm + r * BW;
+  int nm = 0;
+  for (int w = 0; w < nw; w++) nm += val ? __popc(bw[w]) : 0;
+  unsigned mk = val ? bw[0] : 0u;
+  int wi = 0;
+  const int mmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)nm);
+  const float4 *xr = reinterpret_cast<const float4 *>(X + (long)(val ? r : 0) * d);
+  const int i0 = (lane >> 1) % max(nh, 1);  // this lane's first column
   float e1 = INFINITY, e2 = INFINITY;
   int j1 = -1;
-  for (int m = 0; m < nm; m++) {
-    const int j = cnt > BMAX ? m : bl[r0 * (BMAX + 1) + 1 + m];
-    float e;
-    if (m == 0) {
-      e = row_dist<ND4>(x, c0, lane, d4);
-    } else {
-      float4 c[ND4];
-#pragma unroll
-      for (int q = 0; q < ND4; q++) {
-        const int c4 = lane + 32 * q;
-        c[q] = c4 < d4 ? cload(Ci + (long)j * d + 4 * c4, P.csm != 0)
-                       : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      e = row_dist<ND4>(x, c, lane, d4);
+  for (int m = 0; m < mmax; m++) {
+    int j = 0;
+    if (m < nm) {  // the next member (one is left)
+      while (mk == 0u) mk = bw[++wi];
+      j = wi * 32 + __ffs(mk) - 1;
+      mk &= mk - 1;
     }
-    // members come in increasing index order: strict '<' keeps the lower
-    // index on equal values
-    if (e < e1) { e2 = e1; e1 = e; j1 = j; } else if (e < e2) { e2 = e; }
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    if (m < nm) {
+      const float4 *cr = reinterpret_cast<const float4 *>(Ci + (long)j * d);
+#pragma unroll 4
+      for (int t = 0; t < nh; t++) {
+        int i = i0 + t;
+        if (i >= nh) i -= nh;
+        const int q = 2 * i + h;
+        const float4 xv = xr[q];
+        const float4 cv = CSM ? cr[q] : __ldg(cr + q);
+        float u = xv.x - cv.x;
+        s0 = fmaf(u, u, s0);
+        u = xv.y - cv.y;
+        s1 = fmaf(u, u, s1);
+        u = xv.z - cv.z;
+        s2 = fmaf(u, u, s2);
+        u = xv.w - cv.w;
+        s3 = fmaf(u, u, s3);
+      }
+    }
+    float e = (s0 + s1) + (s2 + s3);
+    e += __shfl_xor_sync(0xffffffffu, e, 1);  // the other half (same sum in both lanes)
+    if (m < nm) {
+      if (e < e1) { e2 = e1; e1 = e; j1 = j; } else if (e < e2) { e2 = e; }
+    }
   }
   int oj = -1;
   float od = 1e30f;
-  if (j1 >= 0 && e1 < 1e30f) {
-    oj = j1;
-    od = e1;
-    if (e2 < INFINITY && e2 - e1 <= rho * (e1 + e2)) {
-      // near tie: FP64 over the members, sequential over coordinates, a lane
-      // per member; lowest index on equal values
-      double best = INFINITY;
-      int bj = INT_MAX;
-      for (int m = lane; m < nm; m += 32) {
-        const int j = cnt > BMAX ? m : bl[r0 * (BMAX + 1) + 1 + m];
-        const float *cr = Ci + (long)j * d, *xr = P.v + p * d;
-        double s = 0;
+  if (j1 >= 0 && e1 < 1e30f) { oj = j1; od = e1; }
+  const bool tie = oj >= 0 && e2 < INFINITY && e2 - e1 <= rho * (e1 + e2);
+  if (__any_sync(0xffffffffu, tie)) {
+    // near tie: FP64 over the members, sequential over coordinates, the two
+    // lanes of the point taking alternate members
+    double best = INFINITY;
+    int bj = INT_MAX;
+    if (tie) {
+      const float *xs = X + (long)r * d;
+      unsigned tk = bw[0];
+      int tw = 0;
+      for (int m = 0; m < nm; m++) {
+        while (tk == 0u) tk = bw[++tw];
+        const int j = tw * 32 + __ffs(tk) - 1;
+        tk &= tk - 1;
+        if ((m & 1) != h) continue;
+        const float *cr = Ci + (long)j * d;
+        double sd = 0;
         for (int c = 0; c < d; c++) {
-          const double t = (double)xr[c] - (double)cr[c];
-          s += t * t;
+          const double t = (double)xs[c] - (double)cr[c];
+          sd = add_sq64(sd, t);
         }
-        if (s < best || (s == best && j < bj)) { best = s; bj = j; }
+        if (sd < best || (sd == best && j < bj)) { best = sd; bj = j; }
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oj2 = __shfl_xor_sync(0xffffffffu, bj, o);
-        if (ob < best || (ob == best && oj2 < bj)) { best = ob; bj = oj2; }
-      }
+    }
+    const double ob = __shfl_xor_sync(0xffffffffu, best, 1);
+    const int oj2 = __shfl_xor_sync(0xffffffffu, bj, 1);
+    if (ob < best || (ob == best && oj2 < bj)) { best = ob; bj = oj2; }
+    if (tie) {
       if (bj != INT_MAX && best < 1e30) { oj = bj; od = (float)best; }
       else { oj = -1; od = 1e30f; }
     }
   }
-  if (lane == 0) {
-    P.assign[p] = oj;
-    P.dis[p] = od;
-  }
-  if (fuse && oj >= 0) {
-    // the instance's shared-memory sums, or the global ones directly
-    const long g = (long)inst * k + oj;
-    unsigned long long *row_acc =
-        P.acc_global ? reinterpret_cast<unsigned long long *>(P.acc) + g * d
-                     : sacc + (long)oj * d;
-#pragma unroll
-    for (int q = 0; q < ND4; q++) {
-      const int c4 = lane + 32 * q;
-      if (c4 < d4) {
-        atomicAdd(row_acc + 4 * c4 + 0, (unsigned long long)fixed_of(x[q].x, sh));
-        atomicAdd(row_acc + 4 * c4 + 1, (unsigned long long)fixed_of(x[q].y, sh));
-        atomicAdd(row_acc + 4 * c4 + 2, (unsigned long long)fixed_of(x[q].z, sh));
-        atomicAdd(row_acc + 4 * c4 + 3, (unsigned long long)fixed_of(x[q].w, sh));
-      }
+  if (val && h == 0) {
+    P.assign[p0 + r] = oj;
+    P.dis[p0 + r] = od;
+    if (toj) {
+      toj[r] = oj != oa ? oj : -1;
+      toj[128 + r] = oj != oa ? oa : -1;
     }
-    if (lane == 0) {
-      if (P.acc_global) atomicAdd(P.counts + g, 1);
-      else atomicAdd(scnt + oj, 1);
+  } else if (toj && h == 0) {
+    toj[r] = -1;
+    toj[128 + r] = -1;
+  }
+}
+
+// The fused sums of one tile, after every point's move is in toj (joins:
+// toj[r], leaves: toj[128 + r]): warp ew owns the centroids j = ew (mod 8)
+// and adds (or subtracts) the moving points' fixed-point rows to their sums,
+// lanes over coordinates (lane + 32 i).  An owned centroid's sums are touched
+// by no other warp: plain reads and writes; integer sums, whose result does
+// not depend on the order.  X: the tile's rows.
+template <int N32>
+__device__ __forceinline__ void phase_b_sums_owned(const int *toj, int np, const float *X,
+                                                   int ew, int lane, int d, int sh,
+                                                   unsigned long long *sacc, int *scnt) {
+#pragma unroll 1
+  for (int c = 0; c < 256; c += 32) {
+    const int r = (c & 127) + lane;
+    const int o = r < np ? toj[c + lane] : -1;
+    unsigned m = __ballot_sync(0xffffffffu, o >= 0 && (o & 7) == ew);
+    const bool leave = c >= 128;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const int j = __shfl_sync(0xffffffffu, o, b);
+      const float *xr = X + (long)((c & 127) + b) * d;
+      unsigned long long *row = sacc + (long)j * d;
+      long long v[N32];
+#pragma unroll
+      for (int i = 0; i < N32; i++) {
+        const int col = lane + 32 * i;
+        const long long f = col < d ? fixed_of_nb(xr[col], sh) : 0;
+        v[i] = leave ? -f : f;
+      }
+#pragma unroll
+      for (int i = 0; i < N32; i++) {
+        const int col = lane + 32 * i;
+        if (col < d) row[col] += (unsigned long long)v[i];
+      }
+      if (lane == 0) scnt[j] += leave ? -1 : 1;
+      __syncwarp();
     }
   }
 }
 
-template <int ND4>
+// The sums straight to the global accumulators (k x d too large for shared
+// memory): the warp's sixteen points' moves, one after another, lanes over
+// coordinates; integer atomics, whose result does not depend on their order.
+template <int N32>
+__device__ __forceinline__ void phase_b_sums_global(const Params &P, const int *toj, int r0,
+                                                    int np, const float *X, int lane, int d,
+                                                    int k, int sh, int inst) {
+  // lanes 0-15 the joins of the sixteen points, 16-31 their leaves
+  const int r = r0 + (lane & 15);
+  const int o = r < np ? toj[(lane >> 4) * 128 + r] : -1;
+  unsigned m = __ballot_sync(0xffffffffu, o >= 0);
+  while (m) {
+    const int b = __ffs(m) - 1;
+    m &= m - 1;
+    const int j = __shfl_sync(0xffffffffu, o, b);
+    const bool leave = b >= 16;
+    const float *xr = X + (long)(r0 + (b & 15)) * d;
+    const long g = (long)inst * k + j;
+    unsigned long long *row = reinterpret_cast<unsigned long long *>(P.acc) + g * d;
+#pragma unroll
+    for (int i = 0; i < N32; i++) {
+      const int col = lane + 32 * i;
+      if (col < d) {
+        const long long f = fixed_of_nb(xr[col], sh);
+        atomicAdd(row + col, (unsigned long long)(leave ? -f : f));
+      }
+    }
+    if (lane == 0) atomicAdd(P.counts + g, leave ? -1 : 1);
+  }
+}
+
+template <int ND>
 __global__ void __launch_bounds__(NT, 1)
     km_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAs,
                  const __grid_constant__ CUtensorMap mapB, const __grid_constant__ CUtensorMap mapBs,
                  const __grid_constant__ CUtensorMap mapC, int S, Params P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t *base = reinterpret_cast<uint8_t *>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  // aligned by pointer arithmetic on smem_raw (not through an integer), so
+  // that the compiler keeps these pointers in the shared address space
+  uint8_t *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const int nkb = P.Kp / 64, N = P.N, k = P.k, d = P.d;
   const bool fuse = P.acc != nullptr;
   const bool sfuse = fuse && !P.acc_global;  // shared-memory sums
-  const Lay lay = make_lay(nkb, N, S, sfuse ? 1 : 0, k, d, P.csm);
+  const Lay lay = make_lay(nkb, N, S, sfuse ? 1 : 0, k, d, P.csm, P.xs);
   uint8_t *Stg = base;
   uint8_t *Bs = base + lay.b_off;
   uint8_t *Bside = base + lay.bside_off;
   float *Cf = reinterpret_cast<float *>(base + lay.cf_off);
-  int *band = reinterpret_cast<int *>(base + lay.band_off);  // [2][128][BMAX + 1]
+  unsigned *band = reinterpret_cast<unsigned *>(base + lay.band_off);  // [2][128][BW]
+  int *toj = reinterpret_cast<int *>(base + lay.lst_off);    // the tile's chosen centroids
   unsigned long long *sacc = reinterpret_cast<unsigned long long *>(base + lay.acc_off);
   int *scnt = reinterpret_cast<int *>(base + lay.cnt_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(base + lay.bar_off);
@@ -250,7 +346,8 @@ __global__ void __launch_bounds__(NT, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      // the MMAs' commit, and with staged rows the eight epilogue warps too
+      mbar_init(&empty[s], P.xs ? 9 : 1);
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(&tfull[a], 1);
@@ -284,7 +381,7 @@ __global__ void __launch_bounds__(NT, 1)
       uint32_t issued = 0, last_par = 0;  // per stage: issued at least once, parity of the last
       int cur = -1, nbl = 0;
       bool ok = true;
-      const uint32_t abytes = (uint32_t)(nkb * A_BLK + A_SIDE);
+      const uint32_t abytes0 = (uint32_t)(nkb * A_BLK + A_SIDE);
       const uint32_t bbytes = (uint32_t)(nkb * N * 128 + N * 32 + (P.csm ? N * d * 4 : 0));
       for (int w = w0; w < w1 && ok; w++) {
         const KmTcUnit u = P.units[w];
@@ -313,7 +410,9 @@ __global__ void __launch_bounds__(NT, 1)
         if (++sn == S) { sn = 0; phn ^= 1; }
         if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, wl)) { ok = false; break; }
         uint8_t *sp = Stg + (size_t)s * lay.stage_bytes;
-        mbar_arrive_expect_tx(&full[s], abytes);
+        const uint32_t xbytes = P.xs ? (uint32_t)u.np * d * 4 : 0u;
+        mbar_arrive_expect_tx(&full[s], abytes0 + xbytes);
+        if (P.xs) bulk_load(sp + lay.x_off, P.v + u.p0 * d, xbytes, &full[s]);
         for (int kb = 0; kb < nkb; kb++)
           tma_load_2d(&mapA, &full[s], sp + (size_t)kb * A_BLK, kb * 64, (int)u.p0);
         tma_load_2d(&mapAs, &full[s], sp + (size_t)nkb * A_BLK, 0, (int)u.p0);
@@ -386,7 +485,6 @@ __global__ void __launch_bounds__(NT, 1)
     const float dB = __uint_as_float(P.cs->max_resid_bits);
     const float Kt = (float)(P.Kp + 16);
     const float un = (float)((d + 31) / 32 + 6) * u24;
-    const int d4 = d >> 2;
     int it = 0, cur = -1;
     bool ok = true;
     auto flush = [&](int inst) {
@@ -404,6 +502,8 @@ __global__ void __launch_bounds__(NT, 1)
       asm volatile("bar.sync 1, 256;" ::: "memory");
     };
     int nbl = 0;  // centroid tiles seen (the staged FP32 rows' bfull phases)
+    int esn = 0;  // the ring's stage and phase, followed as the producer does
+    uint32_t ephn = 0;
     for (int w = w0; w < w1 && ok; w++) {
       const KmTcUnit u = P.units[w];
       if (!P.active[u.inst]) continue;
@@ -422,23 +522,41 @@ __global__ void __launch_bounds__(NT, 1)
         cur = u.inst;
       }
       const int a = it & 1;
-      int *bl = band + a * 128 * (BMAX + 1);
+      unsigned *bl = band + a * 128 * BW;
+      const int xs_s = esn;  // the stage this tile came in
+      const uint32_t xs_ph = ephn;
+      if (++esn == S) { esn = 0; ephn ^= 1; }
       if (ew < 4) {
         const uint32_t uu = (uint32_t)(it >> 1);
+        // the point's norm and packing error, loaded before the wait
+        const bool rv = row < u.np;
+        const long p = u.p0 + row;
+        double xn = 0.0;
+        float dq = 0.f;
+        if (rv) {
+          xn = P.xn64[p];
+          dq = P.xres[p];
+        }
         ok = ok && mbar_wait(&tfull[a], uu & 1, abort_flag, wl);
         __syncwarp();
         ok = __all_sync(0xffffffffu, ok);
         if (ok) {
           tc_fence_after();
-          const bool rv = row < u.np;
-          const long p = u.p0 + row;
           float eps = 0.f;
           if (rv) {
-            const float qn = sqrtf(fmaxf((float)P.xn64[p], 0.f)) * (1.f + 1e-5f);
-            const float dq = P.xres[p];
+            const float qn = sqrtf(fmaxf((float)xn, 0.f)) * (1.f + 1e-5f);
             const float dot = dq * (B + dB) + qn * dB;
             const float accb = Kt * 2.f * u24 * (2.f * (qn + dq) * (B + dB) + 1.001f * B * B);
-            eps = (2.f * dot + u24 * B * B + accb + un * (qn * qn + B * B)) * 1.1f + 1e-30f;
+            // the translation: x' = fl(x - mu), c' = fl(c - mu) are off by
+            // at most u ||x'||, u ||c'||, which moves ||x - c||^2 - ||x'||^2
+            // away from ||x' - c'||^2 - ||x'||^2 by at most 2 u (qn + B)^2 (1 + tiny)
+            const float tr = P.centered ? 2.01f * u24 * (qn + B) * (qn + B) : 0.f;
+            // (fp16 norm parts: their sum is within 2^-25 of ||c'||^2)
+            eps = (2.f * dot + u24 * B * B + accb + un * (qn * qn + B * B) + tr +
+                   (P.f16 ? u24 : 0.f)) * 1.1f + 1e-30f;
+            // an infinite residual (a row fp16 cannot hold) times a zero one
+            // is NaN: such a point re-checks every centroid
+            if (!(eps <= 3.0e38f)) eps = INFINITY;
           }
           const uint32_t tc = tmem + lane_base + (uint32_t)(a * N);
           uint32_t r[32];
@@ -451,61 +569,61 @@ __global__ void __launch_bounds__(NT, 1)
               if (c0 + i < k) vmin = fminf(vmin, __uint_as_float(r[i]));
           }
           const float lim = vmin + 2.f * eps;
-          int cnt = 0;
+          // the members: a bit per centroid within 2 eps of the smallest; all
+          // of them without a usable bound, none for no point (or no finite
+          // distance)
+          const bool all = rv && eps == INFINITY, none = !rv || (!all && !(vmin < INFINITY));
           for (int c0 = 0; c0 < N; c0 += 32) {
-            tmem_ld32(tc + (uint32_t)c0, r);
-            tmem_ld_wait(r);
-#pragma unroll
-            for (int i = 0; i < 32; i++) {
-              if (c0 + i < k && __uint_as_float(r[i]) <= lim) {
-                if (cnt < BMAX) bl[row * (BMAX + 1) + 1 + cnt] = c0 + i;
-                cnt++;
-              }
+            if (N > 32) {  // with one chunk r still holds it
+              tmem_ld32(tc + (uint32_t)c0, r);
+              tmem_ld_wait(r);
             }
+            unsigned mk = 0u;
+#pragma unroll
+            for (int i = 0; i < 32; i++)
+              mk |= (c0 + i < k && (all || __uint_as_float(r[i]) <= lim)) ? 1u << i : 0u;
+            bl[row * BW + (c0 >> 5)] = none ? 0u : mk;
           }
           tc_fence_before();
-          bl[row * (BMAX + 1)] = (rv && vmin < INFINITY) ? cnt : 0;
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[a]);
+      }
+      if (P.xs) {
+        // the tile's rows were copied with its packed rows: this wait only
+        // makes the copy visible here (the MMAs already waited for it)
+        ok = ok && mbar_wait(&full[xs_s], xs_ph, abort_flag, wl);
+        __syncwarp();
+        ok = __all_sync(0xffffffffu, ok);
       }
       // the band lists of this tile are written (and the other buffer's were
       // read by every warp before it): one barrier per tile, all warps agree
       ok = bar_red_and_256(ok);
       if (!ok) break;
-      // phase B: a warp takes rows ew, ew + 8, ..., eight at a time, with the
-      // point rows and each point's first band member loaded for all eight
-      // before any is used (the loads are the latency of this phase)
+      // phase B: the exact decision, sixteen points per warp, then the sums
       const int sh = fuse ? P.shift[u.inst] : 0;
       const float *Ci = P.csm ? Cf : P.C + (long)u.inst * k * d;
-#pragma unroll 1
-      for (int i0 = 0; i0 < 128 / 8; i0 += G) {
-        if (ew + 8 * i0 >= u.np) break;  // uniform over the warp
-        float4 xb[G][ND4], cb[G][ND4];
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-          const int r0 = ew + 8 * (i0 + g);
-          const bool val = r0 < u.np;
-          const int cnt = val ? bl[r0 * (BMAX + 1)] : 0;
-          const int j0 = cnt > BMAX ? 0 : cnt > 0 ? bl[r0 * (BMAX + 1) + 1] : 0;
-          const long p = u.p0 + r0;
-#pragma unroll
-          for (int q = 0; q < ND4; q++) {
-            const int c4 = lane + 32 * q;
-            const bool in = val && c4 < d4;
-            xb[g][q] = in ? __ldg(reinterpret_cast<const float4 *>(P.v + p * d) + c4)
-                          : make_float4(0.f, 0.f, 0.f, 0.f);
-            cb[g][q] = in && cnt > 0 ? cload(Ci + (long)j0 * d + 4 * c4, P.csm != 0)
-                                     : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-        }
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-          const int r0 = ew + 8 * (i0 + g);
-          if (r0 < u.np)
-            finish_row<ND4>(P, bl, r0, u.p0 + r0, Ci, xb[g], cb[g], lane, d, d4, k, rho, fuse,
-                            sacc, scnt, sh, u.inst);
-        }
+      const float *Xs = reinterpret_cast<const float *>(Stg + (size_t)xs_s * lay.stage_bytes +
+                                                        lay.x_off);
+      const float *X = P.xs ? Xs : P.v + u.p0 * d;
+      if (P.csm)
+        phase_b_decide<true>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
+                             fuse ? toj : nullptr);
+      else
+        phase_b_decide<false>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
+                              fuse ? toj : nullptr);
+      if (sfuse) {
+        // every point's centroid is in toj; the next tile's are written after
+        // the next per-tile barrier, when every warp is done with these
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        phase_b_sums_owned<ND>(toj, u.np, X, ew, lane, d, sh, sacc, scnt);
+      } else if (fuse) {
+        __syncwarp();
+        phase_b_sums_global<ND>(P, toj, ew * 16, u.np, X, lane, d, k, sh, u.inst);
+      }
+      if (P.xs) {
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[xs_s]);  // this warp is done with the tile's rows
       }
       it++;
     }
@@ -556,7 +674,7 @@ bool km_tc_supported(int d, int k, const float *v, const float *C) {
   // a ring of two stages beside the centroid tile, without staging or
   // shared-memory sums, must fit (not so for d > 128 with k > 224)
   const int Kp = ((d + 63) / 64) * 64, N = ((k + 31) / 32) * 32;
-  return kmtc::make_lay(Kp / 64, N, 2, 0, k, d, 0).total <= 227 * 1024;
+  return kmtc::make_lay(Kp / 64, N, 2, 0, k, d, 0, 0).total <= 227 * 1024;
 }
 
 bool km_tc_fuses(int d, int k) { return (size_t)k * d * 8 <= 48 * 1024; }
@@ -564,7 +682,8 @@ bool km_tc_fuses(int d, int k) { return (size_t)k * d * 8 <= 48 * 1024; }
 int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const float *v, int d,
                  const float *C, int ninst, int k, void *cpk, void *cside, float *cres,
                  SetStats *cstats, const unsigned char *active, int *assign, float *dis,
-                 long long *acc, int *counts, const int *shift, int *err, cudaStream_t st) {
+                 long long *acc, int *counts, const int *shift, int delta, int *err,
+                 cudaStream_t st) {
   using namespace kmtc;
   if (nunits <= 0) return OK;
   if (!km_tc_supported(d, k, v, C) || P.Kp != ((d + 63) / 64) * 64) {
@@ -575,8 +694,12 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   const long ncl = (long)ninst * k;
   // the centroids, packed as the points are (same 16-bit format)
   YG_CHECK(stats_reset(cstats, st));
+  RowShift rs;
+  rs.mu = P.mu;
+  rs.rows_per_inst = k;
   YG_CHECK(prep_rows(C, d, (int)ncl, d, 1.f, nullptr, nullptr, nullptr, cres,
-                     (__nv_bfloat16 *)cpk, P.Kp, (__nv_bfloat16 *)cside, 1, cstats, st, 8, P.f16));
+                     (__nv_bfloat16 *)cpk, P.Kp, (__nv_bfloat16 *)cside, 1, cstats, st, 8, P.f16,
+                     rs));
   // the sums go through shared memory when an instance's k x d fit, else
   // straight to the global accumulators; the instance's FP32 centroid rows
   // are staged when they are few.  Both give way, staging first, when a ring
@@ -584,9 +707,12 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   int acc_global = acc != nullptr && !km_tc_fuses(d, k);
   int fuse = acc != nullptr && !acc_global;
   int csm = (size_t)N * d * 4 <= 32 * 1024;
+  int xs = 1;
   auto fits = [&](int S_) {
-    return make_lay(nkb, N, S_, fuse, k, d, csm).total <= 227 * 1024;
+    return make_lay(nkb, N, S_, fuse, k, d, csm, xs).total <= 227 * 1024;
   };
+  // the tile's FP32 rows are staged when two stages still fit with them
+  if (!fits(2)) xs = 0;
   if (!fits(2)) csm = 0;
   if (!fits(2) && fuse) {
     fuse = 0;
@@ -594,13 +720,15 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   }
   int S = 6;
   while (S > 2 && !fits(S)) S--;
-  const Lay lay = make_lay(nkb, N, S, fuse, k, d, csm);
+  const Lay lay = make_lay(nkb, N, S, fuse, k, d, csm, xs);
   if (lay.total > 227 * 1024) {
     set_error(E_UNSUPPORTED, "km_tc_assign: shared memory %zu too large (d=%d k=%d)", lay.total,
               d, k);
     return E_UNSUPPORTED;
   }
-  auto kern = d <= 128 ? km_tc_kernel<1> : km_tc_kernel<2>;
+  const int d4 = d / 4;
+  auto kern = d4 <= 16 ? km_tc_kernel<2> : d4 <= 24 ? km_tc_kernel<3> : d4 <= 32 ? km_tc_kernel<4>
+              : d4 <= 48 ? km_tc_kernel<6> : km_tc_kernel<8>;
   YG_CHECK(ensure_smem((const void *)kern, lay.total));
   CUtensorMap mA, mAs, mB, mBs, mC;
   YG_CHECK(tck::make_map(&mA, P.pk, P.Kp, P.n, (uint64_t)P.Kp * 2, 64, 128,
@@ -620,6 +748,9 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   p.assign = assign; p.dis = dis; p.acc = acc; p.counts = counts; p.shift = shift; p.err = err;
   p.acc_global = acc_global;
   p.csm = csm;
+  p.xs = xs;
+  p.centered = P.mu != nullptr;
+  p.delta = acc != nullptr && delta ? 1 : 0;
   p.wait_ns = wait_limit_ns();
   p.withhold = test_withhold_loads() ? 1 : 0;
   const unsigned g = (unsigned)(nunits < nsm ? nunits : nsm);

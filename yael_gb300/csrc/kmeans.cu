@@ -38,7 +38,7 @@ enum KmSlot : int {
   KS_AKEYS, KS_AKEYS2, KS_AVALS, KS_AVALS2, KS_AOFFS, KS_ATMP, KS_ASORT,
   // the small-k tensor-core assignment
   KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
-  KS_TCERR, KS_PRIOR,
+  KS_TCERR, KS_PRIOR, KS_TCMU, KS_TCMUPART, KS_TCSLF, KS_TCNPT, KS_TCHMAX,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -190,6 +190,7 @@ struct Engine {
   // cores with an exact band re-check, and, when k * d fits shared memory, the
   // centroid sums fused into it (no second pass over the points).
   bool tc = false, tc_fuse = false;
+  bool tc_live = false;  // the fused sums hold the last assignment's (reset per run)
   KmTcUnit *tc_units = nullptr;
   int tc_nunits = 0;
   KmTcPoints tcP;
@@ -237,8 +238,10 @@ struct Engine {
     const int rc = body();
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
+    // uploaded here, so that the first replay does not carry the upload
     bool ok = rc == OK && e == cudaSuccess && g != nullptr &&
-              cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+              cudaGraphInstantiate(exec, g, 0) == cudaSuccess &&
+              cudaGraphUpload(*exec, st) == cudaSuccess;
     if (g) cudaGraphDestroy(g);
     if (!ok) {
       (void)cudaGetLastError();
@@ -324,6 +327,42 @@ struct Engine {
     Workspace &ws = ctx->ws;
     const int ni = (int)in.size();
     const long ncl = (long)ni * k;
+    // every instance's mean, the translation of its packed rows (points and
+    // centroids): the 16-bit rounding errors then scale with the instance's
+    // spread, which is what the bound on the distances needs
+    float *mu, *hmc;
+    double *mpart;
+    int *slf;
+    long *npt;
+    YG_CHECK(ws_get(ws, KS_TCMU, (size_t)ni * d, &mu));
+    YG_CHECK(ws_get(ws, KS_TCMUPART, (size_t)std::max(1, nsl) * d, &mpart));
+    YG_CHECK(ws_get(ws, KS_TCSLF, (size_t)ni * 2, &slf));
+    YG_CHECK(ws_get(ws, KS_TCNPT, (size_t)ni, &npt));
+    YG_CHECK(ws_get(ws, KS_TCHMAX, (size_t)ni, &hmc));
+    {
+      std::vector<int> hf((size_t)ni * 2, 0);
+      std::vector<long> hn(ni);
+      for (int s = nsl - 1; s >= 0; s--) {
+        hf[hsl[s].inst] = s;
+        hf[ni + hsl[s].inst]++;
+      }
+      for (int i = 0; i < ni; i++) hn[i] = in[i].n;
+      YG_CUDA(cudaMemcpyAsync(slf, hf.data(), sizeof(int) * hf.size(), cudaMemcpyHostToDevice,
+                              st));
+      YG_CUDA(cudaMemcpyAsync(npt, hn.data(), sizeof(long) * ni, cudaMemcpyHostToDevice, st));
+      YG_CHECK(km_means(slices, nsl, v, d, ni, slf, slf + ni, npt, mpart, mu, st));
+      YG_CUDA(cudaMemsetAsync(hmc, 0, sizeof(float) * ni, st));
+      YG_CHECK(km_absmax_centred(slices, nsl, v, d, mu, hmc, st));
+      std::vector<float> hh(ni);
+      YG_CUDA(cudaMemcpyAsync(hh.data(), hmc, sizeof(float) * ni, cudaMemcpyDeviceToHost, st));
+      YG_CUDA(cudaStreamSynchronize(st));  // hf, hn, hh are host buffers
+      float hc = 0.f;
+      for (int i = 0; i < ni; i++) hc = hh[i] > hc ? hh[i] : (hh[i] >= 0.f ? hc : NAN);
+      // centroids are means of the instance's points (a split moves one by
+      // 1e-7 relative), so |c - mu| stays within the points' |x - mu| plus
+      // that much of max |x|
+      hmax = hmax >= 0.f && hc >= 0.f ? hc + 1e-6f * hmax : NAN;
+    }
     std::vector<KmTcUnit> hu;
     for (int i = 0; i < ni; i++)
       for (long o = 0; o < in[i].n; o += 128)
@@ -350,9 +389,14 @@ struct Engine {
     tcP.side = side;
     tc_cpk = cpk;
     tc_cside = cside;
+    tcP.mu = mu;
+    RowShift rs;
+    rs.mu = mu;
+    rs.row_inst = ni > 1 ? pinst : nullptr;
+    rs.rows_per_inst = (int)ntot;
     YG_CHECK(prep_rows(v, d, (int)ntot, d, -2.f, tcP.xn64, nullptr, nullptr, tcP.xres,
                        (__nv_bfloat16 *)pk, tcP.Kp, (__nv_bfloat16 *)side, 2, nullptr, st, 8,
-                       tcP.f16));
+                       tcP.f16, rs));
     assign_settled = true;  // no variant tuner on this path
     return OK;
   }
@@ -432,14 +476,19 @@ struct Engine {
   int assign_step() {
     if (tc) {
       const long ncl = (long)in.size() * k;
-      if (tc_fuse) {
+      // the sums start from zero once per run; later assignments add the
+      // points that change centroid (the sums stay those of the assignment)
+      const int delta = tc_fuse && tc_live ? 1 : 0;
+      if (tc_fuse && !tc_live) {
         YG_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * ncl * d, st));
         YG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * ncl, st));
       }
+      tc_live = tc_fuse;
       prec_used = tcP.f16 ? PREC_FP16 : PREC_BF16;
       return km_tc_assign(tc_units, tc_nunits, tcP, v, d, C, (int)in.size(), k, tc_cpk,
                           tc_cside, nullptr, tc_cstats, active, assign, dis,
-                          tc_fuse ? acc : nullptr, tc_fuse ? counts : nullptr, shift, tc_err, st);
+                          tc_fuse ? acc : nullptr, tc_fuse ? counts : nullptr, shift, delta,
+                          tc_err, st);
     }
     if (alt_mode()) {
       // yael/kmeans.c:242-244: knn_full with distance type 1 (L1) or 3 (chi2)
@@ -565,7 +614,9 @@ struct Engine {
     const bool use_graphs = graphs_wanted() && eager_done;
     // the assignment is captured once its kernel variant is tuned (the
     // tuner's trials run eagerly)
-    const bool graph_assign = use_graphs && assign_graph_wanted() && assign_settled;
+    // (a run's first fused assignment starts its sums: eager, as it differs)
+    const bool graph_assign =
+        use_graphs && assign_graph_wanted() && assign_settled && !(tc_fuse && !tc_live);
     if (use_graphs && !g_update && !capture(update_body, &g_update, &g_update_n))
       graphs_failed = true;
     if (graph_assign && !g_assign && !graphs_failed &&
@@ -711,7 +762,7 @@ __global__ void kpp_kernel(const float *v, int d, long n, long newsel, float *be
   double s = 0;
   for (int c = 0; c < d; c++) {
     const double t = (double)v[i * d + c] - (double)v[newsel * d + c];
-    s += t * t;
+    s = add_sq64(s, t);
   }
   const float f = (float)s;
   if (f < best[i]) best[i] = f;
@@ -830,6 +881,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
     x.core = rand_r(&x.seed);
     x.tot_re = 0; x.iters = 0; x.ret = 0; x.done = false;
     E.have_prev = false;
+    E.tc_live = false;
     x.qerr = HUGE_VAL; x.qerr_old = HUGE_VAL;
     YG_CHECK(E.set_active());
     while (!E.all_done()) YG_CHECK(E.iterate());
@@ -1027,7 +1079,7 @@ __global__ void hkm_quantize_kernel(const float *cent, int nlevel, int bf, int d
         double s = 0;
         for (int c = 0; c < d; c++) {
           const double t = (double)x[c] - (double)C[(long)j * d + c];
-          s += t * t;
+          s = add_sq64(s, t);
         }
         if (s < best) { best = s; i1 = j; }
       }

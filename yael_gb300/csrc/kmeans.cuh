@@ -38,6 +38,15 @@ __device__ __forceinline__ long long fixed_of(float x, int S) {
   return (u >> 31) ? -(long long)r : (long long)r;
 }
 
+// fixed_of(x, S) for -126 <= S <= 127, with scale = 2^S (a normal float):
+// x * 2^S is then exact (the shift keeps |x| 2^S below 2^62; a product that
+// underflows is below 1/2, and both forms give 0 for it), and the conversion
+// rounds to nearest even as fixed_of does
+__device__ __forceinline__ long long fixed_of_scaled(float x, float scale) {
+  if ((__float_as_uint(x) & 0x7f800000u) == 0x7f800000u) return 0;
+  return __float2ll_rn(x * scale);
+}
+
 struct KmWork {      // one block of the grouped assignment kernel
   int inst;          // instance
   long p0;           // first point (global index)
@@ -73,6 +82,11 @@ struct KmTcPoints {
   float *xres = nullptr;
   long n = 0;
   int Kp = 0, f16 = 0;
+  // with mu != null every packed row is translated first: the points by
+  // their instance's row of mu (mu: ninst x d), the centroids likewise, so
+  // the packing errors scale with the spread of an instance, not with its
+  // distance from the origin (distances do not change under a translation)
+  const float *mu = nullptr;
 };
 
 // shapes the kernel takes: d % 4 == 0, d <= 256, k <= 256, 16-byte aligned rows
@@ -89,13 +103,17 @@ bool km_tc_supported(int d, int k, const float *v, const float *C);
 // the counts are added to acc[g][d] / counts[g] (g = inst*k + j; both zeroed
 // by the caller), accumulated in shared memory first when an instance's
 // k*d*8 bytes fit (km_tc_fuses), else added to them directly (integer
-// atomics: the result does not depend on their order).  Units of instances
-// with active[inst] == 0 are skipped.
+// atomics: the result does not depend on their order).  With delta != 0 the
+// sums and counts already hold the assignment found in `assign` (the previous
+// call's): only the points whose centroid changes are subtracted from the old
+// one and added to the new one (integer sums: exactly the full sums).  Units
+// of instances with active[inst] == 0 are skipped.
 bool km_tc_fuses(int d, int k);
 int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const float *v, int d,
                  const float *C, int ninst, int k, void *cpk, void *cside, float *cres,
                  SetStats *cstats, const unsigned char *active, int *assign, float *dis,
-                 long long *acc, int *counts, const int *shift, int *err, cudaStream_t st);
+                 long long *acc, int *counts, const int *shift, int delta, int *err,
+                 cudaStream_t st);
 
 // After the caller's synchronisation: reports a timed trial of the grouped
 // assignment's variant tuner (autotune.cuh); true once the variant choice of
@@ -161,6 +179,15 @@ int km_slice_sums(const KmSlice *sl, int nsl, const float *dis, double *out, cud
 
 // out[inst] = max |v| over the instance's slices (out zeroed by the caller)
 int km_absmax(const KmSlice *sl, int nsl, const float *v, int d, float *out, cudaStream_t st);
+
+// mu[i] = the mean of instance i's points (FP64 sums over its slices, which
+// are listed in instance order: first[i], count[i] of them, npts[i] points;
+// part holds nsl x d doubles), rounded to float
+int km_means(const KmSlice *sl, int nsl, const float *v, int d, int ninst, const int *first,
+             const int *count, const long *npts, double *part, float *mu, cudaStream_t st);
+// out[inst] = max |fl(v - mu[inst])| (out zeroed by the caller)
+int km_absmax_centred(const KmSlice *sl, int nsl, const float *v, int d, const float *mu,
+                      float *out, cudaStream_t st);
 
 // C[i] = v[sel[i]] for rows of the listed instances
 int km_gather(const float *v, int d, const long *rows, long nrows, float *C, cudaStream_t st);

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(256)
           double sd = 0;
           for (int c = 0; c < d; c++) {
             const double t = (double)x[c] - (double)cs[j * d + c];
-            sd += t * t;
+            sd = add_sq64(sd, t);
           }
           if (sd < best) {
             best = sd;
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256)
             double sd = 0;
             for (int c = 0; c < d; c++) {
               const double tt = (double)(FULL ? xs[c * XS + p] : x[c]) - (double)cst[c * K + j];
-              sd += tt * tt;
+              sd = add_sq64(sd, tt);
             }
             if (sd < best) { best = sd; bi = j; }
           }
@@ -668,6 +668,46 @@ __global__ void absmax_kernel(const KmSlice *sl, const float *v, int d, float *o
   }
 }
 
+// column sums of one slice in FP64, rows in order (deterministic)
+__global__ void slice_colsum_kernel(const KmSlice *sl, const float *v, int d, double *part) {
+  const KmSlice s = sl[blockIdx.x];
+  for (int c = threadIdx.x; c < d; c += blockDim.x) {
+    double a = 0;
+    for (int i = 0; i < s.n; i++) a += (double)v[(s.p0 + i) * d + c];
+    part[(long)blockIdx.x * d + c] = a;
+  }
+}
+
+// mean of an instance from its slices' sums, in slice order
+__global__ void inst_mean_kernel(const int *first, const int *count, const long *npts,
+                                 const double *part, int d, float *mu) {
+  const int i = blockIdx.x;
+  for (int c = threadIdx.x; c < d; c += blockDim.x) {
+    double a = 0;
+    for (int s = 0; s < count[i]; s++) a += part[(long)(first[i] + s) * d + c];
+    mu[(long)i * d + c] = npts[i] > 0 ? (float)(a / (double)npts[i]) : 0.f;
+  }
+}
+
+// max |v - mu_inst| over a slice, v - mu rounded to FP32 as the packing does
+__global__ void absmax_centred_kernel(const KmSlice *sl, const float *v, int d, const float *mu,
+                                      float *out) {
+  const KmSlice s = sl[blockIdx.x];
+  const float *m = mu + (long)s.inst * d;
+  float a = 0.f;
+  for (long i = threadIdx.x; i < (long)s.n * d; i += blockDim.x)
+    a = fmaxf(a, fabsf(__fsub_rn(v[s.p0 * d + i], m[i % d])));
+  for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+  __shared__ float wm[8];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = fmaxf(a, wm[w]);
+    a = fmaxf(a, wm[0]);
+    atomicMax((unsigned int *)out + s.inst, __float_as_uint(a));
+  }
+}
+
 __global__ void slice_sum_kernel(const KmSlice *sl, const float *dis, double *out) {
   const KmSlice s = sl[blockIdx.x];
   __shared__ double red[256];
@@ -923,6 +963,25 @@ int km_absmax(const KmSlice *sl, int nsl, const float *v, int d, float *out,
                      cudaStream_t st) {
   if (nsl <= 0) return OK;
   absmax_kernel<<<nsl, 256, 0, st>>>(sl, v, d, out);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int km_means(const KmSlice *sl, int nsl, const float *v, int d, int ninst, const int *first,
+             const int *count, const long *npts, double *part, float *mu, cudaStream_t st) {
+  if (nsl <= 0 || ninst <= 0) return OK;
+  const int t = d < 128 ? ((d + 31) / 32) * 32 : 128;
+  slice_colsum_kernel<<<nsl, t, 0, st>>>(sl, v, d, part);
+  YG_LAUNCH_CHECK();
+  inst_mean_kernel<<<ninst, t, 0, st>>>(first, count, npts, part, d, mu);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
+
+int km_absmax_centred(const KmSlice *sl, int nsl, const float *v, int d, const float *mu,
+                      float *out, cudaStream_t st) {
+  if (nsl <= 0) return OK;
+  absmax_centred_kernel<<<nsl, 256, 0, st>>>(sl, v, d, mu, out);
   YG_LAUNCH_CHECK();
   return OK;
 }

@@ -30,16 +30,33 @@ __device__ __forceinline__ float pack_err(float v, float scale, uint16_t packed)
   return v - __bfloat162float(__float2bfloat16_rn(v));
 }
 
-// the float norm as three 16-bit parts whose exact sum is n32 (11 + 11 + 11
-// or 8 + 8 + 8 significant bits); *ok = false when fp16 cannot hold it
+// the translation row of row r (null without one)
+__device__ __forceinline__ const float *row_mu(const RowShift &sh, long r, int d) {
+  if (!sh.mu) return nullptr;
+  const long i = sh.row_inst ? (long)sh.row_inst[r] : r / sh.rows_per_inst;
+  return sh.mu + i * d;
+}
+
+__device__ __forceinline__ float4 sub4(float4 a, float4 b) {
+  return make_float4(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z),
+                     __fsub_rn(a.w, b.w));
+}
+
+// the float norm as three 16-bit parts (11 + 11 + 11 or 8 + 8 + 8 significant
+// bits).  bf16 parts sum to n32 exactly.  fp16 parts do when n32 >= 1/2; below
+// that the last part may fall among fp16's subnormals, whose spacing is 2^-24,
+// and the sum is then within 2^-25 of n32 (the distance bounds of the fp16
+// passes add 2^-24 for it).  *ok = false when fp16 cannot hold the norm
+// (n32 >= 2^15), *exact = false when the sum is not n32.
 template <bool F16>
-__device__ __forceinline__ void norm_parts(float n32, uint16_t *p, bool *ok) {
+__device__ __forceinline__ void norm_parts(float n32, uint16_t *p, bool *ok, bool *exact) {
   p[0] = to16<F16>(n32);
   const float r1 = n32 - from16<F16>(p[0]);
   p[1] = to16<F16>(r1);
   const float r2 = r1 - from16<F16>(p[1]);
   p[2] = to16<F16>(r2);
-  *ok = !F16 || (n32 < 32768.f && r2 - from16<F16>(p[2]) == 0.f);
+  *ok = !F16 || n32 < 32768.f;
+  *exact = !F16 || (*ok && r2 - from16<F16>(p[2]) == 0.f);
 }
 
 template <bool F16>
@@ -47,7 +64,7 @@ __global__ void __launch_bounds__(PW * 32)
     prep_rows_kernel(const float *__restrict__ x, long ld, int n, int d, float scale,
                      double *norm64, float *norm32, unsigned char *flags, float *resid,
                      uint16_t *packed, int Kp, uint16_t *normpart,
-                     int normpart_mode, SetStats *stats) {
+                     int normpart_mode, SetStats *stats, RowShift sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long nwarps = (long)gridDim.x * PW;
   // per-warp running statistics, reduced once per block at the end
@@ -59,6 +76,7 @@ __global__ void __launch_bounds__(PW * 32)
                    (!packed || Kp % 4 == 0);
   for (long row = (long)blockIdx.x * PW + wid; row < n; row += nwarps) {
     const float *xr = x + row * ld;
+    const float *mr = row_mu(sh, row, d);
     // FP32 per element: exact for integer data (partial sums < 2^24), within
     // (d/32 + 6) ulp otherwise -- the certificate's error bound covers that
     float s = 0.f, r = 0.f;
@@ -67,6 +85,7 @@ __global__ void __launch_bounds__(PW * 32)
       for (int c = lane * 4; c < cols; c += 128) {
         float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (c < d) q4 = __ldg(reinterpret_cast<const float4 *>(xr + c));
+        if (mr && c < d) q4 = sub4(q4, __ldg(reinterpret_cast<const float4 *>(mr + c)));
         const float e[4] = {q4.x, q4.y, q4.z, q4.w};
         uint16_t hb[4];
 #pragma unroll
@@ -90,7 +109,8 @@ __global__ void __launch_bounds__(PW * 32)
       }
     } else {
       for (int c = lane; c < cols; c += 32) {
-        const float v = c < d ? __ldg(xr + c) : 0.f;
+        const float v = c < d ? (mr ? __fsub_rn(__ldg(xr + c), __ldg(mr + c)) : __ldg(xr + c))
+                              : 0.f;
         const uint16_t h = to16<F16>(scale * v);
         if (c < d) {
           s = fmaf(v, v, s);
@@ -110,12 +130,12 @@ __global__ void __launch_bounds__(PW * 32)
       bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     exact &= (s <= kExactNorm2Max) && !bad;
-    bool nok = true;
+    bool nok = true, nexact = true;
     if (normpart && lane < 16) {
       uint16_t val = to16<F16>(0.f);
       if (normpart_mode == 1) {
         uint16_t p[3];
-        norm_parts<F16>((float)s, p, &nok);
+        norm_parts<F16>((float)s, p, &nok, &nexact);
         val = lane < 3 ? p[lane] : val;
       } else if (normpart_mode == 2) {
         val = to16<F16>(lane < 3 ? 1.f : 0.f);
@@ -125,7 +145,7 @@ __global__ void __launch_bounds__(PW * 32)
     const float rr = nok ? sqrtf(r) * (1.f + 1e-5f) : INFINITY;
     // exact class also needs every packed value and norm part to be exact,
     // which fp16 cannot promise for large values and norms
-    if (F16) exact &= nok && r == 0.f;
+    if (F16) exact &= nok && nexact && r == 0.f;
     if (lane == 0) {
       if (norm64) norm64[row] = (double)s;
       if (norm32) norm32[row] = (float)s;
@@ -175,7 +195,7 @@ __global__ void __launch_bounds__(PW * 32)
     prep_rows_vec_kernel(const float *__restrict__ x, long ld, int n, int d, float scale,
                          double *norm64, float *norm32, unsigned char *flags, float *resid,
                          uint16_t *packed, int Kp, uint16_t *normpart,
-                         int normpart_mode, SetStats *stats) {
+                         int normpart_mode, SetStats *stats, RowShift sh) {
   constexpr int RPW = 32 / LPR;  // rows per warp step
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int sub = lane / LPR, sl = lane % LPR;
@@ -188,6 +208,7 @@ __global__ void __launch_bounds__(PW * 32)
     const long row = rbase + sub;
     const bool rv = row < n;
     const float *xr = x + row * ld;
+    const float *mr = rv ? row_mu(sh, row, d) : nullptr;
     float s = 0.f, r = 0.f;
     int exact = 1, bad = 0;
     // every load of the row first (cols <= 128, the launch condition), then
@@ -199,6 +220,7 @@ __global__ void __launch_bounds__(PW * 32)
       const int c = sl * 4 + it * 4 * LPR;
       q4s[it] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (rv && c < d) q4s[it] = __ldg(reinterpret_cast<const float4 *>(xr + c));
+      if (mr && c < d) q4s[it] = sub4(q4s[it], __ldg(reinterpret_cast<const float4 *>(mr + c)));
     }
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
@@ -234,17 +256,17 @@ __global__ void __launch_bounds__(PW * 32)
       bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     exact &= (s <= kExactNorm2Max) && !bad;
-    bool nok = true;
+    bool nok = true, nexact = true;
     uint16_t part[16];
 #pragma unroll
     for (int i = 0; i < 16; i++) part[i] = to16<F16>(0.f);
     if (normpart_mode == 1) {
-      norm_parts<F16>(s, part, &nok);
+      norm_parts<F16>(s, part, &nok, &nexact);
     } else if (normpart_mode == 2) {
       part[0] = part[1] = part[2] = to16<F16>(1.f);
     }
     const float rr = nok ? sqrtf(r) * (1.f + 1e-5f) : INFINITY;
-    if (F16) exact &= nok && r == 0.f;
+    if (F16) exact &= nok && nexact && r == 0.f;
     if (rv && sl == 0) {
       if (normpart) {
         uint4 w0, w1;
@@ -424,7 +446,8 @@ int stats_reset(SetStats *stats, cudaStream_t st) {
 int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64,
               float *norm32, unsigned char *flags, float *resid,
               __nv_bfloat16 *packed_bf, int Kp, __nv_bfloat16 *normpart_bf,
-              int normpart_mode, SetStats *stats, cudaStream_t st, int warps, int f16) {
+              int normpart_mode, SetStats *stats, cudaStream_t st, int warps, int f16,
+              RowShift shift) {
   uint16_t *packed = reinterpret_cast<uint16_t *>(packed_bf);
   uint16_t *normpart = reinterpret_cast<uint16_t *>(normpart_bf);
   if (n <= 0) return OK;
@@ -440,20 +463,25 @@ int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64
   const int cols = packed ? (Kp > d ? Kp : d) : d;
   const bool vec = (d % 4 == 0) && (ld % 4 == 0) &&
                    ((reinterpret_cast<uintptr_t>(x) & 15) == 0) && (!packed || Kp % 4 == 0) &&
-                   (!normpart || (reinterpret_cast<uintptr_t>(normpart) & 15) == 0);
+                   (!normpart || (reinterpret_cast<uintptr_t>(normpart) & 15) == 0) &&
+                   (!shift.mu || (reinterpret_cast<uintptr_t>(shift.mu) & 15) == 0);
+  if (shift.mu && !shift.row_inst && shift.rows_per_inst < 1) {
+    set_error(E_ARG, "prep_rows: rows_per_inst = %d", shift.rows_per_inst);
+    return E_ARG;
+  }
   if (vec && cols <= 128) {
     const int wpb = warps >= 1 && warps <= PW ? warps : PW;
     long blocks = ceil_div(n, wpb * 4);
     if (blocks > cap * PW / wpb) blocks = cap * PW / wpb;
     auto kern = f16 ? prep_rows_vec_kernel<8, true> : prep_rows_vec_kernel<8, false>;
     kern<<<(unsigned)blocks, wpb * 32, 0, st>>>(x, ld, n, d, scale, norm64, norm32, flags, resid,
-                                              packed, Kp, normpart, normpart_mode, stats);
+                                              packed, Kp, normpart, normpart_mode, stats, shift);
   } else {
     long blocks = ceil_div(n, PW);
     if (blocks > cap) blocks = cap;
     auto kern = f16 ? prep_rows_kernel<true> : prep_rows_kernel<false>;
     kern<<<(unsigned)blocks, PW * 32, 0, st>>>(x, ld, n, d, scale, norm64, norm32, flags, resid,
-                                               packed, Kp, normpart, normpart_mode, stats);
+                                               packed, Kp, normpart, normpart_mode, stats, shift);
   }
   YG_LAUNCH_CHECK();
   return OK;

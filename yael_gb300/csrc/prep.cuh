@@ -38,11 +38,19 @@ constexpr double kExactNorm2Max = 4194304.0;  // 2^22
 // f16 = 1: the packed row and the norm parts are IEEE fp16 instead of bf16
 // (same layout; resid is then the error of the fp16 packing, infinite for a
 // row that fp16 cannot hold: |scale x| > 65504 or ||x||^2 >= 2^15)
+// Rows translated before everything else: with mu != null, row r is taken
+// as fl(x_r - mu_i) (FP32 subtraction), mu_i = mu + i * d with
+// i = row_inst[r] when row_inst != null, else r / rows_per_inst.
+struct RowShift {
+  const float *mu = nullptr;
+  const int *row_inst = nullptr;
+  int rows_per_inst = 1;
+};
 int prep_rows(const float *x, long ld, int n, int d, float scale, double *norm64,
               float *norm32, unsigned char *flags, float *resid,
               __nv_bfloat16 *packed, int Kp, __nv_bfloat16 *normpart,
               int normpart_mode, SetStats *stats, cudaStream_t st, int warps = 8,
-              int f16 = 0);
+              int f16 = 0, RowShift shift = RowShift());
 
 // Split ("3xBF16") packing: x = hi + lo + r with hi = bf16(x), lo = bf16(x - hi),
 // written as three K segments of Kp1 = 64*ceil(d/64) columns each:

@@ -80,9 +80,9 @@ __device__ __forceinline__ double dist64_seq(const float *qv, const float *brow,
   for (int c = 0; c < d; c++) {
     if (metric == METRIC_L2) {
       const double t = (double)qv[c] - (double)__ldg(brow + c);
-      s += t * t;
+      s = add_sq64(s, t);
     } else {
-      s += (double)qv[c] * (double)__ldg(brow + c);
+      s = add_mul64(s, (double)qv[c], (double)__ldg(brow + c));
     }
   }
   return s;
@@ -513,6 +513,29 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
       kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
     }
   }
+  if (!ok && thresh && nvalid >= k && kth_hi == INFINITY && a.kth_out) {
+    // a region overflowed: the candidates it did keep are rows of the base,
+    // so the k-th smallest of their exact distances bounds the query's k-th
+    // from above; the band pass that settles the query starts from it instead
+    // of the looser threshold this pass was given
+    group_sort<G>(key, id, gm);  // the valid ones first
+    float e = INFINITY;
+    for (int c = 0; c < nvalid; c++) {
+      const int cid = __shfl_sync(gm, id, c, G);
+      const float ec = group_dist32<G>(qv, a.b + (long)cid * a.ldb, d, a.metric, gm);
+      if (gl == c) e = ec;
+    }
+    unsigned long long ekey = gl < nvalid ? (unsigned long long)f2ord(e) : ~0ull;
+    int eid = id;
+    group_sort<G>(ekey, eid, gm);
+    const float ek = ord2f((unsigned)__shfl_sync(gm, ekey, k - 1, G));
+    const float rho = (float)(d + 4) * kU;
+    float eta = 0.f;
+    if (!L2) eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64[q], 0.0)) *
+                   __uint_as_float(a.bstats->max_norm_bits);
+    const double hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
+    kth_hi = __double2float_ru(hi + 2.0 * (double)rho * fabs(hi) + 2.0 * (double)eta);
+  }
   if (!ok && gl == 0) {
     const int pos = atomicAdd(a.fail_cnt, 1);
     a.fail_list[pos] = q;
@@ -551,6 +574,8 @@ __global__ void eps_kernel(int nq, int d, int prec, int metric, const double *qn
   }
   // ||q||^2 (added in the re-rank) and ||b||^2 (inside v) each off by un relative
   e += un * (qn * qn + B * B);
+  // fp16 norm parts: their sum is within 2^-25 of ||b||^2
+  if (prec == PREC_FP16) e += u;
   e = e * 1.1 + 1e-30;
   eps[q] = isfinite(e) ? (float)e : INFINITY;
 }

@@ -141,8 +141,9 @@ __global__ void __launch_bounds__(NT_TC, 1)
                    const __grid_constant__ CUtensorMap mapBn, int nq, int nb, int nkb,
                    int S, ScanSel sel, int *err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t *base = reinterpret_cast<uint8_t *>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  // aligned by pointer arithmetic on smem_raw (not through an integer), so
+  // that the compiler keeps these pointers in the shared address space
+  uint8_t *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const Layout lay = make_layout(nkb, S, MODE, C, QS, PAIR);
   const size_t SB = lay.stage_bytes;
   constexpr int BHALF = PAIR ? STAGE_BYTES / 2 : STAGE_BYTES;  // base bytes per stage, this CTA
