@@ -161,6 +161,8 @@ struct Engine {
   std::vector<Instance> in;
   // device buffers
   float *C, *dis, *amax;
+  float *inst_mu = nullptr, *inst_cmax = nullptr;  // per instance: mean, max |v - mean|
+  std::vector<float> hcmax;
   int *assign, *counts, *shift, *pinst;
   unsigned char *active;
   long *offs, *cursor, *perm, *rows;
@@ -290,9 +292,34 @@ struct Engine {
       YG_CHECK(ws_get(ws, KS_PINST, (size_t)ntot, &pinst));
       YG_CUDA(cudaMemcpyAsync(pinst, hpinst.data(), sizeof(int) * ntot, cudaMemcpyHostToDevice, st));
     }
-    // fixed-point shift per instance from its data (exact integer sums)
-    YG_CUDA(cudaMemsetAsync(amax, 0, sizeof(float) * ni, st));
-    YG_CHECK(km_absmax(slices, nsl, v, d, amax, st));
+    // per instance: max |v| (the fixed-point shift of the exact integer sums),
+    // the mean mu and max |v - mu| (the translation of the 16-bit packing)
+    {
+      float *part;
+      int *slf;
+      long *npt;
+      YG_CHECK(ws_get(ws, KS_TCMU, (size_t)ni * d, &inst_mu));
+      YG_CHECK(ws_get(ws, KS_TCMUPART, (size_t)std::max(1, nsl) * d * 3, &part));
+      YG_CHECK(ws_get(ws, KS_TCSLF, (size_t)ni * 2, &slf));
+      YG_CHECK(ws_get(ws, KS_TCNPT, (size_t)ni, &npt));
+      YG_CHECK(ws_get(ws, KS_TCHMAX, (size_t)ni, &inst_cmax));
+      std::vector<int> hf((size_t)ni * 2, 0);
+      std::vector<long> hn(ni);
+      for (int s = nsl - 1; s >= 0; s--) {
+        hf[hsl[s].inst] = s;
+        hf[ni + hsl[s].inst]++;
+      }
+      for (int i = 0; i < ni; i++) hn[i] = in[i].n;
+      YG_CUDA(cudaMemcpyAsync(slf, hf.data(), sizeof(int) * hf.size(), cudaMemcpyHostToDevice,
+                              st));
+      YG_CUDA(cudaMemcpyAsync(npt, hn.data(), sizeof(long) * ni, cudaMemcpyHostToDevice, st));
+      YG_CHECK(km_inst_stats(slices, nsl, v, d, ni, slf, slf + ni, npt, part, inst_mu, amax,
+                             inst_cmax, st));
+      hcmax.resize(ni);
+      YG_CUDA(cudaMemcpyAsync(hcmax.data(), inst_cmax, sizeof(float) * ni,
+                              cudaMemcpyDeviceToHost, st));
+      YG_CUDA(cudaStreamSynchronize(st));  // hf, hn are host buffers
+    }
     std::vector<float> ha(ni);
     YG_CUDA(cudaMemcpyAsync(ha.data(), amax, sizeof(float) * ni, cudaMemcpyDeviceToHost, st));
     YG_CUDA(cudaStreamSynchronize(st));
@@ -327,37 +354,12 @@ struct Engine {
     Workspace &ws = ctx->ws;
     const int ni = (int)in.size();
     const long ncl = (long)ni * k;
-    // every instance's mean, the translation of its packed rows (points and
-    // centroids): the 16-bit rounding errors then scale with the instance's
-    // spread, which is what the bound on the distances needs
-    float *mu, *hmc;
-    double *mpart;
-    int *slf;
-    long *npt;
-    YG_CHECK(ws_get(ws, KS_TCMU, (size_t)ni * d, &mu));
-    YG_CHECK(ws_get(ws, KS_TCMUPART, (size_t)std::max(1, nsl) * d, &mpart));
-    YG_CHECK(ws_get(ws, KS_TCSLF, (size_t)ni * 2, &slf));
-    YG_CHECK(ws_get(ws, KS_TCNPT, (size_t)ni, &npt));
-    YG_CHECK(ws_get(ws, KS_TCHMAX, (size_t)ni, &hmc));
+    // every instance's rows (points and centroids) are packed relative to its
+    // mean: the 16-bit rounding errors then scale with the instance's spread,
+    // which is what the bound on the distances needs
     {
-      std::vector<int> hf((size_t)ni * 2, 0);
-      std::vector<long> hn(ni);
-      for (int s = nsl - 1; s >= 0; s--) {
-        hf[hsl[s].inst] = s;
-        hf[ni + hsl[s].inst]++;
-      }
-      for (int i = 0; i < ni; i++) hn[i] = in[i].n;
-      YG_CUDA(cudaMemcpyAsync(slf, hf.data(), sizeof(int) * hf.size(), cudaMemcpyHostToDevice,
-                              st));
-      YG_CUDA(cudaMemcpyAsync(npt, hn.data(), sizeof(long) * ni, cudaMemcpyHostToDevice, st));
-      YG_CHECK(km_means(slices, nsl, v, d, ni, slf, slf + ni, npt, mpart, mu, st));
-      YG_CUDA(cudaMemsetAsync(hmc, 0, sizeof(float) * ni, st));
-      YG_CHECK(km_absmax_centred(slices, nsl, v, d, mu, hmc, st));
-      std::vector<float> hh(ni);
-      YG_CUDA(cudaMemcpyAsync(hh.data(), hmc, sizeof(float) * ni, cudaMemcpyDeviceToHost, st));
-      YG_CUDA(cudaStreamSynchronize(st));  // hf, hn, hh are host buffers
       float hc = 0.f;
-      for (int i = 0; i < ni; i++) hc = hh[i] > hc ? hh[i] : (hh[i] >= 0.f ? hc : NAN);
+      for (int i = 0; i < ni; i++) hc = hcmax[i] > hc ? hcmax[i] : (hcmax[i] >= 0.f ? hc : NAN);
       // centroids are means of the instance's points (a split moves one by
       // 1e-7 relative), so |c - mu| stays within the points' |x - mu| plus
       // that much of max |x|
@@ -389,9 +391,9 @@ struct Engine {
     tcP.side = side;
     tc_cpk = cpk;
     tc_cside = cside;
-    tcP.mu = mu;
+    tcP.mu = inst_mu;
     RowShift rs;
-    rs.mu = mu;
+    rs.mu = inst_mu;
     rs.row_inst = ni > 1 ? pinst : nullptr;
     rs.rows_per_inst = (int)ntot;
     YG_CHECK(prep_rows(v, d, (int)ntot, d, -2.f, tcP.xn64, nullptr, nullptr, tcP.xres,
@@ -559,13 +561,13 @@ struct Engine {
     cudaEventCreate(&e2);
     auto update_body = [&]() -> int {
       if (tc_fuse) {
-        // the sums and counts came with the assignment
-        YG_CHECK(km_finalize(acc, counts, ncl, d, k, shift, active, C, st));
+        // the sums and counts came with the assignment; the counts, the error
+        // flag and the objective's slice sums are written straight to the
+        // pinned host buffers (no copies in the step)
+        YG_CHECK(km_finalize(acc, counts, ncl, d, k, shift, active, C, st, ph_counts, tc_err,
+                             ph_err));
         if (flags & YAEL_KMEANS_NORMALIZE_CENTS) YG_CHECK(km_normalize(C, ncl, d, k, active, st));
-        YG_CHECK(km_slice_sums(slices, nsl, dis, part, st));
-        YG_CUDA(cudaMemcpyAsync(ph_counts, counts, sizeof(int) * ncl, cudaMemcpyDeviceToHost, st));
-        YG_CUDA(cudaMemcpyAsync(ph_part, part, sizeof(double) * nsl, cudaMemcpyDeviceToHost, st));
-        YG_CUDA(cudaMemcpyAsync(ph_err, tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        YG_CHECK(km_slice_sums(slices, nsl, dis, ph_part, st));
         return OK;
       }
       if (tc) YG_CUDA(cudaMemcpyAsync(ph_err, tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));

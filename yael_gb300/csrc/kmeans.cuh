@@ -159,9 +159,12 @@ int km_update(const long *perm, const long *total, long nmax, const int *assign,
 int km_prior_bound(const float *v, int d, long n, const int *assign, const float *C, float *kth,
                    cudaStream_t st);
 
-// the readout of km_update alone, for sums accumulated elsewhere (km_tc_assign)
+// the readout of km_update alone, for sums accumulated elsewhere (km_tc_assign);
+// with counts_out / err_out (host-mapped memory, say) it also copies the
+// counts and *err there
 int km_finalize(const long long *acc, const int *counts, long ncl, int d, int k,
-                const int *shift, const unsigned char *active, float *C, cudaStream_t st);
+                const int *shift, const unsigned char *active, float *C, cudaStream_t st,
+                int *counts_out = nullptr, const int *err = nullptr, int *err_out = nullptr);
 
 // rows of C scaled to unit L2 norm (yael/vector.c:2016-2025 arithmetic)
 int km_normalize(float *C, long ncl, int d, int k, const unsigned char *active,
@@ -177,17 +180,13 @@ struct KmSlice {
 constexpr int kSliceLen = 4096;
 int km_slice_sums(const KmSlice *sl, int nsl, const float *dis, double *out, cudaStream_t st);
 
-// out[inst] = max |v| over the instance's slices (out zeroed by the caller)
-int km_absmax(const KmSlice *sl, int nsl, const float *v, int d, float *out, cudaStream_t st);
-
-// mu[i] = the mean of instance i's points (FP64 sums over its slices, which
-// are listed in instance order: first[i], count[i] of them, npts[i] points;
-// part holds nsl x d doubles), rounded to float
-int km_means(const KmSlice *sl, int nsl, const float *v, int d, int ninst, const int *first,
-             const int *count, const long *npts, double *part, float *mu, cudaStream_t st);
-// out[inst] = max |fl(v - mu[inst])| (out zeroed by the caller)
-int km_absmax_centred(const KmSlice *sl, int nsl, const float *v, int d, const float *mu,
-                      float *out, cudaStream_t st);
+// Per instance i (slices first[i] .. + count[i] - 1, listed in instance
+// order, npts[i] points): mu[i] = the mean of its points (FP32 sums in a fixed
+// order, deterministic), amax[i] = max |v| and cmax[i] >= max |fl(v - mu[i])|.
+// part: 3 x nsl x d floats of scratch.
+int km_inst_stats(const KmSlice *sl, int nsl, const float *v, int d, int ninst,
+                  const int *first, const int *count, const long *npts, float *part, float *mu,
+                  float *amax, float *cmax, cudaStream_t st);
 
 // C[i] = v[sel[i]] for rows of the listed instances
 int km_gather(const float *v, int d, const long *rows, long nrows, float *C, cudaStream_t st);

@@ -497,10 +497,12 @@ __global__ void __launch_bounds__(256)
 
 __global__ void finalize_kernel(const long long *acc, const int *counts, long ncl, int d,
                                 int k, const int *shift, const unsigned char *active,
-                                float *C) {
+                                float *C, int *counts_out, const int *err, int *err_out) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && err_out) *err_out = *err;
   if (i >= ncl * d) return;
   const long g = i / d;
+  if (counts_out && i == g * d) counts_out[g] = counts[g];
   const int inst = (int)(g / k);
   if (!active[inst]) return;
   const double inv = ldexp(1.0, -shift[inst]);
@@ -653,58 +655,78 @@ __global__ void cluster_offsets_kernel(const int *sorted, long n, int k, int *of
   offs[g] = (int)lo;
 }
 
-__global__ void absmax_kernel(const KmSlice *sl, const float *v, int d, float *out) {
+// Per (slice, group of 32 columns): the column sums in FP32 (rows taken in
+// a fixed order: deterministic), minima and maxima.  Block (32, 8).
+__global__ void slice_stats_kernel(const KmSlice *sl, const float *v, int d, float *psum,
+                                   float *pmin, float *pmax) {
   const KmSlice s = sl[blockIdx.x];
-  float m = 0.f;
-  for (long i = threadIdx.x; i < (long)s.n * d; i += blockDim.x) m = fmaxf(m, fabsf(v[s.p0 * d + i]));
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ float wm[8];
-  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  const int c = blockIdx.y * 32 + threadIdx.x;
+  float a = 0.f, lo = INFINITY, hi = -INFINITY;
+  if (c < d)
+    for (int i = threadIdx.y; i < s.n; i += 8) {
+      const float x = v[(s.p0 + i) * d + c];
+      a += x;
+      lo = fminf(lo, x);
+      hi = fmaxf(hi, x);
+    }
+  __shared__ float sa[8][32], sl_[8][32], sh[8][32];
+  sa[threadIdx.y][threadIdx.x] = a;
+  sl_[threadIdx.y][threadIdx.x] = lo;
+  sh[threadIdx.y][threadIdx.x] = hi;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wm[w]);
-    m = fmaxf(m, wm[0]);
-    atomicMax((unsigned int *)out + s.inst, __float_as_uint(m));
+  if (threadIdx.y == 0 && c < d) {
+    for (int y = 1; y < 8; y++) {
+      a += sa[y][threadIdx.x];
+      lo = fminf(lo, sl_[y][threadIdx.x]);
+      hi = fmaxf(hi, sh[y][threadIdx.x]);
+    }
+    const long o = (long)blockIdx.x * d + c;
+    psum[o] = a;
+    pmin[o] = lo;
+    pmax[o] = hi;
   }
 }
 
-// column sums of one slice in FP64, rows in order (deterministic)
-__global__ void slice_colsum_kernel(const KmSlice *sl, const float *v, int d, double *part) {
-  const KmSlice s = sl[blockIdx.x];
-  for (int c = threadIdx.x; c < d; c += blockDim.x) {
-    double a = 0;
-    for (int i = 0; i < s.n; i++) a += (double)v[(s.p0 + i) * d + c];
-    part[(long)blockIdx.x * d + c] = a;
-  }
-}
-
-// mean of an instance from its slices' sums, in slice order
-__global__ void inst_mean_kernel(const int *first, const int *count, const long *npts,
-                                 const double *part, int d, float *mu) {
+// Per instance (its slices first[i] .. + count[i] - 1, npts[i] points): the
+// mean mu (FP32 sums in slice order), amax = max |v| and cmax >= max |fl(v -
+// mu)| (the column extremes' distances to mu, rounded up).
+__global__ void inst_stats_kernel(const int *first, const int *count, const long *npts,
+                                  const float *psum, const float *pmin, const float *pmax,
+                                  int d, float *mu, float *amax, float *cmax) {
   const int i = blockIdx.x;
+  float am = 0.f, cm = 0.f;
   for (int c = threadIdx.x; c < d; c += blockDim.x) {
-    double a = 0;
-    for (int s = 0; s < count[i]; s++) a += part[(long)(first[i] + s) * d + c];
-    mu[(long)i * d + c] = npts[i] > 0 ? (float)(a / (double)npts[i]) : 0.f;
+    float a = 0.f, lo = INFINITY, hi = -INFINITY;
+    for (int s = 0; s < count[i]; s++) {
+      const long o = (long)(first[i] + s) * d + c;
+      a += psum[o];
+      lo = fminf(lo, pmin[o]);
+      hi = fmaxf(hi, pmax[o]);
+    }
+    const float m = npts[i] > 0 ? a / (float)npts[i] : 0.f;
+    mu[(long)i * d + c] = m;
+    if (lo <= hi) {  // a column of NaNs alone leaves both as they are
+      am = fmaxf(am, fmaxf(fabsf(lo), fabsf(hi)));
+      cm = fmaxf(cm, fmaxf(__fsub_ru(hi, m), __fsub_ru(m, lo)));
+    }
   }
-}
-
-// max |v - mu_inst| over a slice, v - mu rounded to FP32 as the packing does
-__global__ void absmax_centred_kernel(const KmSlice *sl, const float *v, int d, const float *mu,
-                                      float *out) {
-  const KmSlice s = sl[blockIdx.x];
-  const float *m = mu + (long)s.inst * d;
-  float a = 0.f;
-  for (long i = threadIdx.x; i < (long)s.n * d; i += blockDim.x)
-    a = fmaxf(a, fabsf(__fsub_rn(v[s.p0 * d + i], m[i % d])));
-  for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
-  __shared__ float wm[8];
-  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = a;
+  for (int o = 16; o > 0; o >>= 1) {
+    am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
+    cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+  }
+  __shared__ float wa[8], wc[8];
+  if ((threadIdx.x & 31) == 0) {
+    wa[threadIdx.x >> 5] = am;
+    wc[threadIdx.x >> 5] = cm;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); w++) a = fmaxf(a, wm[w]);
-    a = fmaxf(a, wm[0]);
-    atomicMax((unsigned int *)out + s.inst, __float_as_uint(a));
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      am = fmaxf(am, wa[w]);
+      cm = fmaxf(cm, wc[w]);
+    }
+    amax[i] = am;
+    cmax[i] = cm;
   }
 }
 
@@ -902,8 +924,8 @@ int km_update(const long *perm, const long *total, long nmax, const int *assign,
     }
     YG_LAUNCH_CHECK();
   }
-  finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(acc, counts, ncl, d, k, shift,
-                                                                     active, C);
+  finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(
+      acc, counts, ncl, d, k, shift, active, C, nullptr, nullptr, nullptr);
   YG_LAUNCH_CHECK();
   return OK;
 }
@@ -945,9 +967,10 @@ int km_prior_bound(const float *v, int d, long n, const int *assign, const float
 }
 
 int km_finalize(const long long *acc, const int *counts, long ncl, int d, int k,
-                const int *shift, const unsigned char *active, float *C, cudaStream_t st) {
-  finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(acc, counts, ncl, d, k, shift,
-                                                                     active, C);
+                const int *shift, const unsigned char *active, float *C, cudaStream_t st,
+                int *counts_out, const int *err, int *err_out) {
+  finalize_kernel<<<(unsigned)ceil_div(ncl * d, 256), 256, 0, st>>>(
+      acc, counts, ncl, d, k, shift, active, C, counts_out, err, err_out);
   YG_LAUNCH_CHECK();
   return OK;
 }
@@ -959,29 +982,16 @@ int km_normalize(float *C, long ncl, int d, int k, const unsigned char *active,
   return OK;
 }
 
-int km_absmax(const KmSlice *sl, int nsl, const float *v, int d, float *out,
-                     cudaStream_t st) {
-  if (nsl <= 0) return OK;
-  absmax_kernel<<<nsl, 256, 0, st>>>(sl, v, d, out);
-  YG_LAUNCH_CHECK();
-  return OK;
-}
-
-int km_means(const KmSlice *sl, int nsl, const float *v, int d, int ninst, const int *first,
-             const int *count, const long *npts, double *part, float *mu, cudaStream_t st) {
+int km_inst_stats(const KmSlice *sl, int nsl, const float *v, int d, int ninst,
+                  const int *first, const int *count, const long *npts, float *part, float *mu,
+                  float *amax, float *cmax, cudaStream_t st) {
   if (nsl <= 0 || ninst <= 0) return OK;
-  const int t = d < 128 ? ((d + 31) / 32) * 32 : 128;
-  slice_colsum_kernel<<<nsl, t, 0, st>>>(sl, v, d, part);
+  float *psum = part, *pmin = part + (size_t)nsl * d, *pmax = part + 2 * (size_t)nsl * d;
+  slice_stats_kernel<<<dim3((unsigned)nsl, (unsigned)ceil_div(d, 32)), dim3(32, 8), 0, st>>>(
+      sl, v, d, psum, pmin, pmax);
   YG_LAUNCH_CHECK();
-  inst_mean_kernel<<<ninst, t, 0, st>>>(first, count, npts, part, d, mu);
-  YG_LAUNCH_CHECK();
-  return OK;
-}
-
-int km_absmax_centred(const KmSlice *sl, int nsl, const float *v, int d, const float *mu,
-                      float *out, cudaStream_t st) {
-  if (nsl <= 0) return OK;
-  absmax_centred_kernel<<<nsl, 256, 0, st>>>(sl, v, d, mu, out);
+  inst_stats_kernel<<<ninst, 128, 0, st>>>(first, count, npts, psum, pmin, pmax, d, mu, amax,
+                                           cmax);
   YG_LAUNCH_CHECK();
   return OK;
 }
