@@ -39,6 +39,7 @@ enum KmSlot : int {
   // the small-k tensor-core assignment
   KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
   KS_TCERR, KS_PRIOR, KS_TCMU, KS_TCMUPART, KS_TCSLF, KS_TCNPT, KS_TCHMAX,
+  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -164,6 +165,7 @@ struct Engine {
   float *inst_mu = nullptr, *inst_cmax = nullptr;  // per instance: mean, max |v - mean|
   std::vector<float> hcmax;
   int *assign, *counts, *shift, *pinst;
+  const int *pinst_given = nullptr;  // the points' instances, when the caller has them on the device
   unsigned char *active;
   long *offs, *cursor, *perm, *rows;
   long long *acc;
@@ -272,13 +274,14 @@ struct Engine {
     std::vector<KmWork> hw;
     hsl.clear();
     std::vector<int> hpinst;
-    if (ni > 1) hpinst.resize(ntot);
+    const bool host_pinst = ni > 1 && !pinst_given;
+    if (host_pinst) hpinst.resize(ntot);
     for (int i = 0; i < ni; i++) {
       for (long o = 0; o < in[i].n; o += kAssignChunk)
         hw.push_back({i, in[i].p0 + o, (int)std::min<long>(kAssignChunk, in[i].n - o)});
       for (long o = 0; o < in[i].n; o += kSliceLen)
         hsl.push_back({in[i].p0 + o, (int)std::min<long>(kSliceLen, in[i].n - o), i});
-      if (ni > 1)
+      if (host_pinst)
         for (long p = 0; p < in[i].n; p++) hpinst[in[i].p0 + p] = i;
     }
     nwork = (int)hw.size();
@@ -288,9 +291,11 @@ struct Engine {
     YG_CHECK(ws_get(ws, KS_PART, (size_t)nsl, &part));
     YG_CUDA(cudaMemcpyAsync(work, hw.data(), sizeof(KmWork) * nwork, cudaMemcpyHostToDevice, st));
     YG_CUDA(cudaMemcpyAsync(slices, hsl.data(), sizeof(KmSlice) * nsl, cudaMemcpyHostToDevice, st));
-    if (ni > 1) {
+    if (host_pinst) {
       YG_CHECK(ws_get(ws, KS_PINST, (size_t)ntot, &pinst));
       YG_CUDA(cudaMemcpyAsync(pinst, hpinst.data(), sizeof(int) * ntot, cudaMemcpyHostToDevice, st));
+    } else if (ni > 1) {
+      pinst = const_cast<int *>(pinst_given);
     }
     // per instance: max |v| (the fixed-point shift of the exact integer sums),
     // the mean mu and max |v - mu| (the translation of the 16-bit packing)
@@ -971,8 +976,6 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   YG_CHECK(ws_get(ctx->ws, KS_TMP, (size_t)n * 2, &sorted));
   YG_CUDA(cudaMemcpyAsync(dv, points, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, st));
   YG_CUDA(cudaMemsetAsync(node, 0, sizeof(int) * n, st));
-  std::vector<int> hnode(n, 0);
-  std::vector<long> hperm(n);
   long k = 1, iters = 0;
   yael_gpu_call_stats stats = {};
   cudaEvent_t t0, t1;
@@ -981,20 +984,24 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   cudaEventRecord(t0, st);
   for (int l = 0; l < nlevel; l++) {
     NvtxRange nv_level("hkm.level");
-    // points grouped by parent, stable in point index (ivec_sort_index, hkm.c:56-62)
+    // points grouped by parent, stable in point index (ivec_sort_index,
+    // hkm.c:56-62), on the device; the nodes' first points come back
     std::vector<long> start(k + 1, 0);
-    for (int i = 0; i < n; i++) start[hnode[i] + 1]++;
-    for (long p = 0; p < k; p++) start[p + 1] += start[p];
-    {
-      std::vector<long> pos(start.begin(), start.end() - 1);
-      for (int i = 0; i < n; i++) hperm[pos[hnode[i]]++] = i;
-    }
-    YG_CUDA(cudaMemcpyAsync(sorted, hperm.data(), sizeof(long) * n, cudaMemcpyHostToDevice, st));
+    long *dstart;
+    int *dpinst;
+    YG_CHECK(ws_get(ctx->ws, KS_HSTART, (size_t)k + 1, &dstart));
+    YG_CHECK(ws_get(ctx->ws, KS_HPINST, (size_t)n, &dpinst));
+    YG_CHECK(km_group_by_key(node, n, (int)k, sorted, dstart, k > 1 ? dpinst : nullptr, ctx->ws,
+                             KS_GCNT, KS_GTOT, st));
+    YG_CUDA(cudaMemcpyAsync(start.data(), dstart, sizeof(long) * (size_t)(k + 1),
+                            cudaMemcpyDeviceToHost, st));
     YG_CHECK(km_gather(dv, d, sorted, n, vs, st));
+    YG_CUDA(cudaStreamSynchronize(st));  // start
     Engine E;
     E.ctx = ctx; E.st = st; E.d = d; E.k = bf; E.niter = niter == 0 ? 1000000 : niter;
     E.flags = YAEL_KMEANS_INIT_RANDOM | YAEL_KMEANS_QUIET;
     E.prec = prec; E.verbose = false; E.v = vs; E.ntot = n;
+    E.pinst_given = k > 1 ? dpinst : nullptr;
     E.in.resize(k);
     for (long p = 0; p < k; p++) {
       const long na = start[p + 1] - start[p];
@@ -1039,7 +1046,6 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
                             cudaMemcpyDeviceToHost, st));
     node_update_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(sorted, E.assign, n, bf, node);
     YG_LAUNCH_CHECK();
-    YG_CUDA(cudaMemcpyAsync(hnode.data(), node, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
     YG_CUDA(cudaStreamSynchronize(st));
     k *= bf;
   }
@@ -1048,7 +1054,10 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   if (ms_out) cudaEventElapsedTime(ms_out, t0, t1);
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
-  if (assign_out) memcpy(assign_out, hnode.data(), sizeof(int) * n);
+  if (assign_out) {
+    YG_CHECK(copy_out(st, assign_out, node, sizeof(int) * (size_t)n, false));
+    YG_CUDA(cudaStreamSynchronize(st));
+  }
   if (iters_out) *iters_out = iters;
   stats.instance_iterations = iters;
   g_last_stats = stats;

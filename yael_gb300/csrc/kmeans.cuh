@@ -188,6 +188,13 @@ int km_inst_stats(const KmSlice *sl, int nsl, const float *v, int d, int ninst,
                   const int *first, const int *count, const long *npts, float *part, float *mu,
                   float *amax, float *cmax, cudaStream_t st);
 
+// Stable grouping of n points by key[i] in [0, k): perm lists the points
+// key by key, each key's in index order (start[b] .. start[b + 1] - 1, start
+// has k + 1 entries); key_of[j] = key[perm[j]] when not null.  Scratch in the
+// workspace slots slot_cnt / slot_tot.
+int km_group_by_key(const int *key, long n, int k, long *perm, long *start, int *key_of,
+                    Workspace &ws, int slot_cnt, int slot_tot, cudaStream_t st);
+
 // C[i] = v[sel[i]] for rows of the listed instances
 int km_gather(const float *v, int d, const long *rows, long nrows, float *C, cudaStream_t st);
 

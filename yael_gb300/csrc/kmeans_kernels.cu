@@ -982,6 +982,94 @@ int km_normalize(float *C, long ncl, int d, int k, const unsigned char *active,
   return OK;
 }
 
+// ---- stable grouping of points by a small key (hkm: by node) ----------------
+
+// cnt[c * k + b] = points of chunk c with key b
+__global__ void group_count_kernel(const int *key, long n, int k, long chunk, int *cnt) {
+  const long c = blockIdx.x;
+  const long i0 = c * chunk, i1 = min(n, i0 + chunk);
+  int *row = cnt + c * (long)k;
+  for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) atomicAdd(row + key[i], 1);
+}
+
+// per key b: cnt[c * k + b] := the points of chunks before c with key b;
+// tot[b] = all of them
+__global__ void group_prefix_kernel(int *cnt, long nchunk, int k, long *tot) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= k) return;
+  long a = 0;
+  for (long c = 0; c < nchunk; c++) {
+    const int x = cnt[c * k + b];
+    cnt[c * k + b] = (int)a;
+    a += x;
+  }
+  tot[b] = a;
+}
+
+// start[b] = sum of tot[b'] for b' < b (start[k] = n), one thread
+__global__ void group_start_kernel(const long *tot, int k, long *start) {
+  long a = 0;
+  for (int b = 0; b < k; b++) {
+    start[b] = a;
+    a += tot[b];
+  }
+  start[k] = a;
+}
+
+// one warp per chunk, 32 points at a time in index order: a point's place is
+// its key's start, the points of that key in earlier chunks, those already
+// placed from this chunk and those of earlier lanes (stable)
+__global__ void group_scatter_kernel(const int *key, long n, int k, long chunk, int *cnt,
+                                     const long *start, long *perm) {
+  const long c = blockIdx.x;
+  const int lane = threadIdx.x;
+  const long i0 = c * chunk, i1 = min(n, i0 + chunk);
+  int *row = cnt + c * (long)k;
+  for (long g = i0; g < i1; g += 32) {
+    const long i = g + lane;
+    const bool v = i < i1;
+    const int b = v ? key[i] : -1 - lane;  // distinct dummies for the lanes past the end
+    const unsigned same = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(same & ((1u << lane) - 1u));
+    if (v) perm[start[b] + row[b] + rank] = i;
+    __syncwarp();
+    if (v && rank == 0) row[b] += __popc(same);
+    __syncwarp();
+  }
+}
+
+// pinst[j] = key[perm[j]]
+__global__ void group_key_of_kernel(const int *key, const long *perm, long n, int *out) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) out[j] = key[perm[j]];
+}
+
+int km_group_by_key(const int *key, long n, int k, long *perm, long *start, int *key_of,
+                    Workspace &ws, int slot_cnt, int slot_tot, cudaStream_t st) {
+  if (n <= 0) return OK;
+  long chunk = 2048;
+  while ((double)ceil_div(n, chunk) * k > 16e6) chunk *= 2;
+  const long nchunk = ceil_div(n, chunk);
+  int *cnt;
+  long *tot;
+  YG_CHECK(ws.get(slot_cnt, sizeof(int) * (size_t)nchunk * k, reinterpret_cast<void **>(&cnt)));
+  YG_CHECK(ws.get(slot_tot, sizeof(long) * (size_t)k, reinterpret_cast<void **>(&tot)));
+  YG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)nchunk * k, st));
+  group_count_kernel<<<(unsigned)nchunk, 256, 0, st>>>(key, n, k, chunk, cnt);
+  YG_LAUNCH_CHECK();
+  group_prefix_kernel<<<(unsigned)ceil_div(k, 128), 128, 0, st>>>(cnt, nchunk, k, tot);
+  YG_LAUNCH_CHECK();
+  group_start_kernel<<<1, 1, 0, st>>>(tot, k, start);
+  YG_LAUNCH_CHECK();
+  group_scatter_kernel<<<(unsigned)nchunk, 32, 0, st>>>(key, n, k, chunk, cnt, start, perm);
+  YG_LAUNCH_CHECK();
+  if (key_of) {
+    group_key_of_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(key, perm, n, key_of);
+    YG_LAUNCH_CHECK();
+  }
+  return OK;
+}
+
 int km_inst_stats(const KmSlice *sl, int nsl, const float *v, int d, int ninst,
                   const int *first, const int *count, const long *npts, float *part, float *mu,
                   float *amax, float *cmax, cudaStream_t st) {
