@@ -153,8 +153,8 @@ __device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *
   const int mmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)nm);
   const float4 *xr = reinterpret_cast<const float4 *>(X + (long)(val ? r : 0) * d);
   const int i0 = (lane >> 1) % max(nh, 1);  // this lane's first column
-  float e1 = INFINITY, e2 = INFINITY;
-  int j1 = -1;
+  float e1 = INFINITY, e2 = INFINITY, e3 = INFINITY;
+  int j1 = -1, j2 = -1;
   for (int m = 0; m < mmax; m++) {
     int j = 0;
     if (m < nm) {  // the next member (one is left)
@@ -185,19 +185,73 @@ __device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *
     float e = (s0 + s1) + (s2 + s3);
     e += __shfl_xor_sync(0xffffffffu, e, 1);  // the other half (same sum in both lanes)
     if (m < nm) {
-      if (e < e1) { e2 = e1; e1 = e; j1 = j; } else if (e < e2) { e2 = e; }
+      if (e < e1) {
+        e3 = e2; e2 = e1; j2 = j1; e1 = e; j1 = j;
+      } else if (e < e2) {
+        e3 = e2; e2 = e; j2 = j;
+      } else if (e < e3) {
+        e3 = e;
+      }
     }
   }
   int oj = -1;
   float od = 1e30f;
   if (j1 >= 0 && e1 < 1e30f) { oj = j1; od = e1; }
   const bool tie = oj >= 0 && e2 < INFINITY && e2 - e1 <= rho * (e1 + e2);
+  bool need64 = tie;
   if (__any_sync(0xffffffffu, tie)) {
+    // A near tie of the best two alone (a third is clearly worse than the
+    // best): the sign of D_a - D_b = sum_c (a_c - b_c)(a_c + b_c - 2 x_c)
+    // (a = j1, b = j2) in FP32 with its rounding bound.  When the sum clears
+    // that bound plus the rounding of the two FP64 sequential sums that decide
+    // a tie (each within (d + 2) 2^-53 of its value), FP64 would find the same
+    // order: typically the two halves of a split centroid, 1e-7 apart.
+    const bool pair = tie && !(e3 < INFINITY && e3 - e1 <= rho * (e1 + e3));
+    float dl = 0.f, sa = 0.f, sb = 0.f;
+    if (pair) {
+      const float4 *ca = reinterpret_cast<const float4 *>(Ci + (long)j1 * d);
+      const float4 *cb = reinterpret_cast<const float4 *>(Ci + (long)j2 * d);
+      for (int t = 0; t < nh; t++) {
+        int i = i0 + t;
+        if (i >= nh) i -= nh;
+        const int q = 2 * i + h;
+        const float4 xv = xr[q];
+        const float4 av = CSM ? ca[q] : __ldg(ca + q);
+        const float4 bv = CSM ? cb[q] : __ldg(cb + q);
+        const float ax[4] = {av.x, av.y, av.z, av.w}, bx[4] = {bv.x, bv.y, bv.z, bv.w};
+        const float xx[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const float pp = __fsub_rn(ax[c], bx[c]), s1 = __fadd_rn(ax[c], bx[c]);
+          const float tt = __fmul_rn(pp, __fsub_rn(s1, __fadd_rn(xx[c], xx[c])));
+          dl = __fadd_rn(dl, tt);
+          sa = __fadd_rn(sa, fabsf(tt));
+          sb = __fadd_rn(sb, fabsf(pp) * fabsf(s1));
+        }
+      }
+    }
+    dl += __shfl_xor_sync(0xffffffffu, dl, 1);
+    sa += __shfl_xor_sync(0xffffffffu, sa, 1);
+    sb += __shfl_xor_sync(0xffffffffu, sb, 1);
+    if (pair) {
+      // per coordinate p = fl(a - b), s = fl(a + b), t = fl(p fl(s - 2x)):
+      // |t - exact| <= u |p| (|a + b| + 3 |s - 2x|) to first order, and the
+      // d / 2 + 1 additions add u per term: |dl - (D_a - D_b)| <=
+      // 1.02 u (sum |p| |s| + (d + 10) sum |t|); then the FP64 sums' error
+      const float bound = 1.02f * 5.9604645e-08f * (sb + (float)(d + 10) * sa) +
+                          (float)(d + 4) * 1.12e-16f * (e1 + e2) * 1.1f;
+      if (fabsf(dl) > bound) {
+        need64 = false;
+        if (dl > 0.f) { oj = j2; od = e2; }
+      }
+    }
+  }
+  if (__any_sync(0xffffffffu, need64)) {
     // near tie: FP64 over the members, sequential over coordinates, the two
     // lanes of the point taking alternate members
     double best = INFINITY;
     int bj = INT_MAX;
-    if (tie) {
+    if (need64) {
       const float *xs = X + (long)r * d;
       unsigned tk = bw[0];
       int tw = 0;
@@ -218,7 +272,7 @@ __device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *
     const double ob = __shfl_xor_sync(0xffffffffu, best, 1);
     const int oj2 = __shfl_xor_sync(0xffffffffu, bj, 1);
     if (ob < best || (ob == best && oj2 < bj)) { best = ob; bj = oj2; }
-    if (tie) {
+    if (need64) {
       if (bj != INT_MAX && best < 1e30) { oj = bj; od = (float)best; }
       else { oj = -1; od = 1e30f; }
     }
