@@ -118,23 +118,42 @@ __device__ __forceinline__ long long fixed_of_nb(float x, int S) {
   return ex == 0xff ? 0 : (u >> 31) ? -r : r;
 }
 
+// fixed_of when x 2^S is an integer (exponent field ex >= 150 - S, not
+// Inf/NaN): the 24-bit mantissa shifted left, with the sign
+__device__ __forceinline__ long long fixed_of_shift(float x, int S) {
+  const unsigned u = __float_as_uint(x);
+  const int ex = (int)((u >> 23) & 0xffu);
+  const unsigned m = (u & 0x7fffffu) | (ex ? 0x800000u : 0u);
+  const unsigned long long r = (unsigned long long)m << (ex - 150 + S);
+  const unsigned long long sg = (unsigned long long)((long long)(int)u >> 31);  // 0 or all ones
+  return (long long)((r ^ sg) - sg);
+}
+
+// whether fixed_of_shift gives fixed_of(x, S): a normal x with x 2^S an
+// integer, or +-0 (subnormals, Inf and NaN take fixed_of_nb)
+__device__ __forceinline__ bool fixed_shift_ok(float x, int S) {
+  const int ex = (int)((__float_as_uint(x) >> 23) & 0xffu);
+  return (ex >= 150 - S && ex != 0xff && ex != 0) || (__float_as_uint(x) << 1) == 0u;
+}
+
 // The exact decision for the sixteen points r0 .. r0 + 15 of a warp, two
 // lanes per point (lanes 2 p and 2 p + 1 for point p; h = lane & 1 takes the
 // float4 columns q = 2 i + h).  The lanes of point p start at i = p and wrap
 // around, so that any eight consecutive lanes (four points, both halves) read
-// eight different bank groups when the rows are a multiple of 128 bytes.  Per band member the FP32 distance
-// sum_c (x_c - c_c)^2 is summed in that order (four partial sums, the two
-// halves added last: deterministic); members come in increasing index order
-// and strict '<' keeps the lower index on equal values; when the best two are
-// closer than their rounding bound the members are compared in FP64 (lowest
-// index on equal values).  Writes assign / dis and, for the fused sums, the
+// eight different bank groups when the rows are a multiple of 128 bytes.
+// Per band member the FP32 distance sum_c (x_c - c_c)^2 is summed in that
+// order (four partial sums, the two halves added last: deterministic); members come in increasing index order and
+// strict '<' keeps the lower index on equal values; a near tie of the best
+// two is settled by the sign of their distance difference when that clears
+// its rounding bound, by FP64 otherwise (lowest index on equal values).  Writes assign / dis and, for the fused sums, the
 // point's move: the centroid it joins to toj and the one it leaves to toa
 // (-1 for none; with P.delta == 0 every point joins and none leaves, else
-// only a point whose centroid changed moves).
+// only a point whose centroid changed moves).  Returns true in the lane that
+// wrote a move.
 // X: the tile's rows (staged, or global from the tile's first point);
 // Ci: the instance's centroid rows (staged or global).
 template <bool CSM>
-__device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *bm, int r0,
+__device__ __forceinline__ bool phase_b_decide(const Params &P, const unsigned *bm, int r0,
                                                int np, long p0, const float *X, const float *Ci,
                                                int lane, int d, int k, float rho, int *toj) {
   const int r = r0 + (lane >> 1), h = lane & 1;
@@ -284,10 +303,13 @@ __device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *
       toj[r] = oj != oa ? oj : -1;
       toj[128 + r] = oj != oa ? oa : -1;
     }
-  } else if (toj && h == 0) {
+    return oj != oa;
+  }
+  if (toj && h == 0) {
     toj[r] = -1;
     toj[128 + r] = -1;
   }
+  return false;
 }
 
 // The fused sums of one tile, after every point's move is in toj (joins:
@@ -300,23 +322,43 @@ template <int N32>
 __device__ __forceinline__ void phase_b_sums_owned(const int *toj, int np, const float *X,
                                                    int ew, int lane, int d, int sh,
                                                    unsigned long long *sacc, int *scnt) {
+  // the eight words of moves first (independent loads), then their masks
+  int o[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) o[c] = ((c & 3) * 32 + lane) < np ? toj[c * 32 + lane] : -1;
+  unsigned mk[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) mk[c] = __ballot_sync(0xffffffffu, o[c] >= 0 && (o[c] & 7) == ew);
 #pragma unroll 1
-  for (int c = 0; c < 256; c += 32) {
-    const int r = (c & 127) + lane;
-    const int o = r < np ? toj[c + lane] : -1;
-    unsigned m = __ballot_sync(0xffffffffu, o >= 0 && (o & 7) == ew);
-    const bool leave = c >= 128;
+  for (int c = 0; c < 8; c++) {
+    const bool leave = c >= 4;
+    unsigned m = mk[0];
+    int oc = o[0];
+#pragma unroll
+    for (int cc = 1; cc < 8; cc++)  // (registers, not a runtime index)
+      if (cc == c) {
+        m = mk[cc];
+        oc = o[cc];
+      }
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;
-      const int j = __shfl_sync(0xffffffffu, o, b);
-      const float *xr = X + (long)((c & 127) + b) * d;
+      const int j = __shfl_sync(0xffffffffu, oc, b);
+      const float *xr = X + (long)((c & 3) * 32 + b) * d;
       unsigned long long *row = sacc + (long)j * d;
-      long long v[N32];
+      float xv[N32];
+      bool fast = true;
 #pragma unroll
       for (int i = 0; i < N32; i++) {
         const int col = lane + 32 * i;
-        const long long f = col < d ? fixed_of_nb(xr[col], sh) : 0;
+        xv[i] = col < d ? xr[col] : 0.f;
+        fast = fast && fixed_shift_ok(xv[i], sh);
+      }
+      fast = __all_sync(0xffffffffu, fast);  // almost always: no tiny coordinate
+      long long v[N32];
+#pragma unroll
+      for (int i = 0; i < N32; i++) {
+        const long long f = fast ? fixed_of_shift(xv[i], sh) : fixed_of_nb(xv[i], sh);
         v[i] = leave ? -f : f;
       }
 #pragma unroll
@@ -349,11 +391,20 @@ __device__ __forceinline__ void phase_b_sums_global(const Params &P, const int *
     const float *xr = X + (long)(r0 + (b & 15)) * d;
     const long g = (long)inst * k + j;
     unsigned long long *row = reinterpret_cast<unsigned long long *>(P.acc) + g * d;
+    float xv[N32];
+    bool fast = true;
+#pragma unroll
+    for (int i = 0; i < N32; i++) {
+      const int col = lane + 32 * i;
+      xv[i] = col < d ? xr[col] : 0.f;
+      fast = fast && fixed_shift_ok(xv[i], sh);
+    }
+    fast = __all_sync(0xffffffffu, fast);
 #pragma unroll
     for (int i = 0; i < N32; i++) {
       const int col = lane + 32 * i;
       if (col < d) {
-        const long long f = fixed_of_nb(xr[col], sh);
+        const long long f = fast ? fixed_of_shift(xv[i], sh) : fixed_of_nb(xv[i], sh);
         atomicAdd(row + col, (unsigned long long)(leave ? -f : f));
       }
     }
@@ -618,9 +669,17 @@ __global__ void __launch_bounds__(NT, 1)
           for (int c0 = 0; c0 < N; c0 += 32) {
             tmem_ld32(tc + (uint32_t)c0, r);
             tmem_ld_wait(r);
+            // a tree of minima (fminf: any order gives the same minimum)
+            float m16[16];
 #pragma unroll
-            for (int i = 0; i < 32; i++)
-              if (c0 + i < k) vmin = fminf(vmin, __uint_as_float(r[i]));
+            for (int i = 0; i < 16; i++)
+              m16[i] = fminf(c0 + i < k ? __uint_as_float(r[i]) : INFINITY,
+                             c0 + i + 16 < k ? __uint_as_float(r[i + 16]) : INFINITY);
+#pragma unroll
+            for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+              for (int i = 0; i < w; i++) m16[i] = fminf(m16[i], m16[i + w]);
+            vmin = fminf(vmin, m16[0]);
           }
           const float lim = vmin + 2.f * eps;
           // the members: a bit per centroid within 2 eps of the smallest; all
@@ -660,17 +719,18 @@ __global__ void __launch_bounds__(NT, 1)
       const float *Xs = reinterpret_cast<const float *>(Stg + (size_t)xs_s * lay.stage_bytes +
                                                         lay.x_off);
       const float *X = P.xs ? Xs : P.v + u.p0 * d;
-      if (P.csm)
-        phase_b_decide<true>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
-                             fuse ? toj : nullptr);
-      else
-        phase_b_decide<false>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
-                              fuse ? toj : nullptr);
+      const bool moved =
+          P.csm ? phase_b_decide<true>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
+                                       fuse ? toj : nullptr)
+                : phase_b_decide<false>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
+                                        fuse ? toj : nullptr);
       if (sfuse) {
-        // every point's centroid is in toj; the next tile's are written after
-        // the next per-tile barrier, when every warp is done with these
-        asm volatile("bar.sync 1, 256;" ::: "memory");
-        phase_b_sums_owned<ND>(toj, u.np, X, ew, lane, d, sh, sacc, scnt);
+        // every point's move is in toj (the next tile's are written after the
+        // next per-tile barrier, when every warp is done with these); a tile
+        // without one has no sums to change
+        if (bar_red_or_256(moved)) {
+          phase_b_sums_owned<ND>(toj, u.np, X, ew, lane, d, sh, sacc, scnt);
+        }
       } else if (fuse) {
         __syncwarp();
         phase_b_sums_global<ND>(P, toj, ew * 16, u.np, X, lane, d, k, sh, u.inst);
