@@ -44,8 +44,8 @@ constexpr int A_SIDE = 128 * 32;  // 128 rows x 16 16-bit columns
 
 struct Lay {
   int nkb, N, S, fuse, csm, xs;
-  size_t stage_bytes, x_off, b_off, bside_off, cf_off, band_off, lst_off, acc_off, cnt_off, bar_off,
-      total;
+  size_t stage_bytes, x_off, ts_off, b_off, bside_off, cf_off, band_off, lst_off, acc_off, cnt_off,
+      bar_off, total;
 };
 
 // xs: every stage also holds the tile's FP32 point rows (128 x d floats)
@@ -55,7 +55,9 @@ __host__ __device__ inline Lay make_lay(int nkb, int N, int S, int fuse, int k, 
   L.nkb = nkb; L.N = N; L.S = S; L.fuse = fuse; L.csm = csm; L.xs = xs;
   size_t off = 0;
   L.x_off = (size_t)nkb * A_BLK + A_SIDE;
-  L.stage_bytes = L.x_off + (xs ? (((size_t)128 * d * 4 + 1023) & ~(size_t)1023) : 0);
+  // the tile's per-point norm and packing error (128 x float2) after its rows
+  L.ts_off = L.x_off + (xs ? (((size_t)128 * d * 4 + 1023) & ~(size_t)1023) : 0);
+  L.stage_bytes = L.ts_off + 1024;
   off += (size_t)S * L.stage_bytes;
   L.b_off = off;     off += (size_t)nkb * N * 128;  // N % 32 == 0: 1024-aligned blocks
   L.bside_off = off; off += (size_t)N * 32;
@@ -76,8 +78,7 @@ struct Params {
   int nunits;
   int d, k, N, Kp, f16;
   const float *v, *C;
-  const double *xn64;
-  const float *xres;
+  const float2 *tside;         // per unit, per point: (||x'|| rounded up, packing error)
   const SetStats *cs;
   const unsigned char *active;
   int *assign;
@@ -451,8 +452,9 @@ __global__ void __launch_bounds__(NT, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
       mbar_init(&full[s], 1);
-      // the MMAs' commit, and with staged rows the eight epilogue warps too
-      mbar_init(&empty[s], P.xs ? 9 : 1);
+      // the MMAs' commit and the eight epilogue warps (the stage's side data,
+      // and its FP32 rows when staged)
+      mbar_init(&empty[s], 9);
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(&tfull[a], 1);
@@ -516,8 +518,9 @@ __global__ void __launch_bounds__(NT, 1)
         if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, wl)) { ok = false; break; }
         uint8_t *sp = Stg + (size_t)s * lay.stage_bytes;
         const uint32_t xbytes = P.xs ? (uint32_t)u.np * d * 4 : 0u;
-        mbar_arrive_expect_tx(&full[s], abytes0 + xbytes);
+        mbar_arrive_expect_tx(&full[s], abytes0 + xbytes + 1024u);
         if (P.xs) bulk_load(sp + lay.x_off, P.v + u.p0 * d, xbytes, &full[s]);
+        bulk_load(sp + lay.ts_off, P.tside + (long)w * 128, 1024u, &full[s]);
         for (int kb = 0; kb < nkb; kb++)
           tma_load_2d(&mapA, &full[s], sp + (size_t)kb * A_BLK, kb * 64, (int)u.p0);
         tma_load_2d(&mapAs, &full[s], sp + (size_t)nkb * A_BLK, 0, (int)u.p0);
@@ -631,17 +634,16 @@ __global__ void __launch_bounds__(NT, 1)
       const int xs_s = esn;  // the stage this tile came in
       const uint32_t xs_ph = ephn;
       if (++esn == S) { esn = 0; ephn ^= 1; }
+      // the tile's copies have landed (the MMAs waited for them too: this
+      // wait only makes them visible here)
+      ok = ok && mbar_wait(&full[xs_s], xs_ph, abort_flag, wl);
+      __syncwarp();
+      ok = __all_sync(0xffffffffu, ok);
+      const float2 *ts = reinterpret_cast<const float2 *>(Stg + (size_t)xs_s * lay.stage_bytes +
+                                                          lay.ts_off);
       if (ew < 4) {
         const uint32_t uu = (uint32_t)(it >> 1);
-        // the point's norm and packing error, loaded before the wait
         const bool rv = row < u.np;
-        const long p = u.p0 + row;
-        double xn = 0.0;
-        float dq = 0.f;
-        if (rv) {
-          xn = P.xn64[p];
-          dq = P.xres[p];
-        }
         ok = ok && mbar_wait(&tfull[a], uu & 1, abort_flag, wl);
         __syncwarp();
         ok = __all_sync(0xffffffffu, ok);
@@ -649,7 +651,8 @@ __global__ void __launch_bounds__(NT, 1)
           tc_fence_after();
           float eps = 0.f;
           if (rv) {
-            const float qn = sqrtf(fmaxf((float)xn, 0.f)) * (1.f + 1e-5f);
+            const float2 nd = ts[row];
+            const float qn = nd.x, dq = nd.y;
             const float dot = dq * (B + dB) + qn * dB;
             const float accb = Kt * 2.f * u24 * (2.f * (qn + dq) * (B + dB) + 1.001f * B * B);
             // the translation: x' = fl(x - mu), c' = fl(c - mu) are off by
@@ -702,13 +705,6 @@ __global__ void __launch_bounds__(NT, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[a]);
       }
-      if (P.xs) {
-        // the tile's rows were copied with its packed rows: this wait only
-        // makes the copy visible here (the MMAs already waited for it)
-        ok = ok && mbar_wait(&full[xs_s], xs_ph, abort_flag, wl);
-        __syncwarp();
-        ok = __all_sync(0xffffffffu, ok);
-      }
       // the band lists of this tile are written (and the other buffer's were
       // read by every warp before it): one barrier per tile, all warps agree
       ok = bar_red_and_256(ok);
@@ -735,10 +731,8 @@ __global__ void __launch_bounds__(NT, 1)
         __syncwarp();
         phase_b_sums_global<ND>(P, toj, ew * 16, u.np, X, lane, d, k, sh, u.inst);
       }
-      if (P.xs) {
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[xs_s]);  // this warp is done with the tile's rows
-      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[xs_s]);  // this warp is done with the tile's stage
       it++;
     }
     if (sfuse && ok && cur >= 0) flush(cur);
@@ -780,6 +774,29 @@ int make_map_f32(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t rows, 
   return OK;
 }
 }  // namespace
+
+namespace {
+__global__ void tile_side_kernel(const KmTcUnit *units, const double *xn64, const float *xres,
+                                 float2 *tside) {
+  const KmTcUnit u = units[blockIdx.x];
+  const int r = threadIdx.x;
+  float2 o = make_float2(0.f, 0.f);
+  if (r < u.np) {
+    const long p = u.p0 + r;
+    o.x = sqrtf(fmaxf((float)xn64[p], 0.f)) * (1.f + 1e-5f);
+    o.y = xres[p];
+  }
+  tside[(long)blockIdx.x * 128 + r] = o;
+}
+}  // namespace
+
+int km_tc_tile_side(const KmTcUnit *units, int nunits, const double *xn64, const float *xres,
+                    float2 *tside, cudaStream_t st) {
+  if (nunits <= 0) return OK;
+  tile_side_kernel<<<nunits, 128, 0, st>>>(units, xn64, xres, tside);
+  YG_LAUNCH_CHECK();
+  return OK;
+}
 
 bool km_tc_supported(int d, int k, const float *v, const float *C) {
   if (!(d >= 4 && d % 4 == 0 && d <= 256 && k >= 1 && k <= kTcMaxK &&
@@ -858,7 +875,7 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   Params p;
   p.units = units; p.nunits = nunits; p.d = d; p.k = k; p.N = N; p.Kp = P.Kp; p.f16 = P.f16;
-  p.v = v; p.C = C; p.xn64 = P.xn64; p.xres = P.xres; p.cs = cstats; p.active = active;
+  p.v = v; p.C = C; p.tside = P.tside; p.cs = cstats; p.active = active;
   p.assign = assign; p.dis = dis; p.acc = acc; p.counts = counts; p.shift = shift; p.err = err;
   p.acc_global = acc_global;
   p.csm = csm;

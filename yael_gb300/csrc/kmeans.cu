@@ -39,7 +39,7 @@ enum KmSlot : int {
   // the small-k tensor-core assignment
   KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
   KS_TCERR, KS_PRIOR, KS_TCMU, KS_TCMUPART, KS_TCSLF, KS_TCNPT, KS_TCHMAX,
-  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT,
+  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT, KS_TCTSIDE,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -404,6 +404,8 @@ struct Engine {
     YG_CHECK(prep_rows(v, d, (int)ntot, d, -2.f, tcP.xn64, nullptr, nullptr, tcP.xres,
                        (__nv_bfloat16 *)pk, tcP.Kp, (__nv_bfloat16 *)side, 2, nullptr, st, 8,
                        tcP.f16, rs));
+    YG_CHECK(ws_get(ws, KS_TCTSIDE, (size_t)tc_nunits * 128, &tcP.tside));
+    YG_CHECK(km_tc_tile_side(tc_units, tc_nunits, tcP.xn64, tcP.xres, tcP.tside, st));
     assign_settled = true;  // no variant tuner on this path
     return OK;
   }

@@ -87,7 +87,14 @@ struct KmTcPoints {
   // the packing errors scale with the spread of an instance, not with its
   // distance from the origin (distances do not change under a translation)
   const float *mu = nullptr;
+  // per unit of the unit table, per point of its tile: (||x'|| rounded up,
+  // ||x' - 16(x')||), copied with the tile (km_tc_tile_side fills it)
+  float2 *tside = nullptr;
 };
+
+// tside[w][r] for the unit table (0 past a tile's points)
+int km_tc_tile_side(const KmTcUnit *units, int nunits, const double *xn64, const float *xres,
+                    float2 *tside, cudaStream_t st);
 
 // shapes the kernel takes: d % 4 == 0, d <= 256, k <= 256, 16-byte aligned rows
 bool km_tc_supported(int d, int k, const float *v, const float *C);
