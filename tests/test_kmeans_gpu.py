@@ -180,6 +180,45 @@ def test_kmeans_redo_keeps_best():
     same(gpu_kmeans(v, 10, 10, QUIET, 5, 3, "fp32"), oracle_kmeans(v, 10, 10, QUIET, 5, 3))
 
 
+@pytest.mark.parametrize("prec", ["bf16", "fp32"])
+def test_kmeans_empty_cluster_splits_both_forms(prec):
+    """Empty clusters split into pairs of centroids 1e-7 apart: every point of
+    the original cluster is then a near tie of the pair, settled in the
+    tensor-core form by the sign of the two distances' difference (or FP64);
+    bit-identical to the oracle either way."""
+    g = np.load(os.path.join(GOLDEN, "kmeans_empty.npz"))
+    v = g["v"]
+    r = gpu_kmeans(v, 40, 20, QUIET, 77, 1, prec)
+    same(r, oracle_kmeans(v, 40, 20, QUIET, 77, 1))
+
+
+@pytest.mark.parametrize("flags", [QUIET, yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
+                                   | yg.KMEANS_NORMALIZE_CENTS])
+def test_kmeans_tensor_core_redo(flags):
+    """Several runs (nredo = 3) through the tensor-core assignment: each run
+    starts its incremental centroid sums from zero; the best run is kept as
+    in the oracle."""
+    v, _, _ = synth.gaussian_mixture(9000, 32, 24, 0.25, seed=15)
+    g = gpu_kmeans(v, 24, 9, flags, 321, 3, "bf16")
+    assert g["prec_used"] == 3
+    same(g, oracle_kmeans(v, 24, 9, flags, 321, 3))
+
+
+@pytest.mark.parametrize("offset,sigma", [(40.0, 0.3), (3.0, 1e-3)])
+def test_kmeans_tensor_core_centred_packing(offset, sigma):
+    """Points far from the origin (40 + N(0, 0.3)): packed relative to their
+    mean they fit fp16; a very tight cloud (3 + 1e-3 N(0, 1)): the centred
+    centroid norms are tiny and their fp16 norm parts fall among fp16's
+    subnormals.  Both exact against the oracle."""
+    rng = np.random.default_rng(int(offset * 10))
+    centres = rng.standard_normal((12, 48)).astype(np.float32) * (10 * sigma)
+    lab = rng.integers(0, 12, 7000)
+    v = (offset + centres[lab] + sigma * rng.standard_normal((7000, 48))).astype(np.float32)
+    g = gpu_kmeans(v, 12, 8, QUIET, 41, 1, "bf16")
+    assert g["prec_used"] == 3
+    same(g, oracle_kmeans(v, 12, 8, QUIET, 41, 1))
+
+
 def test_kmeans_plus_plus_init():
     g = np.load(os.path.join(GOLDEN, "kmeans_pp.npz"))
     v = g["v"]

@@ -986,6 +986,7 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   cudaEventRecord(t0, st);
   for (int l = 0; l < nlevel; l++) {
     NvtxRange nv_level("hkm.level");
+    const double tl0 = trace_enabled() ? wall_ms() : 0.0;
     // points grouped by parent, stable in point index (ivec_sort_index,
     // hkm.c:56-62), on the device; the nodes' first points come back
     std::vector<long> start(k + 1, 0);
@@ -1036,7 +1037,9 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
     }
     YG_CUDA(cudaStreamSynchronize(st));
     YG_CHECK(E.set_active());
+    const double tl1 = trace_enabled() ? wall_ms() : 0.0;
     while (!E.all_done()) YG_CHECK(E.iterate());
+    const double tl2 = trace_enabled() ? wall_ms() : 0.0;
     for (auto &x : E.in) iters += x.iters;
     stats.point_iterations += E.point_iters;
     stats.level_iterations += E.engine_iters;
@@ -1049,6 +1052,9 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
     node_update_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(sorted, E.assign, n, bf, node);
     YG_LAUNCH_CHECK();
     YG_CUDA(cudaStreamSynchronize(st));
+    if (trace_enabled())
+      fprintf(stderr, "[yael_gpu] hkm level %d: %ld nodes, set-up %.3f ms, iterations %.3f ms, "
+              "wrap-up %.3f ms (host clock)\n", l, k, tl1 - tl0, tl2 - tl1, wall_ms() - tl2);
     k *= bf;
   }
   cudaEventRecord(t1, st);
