@@ -79,6 +79,7 @@ struct Params {
   int d, k, N, Kp, f16;
   const float *v, *C;
   const float2 *tside;         // per unit, per point: (||x'|| rounded up, packing error)
+  const float2 *ib;            // per instance: (max centroid norm, max centroid packing error)
   const SetStats *cs;
   const unsigned char *active;
   int *assign;
@@ -589,8 +590,6 @@ __global__ void __launch_bounds__(NT, 1)
     const uint32_t lane_base = (uint32_t)(grp * 32) << 16;
     const float u24 = 5.9604645e-08f;
     const float rho = (float)(d + 4) * u24;
-    const float B = __uint_as_float(P.cs->max_norm_bits);
-    const float dB = __uint_as_float(P.cs->max_resid_bits);
     const float Kt = (float)(P.Kp + 16);
     const float un = (float)((d + 31) / 32 + 6) * u24;
     int it = 0, cur = -1;
@@ -653,6 +652,8 @@ __global__ void __launch_bounds__(NT, 1)
           if (rv) {
             const float2 nd = ts[row];
             const float qn = nd.x, dq = nd.y;
+            const float2 bd = P.ib[u.inst];  // the instance's centroids
+            const float B = bd.x, dB = bd.y;
             const float dot = dq * (B + dB) + qn * dB;
             const float accb = Kt * 2.f * u24 * (2.f * (qn + dq) * (B + dB) + 1.001f * B * B);
             // the translation: x' = fl(x - mu), c' = fl(c - mu) are off by
@@ -798,6 +799,26 @@ int km_tc_tile_side(const KmTcUnit *units, int nunits, const double *xn64, const
   return OK;
 }
 
+namespace {
+// per instance, over its k centroid rows: (max ||c'|| as the packing's
+// statistics round it, max packing error).  fmaxf passes over NaN (a row with
+// a NaN value is never chosen: its distances are NaN) and keeps +inf (an
+// overflowing norm or a row fp16 cannot hold: no usable bound)
+__global__ void inst_bound_kernel(const float *cnorm, const float *cres, int k, float2 *ib) {
+  const long r0 = (long)blockIdx.x * k;
+  float b = 0.f, e = 0.f;
+  for (int j = threadIdx.x; j < k; j += 32) {
+    b = fmaxf(b, sqrtf(cnorm[r0 + j]) * (1.f + 1e-5f));
+    e = fmaxf(e, cres[r0 + j]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+  }
+  if (threadIdx.x == 0) ib[blockIdx.x] = make_float2(b, e);
+}
+}  // namespace
+
 bool km_tc_supported(int d, int k, const float *v, const float *C) {
   if (!(d >= 4 && d % 4 == 0 && d <= 256 && k >= 1 && k <= kTcMaxK &&
         (reinterpret_cast<uintptr_t>(v) & 15) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0))
@@ -811,9 +832,9 @@ bool km_tc_supported(int d, int k, const float *v, const float *C) {
 bool km_tc_fuses(int d, int k) { return (size_t)k * d * 8 <= 48 * 1024; }
 
 int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const float *v, int d,
-                 const float *C, int ninst, int k, void *cpk, void *cside, float *cres,
-                 SetStats *cstats, const unsigned char *active, int *assign, float *dis,
-                 long long *acc, int *counts, const int *shift, int delta, int *err,
+                 const float *C, int ninst, int k, void *cpk, void *cside, float *cscratch,
+                 float2 *ibound, SetStats *cstats, const unsigned char *active, int *assign,
+                 float *dis, long long *acc, int *counts, const int *shift, int delta, int *err,
                  cudaStream_t st) {
   using namespace kmtc;
   if (nunits <= 0) return OK;
@@ -828,9 +849,14 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   RowShift rs;
   rs.mu = P.mu;
   rs.rows_per_inst = k;
-  YG_CHECK(prep_rows(C, d, (int)ncl, d, 1.f, nullptr, nullptr, nullptr, cres,
+  float *cnorm = cscratch, *cres = cscratch + ncl;
+  YG_CHECK(prep_rows(C, d, (int)ncl, d, 1.f, nullptr, cnorm, nullptr, cres,
                      (__nv_bfloat16 *)cpk, P.Kp, (__nv_bfloat16 *)cside, 1, cstats, st, 8, P.f16,
                      rs));
+  // each instance's own largest centroid norm and packing error: a point is
+  // compared with its instance's centroids only, so these bound its errors
+  inst_bound_kernel<<<(unsigned)ninst, 32, 0, st>>>(cnorm, cres, k, ibound);
+  YG_LAUNCH_CHECK();
   // the sums go through shared memory when an instance's k x d fit, else
   // straight to the global accumulators; the instance's FP32 centroid rows
   // are staged when they are few.  Both give way, staging first, when a ring
@@ -875,7 +901,7 @@ int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const f
   YG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   Params p;
   p.units = units; p.nunits = nunits; p.d = d; p.k = k; p.N = N; p.Kp = P.Kp; p.f16 = P.f16;
-  p.v = v; p.C = C; p.tside = P.tside; p.cs = cstats; p.active = active;
+  p.v = v; p.C = C; p.tside = P.tside; p.ib = ibound; p.cs = cstats; p.active = active;
   p.assign = assign; p.dis = dis; p.acc = acc; p.counts = counts; p.shift = shift; p.err = err;
   p.acc_global = acc_global;
   p.csm = csm;

@@ -39,7 +39,7 @@ enum KmSlot : int {
   // the small-k tensor-core assignment
   KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
   KS_TCERR, KS_PRIOR, KS_TCMU, KS_TCMUPART, KS_TCSLF, KS_TCNPT, KS_TCHMAX,
-  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT, KS_TCTSIDE,
+  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT, KS_TCTSIDE, KS_TCCSCR, KS_TCIB,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -494,8 +494,12 @@ struct Engine {
       }
       tc_live = tc_fuse;
       prec_used = tcP.f16 ? PREC_FP16 : PREC_BF16;
+      float *cscr;
+      float2 *ib;
+      YG_CHECK(ws_get(ctx->ws, KS_TCCSCR, (size_t)ncl * 2, &cscr));
+      YG_CHECK(ws_get(ctx->ws, KS_TCIB, in.size(), &ib));
       return km_tc_assign(tc_units, tc_nunits, tcP, v, d, C, (int)in.size(), k, tc_cpk,
-                          tc_cside, nullptr, tc_cstats, active, assign, dis,
+                          tc_cside, cscr, ib, tc_cstats, active, assign, dis,
                           tc_fuse ? acc : nullptr, tc_fuse ? counts : nullptr, shift, delta,
                           tc_err, st);
     }

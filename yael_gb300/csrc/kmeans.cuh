@@ -106,7 +106,9 @@ bool km_tc_supported(int d, int k, const float *v, const float *C);
 // the best two are closer than their rounding bound (ties to the lowest
 // index).  Points whose distances are all NaN get -1 / 1e30.  The centroids
 // are packed here (cpk, cside: [ninst*k][Kp] and [ninst*k][16], cstats reset
-// and filled).  With acc != null the exact fixed-point sums of the points and
+// and filled; cscratch: 2 x ninst*k floats of norms and packing errors, from
+// which ibound[ninst] takes each instance's largest, the bound's terms for
+// its points).  With acc != null the exact fixed-point sums of the points and
 // the counts are added to acc[g][d] / counts[g] (g = inst*k + j; both zeroed
 // by the caller), accumulated in shared memory first when an instance's
 // k*d*8 bytes fit (km_tc_fuses), else added to them directly (integer
@@ -117,9 +119,9 @@ bool km_tc_supported(int d, int k, const float *v, const float *C);
 // of instances with active[inst] == 0 are skipped.
 bool km_tc_fuses(int d, int k);
 int km_tc_assign(const KmTcUnit *units, int nunits, const KmTcPoints &P, const float *v, int d,
-                 const float *C, int ninst, int k, void *cpk, void *cside, float *cres,
-                 SetStats *cstats, const unsigned char *active, int *assign, float *dis,
-                 long long *acc, int *counts, const int *shift, int delta, int *err,
+                 const float *C, int ninst, int k, void *cpk, void *cside, float *cscratch,
+                 float2 *ibound, SetStats *cstats, const unsigned char *active, int *assign,
+                 float *dis, long long *acc, int *counts, const int *shift, int delta, int *err,
                  cudaStream_t st);
 
 // After the caller's synchronisation: reports a timed trial of the grouped
