@@ -70,6 +70,7 @@ struct Workspace {
     size_t n = 0;
   };
   std::vector<Buf> bufs;
+  bool host = false;  // pinned host memory (cudaMallocHost) instead of device memory
   // slot-addressed scratch: the same slot is reused by every call.
   int get(int slot, size_t bytes, void **out);
   void release_all();
@@ -84,6 +85,7 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // host uploads overlapped with passes (lazy)
   Workspace ws;
+  Workspace pinned;  // grow-only pinned host buffers (host = true), by slot
   void *pinned_status = nullptr;  // kPinnedStatusBytes of pinned host memory (lazy)
 };
 

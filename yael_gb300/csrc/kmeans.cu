@@ -211,9 +211,6 @@ struct Engine {
   ~Engine() {
     if (g_assign) cudaGraphExecDestroy(g_assign);
     if (g_update) cudaGraphExecDestroy(g_update);
-    if (ph_counts) cudaFreeHost(ph_counts);
-    if (ph_part) cudaFreeHost(ph_part);
-    if (ph_err) cudaFreeHost(ph_err);
   }
 
   // L1 / chi2 k-means (one instance): per-coordinate distances searched
@@ -337,13 +334,20 @@ struct Engine {
     YG_CUDA(cudaMemcpyAsync(shift, hs.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, st));
     hcounts.resize(ncl);
     hpart.resize(nsl);
-    YG_CUDA(cudaMallocHost(&ph_counts, sizeof(int) * (size_t)ncl));
-    YG_CUDA(cudaMallocHost(&ph_part, sizeof(double) * (size_t)std::max(1, nsl)));
-    YG_CUDA(cudaMallocHost(&ph_err, sizeof(int)));
+    // pinned host buffers of the context (grow-only, kept across calls)
+    YG_CHECK(ctx->pinned.get(0, sizeof(int) * (size_t)ncl, reinterpret_cast<void **>(&ph_counts)));
+    YG_CHECK(ctx->pinned.get(1, sizeof(double) * (size_t)std::max(1, nsl),
+                             reinterpret_cast<void **>(&ph_part)));
+    YG_CHECK(ctx->pinned.get(2, sizeof(int), reinterpret_cast<void **>(&ph_err)));
     *ph_err = 0;
     float hmax = 0.f;
     for (int i = 0; i < ni; i++) hmax = ha[i] > hmax ? ha[i] : (ha[i] >= 0.f ? hmax : NAN);
+    const double ts0 = trace_enabled() ? wall_ms() : 0.0;
     YG_CHECK(setup_tc(hmax));
+    if (trace_enabled()) {
+      YG_CUDA(cudaStreamSynchronize(st));
+      fprintf(stderr, "[yael_gpu] engine set-up: tensor-core packing %.3f ms\n", wall_ms() - ts0);
+    }
     YG_CUDA(cudaStreamSynchronize(st));
     return OK;
   }
@@ -1004,6 +1008,7 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
                             cudaMemcpyDeviceToHost, st));
     YG_CHECK(km_gather(dv, d, sorted, n, vs, st));
     YG_CUDA(cudaStreamSynchronize(st));  // start
+    const double tla = trace_enabled() ? wall_ms() : 0.0;
     Engine E;
     E.ctx = ctx; E.st = st; E.d = d; E.k = bf; E.niter = niter == 0 ? 1000000 : niter;
     E.flags = YAEL_KMEANS_INIT_RANDOM | YAEL_KMEANS_QUIET;
@@ -1030,6 +1035,7 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
       x.done = na < bf;              // small node: no k-means (see yael_gpu_hkm_learn_ex)
     }
     YG_CHECK(E.setup());
+    const double tlb = trace_enabled() ? wall_ms() : 0.0;
     YG_CHECK(E.init_random());
     std::vector<int> iota(bf);
     for (int j = 0; j < bf; j++) iota[j] = j;
@@ -1057,8 +1063,9 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
     YG_LAUNCH_CHECK();
     YG_CUDA(cudaStreamSynchronize(st));
     if (trace_enabled())
-      fprintf(stderr, "[yael_gpu] hkm level %d: %ld nodes, set-up %.3f ms, iterations %.3f ms, "
-              "wrap-up %.3f ms (host clock)\n", l, k, tl1 - tl0, tl2 - tl1, wall_ms() - tl2);
+      fprintf(stderr, "[yael_gpu] hkm level %d: %ld nodes, set-up %.3f ms (grouping %.3f, engine "
+              "%.3f, init %.3f), iterations %.3f ms, wrap-up %.3f ms (host clock)\n", l, k,
+              tl1 - tl0, tla - tl0, tlb - tla, tl1 - tlb, tl2 - tl1, wall_ms() - tl2);
     k *= bf;
   }
   cudaEventRecord(t1, st);

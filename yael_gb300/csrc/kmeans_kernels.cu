@@ -751,6 +751,19 @@ __global__ void gather_kernel(const float *v, int d, const long *rows, long nrow
   C[i] = v[rows[r] * d + (i - r * d)];
 }
 
+// the same for rows of d4 float4 (16-byte aligned rows): a warp per row
+// step, lanes over the row's float4
+__global__ void gather4_kernel(const float4 *v, int d4, const long *rows, long nrows, float4 *C) {
+  const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const long nw = ((long)gridDim.x * blockDim.x) >> 5;
+  for (long r = w; r < nrows; r += nw) {
+    const float4 *src = v + rows[r] * d4;
+    float4 *dst = C + r * d4;
+    for (int c = lane; c < d4; c += 32) dst[c] = __ldg(src + c);
+  }
+}
+
 template <int K, bool VEC>
 int launch_assign(const KmWork *work, int nwork, const float *v, int d, const float *C, int k,
                   const unsigned char *active, int *assign, float *dis, cudaStream_t st) {
@@ -992,18 +1005,26 @@ __global__ void group_count_kernel(const int *key, long n, int k, long chunk, in
   for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) atomicAdd(row + key[i], 1);
 }
 
-// per key b: cnt[c * k + b] := the points of chunks before c with key b;
-// tot[b] = all of them
+// per key b (a warp each, 32 chunks per step): cnt[c * k + b] := the points
+// of chunks before c with key b; tot[b] = all of them
 __global__ void group_prefix_kernel(int *cnt, long nchunk, int k, long *tot) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const long b = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (b >= k) return;
-  long a = 0;
-  for (long c = 0; c < nchunk; c++) {
-    const int x = cnt[c * k + b];
-    cnt[c * k + b] = (int)a;
-    a += x;
+  long base = 0;
+  for (long c0 = 0; c0 < nchunk; c0 += 32) {
+    const long c = c0 + lane;
+    const int x = c < nchunk ? cnt[c * k + b] : 0;
+    int incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (c < nchunk) cnt[c * k + b] = (int)(base + incl - x);
+    base += __shfl_sync(0xffffffffu, incl, 31);
   }
-  tot[b] = a;
+  if (lane == 0) tot[b] = base;
 }
 
 // start[b] = sum of tot[b'] for b' < b (start[k] = n), one thread
@@ -1057,7 +1078,7 @@ int km_group_by_key(const int *key, long n, int k, long *perm, long *start, int 
   YG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)nchunk * k, st));
   group_count_kernel<<<(unsigned)nchunk, 256, 0, st>>>(key, n, k, chunk, cnt);
   YG_LAUNCH_CHECK();
-  group_prefix_kernel<<<(unsigned)ceil_div(k, 128), 128, 0, st>>>(cnt, nchunk, k, tot);
+  group_prefix_kernel<<<(unsigned)ceil_div((long)k * 32, 256), 256, 0, st>>>(cnt, nchunk, k, tot);
   YG_LAUNCH_CHECK();
   group_start_kernel<<<1, 1, 0, st>>>(tot, k, start);
   YG_LAUNCH_CHECK();
@@ -1093,7 +1114,17 @@ int km_slice_sums(const KmSlice *sl, int nsl, const float *dis, double *out, cud
 
 int km_gather(const float *v, int d, const long *rows, long nrows, float *C, cudaStream_t st) {
   if (nrows <= 0) return OK;
-  gather_kernel<<<(unsigned)ceil_div(nrows * d, 256), 256, 0, st>>>(v, d, rows, nrows, C);
+  if (d % 4 == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0 &&
+      (reinterpret_cast<uintptr_t>(C) & 15) == 0) {
+    int dev = 0, sms = 0;
+    YG_CUDA(cudaGetDevice(&dev));
+    YG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const long blocks = std::min<long>(ceil_div(nrows, 8), (long)sms * 16);
+    gather4_kernel<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const float4 *>(v), d / 4,
+                                                    rows, nrows, reinterpret_cast<float4 *>(C));
+  } else {
+    gather_kernel<<<(unsigned)ceil_div(nrows * d, 256), 256, 0, st>>>(v, d, rows, nrows, C);
+  }
   YG_LAUNCH_CHECK();
   return OK;
 }

@@ -44,7 +44,7 @@ int Workspace::get(int slot, size_t bytes, void **out) {
   if (bytes == 0) bytes = 256;
   if (b.n < bytes) {
     if (b.p) {
-      cudaError_t e = cudaFree(b.p);
+      cudaError_t e = host ? cudaFreeHost(b.p) : cudaFree(b.p);
       b.p = nullptr;
       b.n = 0;
       if (e != cudaSuccess) {
@@ -54,12 +54,14 @@ int Workspace::get(int slot, size_t bytes, void **out) {
     }
     size_t n = bytes + bytes / 8;  // headroom so slowly growing sizes do not thrash
     n = (n + 255) & ~(size_t)255;
-    cudaError_t e = test_fail_alloc() ? cudaErrorMemoryAllocation : cudaMalloc(&b.p, n);
+    cudaError_t e = test_fail_alloc() ? cudaErrorMemoryAllocation
+                    : host            ? cudaMallocHost(&b.p, n)
+                                      : cudaMalloc(&b.p, n);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
       b.p = nullptr;
-      set_error(E_NOMEM, "cudaMalloc(%zu bytes, workspace slot %d): %s", n, slot,
-                cudaGetErrorString(e));
+      set_error(E_NOMEM, "%s(%zu bytes, workspace slot %d): %s",
+                host ? "cudaMallocHost" : "cudaMalloc", n, slot, cudaGetErrorString(e));
       return E_NOMEM;
     }
     b.n = n;
@@ -70,7 +72,10 @@ int Workspace::get(int slot, size_t bytes, void **out) {
 
 void Workspace::release_all() {
   for (auto &b : bufs)
-    if (b.p) cudaFree(b.p);
+    if (b.p) {
+      if (host) cudaFreeHost(b.p);
+      else cudaFree(b.p);
+    }
   bufs.clear();
 }
 
@@ -101,6 +106,7 @@ int ctx_get(Ctx **out) {
   c->cc_major = p.major;
   c->cc_minor = p.minor;
   c->smem_optin = p.sharedMemPerBlockOptin;
+  c->pinned.host = true;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
