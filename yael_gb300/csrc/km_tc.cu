@@ -150,12 +150,11 @@ __device__ __forceinline__ bool fixed_shift_ok(float x, int S) {
 // its rounding bound, by FP64 otherwise (lowest index on equal values).  Writes assign / dis and, for the fused sums, the
 // point's move: the centroid it joins to toj and the one it leaves to toa
 // (-1 for none; with P.delta == 0 every point joins and none leaves, else
-// only a point whose centroid changed moves).  Returns true in the lane that
-// wrote a move.
+// only a point whose centroid changed moves).
 // X: the tile's rows (staged, or global from the tile's first point);
 // Ci: the instance's centroid rows (staged or global).
 template <bool CSM>
-__device__ __forceinline__ bool phase_b_decide(const Params &P, const unsigned *bm, int r0,
+__device__ __forceinline__ void phase_b_decide(const Params &P, const unsigned *bm, int r0,
                                                int np, long p0, const float *X, const float *Ci,
                                                int lane, int d, int k, float rho, int *toj) {
   const int r = r0 + (lane >> 1), h = lane & 1;
@@ -305,82 +304,23 @@ __device__ __forceinline__ bool phase_b_decide(const Params &P, const unsigned *
       toj[r] = oj != oa ? oj : -1;
       toj[128 + r] = oj != oa ? oa : -1;
     }
-    return oj != oa;
-  }
-  if (toj && h == 0) {
+  } else if (toj && h == 0) {
     toj[r] = -1;
     toj[128 + r] = -1;
   }
-  return false;
 }
 
-// The fused sums of one tile, after every point's move is in toj (joins:
-// toj[r], leaves: toj[128 + r]): warp ew owns the centroids j = ew (mod 8)
-// and adds (or subtracts) the moving points' fixed-point rows to their sums,
-// lanes over coordinates (lane + 32 i).  An owned centroid's sums are touched
-// by no other warp: plain reads and writes; integer sums, whose result does
-// not depend on the order.  X: the tile's rows.
+// The fused sums of the warp's sixteen points (r0 .. r0 + 15): their moves
+// (joins toj[r], leaves toj[128 + r], written by the warp's own decision),
+// one after another, lanes over coordinates (lane + 32 i), as 64-bit integer
+// atomics into the sums (rows: k x d, in shared memory for an instance whose
+// sums fit there, else the instance's global ones) and counts.  Integer sums,
+// whose result does not depend on the order; the warps need not wait for one
+// another.  X: the tile's rows.
 template <int N32>
-__device__ __forceinline__ void phase_b_sums_owned(const int *toj, int np, const float *X,
-                                                   int ew, int lane, int d, int sh,
-                                                   unsigned long long *sacc, int *scnt) {
-  // the eight words of moves first (independent loads), then their masks
-  int o[8];
-#pragma unroll
-  for (int c = 0; c < 8; c++) o[c] = ((c & 3) * 32 + lane) < np ? toj[c * 32 + lane] : -1;
-  unsigned mk[8];
-#pragma unroll
-  for (int c = 0; c < 8; c++) mk[c] = __ballot_sync(0xffffffffu, o[c] >= 0 && (o[c] & 7) == ew);
-#pragma unroll 1
-  for (int c = 0; c < 8; c++) {
-    const bool leave = c >= 4;
-    unsigned m = mk[0];
-    int oc = o[0];
-#pragma unroll
-    for (int cc = 1; cc < 8; cc++)  // (registers, not a runtime index)
-      if (cc == c) {
-        m = mk[cc];
-        oc = o[cc];
-      }
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      const int j = __shfl_sync(0xffffffffu, oc, b);
-      const float *xr = X + (long)((c & 3) * 32 + b) * d;
-      unsigned long long *row = sacc + (long)j * d;
-      float xv[N32];
-      bool fast = true;
-#pragma unroll
-      for (int i = 0; i < N32; i++) {
-        const int col = lane + 32 * i;
-        xv[i] = col < d ? xr[col] : 0.f;
-        fast = fast && fixed_shift_ok(xv[i], sh);
-      }
-      fast = __all_sync(0xffffffffu, fast);  // almost always: no tiny coordinate
-      long long v[N32];
-#pragma unroll
-      for (int i = 0; i < N32; i++) {
-        const long long f = fast ? fixed_of_shift(xv[i], sh) : fixed_of_nb(xv[i], sh);
-        v[i] = leave ? -f : f;
-      }
-#pragma unroll
-      for (int i = 0; i < N32; i++) {
-        const int col = lane + 32 * i;
-        if (col < d) row[col] += (unsigned long long)v[i];
-      }
-      if (lane == 0) scnt[j] += leave ? -1 : 1;
-      __syncwarp();
-    }
-  }
-}
-
-// The sums straight to the global accumulators (k x d too large for shared
-// memory): the warp's sixteen points' moves, one after another, lanes over
-// coordinates; integer atomics, whose result does not depend on their order.
-template <int N32>
-__device__ __forceinline__ void phase_b_sums_global(const Params &P, const int *toj, int r0,
-                                                    int np, const float *X, int lane, int d,
-                                                    int k, int sh, int inst) {
+__device__ __forceinline__ void phase_b_sums(unsigned long long *rows, int *cnts, const int *toj,
+                                             int r0, int np, const float *X, int lane, int d,
+                                             int sh) {
   // lanes 0-15 the joins of the sixteen points, 16-31 their leaves
   const int r = r0 + (lane & 15);
   const int o = r < np ? toj[(lane >> 4) * 128 + r] : -1;
@@ -391,8 +331,7 @@ __device__ __forceinline__ void phase_b_sums_global(const Params &P, const int *
     const int j = __shfl_sync(0xffffffffu, o, b);
     const bool leave = b >= 16;
     const float *xr = X + (long)(r0 + (b & 15)) * d;
-    const long g = (long)inst * k + j;
-    unsigned long long *row = reinterpret_cast<unsigned long long *>(P.acc) + g * d;
+    unsigned long long *row = rows + (long)j * d;
     float xv[N32];
     bool fast = true;
 #pragma unroll
@@ -401,7 +340,7 @@ __device__ __forceinline__ void phase_b_sums_global(const Params &P, const int *
       xv[i] = col < d ? xr[col] : 0.f;
       fast = fast && fixed_shift_ok(xv[i], sh);
     }
-    fast = __all_sync(0xffffffffu, fast);
+    fast = __all_sync(0xffffffffu, fast);  // almost always: no tiny coordinate
 #pragma unroll
     for (int i = 0; i < N32; i++) {
       const int col = lane + 32 * i;
@@ -410,7 +349,7 @@ __device__ __forceinline__ void phase_b_sums_global(const Params &P, const int *
         atomicAdd(row + col, (unsigned long long)(leave ? -f : f));
       }
     }
-    if (lane == 0) atomicAdd(P.counts + g, leave ? -1 : 1);
+    if (lane == 0) atomicAdd(cnts + j, leave ? -1 : 1);
   }
 }
 
@@ -716,21 +655,19 @@ __global__ void __launch_bounds__(NT, 1)
       const float *Xs = reinterpret_cast<const float *>(Stg + (size_t)xs_s * lay.stage_bytes +
                                                         lay.x_off);
       const float *X = P.xs ? Xs : P.v + u.p0 * d;
-      const bool moved =
-          P.csm ? phase_b_decide<true>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
-                                       fuse ? toj : nullptr)
-                : phase_b_decide<false>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
-                                        fuse ? toj : nullptr);
-      if (sfuse) {
-        // every point's move is in toj (the next tile's are written after the
-        // next per-tile barrier, when every warp is done with these); a tile
-        // without one has no sums to change
-        if (bar_red_or_256(moved)) {
-          phase_b_sums_owned<ND>(toj, u.np, X, ew, lane, d, sh, sacc, scnt);
-        }
-      } else if (fuse) {
-        __syncwarp();
-        phase_b_sums_global<ND>(P, toj, ew * 16, u.np, X, lane, d, k, sh, u.inst);
+      if (P.csm)
+        phase_b_decide<true>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
+                             fuse ? toj : nullptr);
+      else
+        phase_b_decide<false>(P, bl, ew * 16, u.np, u.p0, X, Ci, lane, d, k, rho,
+                              fuse ? toj : nullptr);
+      if (fuse) {
+        __syncwarp();  // the warp's own moves are in toj
+        if (sfuse)
+          phase_b_sums<ND>(sacc, scnt, toj, ew * 16, u.np, X, lane, d, sh);
+        else
+          phase_b_sums<ND>(reinterpret_cast<unsigned long long *>(P.acc) + (long)u.inst * k * d,
+                           P.counts + (long)u.inst * k, toj, ew * 16, u.np, X, lane, d, sh);
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[xs_s]);  // this warp is done with the tile's stage

@@ -98,18 +98,6 @@ __device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity) 
   return true;
 }
 
-// named barrier 1 over the 256 selection threads, with the OR of their flags
-__device__ __forceinline__ bool bar_red_or_256(bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, 256, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)v)
-      : "memory");
-  return r != 0;
-}
-
 // named barrier 1 over the 256 selection threads, with the AND of their flags
 __device__ __forceinline__ bool bar_red_and_256(bool v) {
   uint32_t r;
