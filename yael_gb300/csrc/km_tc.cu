@@ -7,22 +7,27 @@
 // One persistent CTA per SM walks a contiguous range of units (128-point
 // tiles of one instance), so consecutive units mostly share an instance:
 //   warp 0      TMA producer: a ring of S stages, each the tile's packed
-//               16-bit points (Kp/64 blocks of 128 rows x 128 B, 128B swizzle)
-//               and their 16-column side block of ones; the instance's packed
-//               centroids (and their norm parts) in one resident slot,
-//               reloaded when the instance changes and its last MMA is done.
+//               16-bit points (Kp/64 blocks of 128 rows x 128 B, 128B swizzle),
+//               their 16-column side block of ones, their per-point norm and
+//               packing error (1 KB) and, when two stages fit with them, their
+//               FP32 rows (one untiled bulk copy); the instance's packed
+//               centroids (and their norm parts, and their FP32 rows when few)
+//               in one resident slot, reloaded when the instance changes and
+//               its last MMA is done.
 //   warp 1      TMEM owner (two 128 x N FP32 accumulators) and MMA issuer:
 //               Kp/16 tcgen05.mma 128xNx16 per tile plus one K = 16 step over
 //               the side blocks, so the accumulator holds
-//               v_j = ||c_j||^2 - 2 x.c_j of every centroid j.
+//               v_j = ||c_j'||^2 - 2 x'.c_j' of every centroid j (x', c': the
+//               rows less their instance's mean).
 //   warps 2-9   epilogue.  Warps 2-5 (one TMEM lane quadrant each, a thread
-//               per point) find the smallest v and list the band of centroids
+//               per point) find the smallest v and mark the band of centroids
 //               within 2 eps of it (eps: the rigorous error bound of the
-//               16-bit products, the k-NN certificate's bound); all eight
-//               warps then take the points one at a time (a lane per four
-//               coordinates): FP32 direct differences over the band, FP64 on
-//               near ties, the winner's fixed-point row added to the shared
-//               memory sums of its centroid.
+//               16-bit products, the k-NN certificate's bound with the
+//               instance's own centroid norms and errors); all eight warps
+//               then take sixteen points each (two lanes per point): FP32
+//               direct differences over the band, near ties settled by the
+//               sign of the distance difference or FP64, and the points that
+//               change centroid moved in the fixed-point sums (atomics).
 // Every wait is bounded (tc_ptx.cuh); on expiry *err is set, every role leaves
 // its loop, the copies and MMAs already issued are waited for, and TMEM is
 // freed.
