@@ -219,6 +219,19 @@ def test_kmeans_tensor_core_centred_packing(offset, sigma):
     same(g, oracle_kmeans(v, 12, 8, QUIET, 41, 1))
 
 
+def test_kmeans1_full_size_vs_oracle():
+    """The kmeans1 configuration at full size (n = 100k, d = 128, k = 256, 20
+    iterations, random init, seed 0) through the chosen form: assignments,
+    counts and centroids bit-identical to the oracle's exact mode (FP64
+    nearest centroid, exact sums)."""
+    v, _, _ = synth.gaussian_mixture(100_000, 128, 256, 0.15, seed=0)
+    srand48(0)  # seed 0: the k-means seed comes from lrand48()
+    g = gpu_kmeans(v, 256, 20, QUIET, 0, 1, "bf16")
+    assert g["prec_used"] == 3
+    srand48(0)
+    same(g, oracle_kmeans(v, 256, 20, QUIET, 0, 1))
+
+
 def test_kmeans_plus_plus_init():
     g = np.load(os.path.join(GOLDEN, "kmeans_pp.npz"))
     v = g["v"]
