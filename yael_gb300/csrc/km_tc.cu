@@ -326,17 +326,17 @@ template <int N32>
 __device__ __forceinline__ void phase_b_sums(unsigned long long *rows, int *cnts, const int *toj,
                                              int r0, int np, const float *X, int lane, int d,
                                              int sh) {
-  // lanes 0-15 the joins of the sixteen points, 16-31 their leaves
+  // lanes 0-15 hold the sixteen points' (join, leave); a moving point's row
+  // is read and converted once for both
   const int r = r0 + (lane & 15);
-  const int o = r < np ? toj[(lane >> 4) * 128 + r] : -1;
-  unsigned m = __ballot_sync(0xffffffffu, o >= 0);
+  const bool pv = lane < 16 && r < np;
+  const int oj = pv ? toj[r] : -1, oa = pv ? toj[128 + r] : -1;
+  unsigned m = __ballot_sync(0xffffffffu, oj >= 0 || oa >= 0);
   while (m) {
     const int b = __ffs(m) - 1;
     m &= m - 1;
-    const int j = __shfl_sync(0xffffffffu, o, b);
-    const bool leave = b >= 16;
-    const float *xr = X + (long)(r0 + (b & 15)) * d;
-    unsigned long long *row = rows + (long)j * d;
+    const int jn = __shfl_sync(0xffffffffu, oj, b), jo = __shfl_sync(0xffffffffu, oa, b);
+    const float *xr = X + (long)(r0 + b) * d;
     float xv[N32];
     bool fast = true;
 #pragma unroll
@@ -351,10 +351,14 @@ __device__ __forceinline__ void phase_b_sums(unsigned long long *rows, int *cnts
       const int col = lane + 32 * i;
       if (col < d) {
         const long long f = fast ? fixed_of_shift(xv[i], sh) : fixed_of_nb(xv[i], sh);
-        atomicAdd(row + col, (unsigned long long)(leave ? -f : f));
+        if (jn >= 0) atomicAdd(rows + (long)jn * d + col, (unsigned long long)f);
+        if (jo >= 0) atomicAdd(rows + (long)jo * d + col, (unsigned long long)(-f));
       }
     }
-    if (lane == 0) atomicAdd(cnts + j, leave ? -1 : 1);
+    if (lane == 0) {
+      if (jn >= 0) atomicAdd(cnts + jn, 1);
+      if (jo >= 0) atomicAdd(cnts + jo, -1);
+    }
   }
 }
 
