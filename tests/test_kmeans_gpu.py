@@ -192,6 +192,19 @@ def test_kmeans_empty_cluster_splits_both_forms(prec):
     same(r, oracle_kmeans(v, 40, 20, QUIET, 77, 1))
 
 
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_kmeans_large_k_splits(prec):
+    """k = 300 (the k-NN assignment and its short re-rank) on points with many
+    duplicates: random init draws equal centroids, the empty clusters split
+    into pairs ~1e-7 of their norm apart, and the split cluster's points are
+    near ties of the pair, settled by the sign of the distance difference
+    (FP64 where it does not clear its bound); bit-identical to the oracle."""
+    rng = np.random.default_rng(43)
+    v = rng.integers(0, 4, (6000, 6)).astype(np.float32)
+    r = gpu_kmeans(v, 300, 12, QUIET, 91, 1, prec)
+    same(r, oracle_kmeans(v, 300, 12, QUIET, 91, 1))
+
+
 @pytest.mark.parametrize("flags", [QUIET, yg.KMEANS_QUIET | yg.KMEANS_INIT_RANDOM
                                    | yg.KMEANS_NORMALIZE_CENTS])
 def test_kmeans_tensor_core_redo(flags):

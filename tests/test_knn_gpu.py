@@ -61,6 +61,25 @@ def test_golden_float(prec):
     np.testing.assert_array_equal(idx, g["idx_k1"])
 
 
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_k1_near_twin_rows(prec):
+    """Base rows in pairs ~2e-7 of their norm apart (as an empty-cluster split
+    leaves them): a query near a pair is a near tie in FP32, settled by the
+    sign of the two distances' difference; ids identical to the FP64 oracle."""
+    rng = np.random.default_rng(41)
+    b0 = rng.standard_normal((6000, 64)).astype(np.float32)
+    tw = rng.choice(6000, 1500, replace=False)
+    e = (rng.standard_normal((1500, 64)) *
+         (np.linalg.norm(b0[tw], axis=1, keepdims=True) * 1e-7)).astype(np.float32)
+    b = np.concatenate([b0, b0[tw] - e]).astype(np.float32)
+    b[tw] += e
+    q = (b0[rng.choice(tw, 4000)] + 0.05 * rng.standard_normal((4000, 64))).astype(np.float32)
+    idx, dis, _ = gpu_knn(b, q, 1, prec)
+    ridx, rdis, _ = knn_exact(b, q, 1, NT)
+    np.testing.assert_array_equal(idx, ridx)
+    np.testing.assert_allclose(dis, rdis, rtol=5e-6, atol=1e-7)
+
+
 @pytest.mark.parametrize("prec", PRECS + ["bf16x3", "fp16"])
 @pytest.mark.parametrize("nq,nb,d,k", [(1, 1, 1, 1), (7, 5, 3, 5), (33, 300, 129, 17),
                                         (130, 2000, 64, 100), (300, 9000, 96, 33),

@@ -93,6 +93,15 @@ constexpr size_t kPinnedStatusBytes = 4096;
 // the context's pinned status buffer: small device -> host reads stay async
 int ctx_pinned_status(Ctx *c, void **out);
 
+// pinned slots 3 and 4: the staging pieces of copy_to_host
+constexpr int kPinnedStageSlot = 3;
+// Device -> host copy into caller memory, complete on return (the stream is
+// synchronised): pinned or registered memory directly, pageable memory
+// through two 4 MB pinned pieces of the context (the copy of one piece runs
+// while the host copies the previous one out), several times faster than the
+// driver's own staging of a pageable destination.
+int copy_to_host(Ctx *c, cudaStream_t st, void *dst, const void *src, size_t bytes);
+
 // returns the calling thread's context (created on first use)
 int ctx_get(Ctx **out);
 

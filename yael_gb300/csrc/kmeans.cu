@@ -38,7 +38,8 @@ enum KmSlot : int {
   // the small-k tensor-core assignment
   KS_TCU = 160, KS_TCPK, KS_TCSIDE, KS_TCXN, KS_TCXRES, KS_TCCPK, KS_TCCSIDE, KS_TCSTATS,
   KS_TCERR, KS_PRIOR, KS_TCMU, KS_TCMUPART, KS_TCSLF, KS_TCNPT, KS_TCHMAX,
-  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT, KS_TCTSIDE, KS_TCCSCR, KS_TCIB,
+  KS_HSTART, KS_HPINST, KS_GCNT, KS_GTOT, KS_TCTSIDE, KS_TCCSCR, KS_TCIB, KS_SPLITROWS,
+  KS_SPLITBUF,
 };
 
 // ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
@@ -101,10 +102,19 @@ void mul_by(float *v, long n, double s) {
   for (long i = 0; i < n; i++) v[i] *= s;
 }
 
-// kmeans_reassign_empty (yael/kmeans.c:166-209) on a host copy of the centroids
-int reassign_empty(int d, int k, float *C, const int *nassign, unsigned seed) {
+// kmeans_reassign_empty (yael/kmeans.c:166-209) in two halves.  Which row
+// each empty cluster copies depends on the counts and the random stream
+// alone, so the plan (the draws, in the reference's order) comes first; the
+// centroid arithmetic then runs on just the rows the plan touches, gathered
+// from the device, instead of a host copy of all k rows.
+struct SplitStep {
+  int c, j;     // the empty cluster and the row it copies
+  unsigned s2;  // the seed of its perturbation's Gaussian draws
+};
+
+int split_plan(int k, const int *nassign, unsigned seed, std::vector<SplitStep> &plan) {
   int nre = 0;
-  std::vector<float> p(k), eps(d);
+  std::vector<float> p(k);
   for (int c = 0; c < k; c++) {
     // nassign^2 - 1 in int arithmetic (wraps for large clusters, like the reference)
     const unsigned sq = (unsigned)nassign[c] * (unsigned)nassign[c] - 1u;
@@ -120,17 +130,37 @@ int reassign_empty(int d, int k, float *C, const int *nassign, unsigned seed) {
       rd -= p[j];
       if (rd < 0) break;
     }
-    memcpy(C + (long)c * d, C + (long)j * d, sizeof(float) * d);
-    const double s = l2(C + (long)j * d, d) * 0.0000001;
-    unsigned s2 = rand_r(&seed);
-    for (int i = 0; i < d; i++) eps[i] = (float)gaussrand_r_(&s2);
-    mul_by(eps.data(), d, s);
-    for (int i = 0; i < d; i++) C[(long)j * d + i] += eps[i];
-    for (int i = 0; i < d; i++) C[(long)c * d + i] -= eps[i];
+    plan.push_back(SplitStep{c, j, (unsigned)rand_r(&seed)});
     p[j] = 0;
     mul_by(p.data(), k, 1. / l1(p.data(), k));
   }
   return nre;
+}
+
+// One instance's steps on its rows: row r of the instance at R + slot[r] * d
+// (every row a step names has a slot).  The same operations, in the same
+// order, as on the full array: copy, norm of the source, perturbation
+// added to the source and subtracted from the copy.
+void split_apply(int d, const SplitStep *st, int nst, float *R, const int *slot) {
+  std::vector<float> eps(d);
+  for (int t = 0; t < nst; t++) {
+    float *rc = R + (long)slot[st[t].c] * d, *rj = R + (long)slot[st[t].j] * d;
+    if (rc != rj) memcpy(rc, rj, sizeof(float) * d);
+    const double s = l2(rj, d) * 0.0000001;
+    unsigned s2 = st[t].s2;
+    for (int i = 0; i < d; i++) eps[i] = (float)gaussrand_r_(&s2);
+    mul_by(eps.data(), d, s);
+    for (int i = 0; i < d; i++) rj[i] += eps[i];
+    for (int i = 0; i < d; i++) rc[i] -= eps[i];
+  }
+}
+
+__global__ void scatter_rows64_kernel(const float *src, const long *rows, long m, int d,
+                                      float *dst) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m * d) return;
+  const long r = t / d;
+  dst[rows[r] * d + (t - r * d)] = src[t];
 }
 
 int fixed_shift(long n, float maxabs) {
@@ -718,8 +748,10 @@ struct Engine {
     }
 
     nv.reset(new NvtxRange("kmeans.split_and_stop"));
-    std::vector<float> hc;
-    bool any_split = false;
+    // the splits: planned per instance here, applied to the rows they touch
+    // after the loop (an instance's steps touch its own rows only)
+    std::vector<SplitStep> plan;
+    std::vector<int> plan_inst, plan_at;  // instance, first step
     for (int i = 0; i < ni; i++) {
       Instance &x = in[i];
       if (x.done) continue;
@@ -730,15 +762,9 @@ struct Engine {
       for (int c = 0; c < k; c++) empty |= cnt[c] == 0;
       int nre = 0;
       if (empty) {
-        hc.resize((size_t)k * d);
-        YG_CUDA(cudaMemcpyAsync(hc.data(), C + (long)i * k * d, sizeof(float) * k * d,
-                                cudaMemcpyDeviceToHost, st));
-        YG_CUDA(cudaStreamSynchronize(st));
-        nre = reassign_empty(d, k, hc.data(), cnt, sseed);
-        YG_CUDA(cudaMemcpyAsync(C + (long)i * k * d, hc.data(), sizeof(float) * k * d,
-                                cudaMemcpyHostToDevice, st));
-        YG_CUDA(cudaStreamSynchronize(st));
-        any_split = true;
+        plan_inst.push_back(i);
+        plan_at.push_back((int)plan.size());
+        nre = split_plan(k, cnt, sseed, plan);
         if (nre > 0 && verbose)
           fprintf(stderr, "# kmeans warning: %d empty clusters -> split\n", nre);
       }
@@ -761,8 +787,52 @@ struct Engine {
       }
       if (x.iters >= niter) x.done = true;
     }
-    (void)any_split;
+    if (!plan.empty()) YG_CHECK(apply_splits(plan, plan_inst, plan_at));
     return set_active();
+  }
+
+  // the planned splits on the device centroids: the rows they touch
+  // gathered, split on the host, put back
+  int apply_splits(const std::vector<SplitStep> &plan, const std::vector<int> &pinst,
+                   const std::vector<int> &pat) {
+    std::vector<long> rows;
+    std::vector<int> slot((size_t)k, -1);
+    std::vector<int> first(pinst.size() + 1);
+    // rows in instance order, each instance's slots its own
+    for (size_t b = 0; b < pinst.size(); b++) {
+      first[b] = (int)rows.size();
+      const int e = b + 1 < pinst.size() ? pat[b + 1] : (int)plan.size();
+      for (int t = pat[b]; t < e; t++)
+        for (int r : {plan[t].c, plan[t].j})
+          if (slot[r] < 0) {
+            slot[r] = (int)rows.size() - first[b];
+            rows.push_back((long)pinst[b] * k + r);
+          }
+      for (int t = pat[b]; t < e; t++) slot[plan[t].c] = slot[plan[t].j] = -1;
+    }
+    first[pinst.size()] = (int)rows.size();
+    const long m = (long)rows.size();
+    long *drows;
+    float *dbuf;
+    YG_CHECK(ws_get(ctx->ws, KS_SPLITROWS, (size_t)m, &drows));
+    YG_CHECK(ws_get(ctx->ws, KS_SPLITBUF, (size_t)m * d, &dbuf));
+    std::vector<float> R((size_t)m * d);
+    YG_CUDA(cudaMemcpyAsync(drows, rows.data(), sizeof(long) * m, cudaMemcpyHostToDevice, st));
+    YG_CHECK(km_gather(C, d, drows, m, dbuf, st));
+    YG_CUDA(cudaMemcpyAsync(R.data(), dbuf, sizeof(float) * m * d, cudaMemcpyDeviceToHost, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    for (size_t b = 0; b < pinst.size(); b++) {
+      const int e = b + 1 < pinst.size() ? pat[b + 1] : (int)plan.size();
+      for (int r = first[b]; r < first[b + 1]; r++) slot[rows[r] - (long)pinst[b] * k] = r - first[b];
+      split_apply(d, plan.data() + pat[b], e - pat[b], R.data() + (size_t)first[b] * d,
+                  slot.data());
+      for (int r = first[b]; r < first[b + 1]; r++) slot[rows[r] - (long)pinst[b] * k] = -1;
+    }
+    YG_CUDA(cudaMemcpyAsync(dbuf, R.data(), sizeof(float) * m * d, cudaMemcpyHostToDevice, st));
+    scatter_rows64_kernel<<<(unsigned)ceil_div(m * d, 256), 256, 0, st>>>(dbuf, drows, m, d, C);
+    YG_LAUNCH_CHECK();
+    YG_CUDA(cudaStreamSynchronize(st));  // R is a stack buffer
+    return OK;
   }
 
   bool all_done() const {
@@ -773,10 +843,10 @@ struct Engine {
 };
 
 // D2H of whichever outputs are requested (device or host destinations)
-int copy_out(cudaStream_t st, void *dst, const void *src, size_t bytes, bool dev) {
+int copy_out(Ctx *ctx, cudaStream_t st, void *dst, const void *src, size_t bytes, bool dev) {
   if (!dst || bytes == 0) return OK;
-  YG_CUDA(cudaMemcpyAsync(dst, src, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                          st));
+  if (!dev) return copy_to_host(ctx, st, dst, src, bytes);
+  YG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
   return OK;
 }
 
@@ -855,6 +925,9 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
     set_error(E_ARG, "kmeans: k=%d n=%d d=%d (the reference asserts k <= n)", k, n, d);
     return E_ARG;
   }
+  const bool tr = trace_enabled();
+  const double t_call = tr ? wall_ms() : 0.0;
+  double t_init = 0.0, t_iter = 0.0;
   const float *v = v_in;
   if (!dev) {
     float *dv;
@@ -877,6 +950,8 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
     E.probe = xo;
   }
   YG_CHECK(E.setup());
+  if (tr) YG_CUDA(cudaStreamSynchronize(st));
+  const double t_setup = tr ? wall_ms() : 0.0;
   double best = HUGE_VAL;
   long iter_tot = 0;
   int core_ret = 0;
@@ -885,6 +960,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
   std::vector<int> bnassign(k);
   for (int run = 0; run < redo; run++) {
     if (verbose) printf("<><><><> kmeans / run %d <><><><><>\n", run);
+    const double t_r0 = tr ? wall_ms() : 0.0;
     Instance &x = E.in[0];
     if (user) {
       YG_CUDA(cudaMemcpyAsync(E.C, C_out, sizeof(float) * (size_t)k * d,
@@ -911,7 +987,14 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
     E.tc_live = false;
     x.qerr = HUGE_VAL; x.qerr_old = HUGE_VAL;
     YG_CHECK(E.set_active());
+    if (tr) YG_CUDA(cudaStreamSynchronize(st));
+    const double t_run = tr ? wall_ms() : 0.0;
     while (!E.all_done()) YG_CHECK(E.iterate());
+    if (tr) {
+      const double t_end = wall_ms();
+      t_init += t_run - t_r0;
+      t_iter += t_end - t_run;
+    }
     if (verbose) printf("\n");
     iter_tot += x.iters;
     core_ret = x.ret;
@@ -932,6 +1015,7 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
       bnassign.assign(E.hcounts.begin(), E.hcounts.begin() + k);
     }
   }
+  const double t_loop = tr ? wall_ms() : 0.0;
   if (trace_enabled())
     fprintf(stderr,
             "[yael_gpu] kmeans n=%d k=%d d=%d iterations=%ld assign=%.3fms update=%.3fms "
@@ -949,15 +1033,20 @@ int kmeans_run(int d, int n, int k, int niter, const float *v_in, int flags, lon
     printf("Unbalanced factor of last iteration: %g\n", uf * k / (tot * tot));
   }
   if (best < HUGE_VAL && bC) {
-    YG_CHECK(copy_out(st, C_out, bC, sizeof(float) * (size_t)k * d, dev));
-    YG_CHECK(copy_out(st, dis_out, bdis, sizeof(float) * (size_t)n, dev));
-    YG_CHECK(copy_out(st, assign_out, bassign, sizeof(int) * (size_t)n, dev));
+    YG_CHECK(copy_out(ctx, st, C_out, bC, sizeof(float) * (size_t)k * d, dev));
+    YG_CHECK(copy_out(ctx, st, dis_out, bdis, sizeof(float) * (size_t)n, dev));
+    YG_CHECK(copy_out(ctx, st, assign_out, bassign, sizeof(int) * (size_t)n, dev));
     if (nassign_out) {
       YG_CUDA(cudaMemcpyAsync(nassign_out, bnassign.data(), sizeof(int) * k,
                               dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost, st));
     }
   }
   YG_CUDA(cudaStreamSynchronize(st));
+  if (tr)
+    fprintf(stderr,
+            "[yael_gpu] kmeans call: set-up %.3f ms, init %.3f ms, iterations %.3f ms, wrap-up "
+            "%.3f ms (host clock)\n",
+            t_setup - t_call, t_init, t_iter, wall_ms() - t_loop);
   if (iters_out) *iters_out = iter_tot;
   if (fallback_out) *fallback_out = E.n_fallback;
   if (second_out) *second_out = E.n_second;
@@ -1067,11 +1156,9 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
     stats.ms_update += E.ms_update;
     stats.prec_used = E.prec_used;
     // centroids of this level, then node = node * bf + child
-    YG_CUDA(cudaMemcpyAsync(levels_out[l], E.C, sizeof(float) * (size_t)k * bf * d,
-                            cudaMemcpyDeviceToHost, st));
     node_update_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(sorted, E.assign, n, bf, node);
     YG_LAUNCH_CHECK();
-    YG_CUDA(cudaStreamSynchronize(st));
+    YG_CHECK(copy_to_host(ctx, st, levels_out[l], E.C, sizeof(float) * (size_t)k * bf * d));
     if (trace_enabled())
       fprintf(stderr, "[yael_gpu] hkm level %d: %ld nodes, set-up %.3f ms (grouping %.3f, engine "
               "%.3f, init %.3f), iterations %.3f ms, wrap-up %.3f ms (host clock)\n", l, k,
@@ -1083,10 +1170,7 @@ int hkm_run(int n, int d, int nlevel, int bf, const float *points, int niter, bo
   if (ms_out) cudaEventElapsedTime(ms_out, t0, t1);
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
-  if (assign_out) {
-    YG_CHECK(copy_out(st, assign_out, node, sizeof(int) * (size_t)n, false));
-    YG_CUDA(cudaStreamSynchronize(st));
-  }
+  if (assign_out) YG_CHECK(copy_to_host(ctx, st, assign_out, node, sizeof(int) * (size_t)n));
   if (iters_out) *iters_out = iters;
   stats.instance_iterations = iters;
   g_last_stats = stats;

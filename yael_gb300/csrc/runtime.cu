@@ -3,6 +3,7 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -130,6 +131,54 @@ int ctx_pinned_status(Ctx *c, void **out) {
   }
   *out = c->pinned_status;
   return OK;
+}
+
+int copy_to_host(Ctx *c, cudaStream_t st, void *dst, const void *src, size_t bytes) {
+  if (!dst || bytes == 0) return OK;
+  cudaPointerAttributes at;
+  const cudaError_t ea = cudaPointerGetAttributes(&at, dst);
+  if (ea != cudaSuccess) (void)cudaGetLastError();
+  if (ea == cudaSuccess && at.type != cudaMemoryTypeUnregistered) {
+    YG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st));
+    YG_CUDA(cudaStreamSynchronize(st));
+    return OK;
+  }
+  constexpr size_t kPiece = (size_t)4 << 20;
+  void *stage[2];
+  for (int i = 0; i < 2; i++)
+    YG_CHECK(c->pinned.get(kPinnedStageSlot + i, std::min(bytes, kPiece), &stage[i]));
+  cudaEvent_t ev[2];
+  for (int i = 0; i < 2; i++) YG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+  int rc = OK;
+  size_t prev_off = 0, prev_len = 0;
+  int i = 0;
+  for (size_t off = 0; off < bytes && rc == OK; off += kPiece, i++) {
+    const size_t len = std::min(kPiece, bytes - off);
+    cudaError_t e = cudaMemcpyAsync(stage[i & 1], static_cast<const char *>(src) + off, len,
+                                    cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[i & 1], st);
+    if (e == cudaSuccess && i > 0) e = cudaEventSynchronize(ev[(i - 1) & 1]);
+    if (e != cudaSuccess) {
+      set_error(E_CUDA, "copy_to_host: %s", cudaGetErrorString(e));
+      rc = E_CUDA;
+      break;
+    }
+    if (i > 0) memcpy(static_cast<char *>(dst) + prev_off, stage[(i - 1) & 1], prev_len);
+    prev_off = off;
+    prev_len = len;
+  }
+  if (rc == OK && prev_len) {
+    const cudaError_t e = cudaEventSynchronize(ev[(i - 1) & 1]);
+    if (e != cudaSuccess) {
+      set_error(E_CUDA, "copy_to_host: %s", cudaGetErrorString(e));
+      rc = E_CUDA;
+    } else {
+      memcpy(static_cast<char *>(dst) + prev_off, stage[(i - 1) & 1], prev_len);
+    }
+  }
+  if (rc != OK) (void)cudaStreamSynchronize(st);  // nothing in flight into the stage
+  for (int j = 0; j < 2; j++) cudaEventDestroy(ev[j]);
+  return rc;
 }
 
 int default_precision() {

@@ -370,19 +370,77 @@ __device__ __forceinline__ float group_dist32(const float *qv, const float *brow
   return acc;
 }
 
+// Two base rows at once (their loads overlap): each value is the one
+// group_dist32 gives, the same per-lane order and the same butterfly.
+template <int G>
+__device__ __forceinline__ void group_dist32x2(const float *qv, const float *ra, const float *rb,
+                                               int d, int metric, unsigned gm, float &ea,
+                                               float &eb) {
+  const int gl = threadIdx.x & (G - 1);
+  float aa = 0.f, ab = 0.f;
+  for (int c = gl; c < d; c += G) {
+    const float va = __ldg(ra + c), vb = __ldg(rb + c), x = qv[c];
+    if (metric == METRIC_L2) {
+      const float ta = x - va, tb = x - vb;
+      aa = fmaf(ta, ta, aa);
+      ab = fmaf(tb, tb, ab);
+    } else {
+      aa = fmaf(x, va, aa);
+      ab = fmaf(x, vb, ab);
+    }
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    aa += __shfl_xor_sync(gm, aa, o);
+    ab += __shfl_xor_sync(gm, ab, o);
+  }
+  ea = aa;
+  eb = ab;
+}
+
+// D_a - D_b = sum_c (a_c - b_c)(a_c + b_c - 2 x_c) for base rows a, b, in
+// FP32 without contraction, the group's lanes over strided coordinates then a
+// butterfly (every term goes through at most d / G + log2 G <= d + 7
+// additions), with the two sums its rounding bound needs: sum |t| and
+// sum |a - b| |a + b| (t the rounded terms).
+template <int G>
+__device__ __forceinline__ void group_pair_diff(const float *qv, const float *ra, const float *rb,
+                                                int d, unsigned gm, float &dl, float &st,
+                                                float &sps) {
+  const int gl = threadIdx.x & (G - 1);
+  float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+  for (int c = gl; c < d; c += G) {
+    const float av = __ldg(ra + c), bv = __ldg(rb + c), x = qv[c];
+    const float pp = __fsub_rn(av, bv), s1 = __fadd_rn(av, bv);
+    const float tt = __fmul_rn(pp, __fsub_rn(s1, __fadd_rn(x, x)));
+    t0 = __fadd_rn(t0, tt);
+    t1 = __fadd_rn(t1, fabsf(tt));
+    t2 = __fadd_rn(t2, __fmul_rn(fabsf(pp), fabsf(s1)));
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    t0 = __fadd_rn(t0, __shfl_xor_sync(gm, t0, o));
+    t1 = __fadd_rn(t1, __shfl_xor_sync(gm, t1, o));
+    t2 = __fadd_rn(t2, __shfl_xor_sync(gm, t2, o));
+  }
+  dl = t0;
+  st = t1;
+  sps = t2;
+}
+
 __device__ __forceinline__ double ord2d(unsigned long long k) {
   const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
   return __longlong_as_double((long long)u);
 }
 
+// One query q by its group of G lanes; returns the number of candidates the
+// re-rank looked at (in the group's first lane, 0 elsewhere).
 template <int G>
-__global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
-  constexpr int QPB = 256 / G;  // queries per block
+__device__ __forceinline__ unsigned rerank_small_query(const RerankArgs &a, int q) {
   const int gl = threadIdx.x & (G - 1);
   const int gbase = (threadIdx.x & 31) & ~(G - 1);  // first lane of the group in its warp
   const unsigned gm = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gbase);
-  const int q = blockIdx.x * QPB + (int)(threadIdx.x / G);
-  if (q >= a.nq) return;  // uniform per group
+  unsigned ncand = 0;
   auto gballot = [&](bool p) -> unsigned {
     const unsigned b = __ballot_sync(gm, p);
     return G == 32 ? b : (b >> gbase) & ((1u << G) - 1u);
@@ -438,11 +496,7 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
   bool ok = nvalid >= k && gballot(overflow) == 0u;
   float kth_hi = INFINITY;  // upper bound of the k-th exact distance, when found
   if (ok) {
-    if (a.n_cand) {  // one atomic per set of converged lanes, not per query
-      const unsigned am = __activemask();
-      const unsigned tot = __reduce_add_sync(am, gl == 0 ? (unsigned)nvalid : 0u);
-      if ((int)(threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(a.n_cand, (unsigned long long)tot);
-    }
+    if (gl == 0) ncand = (unsigned)nvalid;
     group_sort<G>(key, id, gm);
     if (ex) {
       // THRESH: non-candidates are above thr, so the sorted prefix is the answer
@@ -463,12 +517,16 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
       const double lim = (double)ak + 2.0 * (double)eps + 4e-7 * fabs((double)ak) + 1e-30;
       const bool inband = id != 0x7fffffff && (double)ord2f((unsigned)key) <= lim;
       const int nband = __popc(gballot(inband));
-      // FP32 re-rank of the band, one candidate at a time across the group
+      // FP32 re-rank of the band, two candidates at a time across the group
       float e = INFINITY;
-      for (int c = 0; c < nband; c++) {
-        const int cid = __shfl_sync(gm, id, c, G);
-        const float ec = group_dist32<G>(qv, a.b + (long)cid * a.ldb, d, a.metric, gm);
-        if (gl == c) e = ec;
+      for (int c = 0; c < nband; c += 2) {
+        const int ca = __shfl_sync(gm, id, c, G);
+        const int cb = __shfl_sync(gm, id, imin(c + 1, nband - 1), G);
+        float ea, eb;
+        group_dist32x2<G>(qv, a.b + (long)ca * a.ldb, a.b + (long)cb * a.ldb, d, a.metric, gm,
+                          ea, eb);
+        if (gl == c) e = ea;
+        if (gl == c + 1) e = eb;
       }
       key = gl < nband ? (unsigned long long)f2ord(e) : ~0ull;
       if (gl >= nband) id = 0x7fffffff;
@@ -480,8 +538,40 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
       const float e0 = ord2f((unsigned)key);
       const float e1 = ord2f((unsigned)__shfl_down_sync(gm, key, 1, G));
       const bool tie = gl < imin(k, nband - 1) && (e1 - e0 <= rho * (fabsf(e0) + fabsf(e1)) + 2.f * eta);
+      bool need64 = __any_sync(gm, tie);
+      if (need64 && k == 1 && L2) {
+        // A near tie of the best two alone (the third, if any, clearly worse
+        // than the best): the sign of D_a - D_b = sum_c (a_c - b_c)(a_c +
+        // b_c - 2 x_c) in FP32 with its rounding bound.  Per coordinate
+        // p = fl(a - b), s = fl(a + b), t = fl(p fl(s - 2x)) is within
+        // u (|p| |s| + 3 |t|) of its exact term to first order, and the sum
+        // adds at most (d + 7) u |t| per term, so |dl - (D_a - D_b)| <=
+        // 1.02 u (sum |p| |s| + (d + 10) sum |t|); past that and the rounding
+        // of the two FP64 sequential sums that decide a tie (each within
+        // (d + 2) 2^-53 of its value), FP64 finds the same order.  Typically
+        // the two halves of a split centroid, ~1e-7 of their norm apart.
+        const float ea = ord2f((unsigned)__shfl_sync(gm, key, 0, G));
+        const float eb = ord2f((unsigned)__shfl_sync(gm, key, 1, G));
+        const float ec = nband > 2 ? ord2f((unsigned)__shfl_sync(gm, key, 2, G)) : INFINITY;
+        if (!(ec < INFINITY && ec - ea <= rho * (ea + ec))) {
+          const int ja = __shfl_sync(gm, id, 0, G), jb = __shfl_sync(gm, id, 1, G);
+          float dl, st, sps;
+          group_pair_diff<G>(qv, a.b + (long)ja * a.ldb, a.b + (long)jb * a.ldb, d, gm, dl, st,
+                             sps);
+          const float bound = 1.02f * kU * (sps + (float)(d + 10) * st) +
+                              (float)(d + 4) * 1.12e-16f * (ea + eb) * 1.1f;
+          if (fabsf(dl) > bound) {
+            need64 = false;
+            if (dl > 0.f) {  // b is nearer: it takes the first place
+              const unsigned long long ko = __shfl_xor_sync(gm, key, 1);
+              const int io = __shfl_xor_sync(gm, id, 1);
+              if (gl < 2) { key = ko; id = io; }
+            }
+          }
+        }
+      }
       double ek_hi;
-      if (__any_sync(gm, tie)) {
+      if (need64) {
         // FP64, sequential over coordinates, for the whole band
         unsigned long long k64 = ~0ull;
         if (gl < nband) k64 = d2ord(dist64_seq(qv, a.b + (long)id * a.ldb, d, a.metric));
@@ -540,6 +630,37 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
     const int pos = atomicAdd(a.fail_cnt, 1);
     a.fail_list[pos] = q;
     if (a.kth_out) a.kth_out[q] = kth_hi;
+  }
+  return ncand;
+}
+
+// A group of G lanes per query; the candidate count goes to a.n_cand once
+// per block, from the block's last warp to finish (no barrier at the end: a
+// warp whose queries are done leaves at once, however long the others take).
+template <int G>
+__global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
+  constexpr int QPB = 256 / G;  // queries per block
+  __shared__ unsigned long long s_cand;
+  __shared__ unsigned s_done;
+  if (threadIdx.x == 0) {
+    s_cand = 0;
+    s_done = 0;
+  }
+  __syncthreads();
+  const int q = blockIdx.x * QPB + (int)(threadIdx.x / G);
+  unsigned nc = 0;
+  if (q < a.nq) nc = rerank_small_query<G>(a, q);  // uniform per group
+  if (a.n_cand) {
+    const unsigned w = __reduce_add_sync(0xffffffffu, nc);
+    if ((threadIdx.x & 31) == 0) {
+      if (w) atomicAdd(&s_cand, (unsigned long long)w);
+      __threadfence_block();
+      if (atomicAdd(&s_done, 1u) == blockDim.x / 32 - 1) {
+        __threadfence_block();
+        const unsigned long long t = atomicAdd(&s_cand, 0ull);  // every warp's count is in
+        if (t) atomicAdd(a.n_cand, t);
+      }
+    }
   }
 }
 
