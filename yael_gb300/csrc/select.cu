@@ -634,10 +634,234 @@ __device__ __forceinline__ unsigned rerank_small_query(const RerankArgs &a, int 
   return ncand;
 }
 
-// A group of G lanes per query; the candidate count goes to a.n_cand once
-// per block, from the block's last warp to finish (no barrier at the end: a
-// warp whose queries are done leaves at once, however long the others take).
+// The lexicographic minimum of (key, id) over the group's lanes (ids as
+// unsigned), by two reductions: the least key, then the least id holding it.
 template <int G>
+__device__ __forceinline__ void group_argmin(unsigned key, int id, unsigned gm, unsigned &mk,
+                                             int &mi) {
+  mk = __reduce_min_sync(gm, key);
+  mi = (int)__reduce_min_sync(gm, key == mk ? (unsigned)id : 0xffffffffu);
+}
+
+// rerank_small_query for k = 1 (the k-means assignment): the same candidates,
+// band, distances, tie rules, certificate and outputs, with the orderings
+// the general form takes from two sorts of the group's lanes read off by
+// reductions instead (the least, second and third (value, id) of the band).
+template <int G>
+__device__ __forceinline__ unsigned rerank_small_k1(const RerankArgs &a, int q) {
+  const int gl = threadIdx.x & (G - 1);
+  const int gbase = (threadIdx.x & 31) & ~(G - 1);  // first lane of the group in its warp
+  const unsigned gm = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+  unsigned ncand = 0;
+  auto gballot = [&](bool p) -> unsigned {
+    const unsigned b = __ballot_sync(gm, p);
+    return G == 32 ? b : (b >> gbase) & ((1u << G) - 1u);
+  };
+  const ScanSel &s = a.sel;
+  const bool thresh = s.mode == SCAN_THRESH;
+  const int d = a.d;
+  const bool L2 = a.metric == METRIC_L2;
+  const double qn = L2 ? a.qn64[q] : 0.0;
+  const float eps = a.eps ? a.eps[q] : 0.f;
+  const bool ex = a.qexact ? a.qexact[q] != 0 : false;
+  const float *qv = a.q + (long)q * a.ldq;
+
+  unsigned key = 0xffffffffu;  // f2ord of the approximate value
+  int id = 0x7fffffff;         // 0x7fffffff: no candidate in this lane
+  unsigned long long tkey = ~0ull;
+  bool overflow = false;
+  if (thresh) {
+    if (gl < s.nregion() * s.cap) {
+      const int r = gl / s.cap, sl = gl - r * s.cap;
+      const int cnt = s.cnt[(long)r * a.nq + q];
+      overflow = cnt > s.cap;
+      if (sl < cnt && sl < s.cap) {
+        const long o = ((long)r * a.nq + q) * s.cap + sl;
+        const float v = s.candv[o];
+        key = f2ord(L2 ? (float)((double)v + qn) : v);
+        id = s.candi[o];
+      }
+    }
+  } else {
+    const int M = s.nchunk * s.C;
+    unsigned tk = 0xffffffffu, ti = 0xffffffffu;
+    if (gl < M) {
+      const int ch = gl / s.C, sl = gl - ch * s.C;
+      const long o = ((long)ch * a.nq + q) * s.C + sl;
+      const int j = s.topi[o];
+      if (j >= 0) {
+        const float v = s.topv[o];
+        const float av = L2 ? (float)((double)v + qn) : v;
+        key = f2ord(av);
+        id = j;
+        if (sl == s.C - 1) { tk = key; ti = (unsigned)j; }
+      }
+    }
+    // boundary: smallest (value, id) that closes a full chunk list
+    const unsigned mtk = __reduce_min_sync(gm, tk);
+    const unsigned mti = __reduce_min_sync(gm, tk == mtk ? ti : 0xffffffffu);
+    tkey = ((unsigned long long)mtk << 32) | mti;
+  }
+  const bool valid = id != 0x7fffffff;
+  const int nvalid = __popc(gballot(valid));
+  bool ok = nvalid >= 1 && gballot(overflow) == 0u;
+  float kth_hi = INFINITY;  // upper bound of the exact nearest distance, when found
+  if (ok) {
+    if (gl == 0) ncand = (unsigned)nvalid;
+    unsigned k0;
+    int i0;
+    group_argmin<G>(key, id, gm, k0, i0);
+    if (ex) {
+      // THRESH: non-candidates are above thr, so the least is the answer
+      if (!thresh && tkey != ~0ull) {
+        const unsigned tk = (unsigned)(tkey >> 32);
+        const unsigned tid_b = (unsigned)(tkey & 0xffffffffu);
+        ok = k0 < tk || (k0 == tk && (unsigned)i0 <= tid_b);
+        kth_hi = ord2f(k0);  // exact values
+      }
+      if (ok && gl == 0) {
+        a.out_idx[q] = i0;
+        a.out_dis[q] = ord2f(k0);
+      }
+    } else {
+      const float ak = ord2f(k0);
+      const double lim = (double)ak + 2.0 * (double)eps + 4e-7 * fabs((double)ak) + 1e-30;
+      const bool inband = valid && (double)ord2f(key) <= lim;
+      const unsigned bmask = gballot(inband);
+      const int nband = __popc(bmask);
+      // FP32 distances of the band's members, two at a time across the group
+      float e = INFINITY;
+      for (unsigned m = bmask; m;) {
+        const int la = __ffs(m) - 1;
+        m &= m - 1;
+        const int lb = m ? __ffs(m) - 1 : la;
+        if (m) m &= m - 1;
+        const int ca = __shfl_sync(gm, id, la, G);
+        const int cb = __shfl_sync(gm, id, lb, G);
+        float ea, eb;
+        group_dist32x2<G>(qv, a.b + (long)ca * a.ldb, a.b + (long)cb * a.ldb, d, a.metric, gm,
+                          ea, eb);
+        if (gl == la) e = ea;
+        if (gl == lb) e = eb;
+      }
+      const unsigned ek32 = inband ? f2ord(e) : 0xffffffffu;
+      const int eid = inband ? id : 0x7fffffff;
+      unsigned e0k, e1k = 0xffffffffu, e2k = 0xffffffffu;
+      int j0, j1 = 0x7fffffff;
+      group_argmin<G>(ek32, eid, gm, e0k, j0);
+      if (nband > 1) {
+        const bool r1 = eid != j0;
+        group_argmin<G>(r1 ? ek32 : 0xffffffffu, r1 ? eid : 0x7fffffff, gm, e1k, j1);
+      }
+      const float rho = (float)(d + 4) * kU;
+      float eta = 0.f;
+      if (!L2) eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64[q], 0.0)) *
+                     __uint_as_float(a.bstats->max_norm_bits);
+      const float e0 = ord2f(e0k), e1 = ord2f(e1k);
+      bool need64 = nband > 1 && (e1 - e0 <= rho * (fabsf(e0) + fabsf(e1)) + 2.f * eta);
+      unsigned wk = e0k;
+      int wj = j0;
+      if (need64 && L2) {
+        // the near tie of the best two alone, settled by the sign of their
+        // distance difference (rerank_small_query gives the bound)
+        if (nband > 2) {
+          const bool r2 = eid != j0 && eid != j1;
+          e2k = __reduce_min_sync(gm, r2 ? ek32 : 0xffffffffu);
+        }
+        const float ec = nband > 2 ? ord2f(e2k) : INFINITY;
+        if (!(ec < INFINITY && ec - e0 <= rho * (e0 + ec))) {
+          float dl, st, sps;
+          group_pair_diff<G>(qv, a.b + (long)j0 * a.ldb, a.b + (long)j1 * a.ldb, d, gm, dl, st,
+                             sps);
+          const float bound = 1.02f * kU * (sps + (float)(d + 10) * st) +
+                              (float)(d + 4) * 1.12e-16f * (e0 + e1) * 1.1f;
+          if (fabsf(dl) > bound) {
+            need64 = false;
+            if (dl > 0.f) { wk = e1k; wj = j1; }
+          }
+        }
+      }
+      double ek_hi;
+      if (need64) {
+        // FP64, sequential over coordinates, for the whole band
+        unsigned long long k64 = ~0ull;
+        int i64 = 0x7fffffff;
+        if (inband) {
+          k64 = d2ord(dist64_seq(qv, a.b + (long)id * a.ldb, d, a.metric));
+          i64 = id;
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+          const unsigned long long pk = __shfl_xor_sync(gm, k64, o);
+          const int pi = __shfl_xor_sync(gm, i64, o);
+          if (lex_less(pk, pi, k64, i64)) { k64 = pk; i64 = pi; }
+        }
+        const double ek = ord2d(k64);
+        ek_hi = ek + 1e-12 * fabs(ek);
+        if (gl == 0) {
+          a.out_idx[q] = i64;
+          a.out_dis[q] = (float)ek;
+        }
+      } else {
+        const float ek = ord2f(wk);
+        ek_hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
+        if (gl == 0) {
+          a.out_idx[q] = wj;
+          a.out_dis[q] = ek;
+        }
+      }
+      if (thresh) {
+        // every non-candidate has approx > thr, so exact > thr + ||q||^2 - eps
+        const float t = s.thr[q];
+        const double bound = L2 ? (double)t + qn : (double)t;
+        ok = ek_hi <= bound - (double)eps - 4e-7 * fabs(bound);
+      } else {
+        const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
+        ok = ek_hi < bound - (double)eps - 4e-7 * fabs(bound);
+      }
+      kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
+    }
+  }
+  if (!ok && thresh && nvalid >= 1 && kth_hi == INFINITY && a.kth_out) {
+    // a region overflowed: the candidates it did keep are rows of the base,
+    // so the least of their exact distances bounds the query's nearest from
+    // above; the band pass that settles the query starts from it
+    const unsigned vmask = gballot(valid);
+    float e = INFINITY;
+    for (unsigned m = vmask; m;) {
+      const int la = __ffs(m) - 1;
+      m &= m - 1;
+      const int lb = m ? __ffs(m) - 1 : la;
+      if (m) m &= m - 1;
+      const int ca = __shfl_sync(gm, id, la, G);
+      const int cb = __shfl_sync(gm, id, lb, G);
+      float ea, eb;
+      group_dist32x2<G>(qv, a.b + (long)ca * a.ldb, a.b + (long)cb * a.ldb, d, a.metric, gm, ea,
+                        eb);
+      if (gl == la) e = ea;
+      if (gl == lb) e = eb;
+    }
+    const float ek = ord2f(__reduce_min_sync(gm, valid ? f2ord(e) : 0xffffffffu));
+    const float rho = (float)(d + 4) * kU;
+    float eta = 0.f;
+    if (!L2) eta = (float)(d + 4) * kU * (float)sqrt(fmax(a.qn64[q], 0.0)) *
+                   __uint_as_float(a.bstats->max_norm_bits);
+    const double hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
+    kth_hi = __double2float_ru(hi + 2.0 * (double)rho * fabs(hi) + 2.0 * (double)eta);
+  }
+  if (!ok && gl == 0) {
+    const int pos = atomicAdd(a.fail_cnt, 1);
+    a.fail_list[pos] = q;
+    if (a.kth_out) a.kth_out[q] = kth_hi;
+  }
+  return ncand;
+}
+
+// A group of G lanes per query (K1: the k = 1 form); the candidate count goes
+// to a.n_cand once per block, from the block's last warp to finish (no
+// barrier at the end: a warp whose queries are done leaves at once, however
+// long the others take).
+template <int G, bool K1>
 __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
   constexpr int QPB = 256 / G;  // queries per block
   __shared__ unsigned long long s_cand;
@@ -649,7 +873,8 @@ __global__ void __launch_bounds__(256) rerank_small_kernel(RerankArgs a) {
   __syncthreads();
   const int q = blockIdx.x * QPB + (int)(threadIdx.x / G);
   unsigned nc = 0;
-  if (q < a.nq) nc = rerank_small_query<G>(a, q);  // uniform per group
+  if (q < a.nq)  // uniform per group
+    nc = K1 ? rerank_small_k1<G>(a, q) : rerank_small_query<G>(a, q);
   if (a.n_cand) {
     const unsigned w = __reduce_add_sync(0xffffffffu, nc);
     if ((threadIdx.x & 31) == 0) {
@@ -947,12 +1172,17 @@ int rerank(const RerankArgs &a, cudaStream_t st) {
                             a.sel.nregion() * a.sel.cap <= 32;
   if (small_topc || small_thresh) {
     const int M = small_topc ? a.sel.nchunk * a.sel.C : a.sel.nregion() * a.sel.cap;
-    if (M <= 8)
-      rerank_small_kernel<8><<<(unsigned)ceil_div(a.nq, 32), 256, 0, st>>>(a);
-    else if (M <= 16)
-      rerank_small_kernel<16><<<(unsigned)ceil_div(a.nq, 16), 256, 0, st>>>(a);
-    else
-      rerank_small_kernel<32><<<(unsigned)ceil_div(a.nq, 8), 256, 0, st>>>(a);
+    const bool k1 = a.k == 1;
+    if (M <= 8) {
+      if (k1) rerank_small_kernel<8, true><<<(unsigned)ceil_div(a.nq, 32), 256, 0, st>>>(a);
+      else rerank_small_kernel<8, false><<<(unsigned)ceil_div(a.nq, 32), 256, 0, st>>>(a);
+    } else if (M <= 16) {
+      if (k1) rerank_small_kernel<16, true><<<(unsigned)ceil_div(a.nq, 16), 256, 0, st>>>(a);
+      else rerank_small_kernel<16, false><<<(unsigned)ceil_div(a.nq, 16), 256, 0, st>>>(a);
+    } else {
+      if (k1) rerank_small_kernel<32, true><<<(unsigned)ceil_div(a.nq, 8), 256, 0, st>>>(a);
+      else rerank_small_kernel<32, false><<<(unsigned)ceil_div(a.nq, 8), 256, 0, st>>>(a);
+    }
     YG_LAUNCH_CHECK();
     return OK;
   }
