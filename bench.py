@@ -464,6 +464,7 @@ def hkm_record(args, local):
     # would: a level-1 child gets fewer points than bf, and small_nodes = 1
     # gives such a node one child per point instead.)
     rec["value"] = it.value / (ms.value / 1e3)
+    rec["ms_per_step"] = ms.value  # the tree on the device (the value's time)
     rec["e2e"] = {"value": it.value / dt, "unit": "instance-iterations/s",
                   "h2d_bytes_per_step": 4 * n * d, "d2h_bytes_per_step": 4 * (ncent * d + n),
                   "api": "yael_gpu_hkm_learn_ex (small_nodes = 1), pinned host buffer"}

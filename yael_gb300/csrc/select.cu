@@ -725,8 +725,15 @@ __device__ __forceinline__ unsigned rerank_small_k1(const RerankArgs &a, int q) 
       }
     } else {
       const float ak = ord2f(k0);
-      const double lim = (double)ak + 2.0 * (double)eps + 4e-7 * fabs((double)ak) + 1e-30;
-      const bool inband = valid && (double)ord2f(key) <= lim;
+      // The band's limit ak + 2 eps + 4e-7 |ak| + 1e-30 in FP32, rounded up,
+      // with larger constants and a relative margin: at least its FP64 value,
+      // so the band holds every row whose exact distance can be the least.
+      // (This part's FP64 pipe runs at 1/64 of the FP32 rate: FP64 is kept
+      // for the keys and the THRESH bound.)
+      float limf = __fadd_ru(__fadd_ru(ak, __fmul_ru(2.f, eps)),
+                             __fadd_ru(__fmul_ru(4.01e-7f, fabsf(ak)), 1.01e-30f));
+      limf = __fadd_ru(limf, __fmul_ru(fabsf(limf), 1.2e-7f));
+      const bool inband = valid && ord2f(key) <= limf;
       const unsigned bmask = gballot(inband);
       const int nband = __popc(bmask);
       // FP32 distances of the band's members, two at a time across the group
@@ -781,7 +788,9 @@ __device__ __forceinline__ unsigned rerank_small_k1(const RerankArgs &a, int q) 
           }
         }
       }
-      double ek_hi;
+      // ekh: an upper bound of the exact nearest distance, rounded up to FP32
+      float ekh, ekf = 0.f;
+      double ek_hi64 = 0.0;
       if (need64) {
         // FP64, sequential over coordinates, for the whole band
         unsigned long long k64 = ~0ull;
@@ -797,29 +806,44 @@ __device__ __forceinline__ unsigned rerank_small_k1(const RerankArgs &a, int q) 
           if (lex_less(pk, pi, k64, i64)) { k64 = pk; i64 = pi; }
         }
         const double ek = ord2d(k64);
-        ek_hi = ek + 1e-12 * fabs(ek);
+        ek_hi64 = ek + 1e-12 * fabs(ek);
+        ekh = __double2float_ru(ek_hi64);
         if (gl == 0) {
           a.out_idx[q] = i64;
           a.out_dis[q] = (float)ek;
         }
       } else {
-        const float ek = ord2f(wk);
-        ek_hi = (double)ek + (double)rho * fabs((double)ek) + (double)eta;
+        ekf = ord2f(wk);
+        ekh = __fadd_ru(__fadd_ru(ekf, __fmul_ru(rho, fabsf(ekf))), eta);
         if (gl == 0) {
           a.out_idx[q] = wj;
-          a.out_dis[q] = ek;
+          a.out_dis[q] = ekf;
         }
       }
+      // The certificate ek_hi <= bound - eps - 4e-7 |bound| in FP32 with
+      // outward rounding (and 4.01e-7 for the FP64 roundings of the bound): it
+      // holds only where the FP64 form holds, so every query it accepts is
+      // settled; the few it may reject at the edge go to the band pass.
       if (thresh) {
         // every non-candidate has approx > thr, so exact > thr + ||q||^2 - eps
         const float t = s.thr[q];
-        const double bound = L2 ? (double)t + qn : (double)t;
-        ok = ek_hi <= bound - (double)eps - 4e-7 * fabs(bound);
+        float blo = t, babs = fabsf(t);
+        if (L2) {
+          const double bd = (double)t + qn;
+          blo = __double2float_rd(bd);
+          babs = fmaxf(fabsf(blo), fabsf(__double2float_ru(bd)));
+        }
+        ok = ekh <= __fsub_rd(__fsub_rd(blo, eps), __fmul_ru(4.01e-7f, babs));
       } else {
-        const double bound = tkey == ~0ull ? INFINITY : (double)ord2f((unsigned)(tkey >> 32));
-        ok = ek_hi < bound - (double)eps - 4e-7 * fabs(bound);
+        const float b = tkey == ~0ull ? INFINITY : ord2f((unsigned)(tkey >> 32));
+        ok = ekh < __fsub_rd(__fsub_rd(b, eps), __fmul_ru(4.01e-7f, fabsf(b)));
       }
-      kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
+      if (!ok) {
+        // the bound the band pass starts from (as the general form gives it)
+        const double ek_hi =
+            need64 ? ek_hi64 : (double)ekf + (double)rho * fabs((double)ekf) + (double)eta;
+        kth_hi = __double2float_ru(ek_hi + 2.0 * (double)rho * fabs(ek_hi) + 2.0 * (double)eta);
+      }
     }
   }
   if (!ok && thresh && nvalid >= 1 && kth_hi == INFINITY && a.kth_out) {
