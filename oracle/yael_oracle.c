@@ -734,6 +734,11 @@ static int reassign_empty(int d, int k, float *C, const int *nassign, unsigned i
   return nre;
 }
 
+int orc_reassign_empty(int d, int k, float *C, const int *nassign, unsigned int seed)
+{
+  return reassign_empty(d, k, C, nassign, seed);
+}
+
 /* ------------------------------------------------------------------ */
 /* exact fixed-point centroid sums                                     */
 

@@ -119,6 +119,12 @@ double orc_objective64(int d, int n, const float *v, const float *c, const int *
 /* The fixed-point shift used by ORC_EXACT centroid sums for this data. */
 int orc_fixed_shift(long n, long d, const float *v);
 
+/* The empty-cluster split of k-means (yael/kmeans.c:166-209) on the k x d
+ * centroids C, with the counts nassign and the seed its caller draws;
+ * returns the number of clusters split.  Test utility: the restatement the
+ * k-means loop already uses, exported to check the GPU library's host split. */
+int orc_reassign_empty(int d, int k, float *C, const int *nassign, unsigned int seed);
+
 /* hierarchical k-means (yael/hkm.c:36-116).  centroids_out receives the
  * levels concatenated (level l holds bf^(l+1) rows of d floats).  assign_out
  * (n ints, may be NULL).  Returns 0, or -1 when a node is empty (where the

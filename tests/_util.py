@@ -68,6 +68,8 @@ def oracle():
         o.orc_kmeans_step_exact.argtypes = [I, I, I, P, P, P, P, P, P, I]
         o.orc_fixed_shift.argtypes = [L, L, P]
         o.orc_fixed_shift.restype = I
+        o.orc_reassign_empty.argtypes = [I, I, P, P, ctypes.c_uint]
+        o.orc_reassign_empty.restype = I
         o.orc_hkm_learn.argtypes = [I, I, I, I, P, I, P, P, I]
         o.orc_hkm_learn.restype = I
         o.orc_hkm_quantize.argtypes = [I, I, I, P, I, P, P, I]

@@ -16,6 +16,7 @@
 #include "alt.cuh"
 #include "kmeans.cuh"
 #include "knn.cuh"
+#include "split_host.h"
 #include "../../include/yael_gpu.h"
 
 namespace yg {
@@ -42,25 +43,6 @@ enum KmSlot : int {
   KS_SPLITBUF,
 };
 
-// ---- reference RNG usage (yael/vector.c:134-155, yael/kmeans.c:15-24) --------
-
-double drand_r_(unsigned *seed) { return rand_r(seed) / ((double)RAND_MAX + 1.0); }
-
-// Kinderman-Monahan ratio of uniforms, with the reference's float / double
-// roundings: u1, u2 and zz are held in float.
-double gaussrand_r_(unsigned *seed) {
-  const double magic = 1.71552776992141;  // 4 exp(-1/2) / sqrt(2)
-  double z;
-  for (;;) {
-    const float u1 = (float)drand_r_(seed);
-    const float u2 = (float)drand_r_(seed);
-    z = magic * (u1 - .5) / u2;
-    const float zz = (float)(z * z / 4.0);
-    if (zz < -log(u2)) break;
-  }
-  return z;
-}
-
 // the first k entries of the partial Fisher-Yates shuffle of 0..n-1 that
 // ivec_new_random_perm_r performs (only the first k swaps reach them)
 void random_init_first_k(int n, int k, unsigned seed, long *sel) {
@@ -85,73 +67,6 @@ void random_init_first_k(int n, int k, unsigned seed, long *sel) {
     const unsigned h = slot(j);
     key[h] = j;
     val[h] = vi;
-  }
-}
-
-double l1(const float *v, long n) {
-  double s = 0;
-  for (long i = 0; i < n; i++) s += fabs(v[i]);
-  return s;
-}
-double l2(const float *v, long n) {
-  double s = 0;
-  for (long i = 0; i < n; i++) s += v[i] * v[i];
-  return sqrt(s);
-}
-void mul_by(float *v, long n, double s) {
-  for (long i = 0; i < n; i++) v[i] *= s;
-}
-
-// kmeans_reassign_empty (yael/kmeans.c:166-209) in two halves.  Which row
-// each empty cluster copies depends on the counts and the random stream
-// alone, so the plan (the draws, in the reference's order) comes first; the
-// centroid arithmetic then runs on just the rows the plan touches, gathered
-// from the device, instead of a host copy of all k rows.
-struct SplitStep {
-  int c, j;     // the empty cluster and the row it copies
-  unsigned s2;  // the seed of its perturbation's Gaussian draws
-};
-
-int split_plan(int k, const int *nassign, unsigned seed, std::vector<SplitStep> &plan) {
-  int nre = 0;
-  std::vector<float> p(k);
-  for (int c = 0; c < k; c++) {
-    // nassign^2 - 1 in int arithmetic (wraps for large clusters, like the reference)
-    const unsigned sq = (unsigned)nassign[c] * (unsigned)nassign[c] - 1u;
-    p[c] = nassign[c] < 2 ? 0.f : (float)(int)sq;
-  }
-  mul_by(p.data(), k, 1. / l1(p.data(), k));
-  for (int c = 0; c < k; c++) {
-    if (nassign[c] != 0) continue;
-    nre++;
-    double rd = drand_r_(&seed);
-    int j;
-    for (j = 0; j < k - 1; j++) {
-      rd -= p[j];
-      if (rd < 0) break;
-    }
-    plan.push_back(SplitStep{c, j, (unsigned)rand_r(&seed)});
-    p[j] = 0;
-    mul_by(p.data(), k, 1. / l1(p.data(), k));
-  }
-  return nre;
-}
-
-// One instance's steps on its rows: row r of the instance at R + slot[r] * d
-// (every row a step names has a slot).  The same operations, in the same
-// order, as on the full array: copy, norm of the source, perturbation
-// added to the source and subtracted from the copy.
-void split_apply(int d, const SplitStep *st, int nst, float *R, const int *slot) {
-  std::vector<float> eps(d);
-  for (int t = 0; t < nst; t++) {
-    float *rc = R + (long)slot[st[t].c] * d, *rj = R + (long)slot[st[t].j] * d;
-    if (rc != rj) memcpy(rc, rj, sizeof(float) * d);
-    const double s = l2(rj, d) * 0.0000001;
-    unsigned s2 = st[t].s2;
-    for (int i = 0; i < d; i++) eps[i] = (float)gaussrand_r_(&s2);
-    mul_by(eps.data(), d, s);
-    for (int i = 0; i < d; i++) rj[i] += eps[i];
-    for (int i = 0; i < d; i++) rc[i] -= eps[i];
   }
 }
 
@@ -795,43 +710,23 @@ struct Engine {
   // gathered, split on the host, put back
   int apply_splits(const std::vector<SplitStep> &plan, const std::vector<int> &pinst,
                    const std::vector<int> &pat) {
-    std::vector<long> rows;
-    std::vector<int> slot((size_t)k, -1);
-    std::vector<int> first(pinst.size() + 1);
-    // rows in instance order, each instance's slots its own
-    for (size_t b = 0; b < pinst.size(); b++) {
-      first[b] = (int)rows.size();
-      const int e = b + 1 < pinst.size() ? pat[b + 1] : (int)plan.size();
-      for (int t = pat[b]; t < e; t++)
-        for (int r : {plan[t].c, plan[t].j})
-          if (slot[r] < 0) {
-            slot[r] = (int)rows.size() - first[b];
-            rows.push_back((long)pinst[b] * k + r);
-          }
-      for (int t = pat[b]; t < e; t++) slot[plan[t].c] = slot[plan[t].j] = -1;
-    }
-    first[pinst.size()] = (int)rows.size();
-    const long m = (long)rows.size();
+    SplitRows sr;
+    split_rows(k, plan, pinst, pat, sr);
+    const long m = (long)sr.rows.size();
     long *drows;
     float *dbuf;
     YG_CHECK(ws_get(ctx->ws, KS_SPLITROWS, (size_t)m, &drows));
     YG_CHECK(ws_get(ctx->ws, KS_SPLITBUF, (size_t)m * d, &dbuf));
     std::vector<float> R((size_t)m * d);
-    YG_CUDA(cudaMemcpyAsync(drows, rows.data(), sizeof(long) * m, cudaMemcpyHostToDevice, st));
+    YG_CUDA(cudaMemcpyAsync(drows, sr.rows.data(), sizeof(long) * m, cudaMemcpyHostToDevice, st));
     YG_CHECK(km_gather(C, d, drows, m, dbuf, st));
     YG_CUDA(cudaMemcpyAsync(R.data(), dbuf, sizeof(float) * m * d, cudaMemcpyDeviceToHost, st));
     YG_CUDA(cudaStreamSynchronize(st));
-    for (size_t b = 0; b < pinst.size(); b++) {
-      const int e = b + 1 < pinst.size() ? pat[b + 1] : (int)plan.size();
-      for (int r = first[b]; r < first[b + 1]; r++) slot[rows[r] - (long)pinst[b] * k] = r - first[b];
-      split_apply(d, plan.data() + pat[b], e - pat[b], R.data() + (size_t)first[b] * d,
-                  slot.data());
-      for (int r = first[b]; r < first[b + 1]; r++) slot[rows[r] - (long)pinst[b] * k] = -1;
-    }
+    split_apply_rows(d, k, plan, pinst, pat, sr, R.data());
     YG_CUDA(cudaMemcpyAsync(dbuf, R.data(), sizeof(float) * m * d, cudaMemcpyHostToDevice, st));
     scatter_rows64_kernel<<<(unsigned)ceil_div(m * d, 256), 256, 0, st>>>(dbuf, drows, m, d, C);
     YG_LAUNCH_CHECK();
-    YG_CUDA(cudaStreamSynchronize(st));  // R is a stack buffer
+    YG_CUDA(cudaStreamSynchronize(st));  // R and sr are stack buffers
     return OK;
   }
 
