@@ -1,10 +1,15 @@
-// Test shim: the GPU library's host-side empty-cluster split (split_host.h)
-// on host arrays, the device gather and scatter of the touched rows replaced
-// by host copies, so that a CPU test compares it with the oracle's
-// restatement on the whole centroid array.
+// Test shim: the GPU library's host-side k-means draws (km_host.h) on host
+// arrays, so that a CPU test compares them with the oracle's restatements:
+// the random initialisation, and the empty-cluster split with the device
+// gather and scatter of the touched rows replaced by host copies.
 #include <string.h>
 
-#include "../yael_gb300/csrc/split_host.h"
+#include "../yael_gb300/csrc/km_host.h"
+
+// the first k of the partial Fisher-Yates shuffle of 0..n-1 from seed
+extern "C" void shim_random_init(int n, int k, unsigned seed, long *sel) {
+  yg::random_init_first_k(n, k, seed, sel);
+}
 
 // ni instances of k centroids (C: ni * k * d floats, nassign: ni * k counts),
 // each split with its own seed when it has an empty cluster; nre receives

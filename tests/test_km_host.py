@@ -1,8 +1,12 @@
-"""The GPU library's host split of empty clusters (yael_gb300/csrc/split_host.h:
-planned from the counts and the seed, then applied to the touched rows only)
-against the oracle's restatement of kmeans_reassign_empty
-(yael/kmeans.c:166-209) on the whole centroid array: the same rows, bit for
-bit, and the same number of splits.  Host code only (no GPU)."""
+"""The GPU library's host-side k-means draws (yael_gb300/csrc/km_host.h)
+against the oracle's restatements, on the host (no GPU):
+* the random initialisation's first k of a partial Fisher-Yates shuffle
+  (an open-addressing table instead of an n-entry permutation) against
+  orc_random_init;
+* the empty-cluster split (planned from the counts and the seed, then applied
+  to the touched rows only) against the oracle's kmeans_reassign_empty
+  (yael/kmeans.c:166-209) on the whole centroid array: the same rows, bit for
+  bit, and the same number of splits."""
 import ctypes
 import os
 import subprocess
@@ -17,13 +21,27 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 @pytest.fixture(scope="module")
 def shim(tmp_path_factory):
-    out = str(tmp_path_factory.mktemp("split") / "libsplitshim.so")
+    out = str(tmp_path_factory.mktemp("kmhost") / "libkmhostshim.so")
     subprocess.run(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-o", out,
-                    os.path.join(HERE, "split_shim.cpp")], check=True)
+                    os.path.join(HERE, "km_host_shim.cpp")], check=True)
     lib = ctypes.CDLL(out)
     lib.shim_split.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4
     lib.shim_split.restype = ctypes.c_int
+    lib.shim_random_init.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_void_p]
+    lib.shim_random_init.restype = None
     return lib
+
+
+@pytest.mark.parametrize("n,k,seed", [(1, 1, 5), (10, 10, 7), (1000, 3, 11), (5000, 4999, 3),
+                                      (2_000_000, 32, 12345), (10_000_000, 65536, 99),
+                                      (65537, 65536, 2**31 - 1)])
+def test_random_init_matches_oracle(shim, n, k, seed):
+    got = np.empty(k, np.int64)
+    shim.shim_random_init(n, k, seed, ptr(got))
+    want = np.empty(k, np.int32)
+    oracle().orc_random_init(n, k, seed, ptr(want))
+    np.testing.assert_array_equal(got, want)
+    assert len(np.unique(got)) == k
 
 
 def counts(rng, k, kind):

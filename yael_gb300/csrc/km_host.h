@@ -1,8 +1,9 @@
 // Host side of the k-means control flow that replays the reference's
-// random draws: its RNG helpers (yael/vector.c:134-155, yael/kmeans.c:15-24)
-// and the empty-cluster split (yael/kmeans.c:166-209), planned from the
-// counts and applied to just the centroid rows it touches.  Plain C++ (no
-// CUDA), so the tests compile it on its own against the oracle.
+// random draws: its RNG helpers (yael/vector.c:134-155, yael/kmeans.c:15-24),
+// the random initialisation's partial Fisher-Yates shuffle, and the
+// empty-cluster split (yael/kmeans.c:166-209), planned from the counts and
+// applied to just the centroid rows it touches.  Plain C++ (no CUDA), so the
+// tests compile it on its own against the oracle.
 #pragma once
 
 #include <math.h>
@@ -30,6 +31,33 @@ inline double gaussrand_r_(unsigned *seed) {
     if (zz < -log(u2)) break;
   }
   return z;
+}
+
+// the first k entries of the partial Fisher-Yates shuffle of 0..n-1 that
+// ivec_new_random_perm_r performs (only the first k swaps reach them)
+inline void random_init_first_k(int n, int k, unsigned seed, long *sel) {
+  // the permuted positions, in an open-addressing table (keys >= 0, -1 free):
+  // at most k entries, so 4k slots stay sparse
+  int cap = 16;
+  while (cap < 4 * k) cap <<= 1;
+  std::vector<int> key(cap, -1), val(cap);
+  auto slot = [&](int i) {
+    unsigned h = (unsigned)i * 2654435761u & (unsigned)(cap - 1);
+    while (key[h] != -1 && key[h] != i) h = (h + 1) & (unsigned)(cap - 1);
+    return h;
+  };
+  auto at = [&](int i) {
+    const unsigned h = slot(i);
+    return key[h] == i ? val[h] : i;
+  };
+  for (int i = 0; i < k && i < n; i++) {
+    const int j = i + rand_r(&seed) % (n - i);
+    const int vi = at(i), vj = at(j);
+    sel[i] = vj;
+    const unsigned h = slot(j);
+    key[h] = j;
+    val[h] = vi;
+  }
 }
 
 inline double l1(const float *v, long n) {

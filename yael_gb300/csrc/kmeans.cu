@@ -16,7 +16,7 @@
 #include "alt.cuh"
 #include "kmeans.cuh"
 #include "knn.cuh"
-#include "split_host.h"
+#include "km_host.h"
 #include "../../include/yael_gpu.h"
 
 namespace yg {
@@ -43,33 +43,7 @@ enum KmSlot : int {
   KS_SPLITBUF,
 };
 
-// the first k entries of the partial Fisher-Yates shuffle of 0..n-1 that
-// ivec_new_random_perm_r performs (only the first k swaps reach them)
-void random_init_first_k(int n, int k, unsigned seed, long *sel) {
-  // the permuted positions, in an open-addressing table (keys >= 0, -1 free):
-  // at most k entries, so 4k slots stay sparse
-  int cap = 16;
-  while (cap < 4 * k) cap <<= 1;
-  std::vector<int> key(cap, -1), val(cap);
-  auto slot = [&](int i) {
-    unsigned h = (unsigned)i * 2654435761u & (unsigned)(cap - 1);
-    while (key[h] != -1 && key[h] != i) h = (h + 1) & (unsigned)(cap - 1);
-    return h;
-  };
-  auto at = [&](int i) {
-    const unsigned h = slot(i);
-    return key[h] == i ? val[h] : i;
-  };
-  for (int i = 0; i < k && i < n; i++) {
-    const int j = i + rand_r(&seed) % (n - i);
-    const int vi = at(i), vj = at(j);
-    sel[i] = vj;
-    const unsigned h = slot(j);
-    key[h] = j;
-    val[h] = vi;
-  }
-}
-
+// the split centroid rows put back: row r of src to row rows[r] of dst
 __global__ void scatter_rows64_kernel(const float *src, const long *rows, long m, int d,
                                       float *dst) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
