@@ -987,13 +987,16 @@ def main():
                          "separately")
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.impl == "reference" and args.workload != "knn":
+        # the reference arm times the headline configuration; every other
+        # workload's record carries its own CPU figure
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference's CPU figure for this workload is the "
+                              "cpu_baseline of the ours line (the oracle's port on a "
+                              "bounded sample)"}), flush=True)
+        return
     if args.workload in ("gmm", "kmlsh", "vlad", "alt", "kmeans_l1"):
-        if args.impl == "reference":
-            if rank == 0:
-                print(json.dumps({"impl": "reference", "unavailable":
-                                  "the reference's CPU figure for this workload is the "
-                                  "cpu_baseline of the ours line"}), flush=True)
-            return
         run_callers(args, world, rank, local)
         return
     if args.workload == "knn_batch" and args.impl != "reference":
