@@ -154,13 +154,15 @@ def test_nan_rows_follow_reference_padding():
 
 
 @pytest.mark.parametrize("prec", PRECS + ["fp16"])
-def test_dot_product_metric(prec):
+@pytest.mark.parametrize("k", [7, 1])
+def test_dot_product_metric(prec, k):
+    """k = 1 takes the short re-rank's k = 1 form (reductions, FP32 certificate)."""
     rng = np.random.default_rng(6)
     b = rng.standard_normal((3000, 40)).astype(np.float32)
     q = rng.standard_normal((50, 40)).astype(np.float32)
-    idx, dis, _ = gpu_knn(b, q, 7, prec, dt=16)
+    idx, dis, _ = gpu_knn(b, q, k, prec, dt=16)
     full = q.astype(np.float64) @ b.astype(np.float64).T
-    order = np.lexsort((np.broadcast_to(np.arange(3000), full.shape), full), axis=1)[:, :7]
+    order = np.lexsort((np.broadcast_to(np.arange(3000), full.shape), full), axis=1)[:, :k]
     np.testing.assert_array_equal(idx, order)
     np.testing.assert_allclose(dis, np.take_along_axis(full, order, 1), rtol=1e-5, atol=1e-5)
 
