@@ -6,7 +6,9 @@
 //                     |a - exact| <= eps[q]   (eps[q] = 0 for exact-class data)
 //   exact e(q,j)   -- FP32 direct difference sum (q_c - b_c)^2, relative error
 //                     <= rho; adjacent values closer than their error bound
-//                     are re-evaluated in FP64 and ordered by (FP64, id).
+//                     are re-evaluated in FP64 and ordered by (FP64, id)
+//                     (for k = 1, L2, a near tie of the best two alone is
+//                     first tried by the exact sign of their difference).
 // The k results of a query are the k smallest (exact, id).  A query whose
 // candidate set cannot be proven to contain them is re-computed by the
 // exhaustive path (FP64 distances to every base row, radix select).
